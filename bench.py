@@ -1,0 +1,306 @@
+"""Benchmark: HT decomposition of a 1024^3 FP32 tensor at rank 32 on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the headline configuration): a 1024 x 1024 x 1024 FP32 tensor
+(4 GiB) whose every matricisation has singular values r^-1.5 (orthonormal
+Gaussian factors, seeded), reference dimension tree {1,2,3}->{1,2},{3}, rank 32
+at every node.  One step = one full decomposition (leaf bases U_t and transfer
+tensors B_t) by the mixed-precision path (BF16 tcgen05 GEMMs, FP32
+accumulation) with the tensor resident in HBM.  The tensor (4 GiB) is 32x the
+L2, so no flush is needed between steps.
+
+Also measured, outside the headline value: the plain FP32 path (FP32 CUDA-core
+GEMMs) on the same GPU, the end-to-end time through the C ABI with the tensor
+in pinned host memory (host->device copy inside the timed region), the
+relative errors against the FP64 optimum (exact for this family), the
+roofline of the dominant kernel (the BF16 Gram), and the CPU baseline: the
+numpy restatement of the reference's HT_TensorLy.py on the host cores.
+
+--impl reference: times the reference's CPU implementation of the path (the
+numpy port of HT_TensorLy.py; the Python statement itself needs tensorly and
+torch.eig, neither available) on this machine's host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_FULL, RANK, DECAY = 1024, 32, 1.5
+CPU_SAMPLE_N = 512
+METRIC = "HT-decomp ms @1024^3 r32, err<=1e-3 vs FP64: mixed/learned vs plain FP32"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.rows, self.proc, self.dev = [], None, device_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) >= 9:
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ CPU leg
+def cpu_baseline(sample_n=CPU_SAMPLE_N, reps=1):
+    """The reference's CPU path (numpy port of HT_TensorLy.py, FP32, timed region
+    = decomposition + reconstruction + error as in the Python statement) on a
+    sample_n^3 tensor of the same family, scaled by (N/sample_n)^4 -- the
+    operation count of the Gram GEMMs and the n^2 x n SVD -- to the full size."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ht_oracle as O
+    from ht_tensor_learning_using_gpu_tensor_cores_gb300 import synth, tree as T
+    X = synth.odeco(sample_n, decay=DECAY, seed=1)
+    tr = T.reference_tree_3d([1, RANK, RANK, RANK, RANK])
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        U, B, _ = O.ht_decompose(X, tr, dtype=np.float32)
+        err = O.ht_error(X, tr, U, B)
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    scale = (N_FULL / sample_n) ** 4
+    try:
+        import threadpoolctl
+        info = threadpoolctl.threadpool_info()
+        threads = max((i.get("num_threads", 1) for i in info), default=os.cpu_count())
+        blas = ",".join(sorted({i.get("internal_api", "?") for i in info}))
+    except Exception:
+        threads, blas = os.cpu_count(), "unknown"
+    return {"value": t * scale * 1e3, "unit": "ms", "cores": int(threads), "kind": "port",
+            "sample": f"full FP32 decomposition+reconstruction+error of a {sample_n}^3 tensor of the same family "
+                      f"(numpy port of HT_TensorLy.py), {t:.2f} s measured, scaled x{scale:.0f} by the n^4 "
+                      f"operation count to {N_FULL}^3",
+            "blas": blas, "sample_seconds": t, "sample_err": err}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        pass
+    vals = []
+    cb = None
+    for _ in range(max(1, args.steps)):
+        cb = cpu_baseline(CPU_SAMPLE_N, reps=1)
+        vals.append(cb["value"])
+    v = statistics.median(vals)
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"HT decomposition {N_FULL}^3 rank {RANK}, reference tree, r^-1.5 spectrum",
+                       "path": "numpy port of HT_TensorLy.py on host cores"},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU leg
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+    import ht_tensor_learning_using_gpu_tensor_cores_gb300 as ht
+    from ht_tensor_learning_using_gpu_tensor_cores_gb300 import synth
+
+    torch.cuda.set_device(local)
+    n, k = args.n, RANK
+    tree = ht.reference_tree_3d([1, k, k, k, k])
+    X = synth.odeco(n, decay=DECAY, seed=1 + rank, assemble_on=torch.device("cuda", local))   # column-major memory
+    torch.cuda.synchronize()
+    e_opt = synth.odeco_optimal_error(n, k, DECAY)
+    stream = torch.cuda.current_stream()
+
+    def one(prec, compute_error=False):
+        return ht.decompose(X, tree, precision=prec, compute_error=compute_error)
+
+    # correctness of both paths against the FP64 optimum (not timed)
+    mixed = one("bf16", compute_error=True)
+    plain = one("fp32", compute_error=True)
+    err_mixed, err_plain = mixed.report["rel_err"], plain.report["rel_err"]
+
+    # ---- headline: mixed path, device-resident input
+    for _ in range(args.warmup):
+        one("bf16")
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    l0 = ht.kernel_launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stage_ms = []
+    ev0.record(stream)
+    for _ in range(args.steps):
+        r = one("bf16")
+        stage_ms.append(r.report["ms_stage"])
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = clk.stop()
+    launches = (ht.kernel_launch_count() - l0) / max(1, args.steps)
+    ms = ev0.elapsed_time(ev1) / max(1, args.steps)
+    ms = allmax(ms, world)
+
+    # ---- plain FP32 path on the same GPU (denominator of the headline ratio)
+    one("fp32")
+    torch.cuda.synchronize()
+    psteps = max(1, min(args.steps, 5))
+    ev0.record(stream)
+    for _ in range(psteps):
+        one("fp32")
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms_plain = ev0.elapsed_time(ev1) / psteps
+
+    # ---- end to end through the C ABI with the tensor in pinned host memory
+    Xh = torch.empty(X.shape, dtype=torch.float32, pin_memory=True)
+    Xh.copy_(X)
+    Xh_np = Xh.numpy()   # shares the pinned buffer; memory is the column-major tensor
+    dims = (n, n, n)
+    flat = Xh_np.reshape(-1)
+    ht.decompose(flat, tree, dims=dims, precision="bf16")   # warm: workspace sized for host input
+    torch.cuda.synchronize()
+    e2e_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        res_h = ht.decompose(flat, tree, dims=dims, precision="bf16")
+    t1 = time.perf_counter()
+    e2e_ms = (t1 - t0) * 1e3 / e2e_steps
+    e2e_ms = allmax(e2e_ms, world)
+    d2h = sum(int(np.asarray(a).nbytes) for a in list(res_h.U.values()) + list(res_h.B.values()))
+    h2d = n * n * n * 4
+
+    # ---- roofline of the dominant kernel: the BF16 Gram (3 launches per step)
+    pk = peaks()
+    grams_ms = statistics.median([s["grams"] for s in stage_ms])
+    gram_flops = 3 * float(n) ** 2 * float(n) ** 2          # SYRK: n^2 K per mode, K = n^2
+    achieved = gram_flops / (grams_ms * 1e-3) / 1e12
+    stage_med = {kk: statistics.median([s[kk] for s in stage_ms]) for kk in stage_ms[0]}
+    cpu = cpu_baseline(CPU_SAMPLE_N) if (rank == 0 and not args.no_cpu) else None
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+            "data": "synthetic",
+            "config": {"workload": f"HT decomposition {n}^3 FP32 rank {k}, reference tree {{1,2,3}}->{{1,2}},{{3}}, "
+                                   f"r^-{DECAY} spectrum on every matricisation",
+                       "n": n, "rank": k, "path": "mixed: BF16 tcgen05 Gram/TTM, FP32 accumulation",
+                       "l2_policy": "inputs larger than L2 (4 GiB vs 129 MB), no flush",
+                       "parallelism": f"replicas x{world}"},
+            "plain_fp32_ms": ms_plain, "speedup_vs_plain_fp32": ms_plain / ms,
+            "rel_err": {"mixed": err_mixed, "plain_fp32": err_plain, "fp64_optimum": e_opt,
+                        "mixed_minus_fp64": err_mixed - e_opt, "plain_minus_fp64": err_plain - e_opt},
+            "stage_ms": stage_med,
+            "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "tensor", "kernel": "tc_gemm_kernel<256> (leaf Grams, 3 launches + reduce)",
+                         "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                         "frac": achieved / pk["bf16_tflops"], "traffic": None,
+                         "peak_source": pk["source"] + " bf16 burst"},
+            "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=N_FULL)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,358 @@
+"""GB300-native hierarchical Tucker (HT) decomposition.
+
+Host-side mirror of the reference's entry points
+(``third_order_tensor_decompsition/CUDA/Optimized/function.h:6`` ``htd``,
+``fourth_order_tensor_decomposition/single_GPU/CUDA/Optimized/function.h:6``
+``htd4``) over the C ABI in ``include/htgb.h``.  All compute runs in the
+hand-written sm_103a kernels of ``libhtgb.so``; there is no CPU fallback.
+
+Tensors are column-major (first index fastest), as in the reference's CUDA
+code.  A numpy input is a Fortran-ordered array of shape ``dims``; a torch
+CUDA input is a contiguous tensor whose memory is the column-major tensor,
+i.e. a C-contiguous tensor of shape ``dims[::-1]``.
+
+    import ht_tensor_learning_using_gpu_tensor_cores_gb300 as ht
+    tree = ht.reference_tree_3d([1, 32, 32, 32, 32])
+    res = ht.decompose(X, tree, precision="bf16", compute_error=True)
+    res.U[3], res.B[1], res.report["rel_err"]
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import c_double, c_int, c_long, c_ulonglong, c_void_p
+from dataclasses import dataclass, field
+from typing import Dict, Optional, Sequence
+
+import numpy as np
+
+from . import synth
+from ._lib import (FLAG_COMPUTE_ERROR, HTError, HtConfig, HtReport, HtTree, LEAF_GRAM, PREC_BF16, PREC_FP32, check,
+                   lib)
+from .tree import (DimTree, balanced_tree_4d, left_first_tree_3d, middle_tree_3d, reference_tree_3d,
+                   uniform_ranks)
+
+__all__ = ["DimTree", "reference_tree_3d", "left_first_tree_3d", "middle_tree_3d", "balanced_tree_4d",
+           "uniform_ranks", "decompose", "reconstruct_error", "htd", "htd4", "HTResult", "HTError", "synth",
+           "workspace_size", "release_workspace", "kernel_launch_count"]
+
+_PREC = {"fp32": PREC_FP32, "bf16": PREC_BF16}
+
+
+def _tree_struct(tree: DimTree) -> HtTree:
+    f = tree.as_struct_fields()
+    t = HtTree()
+    t.order, t.n_nodes = f["order"], f["n_nodes"]
+    for name in ("parent", "left", "right", "mode_mask", "rank"):
+        arr = getattr(t, name)
+        for i, v in enumerate(f[name]):
+            arr[i] = int(v) if v is not None else -1
+    return t
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+@dataclass
+class HTResult:
+    """U[t] for leaves (n_t x k_t, column-major), B[t] for interior nodes and the
+    root (k_left x k_right x k_t, column-major) and the run report."""
+    tree: DimTree
+    dims: tuple
+    U: Dict[int, object] = field(default_factory=dict)
+    B: Dict[int, object] = field(default_factory=dict)
+    report: Dict[str, object] = field(default_factory=dict)
+
+
+def _dims_of(x, tree: DimTree, dims: Optional[Sequence[int]]):
+    if dims is not None:
+        dims = tuple(int(d) for d in dims)
+    elif _is_torch(x):
+        if x.dim() != tree.order:
+            raise ValueError("pass dims= for a torch tensor that is not shaped dims[::-1]")
+        dims = tuple(int(d) for d in reversed(x.shape))
+    else:
+        if x.ndim != tree.order:
+            raise ValueError("pass dims= for a flat numpy buffer")
+        dims = tuple(int(d) for d in x.shape)
+    if len(dims) != tree.order:
+        raise ValueError(f"tree has order {tree.order}, dims has {len(dims)} entries")
+    return dims
+
+
+def _host_input(x, dims):
+    a = np.asarray(x)
+    if a.dtype != np.float32:
+        raise TypeError("the tensor must be float32")
+    if a.ndim == len(dims) and tuple(a.shape) == tuple(dims):
+        a = np.asfortranarray(a)
+        return a, a.ctypes.data
+    a = np.ascontiguousarray(a).reshape(-1)
+    if a.size != int(np.prod(dims)):
+        raise ValueError("buffer size does not match dims")
+    return a, a.ctypes.data
+
+
+def _out_buffers(tree: DimTree, dims, like):
+    U, B = {}, {}
+    if like is None:
+        for t in tree.leaves():
+            U[t] = np.zeros((dims[tree.modes[t][0]], tree.ranks[t]), dtype=np.float32, order="F")
+        for t in [0] + tree.interior():
+            kl, kr = tree.ranks[tree.left[t]], tree.ranks[tree.right[t]]
+            B[t] = np.zeros((kl, kr, tree.ranks[t]), dtype=np.float32, order="F")
+        ptr = lambda a: a.ctypes.data
+    else:
+        import torch
+        dev = like.device
+        for t in tree.leaves():
+            n, k = dims[tree.modes[t][0]], tree.ranks[t]
+            U[t] = torch.zeros((k, n), dtype=torch.float32, device=dev).t()
+        for t in [0] + tree.interior():
+            kl, kr = tree.ranks[tree.left[t]], tree.ranks[tree.right[t]]
+            B[t] = torch.zeros((tree.ranks[t], kr, kl), dtype=torch.float32, device=dev).permute(2, 1, 0)
+        ptr = lambda a: a.data_ptr()
+    uptr = (c_void_p * 7)()
+    bptr = (c_void_p * 7)()
+    for t, a in U.items():
+        uptr[t] = ptr(a)
+    for t, a in B.items():
+        bptr[t] = ptr(a)
+    return U, B, uptr, bptr
+
+
+def _config(precision: str, oversample: int, eig_iters: int, power_steps: int, seed: int, flags: int,
+            sketch=None, eig_tol: float = 0.0) -> tuple:
+    cfg = HtConfig()
+    check(lib().ht_config_default(ctypes.byref(cfg)))
+    if precision not in _PREC:
+        raise ValueError(f"precision must be one of {sorted(_PREC)}")
+    cfg.precision = _PREC[precision]
+    cfg.leaf_method = LEAF_GRAM
+    cfg.oversample = int(oversample)
+    cfg.eig_iters = int(eig_iters)
+    cfg.power_steps = int(power_steps)
+    cfg.seed = int(seed)
+    cfg.flags = int(flags)
+    cfg.eig_tol = float(eig_tol)
+    keep = []
+    if sketch is not None:
+        for m, s in enumerate(sketch):
+            if s is None:
+                continue
+            if _is_torch(s):
+                s = s.contiguous()
+                keep.append(s)
+                cfg.sketch[m] = s.data_ptr()
+            else:
+                a = np.asfortranarray(np.asarray(s, dtype=np.float32))
+                keep.append(a)
+                cfg.sketch[m] = a.ctypes.data
+    return cfg, keep
+
+
+def decompose(x, tree: DimTree, dims: Optional[Sequence[int]] = None, precision: str = "bf16", oversample: int = 16,
+              eig_iters: int = 10, power_steps: int = 1, seed: int = 1234, compute_error: bool = False,
+              sketch=None, eig_tol: float = 0.0, stream=None) -> HTResult:
+    """HT decomposition of a column-major 3rd/4th-order float32 tensor.
+
+    precision="bf16": BF16 tcgen05 GEMMs with FP32 accumulation (the mixed path);
+    precision="fp32": every product in FP32 on CUDA cores (the plain path).
+    sketch: optional per-mode start blocks (n_m x (k+p)) for the leaf eigen-solver.
+    """
+    dims = _dims_of(x, tree, dims)
+    tree.check_ranks(dims)
+    flags = FLAG_COMPUTE_ERROR if compute_error else 0
+    cfg, keep = _config(precision, oversample, eig_iters, power_steps, seed, flags, sketch, eig_tol)
+    ts = _tree_struct(tree)
+    cdims = (c_long * 4)(*dims)
+    if _is_torch(x):
+        import torch
+        if not x.is_cuda or x.dtype != torch.float32 or not x.is_contiguous():
+            raise TypeError("torch input must be a contiguous float32 CUDA tensor")
+        xptr, like = x.data_ptr(), x
+        if stream is None:
+            stream = torch.cuda.current_stream(x.device).cuda_stream
+    else:
+        xa, xptr = _host_input(x, dims)
+        keep.append(xa)
+        like = None
+    U, B, uptr, bptr = _out_buffers(tree, dims, like)
+    rep = HtReport()
+    st = lib().ht_decompose(c_void_p(xptr), cdims, len(dims), ctypes.byref(ts), ctypes.byref(cfg), uptr, bptr,
+                            ctypes.byref(rep), c_void_p(stream) if stream else None)
+    check(st)
+    report = {
+        "rel_err": rep.rel_err if compute_error else None,
+        "norm_x": rep.norm_x,
+        "ms_total": rep.ms_total,
+        "ms_stage": {name: rep.ms_stage[i] for i, name in
+                     enumerate(["convert", "grams", "eig", "core_pass", "transfer", "error", "h2d", "d2h"])},
+        "eig_residual": {t: rep.eig_residual[t] for t in tree.leaves()},
+        "gpu_launches": rep.gpu_launches,
+        "path": {"tcgen05": bool(rep.path_flags & 1), "simt": bool(rep.path_flags & 2)},
+    }
+    del keep
+    return HTResult(tree, dims, U, B, report)
+
+
+def reconstruct_error(x, tree: DimTree, U: Dict[int, object], B: Dict[int, object],
+                      dims: Optional[Sequence[int]] = None, stream=None) -> float:
+    """||X - Xhat||_F / ||X||_F computed on the GPU without materialising Xhat."""
+    dims = _dims_of(x, tree, dims)
+    ts = _tree_struct(tree)
+    cdims = (c_long * 4)(*dims)
+    keep = []
+    if _is_torch(x):
+        import torch
+        xptr = x.data_ptr()
+        if stream is None:
+            stream = torch.cuda.current_stream(x.device).cuda_stream
+    else:
+        xa, xptr = _host_input(x, dims)
+        keep.append(xa)
+    uptr = (c_void_p * 7)()
+    bptr = (c_void_p * 7)()
+
+    def p(a):
+        if _is_torch(a):
+            # factors must be column-major
+            if a.dim() == 2 and a.stride() != (1, a.shape[0]):
+                a = a.t().contiguous().t()
+            keep.append(a)
+            return a.data_ptr()
+        a = np.asfortranarray(np.asarray(a, dtype=np.float32))
+        keep.append(a)
+        return a.ctypes.data
+
+    for t, a in U.items():
+        uptr[t] = p(a)
+    for t, a in B.items():
+        if _is_torch(a) and a.dim() == 3:
+            a = a.permute(2, 1, 0).contiguous().permute(2, 1, 0)
+        bptr[t] = p(a)
+    out = c_double(0.0)
+    check(lib().ht_reconstruct_error(c_void_p(xptr), cdims, len(dims), ctypes.byref(ts), uptr, bptr,
+                                     ctypes.byref(out), c_void_p(stream) if stream else None))
+    return float(out.value)
+
+
+def htd(x: np.ndarray, k: Sequence[int]) -> float:
+    """Mirror of ``float htd(dt *x, long a, long b, long c, int *k)``
+    (3D/Opt/function.h:6): x is a host a x b x c column-major tensor, k the
+    5 ranks by node id; returns the relative reconstruction error."""
+    a = np.asfortranarray(np.asarray(x, dtype=np.float32))
+    if a.ndim != 3:
+        raise ValueError("htd takes a 3rd-order tensor")
+    kk = (c_int * 5)(*[int(v) for v in k])
+    e = lib().htd(c_void_p(a.ctypes.data), a.shape[0], a.shape[1], a.shape[2], kk)
+    if e < 0:
+        raise HTError(1, lib().ht_last_error().decode(errors="replace"))
+    return float(e)
+
+
+def htd4(x: np.ndarray, k: Sequence[int]) -> None:
+    """Mirror of ``void htd4(dt *X, long a, long b, long c, long d, int *k, ...)``
+    (4D/Opt/function.h:6); prints the error rate as the reference does."""
+    a = np.asfortranarray(np.asarray(x, dtype=np.float32))
+    if a.ndim != 4:
+        raise ValueError("htd4 takes a 4th-order tensor")
+    kk = (c_int * 7)(*[int(v) for v in k])
+    lib().htd4(c_void_p(a.ctypes.data), a.shape[0], a.shape[1], a.shape[2], a.shape[3], kk, None, None)
+
+
+def workspace_size(dims: Sequence[int], tree: DimTree, precision: str = "bf16", compute_error: bool = False) -> int:
+    cfg, _ = _config(precision, 16, 10, 1, 1234, FLAG_COMPUTE_ERROR if compute_error else 0)
+    out = c_ulonglong(0)
+    check(lib().ht_workspace_size((c_long * 4)(*dims), len(dims), ctypes.byref(_tree_struct(tree)),
+                                  ctypes.byref(cfg), ctypes.byref(out)))
+    return int(out.value)
+
+
+def release_workspace() -> None:
+    check(lib().ht_release_workspace())
+
+
+def kernel_launch_count() -> int:
+    return int(lib().ht_kernel_launch_count())
+
+
+def _prim_input(x, dims):
+    if _is_torch(x):
+        return x, x.data_ptr(), x
+    a, p = _host_input(x, dims)
+    return a, p, None
+
+
+def _prim_view(dims, lo, hi):
+    L = int(np.prod(dims[:lo])) if lo > 0 else 1
+    N = int(np.prod(dims[lo:hi + 1]))
+    R = int(np.prod(dims[hi + 1:])) if hi + 1 < len(dims) else 1
+    return L, N, R
+
+
+def _prim_out(shape, like):
+    if like is None:
+        a = np.zeros(shape, dtype=np.float32, order="F")
+        return a, a.ctypes.data
+    import torch
+    t = torch.zeros(tuple(reversed(shape)), dtype=torch.float32, device=like.device).t()
+    return t, t.data_ptr()
+
+
+def _prim_mat(m, like):
+    if _is_torch(m):
+        m = m.t().contiguous().t() if m.stride(0) != 1 else m
+        return m, m.data_ptr()
+    a = np.asfortranarray(np.asarray(m, dtype=np.float32))
+    return a, a.ctypes.data
+
+
+def _stream_of(like):
+    if like is None:
+        return None
+    import torch
+    return c_void_p(torch.cuda.current_stream(like.device).cuda_stream)
+
+
+def mode_gram(x, dims: Sequence[int], lo: int, hi: Optional[int] = None, precision: str = "bf16"):
+    """G = X_(g) X_(g)^T for the contiguous mode group lo..hi (0-based)."""
+    hi = lo if hi is None else hi
+    dims = tuple(int(d) for d in dims)
+    keep, xp, like = _prim_input(x, dims)
+    L, N, R = _prim_view(dims, lo, hi)
+    out, op = _prim_out((N, N), like)
+    check(lib().ht_mode_gram(c_void_p(xp), (c_long * 4)(*dims), len(dims), lo, hi, _PREC[precision], c_void_p(op),
+                             _stream_of(like)))
+    return out
+
+
+def mode_product(x, dims: Sequence[int], lo: int, W, hi: Optional[int] = None, precision: str = "bf16"):
+    """Z ((L*R) x k) = X_(g)^T W: the mode-group product with W (N x k)."""
+    hi = lo if hi is None else hi
+    dims = tuple(int(d) for d in dims)
+    keep, xp, like = _prim_input(x, dims)
+    L, N, R = _prim_view(dims, lo, hi)
+    Wk, wp = _prim_mat(W, like)
+    k = int(Wk.shape[1])
+    out, op = _prim_out((L * R, k), like)
+    check(lib().ht_mode_product(c_void_p(xp), (c_long * 4)(*dims), len(dims), lo, hi, c_void_p(wp), k,
+                                _PREC[precision], c_void_p(op), _stream_of(like)))
+    return out
+
+
+def corange_product(x, dims: Sequence[int], lo: int, Q, hi: Optional[int] = None, precision: str = "bf16"):
+    """Z (N x k) = X_(g) Q: contract every mode outside the group with Q ((L*R) x k)."""
+    hi = lo if hi is None else hi
+    dims = tuple(int(d) for d in dims)
+    keep, xp, like = _prim_input(x, dims)
+    L, N, R = _prim_view(dims, lo, hi)
+    Qk, qp = _prim_mat(Q, like)
+    k = int(Qk.shape[1])
+    out, op = _prim_out((N, k), like)
+    check(lib().ht_corange_product(c_void_p(xp), (c_long * 4)(*dims), len(dims), lo, hi, c_void_p(qp), k,
+                                   _PREC[precision], c_void_p(op), _stream_of(like)))
+    return out
+
+
+__all__ += ["mode_gram", "mode_product", "corange_product"]

@@ -1,0 +1,1254 @@
+// C ABI and host orchestration of the HT decomposition (see include/htgb.h).
+//
+// Algorithm (root-to-leaf hierarchical SVD, the reference's algorithm:
+// third_order_tensor_decompsition/CUDA/Optimized/htd_batch.cu:78-165,
+// Python/HT_TensorLy.py:52-72, 4D/.../htd4_tensorcore.cu:2-228):
+//   leaves      U_t = top-k_t eigenvectors of G_t = X_(t) X_(t)^T
+//   interior    U_t = top-k_t left singular vectors of X_(t)
+//   transfer    B_t = (U_r kron U_l)^T U_t,   B_root = U_l^T X_(l) U_r
+//
+// 3rd order.  The root's children are an interior node t = {p,q} and a leaf c
+// (the complementary mode).  X_(t)^T X_(t) = G_c, so with V = the top-k_t
+// eigenvectors of G_c the top-k_t left singular vectors of X_(t) are
+// U_t = X_(t) V P Lambda^-1/2, where V^T G_c V = P Lambda P^T.  Therefore
+//   B_t    = (U_q kron U_p)^T X_(t) V P Lambda^-1/2 = C_V P Lambda^-1/2
+//   B_root = U_t^T X_(t) U_c = Lambda^-1/2 P^T V^T G_c U_c
+// where C_V = X x_p U_p^T x_q U_q^T x_c V^T is the projected core.  The
+// interior node costs one streaming pass over X (the mode-c product) instead
+// of the reference's QR + SVD of the n^2 x n matricisation (kernel.cu:719-830).
+//
+// 4th order (balanced tree {1,2},{3,4}).  Both root children are interior:
+// a randomized range finder on A = X_(12) (Gaussian test matrix, oversampling
+// p, q power steps, CholeskyQR) gives Q with A ~ Q Q^T A; W = A^T Q and the
+// SVD of W from its Gram give U_12 = Q U_s, U_34 = W U_s Sigma^-1 and
+// B_root = Sigma (the reference uses the same range-finder idea,
+// 4D/.../Optimized/kernel.cu:419-500).
+//
+// Workspace: one cached device buffer per device, carved by a bump arena.
+// The whole pipeline first runs as a dry run (no launches) to size it.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/htgb.h"
+#include "common.cuh"
+#include "engine.h"
+
+using namespace htgb;
+
+namespace {
+
+thread_local std::string g_last_error;
+std::atomic<unsigned long long> g_launches{0};
+
+ht_status_t fail(ht_status_t s, const std::string &msg) {
+  g_last_error = msg;
+  return s;
+}
+
+#define HT_CUDA(expr)                                                                                   \
+  do {                                                                                                  \
+    cudaError_t _e = (expr);                                                                            \
+    if (_e != cudaSuccess)                                                                              \
+      return fail(_e == cudaErrorMemoryAllocation ? HT_ERR_OUT_OF_MEMORY : HT_ERR_CUDA,                 \
+                  std::string(#expr) + ": " + cudaGetErrorString(_e));                                  \
+  } while (0)
+
+#define HT_TRY(expr)            \
+  do {                          \
+    ht_status_t _s = (expr);    \
+    if (_s != HT_OK) return _s; \
+  } while (0)
+
+// ------------------------------------------------------------ workspace cache
+struct DeviceWorkspace {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+};
+std::mutex g_ws_mutex;
+DeviceWorkspace g_ws[64];
+
+// Bump allocator over one device buffer.  In dry-run mode it only counts.
+struct Arena {
+  char *base = nullptr;
+  size_t cap = 0, off = 0, peak = 0;
+  bool dry = false;
+  template <class T>
+  T *take(size_t count) {
+    const size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+    T *p = reinterpret_cast<T *>(base + off);
+    off += bytes;
+    peak = std::max(peak, off);
+    if (dry) return reinterpret_cast<T *>(static_cast<uintptr_t>(256));   // non-null, aligned placeholder
+    if (off > cap) return nullptr;
+    return p;
+  }
+};
+
+struct Tree {
+  int order = 0, n_nodes = 0;
+  int parent[HT_MAX_NODES], left[HT_MAX_NODES], right[HT_MAX_NODES], mask[HT_MAX_NODES], rank[HT_MAX_NODES];
+  bool leaf(int t) const { return left[t] < 0; }
+  int mode_of_leaf(int t) const {
+    for (int m = 0; m < order; ++m)
+      if (mask[t] == (1 << m)) return m;
+    return -1;
+  }
+  int leaf_of_mode(int m) const {
+    for (int t = 0; t < n_nodes; ++t)
+      if (leaf(t) && mask[t] == (1 << m)) return t;
+    return -1;
+  }
+};
+
+ht_status_t parse_tree(const ht_tree_t *in, const long *dims, int order, Tree &t) {
+  if (!in) return fail(HT_ERR_INVALID_ARG, "tree is NULL");
+  if (order != 3 && order != 4) return fail(HT_ERR_UNSUPPORTED, "only 3rd and 4th order tensors are supported");
+  if (in->order != order) return fail(HT_ERR_INVALID_ARG, "tree order does not match the tensor order");
+  if (in->n_nodes != 2 * order - 1) return fail(HT_ERR_INVALID_ARG, "a binary dimension tree has 2*order-1 nodes");
+  t.order = order;
+  t.n_nodes = in->n_nodes;
+  for (int i = 0; i < t.n_nodes; ++i) {
+    t.parent[i] = in->parent[i];
+    t.left[i] = in->left[i];
+    t.right[i] = in->right[i];
+    t.mask[i] = in->mode_mask[i];
+    t.rank[i] = in->rank[i];
+  }
+  if (t.mask[0] != (1 << order) - 1) return fail(HT_ERR_INVALID_ARG, "node 0 must be the root holding every mode");
+  if (t.parent[0] != -1) return fail(HT_ERR_INVALID_ARG, "the root has no parent");
+  int leaves = 0;
+  for (int i = 0; i < t.n_nodes; ++i) {
+    const int l = t.left[i], r = t.right[i];
+    if ((l < 0) != (r < 0)) return fail(HT_ERR_INVALID_ARG, "node " + std::to_string(i) + " needs zero or two children");
+    if (l >= t.n_nodes || r >= t.n_nodes || l == 0 || r == 0 || (l >= 0 && l == r))
+      return fail(HT_ERR_INVALID_ARG, "bad child index at node " + std::to_string(i));
+    if (l >= 0) {
+      if ((t.mask[l] | t.mask[r]) != t.mask[i] || (t.mask[l] & t.mask[r]) || !t.mask[l] || !t.mask[r])
+        return fail(HT_ERR_INVALID_ARG, "children of node " + std::to_string(i) + " must partition its modes");
+      if (t.parent[l] != i || t.parent[r] != i)
+        return fail(HT_ERR_INVALID_ARG, "parent[] inconsistent with left[]/right[] at node " + std::to_string(i));
+      if (i != 0) {
+        int hi_l = -1, lo_r = 64;
+        for (int m = 0; m < order; ++m) {
+          if (t.mask[l] & (1 << m)) hi_l = m;
+          if ((t.mask[r] & (1 << m)) && m < lo_r) lo_r = m;
+        }
+        if (hi_l > lo_r)
+          return fail(HT_ERR_INVALID_ARG, "node " + std::to_string(i) + ": left child's modes must precede the right child's");
+      }
+    } else {
+      if (__builtin_popcount(static_cast<unsigned>(t.mask[i])) != 1)
+        return fail(HT_ERR_INVALID_ARG, "leaf " + std::to_string(i) + " must hold one mode");
+      ++leaves;
+    }
+  }
+  if (leaves != order) return fail(HT_ERR_INVALID_ARG, "tree must have one leaf per mode");
+  for (int i = 0; i < order; ++i)
+    if (dims[i] < 1 || dims[i] > (1l << 30)) return fail(HT_ERR_INVALID_ARG, "dims must be positive");
+  long long total = 1;
+  for (int i = 0; i < order; ++i) total *= dims[i];
+  if (total > (1ll << 36)) return fail(HT_ERR_UNSUPPORTED, "tensor larger than 2^36 elements");
+  for (int i = 1; i < t.n_nodes; ++i) {
+    long long rows = 1, cols = 1;
+    for (int m = 0; m < order; ++m) (t.mask[i] & (1 << m) ? rows : cols) *= dims[m];
+    const int k = t.rank[i];
+    if (k < 1 || k > rows || k > cols)
+      return fail(HT_ERR_INVALID_ARG, "rank of node " + std::to_string(i) + " must lie in [1, min(rows, cols)]");
+    if (k > 64) return fail(HT_ERR_UNSUPPORTED, "ranks above 64 are not supported");
+    if (!t.leaf(i) && k > t.rank[t.left[i]] * t.rank[t.right[i]])
+      return fail(HT_ERR_INVALID_ARG, "rank of node " + std::to_string(i) + " exceeds k_left * k_right");
+  }
+  if (order == 4) {
+    const int l = t.left[0], r = t.right[0];
+    if (t.leaf(l) || t.leaf(r) || t.mask[l] != 0x3 || t.mask[r] != 0xC)
+      return fail(HT_ERR_UNSUPPORTED, "4th order: the root's children must be {1,2} (left) and {3,4} (right)");
+  } else {
+    if (t.leaf(t.left[0]) == t.leaf(t.right[0]))
+      return fail(HT_ERR_INVALID_ARG, "3rd order: the root needs one leaf and one interior child");
+  }
+  return HT_OK;
+}
+
+struct Ctx {
+  cudaStream_t st = nullptr;
+  int *err = nullptr;   // device error word
+  Arena ar;
+  int launches = 0;
+  int path = 0;         // bit 0 tcgen05, bit 1 SIMT
+  bool tc = false;
+  bool dry() const { return ar.dry; }
+};
+
+View view_of_group(const long *dims, int order, int lo, int hi) {   // modes [lo, hi]
+  View v{1, 1, 1};
+  for (int m = 0; m < order; ++m) {
+    if (m < lo) v.L *= dims[m];
+    else if (m <= hi) v.N *= dims[m];
+    else v.R *= dims[m];
+  }
+  return v;
+}
+
+// Operand whose rows are the middle index of v and whose K runs over (l, r).
+Operand gram_operand(const View &v, const void *x) {
+  Operand o;
+  o.ptr = x;
+  if (v.L == 1) {
+    o.kind = OP_MN3; o.d0 = v.N; o.d1 = v.R; o.d2 = 1;
+  } else {
+    o.kind = OP_KM3; o.d0 = v.L; o.d1 = v.N; o.d2 = v.R;
+  }
+  return o;
+}
+
+int g_sms = 0;
+int sm_count() {
+  if (!g_sms) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaGetLastError();
+    if (g_sms <= 0) g_sms = 148;
+  }
+  return g_sms;
+}
+
+struct GemmReq {
+  Operand a32, b32;                 // FP32 operands (SIMT path)
+  Operand a16, b16;                 // BF16 operands (tcgen05 path); ptr null = unavailable
+  int bn_tc = 128, bn_simt = 128;
+  std::vector<Tile> (*make_tiles)(const void *ctx, int bn) = nullptr;
+  const void *tile_ctx = nullptr;
+  int out_mode = OUT_COLMAJOR;
+  float *out = nullptr;
+  long long ld_out = 0;
+  bool symmetric = false;
+  bool allow_split = true;
+};
+
+// D = A B^T over the tiles: tcgen05 on the BF16 operands when the context
+// allows it and the shapes map to TMA, else SIMT on the FP32 operands.
+ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
+  bool use_tc = c.tc && q.a16.ptr && q.b16.ptr;
+  if (use_tc) {
+    GemmArgs probe;
+    probe.a = q.a16; probe.b = q.b16; probe.splits = 1;
+    std::string why;
+    if (!tc_gemm_supported(probe, q.bn_tc, &why)) use_tc = false;
+  }
+  const int bn = use_tc ? q.bn_tc : q.bn_simt;
+  std::vector<Tile> tiles = q.make_tiles(q.tile_ctx, bn);
+  const int nt = static_cast<int>(tiles.size());
+  int splits = 1;
+  if (q.allow_split && nt < sm_count()) splits = std::max(1, sm_count() / nt);
+  if (use_tc) {
+    const long nkb = tc_num_kblocks(q.a16);
+    long per = (nkb + splits - 1) / splits;
+    per = std::max<long>(per, std::min<long>(nkb, 16));   // keep the smem pipeline busy
+    splits = static_cast<int>((nkb + per - 1) / per);
+  } else {
+    const long kt = simt_k_total(q.a32);
+    long per = (kt + splits - 1) / splits;
+    per = std::max<long>((per + 15) / 16 * 16, 256);
+    splits = static_cast<int>(std::max<long>(1, (kt + per - 1) / per));
+  }
+  const bool partial = splits > 1 || q.out_mode == OUT_PARTIAL;
+  const size_t mark = c.ar.off;
+  Tile *dt = c.ar.take<Tile>(nt);
+  float *part = partial ? c.ar.take<float>(static_cast<size_t>(splits) * nt * 128 * bn) : nullptr;
+  if (c.dry()) {
+    c.ar.off = mark;
+    return HT_OK;
+  }
+  if (!dt || (partial && !part)) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (gemm scratch)");
+  HT_CUDA(cudaMemcpyAsync(dt, tiles.data(), sizeof(Tile) * nt, cudaMemcpyHostToDevice, c.st));
+  GemmArgs g;
+  g.a = use_tc ? q.a16 : q.a32;
+  g.b = use_tc ? q.b16 : q.b32;
+  g.tiles = dt;
+  g.num_tiles = nt;
+  g.splits = splits;
+  g.out_mode = partial ? OUT_PARTIAL : OUT_COLMAJOR;
+  g.out = partial ? part : q.out;
+  g.ld_out = q.ld_out;
+  g.err = c.err;
+  if (use_tc) {
+    HT_CUDA(tc_gemm_launch(g, bn, c.st));
+    c.path |= 1;
+  } else {
+    HT_CUDA(simt_gemm_launch(g, bn, c.st));
+    c.path |= 2;
+  }
+  ++c.launches;
+  if (partial) {
+    HT_CUDA(reduce_partials_launch(part, dt, nt, splits, bn, q.out, q.ld_out, q.symmetric ? 1 : 0, c.st));
+    ++c.launches;
+  }
+  c.ar.off = mark;   // scratch is stream-ordered: later work may reuse it
+  return HT_OK;
+}
+
+// ---- tile generators
+struct GramTiles { long n; };
+std::vector<Tile> gram_tiles(const void *ctx, int bn) {
+  const long n = static_cast<const GramTiles *>(ctx)->n;
+  std::vector<Tile> v;
+  for (long i = 0; i * 128 < n; ++i)
+    for (long j = 0; j * bn < n; ++j) {
+      if (j * bn + bn - 1 < i * 128) continue;   // entirely below the diagonal
+      Tile t;
+      t.a_row = static_cast<int>(i * 128); t.a_z = 0; t.b_row = static_cast<int>(j * bn);
+      t.out_row = i * 128; t.out_col = static_cast<int>(j * bn);
+      t.valid_rows = static_cast<int>(std::min<long>(128, n - i * 128));
+      t.valid_cols = static_cast<int>(std::min<long>(bn, n - j * bn));
+      v.push_back(t);
+    }
+  return v;
+}
+struct RowTiles { long rows; int cols; };
+std::vector<Tile> row_tiles(const void *ctx, int bn) {
+  const RowTiles *r = static_cast<const RowTiles *>(ctx);
+  std::vector<Tile> v;
+  for (long i = 0; i < r->rows; i += 128) {
+    Tile t;
+    t.a_row = static_cast<int>(i); t.a_z = 0; t.b_row = 0;
+    t.out_row = i; t.out_col = 0;
+    t.valid_rows = static_cast<int>(std::min<long>(128, r->rows - i));
+    t.valid_cols = std::min(r->cols, bn);
+    v.push_back(t);
+  }
+  return v;
+}
+struct SlabTiles { long L, R; int cols; };
+std::vector<Tile> slab_tiles(const void *ctx, int bn) {
+  const SlabTiles *s = static_cast<const SlabTiles *>(ctx);
+  std::vector<Tile> v;
+  for (long r = 0; r < s->R; ++r)
+    for (long l = 0; l < s->L; l += 128) {
+      Tile t;
+      t.a_row = static_cast<int>(l); t.a_z = static_cast<int>(r); t.b_row = 0;
+      t.out_row = l + s->L * r; t.out_col = 0;
+      t.valid_rows = static_cast<int>(std::min<long>(128, s->L - l));
+      t.valid_cols = std::min(s->cols, bn);
+      v.push_back(t);
+    }
+  return v;
+}
+
+// G (n x n, column-major, symmetric) = X_(group) X_(group)^T, n = v.N
+ht_status_t gram(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x16, float *G) {
+  GemmReq q;
+  q.a32 = q.b32 = gram_operand(v, x32);
+  if (x16) q.a16 = q.b16 = gram_operand(v, x16);
+  else q.a16.ptr = q.b16.ptr = nullptr;
+  q.bn_tc = v.N >= 256 ? 256 : (v.N > 64 ? 128 : 64);
+  q.bn_simt = v.N > 64 ? 128 : 64;
+  GramTiles gt{v.N};
+  q.make_tiles = gram_tiles;
+  q.tile_ctx = &gt;
+  q.out_mode = OUT_PARTIAL;
+  q.out = G;
+  q.ld_out = v.N;
+  q.symmetric = true;
+  return run_gemm(c, q);
+}
+
+// Z ((L*R) x k, column-major) = contraction of the middle index of view v with W (v.N x k)
+ht_status_t mode_product(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x16, const float *W32,
+                         const __nv_bfloat16 *W16, int k, float *Z) {
+  GemmReq q;
+  auto opA = [&](const void *x) {
+    Operand o;
+    o.ptr = x;
+    if (v.L == 1) {
+      o.kind = OP_KM3; o.d0 = v.N; o.d1 = v.R; o.d2 = 1;
+    } else {
+      o.kind = OP_MN3; o.d0 = v.L; o.d1 = v.N; o.d2 = v.R;
+    }
+    return o;
+  };
+  auto opB = [&](const void *w) {
+    Operand o;
+    o.ptr = w; o.kind = OP_KM3; o.d0 = v.N; o.d1 = k; o.d2 = 1;
+    return o;
+  };
+  q.a32 = opA(x32); q.b32 = opB(W32);
+  if (x16 && W16) { q.a16 = opA(x16); q.b16 = opB(W16); }
+  else q.a16.ptr = q.b16.ptr = nullptr;
+  q.bn_tc = 64; q.bn_simt = 64;
+  RowTiles rt{v.R, k};
+  SlabTiles stl{v.L, v.R, k};
+  if (v.L == 1) { q.make_tiles = row_tiles; q.tile_ctx = &rt; }
+  else { q.make_tiles = slab_tiles; q.tile_ctx = &stl; }
+  q.out_mode = OUT_COLMAJOR;
+  q.out = Z;
+  q.ld_out = v.L * v.R;
+  return run_gemm(c, q);
+}
+
+// Z (v.N x k, column-major) = X_(group) Q with Q ((L*R) x k): contract every index but the middle one
+ht_status_t corange_product(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x16, const float *Q32,
+                            const __nv_bfloat16 *Q16, int k, float *Z) {
+  GemmReq q;
+  auto opB = [&](const void *p) {
+    Operand o;
+    o.ptr = p;
+    if (v.L == 1) {
+      o.kind = OP_KM3; o.d0 = v.R; o.d1 = k; o.d2 = 1;
+    } else {
+      o.kind = OP_KM3Q; o.d0 = v.L; o.d1 = v.R; o.d2 = k;
+    }
+    return o;
+  };
+  q.a32 = gram_operand(v, x32); q.b32 = opB(Q32);
+  if (x16 && Q16) { q.a16 = gram_operand(v, x16); q.b16 = opB(Q16); }
+  else q.a16.ptr = q.b16.ptr = nullptr;
+  q.bn_tc = 64; q.bn_simt = 64;
+  RowTiles rt{v.N, k};
+  q.make_tiles = row_tiles;
+  q.tile_ctx = &rt;
+  q.out_mode = OUT_COLMAJOR;
+  q.out = Z;
+  q.ld_out = v.N;
+  return run_gemm(c, q);
+}
+
+// C[a + kp*b + kp*kq*u] = sum_{i,j} Up[i,a] Uq[j,b] Z[i + np*j, u]   (FP32)
+ht_status_t core_contract(Ctx &c, const float *Z, int np, int nq, int ku, const float *Up, int kp, const float *Uq,
+                          int kq, float *C) {
+  const size_t mark = c.ar.off;
+  const long long rows = static_cast<long long>(nq) * ku;
+  float *T1 = c.ar.take<float>(static_cast<size_t>(rows) * kp);
+  if (!T1) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (core)");
+  // T1[(j + nq*u) + rows*a] = sum_i Z[i + np*(j + nq*u)] Up[i + np*a]
+  GemmReq q;
+  q.a32.kind = OP_KM3; q.a32.ptr = Z; q.a32.d0 = np; q.a32.d1 = rows; q.a32.d2 = 1;
+  q.b32.kind = OP_KM3; q.b32.ptr = Up; q.b32.d0 = np; q.b32.d1 = kp; q.b32.d2 = 1;
+  q.a16.ptr = q.b16.ptr = nullptr;
+  q.bn_simt = 64;
+  RowTiles rt{rows, kp};
+  q.make_tiles = row_tiles;
+  q.tile_ctx = &rt;
+  q.out_mode = OUT_COLMAJOR;
+  q.out = T1;
+  q.ld_out = rows;
+  HT_TRY(run_gemm(c, q));
+  if (!c.dry()) {
+    HT_CUDA(core_step2_launch(T1, rows, nq, kp, Uq, kq, ku, C, c.st));
+    ++c.launches;
+  }
+  c.ar.off = mark;
+  return HT_OK;
+}
+
+bool is_device_ptr(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+ht_status_t check_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(HT_ERR_NO_DEVICE, "no CUDA device");
+  }
+  cudaDeviceProp prop;
+  HT_CUDA(cudaGetDeviceProperties(&prop, dev));
+  if (!(prop.major == 10 && prop.minor == 3))
+    return fail(HT_ERR_NO_DEVICE, std::string("this build targets sm_103a (GB300); device is ") + prop.name);
+  return HT_OK;
+}
+
+ht_status_t acquire_workspace(size_t bytes, void **ptr, cudaStream_t st) {
+  int dev = 0;
+  HT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(HT_ERR_INVALID_ARG, "device index out of range");
+  DeviceWorkspace &w = g_ws[dev];
+  if (w.bytes < bytes) {
+    if (w.ptr) {
+      HT_CUDA(cudaStreamSynchronize(st));
+      HT_CUDA(cudaDeviceSynchronize());
+      HT_CUDA(cudaFree(w.ptr));
+      w.ptr = nullptr;
+      w.bytes = 0;
+    }
+    HT_CUDA(cudaMalloc(&w.ptr, bytes));
+    w.bytes = bytes;
+  }
+  *ptr = w.ptr;
+  return HT_OK;
+}
+
+// ----------------------------------------------------------------- pipeline
+struct Plan3 {
+  int t, c, p, q;           // interior root child, complementary leaf, t's children
+  int mc, mp, mq;           // modes of c, p, q
+  int kt, kc, kp, kq, kw;   // kw = max(kc, kt)
+  bool t_is_left;
+};
+
+Plan3 plan3(const Tree &T) {
+  Plan3 P;
+  const int l = T.left[0], r = T.right[0];
+  P.t_is_left = !T.leaf(l);
+  P.t = P.t_is_left ? l : r;
+  P.c = P.t_is_left ? r : l;
+  P.p = T.left[P.t];
+  P.q = T.right[P.t];
+  P.mc = T.mode_of_leaf(P.c);
+  P.mp = T.mode_of_leaf(P.p);
+  P.mq = T.mode_of_leaf(P.q);
+  P.kt = T.rank[P.t]; P.kc = T.rank[P.c]; P.kp = T.rank[P.p]; P.kq = T.rank[P.q];
+  P.kw = std::max(P.kc, P.kt);
+  return P;
+}
+
+// Device-resident results of one decomposition (workspace pointers).
+struct Result {
+  const float *U[HT_MAX_NODES] = {};   // leaves: n_t x k_t (leading columns of the Ritz block)
+  const float *B[HT_MAX_NODES] = {};   // interior nodes and root
+  const float *resid[HT_MAX_NODES] = {};
+};
+
+struct Timeline {
+  cudaEvent_t ev[8];
+  int n = 0;
+  bool on = false;
+  void mark(cudaStream_t s) {
+    if (on && n < 8) cudaEventRecord(ev[n++], s);
+  }
+};
+
+ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const float *x32,
+                           const __nv_bfloat16 *x16, const long *dims, int order, Result &res, Timeline &tl) {
+  const int p_over = cfg.oversample > 0 ? cfg.oversample : 16;
+  const int iters = cfg.eig_iters > 0 ? cfg.eig_iters : 10;
+  const bool d3 = order == 3;
+  Plan3 P3{};
+  if (d3) P3 = plan3(T);
+
+  // 1. leaf Grams
+  float *G[4] = {};
+  for (int m = 0; m < order; ++m) {
+    G[m] = c.ar.take<float>(static_cast<size_t>(dims[m]) * dims[m]);
+    if (!G[m]) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (Gram)");
+  }
+  for (int m = 0; m < order; ++m) HT_TRY(gram(c, view_of_group(dims, order, m, m), x32, x16, G[m]));
+  tl.mark(c.st);
+
+  // 2. top-K eigenvectors of every leaf Gram, one batch
+  EigProblem ep[4];
+  for (int m = 0; m < order; ++m) {
+    const int leaf = T.leaf_of_mode(m);
+    const int K = (d3 && leaf == P3.c) ? P3.kw : T.rank[leaf];
+    const int n = static_cast<int>(dims[m]);
+    const int s = std::max(K, std::min<int>({n, K + p_over, 64}));
+    if (s > 64) return fail(HT_ERR_UNSUPPORTED, "subspace size above 64");
+    EigProblem &e = ep[m];
+    e.G = G[m]; e.n = n; e.s = s; e.K = K;
+    e.Q = c.ar.take<float>(static_cast<size_t>(n) * s);
+    e.Y = c.ar.take<float>(static_cast<size_t>(n) * s);
+    e.U = c.ar.take<float>(static_cast<size_t>(n) * K);
+    e.GU = c.ar.take<float>(static_cast<size_t>(n) * K);
+    e.theta = c.ar.take<float>(64);
+    e.resid = c.ar.take<float>(4);
+    e.seed = cfg.seed;
+    e.stream_id = static_cast<uint64_t>(m);
+    e.start = nullptr;
+    if (cfg.sketch[m]) {
+      if (is_device_ptr(cfg.sketch[m])) {
+        e.start = cfg.sketch[m];
+      } else {
+        float *d = c.ar.take<float>(static_cast<size_t>(n) * s);
+        if (!d) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (start block)");
+        if (!c.dry()) HT_CUDA(cudaMemcpyAsync(d, cfg.sketch[m], sizeof(float) * n * s, cudaMemcpyHostToDevice, c.st));
+        e.start = d;
+      }
+    }
+    if (!e.Q || !e.Y || !e.U || !e.GU) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (eig)");
+    res.U[leaf] = e.U;
+    res.resid[leaf] = e.resid;
+  }
+  {
+    const size_t mark = c.ar.off;
+    const size_t eb = eig_workspace_bytes(ep, order);
+    void *ews = c.ar.take<char>(eb);
+    if (!ews) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (eig)");
+    if (!c.dry()) HT_CUDA(eig_batched(ep, order, iters, ews, eb, c.err, c.st, &c.launches));
+    c.ar.off = mark;
+  }
+  tl.mark(c.st);
+
+  if (d3) {
+    const Plan3 &P = P3;
+    const View vc = view_of_group(dims, 3, P.mc, P.mc);
+    const long long zrows = vc.L * vc.R;
+    const EigProblem &ec = ep[P.mc];
+    float *C = c.ar.take<float>(static_cast<size_t>(P.kp) * P.kq * P.kt);
+    float *WG = c.ar.take<float>(static_cast<size_t>(P.kw) * P.kw);
+    float *M = c.ar.take<float>(static_cast<size_t>(P.kt) * P.kt);
+    float *Bkt = c.ar.take<float>(static_cast<size_t>(P.kt) * P.kc);
+    float *Broot = c.ar.take<float>(static_cast<size_t>(P.kt) * P.kc);
+    float *Bt = c.ar.take<float>(static_cast<size_t>(P.kp) * P.kq * P.kt);
+    if (!C || !WG || !M || !Bkt || !Broot || !Bt) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (transfer)");
+    const size_t mark = c.ar.off;
+    float *Z = c.ar.take<float>(static_cast<size_t>(zrows) * P.kt);
+    __nv_bfloat16 *V16 = c.tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(dims[P.mc]) * P.kt + 64) : nullptr;
+    if (!Z || (c.tc && !V16)) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (core pass)");
+    // 3. core pass: Z = X_(t) V, V = leading kt columns of the complementary leaf's Ritz block
+    if (V16 && !c.dry()) {
+      HT_CUDA(f32_to_bf16_launch(ec.U, V16, static_cast<long long>(dims[P.mc]) * P.kt, c.st));
+      ++c.launches;
+    }
+    HT_TRY(mode_product(c, vc, x32, x16, ec.U, V16, P.kt, Z));
+    tl.mark(c.st);
+    // 4. transfer tensors
+    HT_TRY(core_contract(c, Z, static_cast<int>(dims[P.mp]), static_cast<int>(dims[P.mq]), P.kt, ep[P.mp].U, P.kp,
+                         ep[P.mq].U, P.kq, C));
+    c.ar.off = mark;
+    if (!c.dry()) {
+      const int nc = static_cast<int>(dims[P.mc]);
+      HT_CUDA(gemm_tn_small_launch(ec.U, nc, ec.GU, nc, WG, P.kw, P.kw, P.kw, nc, c.st));
+      HT_CUDA(transfer_eig_launch(WG, P.kw, P.kt, P.kc, 1, M, Bkt, c.st));
+      const long long kpq = static_cast<long long>(P.kp) * P.kq;
+      HT_CUDA(matmul_nn_launch(C, kpq, M, P.kt, Bt, kpq, kpq, P.kt, P.kt, c.st));
+      c.launches += 3;
+      if (!P.t_is_left) {
+        HT_CUDA(transpose_small_launch(Bkt, P.kt, P.kc, Broot, c.st));
+        ++c.launches;
+      }
+    }
+    res.B[P.t] = Bt;
+    res.B[0] = P.t_is_left ? Bkt : Broot;
+    tl.mark(c.st);
+    return HT_OK;
+  }
+
+  // 4th order: range finder on A = X_(12) (nA x mA, column-major)
+  const int t1 = T.left[0], t2 = T.right[0];
+  const int k1 = T.rank[t1], k2 = T.rank[t2];
+  const long long nA = static_cast<long long>(dims[0]) * dims[1], mA = static_cast<long long>(dims[2]) * dims[3];
+  const int s = static_cast<int>(std::min<long long>({static_cast<long long>(std::max(k1, k2) + p_over), 64ll, nA, mA}));
+  const int qsteps = cfg.power_steps >= 0 ? cfg.power_steps : 1;
+  const int a1 = T.left[t1], b1 = T.right[t1], a2 = T.left[t2], b2 = T.right[t2];
+  float *Broot = c.ar.take<float>(static_cast<size_t>(k1) * k2);
+  float *B12 = c.ar.take<float>(static_cast<size_t>(T.rank[a1]) * T.rank[b1] * k1);
+  float *B34 = c.ar.take<float>(static_cast<size_t>(T.rank[a2]) * T.rank[b2] * k2);
+  if (!Broot || !B12 || !B34) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (transfer)");
+  const size_t mark = c.ar.off;
+  float *Om = c.ar.take<float>(static_cast<size_t>(mA) * s);
+  float *Yq = c.ar.take<float>(static_cast<size_t>(nA) * s);
+  float *Wz = c.ar.take<float>(static_cast<size_t>(mA) * s);
+  __nv_bfloat16 *B16 = c.tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(std::max(nA, mA)) * s + 64) : nullptr;
+  float *GW = c.ar.take<float>(static_cast<size_t>(s) * s);
+  float *M1 = c.ar.take<float>(static_cast<size_t>(s) * s);
+  float *M2 = c.ar.take<float>(static_cast<size_t>(s) * s);
+  float *U12 = c.ar.take<float>(static_cast<size_t>(nA) * k1);
+  float *U34 = c.ar.take<float>(static_cast<size_t>(mA) * k2);
+  EigProblem cq;
+  cq.G = nullptr; cq.n = static_cast<int>(std::max(nA, mA)); cq.s = s; cq.K = s;
+  const size_t cbytes = eig_workspace_bytes(&cq, 1);
+  void *cws = c.ar.take<char>(cbytes);
+  if (!Om || !Yq || !Wz || !GW || !M1 || !M2 || !U12 || !U34 || !cws || (c.tc && !B16))
+    return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (range finder)");
+  const View vy{static_cast<long>(nA), static_cast<long>(mA), 1};
+  auto orth = [&](float *Qm, long long rows) -> ht_status_t {
+    if (c.dry()) return HT_OK;
+    EigProblem e;
+    e.G = nullptr; e.n = static_cast<int>(rows); e.s = s; e.K = s; e.Q = Qm; e.Y = nullptr;
+    e.U = e.GU = e.theta = e.resid = nullptr; e.start = nullptr; e.seed = 0; e.stream_id = 0;
+    HT_CUDA(cholqr_batched(&e, 1, 3, cws, cbytes, c.st, &c.launches));
+    return HT_OK;
+  };
+  auto to16 = [&](const float *src, long long count) -> const __nv_bfloat16 * {
+    if (!B16) return nullptr;
+    if (!c.dry()) {
+      if (f32_to_bf16_launch(src, B16, count, c.st) != cudaSuccess) return nullptr;
+      ++c.launches;
+    }
+    return B16;
+  };
+  if (!c.dry()) {
+    HT_CUDA(gaussian_fill_launch(Om, mA * s, cfg.seed, 100, c.st));
+    ++c.launches;
+  }
+  HT_TRY(mode_product(c, vy, x32, x16, Om, to16(Om, mA * s), s, Yq));        // Y = A Omega
+  HT_TRY(orth(Yq, nA));
+  for (int it = 0; it < qsteps; ++it) {
+    HT_TRY(corange_product(c, vy, x32, x16, Yq, to16(Yq, nA * s), s, Wz));   // Z = A^T Q
+    HT_TRY(orth(Wz, mA));
+    HT_TRY(mode_product(c, vy, x32, x16, Wz, to16(Wz, mA * s), s, Yq));      // Y = A Z
+    HT_TRY(orth(Yq, nA));
+  }
+  HT_TRY(corange_product(c, vy, x32, x16, Yq, to16(Yq, nA * s), s, Wz));     // W = A^T Q
+  tl.mark(c.st);
+  if (!c.dry()) {
+    HT_CUDA(gemm_tn_small_launch(Wz, static_cast<int>(mA), Wz, static_cast<int>(mA), GW, s, s, s, static_cast<int>(mA), c.st));
+    HT_CUDA(svd_from_gram_launch(GW, s, k1, k2, M1, M2, Broot, c.st));
+    HT_CUDA(matmul_nn_launch(Yq, nA, M1, s, U12, nA, nA, k1, s, c.st));
+    HT_CUDA(matmul_nn_launch(Wz, mA, M2, s, U34, mA, mA, k2, s, c.st));
+    c.launches += 4;
+  }
+  HT_TRY(core_contract(c, U12, static_cast<int>(dims[0]), static_cast<int>(dims[1]), k1, ep[0].U, T.rank[a1], ep[1].U,
+                       T.rank[b1], B12));
+  HT_TRY(core_contract(c, U34, static_cast<int>(dims[2]), static_cast<int>(dims[3]), k2, ep[2].U, T.rank[a2], ep[3].U,
+                       T.rank[b2], B34));
+  c.ar.off = mark;
+  res.B[t1] = B12;
+  res.B[t2] = B34;
+  res.B[0] = Broot;
+  tl.mark(c.st);
+  return HT_OK;
+}
+
+// ||X - Xhat||_F^2 of an HT representation, into *dev_out (device double).
+ht_status_t error_core(Ctx &c, const Tree &T, const float *x32, const long *dims, int order, const float *const *U,
+                       const float *const *B, double *dev_out) {
+  const size_t mark = c.ar.off;
+  int nb = 0;
+  double *parts = nullptr;
+  if (order == 3) {
+    const Plan3 P = plan3(T);
+    const long np_ = dims[P.mp], nq_ = dims[P.mq], nc_ = dims[P.mc];
+    float *Bkt = c.ar.take<float>(static_cast<size_t>(P.kt) * P.kc);
+    float *core = c.ar.take<float>(static_cast<size_t>(P.kp) * P.kq * P.kc);
+    float *Tm = c.ar.take<float>(static_cast<size_t>(np_) * P.kq * P.kc);
+    float *Wm = c.ar.take<float>(static_cast<size_t>(np_) * nq_ * P.kc);
+    long long Rr, Cc;
+    int batch = 1;
+    if (P.mc == 2) { Rr = np_ * nq_; Cc = nc_; }
+    else if (P.mc == 0) { Rr = nc_; Cc = np_ * nq_; }
+    else { Rr = np_; Cc = nc_; batch = static_cast<int>(nq_); }
+    nb = error_fused_blocks(Rr, Cc) * batch;
+    parts = c.ar.take<double>(static_cast<size_t>(nb) + 8);
+    if (!Bkt || !core || !Tm || !Wm || !parts) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (error)");
+    if (!c.dry()) {
+      if (P.t_is_left) HT_CUDA(cudaMemcpyAsync(Bkt, B[0], sizeof(float) * P.kt * P.kc, cudaMemcpyDeviceToDevice, c.st));
+      else HT_CUDA(transpose_small_launch(B[0], P.kc, P.kt, Bkt, c.st));
+      const long long kpq = static_cast<long long>(P.kp) * P.kq;
+      HT_CUDA(matmul_nn_launch(B[P.t], kpq, Bkt, P.kt, core, kpq, kpq, P.kc, P.kt, c.st));
+      HT_CUDA(expand2_launch(U[P.p], static_cast<int>(np_), P.kp, core, U[P.q], static_cast<int>(nq_), P.kq, P.kc, Tm,
+                             Wm, c.st));
+      if (P.mc == 2)         // X_(01) = W U_c^T
+        HT_CUDA(error_fused_launch(x32, Rr, 0, Wm, Rr, 0, U[P.c], nc_, Rr, Cc, P.kc, 1, parts, c.st));
+      else if (P.mc == 0)    // X_(0) = U_c W^T
+        HT_CUDA(error_fused_launch(x32, Rr, 0, U[P.c], nc_, 0, Wm, np_ * nq_, Rr, Cc, P.kc, 1, parts, c.st));
+      else                   // slab i2 of X (n0 x n1) = W[(i0, i2), :] U_1^T
+        HT_CUDA(error_fused_launch(x32, np_, np_ * nc_, Wm, np_ * nq_, np_, U[P.c], nc_, Rr, Cc, P.kc, batch, parts,
+                                   c.st));
+      c.launches += 5;
+    }
+  } else {
+    const int t1 = T.left[0], t2 = T.right[0];
+    const int k1 = T.rank[t1], k2 = T.rank[t2];
+    const int a1 = T.left[t1], b1 = T.right[t1], a2 = T.left[t2], b2 = T.right[t2];
+    const long long R = static_cast<long long>(dims[0]) * dims[1], Cn = static_cast<long long>(dims[2]) * dims[3];
+    float *T1 = c.ar.take<float>(static_cast<size_t>(dims[0]) * T.rank[b1] * k1);
+    float *W12 = c.ar.take<float>(static_cast<size_t>(R) * k1);
+    float *A12 = c.ar.take<float>(static_cast<size_t>(R) * k2);
+    float *T2 = c.ar.take<float>(static_cast<size_t>(dims[2]) * T.rank[b2] * k2);
+    float *W34 = c.ar.take<float>(static_cast<size_t>(Cn) * k2);
+    nb = error_fused_blocks(R, Cn);
+    parts = c.ar.take<double>(static_cast<size_t>(nb) + 8);
+    if (!T1 || !W12 || !A12 || !T2 || !W34 || !parts) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (error)");
+    if (!c.dry()) {
+      HT_CUDA(expand2_launch(U[a1], static_cast<int>(dims[0]), T.rank[a1], B[t1], U[b1], static_cast<int>(dims[1]),
+                             T.rank[b1], k1, T1, W12, c.st));
+      HT_CUDA(expand2_launch(U[a2], static_cast<int>(dims[2]), T.rank[a2], B[t2], U[b2], static_cast<int>(dims[3]),
+                             T.rank[b2], k2, T2, W34, c.st));
+      HT_CUDA(matmul_nn_launch(W12, R, B[0], k1, A12, R, R, k2, k1, c.st));
+      HT_CUDA(error_fused_launch(x32, R, 0, A12, R, 0, W34, Cn, R, Cn, k2, 1, parts, c.st));
+      c.launches += 6;
+    }
+  }
+  if (!c.dry()) {
+    HT_CUDA(sumsq_finish_launch(parts, nb, dev_out, c.st));
+    ++c.launches;
+  }
+  c.ar.off = mark;
+  return HT_OK;
+}
+
+size_t factor_count(const Tree &T, const long *dims, int t) {
+  if (T.leaf(t)) return static_cast<size_t>(dims[T.mode_of_leaf(t)]) * T.rank[t];
+  return static_cast<size_t>(T.rank[T.left[t]]) * T.rank[T.right[t]] * T.rank[t];
+}
+
+// One full call (decomposition, outputs, optional error), used both as the
+// dry run that sizes the workspace and for the real run.
+struct CallArgs {
+  const float *x;
+  bool x_dev;
+  const long *dims;
+  int order;
+  float *const *U;
+  float *const *B;
+  bool want_err;
+};
+
+ht_status_t run_call(Ctx &c, const Tree &T, const ht_config_t &cfg, const CallArgs &a, ht_report_t *rep) {
+  long long total = 1;
+  for (int m = 0; m < a.order; ++m) total *= a.dims[m];
+  c.err = c.ar.take<int>(64);
+  double *nparts = c.ar.take<double>(1024);
+  double *dsum = c.ar.take<double>(8);
+  if (!c.err || !nparts || !dsum) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small");
+  Timeline tl;
+  tl.on = rep != nullptr && !c.dry();
+  cudaEvent_t h0 = nullptr, h1 = nullptr;
+  if (tl.on) {
+    for (int i = 0; i < 8; ++i) HT_CUDA(cudaEventCreate(&tl.ev[i]));
+    HT_CUDA(cudaEventCreate(&h0));
+    HT_CUDA(cudaEventCreate(&h1));
+  }
+  struct Guard {
+    Timeline &tl;
+    cudaEvent_t a, b;
+    ~Guard() {
+      if (tl.on) {
+        for (int i = 0; i < 8; ++i) cudaEventDestroy(tl.ev[i]);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+      }
+    }
+  } guard{tl, h0, h1};
+  if (!c.dry()) HT_CUDA(cudaMemsetAsync(c.err, 0, sizeof(int), c.st));
+  if (tl.on) HT_CUDA(cudaEventRecord(h0, c.st));
+  const float *xd = a.x;
+  if (!a.x_dev) {
+    float *t = c.ar.take<float>(static_cast<size_t>(total));
+    if (!t) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (tensor)");
+    if (!c.dry()) HT_CUDA(cudaMemcpyAsync(t, a.x, sizeof(float) * total, cudaMemcpyHostToDevice, c.st));
+    xd = t;
+  }
+  if (tl.on) HT_CUDA(cudaEventRecord(h1, c.st));
+  tl.mark(c.st);
+  __nv_bfloat16 *xb = nullptr;
+  if (c.tc) {
+    xb = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
+    if (!xb) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (bf16 tensor)");
+    if (!c.dry()) HT_CUDA(convert_bf16_launch(xd, xb, total, nparts, 1024, c.st));
+  } else if (!c.dry()) {
+    HT_CUDA(sumsq_launch(xd, total, nparts, 1024, c.st));
+  }
+  if (!c.dry()) {
+    HT_CUDA(sumsq_finish_launch(nparts, 1024, dsum, c.st));
+    c.launches += 2;
+  }
+  tl.mark(c.st);
+  Result res;
+  HT_TRY(decompose_core(c, T, cfg, xd, xb, a.dims, a.order, res, tl));
+  // outputs to the caller's buffers (host or device)
+  for (int t = 0; t < T.n_nodes; ++t) {
+    float *dst = T.leaf(t) ? a.U[t] : a.B[t];
+    const float *src = T.leaf(t) ? res.U[t] : res.B[t];
+    if (dst && !c.dry()) HT_CUDA(cudaMemcpyAsync(dst, src, factor_count(T, a.dims, t) * sizeof(float), cudaMemcpyDefault, c.st));
+  }
+  if (a.want_err) HT_TRY(error_core(c, T, xd, a.dims, a.order, res.U, res.B, dsum + 1));
+  if (c.dry()) return HT_OK;
+  double host_sums[2] = {0.0, 0.0};
+  HT_CUDA(cudaMemcpyAsync(host_sums, dsum, sizeof(double) * (a.want_err ? 2 : 1), cudaMemcpyDeviceToHost, c.st));
+  int errword = 0;
+  HT_CUDA(cudaMemcpyAsync(&errword, c.err, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+  float resid[HT_MAX_NODES] = {};
+  for (int t = 0; t < T.n_nodes; ++t)
+    if (T.leaf(t) && res.resid[t]) HT_CUDA(cudaMemcpyAsync(&resid[t], res.resid[t], sizeof(float), cudaMemcpyDeviceToHost, c.st));
+  HT_CUDA(cudaStreamSynchronize(c.st));
+  HT_CUDA(cudaGetLastError());
+  if (errword & kErrTimeout) return fail(HT_ERR_TIMEOUT, "a kernel's bounded wait expired; results are invalid");
+  if (!std::isfinite(host_sums[0])) return fail(HT_ERR_NUMERICAL, "input tensor contains NaN or Inf");
+  if (rep) {
+    std::memset(rep, 0, sizeof(*rep));
+    rep->norm_x = std::sqrt(host_sums[0]);
+    rep->rel_err = a.want_err ? (host_sums[0] > 0 ? std::sqrt(std::max(host_sums[1], 0.0) / host_sums[0]) : 0.0) : -1.0;
+    float ms = 0.f;
+    if (tl.on) {
+      cudaEventElapsedTime(&ms, h0, h1);
+      rep->ms_stage[6] = ms;
+      // marks: 0 start, 1 input ready, 2 grams, 3 eig, 4 core pass, 5 transfer
+      for (int i = 1; i < tl.n && i <= 5; ++i) {
+        cudaEventElapsedTime(&ms, tl.ev[i - 1], tl.ev[i]);
+        rep->ms_stage[i - 1] = ms;
+      }
+      if (tl.n >= 2) {
+        cudaEventElapsedTime(&ms, tl.ev[0], tl.ev[std::min(tl.n, 6) - 1]);
+        rep->ms_total = ms;
+      }
+    }
+    for (int t = 0; t < T.n_nodes; ++t) rep->eig_residual[t] = resid[t];
+    rep->gpu_launches = c.launches;
+    rep->path_flags = c.path;
+  }
+  g_launches += static_cast<unsigned long long>(c.launches);
+  if (rep && cfg.eig_tol > 0.0)
+    for (int t = 0; t < T.n_nodes; ++t)
+      if (T.leaf(t) && rep->eig_residual[t] > cfg.eig_tol)
+        return fail(HT_ERR_NOT_CONVERGED, "eigen-solver residual above eig_tol at leaf " + std::to_string(t));
+  return HT_OK;
+}
+
+size_t dry_run_bytes(const Tree &T, const ht_config_t &cfg, const CallArgs &a) {
+  Ctx d;
+  d.ar.dry = true;
+  d.tc = cfg.precision == HT_PREC_BF16;
+  run_call(d, T, cfg, a, nullptr);
+  return d.ar.peak + (1 << 20);
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+ht_status_t ht_config_default(ht_config_t *cfg) {
+  if (!cfg) return fail(HT_ERR_INVALID_ARG, "cfg is NULL");
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->precision = HT_PREC_BF16;
+  cfg->leaf_method = HT_LEAF_GRAM;
+  cfg->oversample = 16;
+  cfg->eig_iters = 10;
+  cfg->power_steps = 1;
+  cfg->seed = 1234ull;
+  return HT_OK;
+}
+
+static void fill_tree(ht_tree_t *t, int order, const int *mask, const int *left, const int *right, const int *k) {
+  std::memset(t, 0, sizeof(*t));
+  t->order = order;
+  t->n_nodes = 2 * order - 1;
+  for (int i = 0; i < HT_MAX_NODES; ++i) t->parent[i] = t->left[i] = t->right[i] = -1;
+  for (int i = 0; i < t->n_nodes; ++i) {
+    t->mode_mask[i] = mask[i];
+    t->left[i] = left[i];
+    t->right[i] = right[i];
+    t->rank[i] = (i == 0) ? 1 : (k ? k[i] : 1);
+  }
+  for (int i = 0; i < t->n_nodes; ++i)
+    if (left[i] >= 0) {
+      t->parent[left[i]] = i;
+      t->parent[right[i]] = i;
+    }
+}
+
+ht_status_t ht_tree_reference_3d(ht_tree_t *tree, const int *k) {
+  if (!tree) return fail(HT_ERR_INVALID_ARG, "tree is NULL");
+  const int mask[5] = {7, 3, 4, 1, 2};
+  const int left[5] = {1, 3, -1, -1, -1};
+  const int right[5] = {2, 4, -1, -1, -1};
+  fill_tree(tree, 3, mask, left, right, k);
+  return HT_OK;
+}
+
+ht_status_t ht_tree_balanced_4d(ht_tree_t *tree, const int *k) {
+  if (!tree) return fail(HT_ERR_INVALID_ARG, "tree is NULL");
+  const int mask[7] = {15, 3, 12, 1, 2, 4, 8};
+  const int left[7] = {1, 3, 5, -1, -1, -1, -1};
+  const int right[7] = {2, 4, 6, -1, -1, -1, -1};
+  fill_tree(tree, 4, mask, left, right, k);
+  return HT_OK;
+}
+
+ht_status_t ht_tree_validate(const ht_tree_t *tree, const long *dims, int order) {
+  if (!dims) return fail(HT_ERR_INVALID_ARG, "dims is NULL");
+  Tree T;
+  return parse_tree(tree, dims, order, T);
+}
+
+ht_status_t ht_workspace_size(const long *dims, int order, const ht_tree_t *tree, const ht_config_t *cfg,
+                              unsigned long long *bytes) {
+  if (!dims || !bytes) return fail(HT_ERR_INVALID_ARG, "NULL argument");
+  Tree T;
+  HT_TRY(parse_tree(tree, dims, order, T));
+  ht_config_t def;
+  ht_config_default(&def);
+  float *none[HT_MAX_NODES] = {};
+  CallArgs a{nullptr, true, dims, order, none, none, cfg ? (cfg->flags & HT_FLAG_COMPUTE_ERROR) != 0 : false};
+  *bytes = dry_run_bytes(T, cfg ? *cfg : def, a);
+  return HT_OK;
+}
+
+ht_status_t ht_release_workspace(void) {
+  std::lock_guard<std::mutex> lk(g_ws_mutex);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return HT_OK;
+  }
+  if (dev >= 0 && dev < 64 && g_ws[dev].ptr) {
+    HT_CUDA(cudaDeviceSynchronize());
+    HT_CUDA(cudaFree(g_ws[dev].ptr));
+    g_ws[dev].ptr = nullptr;
+    g_ws[dev].bytes = 0;
+  }
+  return HT_OK;
+}
+
+ht_status_t ht_decompose(const float *x, const long *dims, int order, const ht_tree_t *tree, const ht_config_t *cfg_in,
+                         float *const *U, float *const *B, ht_report_t *report, void *stream) {
+  if (!x || !dims || !U || !B) return fail(HT_ERR_INVALID_ARG, "NULL argument");
+  Tree T;
+  HT_TRY(parse_tree(tree, dims, order, T));
+  ht_config_t cfg;
+  if (cfg_in) cfg = *cfg_in;
+  else ht_config_default(&cfg);
+  if (cfg.precision != HT_PREC_FP32 && cfg.precision != HT_PREC_BF16) return fail(HT_ERR_INVALID_ARG, "unknown precision");
+  if (cfg.leaf_method != HT_LEAF_GRAM) return fail(HT_ERR_UNSUPPORTED, "only the Gram leaf method is implemented");
+  if (cfg.oversample < 0 || cfg.eig_iters < 0) return fail(HT_ERR_INVALID_ARG, "negative oversample / eig_iters");
+  for (int t = 0; t < T.n_nodes; ++t) {
+    if (T.leaf(t) && !U[t]) return fail(HT_ERR_INVALID_ARG, "U[t] is NULL for leaf " + std::to_string(t));
+    if (!T.leaf(t) && !B[t]) return fail(HT_ERR_INVALID_ARG, "B[t] is NULL for interior node " + std::to_string(t));
+  }
+  HT_TRY(check_device());
+  std::lock_guard<std::mutex> lk(g_ws_mutex);
+  CallArgs a{x, is_device_ptr(x), dims, order, U, B, (cfg.flags & HT_FLAG_COMPUTE_ERROR) != 0};
+  const size_t bytes = dry_run_bytes(T, cfg, a);
+  void *ws = nullptr;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  HT_TRY(acquire_workspace(bytes, &ws, st));
+  Ctx c;
+  c.st = st;
+  c.tc = cfg.precision == HT_PREC_BF16;
+  c.ar.base = static_cast<char *>(ws);
+  c.ar.cap = bytes;
+  return run_call(c, T, cfg, a, report);
+}
+
+ht_status_t ht_reconstruct_error(const float *x, const long *dims, int order, const ht_tree_t *tree,
+                                 const float *const *U, const float *const *B, double *rel_err, void *stream) {
+  if (!x || !dims || !U || !B || !rel_err) return fail(HT_ERR_INVALID_ARG, "NULL argument");
+  Tree T;
+  HT_TRY(parse_tree(tree, dims, order, T));
+  for (int t = 0; t < T.n_nodes; ++t)
+    if (!(T.leaf(t) ? U[t] : B[t])) return fail(HT_ERR_INVALID_ARG, "missing factor for node " + std::to_string(t));
+  HT_TRY(check_device());
+  std::lock_guard<std::mutex> lk(g_ws_mutex);
+  long long total = 1;
+  for (int m = 0; m < order; ++m) total *= dims[m];
+  const bool x_dev = is_device_ptr(x);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // size: staged tensor + staged factors + error scratch (dry run of error_core)
+  auto plan = [&](Ctx &c, const float **xd, const float **Ud, const float **Bd, double **sums) -> ht_status_t {
+    c.err = c.ar.take<int>(64);
+    double *np_ = c.ar.take<double>(1024);
+    *sums = c.ar.take<double>(8);
+    *xd = x;
+    if (!x_dev) {
+      float *t = c.ar.take<float>(static_cast<size_t>(total));
+      if (!t) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small");
+      if (!c.dry()) HT_CUDA(cudaMemcpyAsync(t, x, sizeof(float) * total, cudaMemcpyHostToDevice, c.st));
+      *xd = t;
+    }
+    for (int t = 0; t < T.n_nodes; ++t) {
+      const float *src = T.leaf(t) ? U[t] : B[t];
+      const size_t count = factor_count(T, dims, t);
+      const float *d = src;
+      if (!is_device_ptr(src)) {
+        float *tmp = c.ar.take<float>(count);
+        if (!tmp) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small");
+        if (!c.dry()) HT_CUDA(cudaMemcpyAsync(tmp, src, count * sizeof(float), cudaMemcpyHostToDevice, c.st));
+        d = tmp;
+      }
+      (T.leaf(t) ? Ud : Bd)[t] = d;
+    }
+    if (!c.dry()) {
+      HT_CUDA(sumsq_launch(*xd, total, np_, 1024, c.st));
+      HT_CUDA(sumsq_finish_launch(np_, 1024, *sums, c.st));
+      c.launches += 2;
+    }
+    return error_core(c, T, *xd, dims, order, Ud, Bd, *sums + 1);
+  };
+  const float *xd = nullptr, *Ud[HT_MAX_NODES] = {}, *Bd[HT_MAX_NODES] = {};
+  double *sums = nullptr;
+  Ctx d;
+  d.ar.dry = true;
+  plan(d, &xd, Ud, Bd, &sums);
+  const size_t bytes = d.ar.peak + (1 << 20);
+  void *ws = nullptr;
+  HT_TRY(acquire_workspace(bytes, &ws, st));
+  Ctx c;
+  c.st = st;
+  c.ar.base = static_cast<char *>(ws);
+  c.ar.cap = bytes;
+  HT_TRY(plan(c, &xd, Ud, Bd, &sums));
+  double h[2] = {0.0, 0.0};
+  HT_CUDA(cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, c.st));
+  HT_CUDA(cudaStreamSynchronize(c.st));
+  *rel_err = h[0] > 0 ? std::sqrt(std::max(h[1], 0.0) / h[0]) : 0.0;
+  g_launches += static_cast<unsigned long long>(c.launches);
+  return HT_OK;
+}
+
+// Shared driver of the three unfolding primitives.  op 0: Gram, 1: mode product, 2: co-range product.
+static ht_status_t unfolding_op(int op, const float *x, const long *dims, int order, int lo, int hi, const float *Mat,
+                                int k, int precision, float *out, void *stream) {
+  if (!x || !dims || !out || (op != 0 && !Mat)) return fail(HT_ERR_INVALID_ARG, "NULL argument");
+  if (order < 1 || order > HT_MAX_ORDER) return fail(HT_ERR_INVALID_ARG, "order must be 1..4");
+  if (lo < 0 || hi < lo || hi >= order) return fail(HT_ERR_INVALID_ARG, "bad mode group");
+  if (precision != HT_PREC_FP32 && precision != HT_PREC_BF16) return fail(HT_ERR_INVALID_ARG, "unknown precision");
+  for (int m = 0; m < order; ++m)
+    if (dims[m] < 1) return fail(HT_ERR_INVALID_ARG, "dims must be positive");
+  const View v = view_of_group(dims, order, lo, hi);
+  if (op != 0 && (k < 1 || k > 64)) return fail(HT_ERR_UNSUPPORTED, "k must lie in [1, 64]");
+  if (op == 0 && v.N > 32768) return fail(HT_ERR_UNSUPPORTED, "Gram size above 32768");
+  HT_TRY(check_device());
+  std::lock_guard<std::mutex> lk(g_ws_mutex);
+  const long long total = v.L * v.N * v.R;
+  const long long mat_rows = op == 1 ? v.N : v.L * v.R;
+  const long long out_count = op == 0 ? v.N * v.N : (op == 1 ? v.L * v.R * k : v.N * k);
+  const bool x_dev = is_device_ptr(x), m_dev = Mat && is_device_ptr(Mat), o_dev = is_device_ptr(out);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  auto body = [&](Ctx &c) -> ht_status_t {
+    c.err = c.ar.take<int>(64);
+    const float *xd = x, *md = Mat;
+    if (!x_dev) {
+      float *t = c.ar.take<float>(static_cast<size_t>(total));
+      if (!t) return fail(HT_ERR_OUT_OF_MEMORY, "workspace");
+      if (!c.dry()) HT_CUDA(cudaMemcpyAsync(t, x, sizeof(float) * total, cudaMemcpyHostToDevice, c.st));
+      xd = t;
+    }
+    if (Mat && !m_dev) {
+      float *t = c.ar.take<float>(static_cast<size_t>(mat_rows) * k);
+      if (!t) return fail(HT_ERR_OUT_OF_MEMORY, "workspace");
+      if (!c.dry()) HT_CUDA(cudaMemcpyAsync(t, Mat, sizeof(float) * mat_rows * k, cudaMemcpyHostToDevice, c.st));
+      md = t;
+    }
+    float *od = out;
+    if (!o_dev) {
+      od = c.ar.take<float>(static_cast<size_t>(out_count));
+      if (!od) return fail(HT_ERR_OUT_OF_MEMORY, "workspace");
+    }
+    __nv_bfloat16 *x16 = nullptr, *m16 = nullptr;
+    if (c.tc) {
+      x16 = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
+      double *parts = c.ar.take<double>(1024);
+      if (!x16 || !parts) return fail(HT_ERR_OUT_OF_MEMORY, "workspace");
+      if (!c.dry()) HT_CUDA(convert_bf16_launch(xd, x16, total, parts, 1024, c.st));
+      if (Mat) {
+        m16 = c.ar.take<__nv_bfloat16>(static_cast<size_t>(mat_rows) * k + 64);
+        if (!m16) return fail(HT_ERR_OUT_OF_MEMORY, "workspace");
+        if (!c.dry()) HT_CUDA(f32_to_bf16_launch(md, m16, mat_rows * k, c.st));
+      }
+    }
+    if (!c.dry()) HT_CUDA(cudaMemsetAsync(c.err, 0, sizeof(int), c.st));
+    if (op == 0) HT_TRY(gram(c, v, xd, x16, od));
+    else if (op == 1) HT_TRY(mode_product(c, v, xd, x16, md, m16, k, od));
+    else HT_TRY(corange_product(c, v, xd, x16, md, m16, k, od));
+    if (c.dry()) return HT_OK;
+    if (!o_dev) HT_CUDA(cudaMemcpyAsync(out, od, sizeof(float) * out_count, cudaMemcpyDeviceToHost, c.st));
+    int errword = 0;
+    HT_CUDA(cudaMemcpyAsync(&errword, c.err, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+    HT_CUDA(cudaStreamSynchronize(c.st));
+    HT_CUDA(cudaGetLastError());
+    if (errword & kErrTimeout) return fail(HT_ERR_TIMEOUT, "a kernel's bounded wait expired; results are invalid");
+    g_launches += static_cast<unsigned long long>(c.launches);
+    return HT_OK;
+  };
+  Ctx d;
+  d.ar.dry = true;
+  d.tc = precision == HT_PREC_BF16;
+  body(d);
+  const size_t bytes = d.ar.peak + (1 << 20);
+  void *ws = nullptr;
+  HT_TRY(acquire_workspace(bytes, &ws, st));
+  Ctx c;
+  c.st = st;
+  c.tc = precision == HT_PREC_BF16;
+  c.ar.base = static_cast<char *>(ws);
+  c.ar.cap = bytes;
+  return body(c);
+}
+
+ht_status_t ht_mode_gram(const float *x, const long *dims, int order, int lo, int hi, int precision, float *G,
+                         void *stream) {
+  return unfolding_op(0, x, dims, order, lo, hi, nullptr, 0, precision, G, stream);
+}
+
+ht_status_t ht_mode_product(const float *x, const long *dims, int order, int lo, int hi, const float *W, int k,
+                            int precision, float *Z, void *stream) {
+  return unfolding_op(1, x, dims, order, lo, hi, W, k, precision, Z, stream);
+}
+
+ht_status_t ht_corange_product(const float *x, const long *dims, int order, int lo, int hi, const float *Q, int k,
+                               int precision, float *Z, void *stream) {
+  return unfolding_op(2, x, dims, order, lo, hi, Q, k, precision, Z, stream);
+}
+
+const char *ht_status_string(ht_status_t s) {
+  switch (s) {
+    case HT_OK: return "ok";
+    case HT_ERR_INVALID_ARG: return "invalid argument";
+    case HT_ERR_CUDA: return "CUDA error";
+    case HT_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case HT_ERR_NOT_CONVERGED: return "eigen-solver did not converge";
+    case HT_ERR_TIMEOUT: return "kernel wait timed out";
+    case HT_ERR_UNSUPPORTED: return "unsupported";
+    case HT_ERR_NO_DEVICE: return "no suitable device";
+    case HT_ERR_NUMERICAL: return "numerical failure";
+  }
+  return "unknown status";
+}
+
+const char *ht_last_error(void) { return g_last_error.c_str(); }
+
+unsigned long long ht_kernel_launch_count(void) { return g_launches.load(); }
+
+float htd(float *x, long a, long b, long c, int *k) {
+  ht_tree_t tree;
+  if (!x || !k || ht_tree_reference_3d(&tree, k) != HT_OK) return -1.f;
+  const long dims[3] = {a, b, c};
+  ht_config_t cfg;
+  ht_config_default(&cfg);
+  cfg.flags |= HT_FLAG_COMPUTE_ERROR;
+  std::vector<float> u1(static_cast<size_t>(a) * std::max(k[3], 1)), u2(static_cast<size_t>(b) * std::max(k[4], 1)),
+      u3(static_cast<size_t>(c) * std::max(k[2], 1));
+  std::vector<float> b1(static_cast<size_t>(std::max(k[3] * k[4] * k[1], 1))), b0(static_cast<size_t>(std::max(k[1] * k[2], 1)));
+  float *U[5] = {nullptr, nullptr, u3.data(), u1.data(), u2.data()};
+  float *B[5] = {b0.data(), b1.data(), nullptr, nullptr, nullptr};
+  ht_report_t rep;
+  std::memset(&rep, 0, sizeof(rep));
+  if (ht_decompose(x, dims, 3, &tree, &cfg, U, B, &rep, nullptr) != HT_OK) return -1.f;
+  return static_cast<float>(rep.rel_err);
+}
+
+void htd4(float *x, long a, long b, long c, long d, int *k, void *cublas_handle, void *cusolver_handle) {
+  (void)cublas_handle;
+  (void)cusolver_handle;
+  ht_tree_t tree;
+  if (!x || !k || ht_tree_balanced_4d(&tree, k) != HT_OK) {
+    std::printf("htd4: invalid arguments\n");
+    return;
+  }
+  const long dims[4] = {a, b, c, d};
+  ht_config_t cfg;
+  ht_config_default(&cfg);
+  cfg.flags |= HT_FLAG_COMPUTE_ERROR;
+  std::vector<float> u[4] = {std::vector<float>(static_cast<size_t>(a) * std::max(k[3], 1)),
+                             std::vector<float>(static_cast<size_t>(b) * std::max(k[4], 1)),
+                             std::vector<float>(static_cast<size_t>(c) * std::max(k[5], 1)),
+                             std::vector<float>(static_cast<size_t>(d) * std::max(k[6], 1))};
+  std::vector<float> b1(static_cast<size_t>(std::max(k[3] * k[4] * k[1], 1))),
+      b2(static_cast<size_t>(std::max(k[5] * k[6] * k[2], 1))), b0(static_cast<size_t>(std::max(k[1] * k[2], 1)));
+  float *U[7] = {nullptr, nullptr, nullptr, u[0].data(), u[1].data(), u[2].data(), u[3].data()};
+  float *B[7] = {b0.data(), b1.data(), b2.data(), nullptr, nullptr, nullptr, nullptr};
+  ht_report_t rep;
+  std::memset(&rep, 0, sizeof(rep));
+  const ht_status_t s = ht_decompose(x, dims, 4, &tree, &cfg, U, B, &rep, nullptr);
+  if (s != HT_OK) {
+    std::printf("htd4: %s (%s)\n", ht_status_string(s), ht_last_error());
+    return;
+  }
+  std::printf("error rate %g\n", rep.rel_err);
+}
+
+}  // extern "C"

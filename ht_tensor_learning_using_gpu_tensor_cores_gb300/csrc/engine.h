@@ -1,0 +1,130 @@
+// Internal interfaces between the host orchestration (api.cu) and the kernel
+// translation units.  Not part of the public C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace htgb {
+
+// ----------------------------------------------------------------- views
+// A column-major tensor seen as (L, N, R): element (l, n, r) at l + L*n + L*N*r.
+// The matricisation over a contiguous group of modes has N = product of the
+// group's dims, L = product of the dims before it, R = product after it.
+struct View {
+  long L, N, R;
+};
+
+// ------------------------------------------------------ GEMM over unfoldings
+// D[m, j] = sum_k A(m, k) * B(j, k).  Each operand is a 3-D strided tensor
+// (d0 innermost) read in one of three patterns:
+enum OpKind : int {
+  OP_KM3 = 0,   // K-major: row index on d1, k = (l on d0, r on d2), element l + d0*row + d0*d1*r
+  OP_KM3Q = 1,  // K-major: row index on d2, k = (l on d0, r on d1), element l + d0*r + d0*d1*row
+  OP_MN3 = 2    // MN-major: row index on d0, k on d1, fixed z on d2, element row + d0*k + d0*d1*z
+};
+
+struct Operand {
+  int kind;
+  const void *ptr;      // __nv_bfloat16* for the tcgen05 path, float* for the SIMT path
+  long d0, d1, d2;
+};
+
+// One output tile.  a_row / b_row: first row of the A / B operand;
+// a_z: d2 coordinate of an OP_MN3 A operand.  out_row/out_col: where the tile
+// lands in a column-major output (OUT_COLMAJOR); valid_rows/cols clip it.
+struct Tile {
+  int a_row, a_z, b_row, valid_rows;
+  long long out_row;
+  int out_col, valid_cols;
+};
+
+enum OutMode : int { OUT_PARTIAL = 0, OUT_COLMAJOR = 1 };
+
+struct GemmArgs {
+  Operand a, b;
+  const Tile *tiles;     // device array, num_tiles entries
+  int num_tiles;
+  int splits;            // split-K factor (work items = num_tiles * splits)
+  int out_mode;
+  float *out;            // partial buffer [splits][num_tiles][BM][BN] or column-major output
+  long long ld_out;
+  int *err;              // device error word
+};
+
+// tcgen05 path (BF16 operands), BM = 128, BN in {64, 128, 256}.
+// Returns false (and fills *why) when the operand shapes cannot be expressed as
+// TMA tensor maps (strides not multiples of 16 bytes, dims too large).
+bool tc_gemm_supported(const GemmArgs &g, int bn, std::string *why);
+cudaError_t tc_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s);
+// number of 64-wide K blocks of an operand pair (tcgen05 path)
+long tc_num_kblocks(const Operand &a);
+
+// SIMT FP32 path (float operands), BM = 128, BN in {64, 128}.
+cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s);
+long simt_k_total(const Operand &a);
+
+// Sum split-K partial tiles.  mode 0: symmetric Gram (tiles on/above the
+// diagonal, mirror into the lower triangle); mode 1: plain column-major.
+cudaError_t reduce_partials_launch(const float *partial, const Tile *tiles, int num_tiles, int splits, int bn,
+                                   float *out, long long ld_out, int symmetric, cudaStream_t s);
+
+// --------------------------------------------------------------- small ops
+cudaError_t convert_bf16_launch(const float *x, __nv_bfloat16 *xb, long long n, double *sumsq_partials,
+                                int num_partials, cudaStream_t s);
+cudaError_t sumsq_launch(const float *x, long long n, double *partials, int num_partials, cudaStream_t s);
+cudaError_t f32_to_bf16_launch(const float *x, __nv_bfloat16 *y, long long n, cudaStream_t s);
+cudaError_t sumsq_finish_launch(const double *partials, int n, double *out, cudaStream_t s);
+// C (m x n) = A^T B with A (K x m), B (K x n), column-major, compensated FP32.
+cudaError_t gemm_tn_small_launch(const float *A, int lda, const float *B, int ldb, float *C, int ldc, int m, int n,
+                                 int K, cudaStream_t s);
+// C[a + kp*b + kp*kq*c] = sum_j T1[(j + nq*c) + ldt*a] * Uq[j + nq*b]
+cudaError_t core_step2_launch(const float *T1, long long ldt, int nq, int kp, const float *Uq, int kq, int kc, float *C,
+                              cudaStream_t s);
+// W[i0 + n0*i1 + n0*n1*c] = sum_{a,b} U0[i0,a] U1[i1,b] core[a + k0*b + k0*k1*c]  (T: n0*k1*k2 scratch)
+cudaError_t expand2_launch(const float *U0, int n0, int k0, const float *core, const float *U1, int n1, int k1, int k2,
+                           float *T, float *W, cudaStream_t s);
+// C (m x n) = A (m x K) B (K x n), column-major
+cudaError_t matmul_nn_launch(const float *A, long long lda, const float *B, int ldb, float *C, long long ldc,
+                             long long m, int n, int K, cudaStream_t s);
+// per-block partial sums of (X[r + ldx*c] - sum_k A[r + lda*k] B[c + ldb*k])^2 over an R x Cn
+// matrix, repeated for `batch` slices offset by the given strides
+int error_fused_blocks(long long R, long long Cn);
+cudaError_t error_fused_launch(const float *X, long long ldx, long long sx, const float *A, long long lda, long long sa,
+                               const float *B, long long ldb, long long R, long long Cn, int kk, int batch,
+                               double *partials, cudaStream_t s);
+cudaError_t transpose_small_launch(const float *A, int m, int n, float *AT, cudaStream_t s);
+cudaError_t gaussian_fill_launch(float *dst, long long n, uint64_t seed, uint64_t stream, cudaStream_t s);
+
+// ------------------------------------------------------- eigen-solver (batched)
+// Top-K eigenpairs of symmetric PSD FP32 matrices by subspace iteration with
+// CholeskyQR and a final Rayleigh-Ritz step.  All arrays column-major.
+struct EigProblem {
+  const float *G;    // n x n
+  int n, s, K;       // subspace size s (<= 64, <= n), wanted K <= s
+  float *Q, *Y;      // n x s work
+  float *U;          // n x K out: Ritz vectors, descending Ritz values
+  float *GU;         // n x K out: G * U
+  float *theta;      // K out: Ritz values
+  float *resid;      // 1 out: max_j ||G u_j - theta_j u_j|| / theta_1
+  const float *start; // optional n x s start block (NULL = Gaussian)
+  uint64_t seed, stream_id;
+};
+size_t eig_workspace_bytes(const EigProblem *probs, int nprob);
+cudaError_t eig_batched(EigProblem *probs, int nprob, int iters, void *ws, size_t ws_bytes, int *err,
+                        cudaStream_t s, int *launches);
+// Orthonormalise the columns of tall matrices in place (CholeskyQR, `passes`
+// times; the first pass shifted).  Uses the eigen-solver's workspace layout.
+cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, size_t ws_bytes, cudaStream_t s,
+                           int *launches);
+// Transfer-tensor eigen step (see eig.cu).  WG: kw x kw.  M: kt x kt, Bkt: kt x kc.
+cudaError_t transfer_eig_launch(const float *WG, int kw, int kt, int kc, int t_is_left, float *M, float *Broot,
+                                cudaStream_t st);
+// Small SVD from a Gram: GW (s x s) = W^T W.  M1 (s x k1) = top-k1 eigenvectors,
+// M2 (s x k2) = top-k2 eigenvectors scaled by sigma^-1, Broot (k1 x k2) = M1^T GW M2.
+cudaError_t svd_from_gram_launch(const float *GW, int s, int k1, int k2, float *M1, float *M2, float *Broot,
+                                 cudaStream_t st);
+
+}  // namespace htgb

@@ -1,0 +1,251 @@
+// FP32 GEMM over tensor matricisations on CUDA cores (the plain FP32 path),
+// plus the deterministic split-K reduction shared with the tcgen05 path.
+//
+// This is the GB300 restatement of the reference's FP32 cuBLAS calls
+// (third_order_tensor_decompsition/CUDA/Optimized/htd_batch.cu:83-106 leaf
+// Grams with cublasSgemm, ttm.cu:2-36 TTM chains).  Same operand/tile model as
+// tc_gemm.cu: operands are read in place from the column-major tensor.
+//
+// Tile 128 x BN (BN = 128 or 64), K step 16, 256 threads, 8 x (BN/16)
+// register tile per thread, double-buffered shared memory.
+#include "common.cuh"
+#include "engine.h"
+
+namespace htgb {
+namespace {
+
+constexpr int BM = 128;
+constexpr int BKS = 16;
+
+struct SParams {
+  int a_kind, b_kind;
+  const float *a, *b;
+  long long a0, a1, a2, b0, b1, b2;
+  long long k_total;
+  long long k_per_split;
+  int num_tiles, out_mode;
+  const Tile *tiles;
+  float *out;
+  long long ld_out;
+  int a_rows, b_rows;   // operand row extents (for bounds)
+};
+
+HT_DEV const float *op_ptr(int kind, const float *p, long long d0, long long d1, long long row, long long k,
+                           int z) {
+  if (kind == OP_KM3) {
+    const long long r = k / d0, l = k - r * d0;
+    return p + l + d0 * (row + d1 * r);
+  }
+  if (kind == OP_KM3Q) return p + k + d0 * d1 * row;
+  return p + row + d0 * (k + d1 * static_cast<long long>(z));
+}
+
+template <int BN>
+__global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p) {
+  constexpr int TN = BN / 16;   // columns per thread (8 or 4)
+  constexpr int A_PER = BM * BKS / 256;   // 8
+  constexpr int B_PER = BN * BKS / 256;   // 8 or 4
+  __shared__ __align__(16) float As[2][BKS][BM + 4];
+  __shared__ __align__(16) float Bs[2][BKS][BN + 4];
+
+  const int tid = threadIdx.x;
+  const int tile_idx = blockIdx.x % p.num_tiles;
+  const int split = blockIdx.x / p.num_tiles;
+  const Tile tile = p.tiles[tile_idx];
+  const long long kbeg = static_cast<long long>(split) * p.k_per_split;
+  const long long kend = min(p.k_total, kbeg + p.k_per_split);
+
+  // load-slot geometry: K-contiguous operands load k-fast, MN3 loads row-fast
+  const bool a_kfast = p.a_kind != OP_MN3;
+  const bool b_kfast = p.b_kind != OP_MN3;
+
+  float ra[A_PER], rb[B_PER];
+  // KM3 operands whose contiguous extent d0 is a multiple of BKS never split a
+  // 16-wide K step across two outer indices: decompose k once per step.
+  const bool a_fast = p.a_kind == OP_KM3 && (p.a0 % BKS) == 0;
+  const bool b_fast = p.b_kind == OP_KM3 && (p.b0 % BKS) == 0;
+  auto load_tiles = [&](long long k0) {
+    const float *abase = nullptr, *bbase = nullptr;
+    if (a_fast) {
+      const long long r0 = k0 / p.a0, l0 = k0 - r0 * p.a0;
+      abase = p.a + l0 + p.a0 * p.a1 * r0;
+    }
+    if (b_fast) {
+      const long long r0 = k0 / p.b0, l0 = k0 - r0 * p.b0;
+      bbase = p.b + l0 + p.b0 * p.b1 * r0;
+    }
+#pragma unroll
+    for (int i = 0; i < A_PER; ++i) {
+      const int e = tid + 256 * i;
+      const int kk = a_kfast ? (e % BKS) : (e / BM);
+      const int rr = a_kfast ? (e / BKS) : (e % BM);
+      const long long k = k0 + kk;
+      const long long row = tile.a_row + rr;
+      float v = 0.f;
+      if (k < kend && row < p.a_rows)
+        v = __ldg(a_fast ? abase + kk + p.a0 * row : op_ptr(p.a_kind, p.a, p.a0, p.a1, row, k, tile.a_z));
+      ra[i] = v;
+    }
+#pragma unroll
+    for (int i = 0; i < B_PER; ++i) {
+      const int e = tid + 256 * i;
+      const int kk = b_kfast ? (e % BKS) : (e / BN);
+      const int rr = b_kfast ? (e / BKS) : (e % BN);
+      const long long k = k0 + kk;
+      const long long row = tile.b_row + rr;
+      float v = 0.f;
+      if (k < kend && row < p.b_rows)
+        v = __ldg(b_fast ? bbase + kk + p.b0 * row : op_ptr(p.b_kind, p.b, p.b0, p.b1, row, k, 0));
+      rb[i] = v;
+    }
+  };
+  auto store_tiles = [&](int buf) {
+#pragma unroll
+    for (int i = 0; i < A_PER; ++i) {
+      const int e = tid + 256 * i;
+      const int kk = a_kfast ? (e % BKS) : (e / BM);
+      const int rr = a_kfast ? (e / BKS) : (e % BM);
+      As[buf][kk][rr] = ra[i];
+    }
+#pragma unroll
+    for (int i = 0; i < B_PER; ++i) {
+      const int e = tid + 256 * i;
+      const int kk = b_kfast ? (e % BKS) : (e / BN);
+      const int rr = b_kfast ? (e / BKS) : (e % BN);
+      Bs[buf][kk][rr] = rb[i];
+    }
+  };
+
+  const int tx = tid % 16, ty = tid / 16;
+  float acc[8][TN];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = 0.f;
+
+  int buf = 0;
+  if (kbeg < kend) {
+    load_tiles(kbeg);
+    store_tiles(0);
+  }
+  __syncthreads();
+  for (long long k0 = kbeg; k0 < kend; k0 += BKS) {
+    const bool more = k0 + BKS < kend;
+    if (more) load_tiles(k0 + BKS);
+#pragma unroll
+    for (int kk = 0; kk < BKS; ++kk) {
+      float a[8], b[TN];
+      const float4 a0 = *reinterpret_cast<const float4 *>(&As[buf][kk][ty * 4]);
+      const float4 a1 = *reinterpret_cast<const float4 *>(&As[buf][kk][64 + ty * 4]);
+      a[0] = a0.x; a[1] = a0.y; a[2] = a0.z; a[3] = a0.w;
+      a[4] = a1.x; a[5] = a1.y; a[6] = a1.z; a[7] = a1.w;
+      const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][tx * 4]);
+      b[0] = b0.x; b[1] = b0.y; b[2] = b0.z; b[3] = b0.w;
+      if constexpr (TN == 8) {
+        const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][64 + tx * 4]);
+        b[4] = b1.x; b[5] = b1.y; b[6] = b1.z; b[7] = b1.w;
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    if (more) store_tiles(buf ^ 1);
+    __syncthreads();
+    buf ^= 1;
+  }
+
+  // write out
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int row = (i < 4) ? (ty * 4 + i) : (64 + ty * 4 + i - 4);
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int col = (j < 4) ? (tx * 4 + j) : (64 + tx * 4 + j - 4);
+      if (p.out_mode == OUT_PARTIAL) {
+        p.out[((static_cast<size_t>(split) * p.num_tiles + tile_idx) * BM + row) * BN + col] = acc[i][j];
+      } else if (row < tile.valid_rows && col < tile.valid_cols) {
+        p.out[tile.out_row + row + p.ld_out * static_cast<long long>(tile.out_col + col)] = acc[i][j];
+      }
+    }
+  }
+}
+
+// Sum partial tiles [splits][num_tiles][128][bn] in a fixed order.
+__global__ void reduce_partials_kernel(const float *__restrict__ part, const Tile *__restrict__ tiles, int num_tiles,
+                                       int splits, int bn, float *__restrict__ out, long long ld, int symmetric) {
+  const long long per_tile = 128ll * bn;
+  const long long total = per_tile * num_tiles;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int t = static_cast<int>(idx / per_tile);
+    const int within = static_cast<int>(idx - t * per_tile);
+    const int row = within / bn, col = within % bn;
+    const Tile tl = tiles[t];
+    if (row >= tl.valid_rows || col >= tl.valid_cols) continue;
+    float s = 0.f;
+    for (int k = 0; k < splits; ++k) s += part[(static_cast<long long>(k) * num_tiles + t) * per_tile + within];
+    const long long gr = tl.out_row + row, gc = tl.out_col + col;
+    if (symmetric) {
+      if (gc < gr) continue;   // the mirror element is produced by the tile holding (gc, gr)
+      out[gr + ld * gc] = s;
+      out[gc + ld * gr] = s;
+    } else {
+      out[gr + ld * gc] = s;
+    }
+  }
+}
+
+int rows_of(int kind, long long d0, long long d1, long long d2) {
+  return static_cast<int>(kind == OP_KM3 ? d1 : (kind == OP_KM3Q ? d2 : d0));
+}
+
+}  // namespace
+
+long simt_k_total(const Operand &a) {
+  if (a.kind == OP_KM3) return a.d0 * a.d2;
+  if (a.kind == OP_KM3Q) return a.d0 * a.d1;
+  return a.d1;
+}
+
+cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s) {
+  SParams p;
+  p.a_kind = g.a.kind;
+  p.b_kind = g.b.kind;
+  p.a = static_cast<const float *>(g.a.ptr);
+  p.b = static_cast<const float *>(g.b.ptr);
+  p.a0 = g.a.d0; p.a1 = g.a.d1; p.a2 = g.a.d2;
+  p.b0 = g.b.d0; p.b1 = g.b.d1; p.b2 = g.b.d2;
+  p.k_total = simt_k_total(g.a);
+  if (simt_k_total(g.b) != p.k_total) return cudaErrorInvalidValue;
+  const int splits = g.splits < 1 ? 1 : g.splits;
+  long long kps = (p.k_total + splits - 1) / splits;
+  kps = (kps + BKS - 1) / BKS * BKS;
+  p.k_per_split = kps;
+  p.num_tiles = g.num_tiles;
+  p.out_mode = g.out_mode;
+  p.tiles = g.tiles;
+  p.out = g.out;
+  p.ld_out = g.ld_out;
+  p.a_rows = rows_of(g.a.kind, g.a.d0, g.a.d1, g.a.d2);
+  p.b_rows = rows_of(g.b.kind, g.b.d0, g.b.d1, g.b.d2);
+  const int grid = g.num_tiles * splits;
+  if (bn == 128)
+    simt_gemm_kernel<128><<<grid, 256, 0, s>>>(p);
+  else if (bn == 64)
+    simt_gemm_kernel<64><<<grid, 256, 0, s>>>(p);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t reduce_partials_launch(const float *partial, const Tile *tiles, int num_tiles, int splits, int bn,
+                                   float *out, long long ld_out, int symmetric, cudaStream_t s) {
+  const long long total = 128ll * bn * num_tiles;
+  int grid = static_cast<int>((total + 255) / 256);
+  if (grid > 152 * 16) grid = 152 * 16;
+  reduce_partials_kernel<<<grid, 256, 0, s>>>(partial, tiles, num_tiles, splits, bn, out, ld_out, symmetric);
+  return cudaGetLastError();
+}
+
+}  // namespace htgb

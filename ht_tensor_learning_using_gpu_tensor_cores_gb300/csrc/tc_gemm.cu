@@ -1,0 +1,331 @@
+// tcgen05 + TMA GEMM over tensor matricisations (BF16 in, FP32 accumulation in TMEM).
+//
+// One kernel serves the three unfolding products of the HT path, replacing the
+// reference's cuBLAS calls (third_order_tensor_decompsition/CUDA/Optimized/
+// htd_tensorcore.cu:83-121 leaf Grams, ttm.cu:38-87 TTMs, kernel.cu:610/618
+// rsvd products):
+//   Gram        G = X_(t) X_(t)^T           (A = B = the matricisation)
+//   mode product Z = X_(t)^T-side * W       (contract one mode with a small matrix)
+//   co-range    Z = X_(t) * Q               (contract all other modes)
+// Operands are read straight from the column-major tensor through 3-D TMA
+// tensor maps -- no permutation pass (the reference's mode2/mode2h kernels,
+// kernel.cu:46-72) -- either K-major or MN-major, both with 128-byte swizzle.
+//
+// CTA layout (192 threads, one CTA per SM):
+//   warp 0      TMA producer (one elected thread), STAGES-deep smem ring
+//   warp 1      TMEM allocator + MMA issuer (one thread issues tcgen05.mma)
+//   warps 2..5  epilogue: tcgen05.ld TMEM -> registers -> global
+// Tile: M = 128 (TMEM lanes), N = BN (TMEM columns), K block = 64 (one 128 B row).
+// Split-K across CTAs writes deterministic partial tiles that a separate
+// kernel sums in a fixed order.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "common.cuh"
+#include "engine.h"
+
+namespace htgb {
+namespace {
+
+constexpr int BM = 128;
+constexpr int BK = 64;
+constexpr int kThreads = 192;
+
+template <int BN>
+struct TcCfg {
+  static constexpr int STAGES = BN == 256 ? 4 : (BN == 128 ? 6 : 8);
+  static constexpr uint32_t A_BYTES = BM * BK * 2;
+  static constexpr uint32_t B_BYTES = BN * BK * 2;
+  static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr size_t SMEM = 1024 + size_t(STAGES) * STAGE_BYTES + 256;
+};
+
+struct KParams {
+  int a_kind, b_kind;
+  int a_lblocks, b_lblocks;
+  int num_kb, kb_per_split;
+  int num_tiles, out_mode;
+  const Tile *tiles;
+  float *out;
+  long long ld_out;
+  int *err;
+};
+
+// Issue the TMA loads of one operand tile (ROWS x 64 K) for k-block kb.
+template <int ROWS>
+HT_DEV void load_operand(const CUtensorMap *map, int kind, int lblocks, int kb, int row, int z, uint8_t *dst,
+                         uint64_t *bar) {
+  if (kind == OP_MN3) {
+    // ROWS/64 chunks of 64 MN-contiguous elements x 64 K rows (8 KiB each)
+#pragma unroll
+    for (int c = 0; c < ROWS / 64; ++c) tma_load_3d(dst + c * 8192, map, bar, row + 64 * c, kb * BK, z);
+  } else {
+    const int lb = kb % lblocks, r = kb / lblocks;
+    if (kind == OP_KM3)
+      tma_load_3d(dst, map, bar, lb * BK, row, r);
+    else
+      tma_load_3d(dst, map, bar, lb * BK, r, row);
+  }
+}
+
+// Descriptor of the kk-th 16-wide K slice of an operand tile at smem address base.
+HT_DEV uint64_t op_desc(int kind, uint32_t base, int kk) {
+  if (kind == OP_MN3) return make_sdesc_sw128(base + kk * 2048, 8192, 1024);
+  return make_sdesc_sw128(base + kk * 32, 16, 1024);
+}
+
+template <int BN>
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   const KParams p) {
+  using C = TcCfg<BN>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + C::STAGES * C::STAGE_BYTES);
+  uint64_t *empty = full + C::STAGES;
+  uint64_t *done = empty + C::STAGES;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile_idx = blockIdx.x % p.num_tiles;
+  const int split = blockIdx.x / p.num_tiles;
+  const Tile tile = p.tiles[tile_idx];
+  const int kb0 = split * p.kb_per_split;
+  const int nk = max(0, min(p.num_kb, kb0 + p.kb_per_split) - kb0);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < C::STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    mbar_fence_init();
+    tma_prefetch_desc(&tmA);
+    tma_prefetch_desc(&tmB);
+  }
+  if (warp == 1) {
+    tmem_alloc(tmem_slot, BN);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int issued = 0;
+      for (int i = 0; i < nk; ++i) {
+        const int s = i % C::STAGES;
+        const uint32_t ph = (i / C::STAGES) & 1;
+        if (!mbar_wait_bounded(&empty[s], ph ^ 1, abort_flag)) {
+          *abort_flag = 1;
+          report_error(p.err, kErrTimeout);
+          break;
+        }
+        uint8_t *sa = smem + s * C::STAGE_BYTES;
+        uint8_t *sb = sa + C::A_BYTES;
+        mbar_arrive_expect_tx(&full[s], C::STAGE_BYTES);
+        load_operand<BM>(&tmA, p.a_kind, p.a_lblocks, kb0 + i, tile.a_row, tile.a_z, sa, &full[s]);
+        load_operand<BN>(&tmB, p.b_kind, p.b_lblocks, kb0 + i, tile.b_row, 0, sb, &full[s]);
+        issued = i + 1;
+      }
+      if (*abort_flag) {
+        // let copies still in flight land before the CTA's smem is released
+        for (int i = max(0, issued - C::STAGES); i < issued; ++i) {
+          int dummy = 0;
+          mbar_wait_bounded(&full[i % C::STAGES], (i / C::STAGES) & 1, &dummy);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = make_idesc_bf16(BN, p.a_kind == OP_MN3, p.b_kind == OP_MN3);
+      for (int i = 0; i < nk; ++i) {
+        const int s = i % C::STAGES;
+        const uint32_t ph = (i / C::STAGES) & 1;
+        if (!mbar_wait_bounded(&full[s], ph, abort_flag)) {
+          *abort_flag = 1;
+          report_error(p.err, kErrTimeout);
+          break;
+        }
+        tc_fence_after();
+        const uint32_t sa = smem_u32(smem + s * C::STAGE_BYTES);
+        const uint32_t sb = sa + C::A_BYTES;
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; ++kk)
+          umma_f16(tmem, op_desc(p.a_kind, sa, kk), op_desc(p.b_kind, sb, kk), idesc, (i | kk) != 0 ? 1u : 0u);
+        umma_commit(&empty[s]);   // frees the stage once these MMAs have read it
+      }
+      umma_commit(done);           // accumulator complete (or abandoned)
+    }
+    __syncwarp();
+  } else {
+    const int q = warp & 3;        // TMEM lane quarter this warp may access
+    const int row = q * 32 + lane;
+    bool ok = true;
+    if (nk > 0) ok = mbar_wait_bounded(done, 0, abort_flag);
+    ok = __all_sync(0xffffffffu, ok);
+    if (!ok) report_error(p.err, kErrTimeout);
+    tc_fence_after();
+    const bool have = (nk > 0) && ok;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      float v[32];
+      if (have) {
+        tmem_ld_32x32b_x32(tmem + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(c0), v);
+        tmem_ld_wait();
+      } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] = 0.f;
+      }
+      if (p.out_mode == OUT_PARTIAL) {
+        float *dst = p.out + ((static_cast<size_t>(split) * p.num_tiles + tile_idx) * BM + row) * BN + c0;
+#pragma unroll
+        for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4 *>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+      } else if (row < tile.valid_rows) {
+        float *dst = p.out + tile.out_row + row + p.ld_out * static_cast<long long>(tile.out_col + c0);
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (c0 + j < tile.valid_cols) dst[p.ld_out * j] = v[j];
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, BN);
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  });
+  return fn;
+}
+
+bool check_operand(const Operand &o, std::string *why) {
+  const long long d[3] = {o.d0, o.d1, o.d2};
+  for (int i = 0; i < 3; ++i)
+    if (d[i] < 1 || d[i] > (1ll << 31) - 1) {
+      if (why) *why = "tensor-map dimension out of range";
+      return false;
+    }
+  if ((o.d0 * 2) % 16 != 0) {
+    if (why) *why = "innermost extent must be a multiple of 8 bf16 elements for TMA";
+    return false;
+  }
+  if ((reinterpret_cast<uintptr_t>(o.ptr) & 15u) != 0) {
+    if (why) *why = "operand base not 16-byte aligned";
+    return false;
+  }
+  return true;
+}
+
+bool make_map(const Operand &o, int rows_box, CUtensorMap *map, std::string *why) {
+  auto enc = encode_fn();
+  if (!enc) {
+    if (why) *why = "cuTensorMapEncodeTiled unavailable";
+    return false;
+  }
+  cuuint64_t dims[3] = {cuuint64_t(o.d0), cuuint64_t(o.d1), cuuint64_t(o.d2)};
+  cuuint64_t strides[2] = {cuuint64_t(o.d0) * 2, cuuint64_t(o.d0) * cuuint64_t(o.d1) * 2};
+  cuuint32_t box[3];
+  if (o.kind == OP_KM3) {
+    box[0] = BK; box[1] = rows_box; box[2] = 1;
+  } else if (o.kind == OP_KM3Q) {
+    box[0] = BK; box[1] = 1; box[2] = rows_box;
+  } else {
+    box[0] = 64; box[1] = BK; box[2] = 1;
+  }
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(o.ptr), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    if (why) *why = "cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")";
+    return false;
+  }
+  return true;
+}
+
+long kblocks_of(const Operand &o) {
+  if (o.kind == OP_MN3) return (o.d1 + BK - 1) / BK;
+  const long lb = (o.d0 + BK - 1) / BK;
+  return lb * (o.kind == OP_KM3 ? o.d2 : o.d1);
+}
+
+template <int BN>
+cudaError_t launch_bn(const GemmArgs &g, cudaStream_t s) {
+  using C = TcCfg<BN>;
+  CUtensorMap ma, mb;
+  std::string why;
+  if (!make_map(g.a, BM, &ma, &why) || !make_map(g.b, BN, &mb, &why)) return cudaErrorInvalidValue;
+  KParams p;
+  p.a_kind = g.a.kind;
+  p.b_kind = g.b.kind;
+  p.a_lblocks = int((g.a.d0 + BK - 1) / BK);
+  p.b_lblocks = int((g.b.d0 + BK - 1) / BK);
+  p.num_kb = int(kblocks_of(g.a));
+  const int splits = g.splits < 1 ? 1 : g.splits;
+  p.kb_per_split = (p.num_kb + splits - 1) / splits;
+  p.num_tiles = g.num_tiles;
+  p.out_mode = g.out_mode;
+  p.tiles = g.tiles;
+  p.out = g.out;
+  p.ld_out = g.ld_out;
+  p.err = g.err;
+  cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(C::SMEM));
+  if (e != cudaSuccess) return e;
+  tc_gemm_kernel<BN><<<g.num_tiles * splits, kThreads, C::SMEM, s>>>(ma, mb, p);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+long tc_num_kblocks(const Operand &a) { return kblocks_of(a); }
+
+bool tc_gemm_supported(const GemmArgs &g, int bn, std::string *why) {
+  if (bn != 64 && bn != 128 && bn != 256) {
+    if (why) *why = "BN must be 64, 128 or 256";
+    return false;
+  }
+  if (!check_operand(g.a, why) || !check_operand(g.b, why)) return false;
+  if (g.b.kind == OP_MN3 && bn % 64 != 0) return false;
+  if (kblocks_of(g.a) != kblocks_of(g.b)) {
+    if (why) *why = "operand K extents differ";
+    return false;
+  }
+  if (kblocks_of(g.a) > (1l << 30)) {
+    if (why) *why = "K too large";
+    return false;
+  }
+  if (!encode_fn()) {
+    if (why) *why = "cuTensorMapEncodeTiled unavailable";
+    return false;
+  }
+  return true;
+}
+
+cudaError_t tc_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s) {
+  switch (bn) {
+    case 64: return launch_bn<64>(g, s);
+    case 128: return launch_bn<128>(g, s);
+    case 256: return launch_bn<256>(g, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace htgb

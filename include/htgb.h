@@ -1,0 +1,177 @@
+/*
+ * htgb -- hierarchical Tucker (HT) decomposition on one GB300 (sm_103a).
+ *
+ * C ABI.  Plain pointers and sizes only; no exceptions cross this boundary and
+ * every entry point except the two reference-compatible shims returns an
+ * ht_status_t.  The last error message of the calling thread is available from
+ * ht_last_error().
+ *
+ * Tensors are column-major (first index fastest), as in the reference's CUDA
+ * code (third_order_tensor_decompsition/CUDA/Optimized/htd_tensorcore.cu:12):
+ * element (i1, i2, i3) of an n1 x n2 x n3 tensor is x[i1 + n1*i2 + n1*n2*i3].
+ *
+ * Dimension tree and ranks: node 0 is the root.  Leaves hold one mode.  The
+ * reference's node numbering and rank vector k[] (k[0] = 1) are kept:
+ *   3rd order (ht_init.cu:16-20, HT_TensorLy.py:23-24): 0 root, 1 = {1,2},
+ *             2 = {3}, 3 = {1}, 4 = {2};
+ *   4th order (4D/.../Optimized/ht_init.cu:19-23): 0 root, 1 = {1,2},
+ *             2 = {3,4}, 3..6 = {1}..{4}.
+ *
+ * Outputs follow the reference's transfer-tensor layout (CUDA/Optimized/ttm.cu:2-36):
+ *   U[t] for every leaf t: n_t x k_t, column-major, orthonormal columns in
+ *        descending order of the mode Gram's eigenvalues;
+ *   B[t] for every interior node t (root included): k_left x k_right x k_t,
+ *        column-major, so that U_t = (U_right kron U_left) B_t and the tensor
+ *        is X ~= reshape(U_left_root B_0 U_right_root^T).
+ */
+#ifndef HTGB_H
+#define HTGB_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HT_MAX_ORDER 4
+#define HT_MAX_NODES 7
+
+typedef enum {
+    HT_OK = 0,
+    HT_ERR_INVALID_ARG = 1,    /* bad dims, tree, ranks or pointers            */
+    HT_ERR_CUDA = 2,           /* a CUDA runtime call failed                   */
+    HT_ERR_OUT_OF_MEMORY = 3,  /* device workspace could not be allocated      */
+    HT_ERR_NOT_CONVERGED = 4,  /* eigen-solver residual above tolerance        */
+    HT_ERR_TIMEOUT = 5,        /* a kernel's bounded wait expired (no hang)    */
+    HT_ERR_UNSUPPORTED = 6,    /* shape/tree combination not implemented       */
+    HT_ERR_NO_DEVICE = 7,      /* no CUDA device / not an sm_103 device        */
+    HT_ERR_NUMERICAL = 8       /* NaN/Inf in the input or a breakdown          */
+} ht_status_t;
+
+typedef enum {
+    HT_PREC_FP32 = 0,  /* plain path: every product in FP32 on CUDA cores          */
+    HT_PREC_BF16 = 1   /* mixed path: BF16 tcgen05 GEMMs, FP32 accumulation in TMEM */
+} ht_precision_t;
+
+typedef enum {
+    HT_LEAF_GRAM = 0,   /* leaf bases from the mode Gram X_(t) X_(t)^T               */
+    HT_LEAF_SKETCH = 1  /* leaf bases from a randomized range finder on X_(t)        */
+} ht_leaf_method_t;
+
+/* Flags */
+#define HT_FLAG_COMPUTE_ERROR  1   /* fill ht_report_t.rel_err (one extra pass)   */
+#define HT_FLAG_SYNC_TIMING    2   /* per-stage times in ht_report_t.ms_stage    */
+
+typedef struct {
+    int order;                   /* 3 or 4                                        */
+    int n_nodes;                 /* 2*order-1                                     */
+    int parent[HT_MAX_NODES];    /* -1 for the root                               */
+    int left[HT_MAX_NODES];      /* -1 for leaves                                 */
+    int right[HT_MAX_NODES];
+    int mode_mask[HT_MAX_NODES]; /* bit m set when mode m (0-based) is in node t  */
+    int rank[HT_MAX_NODES];      /* k_t; rank[0] = 1                              */
+} ht_tree_t;
+
+typedef struct {
+    int precision;        /* ht_precision_t                                      */
+    int leaf_method;      /* ht_leaf_method_t                                    */
+    int oversample;       /* subspace size = k + oversample (default 16)         */
+    int eig_iters;        /* subspace iterations per leaf Gram (default 10)      */
+    int power_steps;      /* power steps of the range finder (default 1)         */
+    unsigned long long seed;  /* Gaussian start / test matrices (default 1234)   */
+    const float *sketch[HT_MAX_ORDER]; /* optional start matrices per mode, n_m x (k+p),
+                                          column-major, host or device; NULL = Gaussian */
+    int flags;            /* HT_FLAG_*                                           */
+    double eig_tol;       /* residual tolerance reported as HT_ERR_NOT_CONVERGED
+                             when exceeded (0 = do not check)                    */
+} ht_config_t;
+
+typedef struct {
+    double rel_err;          /* ||X - Xhat||_F / ||X||_F (HT_FLAG_COMPUTE_ERROR)  */
+    double norm_x;           /* ||X||_F                                           */
+    float ms_total;          /* device time of the decomposition (CUDA events)    */
+    float ms_stage[8];       /* 0 input/convert, 1 grams, 2 eig, 3 core pass,
+                                4 transfer tensors, 5 error, 6 h2d, 7 d2h         */
+    double eig_residual[HT_MAX_NODES]; /* max_j ||G u_j - theta_j u_j|| / theta_1   */
+    int gpu_launches;        /* kernels launched by this call                     */
+    int path_flags;          /* bit 0: tcgen05 path used, bit 1: SIMT path used   */
+} ht_report_t;
+
+/* ------------------------------------------------------------------ setup */
+ht_status_t ht_config_default(ht_config_t *cfg);
+/* Trees of the reference: htd (3rd order) and htd4 (4th order).  k has
+ * 5 / 7 entries indexed by node id; k[0] is ignored (set to 1). */
+ht_status_t ht_tree_reference_3d(ht_tree_t *tree, const int *k);
+ht_status_t ht_tree_balanced_4d(ht_tree_t *tree, const int *k);
+ht_status_t ht_tree_validate(const ht_tree_t *tree, const long *dims, int order);
+
+/* -------------------------------------------------------------- decompose */
+/*
+ * HT decomposition of x (host or device pointer, column-major, dims[0..order)).
+ * Replaces htd() (3D/Opt/htd_tensorcore.cu:2, 3D/Opt/htd_batch.cu:2,
+ * 3D/Base/htd_unopt.cu:2) and htd4() (4D/Opt/htd4_tensorcore.cu:2) with the
+ * factors returned instead of freed.
+ * U[t] (leaves) and B[t] (interior nodes, root) are caller-allocated, host or
+ * device; other entries of U/B are ignored and may be NULL.  stream may be
+ * NULL (legacy default stream).  The call is synchronous with respect to the
+ * host: it returns after the outputs are written.
+ */
+ht_status_t ht_decompose(const float *x, const long *dims, int order,
+                         const ht_tree_t *tree, const ht_config_t *cfg,
+                         float *const *U, float *const *B,
+                         ht_report_t *report, void *stream);
+
+/* Relative reconstruction error ||X - Xhat||_F / ||X||_F of an HT
+ * representation (one fused pass over x on the GPU; htd_batch.cu:196-244). */
+ht_status_t ht_reconstruct_error(const float *x, const long *dims, int order,
+                                 const ht_tree_t *tree,
+                                 const float *const *U, const float *const *B,
+                                 double *rel_err, void *stream);
+
+/* ---------------------------------------------------- unfolding primitives */
+/* The three matricisation products the decomposition is built from, exposed
+ * for direct use.  Modes lo..hi (0-based, contiguous) form the group g; with
+ * L = prod(dims[<lo]), N = prod(dims[lo..hi]), R = prod(dims[>hi]) the tensor
+ * is seen as (L, N, R) and X_(g) is N x (L*R).  precision: ht_precision_t.
+ * All pointers may be host or device; outputs are column-major.
+ *
+ * ht_mode_gram:     G (N x N) = X_(g) X_(g)^T
+ *   (the leaf Gram GEMMs, 3D/Opt/htd_tensorcore.cu:83-121, htd_batch.cu:83-106)
+ * ht_mode_product:  Z ((L*R) x k) = X_(g)^T W, W: N x k
+ *   (the mode-n TTM, 3D/Opt/ttm.cu:2-36 and the root transfer htd_batch.cu:165)
+ * ht_corange_product: Z (N x k) = X_(g) Q, Q: (L*R) x k
+ *   (the rsvd products B = C^T A, 3D/Opt/kernel.cu:618) */
+ht_status_t ht_mode_gram(const float *x, const long *dims, int order, int lo, int hi, int precision,
+                         float *G, void *stream);
+ht_status_t ht_mode_product(const float *x, const long *dims, int order, int lo, int hi, const float *W, int k,
+                            int precision, float *Z, void *stream);
+ht_status_t ht_corange_product(const float *x, const long *dims, int order, int lo, int hi, const float *Q, int k,
+                               int precision, float *Z, void *stream);
+
+/* Bytes of device workspace ht_decompose needs for this problem. */
+ht_status_t ht_workspace_size(const long *dims, int order, const ht_tree_t *tree,
+                              const ht_config_t *cfg, unsigned long long *bytes);
+/* Free the cached device workspace of the current device. */
+ht_status_t ht_release_workspace(void);
+
+const char *ht_status_string(ht_status_t s);
+const char *ht_last_error(void);
+/* Number of kernels this library launched since load (all threads). */
+unsigned long long ht_kernel_launch_count(void);
+
+/* ----------------------------------------------- reference-compatible shims */
+/* float htd(dt *x, long a, long b, long c, int *k)
+ *   third_order_tensor_decompsition/CUDA/Optimized/function.h:6 (htd_tensorcore.cu:2).
+ * x: host tensor a x b x c (column-major), k[5] ranks by node id.  Runs the
+ * mixed-precision path and returns the relative reconstruction error, as the
+ * reference does; returns a negative value on failure (see ht_last_error). */
+float htd(float *x, long a, long b, long c, int *k);
+
+/* void htd4(dt *X, long a, long b, long c, long d, int *k, cublasHandle_t, cusolverDnHandle_t)
+ *   fourth_order_tensor_decomposition/single_GPU/CUDA/Optimized/function.h:6
+ *   (htd4_tensorcore.cu:2).  The two handle arguments are accepted and ignored.
+ * The error is printed to stdout as the reference does. */
+void htd4(float *x, long a, long b, long c, long d, int *k, void *cublas_handle, void *cusolver_handle);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HTGB_H */

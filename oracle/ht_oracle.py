@@ -1,0 +1,179 @@
+"""CPU oracle for the hierarchical Tucker (HT) decomposition path.
+
+TEST INFRASTRUCTURE ONLY.  Nothing in the product imports this module; it is
+used by ``tests/``, by ``__graft_entry__.smoke()`` as the checker, and by
+``bench.py``'s CPU-baseline leg (``cpu_baseline`` / ``--impl reference``).
+
+It is a numpy restatement of the reference's HT algorithm (root-to-leaf
+"hierarchical SVD"), following
+
+* ``third_order_tensor_decompsition/Python/HT_TensorLy.py:52-82``  (CPU statement,
+  tree and node numbering at ``:23-24``),
+* ``third_order_tensor_decompsition/CUDA/Optimized/htd_batch.cu:78-165``  (plain
+  FP32 CUDA path: leaf Gram + eigendecomposition, QR-SVD for node {1,2},
+  ``ttm`` for the transfer tensors, reconstruction + error ``:196-244``),
+* ``fourth_order_tensor_decomposition/single_GPU/Python/HT_4d_TensorNetwork.py:44-69``
+  and ``.../CUDA/Optimized/htd4_tensorcore.cu:2-291`` for the 4th-order tree.
+
+Per node t below the root:
+  leaf t      U_t = top-k_t eigenvectors of X_(t) X_(t)^T      (htd_batch.cu:83-117, HT_TensorLy.py:61-66)
+  interior t  U_t = top-k_t left singular vectors of X_(t)     (htd_batch.cu:146 -> kernel.cu:719, HT_TensorLy.py:55-59)
+  interior t  B_t = (U_right kron U_left)^T U_t, stored k_l x k_r x k_t  (ttm.cu:2-36, HT_TensorLy.py:68-72)
+  root        B_0 = U_left^T X_(left) U_right                  (htd_batch.cu:165, HT_TensorLy.py:68-72)
+Reconstruction and error follow htd_batch.cu:196-244 / HT_TensorLy.py:76-82.
+
+Documented deviations from the reference (both are fixes, not choices):
+* eigenvectors are taken in DESCENDING eigenvalue order.  ``HT_TensorLy.py:64-66``
+  takes the first k columns of the unsorted ``torch.eig`` output and the CUDA
+  code copies the last k columns of the ascending ``syevd`` output; both mean
+  "top-k" only by accident of ordering.  ``eig_order="geev"`` reproduces the
+  Python statement's unsorted choice exactly (LAPACK ``?geev``, which is what
+  ``torch.eig`` called) so the oracle can be pinned to the reference's own
+  outputs.
+* the interior node uses an exact SVD (the Optimized CUDA ``rsvd`` SVDs only
+  the leading ks x ks block of B, ``kernel.cu:641-657``).
+
+Tensors are column-major numpy arrays (Fortran order) as in the reference's
+CUDA code (``htd_tensorcore.cu:12``).
+"""
+from __future__ import annotations
+
+import os
+import sys
+from typing import Dict, Sequence, Tuple
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+if os.path.dirname(_HERE) not in sys.path:
+    sys.path.insert(0, os.path.dirname(_HERE))
+
+from ht_tensor_learning_using_gpu_tensor_cores_gb300.tree import DimTree  # noqa: E402
+from ht_tensor_learning_using_gpu_tensor_cores_gb300.synth import fold  # noqa: E402
+
+
+def unfold(X: np.ndarray, row_modes: Sequence[int]) -> np.ndarray:
+    """Matricisation X_(t): rows over ``row_modes`` (lowest fastest), columns over
+    the remaining modes (lowest fastest).  For the reference tree this is
+    X_(1) = X as a x (bc) (ld a), X_(12) = X as (ab) x c, X_(3) = X_(12)^T."""
+    d = X.ndim
+    rest = [m for m in range(d) if m not in row_modes]
+    rows = int(np.prod([X.shape[m] for m in row_modes]))
+    return np.reshape(np.transpose(X, list(row_modes) + rest), (rows, -1), order="F")
+
+
+def top_eigvecs(G: np.ndarray, k: int, eig_order: str = "desc") -> Tuple[np.ndarray, np.ndarray]:
+    """Top-k eigenpairs of a symmetric Gram.  ``eig_order='geev'`` returns the
+    first k columns of LAPACK ?geev's unsorted output (torch.eig semantics,
+    HT_TensorLy.py:64-66)."""
+    if eig_order == "geev":
+        from scipy.linalg import lapack
+        geev = lapack.sgeev if G.dtype == np.float32 else lapack.dgeev
+        wr, wi, vl, vr, info = geev(G, compute_vl=0, compute_vr=1)
+        if info != 0:
+            raise RuntimeError(f"geev failed: info={info}")
+        return wr[:k], vr[:, :k]
+    w, V = np.linalg.eigh(G)
+    idx = np.argsort(w)[::-1][:k]
+    return w[idx], V[:, idx]
+
+
+def ht_decompose(X: np.ndarray, tree: DimTree, dtype=np.float64, eig_order: str = "desc",
+                 interior_svd: bool = True):
+    """Root-to-leaf HT decomposition (the reference algorithm).
+
+    Returns (U, B, info): U[t] for every non-root node (leaves and interior
+    nodes), B[t] (k_l x k_r x k_t, Fortran order) for interior nodes and the
+    root (k_l x k_r x 1)."""
+    X = np.asarray(X, dtype=dtype)
+    if not X.flags.f_contiguous:
+        X = np.asfortranarray(X)
+    U: Dict[int, np.ndarray] = {}
+    evals: Dict[int, np.ndarray] = {}
+    for t in range(1, tree.n_nodes):
+        A = unfold(X, tree.modes[t])
+        k = tree.ranks[t]
+        if tree.is_leaf(t) or not interior_svd:
+            G = A @ A.T
+            w, V = top_eigvecs(G, k, eig_order)
+            U[t] = np.ascontiguousarray(V)
+            evals[t] = w
+        else:
+            Us, s, _ = np.linalg.svd(A, full_matrices=False)
+            U[t] = Us[:, :k]
+            evals[t] = s[:k] ** 2
+    B: Dict[int, np.ndarray] = {}
+    for t in tree.interior():
+        l, r = tree.left[t], tree.right[t]
+        B[t] = transfer_tensor(U[t], U[l], U[r])
+    l, r = tree.left[0], tree.right[0]
+    M = U[l].T @ unfold(X, tree.modes[l]) @ U[r]
+    B[0] = M.reshape(M.shape[0], M.shape[1], 1, order="F")
+    return U, B, {"evals": evals}
+
+
+def transfer_tensor(Ut: np.ndarray, Ul: np.ndarray, Ur: np.ndarray) -> np.ndarray:
+    """B_t = (U_r kron U_l)^T U_t as a k_l x k_r x k_t Fortran array (ttm.cu:2-36)."""
+    nl, kl = Ul.shape
+    nr, kr = Ur.shape
+    kt = Ut.shape[1]
+    T = Ut.reshape(nl, nr, kt, order="F")
+    Bt = np.einsum("ijc,ia,jb->abc", T, Ul, Ur, optimize=True)
+    return np.asfortranarray(Bt)
+
+
+def node_basis(tree: DimTree, U: Dict[int, np.ndarray], B: Dict[int, np.ndarray], t: int) -> np.ndarray:
+    """Reconstructed basis of node t: U_t for leaves, (U_r kron U_l) B_t above."""
+    if tree.is_leaf(t):
+        return U[t]
+    l, r = tree.left[t], tree.right[t]
+    Ul = node_basis(tree, U, B, l)
+    Ur = node_basis(tree, U, B, r)
+    kt = B[t].shape[2]
+    T = np.einsum("ia,jb,abc->ijc", Ul, Ur, B[t], optimize=True)
+    return T.reshape(Ul.shape[0] * Ur.shape[0], kt, order="F")
+
+
+def ht_reconstruct(tree: DimTree, dims: Sequence[int], U: Dict[int, np.ndarray], B: Dict[int, np.ndarray]) -> np.ndarray:
+    """Full tensor from (U_leaf, B_t) (htd_batch.cu:196-224, HT_TensorLy.py:76-81)."""
+    l, r = tree.left[0], tree.right[0]
+    Ul = node_basis(tree, U, B, l)
+    Ur = node_basis(tree, U, B, r)
+    M = Ul @ B[0][:, :, 0] @ Ur.T
+    return fold(M, tree.modes[l], dims)
+
+
+def rel_error(X: np.ndarray, Xh: np.ndarray) -> float:
+    """||X - Xhat||_F / ||X||_F in float64 (htd_batch.cu:237-244)."""
+    X = np.asarray(X, dtype=np.float64)
+    return float(np.linalg.norm((X - np.asarray(Xh, dtype=np.float64)).ravel()) / np.linalg.norm(X.ravel()))
+
+
+def ht_error(X: np.ndarray, tree: DimTree, U, B) -> float:
+    return rel_error(X, ht_reconstruct(tree, X.shape, U, B))
+
+
+# ----------------------------------------------------------------- comparators
+def principal_angles(U1: np.ndarray, U2: np.ndarray) -> np.ndarray:
+    """Principal angles (radians) between span(U1) and span(U2); inputs need not
+    be orthonormal."""
+    Q1, _ = np.linalg.qr(np.asarray(U1, dtype=np.float64))
+    Q2, _ = np.linalg.qr(np.asarray(U2, dtype=np.float64))
+    s = np.linalg.svd(Q1.T @ Q2, compute_uv=False)
+    return np.arccos(np.clip(s, -1.0, 1.0))
+
+
+def orthogonality_defect(U: np.ndarray) -> float:
+    U = np.asarray(U, dtype=np.float64)
+    return float(np.abs(U.T @ U - np.eye(U.shape[1])).max())
+
+
+def procrustes_align(A: np.ndarray, B: np.ndarray) -> np.ndarray:
+    """Orthogonal Q minimising ||A Q - B||_F."""
+    u, _, vt = np.linalg.svd(np.asarray(A, dtype=np.float64).T @ np.asarray(B, dtype=np.float64))
+    return u @ vt
+
+
+def tree_energy_bound(tree: DimTree) -> float:
+    """Quasi-optimality constant of root-to-leaf HT truncation: sqrt(2d-3)."""
+    return float(np.sqrt(2 * tree.order - 3))
