@@ -224,8 +224,10 @@ struct GemmReq {
   Operand a32, b32;                 // FP32 operands (SIMT path)
   Operand a16, b16;                 // BF16 operands (tcgen05 path); ptr null = unavailable
   int bn_tc = 128, bn_simt = 128;
-  std::vector<Tile> (*make_tiles)(const void *ctx, int bn) = nullptr;
-  const void *tile_ctx = nullptr;
+  // tile generator for a given BN (the SIMT and tcgen05 paths may use different BN)
+  int tiles_kind = TILES_ROWS;
+  long long t_rows = 0, t_L = 0, t_R = 0, t_n = 0;
+  int t_cols = 0;
   int out_mode = OUT_COLMAJOR;
   float *out = nullptr;
   long long ld_out = 0;
@@ -244,8 +246,11 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
     if (!tc_gemm_supported(probe, q.bn_tc, &why)) use_tc = false;
   }
   const int bn = use_tc ? q.bn_tc : q.bn_simt;
-  std::vector<Tile> tiles = q.make_tiles(q.tile_ctx, bn);
-  const int nt = static_cast<int>(tiles.size());
+  TileGen gen;
+  if (q.tiles_kind == TILES_ROWS) gen = make_rows_gen(q.t_rows, q.t_cols, bn);
+  else if (q.tiles_kind == TILES_SLABS) gen = make_slabs_gen(q.t_L, q.t_R, q.t_cols, bn);
+  else if (!make_gram_gen(q.t_n, bn, &gen)) return fail(HT_ERR_UNSUPPORTED, "Gram larger than 32768");
+  const int nt = gen.count;
   int splits = 1;
   if (q.allow_split && nt < sm_count()) splits = std::max(1, sm_count() / nt);
   if (use_tc) {
@@ -261,18 +266,16 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
   }
   const bool partial = splits > 1 || q.out_mode == OUT_PARTIAL;
   const size_t mark = c.ar.off;
-  Tile *dt = c.ar.take<Tile>(nt);
   float *part = partial ? c.ar.take<float>(static_cast<size_t>(splits) * nt * 128 * bn) : nullptr;
   if (c.dry()) {
     c.ar.off = mark;
     return HT_OK;
   }
-  if (!dt || (partial && !part)) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (gemm scratch)");
-  HT_CUDA(cudaMemcpyAsync(dt, tiles.data(), sizeof(Tile) * nt, cudaMemcpyHostToDevice, c.st));
+  if (partial && !part) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (gemm scratch)");
   GemmArgs g;
   g.a = use_tc ? q.a16 : q.a32;
   g.b = use_tc ? q.b16 : q.b32;
-  g.tiles = dt;
+  g.gen = gen;
   g.num_tiles = nt;
   g.splits = splits;
   g.out_mode = partial ? OUT_PARTIAL : OUT_COLMAJOR;
@@ -288,58 +291,11 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
   }
   ++c.launches;
   if (partial) {
-    HT_CUDA(reduce_partials_launch(part, dt, nt, splits, bn, q.out, q.ld_out, q.symmetric ? 1 : 0, c.st));
+    HT_CUDA(reduce_partials_launch(part, gen, splits, bn, q.out, q.ld_out, q.symmetric ? 1 : 0, c.st));
     ++c.launches;
   }
   c.ar.off = mark;   // scratch is stream-ordered: later work may reuse it
   return HT_OK;
-}
-
-// ---- tile generators
-struct GramTiles { long n; };
-std::vector<Tile> gram_tiles(const void *ctx, int bn) {
-  const long n = static_cast<const GramTiles *>(ctx)->n;
-  std::vector<Tile> v;
-  for (long i = 0; i * 128 < n; ++i)
-    for (long j = 0; j * bn < n; ++j) {
-      if (j * bn + bn - 1 < i * 128) continue;   // entirely below the diagonal
-      Tile t;
-      t.a_row = static_cast<int>(i * 128); t.a_z = 0; t.b_row = static_cast<int>(j * bn);
-      t.out_row = i * 128; t.out_col = static_cast<int>(j * bn);
-      t.valid_rows = static_cast<int>(std::min<long>(128, n - i * 128));
-      t.valid_cols = static_cast<int>(std::min<long>(bn, n - j * bn));
-      v.push_back(t);
-    }
-  return v;
-}
-struct RowTiles { long rows; int cols; };
-std::vector<Tile> row_tiles(const void *ctx, int bn) {
-  const RowTiles *r = static_cast<const RowTiles *>(ctx);
-  std::vector<Tile> v;
-  for (long i = 0; i < r->rows; i += 128) {
-    Tile t;
-    t.a_row = static_cast<int>(i); t.a_z = 0; t.b_row = 0;
-    t.out_row = i; t.out_col = 0;
-    t.valid_rows = static_cast<int>(std::min<long>(128, r->rows - i));
-    t.valid_cols = std::min(r->cols, bn);
-    v.push_back(t);
-  }
-  return v;
-}
-struct SlabTiles { long L, R; int cols; };
-std::vector<Tile> slab_tiles(const void *ctx, int bn) {
-  const SlabTiles *s = static_cast<const SlabTiles *>(ctx);
-  std::vector<Tile> v;
-  for (long r = 0; r < s->R; ++r)
-    for (long l = 0; l < s->L; l += 128) {
-      Tile t;
-      t.a_row = static_cast<int>(l); t.a_z = static_cast<int>(r); t.b_row = 0;
-      t.out_row = l + s->L * r; t.out_col = 0;
-      t.valid_rows = static_cast<int>(std::min<long>(128, s->L - l));
-      t.valid_cols = std::min(s->cols, bn);
-      v.push_back(t);
-    }
-  return v;
 }
 
 // G (n x n, column-major, symmetric) = X_(group) X_(group)^T, n = v.N
@@ -350,9 +306,8 @@ ht_status_t gram(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x
   else q.a16.ptr = q.b16.ptr = nullptr;
   q.bn_tc = v.N >= 256 ? 256 : (v.N > 64 ? 128 : 64);
   q.bn_simt = v.N > 64 ? 128 : 64;
-  GramTiles gt{v.N};
-  q.make_tiles = gram_tiles;
-  q.tile_ctx = &gt;
+  q.tiles_kind = TILES_GRAM;
+  q.t_n = v.N;
   q.out_mode = OUT_PARTIAL;
   q.out = G;
   q.ld_out = v.N;
@@ -383,10 +338,11 @@ ht_status_t mode_product(Ctx &c, const View &v, const float *x32, const __nv_bfl
   if (x16 && W16) { q.a16 = opA(x16); q.b16 = opB(W16); }
   else q.a16.ptr = q.b16.ptr = nullptr;
   q.bn_tc = 64; q.bn_simt = 64;
-  RowTiles rt{v.R, k};
-  SlabTiles stl{v.L, v.R, k};
-  if (v.L == 1) { q.make_tiles = row_tiles; q.tile_ctx = &rt; }
-  else { q.make_tiles = slab_tiles; q.tile_ctx = &stl; }
+  if (v.L == 1) {
+    q.tiles_kind = TILES_ROWS; q.t_rows = v.R; q.t_cols = k;
+  } else {
+    q.tiles_kind = TILES_SLABS; q.t_L = v.L; q.t_R = v.R; q.t_cols = k;
+  }
   q.out_mode = OUT_COLMAJOR;
   q.out = Z;
   q.ld_out = v.L * v.R;
@@ -411,9 +367,7 @@ ht_status_t corange_product(Ctx &c, const View &v, const float *x32, const __nv_
   if (x16 && Q16) { q.a16 = gram_operand(v, x16); q.b16 = opB(Q16); }
   else q.a16.ptr = q.b16.ptr = nullptr;
   q.bn_tc = 64; q.bn_simt = 64;
-  RowTiles rt{v.N, k};
-  q.make_tiles = row_tiles;
-  q.tile_ctx = &rt;
+  q.tiles_kind = TILES_ROWS; q.t_rows = v.N; q.t_cols = k;
   q.out_mode = OUT_COLMAJOR;
   q.out = Z;
   q.ld_out = v.N;
@@ -433,9 +387,7 @@ ht_status_t core_contract(Ctx &c, const float *Z, int np, int nq, int ku, const 
   q.b32.kind = OP_KM3; q.b32.ptr = Up; q.b32.d0 = np; q.b32.d1 = kp; q.b32.d2 = 1;
   q.a16.ptr = q.b16.ptr = nullptr;
   q.bn_simt = 64;
-  RowTiles rt{rows, kp};
-  q.make_tiles = row_tiles;
-  q.tile_ctx = &rt;
+  q.tiles_kind = TILES_ROWS; q.t_rows = rows; q.t_cols = kp;
   q.out_mode = OUT_COLMAJOR;
   q.out = T1;
   q.ld_out = rows;
@@ -457,16 +409,24 @@ bool is_device_ptr(const void *p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+int g_dev_ok[64];   // 0 unknown, 1 sm_103, -1 other
 ht_status_t check_device() {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
     cudaGetLastError();
     return fail(HT_ERR_NO_DEVICE, "no CUDA device");
   }
-  cudaDeviceProp prop;
-  HT_CUDA(cudaGetDeviceProperties(&prop, dev));
-  if (!(prop.major == 10 && prop.minor == 3))
-    return fail(HT_ERR_NO_DEVICE, std::string("this build targets sm_103a (GB300); device is ") + prop.name);
+  if (dev >= 0 && dev < 64 && g_dev_ok[dev] == 1) return HT_OK;
+  int major = 0, minor = 0;
+  if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(HT_ERR_NO_DEVICE, "cannot query the CUDA device");
+  }
+  if (!(major == 10 && minor == 3))
+    return fail(HT_ERR_NO_DEVICE, "this build targets sm_103a (GB300); device is sm_" + std::to_string(major) +
+                                      std::to_string(minor));
+  if (dev >= 0 && dev < 64) g_dev_ok[dev] = 1;
   return HT_OK;
 }
 
@@ -553,7 +513,9 @@ ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const 
     const int leaf = T.leaf_of_mode(m);
     const int K = (d3 && leaf == P3.c) ? P3.kw : T.rank[leaf];
     const int n = static_cast<int>(dims[m]);
-    const int s = std::max(K, std::min<int>({n, K + p_over, 64}));
+    // modes of size <= 64: the block is the whole space and the eigen-solver
+    // reduces to a Jacobi eigen-decomposition of the Gram itself
+    const int s = n <= 64 ? n : std::max(K, std::min<int>({n, K + p_over, 64}));
     if (s > 64) return fail(HT_ERR_UNSUPPORTED, "subspace size above 64");
     EigProblem &e = ep[m];
     e.G = G[m]; e.n = n; e.s = s; e.K = K;

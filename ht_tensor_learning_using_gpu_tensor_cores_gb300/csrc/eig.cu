@@ -17,8 +17,10 @@
 // as FP64 accumulation while running at FP32 rate -- GB300's FP64 throughput
 // is 1/64 of FP32.  The Cholesky runs on the unit-diagonal scaled matrix with
 // a small shift, so it cannot break down on rank-deficient blocks.
-// mu = 1e-6 * trace(G) bounds the condition number of Y for exactly
-// low-rank Grams without moving any eigenvector.
+// mu = 1e-9 * trace(G) keeps Y nonzero on exactly null directions without
+// moving any eigenvector or slowing convergence.  When the block covers the
+// whole space (s == n, small modes) the iteration is skipped: Q = I and the
+// Rayleigh-Ritz step is a Jacobi eigen-decomposition of G itself.
 #include <vector>
 
 #include "common.cuh"
@@ -66,7 +68,8 @@ __global__ void eig_init_kernel(const EigBatch probs) {
   const long long total = static_cast<long long>(P.n) * P.s;
   for (long long idx = blockIdx.x * 256ll + threadIdx.x; idx < total; idx += gridDim.x * 256ll) {
     float v;
-    if (P.start) v = P.start[idx];
+    if (P.s == P.n) v = (idx % P.n == idx / P.n) ? 1.f : 0.f;   // direct: Q = I
+    else if (P.start) v = P.start[idx];
     else v = gaussian(P.seed, P.stream_id, static_cast<unsigned long long>(idx));
     P.Q[idx] = v;
   }
@@ -80,7 +83,9 @@ __global__ void eig_init_kernel(const EigBatch probs) {
       if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
       __syncthreads();
     }
-    if (threadIdx.x == 0) P.mu[0] = 1e-6f * fmaxf(red[0], 0.f);
+    // far below the FP32 noise floor of G (~1e-7 ||G||): it only keeps Y
+    // nonzero on exactly null directions, and never slows convergence
+    if (threadIdx.x == 0) P.mu[0] = 1e-9f * fmaxf(red[0], 0.f);
   }
 }
 
@@ -91,6 +96,7 @@ __global__ void __launch_bounds__(256) eig_gq_kernel(const EigBatch probs, int m
   const EigDev &P = probs.p[blockIdx.y];
   const int rb = blockIdx.x;
   if (rb >= P.nrb) return;
+  if (mode != 2 && P.s == P.n && P.G) return;   // direct problems skip the iteration
   const int n = P.n, s = P.s;
   const int r0 = rb * RB;
   const int t = threadIdx.x;
@@ -175,6 +181,7 @@ __global__ void eig_reduce_kernel(const EigBatch probs, int which) {
   const int E = which == 0 ? P.s * (P.s + 1) / 2 : P.s * P.s;
   const int stride = which == 0 ? ESMAX : SMAX * SMAX;
   const float *part = which == 0 ? P.partS : P.partH;
+  if (which == 0 && P.s == P.n && P.G) return;
   for (int e = blockIdx.x * 256 + threadIdx.x; e < E; e += gridDim.x * 256) {
     Acc2 a = {0.f, 0.f};
     for (int r = 0; r < P.nrb; ++r) {
@@ -193,6 +200,7 @@ __global__ void __launch_bounds__(256) eig_orth_kernel(const EigBatch probs, int
   const EigDev &P = probs.p[blockIdx.y];
   const int rb = blockIdx.x;
   if (rb >= P.nrb) return;
+  if (P.s == P.n && P.G) return;   // direct problems skip the iteration
   const int n = P.n, s = P.s;
   __shared__ float A[SMAX][SMAX + 1];   // scaled S, overwritten by R (upper)
   __shared__ float dsc[SMAX];
@@ -213,20 +221,22 @@ __global__ void __launch_bounds__(256) eig_orth_kernel(const EigBatch probs, int
     A[i][j] = v;
   }
   __syncthreads();
-  // Cholesky of the upper triangle by warp 0: A = R^T R
-  if (t < 32) {
-    for (int j = 0; j < s; ++j) {
-      const float piv = A[j][j];
-      const float d = sqrtf(fmaxf(piv, 1e-30f));
-      __syncwarp();
-      for (int k = j + t; k < s; k += 32) A[j][k] = (k == j) ? d : A[j][k] / d;
-      __syncwarp();
-      for (int k = j + 1 + t; k < s; k += 32) {
-        const float rjk = A[j][k];
-        for (int i = j + 1; i <= k; ++i) A[i][k] = fmaf(-A[j][i], rjk, A[i][k]);
+  // Right-looking Cholesky A = R^T R on the upper triangle with all threads.
+  // Step j updates rows > j from the still-unscaled row j, then scales row j;
+  // the next step never touches row j again, so one barrier per step suffices.
+  for (int j = 0; j < s; ++j) {
+    const float d = sqrtf(fmaxf(A[j][j], 1e-30f));
+    const float inv = 1.f / d;
+    const int m = s - j - 1;
+    for (int e = t; e < m * m; e += 256) {
+      const int ii = e % m, kk = e / m;
+      if (ii <= kk) {
+        const int i = j + 1 + ii, k = j + 1 + kk;
+        A[i][k] = fmaf(-(A[j][i] * inv), A[j][k] * inv, A[i][k]);
       }
-      __syncwarp();
     }
+    __syncthreads();
+    for (int k = j + t; k < s; k += 256) A[j][k] = (k == j) ? d : A[j][k] * inv;
   }
   __syncthreads();
   // forward substitution q R = x D^-1/2, one half-warp per row
@@ -280,7 +290,7 @@ HT_DEV void jacobi_smem(float (*A)[SMAX + 1], float (*V)[SMAX + 1], int s, int *
     V[i][j] = (i == j) ? 1.f : 0.f;
   }
   __syncthreads();
-  for (int sweep = 0; sweep < 30 && m > 1; ++sweep) {
+  for (int sweep = 0; sweep < 16 && m > 1; ++sweep) {
     float off = 0.f, dia = 0.f;
     for (int e = t; e < s * s; e += 256) {
       const int i = e % s, j = e / s;
@@ -304,7 +314,7 @@ HT_DEV void jacobi_smem(float (*A)[SMAX + 1], float (*V)[SMAX + 1], int s, int *
     const float dias = red[0];
     __syncthreads();
     // FP32 rounding leaves off-diagonal mass near s * eps^2 * diag mass
-    if (offs <= 1e-12f * dias || offs == 0.f) break;
+    if (offs <= 1e-11f * dias || offs == 0.f) break;
     for (int round = 0; round < m - 1; ++round) {
       if (t < m / 2) {
         // position 0 is fixed, positions 1..m-1 rotate by one each round
@@ -315,7 +325,7 @@ HT_DEV void jacobi_smem(float (*A)[SMAX + 1], float (*V)[SMAX + 1], int s, int *
         float c = 1.f, sv = 0.f;
         if (q < s) {
           const float apq = A[p][q];
-          if (fabsf(apq) > 1e-30f) {
+          if (fabsf(apq) > 1e-30f && fabsf(apq) > 1e-9f * sqrtf(fabsf(A[p][p] * A[q][q]))) {
             const float tau = (A[q][q] - A[p][p]) / (2.f * apq);
             const float tt = (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(1.f + tau * tau));
             c = rsqrtf(1.f + tt * tt);

@@ -43,9 +43,25 @@ struct Tile {
 
 enum OutMode : int { OUT_PARTIAL = 0, OUT_COLMAJOR = 1 };
 
+// Output tiles are generated from a small descriptor passed by value in the
+// kernel parameters (no host->device copy on the launch path).
+enum TileKind : int {
+  TILES_ROWS = 0,   // rows [0, rows) in blocks of 128, one column block
+  TILES_SLABS = 1,  // (l-block, r) blocks of a (L, *, R) view, out_row = l + L*r
+  TILES_GRAM = 2    // blocks of an n x n symmetric matrix on or above the diagonal
+};
+constexpr int kMaxGramRows = 256;   // n <= 32768
+struct TileGen {
+  int kind, count, bn, cols;
+  long long rows, L, R, n;
+  int ni;                            // gram: number of 128-row blocks
+  int prefix[kMaxGramRows + 1];      // gram: tiles before row block i
+  int jmin[kMaxGramRows];            // gram: first column block of row block i
+};
+
 struct GemmArgs {
   Operand a, b;
-  const Tile *tiles;     // device array, num_tiles entries
+  TileGen gen;
   int num_tiles;
   int splits;            // split-K factor (work items = num_tiles * splits)
   int out_mode;
@@ -68,8 +84,11 @@ long simt_k_total(const Operand &a);
 
 // Sum split-K partial tiles.  mode 0: symmetric Gram (tiles on/above the
 // diagonal, mirror into the lower triangle); mode 1: plain column-major.
-cudaError_t reduce_partials_launch(const float *partial, const Tile *tiles, int num_tiles, int splits, int bn,
-                                   float *out, long long ld_out, int symmetric, cudaStream_t s);
+cudaError_t reduce_partials_launch(const float *partial, const TileGen &gen, int splits, int bn, float *out,
+                                   long long ld_out, int symmetric, cudaStream_t s);
+TileGen make_rows_gen(long long rows, int cols, int bn);
+TileGen make_slabs_gen(long long L, long long R, int cols, int bn);
+bool make_gram_gen(long long n, int bn, TileGen *g);
 
 // --------------------------------------------------------------- small ops
 cudaError_t convert_bf16_launch(const float *x, __nv_bfloat16 *xb, long long n, double *sumsq_partials,

@@ -10,6 +10,7 @@
 // register tile per thread, double-buffered shared memory.
 #include "common.cuh"
 #include "engine.h"
+#include "tiles.cuh"
 
 namespace htgb {
 namespace {
@@ -24,7 +25,6 @@ struct SParams {
   long long k_total;
   long long k_per_split;
   int num_tiles, out_mode;
-  const Tile *tiles;
   float *out;
   long long ld_out;
   int a_rows, b_rows;   // operand row extents (for bounds)
@@ -41,7 +41,7 @@ HT_DEV const float *op_ptr(int kind, const float *p, long long d0, long long d1,
 }
 
 template <int BN>
-__global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p) {
+__global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p, const TileGen gen) {
   constexpr int TN = BN / 16;   // columns per thread (8 or 4)
   constexpr int A_PER = BM * BKS / 256;   // 8
   constexpr int B_PER = BN * BKS / 256;   // 8 or 4
@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p) {
   const int tid = threadIdx.x;
   const int tile_idx = blockIdx.x % p.num_tiles;
   const int split = blockIdx.x / p.num_tiles;
-  const Tile tile = p.tiles[tile_idx];
+  const Tile tile = gen_tile(gen, tile_idx);
   const long long kbeg = static_cast<long long>(split) * p.k_per_split;
   const long long kend = min(p.k_total, kbeg + p.k_per_split);
 
@@ -172,8 +172,8 @@ __global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p) {
 }
 
 // Sum partial tiles [splits][num_tiles][128][bn] in a fixed order.
-__global__ void reduce_partials_kernel(const float *__restrict__ part, const Tile *__restrict__ tiles, int num_tiles,
-                                       int splits, int bn, float *__restrict__ out, long long ld, int symmetric) {
+__global__ void reduce_partials_kernel(const float *__restrict__ part, const TileGen gen, int num_tiles, int splits,
+                                       int bn, float *__restrict__ out, long long ld, int symmetric) {
   const long long per_tile = 128ll * bn;
   const long long total = per_tile * num_tiles;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
@@ -181,7 +181,7 @@ __global__ void reduce_partials_kernel(const float *__restrict__ part, const Til
     const int t = static_cast<int>(idx / per_tile);
     const int within = static_cast<int>(idx - t * per_tile);
     const int row = within / bn, col = within % bn;
-    const Tile tl = tiles[t];
+    const Tile tl = gen_tile(gen, t);
     if (row >= tl.valid_rows || col >= tl.valid_cols) continue;
     float s = 0.f;
     for (int k = 0; k < splits; ++k) s += part[(static_cast<long long>(k) * num_tiles + t) * per_tile + within];
@@ -224,28 +224,70 @@ cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s) {
   p.k_per_split = kps;
   p.num_tiles = g.num_tiles;
   p.out_mode = g.out_mode;
-  p.tiles = g.tiles;
   p.out = g.out;
   p.ld_out = g.ld_out;
   p.a_rows = rows_of(g.a.kind, g.a.d0, g.a.d1, g.a.d2);
   p.b_rows = rows_of(g.b.kind, g.b.d0, g.b.d1, g.b.d2);
   const int grid = g.num_tiles * splits;
   if (bn == 128)
-    simt_gemm_kernel<128><<<grid, 256, 0, s>>>(p);
+    simt_gemm_kernel<128><<<grid, 256, 0, s>>>(p, g.gen);
   else if (bn == 64)
-    simt_gemm_kernel<64><<<grid, 256, 0, s>>>(p);
+    simt_gemm_kernel<64><<<grid, 256, 0, s>>>(p, g.gen);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 
-cudaError_t reduce_partials_launch(const float *partial, const Tile *tiles, int num_tiles, int splits, int bn,
-                                   float *out, long long ld_out, int symmetric, cudaStream_t s) {
-  const long long total = 128ll * bn * num_tiles;
+cudaError_t reduce_partials_launch(const float *partial, const TileGen &gen, int splits, int bn, float *out,
+                                   long long ld_out, int symmetric, cudaStream_t s) {
+  const long long total = 128ll * bn * gen.count;
   int grid = static_cast<int>((total + 255) / 256);
   if (grid > 152 * 16) grid = 152 * 16;
-  reduce_partials_kernel<<<grid, 256, 0, s>>>(partial, tiles, num_tiles, splits, bn, out, ld_out, symmetric);
+  reduce_partials_kernel<<<grid, 256, 0, s>>>(partial, gen, gen.count, splits, bn, out, ld_out, symmetric);
   return cudaGetLastError();
+}
+
+TileGen make_rows_gen(long long rows, int cols, int bn) {
+  TileGen g{};
+  g.kind = TILES_ROWS;
+  g.rows = rows;
+  g.cols = cols;
+  g.bn = bn;
+  g.count = static_cast<int>((rows + 127) / 128);
+  return g;
+}
+
+TileGen make_slabs_gen(long long L, long long R, int cols, int bn) {
+  TileGen g{};
+  g.kind = TILES_SLABS;
+  g.L = L;
+  g.R = R;
+  g.cols = cols;
+  g.bn = bn;
+  g.count = static_cast<int>(((L + 127) / 128) * R);
+  return g;
+}
+
+bool make_gram_gen(long long n, int bn, TileGen *g) {
+  *g = TileGen{};
+  g->kind = TILES_GRAM;
+  g->n = n;
+  g->bn = bn;
+  const long long ni = (n + 127) / 128, nj = (n + bn - 1) / bn;
+  if (ni > kMaxGramRows) return false;
+  g->ni = static_cast<int>(ni);
+  int c = 0;
+  for (long long i = 0; i < ni; ++i) {
+    // first column block that reaches the diagonal: bn*(j+1) - 1 >= 128*i
+    long long j0 = (128 * i + 1 + bn - 1) / bn - 1;
+    if (j0 < 0) j0 = 0;
+    g->prefix[i] = c;
+    g->jmin[i] = static_cast<int>(j0);
+    c += static_cast<int>(nj - j0);
+  }
+  g->prefix[ni] = c;
+  g->count = c;
+  return true;
 }
 
 }  // namespace htgb

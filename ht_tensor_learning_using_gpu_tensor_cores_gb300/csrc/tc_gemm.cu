@@ -25,6 +25,7 @@
 
 #include "common.cuh"
 #include "engine.h"
+#include "tiles.cuh"
 
 namespace htgb {
 namespace {
@@ -47,7 +48,6 @@ struct KParams {
   int a_lblocks, b_lblocks;
   int num_kb, kb_per_split;
   int num_tiles, out_mode;
-  const Tile *tiles;
   float *out;
   long long ld_out;
   int *err;
@@ -79,7 +79,7 @@ HT_DEV uint64_t op_desc(int kind, uint32_t base, int kk) {
 template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                   const KParams p) {
+                   const KParams p, const TileGen gen) {
   using C = TcCfg<BN>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tile_idx = blockIdx.x % p.num_tiles;
   const int split = blockIdx.x / p.num_tiles;
-  const Tile tile = p.tiles[tile_idx];
+  const Tile tile = gen_tile(gen, tile_idx);
   const int kb0 = split * p.kb_per_split;
   const int nk = max(0, min(p.num_kb, kb0 + p.kb_per_split) - kb0);
 
@@ -283,13 +283,12 @@ cudaError_t launch_bn(const GemmArgs &g, cudaStream_t s) {
   p.kb_per_split = (p.num_kb + splits - 1) / splits;
   p.num_tiles = g.num_tiles;
   p.out_mode = g.out_mode;
-  p.tiles = g.tiles;
   p.out = g.out;
   p.ld_out = g.ld_out;
   p.err = g.err;
   cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(C::SMEM));
   if (e != cudaSuccess) return e;
-  tc_gemm_kernel<BN><<<g.num_tiles * splits, kThreads, C::SMEM, s>>>(ma, mb, p);
+  tc_gemm_kernel<BN><<<g.num_tiles * splits, kThreads, C::SMEM, s>>>(ma, mb, p, g.gen);
   return cudaGetLastError();
 }
 
