@@ -194,6 +194,15 @@ def run_ours(args, world, rank, local):
     def one(prec, compute_error=False):
         return ht.decompose(X, tree, precision=prec, compute_error=compute_error)
 
+    if args.mixed_only:
+        # profiling mode: only the headline step (warm-up + timed steps), no other work
+        for _ in range(args.warmup + args.steps):
+            one("bf16")
+        torch.cuda.synchronize()
+        if rank == 0:
+            print(json.dumps({"mixed_only": True, "steps": args.steps, "warmup": args.warmup}), flush=True)
+        return
+
     # correctness of both paths against the FP64 optimum (not timed)
     mixed = one("bf16", compute_error=True)
     plain = one("fp32", compute_error=True)
@@ -291,6 +300,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=N_FULL)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--mixed-only", action="store_true",
+                    help="run only the headline mixed-path steps (for profiler launch lists)")
     args = ap.parse_args()
     world, rank, local = dist_setup(args)
     if args.impl == "reference":

@@ -6,21 +6,27 @@
 // are needed, so this is block subspace iteration on G with an oversampled
 // block of s <= 64 columns:
 //
-//   Q <- Gaussian (or a supplied start block)
-//   repeat iters:  Y = (G + mu I) Q ;  Q = Y R^-1   (CholeskyQR, shifted)
-//   two more CholeskyQR passes on Q (orthonormal to FP32 rounding)
+//   Q_0 = Gaussian (or a supplied start block)
+//   Y_i = (G + mu I) Q_i,  Q_{i+1} = Y_i T_i   (T_i: shifted CholeskyQR factor of Y_i)
+//   three more CholeskyQR transforms (orthonormal to FP32 rounding)
 //   Rayleigh-Ritz: H = Q^T G Q, Jacobi eigen-decomposition of H (s x s),
 //   U = Q V[:, top K], GU = G U, residual max_j ||G u_j - theta_j u_j|| / theta_1.
 //
-// Precision: G and Q are FP32; the s x s Gram matrices Y^T Y and Q^T G Q are
-// accumulated with compensated FP32 (TwoProduct/TwoSum), which is as accurate
-// as FP64 accumulation while running at FP32 rate -- GB300's FP64 throughput
-// is 1/64 of FP32.  The Cholesky runs on the unit-diagonal scaled matrix with
-// a small shift, so it cannot break down on rank-deficient blocks.
-// mu = 1e-9 * trace(G) keeps Y nonzero on exactly null directions without
-// moving any eigenvector or slowing convergence.  When the block covers the
-// whole space (s == n, small modes) the iteration is skipped: Q = I and the
-// Rayleigh-Ritz step is a Jacobi eigen-decomposition of G itself.
+// One launch per iteration: since Q_{i+1} = Y_i T_i, a CTA computes its rows
+// of Y_{i+1} = (G Y_i + mu Y_i) T_i from the complete Y_i of the previous
+// launch, applies T_i by forward substitution, and writes its partial of the
+// s x s Gram Y_{i+1}^T Y_{i+1}.  The last CTA to finish (a two-level
+// "last block" reduction: atomic tickets, no waiting) sums the partials in a
+// fixed order and factors T_{i+1} for the next launch.
+//
+// Precision: G and the n x s blocks are FP32; the s x s Gram matrices are
+// accumulated with compensated FP32 (TwoProduct/TwoSum), as accurate as FP64
+// accumulation at FP32 rate -- GB300's FP64 throughput is 1/64 of FP32.  The
+// Cholesky runs on the unit-diagonal scaled matrix with a small shift, so it
+// cannot break down on rank-deficient blocks.  mu = 1e-9 trace(G) keeps Y
+// nonzero on exactly null directions without moving any eigenvector or
+// slowing convergence.  Modes with n <= 64 (s == n) skip the iteration: Q = I
+// and the Rayleigh-Ritz step is a Jacobi eigen-decomposition of G itself.
 #include <vector>
 
 #include "common.cuh"
@@ -30,32 +36,42 @@ namespace htgb {
 namespace {
 
 constexpr int SMAX = 64;
-constexpr int ESMAX = SMAX * (SMAX + 1) / 2;
-constexpr int RB = 16;   // rows per CTA
-
+constexpr int ESMAX = SMAX * (SMAX + 1) / 2;   // packed upper triangle
+constexpr int RB = 16;                          // rows per CTA
+constexpr int GROUP = 8;                        // CTAs per first-level reduction group
 constexpr int kMaxProb = 8;
+constexpr int kThreads = 256;
+
+enum StepMode : int { STEP_ITER = 0, STEP_APPLY = 1, STEP_RR = 2 };
 
 struct EigDev {
   const float *G;
-  int n, s, K, nrb;
-  float *Q, *Y, *U, *GU, *theta, *resid;
+  int n, s, K, nrb, ngroups, direct;
+  float *buf[4];            // n x s work blocks
+  float *U, *GU, *theta, *resid;
   const float *start;
   unsigned long long seed, stream_id;
-  float *partS;    // [nrb][ESMAX][2]
-  float *partH;    // [nrb][SMAX*SMAX][2]
-  double *S;       // [ESMAX]
-  double *H;       // [SMAX*SMAX]
-  float *V;        // [SMAX*SMAX] sorted eigenvectors of H
-  float *mu;       // [1]
-  float *colss;    // [nrb][SMAX]
+  float *part;              // [nrb][ESMAX][2]
+  float *gpart;             // [ngroups][ESMAX][2]
+  int *cnt;                 // [ngroups + 1] tickets, zero between launches
+  float *R[2];              // [SMAX*SMAX] upper factors, row-major, ping-pong slots
+  float *dsc[2];            // [SMAX] column scaling
+  float *V;                 // [SMAX*SMAX] Ritz vectors of H, descending
+  float *mu;                // [1]
+  float *colss;             // [nrb][SMAX]
 };
 
 struct EigBatch {
   EigDev p[kMaxProb];
 };
 
+struct StepArgs {
+  int mode, src, dst, dst2, tslot, t_identity, want_s;
+  float shift, mu_scale;
+};
+
+// packed upper triangle, column-major: e = j(j+1)/2 + i, i <= j
 HT_DEV void tri_index(int e, int &i, int &j) {
-  // packed upper triangle, column-major: e = j(j+1)/2 + i, i <= j
   int jj = static_cast<int>((sqrtf(8.f * e + 1.f) - 1.f) * 0.5f);
   while (jj * (jj + 1) / 2 > e) --jj;
   while ((jj + 1) * (jj + 2) / 2 <= e) ++jj;
@@ -63,216 +79,122 @@ HT_DEV void tri_index(int e, int &i, int &j) {
   i = e - jj * (jj + 1) / 2;
 }
 
-__global__ void eig_init_kernel(const EigBatch probs) {
+// fill = 0: only reset the bookkeeping (tickets), for in-place CholeskyQR.
+__global__ void eig_init_kernel(const EigBatch probs, int fill) {
   const EigDev &P = probs.p[blockIdx.y];
-  const long long total = static_cast<long long>(P.n) * P.s;
+  const long long total = fill ? static_cast<long long>(P.n) * P.s : 0;
+  // direct problems start the Rayleigh-Ritz step from Q = I in buffer 2
+  float *dst = P.direct ? P.buf[2] : P.buf[0];
   for (long long idx = blockIdx.x * 256ll + threadIdx.x; idx < total; idx += gridDim.x * 256ll) {
     float v;
-    if (P.s == P.n) v = (idx % P.n == idx / P.n) ? 1.f : 0.f;   // direct: Q = I
+    if (P.direct) v = (idx % P.n == idx / P.n) ? 1.f : 0.f;
     else if (P.start) v = P.start[idx];
     else v = gaussian(P.seed, P.stream_id, static_cast<unsigned long long>(idx));
-    P.Q[idx] = v;
+    dst[idx] = v;
   }
   if (blockIdx.x == 0) {
     __shared__ float red[256];
     float t = 0.f;
-    for (int i = threadIdx.x; i < P.n; i += 256) t += P.G[i + static_cast<long long>(P.n) * i];
+    for (int i = threadIdx.x; i < P.n; i += 256) t += P.G ? P.G[i + static_cast<long long>(P.n) * i] : 0.f;
     red[threadIdx.x] = t;
     __syncthreads();
     for (int w = 128; w > 0; w >>= 1) {
       if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
       __syncthreads();
     }
-    // far below the FP32 noise floor of G (~1e-7 ||G||): it only keeps Y
-    // nonzero on exactly null directions, and never slows convergence
     if (threadIdx.x == 0) P.mu[0] = 1e-9f * fmaxf(red[0], 0.f);
+    for (int i = threadIdx.x; i <= P.ngroups; i += 256) P.cnt[i] = 0;
   }
 }
 
-// mode 0: Y = (G + mu I) Q, partial Y^T Y
-// mode 1: partial Q^T Q (Y untouched)
-// mode 2: Y = G Q, partial Q^T Y (Rayleigh quotient)
-__global__ void __launch_bounds__(256) eig_gq_kernel(const EigBatch probs, int mode) {
-  const EigDev &P = probs.p[blockIdx.y];
-  const int rb = blockIdx.x;
-  if (rb >= P.nrb) return;
-  if (mode != 2 && P.s == P.n && P.G) return;   // direct problems skip the iteration
-  const int n = P.n, s = P.s;
-  const int r0 = rb * RB;
-  const int t = threadIdx.x;
-  __shared__ float Gs[64][RB + 1];
-  __shared__ float Qs[64][SMAX + 1];
-  __shared__ float Ys[RB][SMAX + 1];
-  __shared__ float Qr[RB][SMAX + 1];
-
-  // rows of Q owned by this CTA
-  for (int e = t; e < RB * SMAX; e += 256) {
-    const int i = e % RB, j = e / RB;
-    float v = 0.f;
-    if (r0 + i < n && j < s) v = P.Q[(r0 + i) + static_cast<long long>(n) * j];
-    Qr[i][j] = v;
-  }
-  if (mode != 1) {
-    const int i = t / 16;            // row within the block
-    const int jb = t % 16;           // columns jb, jb+16, jb+32, jb+48
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int kc = 0; kc < n; kc += 64) {
-      __syncthreads();
-      for (int e = t; e < 64 * RB; e += 256) {
-        const int kk = e % 64, ii = e / 64;
-        float v = 0.f;
-        if (kc + kk < n && r0 + ii < n) v = P.G[(kc + kk) + static_cast<long long>(n) * (r0 + ii)];   // G symmetric
-        Gs[kk][ii] = v;
-      }
-      for (int e = t; e < 64 * SMAX; e += 256) {
-        const int kk = e % 64, j = e / 64;
-        float v = 0.f;
-        if (kc + kk < n && j < s) v = P.Q[(kc + kk) + static_cast<long long>(n) * j];
-        Qs[kk][j] = v;
-      }
-      __syncthreads();
-#pragma unroll 8
-      for (int kk = 0; kk < 64; ++kk) {
-        const float g = Gs[kk][i];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc[c] = fmaf(g, Qs[kk][jb + 16 * c], acc[c]);
-      }
-    }
-    const float mu = (mode == 0) ? P.mu[0] : 0.f;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const int j = jb + 16 * c;
-      float y = acc[c] + mu * Qr[i][j];
-      if (r0 + i >= n || j >= s) y = 0.f;
-      Ys[i][j] = y;
-      if (r0 + i < n && j < s) P.Y[(r0 + i) + static_cast<long long>(n) * j] = y;
-    }
-  } else {
-    for (int e = t; e < RB * SMAX; e += 256) Ys[e % RB][e / RB] = Qr[e % RB][e / RB];
-  }
-  __syncthreads();
-  const int rows = min(RB, n - r0);
-  if (mode != 2) {
-    const int E = s * (s + 1) / 2;
-    for (int e = t; e < E; e += 256) {
-      int i, j;
-      tri_index(e, i, j);
-      Acc2 a = {0.f, 0.f};
-      for (int r = 0; r < rows; ++r) acc2_add_prod(a, Ys[r][i], Ys[r][j]);
-      float *dst = P.partS + (static_cast<long long>(rb) * ESMAX + e) * 2;
-      dst[0] = a.s;
-      dst[1] = a.c;
-    }
-  } else {
-    for (int e = t; e < s * s; e += 256) {
-      const int i = e % s, j = e / s;
-      Acc2 a = {0.f, 0.f};
-      for (int r = 0; r < rows; ++r) acc2_add_prod(a, Qr[r][i], Ys[r][j]);
-      float *dst = P.partH + (static_cast<long long>(rb) * SMAX * SMAX + e) * 2;
-      dst[0] = a.s;
-      dst[1] = a.c;
-    }
-  }
-}
-
-// which 0: S (packed triangle), which 1: H (s x s)
-__global__ void eig_reduce_kernel(const EigBatch probs, int which) {
-  const EigDev &P = probs.p[blockIdx.y];
-  const int E = which == 0 ? P.s * (P.s + 1) / 2 : P.s * P.s;
-  const int stride = which == 0 ? ESMAX : SMAX * SMAX;
-  const float *part = which == 0 ? P.partS : P.partH;
-  if (which == 0 && P.s == P.n && P.G) return;
-  for (int e = blockIdx.x * 256 + threadIdx.x; e < E; e += gridDim.x * 256) {
-    Acc2 a = {0.f, 0.f};
-    for (int r = 0; r < P.nrb; ++r) {
-      const float *src = part + (static_cast<long long>(r) * stride + e) * 2;
-      acc2_add(a, src[0], src[1]);
-    }
-    const double v = static_cast<double>(a.s) + static_cast<double>(a.c);
-    if (which == 0) P.S[e] = v;
-    else P.H[e] = v;
-  }
-}
-
-// Q[rows] = X[rows] D^-1/2 R^-1 where R^T R = D^-1/2 S D^-1/2 + shift I and X
-// is Y (src 0) or Q itself (src 1).
-__global__ void __launch_bounds__(256) eig_orth_kernel(const EigBatch probs, int src, float shift) {
-  const EigDev &P = probs.p[blockIdx.y];
-  const int rb = blockIdx.x;
-  if (rb >= P.nrb) return;
-  if (P.s == P.n && P.G) return;   // direct problems skip the iteration
-  const int n = P.n, s = P.s;
-  __shared__ float A[SMAX][SMAX + 1];   // scaled S, overwritten by R (upper)
-  __shared__ float dsc[SMAX];
-  const int t = threadIdx.x;
-  // scaling
-  for (int j = t; j < s; j += 256) {
-    const double d = P.S[j * (j + 1) / 2 + j];
-    dsc[j] = d > 1e-300 ? static_cast<float>(1.0 / sqrt(d)) : 0.f;
-  }
-  __syncthreads();
-  const int E = s * (s + 1) / 2;
-  for (int e = t; e < E; e += 256) {
-    int i, j;
-    tri_index(e, i, j);
-    const double sc = static_cast<double>(dsc[i]) * static_cast<double>(dsc[j]);
-    float v = static_cast<float>(P.S[e] * sc);
-    if (i == j) v = (dsc[j] > 0.f ? 1.f : 0.f) + shift;
-    A[i][j] = v;
-  }
-  __syncthreads();
-  // Right-looking Cholesky A = R^T R on the upper triangle with all threads.
-  // Step j updates rows > j from the still-unscaled row j, then scales row j;
-  // the next step never touches row j again, so one barrier per step suffices.
-  for (int j = 0; j < s; ++j) {
-    const float d = sqrtf(fmaxf(A[j][j], 1e-30f));
-    const float inv = 1.f / d;
-    const int m = s - j - 1;
-    for (int e = t; e < m * m; e += 256) {
-      const int ii = e % m, kk = e / m;
-      if (ii <= kk) {
-        const int i = j + 1 + ii, k = j + 1 + kk;
-        A[i][k] = fmaf(-(A[j][i] * inv), A[j][k] * inv, A[i][k]);
-      }
-    }
-    __syncthreads();
-    for (int k = j + t; k < s; k += 256) A[j][k] = (k == j) ? d : A[j][k] * inv;
-  }
-  __syncthreads();
-  // forward substitution q R = x D^-1/2, one half-warp per row
-  const int half = t / 16, l = t % 16;
-  const int row = rb * RB + half;
-  const bool valid = row < n;
-  const float *X = src == 0 ? P.Y : P.Q;
-  float tv[4];
+// Forward substitution of one row (one half-warp): x <- (x .* dsc) R^-1 with R
+// upper triangular (row-major, stride SMAX) in shared memory.  Lane l owns
+// columns l, l+16, l+32, l+48.
+HT_DEV void apply_factor_row(float *row, const float *Rs, const float *ds, int s, int l, unsigned mask) {
+  float tv[4], q[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     const int j = l + 16 * c;
-    tv[c] = (valid && j < s) ? X[row + static_cast<long long>(n) * j] * dsc[j] : 0.f;
+    tv[c] = j < s ? row[j] * ds[j] : 0.f;
   }
-  float q[4] = {0.f, 0.f, 0.f, 0.f};
-  const unsigned mask = 0xFFFFu << (16 * ((t / 16) & 1));
   for (int j = 0; j < s; ++j) {
-    const int owner = j % 16, c = j / 16;
+    const int owner = j & 15, cj = j >> 4;
     float qj = 0.f;
-    if (l == owner) {
-      qj = tv[c] / A[j][j];
-      q[c] = qj;
-    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      if (l == owner && c == cj) {
+        qj = tv[c] / Rs[j * SMAX + j];
+        q[c] = qj;
+      }
     qj = __shfl_sync(mask, qj, owner, 16);
 #pragma unroll
-    for (int cc = 0; cc < 4; ++cc) {
-      const int k = l + 16 * cc;
-      if (k > j && k < s) tv[cc] = fmaf(-qj, A[j][k], tv[cc]);
-    }
-  }
-  if (valid) {
-#pragma unroll
     for (int c = 0; c < 4; ++c) {
-      const int j = l + 16 * c;
-      if (j < s) P.Q[row + static_cast<long long>(n) * j] = q[c];
+      const int k = l + 16 * c;
+      if (k > j && k < s) tv[c] = fmaf(-qj, Rs[j * SMAX + k], tv[c]);
     }
   }
+  __syncwarp(mask);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const int j = l + 16 * c;
+    if (j < s) row[j] = q[c];
+  }
+}
+
+// Last-block bookkeeping: returns true in exactly one CTA of the group /
+// of the whole problem once every member has published its partial.
+HT_DEV bool arrive(int *counter, int members, int *s_flag) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int tk = atomicAdd(counter, 1);
+    const int last = (tk == members - 1) ? 1 : 0;
+    if (last) *counter = 0;   // every member has arrived: reset for the next launch
+    *s_flag = last;
+  }
+  __syncthreads();
+  const bool last = *s_flag != 0;
+  if (last) __threadfence();
+  return last;
+}
+
+// Scaled, shifted Cholesky of the packed s x s matrix Sd (double): writes the
+// upper factor R (row-major, stride SMAX) and the scaling dsc to global memory.
+HT_DEV void factor_and_store(const double *Sd, int s, float shift, float *A, float *dsc_sm, float *Rout, float *dout) {
+  const int t = threadIdx.x;
+  for (int j = t; j < s; j += kThreads) {
+    const double d = Sd[j * (j + 1) / 2 + j];
+    dsc_sm[j] = d > 1e-300 ? static_cast<float>(1.0 / sqrt(d)) : 0.f;
+  }
+  __syncthreads();
+  const int E = s * (s + 1) / 2;
+  for (int e = t; e < E; e += kThreads) {
+    int i, j;
+    tri_index(e, i, j);
+    float v = static_cast<float>(Sd[e] * static_cast<double>(dsc_sm[i]) * static_cast<double>(dsc_sm[j]));
+    if (i == j) v = (dsc_sm[j] > 0.f ? 1.f : 0.f) + shift;
+    A[i * SMAX + j] = v;
+  }
+  __syncthreads();
+  // right-looking Cholesky A = R^T R on the upper triangle; step j updates rows
+  // > j from the unscaled row j, then scales row j (never touched again)
+  const int warp = t >> 5, lane = t & 31;
+  for (int j = 0; j < s; ++j) {
+    const float d = sqrtf(fmaxf(A[j * SMAX + j], 1e-30f));
+    const float inv = 1.f / d;
+    for (int i = j + 1 + warp; i < s; i += kThreads / 32) {
+      const float rji = A[j * SMAX + i] * inv;
+      for (int k = i + lane; k < s; k += 32) A[i * SMAX + k] = fmaf(-rji, A[j * SMAX + k] * inv, A[i * SMAX + k]);
+    }
+    __syncthreads();
+    for (int k = j + t; k < s; k += kThreads) A[j * SMAX + k] = (k == j) ? d : A[j * SMAX + k] * inv;
+  }
+  __syncthreads();
+  for (int e = t; e < s * SMAX; e += kThreads) {
+    const int i = e / SMAX, k = e % SMAX;
+    Rout[e] = (k >= i && k < s) ? A[e] : 0.f;
+  }
+  for (int j = t; j < s; j += kThreads) dout[j] = dsc_sm[j];
 }
 
 // Cyclic Jacobi on a symmetric s x s matrix held in shared memory (s <= SMAX),
@@ -372,34 +294,230 @@ HT_DEV void jacobi_smem(float (*A)[SMAX + 1], float (*V)[SMAX + 1], int s, int *
   __syncthreads();
 }
 
-// Rayleigh-Ritz: eigen-decomposition of H = Q^T G Q, one CTA per problem.
-__global__ void __launch_bounds__(256) eig_jacobi_kernel(const EigBatch probs) {
-  const EigDev &P = probs.p[blockIdx.x];
-  const int s = P.s;
-  __shared__ float A[SMAX][SMAX + 1];
-  __shared__ float V[SMAX][SMAX + 1];
+// One step of the eigen-solver for every problem of the batch (see the file
+// comment).  ITER: dst = (G src + mu src) T; APPLY: dst = src T (in place
+// allowed); RR: dst = src T, dst2 = (G src) T and the Rayleigh quotient.
+__global__ void __launch_bounds__(kThreads) eig_step_kernel(const EigBatch probs, const StepArgs a) {
+  const EigDev &P = probs.p[blockIdx.y];
+  const int rb = blockIdx.x;
+  if (rb >= P.nrb) return;
+  if (P.direct && a.mode != STEP_RR) return;
+  extern __shared__ __align__(16) float sm[];
+  float *Rs = sm;                                   // SMAX*SMAX
+  float *ds = Rs + SMAX * SMAX;                     // SMAX
+  float *Zs = ds + SMAX;                            // RB*SMAX  (rows of the result)
+  float *Qr = Zs + RB * SMAX;                       // RB*SMAX  (RR: rows of Q)
+  float *Gs = Qr + RB * SMAX;                       // 64*(RB+1)
+  float *Ss = Gs + 64 * (RB + 1);                   // 64*68 (chunk of src), 16-byte aligned rows
+  double *Sd = reinterpret_cast<double *>(Ss + 64 * 68);   // ESMAX (final reducer)
+  float *Vs = reinterpret_cast<float *>(Sd + ESMAX);       // SMAX*(SMAX+1) (RR Jacobi)
+  __shared__ int s_flag;
   __shared__ int order[SMAX];
-  const int t = threadIdx.x;
-  for (int e = t; e < SMAX * SMAX; e += 256) {
-    const int i = e % SMAX, j = e / SMAX;
-    A[i][j] = (i < s && j < s) ? static_cast<float>(0.5 * (P.H[i + s * j] + P.H[j + s * i])) : 0.f;
+  const int n = P.n, s = P.s, t = threadIdx.x;
+  const int r0 = rb * RB;
+  const int rows = min(RB, n - r0);
+  const float *src = P.buf[a.src];
+  const bool ident = a.t_identity || P.direct;
+
+  if (!ident) {
+    for (int e = t; e < SMAX * SMAX; e += kThreads) Rs[e] = P.R[a.tslot][e];
+    for (int j = t; j < SMAX; j += kThreads) ds[j] = P.dsc[a.tslot][j];
+  }
+  // rows of src owned by this CTA
+  for (int e = t; e < RB * SMAX; e += kThreads) {
+    const int i = e % RB, j = e / RB;
+    const float v = (i < rows && j < s) ? src[(r0 + i) + static_cast<long long>(n) * j] : 0.f;
+    if (a.mode == STEP_APPLY) Zs[i * SMAX + j] = v;
+    else Qr[i * SMAX + j] = v;
+  }
+  if (a.mode != STEP_APPLY) {
+    // Z = G[rows, :] src   (G symmetric: read G[k, rows] contiguously in k)
+    const int i = t >> 4, cg = t & 15;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int kc = 0; kc < n; kc += 64) {
+      __syncthreads();
+      for (int e = t; e < 64 * RB; e += kThreads) {
+        const int kk = e % 64, ii = e / 64;
+        Gs[kk * (RB + 1) + ii] =
+            (kc + kk < n && ii < rows) ? P.G[(kc + kk) + static_cast<long long>(n) * (r0 + ii)] : 0.f;
+      }
+      for (int e = t; e < 64 * SMAX; e += kThreads) {
+        const int kk = e % 64, j = e / 64;
+        Ss[kk * 68 + j] = (kc + kk < n && j < s) ? src[(kc + kk) + static_cast<long long>(n) * j] : 0.f;
+      }
+      __syncthreads();
+#pragma unroll 8
+      for (int kk = 0; kk < 64; ++kk) {
+        const float g = Gs[kk * (RB + 1) + i];
+        const float4 q4 = *reinterpret_cast<const float4 *>(&Ss[kk * 68 + 4 * cg]);
+        acc[0] = fmaf(g, q4.x, acc[0]);
+        acc[1] = fmaf(g, q4.y, acc[1]);
+        acc[2] = fmaf(g, q4.z, acc[2]);
+        acc[3] = fmaf(g, q4.w, acc[3]);
+      }
+    }
+    const float mu = (a.mode == STEP_ITER) ? P.mu[0] * a.mu_scale : 0.f;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int j = 4 * cg + c;
+      Zs[i * SMAX + j] = (i < rows && j < s) ? acc[c] + mu * Qr[i * SMAX + j] : 0.f;
+    }
   }
   __syncthreads();
-  jacobi_smem(A, V, s, order);
-  for (int e = t; e < s * s; e += 256) {
-    const int i = e % s, r = e / s;
-    P.V[i + s * r] = V[i][order[r]];
+  // apply the previous factor: one half-warp per row
+  if (!ident) {
+    const int half = t >> 4, l = t & 15;
+    const unsigned mask = 0xFFFFu << (16 * (half & 1));
+    apply_factor_row(Zs + half * SMAX, Rs, ds, s, l, mask);
+    if (a.mode == STEP_RR) apply_factor_row(Qr + half * SMAX, Rs, ds, s, l, mask);
   }
-  for (int r = t; r < P.K; r += 256) P.theta[r] = A[order[r]][order[r]];
+  __syncthreads();
+  float *dst = P.buf[a.dst];
+  if (a.mode == STEP_RR) {
+    float *dst2 = P.buf[a.dst2];
+    for (int e = t; e < RB * SMAX; e += kThreads) {
+      const int i = e % RB, j = e / RB;
+      if (i < rows && j < s) {
+        dst[(r0 + i) + static_cast<long long>(n) * j] = Qr[i * SMAX + j];
+        dst2[(r0 + i) + static_cast<long long>(n) * j] = Zs[i * SMAX + j];
+      }
+    }
+  } else {
+    for (int e = t; e < RB * SMAX; e += kThreads) {
+      const int i = e % RB, j = e / RB;
+      if (i < rows && j < s) dst[(r0 + i) + static_cast<long long>(n) * j] = Zs[i * SMAX + j];
+    }
+  }
+  if (!a.want_s) return;
+  // partial of the s x s Gram (ITER/APPLY: Y^T Y, RR: Q^T Y), packed upper triangle
+  const int E = s * (s + 1) / 2;
+  const float *L = (a.mode == STEP_RR) ? Qr : Zs;
+  for (int e = t; e < E; e += kThreads) {
+    int i, j;
+    tri_index(e, i, j);
+    Acc2 acc = {0.f, 0.f};
+    for (int r = 0; r < rows; ++r) acc2_add_prod(acc, L[r * SMAX + i], Zs[r * SMAX + j]);
+    float *d = P.part + (static_cast<long long>(rb) * ESMAX + e) * 2;
+    d[0] = acc.s;
+    d[1] = acc.c;
+  }
+  // two-level deterministic reduction by the last CTAs to arrive
+  const int g = rb / GROUP;
+  const int gsize = min(GROUP, P.nrb - g * GROUP);
+  if (!arrive(&P.cnt[g], gsize, &s_flag)) return;
+  for (int e = t; e < E; e += kThreads) {
+    Acc2 acc = {0.f, 0.f};
+    for (int r = g * GROUP; r < g * GROUP + gsize; ++r) {
+      const float *p = P.part + (static_cast<long long>(r) * ESMAX + e) * 2;
+      acc2_add(acc, __ldcg(p), __ldcg(p + 1));
+    }
+    float *d = P.gpart + (static_cast<long long>(g) * ESMAX + e) * 2;
+    d[0] = acc.s;
+    d[1] = acc.c;
+  }
+  if (!arrive(&P.cnt[P.ngroups], P.ngroups, &s_flag)) return;
+  for (int e = t; e < E; e += kThreads) {
+    Acc2 acc = {0.f, 0.f};
+    for (int gg = 0; gg < P.ngroups; ++gg) {
+      const float *p = P.gpart + (static_cast<long long>(gg) * ESMAX + e) * 2;
+      acc2_add(acc, __ldcg(p), __ldcg(p + 1));
+    }
+    Sd[e] = static_cast<double>(acc.s) + static_cast<double>(acc.c);
+  }
+  __syncthreads();
+  if (a.mode != STEP_RR) {
+    factor_and_store(Sd, s, a.shift, Rs, ds, P.R[a.tslot ^ 1], P.dsc[a.tslot ^ 1]);
+    return;
+  }
+  // Rayleigh-Ritz: Jacobi on H (symmetrised from the upper triangle)
+  float (*A)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(Rs);
+  float (*VV)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(Vs);
+  for (int e = t; e < SMAX * SMAX; e += kThreads) {
+    const int i = e % SMAX, j = e / SMAX;
+    float v = 0.f;
+    if (i < s && j < s) v = static_cast<float>(i <= j ? Sd[j * (j + 1) / 2 + i] : Sd[i * (i + 1) / 2 + j]);
+    A[i][j] = v;
+  }
+  __syncthreads();
+  jacobi_smem(A, VV, s, order);
+  for (int e = t; e < s * s; e += kThreads) {
+    const int i = e % s, r = e / s;
+    P.V[i + s * r] = VV[i][order[r]];
+  }
+  for (int r = t; r < P.K; r += kThreads) P.theta[r] = A[order[r]][order[r]];
+}
+
+// U = Q V[:, :K], GU = Y V[:, :K], residual max_j ||GU_j - theta_j U_j|| / theta_1.
+__global__ void __launch_bounds__(kThreads) eig_final_kernel(const EigBatch probs, int qbuf, int ybuf) {
+  const EigDev &P = probs.p[blockIdx.y];
+  const int rb = blockIdx.x;
+  if (rb >= P.nrb) return;
+  const int n = P.n, s = P.s, K = P.K;
+  __shared__ float Vsm[SMAX][SMAX + 1];
+  __shared__ float Qr[RB][SMAX + 1];
+  __shared__ float Yr[RB][SMAX + 1];
+  __shared__ float res[RB][SMAX + 1];
+  __shared__ int s_flag;
+  const int t = threadIdx.x;
+  const int r0 = rb * RB;
+  const float *Q = P.buf[qbuf], *Y = P.buf[ybuf];
+  for (int e = t; e < SMAX * SMAX; e += kThreads) {
+    const int i = e % SMAX, j = e / SMAX;
+    Vsm[i][j] = (i < s && j < s) ? P.V[i + s * j] : 0.f;
+  }
+  for (int e = t; e < RB * SMAX; e += kThreads) {
+    const int i = e % RB, j = e / RB;
+    const bool ok = r0 + i < n && j < s;
+    Qr[i][j] = ok ? Q[(r0 + i) + static_cast<long long>(n) * j] : 0.f;
+    Yr[i][j] = ok ? Y[(r0 + i) + static_cast<long long>(n) * j] : 0.f;
+  }
+  __syncthreads();
+  const int i = t / 16, jb = t % 16;
+  for (int c = 0; c < 4; ++c) {
+    const int j = jb + 16 * c;
+    float u = 0.f, gu = 0.f;
+    if (j < K) {
+      for (int k = 0; k < s; ++k) {
+        u = fmaf(Qr[i][k], Vsm[k][j], u);
+        gu = fmaf(Yr[i][k], Vsm[k][j], gu);
+      }
+    }
+    const bool ok = (r0 + i < n) && j < K;
+    if (ok) {
+      P.U[(r0 + i) + static_cast<long long>(n) * j] = u;
+      P.GU[(r0 + i) + static_cast<long long>(n) * j] = gu;
+    }
+    const float d = ok ? gu - P.theta[j] * u : 0.f;
+    res[i][j] = d * d;
+  }
+  __syncthreads();
+  for (int j = t; j < K; j += kThreads) {
+    float acc = 0.f;
+    for (int r = 0; r < RB; ++r) acc += res[r][j];
+    P.colss[static_cast<long long>(rb) * SMAX + j] = acc;
+  }
+  if (!arrive(&P.cnt[P.ngroups], P.nrb, &s_flag)) return;
+  if (t == 0) {
+    float m = 0.f;
+    for (int j = 0; j < K; ++j) {
+      float acc = 0.f;
+      for (int r = 0; r < P.nrb; ++r) acc += __ldcg(P.colss + static_cast<long long>(r) * SMAX + j);
+      m = fmaxf(m, sqrtf(acc));
+    }
+    const float th = P.theta[0];
+    P.resid[0] = th > 0.f ? m / th : m;
+  }
 }
 
 // Transfer-tensor step of the complementary-leaf construction.  WG = W^T G_c W
 // (kw x kw, leading dimension kw) for the complementary leaf's Ritz block W;
 // V = W[:, :kt].  With GV = V^T G_c V = P diag(lam) P^T:
 //   M     = P diag(lam^-1/2)   (columns with lam <= 1e-12 lam_max are zero)
-//   Broot = M^T V^T G_c U_c    (kt x kc; stored transposed when the interior
-//                               node is the root's right child)
-// and the caller forms B_t = C_V M.
+//   Broot = M^T V^T G_c U_c    (kt x kc)
+// and the caller forms B_t = C_V M.  On the columns U_c shares with V
+// (u < min(kt, kc)) V^T G_c U_c = GV[:, u], so Broot = diag(lam^1/2) P^T there:
+// writing it that way makes B_t Broot = C_V P P^T exactly, instead of relying on
+// lam^-1 * lam cancelling in FP32, which fails for ill-conditioned Grams.
 __global__ void __launch_bounds__(256) transfer_eig_kernel(const float *WG, int kw, int kt, int kc, int t_is_left,
                                                            float *M, float *Broot) {
   __shared__ float A[SMAX][SMAX + 1];
@@ -428,77 +546,16 @@ __global__ void __launch_bounds__(256) transfer_eig_kernel(const float *WG, int 
   __syncthreads();
   for (int e = t; e < kt * kc; e += 256) {
     const int r = e % kt, u = e / kt;
-    float acc = 0.f;
     const int oc = order[r];
-    for (int c = 0; c < kt; ++c) acc = fmaf(V[c][oc] * inv[r], 0.5f * (WG[c + kw * u] + WG[u + kw * c]), acc);
+    float acc;
+    if (u < kt) {
+      acc = inv[r] > 0.f ? sqrtf(A[oc][oc]) * V[u][oc] : 0.f;
+    } else {
+      acc = 0.f;
+      for (int c = 0; c < kt; ++c) acc = fmaf(V[c][oc] * inv[r], 0.5f * (WG[c + kw * u] + WG[u + kw * c]), acc);
+    }
     if (t_is_left) Broot[r + kt * u] = acc;
     else Broot[u + kc * r] = acc;
-  }
-}
-
-// U = Q V[:, :K], GU = Y V[:, :K], residual partials.
-__global__ void __launch_bounds__(256) eig_finalize_kernel(const EigBatch probs) {
-  const EigDev &P = probs.p[blockIdx.y];
-  const int rb = blockIdx.x;
-  if (rb >= P.nrb) return;
-  const int n = P.n, s = P.s, K = P.K;
-  __shared__ float Vs[SMAX][SMAX + 1];
-  __shared__ float Qr[RB][SMAX + 1];
-  __shared__ float Yr[RB][SMAX + 1];
-  __shared__ float res[RB][SMAX + 1];
-  const int t = threadIdx.x;
-  const int r0 = rb * RB;
-  for (int e = t; e < SMAX * SMAX; e += 256) {
-    const int i = e % SMAX, j = e / SMAX;
-    Vs[i][j] = (i < s && j < s) ? P.V[i + s * j] : 0.f;
-  }
-  for (int e = t; e < RB * SMAX; e += 256) {
-    const int i = e % RB, j = e / RB;
-    const bool ok = r0 + i < n && j < s;
-    Qr[i][j] = ok ? P.Q[(r0 + i) + static_cast<long long>(n) * j] : 0.f;
-    Yr[i][j] = ok ? P.Y[(r0 + i) + static_cast<long long>(n) * j] : 0.f;
-  }
-  __syncthreads();
-  const int i = t / 16, jb = t % 16;
-  for (int c = 0; c < 4; ++c) {
-    const int j = jb + 16 * c;
-    float u = 0.f, gu = 0.f;
-    if (j < K) {
-      for (int k = 0; k < s; ++k) {
-        u = fmaf(Qr[i][k], Vs[k][j], u);
-        gu = fmaf(Yr[i][k], Vs[k][j], gu);
-      }
-    }
-    const bool ok = (r0 + i < n) && j < K;
-    if (ok) {
-      P.U[(r0 + i) + static_cast<long long>(n) * j] = u;
-      P.GU[(r0 + i) + static_cast<long long>(n) * j] = gu;
-    }
-    const float d = ok ? gu - P.theta[j] * u : 0.f;
-    res[i][j] = d * d;
-  }
-  __syncthreads();
-  for (int j = t; j < K; j += 256) {
-    float a = 0.f;
-    for (int r = 0; r < RB; ++r) a += res[r][j];
-    P.colss[static_cast<long long>(rb) * SMAX + j] = a;
-  }
-}
-
-__global__ void eig_resid_kernel(const EigBatch probs) {
-  const EigDev &P = probs.p[blockIdx.x];
-  __shared__ float red[64];
-  const int j = threadIdx.x;
-  float a = 0.f;
-  if (j < P.K)
-    for (int r = 0; r < P.nrb; ++r) a += P.colss[static_cast<long long>(r) * SMAX + j];
-  red[j] = sqrtf(a);
-  __syncthreads();
-  if (j == 0) {
-    float m = 0.f;
-    for (int i = 0; i < P.K; ++i) m = fmaxf(m, red[i]);
-    const float th = P.theta[0];
-    P.resid[0] = th > 0.f ? m / th : m;
   }
 }
 
@@ -549,16 +606,21 @@ __global__ void __launch_bounds__(256) svd_from_gram_kernel(const float *GW, int
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+constexpr size_t kStepSmem = sizeof(float) * (SMAX * SMAX + SMAX + 2 * RB * SMAX + 64 * (RB + 1) + 64 * 68) +
+                             sizeof(double) * ESMAX + sizeof(float) * SMAX * (SMAX + 1) + 64;
+
 }  // namespace
 
 size_t eig_workspace_bytes(const EigProblem *probs, int nprob) {
-  size_t b = align256(sizeof(EigDev) * nprob);
+  size_t b = 0;
   for (int i = 0; i < nprob; ++i) {
     const int nrb = (probs[i].n + RB - 1) / RB;
+    const int ng = (nrb + GROUP - 1) / GROUP;
+    b += 4 * align256(sizeof(float) * static_cast<size_t>(probs[i].n) * SMAX);
     b += align256(sizeof(float) * nrb * ESMAX * 2);
-    b += align256(sizeof(float) * nrb * SMAX * SMAX * 2);
-    b += align256(sizeof(double) * ESMAX);
-    b += align256(sizeof(double) * SMAX * SMAX);
+    b += align256(sizeof(float) * ng * ESMAX * 2);
+    b += align256(sizeof(int) * (ng + 1));
+    b += 2 * align256(sizeof(float) * SMAX * SMAX) + 2 * align256(sizeof(float) * SMAX);
     b += align256(sizeof(float) * SMAX * SMAX);
     b += align256(sizeof(float) * 4);
     b += align256(sizeof(float) * nrb * SMAX);
@@ -571,7 +633,6 @@ static cudaError_t build_batch(const EigProblem *probs, int nprob, void *ws, siz
   if (nprob > kMaxProb) return cudaErrorInvalidValue;
   if (eig_workspace_bytes(probs, nprob) > ws_bytes) return cudaErrorInvalidValue;
   char *p = static_cast<char *>(ws);
-  p += align256(sizeof(EigDev) * nprob);
   max_nrb = 0;
   for (int i = 0; i < nprob; ++i) {
     const EigProblem &q = probs[i];
@@ -579,18 +640,32 @@ static cudaError_t build_batch(const EigProblem *probs, int nprob, void *ws, siz
     EigDev &d = b.p[i];
     d.G = q.G; d.n = q.n; d.s = q.s; d.K = q.K;
     d.nrb = (q.n + RB - 1) / RB;
+    d.ngroups = (d.nrb + GROUP - 1) / GROUP;
+    d.direct = (q.G != nullptr && q.s == q.n) ? 1 : 0;
     max_nrb = d.nrb > max_nrb ? d.nrb : max_nrb;
-    d.Q = q.Q; d.Y = q.Y; d.U = q.U; d.GU = q.GU; d.theta = q.theta; d.resid = q.resid;
+    d.U = q.U; d.GU = q.GU; d.theta = q.theta; d.resid = q.resid;
     d.start = q.start; d.seed = q.seed; d.stream_id = q.stream_id;
-    d.partS = reinterpret_cast<float *>(p); p += align256(sizeof(float) * d.nrb * ESMAX * 2);
-    d.partH = reinterpret_cast<float *>(p); p += align256(sizeof(float) * d.nrb * SMAX * SMAX * 2);
-    d.S = reinterpret_cast<double *>(p); p += align256(sizeof(double) * ESMAX);
-    d.H = reinterpret_cast<double *>(p); p += align256(sizeof(double) * SMAX * SMAX);
+    for (int k = 0; k < 4; ++k) {
+      d.buf[k] = reinterpret_cast<float *>(p);
+      p += align256(sizeof(float) * static_cast<size_t>(q.n) * SMAX);
+    }
+    d.part = reinterpret_cast<float *>(p); p += align256(sizeof(float) * d.nrb * ESMAX * 2);
+    d.gpart = reinterpret_cast<float *>(p); p += align256(sizeof(float) * d.ngroups * ESMAX * 2);
+    d.cnt = reinterpret_cast<int *>(p); p += align256(sizeof(int) * (d.ngroups + 1));
+    for (int k = 0; k < 2; ++k) {
+      d.R[k] = reinterpret_cast<float *>(p); p += align256(sizeof(float) * SMAX * SMAX);
+      d.dsc[k] = reinterpret_cast<float *>(p); p += align256(sizeof(float) * SMAX);
+    }
     d.V = reinterpret_cast<float *>(p); p += align256(sizeof(float) * SMAX * SMAX);
     d.mu = reinterpret_cast<float *>(p); p += align256(sizeof(float) * 4);
     d.colss = reinterpret_cast<float *>(p); p += align256(sizeof(float) * d.nrb * SMAX);
   }
   return cudaSuccess;
+}
+
+static cudaError_t launch_step(const EigBatch &b, int nprob, int max_nrb, StepArgs a, cudaStream_t st) {
+  eig_step_kernel<<<dim3(max_nrb, nprob), kThreads, kStepSmem, st>>>(b, a);
+  return cudaGetLastError();
 }
 
 cudaError_t eig_batched(EigProblem *probs, int nprob, int iters, void *ws, size_t ws_bytes, int *err, cudaStream_t st,
@@ -601,28 +676,33 @@ cudaError_t eig_batched(EigProblem *probs, int nprob, int iters, void *ws, size_
   int max_nrb = 0;
   cudaError_t e = build_batch(probs, nprob, ws, ws_bytes, b, max_nrb);
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(eig_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kStepSmem));
+  if (e != cudaSuccess) return e;
   int nl = 0;
-  const dim3 rows(max_nrb, nprob);
-  eig_init_kernel<<<dim3(64, nprob), 256, 0, st>>>(b); ++nl;
+  eig_init_kernel<<<dim3(64, nprob), 256, 0, st>>>(b, 1); ++nl;
+  int cur = 0, tslot = 0, ident = 1;
   for (int it = 0; it < iters; ++it) {
-    eig_gq_kernel<<<rows, 256, 0, st>>>(b, 0); ++nl;
-    eig_reduce_kernel<<<dim3((ESMAX + 255) / 256, nprob), 256, 0, st>>>(b, 0); ++nl;
-    eig_orth_kernel<<<rows, 256, 0, st>>>(b, 0, 1e-5f); ++nl;
+    StepArgs a{STEP_ITER, cur, cur ^ 1, 0, tslot, ident, 1, 1e-5f, 1.f};
+    if ((e = launch_step(b, nprob, max_nrb, a, st)) != cudaSuccess) return e;
+    ++nl;
+    ident = 0; tslot ^= 1; cur ^= 1;
   }
-  for (int pass = 0; pass < 2; ++pass) {
-    eig_gq_kernel<<<rows, 256, 0, st>>>(b, 1); ++nl;
-    eig_reduce_kernel<<<dim3((ESMAX + 255) / 256, nprob), 256, 0, st>>>(b, 0); ++nl;
-    eig_orth_kernel<<<rows, 256, 0, st>>>(b, 1, pass == 0 ? 1e-6f : 0.f); ++nl;
-  }
-  eig_gq_kernel<<<rows, 256, 0, st>>>(b, 2); ++nl;
-  eig_reduce_kernel<<<dim3((SMAX * SMAX + 255) / 256, nprob), 256, 0, st>>>(b, 1); ++nl;
-  eig_jacobi_kernel<<<nprob, 256, 0, st>>>(b); ++nl;
-  eig_finalize_kernel<<<rows, 256, 0, st>>>(b); ++nl;
-  eig_resid_kernel<<<nprob, 64, 0, st>>>(b); ++nl;
+  // three CholeskyQR transforms: Y_L T_L -> buffer 2, then twice in place
+  StepArgs f1{STEP_APPLY, cur, 2, 0, tslot, ident, 1, 1e-6f, 0.f};
+  if ((e = launch_step(b, nprob, max_nrb, f1, st)) != cudaSuccess) return e;
+  tslot ^= 1;
+  StepArgs f2{STEP_APPLY, 2, 2, 0, tslot, 0, 1, 0.f, 0.f};
+  if ((e = launch_step(b, nprob, max_nrb, f2, st)) != cudaSuccess) return e;
+  tslot ^= 1;
+  StepArgs rr{STEP_RR, 2, 3, 0, tslot, 0, 1, 0.f, 0.f};
+  if ((e = launch_step(b, nprob, max_nrb, rr, st)) != cudaSuccess) return e;
+  eig_final_kernel<<<dim3(max_nrb, nprob), kThreads, 0, st>>>(b, 3, 0);
+  nl += 4;
   if (launches) *launches += nl;
   return cudaGetLastError();
 }
 
+// In-place CholeskyQR3 of tall blocks (G == nullptr problems, buffer 0 = the matrix).
 cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, size_t ws_bytes, cudaStream_t st,
                            int *launches) {
   if (nprob <= 0) return cudaSuccess;
@@ -630,12 +710,18 @@ cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, s
   int max_nrb = 0;
   cudaError_t e = build_batch(probs, nprob, ws, ws_bytes, b, max_nrb);
   if (e != cudaSuccess) return e;
+  for (int i = 0; i < nprob; ++i) b.p[i].buf[0] = probs[i].Q;   // operate on the caller's matrix in place
+  e = cudaFuncSetAttribute(eig_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kStepSmem));
+  if (e != cudaSuccess) return e;
   int nl = 0;
-  const dim3 rows(max_nrb, nprob);
-  for (int pass = 0; pass < passes; ++pass) {
-    eig_gq_kernel<<<rows, 256, 0, st>>>(b, 1); ++nl;
-    eig_reduce_kernel<<<dim3((ESMAX + 255) / 256, nprob), 256, 0, st>>>(b, 0); ++nl;
-    eig_orth_kernel<<<rows, 256, 0, st>>>(b, 1, pass == 0 ? 1e-6f : 0.f); ++nl;
+  eig_init_kernel<<<dim3(1, nprob), 256, 0, st>>>(b, 0);   // zeroes the tickets only
+  ++nl;
+  int tslot = 0;
+  for (int pass = 0; pass <= passes; ++pass) {
+    StepArgs a{STEP_APPLY, 0, 0, 0, tslot, pass == 0 ? 1 : 0, pass < passes ? 1 : 0, pass == 0 ? 1e-6f : 0.f, 0.f};
+    if ((e = launch_step(b, nprob, max_nrb, a, st)) != cudaSuccess) return e;
+    ++nl;
+    if (pass < passes) tslot ^= 1;
   }
   if (launches) *launches += nl;
   return cudaGetLastError();
