@@ -158,6 +158,27 @@ HT_DEV bool arrive(int *counter, int members, int *s_flag) {
   return last;
 }
 
+// acc += sum of the (hi, lo) pairs of entry e in partials [first, first+count),
+// in order; loads are issued GROUP at a time so their latencies overlap.
+HT_DEV void sum_pairs(Acc2 &acc, const float *base, int first, int count, int e) {
+  for (int r0 = 0; r0 < count; r0 += GROUP) {
+    float hi[GROUP], lo[GROUP];
+#pragma unroll
+    for (int q = 0; q < GROUP; ++q) {
+      if (r0 + q < count) {
+        const float *p = base + (static_cast<long long>(first + r0 + q) * ESMAX + e) * 2;
+        hi[q] = __ldcg(p);
+        lo[q] = __ldcg(p + 1);
+      } else {
+        hi[q] = 0.f;
+        lo[q] = 0.f;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < GROUP; ++q) acc2_add(acc, hi[q], lo[q]);
+  }
+}
+
 // Scaled, shifted Cholesky of the packed s x s matrix Sd (double): writes the
 // upper factor R (row-major, stride SMAX) and the scaling dsc to global memory.
 HT_DEV void factor_and_store(const double *Sd, int s, float shift, float *A, float *dsc_sm, float *Rout, float *dout) {
@@ -212,7 +233,8 @@ HT_DEV void jacobi_smem(float (*A)[SMAX + 1], float (*V)[SMAX + 1], int s, int *
     V[i][j] = (i == j) ? 1.f : 0.f;
   }
   __syncthreads();
-  for (int sweep = 0; sweep < 16 && m > 1; ++sweep) {
+  int extra = -1;   // sweeps still to run once the Frobenius criterion is met
+  for (int sweep = 0; sweep < 20 && m > 1; ++sweep) {
     float off = 0.f, dia = 0.f;
     for (int e = t; e < s * s; e += 256) {
       const int i = e % s, j = e / s;
@@ -235,8 +257,13 @@ HT_DEV void jacobi_smem(float (*A)[SMAX + 1], float (*V)[SMAX + 1], int s, int *
     }
     const float dias = red[0];
     __syncthreads();
-    // FP32 rounding leaves off-diagonal mass near s * eps^2 * diag mass
-    if (offs <= 1e-11f * dias || offs == 0.f) break;
+    // FP32 rounding leaves off-diagonal mass near s * eps^2 * diag mass.  The
+    // Frobenius test can pass with one entry still large relative to a small
+    // eigenvalue, so two more sweeps follow (Jacobi converges quadratically).
+    if (offs == 0.f) break;
+    if (extra < 0 && offs <= 1e-11f * dias) extra = 2;
+    if (extra == 0) break;
+    if (extra > 0) --extra;
     for (int round = 0; round < m - 1; ++round) {
       if (t < m / 2) {
         // position 0 is fixed, positions 1..m-1 rotate by one each round
@@ -407,10 +434,7 @@ __global__ void __launch_bounds__(kThreads) eig_step_kernel(const EigBatch probs
   if (!arrive(&P.cnt[g], gsize, &s_flag)) return;
   for (int e = t; e < E; e += kThreads) {
     Acc2 acc = {0.f, 0.f};
-    for (int r = g * GROUP; r < g * GROUP + gsize; ++r) {
-      const float *p = P.part + (static_cast<long long>(r) * ESMAX + e) * 2;
-      acc2_add(acc, __ldcg(p), __ldcg(p + 1));
-    }
+    sum_pairs(acc, P.part, g * GROUP, gsize, e);
     float *d = P.gpart + (static_cast<long long>(g) * ESMAX + e) * 2;
     d[0] = acc.s;
     d[1] = acc.c;
@@ -418,10 +442,7 @@ __global__ void __launch_bounds__(kThreads) eig_step_kernel(const EigBatch probs
   if (!arrive(&P.cnt[P.ngroups], P.ngroups, &s_flag)) return;
   for (int e = t; e < E; e += kThreads) {
     Acc2 acc = {0.f, 0.f};
-    for (int gg = 0; gg < P.ngroups; ++gg) {
-      const float *p = P.gpart + (static_cast<long long>(gg) * ESMAX + e) * 2;
-      acc2_add(acc, __ldcg(p), __ldcg(p + 1));
-    }
+    sum_pairs(acc, P.gpart, 0, P.ngroups, e);
     Sd[e] = static_cast<double>(acc.s) + static_cast<double>(acc.c);
   }
   __syncthreads();
@@ -497,13 +518,25 @@ __global__ void __launch_bounds__(kThreads) eig_final_kernel(const EigBatch prob
     P.colss[static_cast<long long>(rb) * SMAX + j] = acc;
   }
   if (!arrive(&P.cnt[P.ngroups], P.nrb, &s_flag)) return;
+  __shared__ float colmax[SMAX];
+  if (t < SMAX) {
+    float acc = 0.f;
+    if (t < K) {
+      for (int r0 = 0; r0 < P.nrb; r0 += 8) {
+        float v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          v[q] = (r0 + q < P.nrb) ? __ldcg(P.colss + static_cast<long long>(r0 + q) * SMAX + t) : 0.f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc += v[q];
+      }
+    }
+    colmax[t] = sqrtf(acc);
+  }
+  __syncthreads();
   if (t == 0) {
     float m = 0.f;
-    for (int j = 0; j < K; ++j) {
-      float acc = 0.f;
-      for (int r = 0; r < P.nrb; ++r) acc += __ldcg(P.colss + static_cast<long long>(r) * SMAX + j);
-      m = fmaxf(m, sqrtf(acc));
-    }
+    for (int j = 0; j < K; ++j) m = fmaxf(m, colmax[j]);
     const float th = P.theta[0];
     P.resid[0] = th > 0.f ? m / th : m;
   }

@@ -28,7 +28,57 @@ struct SParams {
   float *out;
   long long ld_out;
   int a_rows, b_rows;   // operand row extents (for bounds)
+  int a_vec, b_vec;     // 0 scalar, 1 float4 along k, 2 float4 along rows
 };
+
+// Vector load geometry of an operand tile of ROWS x BKS: returns per-thread
+// float4 loads; K-contiguous tiles (vec 1) or row-contiguous tiles (vec 2).
+template <int ROWS>
+HT_DEV void load_vec(int vec, int kind, const float *base, long long d0, long long d1, long long k0, int row0, int z,
+                     int rows_total, float *out) {
+  constexpr int NV = ROWS * BKS / 4 / 256;   // float4 per thread
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    const int idx = threadIdx.x + 256 * i;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (vec == 1) {
+      const int row = row0 + (idx >> 2), kq = (idx & 3) * 4;
+      if (row < rows_total) {
+        const float *ptr;
+        if (kind == OP_KM3) {
+          const long long r0 = k0 / d0, l0 = k0 - r0 * d0;
+          ptr = base + l0 + d0 * (static_cast<long long>(row) + d1 * r0) + kq;
+        } else {
+          ptr = base + k0 + d0 * d1 * static_cast<long long>(row) + kq;
+        }
+        v = __ldg(reinterpret_cast<const float4 *>(ptr));
+      }
+    } else {
+      const int kk = idx / (ROWS / 4), rq = (idx % (ROWS / 4)) * 4;
+      const int row = row0 + rq;
+      if (row < rows_total)
+        v = __ldg(reinterpret_cast<const float4 *>(base + row + d0 * (k0 + kk + d1 * static_cast<long long>(z))));
+    }
+    out[4 * i] = v.x; out[4 * i + 1] = v.y; out[4 * i + 2] = v.z; out[4 * i + 3] = v.w;
+  }
+}
+
+template <int ROWS>
+HT_DEV void store_vec(int vec, const float *in, float (*S)[ROWS + 4]) {
+  constexpr int NV = ROWS * BKS / 4 / 256;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    const int idx = threadIdx.x + 256 * i;
+    if (vec == 1) {
+      const int row = idx >> 2, kq = (idx & 3) * 4;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) S[kq + c][row] = in[4 * i + c];
+    } else {
+      const int kk = idx / (ROWS / 4), rq = (idx % (ROWS / 4)) * 4;
+      *reinterpret_cast<float4 *>(&S[kk][rq]) = make_float4(in[4 * i], in[4 * i + 1], in[4 * i + 2], in[4 * i + 3]);
+    }
+  }
+}
 
 HT_DEV const float *op_ptr(int kind, const float *p, long long d0, long long d1, long long row, long long k,
                            int z) {
@@ -64,7 +114,14 @@ __global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p, const T
   // 16-wide K step across two outer indices: decompose k once per step.
   const bool a_fast = p.a_kind == OP_KM3 && (p.a0 % BKS) == 0;
   const bool b_fast = p.b_kind == OP_KM3 && (p.b0 % BKS) == 0;
+  // per k-tile: vector loads when the operand allows them and the tile is full
+  bool a_v = false, b_v = false;
   auto load_tiles = [&](long long k0) {
+    a_v = p.a_vec != 0 && k0 + BKS <= kend;
+    b_v = p.b_vec != 0 && k0 + BKS <= kend;
+    if (a_v) load_vec<BM>(p.a_vec, p.a_kind, p.a, p.a0, p.a1, k0, tile.a_row, tile.a_z, p.a_rows, ra);
+    if (b_v) load_vec<BN>(p.b_vec, p.b_kind, p.b, p.b0, p.b1, k0, tile.b_row, 0, p.b_rows, rb);
+    if (a_v && b_v) return;
     const float *abase = nullptr, *bbase = nullptr;
     if (a_fast) {
       const long long r0 = k0 / p.a0, l0 = k0 - r0 * p.a0;
@@ -76,6 +133,7 @@ __global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p, const T
     }
 #pragma unroll
     for (int i = 0; i < A_PER; ++i) {
+      if (a_v) break;
       const int e = tid + 256 * i;
       const int kk = a_kfast ? (e % BKS) : (e / BM);
       const int rr = a_kfast ? (e / BKS) : (e % BM);
@@ -88,6 +146,7 @@ __global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p, const T
     }
 #pragma unroll
     for (int i = 0; i < B_PER; ++i) {
+      if (b_v) break;
       const int e = tid + 256 * i;
       const int kk = b_kfast ? (e % BKS) : (e / BN);
       const int rr = b_kfast ? (e / BKS) : (e % BN);
@@ -100,8 +159,12 @@ __global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p, const T
     }
   };
   auto store_tiles = [&](int buf) {
+    if (a_v) store_vec<BM>(p.a_vec, ra, As[buf]);
+    if (b_v) store_vec<BN>(p.b_vec, rb, Bs[buf]);
+    if (a_v && b_v) return;
 #pragma unroll
     for (int i = 0; i < A_PER; ++i) {
+      if (a_v) break;
       const int e = tid + 256 * i;
       const int kk = a_kfast ? (e % BKS) : (e / BM);
       const int rr = a_kfast ? (e / BKS) : (e % BM);
@@ -109,6 +172,7 @@ __global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p, const T
     }
 #pragma unroll
     for (int i = 0; i < B_PER; ++i) {
+      if (b_v) break;
       const int e = tid + 256 * i;
       const int kk = b_kfast ? (e % BKS) : (e / BN);
       const int rr = b_kfast ? (e / BKS) : (e % BN);
@@ -184,7 +248,14 @@ __global__ void reduce_partials_kernel(const float *__restrict__ part, const Til
     const Tile tl = gen_tile(gen, t);
     if (row >= tl.valid_rows || col >= tl.valid_cols) continue;
     float s = 0.f;
-    for (int k = 0; k < splits; ++k) s += part[(static_cast<long long>(k) * num_tiles + t) * per_tile + within];
+    for (int k0 = 0; k0 < splits; k0 += 8) {   // 8 loads in flight, summed in order
+      float v[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        v[q] = (k0 + q < splits) ? part[(static_cast<long long>(k0 + q) * num_tiles + t) * per_tile + within] : 0.f;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) s += v[q];
+    }
     const long long gr = tl.out_row + row, gc = tl.out_col + col;
     if (symmetric) {
       if (gc < gr) continue;   // the mirror element is produced by the tile holding (gc, gr)
@@ -228,6 +299,15 @@ cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s) {
   p.ld_out = g.ld_out;
   p.a_rows = rows_of(g.a.kind, g.a.d0, g.a.d1, g.a.d2);
   p.b_rows = rows_of(g.b.kind, g.b.d0, g.b.d1, g.b.d2);
+  auto vec_of = [](const Operand &o) {
+    if ((reinterpret_cast<uintptr_t>(o.ptr) & 15u) != 0) return 0;
+    if (o.kind == OP_KM3 && o.d0 % BKS == 0) return 1;
+    if (o.kind == OP_KM3Q && (o.d0 * o.d1) % 4 == 0) return 1;
+    if (o.kind == OP_MN3 && o.d0 % 4 == 0) return 2;
+    return 0;
+  };
+  p.a_vec = vec_of(g.a);
+  p.b_vec = vec_of(g.b);
   const int grid = g.num_tiles * splits;
   if (bn == 128)
     simt_gemm_kernel<128><<<grid, 256, 0, s>>>(p, g.gen);
