@@ -141,6 +141,76 @@ HT_DEV void apply_factor_row(float *row, const float *Rs, const float *ds, int s
   }
 }
 
+// 16-byte asynchronous global->shared copy; src_bytes < 16 zero-fills the rest.
+HT_DEV void cp_async16(void *smem_dst, const void *gsrc, int src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(smem_dst)), "l"(gsrc), "r"(src_bytes)
+               : "memory");
+}
+HT_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+HT_DEV void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+constexpr int KC = 64;       // k chunk of the G * src product
+constexpr int NSTAGE = 3;    // cp.async pipeline depth
+constexpr int LDK = KC + 4;  // padded row length (keeps float4 alignment)
+
+// Z[i][j] (16 x s, in Zs) = sum_k G[r0+i, k] src[k, j], G symmetric so row
+// r0+i of G is read as column r0+i (contiguous).  Thread t owns rows
+// 4*(t>>6)..+3 of column t&63.  Chunks of KC rows of src stream through a
+// NSTAGE-deep cp.async ring.  Requires n % 4 == 0 and 16-byte aligned bases.
+HT_DEV void gsrc_product_async(const float *G, const float *src, int n, int s, int r0, int rows, float *ring,
+                               float (&acc)[4]) {
+  const int t = threadIdx.x;
+  const int nchunks = (n + KC - 1) / KC;
+  auto issue = [&](int c) {
+    const int kc = c * KC;
+    float *Gd = ring + (c % NSTAGE) * (RB + SMAX) * LDK, *Sd_ = Gd + RB * LDK;
+    // G: RB rows x KC/4 float4 = 256 copies
+    {
+      const int i = t >> 4, k4 = (t & 15) * 4;
+      const int kk = kc + k4;
+      const int bytes = (i < rows && kk < n) ? 4 * min(4, n - kk) : 0;
+      const float *g = G + (bytes ? (static_cast<long long>(kk) + static_cast<long long>(n) * (r0 + i)) : 0);
+      cp_async16(Gd + i * LDK + k4, g, bytes);
+    }
+    // src: SMAX columns x KC/4 float4 = 1024 copies, 4 per thread
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int idx = t + 256 * q;
+      const int j = idx >> 4, k4 = (idx & 15) * 4;
+      const int kk = kc + k4;
+      const int bytes = (j < s && kk < n) ? 4 * min(4, n - kk) : 0;
+      const float *g = src + (bytes ? (static_cast<long long>(kk) + static_cast<long long>(n) * j) : 0);
+      cp_async16(Sd_ + j * LDK + k4, g, bytes);
+    }
+  };
+  for (int c = 0; c < NSTAGE - 1; ++c) {
+    if (c < nchunks) issue(c);
+    cp_async_commit();
+  }
+  const int ig = t >> 6, j = t & 63;
+#pragma unroll
+  for (int c4 = 0; c4 < 4; ++c4) acc[c4] = 0.f;
+  for (int c = 0; c < nchunks; ++c) {
+    if (c + NSTAGE - 1 < nchunks) issue(c + NSTAGE - 1);
+    cp_async_commit();
+    cp_async_wait<NSTAGE - 1>();   // chunk c has landed
+    __syncthreads();
+    const float *Gd = ring + (c % NSTAGE) * (RB + SMAX) * LDK, *Sd_ = Gd + RB * LDK;
+#pragma unroll 4
+    for (int kk = 0; kk < KC; kk += 4) {
+      const float4 q = *reinterpret_cast<const float4 *>(Sd_ + j * LDK + kk);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const float4 g = *reinterpret_cast<const float4 *>(Gd + (4 * ig + r) * LDK + kk);
+        acc[r] = fmaf(g.x, q.x, fmaf(g.y, q.y, fmaf(g.z, q.z, fmaf(g.w, q.w, acc[r]))));
+      }
+    }
+    __syncthreads();   // the stage is refilled NSTAGE-1 chunks later
+  }
+  cp_async_wait<0>();
+}
+
 // Last-block bookkeeping: returns true in exactly one CTA of the group /
 // of the whole problem once every member has published its partial.
 HT_DEV bool arrive(int *counter, int members, int *s_flag) {
@@ -334,10 +404,12 @@ __global__ void __launch_bounds__(kThreads) eig_step_kernel(const EigBatch probs
   float *ds = Rs + SMAX * SMAX;                     // SMAX
   float *Zs = ds + SMAX;                            // RB*SMAX  (rows of the result)
   float *Qr = Zs + RB * SMAX;                       // RB*SMAX  (RR: rows of Q)
-  float *Gs = Qr + RB * SMAX;                       // 64*(RB+1)
-  float *Ss = Gs + 64 * (RB + 1);                   // 64*68 (chunk of src), 16-byte aligned rows
-  double *Sd = reinterpret_cast<double *>(Ss + 64 * 68);   // ESMAX (final reducer)
-  float *Vs = reinterpret_cast<float *>(Sd + ESMAX);       // SMAX*(SMAX+1) (RR Jacobi)
+  float *Gs = Qr + RB * SMAX;                       // 64*(RB+1)   (scalar path)
+  float *Ss = Gs + 64 * (RB + 1);                   // ring of NSTAGE*(RB+SMAX)*LDK floats (async path),
+                                                    // or 64*68 (scalar path); 16-byte aligned
+  // the final reducer's scratch aliases the ring (dead once the product is done)
+  double *Sd = reinterpret_cast<double *>(Ss);              // ESMAX
+  float *Vs = reinterpret_cast<float *>(Sd + ESMAX);        // SMAX*(SMAX+1) (RR Jacobi)
   __shared__ int s_flag;
   __shared__ int order[SMAX];
   const int n = P.n, s = P.s, t = threadIdx.x;
@@ -358,36 +430,48 @@ __global__ void __launch_bounds__(kThreads) eig_step_kernel(const EigBatch probs
     else Qr[i * SMAX + j] = v;
   }
   if (a.mode != STEP_APPLY) {
-    // Z = G[rows, :] src   (G symmetric: read G[k, rows] contiguously in k)
-    const int i = t >> 4, cg = t & 15;
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int kc = 0; kc < n; kc += 64) {
-      __syncthreads();
-      for (int e = t; e < 64 * RB; e += kThreads) {
-        const int kk = e % 64, ii = e / 64;
-        Gs[kk * (RB + 1) + ii] =
-            (kc + kk < n && ii < rows) ? P.G[(kc + kk) + static_cast<long long>(n) * (r0 + ii)] : 0.f;
-      }
-      for (int e = t; e < 64 * SMAX; e += kThreads) {
-        const int kk = e % 64, j = e / 64;
-        Ss[kk * 68 + j] = (kc + kk < n && j < s) ? src[(kc + kk) + static_cast<long long>(n) * j] : 0.f;
-      }
-      __syncthreads();
-#pragma unroll 8
-      for (int kk = 0; kk < 64; ++kk) {
-        const float g = Gs[kk * (RB + 1) + i];
-        const float4 q4 = *reinterpret_cast<const float4 *>(&Ss[kk * 68 + 4 * cg]);
-        acc[0] = fmaf(g, q4.x, acc[0]);
-        acc[1] = fmaf(g, q4.y, acc[1]);
-        acc[2] = fmaf(g, q4.z, acc[2]);
-        acc[3] = fmaf(g, q4.w, acc[3]);
-      }
-    }
     const float mu = (a.mode == STEP_ITER) ? P.mu[0] * a.mu_scale : 0.f;
+    const bool vec = (n % 4 == 0) && ((reinterpret_cast<uintptr_t>(P.G) | reinterpret_cast<uintptr_t>(src)) & 15u) == 0;
+    if (vec) {
+      float acc[4];
+      gsrc_product_async(P.G, src, n, s, r0, rows, Ss, acc);
+      const int ig = t >> 6, j = t & 63;
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const int j = 4 * cg + c;
-      Zs[i * SMAX + j] = (i < rows && j < s) ? acc[c] + mu * Qr[i * SMAX + j] : 0.f;
+      for (int r = 0; r < 4; ++r) {
+        const int i = 4 * ig + r;
+        Zs[i * SMAX + j] = (i < rows && j < s) ? acc[r] + mu * Qr[i * SMAX + j] : 0.f;
+      }
+    } else {
+      // Z = G[rows, :] src, scalar loads (unaligned shapes)
+      const int i = t >> 4, cg = t & 15;
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int kc = 0; kc < n; kc += 64) {
+        __syncthreads();
+        for (int e = t; e < 64 * RB; e += kThreads) {
+          const int kk = e % 64, ii = e / 64;
+          Gs[kk * (RB + 1) + ii] =
+              (kc + kk < n && ii < rows) ? P.G[(kc + kk) + static_cast<long long>(n) * (r0 + ii)] : 0.f;
+        }
+        for (int e = t; e < 64 * SMAX; e += kThreads) {
+          const int kk = e % 64, jj = e / 64;
+          Ss[kk * 68 + jj] = (kc + kk < n && jj < s) ? src[(kc + kk) + static_cast<long long>(n) * jj] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < 64; ++kk) {
+          const float g = Gs[kk * (RB + 1) + i];
+          const float4 q4 = *reinterpret_cast<const float4 *>(&Ss[kk * 68 + 4 * cg]);
+          acc[0] = fmaf(g, q4.x, acc[0]);
+          acc[1] = fmaf(g, q4.y, acc[1]);
+          acc[2] = fmaf(g, q4.z, acc[2]);
+          acc[3] = fmaf(g, q4.w, acc[3]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int j = 4 * cg + c;
+        Zs[i * SMAX + j] = (i < rows && j < s) ? acc[c] + mu * Qr[i * SMAX + j] : 0.f;
+      }
     }
   }
   __syncthreads();
@@ -419,14 +503,21 @@ __global__ void __launch_bounds__(kThreads) eig_step_kernel(const EigBatch probs
   // partial of the s x s Gram (ITER/APPLY: Y^T Y, RR: Q^T Y), packed upper triangle
   const int E = s * (s + 1) / 2;
   const float *L = (a.mode == STEP_RR) ? Qr : Zs;
-  for (int e = t; e < E; e += kThreads) {
-    int i, j;
-    tri_index(e, i, j);
-    Acc2 acc = {0.f, 0.f};
-    for (int r = 0; r < rows; ++r) acc2_add_prod(acc, L[r * SMAX + i], Zs[r * SMAX + j]);
-    float *d = P.part + (static_cast<long long>(rb) * ESMAX + e) * 2;
-    d[0] = acc.s;
-    d[1] = acc.c;
+  {
+    const int j = t & 63, ib = t >> 6;   // column j, rows ib, ib+4, ... <= j
+    if (j < s) {
+      float zc[RB];
+#pragma unroll
+      for (int r = 0; r < RB; ++r) zc[r] = Zs[r * SMAX + j];
+      for (int i = ib; i <= j; i += 4) {
+        Acc2 acc = {0.f, 0.f};
+#pragma unroll
+        for (int r = 0; r < RB; ++r) acc2_add_prod(acc, L[r * SMAX + i], zc[r]);   // rows >= `rows` are zero
+        float *d = P.part + (static_cast<long long>(rb) * ESMAX + j * (j + 1) / 2 + i) * 2;
+        d[0] = acc.s;
+        d[1] = acc.c;
+      }
+    }
   }
   // two-level deterministic reduction by the last CTAs to arrive
   const int g = rb / GROUP;
@@ -639,8 +730,11 @@ __global__ void __launch_bounds__(256) svd_from_gram_kernel(const float *GW, int
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-constexpr size_t kStepSmem = sizeof(float) * (SMAX * SMAX + SMAX + 2 * RB * SMAX + 64 * (RB + 1) + 64 * 68) +
-                             sizeof(double) * ESMAX + sizeof(float) * SMAX * (SMAX + 1) + 64;
+constexpr size_t kRingFloats = NSTAGE * (RB + SMAX) * LDK;
+constexpr size_t kReducerFloats = 2 * ESMAX + SMAX * (SMAX + 1);
+constexpr size_t kStepSmem = sizeof(float) * (SMAX * SMAX + SMAX + 2 * RB * SMAX + 64 * (RB + 1) +
+                                              (kRingFloats > kReducerFloats ? kRingFloats : kReducerFloats)) +
+                             64;
 
 }  // namespace
 
