@@ -233,6 +233,7 @@ struct GemmReq {
   long long ld_out = 0;
   bool symmetric = false;
   bool allow_split = true;
+  bool fold = false;                // tcgen05 only: b16 is a high/low split (GemmArgs::fold)
 };
 
 // D = A B^T over the tiles: tcgen05 on the BF16 operands when the context
@@ -282,6 +283,7 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
   g.out = partial ? part : q.out;
   g.ld_out = q.ld_out;
   g.err = c.err;
+  g.fold = (use_tc && q.fold) ? 1 : 0;
   if (use_tc) {
     HT_CUDA(tc_gemm_launch(g, bn, c.st));
     c.path |= 1;
@@ -316,8 +318,11 @@ ht_status_t gram(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x
 }
 
 // Z ((L*R) x k, column-major) = contraction of the middle index of view v with W (v.N x k)
+// fold_h > 0: W16 is the split_bf16 form of W32 (v.N x 2*fold_h, high part in
+// columns [0, k), low part in [fold_h, fold_h + k)), so the tcgen05 product
+// carries W to about 16 significant bits instead of BF16's 8.
 ht_status_t mode_product(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x16, const float *W32,
-                         const __nv_bfloat16 *W16, int k, float *Z) {
+                         const __nv_bfloat16 *W16, int k, float *Z, int fold_h = 0) {
   GemmReq q;
   auto opA = [&](const void *x) {
     Operand o;
@@ -329,15 +334,16 @@ ht_status_t mode_product(Ctx &c, const View &v, const float *x32, const __nv_bfl
     }
     return o;
   };
-  auto opB = [&](const void *w) {
+  auto opB = [&](const void *w, int cols) {
     Operand o;
-    o.ptr = w; o.kind = OP_KM3; o.d0 = v.N; o.d1 = k; o.d2 = 1;
+    o.ptr = w; o.kind = OP_KM3; o.d0 = v.N; o.d1 = cols; o.d2 = 1;
     return o;
   };
-  q.a32 = opA(x32); q.b32 = opB(W32);
-  if (x16 && W16) { q.a16 = opA(x16); q.b16 = opB(W16); }
+  q.a32 = opA(x32); q.b32 = opB(W32, k);
+  if (x16 && W16) { q.a16 = opA(x16); q.b16 = opB(W16, fold_h > 0 ? 2 * fold_h : k); }
   else q.a16.ptr = q.b16.ptr = nullptr;
-  q.bn_tc = 64; q.bn_simt = 64;
+  q.bn_tc = fold_h > 0 ? 2 * fold_h : 64; q.bn_simt = 64;
+  q.fold = fold_h > 0;
   if (v.L == 1) {
     q.tiles_kind = TILES_ROWS; q.t_rows = v.R; q.t_cols = k;
   } else {
@@ -566,14 +572,20 @@ ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const 
     if (!C || !WG || !M || !Bkt || !Broot || !Bt) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (transfer)");
     const size_t mark = c.ar.off;
     float *Z = c.ar.take<float>(static_cast<size_t>(zrows) * P.kt);
-    __nv_bfloat16 *V16 = c.tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(dims[P.mc]) * P.kt + 64) : nullptr;
+    // V enters the BF16 product as high + low BF16 parts (one MMA tile of
+    // 2*fold_h columns): rounding V itself to BF16 would tilt every column of
+    // Z = X_(t) V by ~2^-9 of X's energy, which dominates the error of nearly
+    // exact low-rank inputs.
+    const int fold_h = P.kt <= 32 ? 32 : 64;
+    __nv_bfloat16 *V16 =
+        c.tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(dims[P.mc]) * 2 * fold_h + 64) : nullptr;
     if (!Z || (c.tc && !V16)) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (core pass)");
     // 3. core pass: Z = X_(t) V, V = leading kt columns of the complementary leaf's Ritz block
     if (V16 && !c.dry()) {
-      HT_CUDA(f32_to_bf16_launch(ec.U, V16, static_cast<long long>(dims[P.mc]) * P.kt, c.st));
+      HT_CUDA(split_bf16_launch(ec.U, dims[P.mc], P.kt, fold_h, V16, c.st));
       ++c.launches;
     }
-    HT_TRY(mode_product(c, vc, x32, x16, ec.U, V16, P.kt, Z));
+    HT_TRY(mode_product(c, vc, x32, x16, ec.U, V16, P.kt, Z, fold_h));
     tl.mark(c.st);
     // 4. transfer tensors
     HT_TRY(core_contract(c, Z, static_cast<int>(dims[P.mp]), static_cast<int>(dims[P.mq]), P.kt, ep[P.mp].U, P.kp,

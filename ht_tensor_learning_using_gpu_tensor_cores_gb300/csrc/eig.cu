@@ -293,9 +293,8 @@ HT_DEV void factor_and_store(const double *Sd, int s, float shift, float *A, flo
 // s/2 disjoint pairs in parallel.  On return A is diagonal to FP32 rounding,
 // V holds the eigenvectors and order[] the indices by descending eigenvalue.
 HT_DEV void jacobi_smem(float (*A)[SMAX + 1], float (*V)[SMAX + 1], int s, int *order) {
-  __shared__ float cs[SMAX / 2], sn[SMAX / 2];
+  __shared__ float rh[SMAX / 2], sn[SMAX / 2];
   __shared__ int pp[SMAX / 2], qq[SMAX / 2];
-  __shared__ float red[256];
   const int t = threadIdx.x;
   const int m = (s + 1) & ~1;   // even number of players (a dummy index when s is odd)
   for (int e = t; e < SMAX * SMAX; e += 256) {
@@ -303,81 +302,79 @@ HT_DEV void jacobi_smem(float (*A)[SMAX + 1], float (*V)[SMAX + 1], int s, int *
     V[i][j] = (i == j) ? 1.f : 0.f;
   }
   __syncthreads();
-  int extra = -1;   // sweeps still to run once the Frobenius criterion is met
+  // A pair rotates while its coupling is above 2.4e-7 (two FP32 units of
+  // rounding) relative to sqrt(a_pp a_qq), the test that keeps small
+  // eigenvalues' vectors accurate (Demmel and Veselic, "Jacobi's method is
+  // more accurate than QR", 1992).  The rotated pair's new diagonal is
+  // formed as a_pp - t a_pq, a_qq + t a_pq and its coupling set to exactly
+  // zero (Rutishauser's update), so rounding does not regenerate it and the
+  // test terminates even between null directions.  Sweeps stop after one
+  // that rotated nothing.  Rotations are applied as x - s (y + rho x),
+  // y + s (x - rho y) with rho = s / (1 + c): for the many tiny late
+  // rotations c rounds to 1, and the plain c x - s y form would then grow every
+  // column of V by s^2/2 per rotation (a 1e-5 loss of orthogonality after ten
+  // sweeps); this form carries that second-order term explicitly.
   for (int sweep = 0; sweep < 20 && m > 1; ++sweep) {
-    float off = 0.f, dia = 0.f;
-    for (int e = t; e < s * s; e += 256) {
-      const int i = e % s, j = e / s;
-      const float v = A[i][j];
-      if (i == j) dia += v * v; else off += v * v;
-    }
-    red[t] = off;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-      if (t < w) red[t] += red[t + w];
-      __syncthreads();
-    }
-    const float offs = red[0];
-    __syncthreads();
-    red[t] = dia;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-      if (t < w) red[t] += red[t + w];
-      __syncthreads();
-    }
-    const float dias = red[0];
-    __syncthreads();
-    // FP32 rounding leaves off-diagonal mass near s * eps^2 * diag mass.  The
-    // Frobenius test can pass with one entry still large relative to a small
-    // eigenvalue, so two more sweeps follow (Jacobi converges quadratically).
-    if (offs == 0.f) break;
-    if (extra < 0 && offs <= 1e-11f * dias) extra = 2;
-    if (extra == 0) break;
-    if (extra > 0) --extra;
+    int rotated = 0;
     for (int round = 0; round < m - 1; ++round) {
+      int did = 0, pme = 0, qme = 0;
+      float tt = 0.f, app = 0.f, aqq = 0.f;
       if (t < m / 2) {
         // position 0 is fixed, positions 1..m-1 rotate by one each round
         const int pa = t, pb = m - 1 - t;
         int p = pa == 0 ? 0 : 1 + ((pa - 1 + round) % (m - 1));
         int q = pb == 0 ? 0 : 1 + ((pb - 1 + round) % (m - 1));
         if (p > q) { const int tmp = p; p = q; q = tmp; }
-        float c = 1.f, sv = 0.f;
+        float rho = 0.f, sv = 0.f;
         if (q < s) {
           const float apq = A[p][q];
-          if (fabsf(apq) > 1e-30f && fabsf(apq) > 1e-9f * sqrtf(fabsf(A[p][p] * A[q][q]))) {
+          if (fabsf(apq) > 1e-30f && fabsf(apq) > 2.4e-7f * sqrtf(fabsf(A[p][p] * A[q][q]))) {
             const float tau = (A[q][q] - A[p][p]) / (2.f * apq);
-            const float tt = (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(1.f + tau * tau));
-            c = rsqrtf(1.f + tt * tt);
+            tt = (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(1.f + tau * tau));
+            const float c = 1.f / sqrtf(1.f + tt * tt);
             sv = tt * c;
+            rho = sv / (1.f + c);
+            app = A[p][p] - tt * apq;
+            aqq = A[q][q] + tt * apq;
+            did = 1;
           }
         }
-        pp[t] = p; qq[t] = q; cs[t] = c; sn[t] = sv;
+        pp[t] = p; qq[t] = q; rh[t] = rho; sn[t] = sv;
+        pme = p; qme = q;
       }
-      __syncthreads();
+      rotated |= __syncthreads_or(did);
       for (int e = t; e < (m / 2) * s; e += 256) {   // rows: A <- J^T A
         const int pr = e / s, j = e % s;
         const int p = pp[pr], q = qq[pr];
         if (q >= s) continue;
-        const float c = cs[pr], sv = sn[pr];
+        const float sv = sn[pr], rho = rh[pr];
         const float ap = A[p][j], aq = A[q][j];
-        A[p][j] = c * ap - sv * aq;
-        A[q][j] = sv * ap + c * aq;
+        A[p][j] = ap - sv * (aq + rho * ap);
+        A[q][j] = aq + sv * (ap - rho * aq);
       }
       __syncthreads();
       for (int e = t; e < (m / 2) * s; e += 256) {   // columns: A <- A J, V <- V J
         const int pr = e / s, i = e % s;
         const int p = pp[pr], q = qq[pr];
         if (q >= s) continue;
-        const float c = cs[pr], sv = sn[pr];
+        const float sv = sn[pr], rho = rh[pr];
         const float ap = A[i][p], aq = A[i][q];
-        A[i][p] = c * ap - sv * aq;
-        A[i][q] = sv * ap + c * aq;
+        A[i][p] = ap - sv * (aq + rho * ap);
+        A[i][q] = aq + sv * (ap - rho * aq);
         const float vp = V[i][p], vq = V[i][q];
-        V[i][p] = c * vp - sv * vq;
-        V[i][q] = sv * vp + c * vq;
+        V[i][p] = vp - sv * (vq + rho * vp);
+        V[i][q] = vq + sv * (vp - rho * vq);
+      }
+      __syncthreads();
+      if (did) {
+        A[pme][pme] = app;
+        A[qme][qme] = aqq;
+        A[pme][qme] = 0.f;
+        A[qme][pme] = 0.f;
       }
       __syncthreads();
     }
+    if (!rotated) break;
   }
   for (int j = t; j < s; j += 256) {   // rank by counting: descending eigenvalues
     const float dj = A[j][j];

@@ -68,6 +68,10 @@ struct GemmArgs {
   float *out;            // partial buffer [splits][num_tiles][BM][BN] or column-major output
   long long ld_out;
   int *err;              // device error word
+  // tcgen05 path, column-major output only: the B operand holds two halves of
+  // BN/2 rows each (a BF16 matrix split into high and low parts) and the
+  // epilogue writes column j as acc[j] + acc[j + BN/2].
+  int fold = 0;
 };
 
 // tcgen05 path (BF16 operands), BM = 128, BN in {64, 128, 256}.
@@ -95,6 +99,9 @@ cudaError_t convert_bf16_launch(const float *x, __nv_bfloat16 *xb, long long n, 
                                 int num_partials, cudaStream_t s);
 cudaError_t sumsq_launch(const float *x, long long n, double *partials, int num_partials, cudaStream_t s);
 cudaError_t f32_to_bf16_launch(const float *x, __nv_bfloat16 *y, long long n, cudaStream_t s);
+// W (rows x k, column-major FP32) -> Y (rows x 2h BF16): columns [0, k) the
+// BF16 rounding hi(W), columns [h, h + k) the rounding of W - hi(W), the rest 0.
+cudaError_t split_bf16_launch(const float *W, long long rows, int k, int h, __nv_bfloat16 *Y, cudaStream_t s);
 cudaError_t sumsq_finish_launch(const double *partials, int n, double *out, cudaStream_t s);
 // C (m x n) = A^T B with A (K x m), B (K x n), column-major, compensated FP32.
 cudaError_t gemm_tn_small_launch(const float *A, int lda, const float *B, int ldb, float *C, int ldc, int m, int n,

@@ -65,6 +65,23 @@ __global__ void f32_to_bf16_kernel(const float *__restrict__ x, __nv_bfloat16 *_
   for (long long i = blockIdx.x * 256ll + threadIdx.x; i < n; i += gridDim.x * 256ll) y[i] = __float2bfloat16_rn(x[i]);
 }
 
+__global__ void split_bf16_kernel(const float *__restrict__ W, long long rows, int k, int h,
+                                  __nv_bfloat16 *__restrict__ Y) {
+  const long long total = rows * 2 * h;
+  for (long long i = blockIdx.x * 256ll + threadIdx.x; i < total; i += gridDim.x * 256ll) {
+    const long long r = i % rows;
+    const int col = static_cast<int>(i / rows);
+    const int j = col < h ? col : col - h;
+    float v = 0.f;
+    if (j < k) {
+      const float w = W[r + rows * j];
+      const float hi = __bfloat162float(__float2bfloat16_rn(w));
+      v = col < h ? hi : w - hi;   // w - hi is exact in FP32
+    }
+    Y[i] = __float2bfloat16_rn(v);
+  }
+}
+
 __global__ void sumsq_finish_kernel(const double *partials, int n, double *out) {
   __shared__ double red[256];
   double s = 0.0;
@@ -276,6 +293,11 @@ cudaError_t sumsq_launch(const float *x, long long n, double *partials, int num_
 
 cudaError_t f32_to_bf16_launch(const float *x, __nv_bfloat16 *y, long long n, cudaStream_t s) {
   f32_to_bf16_kernel<<<grid_for(n), 256, 0, s>>>(x, y, n);
+  return cudaGetLastError();
+}
+
+cudaError_t split_bf16_launch(const float *W, long long rows, int k, int h, __nv_bfloat16 *Y, cudaStream_t s) {
+  split_bf16_kernel<<<grid_for(rows * 2 * h), 256, 0, s>>>(W, rows, k, h, Y);
   return cudaGetLastError();
 }
 

@@ -51,6 +51,7 @@ struct KParams {
   float *out;
   long long ld_out;
   int *err;
+  int fold;
 };
 
 // Issue the TMA loads of one operand tile (ROWS x 64 K) for k-block kb.
@@ -173,12 +174,21 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (!ok) report_error(p.err, kErrTimeout);
     tc_fence_after();
     const bool have = (nk > 0) && ok;
+    const int cols = p.fold ? BN / 2 : BN;
 #pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 32) {
+    for (int c0 = 0; c0 < cols; c0 += 32) {
       float v[32];
       if (have) {
-        tmem_ld_32x32b_x32(tmem + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(c0), v);
+        const uint32_t lane_base = tmem + (static_cast<uint32_t>(q * 32) << 16);
+        tmem_ld_32x32b_x32(lane_base + static_cast<uint32_t>(c0), v);
         tmem_ld_wait();
+        if (p.fold) {   // low half of the split B operand: add its product
+          float w[32];
+          tmem_ld_32x32b_x32(lane_base + static_cast<uint32_t>(c0 + BN / 2), w);
+          tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v[j] += w[j];
+        }
       } else {
 #pragma unroll
         for (int j = 0; j < 32; ++j) v[j] = 0.f;
@@ -286,6 +296,7 @@ cudaError_t launch_bn(const GemmArgs &g, cudaStream_t s) {
   p.out = g.out;
   p.ld_out = g.ld_out;
   p.err = g.err;
+  p.fold = (g.fold && g.out_mode == OUT_COLMAJOR) ? 1 : 0;
   cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(C::SMEM));
   if (e != cudaSuccess) return e;
   tc_gemm_kernel<BN><<<g.num_tiles * splits, kThreads, C::SMEM, s>>>(ma, mb, p, g.gen);
