@@ -23,7 +23,7 @@ FLAG_COMPUTE_ERROR, FLAG_SYNC_TIMING = 1, 2
 EXPORTED = ["ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
             "ht_decompose", "ht_reconstruct_error", "ht_workspace_size", "ht_release_workspace",
             "ht_status_string", "ht_last_error", "ht_kernel_launch_count", "htd", "htd4",
-            "ht_mode_gram", "ht_mode_product", "ht_corange_product"]
+            "ht_mode_gram", "ht_mode_product", "ht_corange_product", "ht_mode_gram_noalloc"]
 
 
 class HtTree(Structure):
@@ -85,9 +85,10 @@ def lib():
     L.ht_mode_gram.argtypes = [c_void_p, POINTER(c_long), c_int, c_int, c_int, c_int, c_void_p, c_void_p]
     L.ht_mode_product.argtypes = [c_void_p, POINTER(c_long), c_int, c_int, c_int, c_void_p, c_int, c_int, c_void_p,
                                   c_void_p]
+    L.ht_mode_gram_noalloc.argtypes = [c_void_p, POINTER(c_long), c_int, c_int, c_int, c_void_p, c_void_p]
     L.ht_corange_product.argtypes = [c_void_p, POINTER(c_long), c_int, c_int, c_int, c_void_p, c_int, c_int,
                                      c_void_p, c_void_p]
-    for name in ("ht_mode_gram", "ht_mode_product", "ht_corange_product", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
+    for name in ("ht_mode_gram", "ht_mode_gram_noalloc", "ht_mode_product", "ht_corange_product", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
                  "ht_decompose", "ht_reconstruct_error", "ht_workspace_size", "ht_release_workspace"):
         getattr(L, name).restype = c_int
     _lib = L

@@ -1158,6 +1158,96 @@ ht_status_t ht_corange_product(const float *x, const long *dims, int order, int 
   return unfolding_op(2, x, dims, order, lo, hi, Q, k, precision, Z, stream);
 }
 
+}  // extern "C"
+
+// ------------------------------------------------ allocation-free Gram entry
+// Scratch of ht_mode_gram_noalloc: the split-K partial tiles of the FP32 Gram.
+// A static device array, so it exists on every device that loads this module
+// and is never allocated or freed by the library.
+__device__ __align__(256) float g_noalloc_scratch[HT_NOALLOC_SCRATCH_BYTES / sizeof(float)];
+
+namespace {
+
+std::mutex g_noalloc_mutex;
+float *g_noalloc_ptr[64];   // device address of g_noalloc_scratch, per device
+
+// The host-side symbol g_noalloc_scratch is not a device address; look the
+// real address up once per device, with that device current.
+ht_status_t noalloc_scratch(float **out) {
+  int dev = 0;
+  HT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(HT_ERR_INVALID_ARG, "device index out of range");
+  std::lock_guard<std::mutex> lk(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      return fail(HT_ERR_CUDA, std::string("ht_mode_gram_noalloc: cudaGetSymbolAddress failed: ") +
+                                   cudaGetErrorString(e));
+    }
+    g_noalloc_ptr[dev] = static_cast<float *>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return HT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ht_status_t ht_mode_gram_noalloc(const float *x, const long *dims, int order, int lo, int hi, float *G,
+                                 void *stream) {
+  if (!x || !dims || !G) return fail(HT_ERR_INVALID_ARG, "NULL argument");
+  if (order < 1 || order > HT_MAX_ORDER) return fail(HT_ERR_INVALID_ARG, "order must be 1..4");
+  if (lo < 0 || hi < lo || hi >= order) return fail(HT_ERR_INVALID_ARG, "bad mode group");
+  for (int m = 0; m < order; ++m)
+    if (dims[m] < 1) return fail(HT_ERR_INVALID_ARG, "dims must be positive");
+  const View v = view_of_group(dims, order, lo, hi);
+  if (v.N > HT_NOALLOC_MAX_GRAM)
+    return fail(HT_ERR_UNSUPPORTED, "ht_mode_gram_noalloc: Gram size " + std::to_string(v.N) +
+                                        " is above the maximum " + std::to_string(HT_NOALLOC_MAX_GRAM) +
+                                        " that its fixed scratch holds; use ht_mode_gram");
+  HT_TRY(check_device());
+  if (!is_device_ptr(x) || !is_device_ptr(G))
+    return fail(HT_ERR_INVALID_ARG, "ht_mode_gram_noalloc: x and G must be device memory");
+  float *scratch = nullptr;
+  HT_TRY(noalloc_scratch(&scratch));
+  const int bn = v.N > 64 ? 128 : 64;
+  TileGen gen;
+  if (!make_gram_gen(v.N, bn, &gen)) return fail(HT_ERR_UNSUPPORTED, "Gram too large");
+  const int nt = gen.count;
+  const long long tile_floats = 128ll * bn;
+  const long long cap_splits = static_cast<long long>(HT_NOALLOC_SCRATCH_BYTES / sizeof(float)) / (tile_floats * nt);
+  if (cap_splits < 1) return fail(HT_ERR_UNSUPPORTED, "ht_mode_gram_noalloc: scratch too small");
+  // split K as the allocating path does, then clip to what the scratch holds
+  int splits = nt < sm_count() ? std::max(1, sm_count() / nt) : 1;
+  GemmArgs g;
+  g.a = g.b = gram_operand(v, x);
+  const long kt = simt_k_total(g.a);
+  long per = (kt + splits - 1) / splits;
+  per = std::max<long>((per + 15) / 16 * 16, 256);
+  splits = static_cast<int>(std::max<long>(1, (kt + per - 1) / per));
+  if (splits > cap_splits) {
+    splits = static_cast<int>(cap_splits);
+    per = (kt + splits - 1) / splits;
+    per = (per + 15) / 16 * 16;
+    splits = static_cast<int>(std::max<long>(1, (kt + per - 1) / per));
+  }
+  g.gen = gen;
+  g.num_tiles = nt;
+  g.splits = splits;
+  g.out_mode = OUT_PARTIAL;
+  g.out = scratch;
+  g.ld_out = v.N;
+  g.err = nullptr;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  HT_CUDA(simt_gemm_launch(g, bn, st));
+  HT_CUDA(reduce_partials_launch(scratch, gen, splits, bn, G, v.N, 1, st));
+  g_launches += 2;
+  return HT_OK;
+}
+
 const char *ht_status_string(ht_status_t s) {
   switch (s) {
     case HT_OK: return "ok";

@@ -146,6 +146,33 @@ ht_status_t ht_mode_product(const float *x, const long *dims, int order, int lo,
 ht_status_t ht_corange_product(const float *x, const long *dims, int order, int lo, int hi, const float *Q, int k,
                                int precision, float *Z, void *stream);
 
+/* ht_mode_gram_noalloc: the FP32 mode Gram G (N x N) = X_(g) X_(g)^T with no
+ * memory allocation at all.  It has no counterpart in the reference.
+ *
+ * It is for callers that must not allocate device memory while they run:
+ * code inside a host-side memory pool or allocator callback, a caller whose
+ * memory budget is fixed when it starts, or one whose device memory belongs to
+ * another framework's caching allocator.  ht_mode_gram may grow the library's
+ * cached workspace with cudaMalloc and stage host data; this entry point never
+ * calls cudaMalloc, cudaFree or any allocating library routine.
+ *
+ * x (the column-major tensor) and G must both be device memory.  The split-K
+ * partial sums live in one fixed scratch array of HT_NOALLOC_SCRATCH_BYTES,
+ * compiled into the library as a static device array: every GPU that loads
+ * the library holds it until the process exits.  N = prod(dims[lo..hi]) may
+ * be at most HT_NOALLOC_MAX_GRAM; larger N returns HT_ERR_UNSUPPORTED.
+ * The first call on each device looks the array's device address up once
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls on a device share the one array and it keeps the last call's
+ * contents (every partial tile is rewritten before it is read, so nothing
+ * needs clearing): calls whose work overlaps on the GPU, on different streams
+ * or from different threads, race and give wrong results; order them on one
+ * stream.  Work is queued on `stream`; the call returns without waiting. */
+#define HT_NOALLOC_SCRATCH_BYTES (16u << 20)
+#define HT_NOALLOC_MAX_GRAM 2048
+ht_status_t ht_mode_gram_noalloc(const float *x, const long *dims, int order, int lo, int hi, float *G,
+                                 void *stream);
+
 /* Bytes of device workspace ht_decompose needs for this problem. */
 ht_status_t ht_workspace_size(const long *dims, int order, const ht_tree_t *tree,
                               const ht_config_t *cfg, unsigned long long *bytes);
