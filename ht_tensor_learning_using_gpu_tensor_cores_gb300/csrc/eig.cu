@@ -27,6 +27,7 @@
 // nonzero on exactly null directions without moving any eigenvector or
 // slowing convergence.  Modes with n <= 64 (s == n) skip the iteration: Q = I
 // and the Rayleigh-Ritz step is a Jacobi eigen-decomposition of G itself.
+#include <cstring>
 #include <vector>
 
 #include "common.cuh"
@@ -249,8 +250,9 @@ HT_DEV void sum_pairs(Acc2 &acc, const float *base, int first, int count, int e)
   }
 }
 
-// Scaled, shifted Cholesky of the packed s x s matrix Sd (double): writes the
-// upper factor R (row-major, stride SMAX) and the scaling dsc to global memory.
+// Scaled, shifted Cholesky of the packed s x s matrix Sd (double): the upper
+// factor R (row-major, stride SMAX) in A and the scaling in dsc_sm, copied to
+// global memory when Rout is not null.
 HT_DEV void factor_and_store(const double *Sd, int s, float shift, float *A, float *dsc_sm, float *Rout, float *dout) {
   const int t = threadIdx.x;
   for (int j = t; j < s; j += kThreads) {
@@ -281,6 +283,7 @@ HT_DEV void factor_and_store(const double *Sd, int s, float shift, float *A, flo
     for (int k = j + t; k < s; k += kThreads) A[j * SMAX + k] = (k == j) ? d : A[j * SMAX + k] * inv;
   }
   __syncthreads();
+  if (!Rout) return;   // the caller keeps the factor in shared memory
   for (int e = t; e < s * SMAX; e += kThreads) {
     const int i = e / SMAX, k = e % SMAX;
     Rout[e] = (k >= i && k < s) ? A[e] : 0.f;
@@ -289,92 +292,190 @@ HT_DEV void factor_and_store(const double *Sd, int s, float shift, float *A, flo
 }
 
 // Cyclic Jacobi on a symmetric s x s matrix held in shared memory (s <= SMAX),
-// 256 threads, round-robin ("circle method") ordering so every round rotates
-// s/2 disjoint pairs in parallel.  On return A is diagonal to FP32 rounding,
-// V holds the eigenvectors and order[] the indices by descending eigenvalue.
-HT_DEV void jacobi_smem(float (*A)[SMAX + 1], float (*V)[SMAX + 1], int s, int *order) {
-  __shared__ float rh[SMAX / 2], sn[SMAX / 2];
-  __shared__ int pp[SMAX / 2], qq[SMAX / 2];
-  const int t = threadIdx.x;
+// 256 threads, round-robin ("circle method") ordering: every round rotates up
+// to s/2 disjoint pairs.  On return A is diagonal to FP32 rounding, V holds the
+// eigenvectors and order[] the indices by descending eigenvalue.  A2 is
+// scratch of the same shape.
+//
+// Rotation rule.  A pair rotates while its coupling is above 2.4e-7 (two FP32
+// units of rounding) relative to sqrt(a_pp a_qq), the test that keeps small
+// eigenvalues' vectors accurate (Demmel and Veselic, "Jacobi's method is more
+// accurate than QR", 1992).  The rotated pair's new diagonal is formed as
+// a_pp - t a_pq, a_qq + t a_pq and its coupling set to exactly zero
+// (Rutishauser's update), so rounding does not regenerate it and the test
+// terminates even between null directions.  Rotations are applied as
+// x - s (y + rho x), y + s (x - rho y) with rho = s / (1 + c): for the many
+// tiny late rotations c rounds to 1, and the plain c x - s y form would then
+// grow every column of V by s^2/2 per rotation (a 1e-5 loss of orthogonality
+// after ten sweeps); this form carries that second-order term explicitly.
+// The cosine uses a correctly rounded square root (an approximate one makes
+// every rotation slightly non-orthogonal, which the exact diagonal update then
+// turns into absolute errors on small eigenvalues).
+//
+// Schedule.  One round is one phase between two barriers: A2 = J^T A J is
+// formed block by block (the 2x2 block of pairs (P, P') only depends on A's
+// old block and the two pairs' rotations), V's columns are rotated, and the
+// threads owning the NEXT round's pairs recompute the three entries they need
+// from the old A with the same arithmetic and choose their rotations.  The
+// iteration stops once m - 1 consecutive rounds (every pair once) chose no
+// rotation, i.e. a full sweep left the matrix unchanged.
+struct JacRot {
+  int p, q, rot;
+  float rho, sn, tt;
+};
+
+HT_DEV JacRot jac_choose(int p, int q, int s, float app, float aqq, float apq) {
+  JacRot r{p, q, 0, 0.f, 0.f, 0.f};
+  if (q < s && fabsf(apq) > 1e-30f && fabsf(apq) > 2.4e-7f * sqrtf(fabsf(app * aqq))) {
+    const float tau = (aqq - app) / (2.f * apq);
+    r.tt = (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(1.f + tau * tau));
+    const float c = 1.f / sqrtf(1.f + r.tt * r.tt);
+    r.sn = r.tt * c;
+    r.rho = r.sn / (1.f + c);
+    r.rot = 1;
+  }
+  return r;
+}
+
+HT_DEV void jac_pair(int round, int m, int idx, int &p, int &q) {
+  const int pa = idx, pb = m - 1 - idx;
+  p = pa == 0 ? 0 : 1 + ((pa - 1 + round) % (m - 1));
+  q = pb == 0 ? 0 : 1 + ((pb - 1 + round) % (m - 1));
+  if (p > q) {
+    const int tmp = p;
+    p = q;
+    q = tmp;
+  }
+}
+
+// New 2x2 block (rows of pair a, columns of pair b) of J^T A J.
+HT_DEV void jac_block(const float (*A)[SMAX + 1], const JacRot &ja, const JacRot &jb, bool diag, float &a2, float &b2,
+                      float &c2, float &d2) {
+  const float a = A[ja.p][jb.p], b = A[ja.p][jb.q], c = A[ja.q][jb.p], d = A[ja.q][jb.q];
+  if (diag) {
+    if (ja.rot) {
+      a2 = __fmaf_rn(-ja.tt, b, a);
+      d2 = __fmaf_rn(ja.tt, b, d);
+      b2 = 0.f;
+      c2 = 0.f;
+    } else {
+      a2 = a; b2 = b; c2 = c; d2 = d;
+    }
+    return;
+  }
+  // x - s (y + rho x) and y + s (x - rho y), as explicit fused operations so
+  // that every thread that evaluates an entry gets the same bits
+  const float a1 = __fmaf_rn(-ja.sn, __fmaf_rn(ja.rho, a, c), a), c1 = __fmaf_rn(ja.sn, __fmaf_rn(-ja.rho, c, a), c);
+  const float b1 = __fmaf_rn(-ja.sn, __fmaf_rn(ja.rho, b, d), b), d1 = __fmaf_rn(ja.sn, __fmaf_rn(-ja.rho, d, b), d);
+  a2 = __fmaf_rn(-jb.sn, __fmaf_rn(jb.rho, a1, b1), a1);
+  b2 = __fmaf_rn(jb.sn, __fmaf_rn(-jb.rho, b1, a1), b1);
+  c2 = __fmaf_rn(-jb.sn, __fmaf_rn(jb.rho, c1, d1), c1);
+  d2 = __fmaf_rn(jb.sn, __fmaf_rn(-jb.rho, d1, c1), d1);
+}
+
+// Entry (i, j) of J^T A J, computed exactly as the block owner computes it.
+HT_DEV float jac_entry(const float (*A)[SMAX + 1], const JacRot *J, const int *owner, int i, int j) {
+  const int oi = owner[i], oj = owner[j];
+  const int a = oi >> 1, b = oj >> 1;
+  float v0, v1, v2, v3;
+  int r, c;   // row / column position inside the computed block
+  if (a <= b) {
+    jac_block(A, J[a], J[b], a == b, v0, v1, v2, v3);
+    r = oi & 1;
+    c = oj & 1;
+  } else {
+    jac_block(A, J[b], J[a], false, v0, v1, v2, v3);
+    r = oj & 1;
+    c = oi & 1;
+  }
+  return r ? (c ? v3 : v2) : (c ? v1 : v0);
+}
+
+HT_DEV void jacobi_smem(float (*A)[SMAX + 1], float (*A2)[SMAX + 1], float (*V)[SMAX + 1], int s, int *order) {
+  __shared__ JacRot Jbuf[2][SMAX / 2];
+  __shared__ int own[2][SMAX];
+  __shared__ unsigned short blk_ab[(SMAX / 2) * (SMAX / 2 + 1) / 2];   // upper block (a, b): a | b << 8
+  __shared__ unsigned char pair_tab[SMAX - 1][SMAX / 2][2];            // round-robin pairs of every round
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int m = (s + 1) & ~1;   // even number of players (a dummy index when s is odd)
+  const int np = m / 2;
+  const int nb = np * (np + 1) / 2;
   for (int e = t; e < SMAX * SMAX; e += 256) {
     const int i = e % SMAX, j = e / SMAX;
     V[i][j] = (i == j) ? 1.f : 0.f;
   }
+  for (int e = t; e < nb; e += 256) {
+    int a, b;
+    tri_index(e, a, b);
+    blk_ab[e] = static_cast<unsigned short>(a | (b << 8));
+  }
+  for (int e = t; e < (m - 1) * np; e += 256) {
+    const int r = e / np, idx = e % np;
+    int p, q;
+    jac_pair(r, m, idx, p, q);
+    pair_tab[r][idx][0] = static_cast<unsigned char>(p);
+    pair_tab[r][idx][1] = static_cast<unsigned char>(q);
+  }
   __syncthreads();
-  // A pair rotates while its coupling is above 2.4e-7 (two FP32 units of
-  // rounding) relative to sqrt(a_pp a_qq), the test that keeps small
-  // eigenvalues' vectors accurate (Demmel and Veselic, "Jacobi's method is
-  // more accurate than QR", 1992).  The rotated pair's new diagonal is
-  // formed as a_pp - t a_pq, a_qq + t a_pq and its coupling set to exactly
-  // zero (Rutishauser's update), so rounding does not regenerate it and the
-  // test terminates even between null directions.  Sweeps stop after one
-  // that rotated nothing.  Rotations are applied as x - s (y + rho x),
-  // y + s (x - rho y) with rho = s / (1 + c): for the many tiny late
-  // rotations c rounds to 1, and the plain c x - s y form would then grow every
-  // column of V by s^2/2 per rotation (a 1e-5 loss of orthogonality after ten
-  // sweeps); this form carries that second-order term explicitly.
-  for (int sweep = 0; sweep < 20 && m > 1; ++sweep) {
-    int rotated = 0;
-    for (int round = 0; round < m - 1; ++round) {
-      int did = 0, pme = 0, qme = 0;
-      float tt = 0.f, app = 0.f, aqq = 0.f;
-      if (t < m / 2) {
-        // position 0 is fixed, positions 1..m-1 rotate by one each round
-        const int pa = t, pb = m - 1 - t;
-        int p = pa == 0 ? 0 : 1 + ((pa - 1 + round) % (m - 1));
-        int q = pb == 0 ? 0 : 1 + ((pb - 1 + round) % (m - 1));
-        if (p > q) { const int tmp = p; p = q; q = tmp; }
-        float rho = 0.f, sv = 0.f;
-        if (q < s) {
-          const float apq = A[p][q];
-          if (fabsf(apq) > 1e-30f && fabsf(apq) > 2.4e-7f * sqrtf(fabsf(A[p][p] * A[q][q]))) {
-            const float tau = (A[q][q] - A[p][p]) / (2.f * apq);
-            tt = (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(1.f + tau * tau));
-            const float c = 1.f / sqrtf(1.f + tt * tt);
-            sv = tt * c;
-            rho = sv / (1.f + c);
-            app = A[p][p] - tt * apq;
-            aqq = A[q][q] + tt * apq;
-            did = 1;
-          }
+  int cur = 0;
+  float (*Ac)[SMAX + 1] = A;
+  float (*An)[SMAX + 1] = A2;
+  int any = 0;
+  if (t < np && m > 1) {
+    const int p = pair_tab[0][t][0], q = pair_tab[0][t][1];
+    Jbuf[0][t] = jac_choose(p, q, s, A[p][p], A[q][q], A[p][q]);
+    own[0][p] = 2 * t;
+    own[0][q] = 2 * t + 1;
+    any = Jbuf[0][t].rot;
+  }
+  int quiet = __syncthreads_or(any) ? 0 : 1;
+  const int max_rounds = m > 1 ? 20 * (m - 1) : 0;
+  int rr = 0;   // round index within the sweep
+  for (int round = 0; round < max_rounds && quiet < m - 1; ++round) {
+    const JacRot *J = Jbuf[cur];
+    const int *ow = own[cur];
+    const int rn = rr + 1 == m - 1 ? 0 : rr + 1;
+    any = 0;
+    if (warp < 7) {
+      // A2 = J^T A J: upper blocks (a <= b) and their mirror
+      for (int e = t; e < nb; e += 224) {
+        const int ab = blk_ab[e], a = ab & 255, b = ab >> 8;
+        const JacRot &ja = J[a], &jb = J[b];
+        float a2, b2, c2, d2;
+        jac_block(Ac, ja, jb, a == b, a2, b2, c2, d2);
+        An[ja.p][jb.p] = a2; An[ja.p][jb.q] = b2; An[ja.q][jb.p] = c2; An[ja.q][jb.q] = d2;
+        An[jb.p][ja.p] = a2; An[jb.q][ja.p] = b2; An[jb.p][ja.q] = c2; An[jb.q][ja.q] = d2;
+      }
+      // V <- V J: warp w rotates pairs w, w + 7, ...; lanes own rows lane, lane + 32
+      for (int a = warp; a < np; a += 7) {
+        const JacRot ja = J[a];
+        if (!ja.rot) continue;
+        for (int i = lane; i < s; i += 32) {
+          const float vp = V[i][ja.p], vq = V[i][ja.q];
+          V[i][ja.p] = __fmaf_rn(-ja.sn, __fmaf_rn(ja.rho, vp, vq), vp);
+          V[i][ja.q] = __fmaf_rn(ja.sn, __fmaf_rn(-ja.rho, vq, vp), vq);
         }
-        pp[t] = p; qq[t] = q; rh[t] = rho; sn[t] = sv;
-        pme = p; qme = q;
       }
-      rotated |= __syncthreads_or(did);
-      for (int e = t; e < (m / 2) * s; e += 256) {   // rows: A <- J^T A
-        const int pr = e / s, j = e % s;
-        const int p = pp[pr], q = qq[pr];
-        if (q >= s) continue;
-        const float sv = sn[pr], rho = rh[pr];
-        const float ap = A[p][j], aq = A[q][j];
-        A[p][j] = ap - sv * (aq + rho * ap);
-        A[q][j] = aq + sv * (ap - rho * aq);
-      }
-      __syncthreads();
-      for (int e = t; e < (m / 2) * s; e += 256) {   // columns: A <- A J, V <- V J
-        const int pr = e / s, i = e % s;
-        const int p = pp[pr], q = qq[pr];
-        if (q >= s) continue;
-        const float sv = sn[pr], rho = rh[pr];
-        const float ap = A[i][p], aq = A[i][q];
-        A[i][p] = ap - sv * (aq + rho * ap);
-        A[i][q] = aq + sv * (ap - rho * aq);
-        const float vp = V[i][p], vq = V[i][q];
-        V[i][p] = vp - sv * (vq + rho * vp);
-        V[i][q] = vq + sv * (vp - rho * vq);
-      }
-      __syncthreads();
-      if (did) {
-        A[pme][pme] = app;
-        A[qme][qme] = aqq;
-        A[pme][qme] = 0.f;
-        A[qme][pme] = 0.f;
-      }
-      __syncthreads();
+    } else if (lane < np) {
+      // the next round's rotations, from the entries this round produces
+      const int p = pair_tab[rn][lane][0], q = pair_tab[rn][lane][1];
+      const float app = jac_entry(Ac, J, ow, p, p), aqq = jac_entry(Ac, J, ow, q, q), apq = jac_entry(Ac, J, ow, p, q);
+      const JacRot jn = jac_choose(p, q, s, app, aqq, apq);
+      Jbuf[cur ^ 1][lane] = jn;
+      own[cur ^ 1][p] = 2 * lane;
+      own[cur ^ 1][q] = 2 * lane + 1;
+      any = jn.rot;
     }
-    if (!rotated) break;
+    quiet = __syncthreads_or(any) ? 0 : quiet + 1;
+    cur ^= 1;
+    rr = rn;
+    float (*tmp)[SMAX + 1] = Ac;
+    Ac = An;
+    An = tmp;
+  }
+  if (Ac != A) {
+    for (int e = t; e < s * s; e += 256) A[e % s][e / s] = Ac[e % s][e / s];
+    __syncthreads();
   }
   for (int j = t; j < s; j += 256) {   // rank by counting: descending eigenvalues
     const float dj = A[j][j];
@@ -541,6 +642,7 @@ __global__ void __launch_bounds__(kThreads) eig_step_kernel(const EigBatch probs
   // Rayleigh-Ritz: Jacobi on H (symmetrised from the upper triangle)
   float (*A)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(Rs);
   float (*VV)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(Vs);
+  float (*AA2)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(Vs + SMAX * (SMAX + 1));
   for (int e = t; e < SMAX * SMAX; e += kThreads) {
     const int i = e % SMAX, j = e / SMAX;
     float v = 0.f;
@@ -548,86 +650,12 @@ __global__ void __launch_bounds__(kThreads) eig_step_kernel(const EigBatch probs
     A[i][j] = v;
   }
   __syncthreads();
-  jacobi_smem(A, VV, s, order);
+  jacobi_smem(A, AA2, VV, s, order);
   for (int e = t; e < s * s; e += kThreads) {
     const int i = e % s, r = e / s;
     P.V[i + s * r] = VV[i][order[r]];
   }
   for (int r = t; r < P.K; r += kThreads) P.theta[r] = A[order[r]][order[r]];
-}
-
-// U = Q V[:, :K], GU = Y V[:, :K], residual max_j ||GU_j - theta_j U_j|| / theta_1.
-__global__ void __launch_bounds__(kThreads) eig_final_kernel(const EigBatch probs, int qbuf, int ybuf) {
-  const EigDev &P = probs.p[blockIdx.y];
-  const int rb = blockIdx.x;
-  if (rb >= P.nrb) return;
-  const int n = P.n, s = P.s, K = P.K;
-  __shared__ float Vsm[SMAX][SMAX + 1];
-  __shared__ float Qr[RB][SMAX + 1];
-  __shared__ float Yr[RB][SMAX + 1];
-  __shared__ float res[RB][SMAX + 1];
-  __shared__ int s_flag;
-  const int t = threadIdx.x;
-  const int r0 = rb * RB;
-  const float *Q = P.buf[qbuf], *Y = P.buf[ybuf];
-  for (int e = t; e < SMAX * SMAX; e += kThreads) {
-    const int i = e % SMAX, j = e / SMAX;
-    Vsm[i][j] = (i < s && j < s) ? P.V[i + s * j] : 0.f;
-  }
-  for (int e = t; e < RB * SMAX; e += kThreads) {
-    const int i = e % RB, j = e / RB;
-    const bool ok = r0 + i < n && j < s;
-    Qr[i][j] = ok ? Q[(r0 + i) + static_cast<long long>(n) * j] : 0.f;
-    Yr[i][j] = ok ? Y[(r0 + i) + static_cast<long long>(n) * j] : 0.f;
-  }
-  __syncthreads();
-  const int i = t / 16, jb = t % 16;
-  for (int c = 0; c < 4; ++c) {
-    const int j = jb + 16 * c;
-    float u = 0.f, gu = 0.f;
-    if (j < K) {
-      for (int k = 0; k < s; ++k) {
-        u = fmaf(Qr[i][k], Vsm[k][j], u);
-        gu = fmaf(Yr[i][k], Vsm[k][j], gu);
-      }
-    }
-    const bool ok = (r0 + i < n) && j < K;
-    if (ok) {
-      P.U[(r0 + i) + static_cast<long long>(n) * j] = u;
-      P.GU[(r0 + i) + static_cast<long long>(n) * j] = gu;
-    }
-    const float d = ok ? gu - P.theta[j] * u : 0.f;
-    res[i][j] = d * d;
-  }
-  __syncthreads();
-  for (int j = t; j < K; j += kThreads) {
-    float acc = 0.f;
-    for (int r = 0; r < RB; ++r) acc += res[r][j];
-    P.colss[static_cast<long long>(rb) * SMAX + j] = acc;
-  }
-  if (!arrive(&P.cnt[P.ngroups], P.nrb, &s_flag)) return;
-  __shared__ float colmax[SMAX];
-  if (t < SMAX) {
-    float acc = 0.f;
-    if (t < K) {
-      for (int r0 = 0; r0 < P.nrb; r0 += 8) {
-        float v[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q)
-          v[q] = (r0 + q < P.nrb) ? __ldcg(P.colss + static_cast<long long>(r0 + q) * SMAX + t) : 0.f;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) acc += v[q];
-      }
-    }
-    colmax[t] = sqrtf(acc);
-  }
-  __syncthreads();
-  if (t == 0) {
-    float m = 0.f;
-    for (int j = 0; j < K; ++j) m = fmaxf(m, colmax[j]);
-    const float th = P.theta[0];
-    P.resid[0] = th > 0.f ? m / th : m;
-  }
 }
 
 // Transfer-tensor step of the complementary-leaf construction.  WG = W^T G_c W
@@ -643,6 +671,8 @@ __global__ void __launch_bounds__(256) transfer_eig_kernel(const float *WG, int 
                                                            float *M, float *Broot) {
   __shared__ float A[SMAX][SMAX + 1];
   __shared__ float V[SMAX][SMAX + 1];
+  extern __shared__ float jac_scratch[];   // SMAX * (SMAX + 1) floats
+  float (*A2)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(jac_scratch);
   __shared__ int order[SMAX];
   __shared__ float inv[SMAX];
   const int t = threadIdx.x;
@@ -651,7 +681,7 @@ __global__ void __launch_bounds__(256) transfer_eig_kernel(const float *WG, int 
     A[i][j] = (i < kt && j < kt) ? 0.5f * (WG[i + kw * j] + WG[j + kw * i]) : 0.f;
   }
   __syncthreads();
-  jacobi_smem(A, V, kt, order);
+  jacobi_smem(A, A2, V, kt, order);
   if (t == 0) {
     const float lmax = A[order[0]][order[0]];
     for (int r = 0; r < kt; ++r) {
@@ -687,6 +717,8 @@ __global__ void __launch_bounds__(256) svd_from_gram_kernel(const float *GW, int
                                                             float *M2, float *Broot) {
   __shared__ float A[SMAX][SMAX + 1];
   __shared__ float V[SMAX][SMAX + 1];
+  extern __shared__ float jac_scratch[];   // SMAX * (SMAX + 1) floats
+  float (*A2)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(jac_scratch);
   __shared__ int order[SMAX];
   __shared__ float inv[SMAX];
   const int t = threadIdx.x;
@@ -695,7 +727,7 @@ __global__ void __launch_bounds__(256) svd_from_gram_kernel(const float *GW, int
     A[i][j] = (i < s && j < s) ? 0.5f * (GW[i + s * j] + GW[j + s * i]) : 0.f;
   }
   __syncthreads();
-  jacobi_smem(A, V, s, order);
+  jacobi_smem(A, A2, V, s, order);
   if (t == 0) {
     const float s1 = sqrtf(fmaxf(A[order[0]][order[0]], 0.f));
     for (int r = 0; r < s; ++r) {
@@ -725,17 +757,604 @@ __global__ void __launch_bounds__(256) svd_from_gram_kernel(const float *GW, int
   }
 }
 
+// ------------------------------------------------------------------------
+// Cooperative eigen-solver: the whole subspace iteration of every problem of
+// the batch in ONE launch.  CTAs of one problem own consecutive row ranges;
+// grid-wide barriers (bounded spins on a counter / generation pair) separate
+// the phases, so there is no single-CTA tail per iteration: the s x s Gram
+// partials are reduced by all CTAs (each sums a slice of the entries over the
+// problem's CTAs, in CTA order) and every CTA of the problem factors the
+// reduced Gram itself.  Direct problems (s == n) run in CTAs of their own that
+// take no part in the barriers.
+constexpr int RBMAX = 32;                 // rows per sub-block
+constexpr int CNS = 4;                    // cp.async stages of the G * Y product
+constexpr int CLD = 68;                   // padded k length of a staged row
+constexpr int kCoopMaxCta = 160;          // >= SMs of the device
+constexpr int kMaxEntPerThread = (ESMAX + 255) / 256;
+
+struct CoopProb {
+  const float *G;
+  int n, s, K;
+  int cta0, ncta, rows;                   // CTAs [cta0, cta0 + ncta), `rows` rows each (last fewer)
+  float *buf[4];                          // n x s blocks (column stride n)
+  float *U, *GU, *theta, *resid;
+  const float *start;
+  unsigned long long seed, stream_id;
+  float *part;                            // [ncta][ESMAX][2]
+  double *S;                              // [ESMAX] reduced Gram / Rayleigh quotient
+  float *V;                               // [SMAX * SMAX] Ritz vectors of H (column j = vector j)
+  float *colss;                           // [ncta][SMAX] residual partials
+};
+
+struct CoopBatch {
+  CoopProb p[kMaxProb];
+  int nprob, iters, nsync, ent_total;
+  int ent_off[kMaxProb + 1];
+  int direct_idx[kMaxProb];               // problem index of direct CTA d (blockIdx.x - nsync)
+  unsigned *bar;                          // [2]: arrivals, generation (zero at launch)
+  int *err;
+};
+
+constexpr size_t kCoopRing = size_t(CNS) * (RBMAX + SMAX) * CLD;              // floats
+constexpr size_t kCoopAlias = 2 * ESMAX + 3 * SMAX * (SMAX + 1);                // Sd (doubles) + A + V + A2
+constexpr size_t kCoopSmem =
+    sizeof(float) * (SMAX * SMAX + SMAX + 2 * RBMAX * SMAX + (kCoopRing > kCoopAlias ? kCoopRing : kCoopAlias)) + 64;
+
+// Bounded grid barrier over the first `members` CTAs.  False (and the error
+// word set) when the wait ran past the limit; the caller then returns.
+HT_DEV bool grid_barrier(unsigned *bar, unsigned members, int *err, int *s_ok) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *gen = bar + 1;
+    const unsigned g = *gen;
+    __threadfence();
+    int ok = 1;
+    if (atomicAdd(bar, 1u) == members - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      const uint64_t t0 = global_timer_ns();
+      while (*gen == g) {
+        __nanosleep(64);
+        if (global_timer_ns() - t0 > kWaitLimitNs) {
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    if (!ok) report_error(err, kErrTimeout);
+    *s_ok = ok;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
+// G * Y product for the CTA's rows, K split across the 8 warps: warp w takes
+// k = 8w .. 8w+7 of every 64-wide chunk, lane l columns l and l + 32, and
+// every row (RT >= rows, padded); the G operand is a broadcast shared-memory
+// load.  The eight partial blocks are summed in a fixed order at the end.
+template <int RT, int NC>
+HT_DEV void coop_product_t(const float *G, const float *Y, int n, int s, int r0, int rows, float *ring, float *Zs) {
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const bool vec = (n % 4 == 0) && ((reinterpret_cast<uintptr_t>(G) | reinterpret_cast<uintptr_t>(Y)) & 15u) == 0;
+  const int nchunks = (n + 63) / 64;
+  constexpr int STAGE = (RBMAX + SMAX) * CLD;
+  auto issue = [&](int c) {
+    const int kc = c * 64;
+    float *Gd = ring + (c % CNS) * STAGE, *Yd = Gd + RBMAX * CLD;
+    if (vec) {
+      for (int idx = t; idx < RT * 16; idx += 256) {
+        const int i = idx >> 4, k4 = (idx & 15) * 4, kk = kc + k4;
+        const int bytes = (i < rows && kk < n) ? 4 * min(4, n - kk) : 0;
+        const float *g = bytes ? G + static_cast<long long>(r0 + i) * n + kk : G;
+        cp_async16(Gd + i * CLD + k4, g, bytes);
+      }
+      for (int idx = t; idx < 32 * NC * 16; idx += 256) {
+        const int j = idx >> 4, k4 = (idx & 15) * 4, kk = kc + k4;
+        const int bytes = (j < s && kk < n) ? 4 * min(4, n - kk) : 0;
+        const float *y = bytes ? Y + static_cast<long long>(j) * n + kk : Y;
+        cp_async16(Yd + j * CLD + k4, y, bytes);
+      }
+    } else {
+      for (int idx = t; idx < RT * 64; idx += 256) {
+        const int i = idx >> 6, k = idx & 63, kk = kc + k;
+        Gd[i * CLD + k] = (i < rows && kk < n) ? __ldcg(G + static_cast<long long>(r0 + i) * n + kk) : 0.f;
+      }
+      for (int idx = t; idx < 32 * NC * 64; idx += 256) {
+        const int j = idx >> 6, k = idx & 63, kk = kc + k;
+        Yd[j * CLD + k] = (j < s && kk < n) ? __ldcg(Y + static_cast<long long>(j) * n + kk) : 0.f;
+      }
+    }
+  };
+  float acc[RT][NC];
+#pragma unroll
+  for (int r = 0; r < RT; ++r)
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[r][c] = 0.f;
+  for (int c = 0; c < CNS - 1; ++c) {
+    if (c < nchunks) issue(c);
+    cp_async_commit();
+  }
+  for (int c = 0; c < nchunks; ++c) {
+    if (c + CNS - 1 < nchunks) issue(c + CNS - 1);
+    cp_async_commit();
+    cp_async_wait<CNS - 1>();
+    __syncthreads();
+    const float *Gd = ring + (c % CNS) * STAGE, *Yd = Gd + RBMAX * CLD;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int kk = 8 * warp + 4 * h;
+      float4 y[NC];
+#pragma unroll
+      for (int q = 0; q < NC; ++q) y[q] = *reinterpret_cast<const float4 *>(Yd + (lane + 32 * q) * CLD + kk);
+#pragma unroll
+      for (int r = 0; r < RT; ++r) {
+        const float4 g = *reinterpret_cast<const float4 *>(Gd + r * CLD + kk);
+#pragma unroll
+        for (int q = 0; q < NC; ++q)
+          acc[r][q] = fmaf(g.x, y[q].x, fmaf(g.y, y[q].y, fmaf(g.z, y[q].z, fmaf(g.w, y[q].w, acc[r][q]))));
+      }
+    }
+    __syncthreads();   // this stage is refilled CNS-1 chunks later
+  }
+  cp_async_wait<0>();
+  __syncthreads();
+  // partials [warp][row][col] in the (now idle) ring, then a fixed-order sum
+  float *red = ring;
+#pragma unroll
+  for (int r = 0; r < RT; ++r)
+#pragma unroll
+    for (int q = 0; q < NC; ++q) red[(warp * RT + r) * SMAX + lane + 32 * q] = acc[r][q];
+  __syncthreads();
+  for (int e = t; e < RBMAX * SMAX; e += 256) {
+    const int i = e / SMAX, j = e % SMAX;
+    float v = 0.f;
+    if (i < rows && j < s) {
+#pragma unroll
+      for (int w = 0; w < 8; ++w) v += red[(w * RT + i) * SMAX + j];
+    }
+    Zs[e] = v;
+  }
+  __syncthreads();
+}
+
+HT_DEV void coop_product(const float *G, const float *Y, int n, int s, int r0, int rows, float *ring, float *Zs) {
+  if (s <= 32) {
+    if (rows <= 8) coop_product_t<8, 1>(G, Y, n, s, r0, rows, ring, Zs);
+    else if (rows <= 16) coop_product_t<16, 1>(G, Y, n, s, r0, rows, ring, Zs);
+    else if (rows <= 24) coop_product_t<24, 1>(G, Y, n, s, r0, rows, ring, Zs);
+    else coop_product_t<32, 1>(G, Y, n, s, r0, rows, ring, Zs);
+  } else {
+    if (rows <= 8) coop_product_t<8, 2>(G, Y, n, s, r0, rows, ring, Zs);
+    else if (rows <= 16) coop_product_t<16, 2>(G, Y, n, s, r0, rows, ring, Zs);
+    else if (rows <= 24) coop_product_t<24, 2>(G, Y, n, s, r0, rows, ring, Zs);
+    else coop_product_t<32, 2>(G, Y, n, s, r0, rows, ring, Zs);
+  }
+}
+
+// Scaled, shifted Cholesky of the packed s x s matrix Sd (double) followed by
+// the explicit transform T = diag(dsc) R^-1 (row-major, stride SMAX, upper
+// triangular) in Ts, so that applying it is a small matrix product.  A is
+// SMAX x SMAX scratch.  The elimination keeps pivot rows unscaled (one barrier
+// per step); R's rows are scaled when T is formed.
+HT_DEV void factor_transform(const double *Sd, int s, float shift, float *A, float *dsc, float *piv, float *Ts) {
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  for (int j = t; j < s; j += 256) {
+    const double d = Sd[j * (j + 1) / 2 + j];
+    dsc[j] = d > 1e-300 ? static_cast<float>(1.0 / sqrt(d)) : 0.f;
+  }
+  __syncthreads();
+  const int E = s * (s + 1) / 2;
+  for (int e = t; e < E; e += 256) {
+    int i, j;
+    tri_index(e, i, j);
+    float v = static_cast<float>(Sd[e] * static_cast<double>(dsc[i]) * static_cast<double>(dsc[j]));
+    if (i == j) v = (dsc[j] > 0.f ? 1.f : 0.f) + shift;
+    A[i * SMAX + j] = v;
+  }
+  __syncthreads();
+  for (int j = 0; j < s; ++j) {
+    const float p = fmaxf(A[j * SMAX + j], 1e-30f);
+    const float pinv = 1.f / p;
+    if (t == 0) piv[j] = p;
+    for (int i = j + 1 + warp; i < s; i += 8) {
+      const float f = A[j * SMAX + i] * pinv;
+      for (int k = i + lane; k < s; k += 32) A[i * SMAX + k] = fmaf(-f, A[j * SMAX + k], A[i * SMAX + k]);
+    }
+    __syncthreads();
+  }
+  // R[i][j] = A[i][j] / sqrt(piv_i) (j > i), R[i][i] = sqrt(piv_i); then
+  // W = R^-1 column by column (thread k solves R w = e_k), T = diag(dsc) W.
+  for (int e = t; e < E; e += 256) {
+    int i, j;
+    tri_index(e, i, j);
+    const float di = sqrtf(piv[i]);
+    A[i * SMAX + j] = (i == j) ? 1.f / di : A[i * SMAX + j] / di;   // diagonal holds 1 / R[i][i]
+  }
+  __syncthreads();
+  if (t < s) {
+    const int k = t;
+    for (int i = k; i >= 0; --i) {
+      float acc = (i == k) ? 1.f : 0.f;
+      for (int j = i + 1; j <= k; ++j) acc = fmaf(-A[i * SMAX + j], Ts[j * SMAX + k], acc);
+      Ts[i * SMAX + k] = acc * A[i * SMAX + i];
+    }
+  }
+  __syncthreads();
+  for (int e = t; e < SMAX * SMAX; e += 256) {
+    const int i = e / SMAX, k = e % SMAX;
+    Ts[e] = (i < s && k < s && k >= i) ? Ts[e] * dsc[i] : 0.f;
+  }
+  __syncthreads();
+}
+
+// X (RBMAX x SMAX rows) <- X T for the upper-triangular T (s x s): thread
+// (row t / 8, columns t % 8 + 8 b) forms its eight outputs, then writes back.
+HT_DEV void coop_apply(float *X, const float *Ts, int s) {
+  const int t = threadIdx.x, r = t >> 3, cb = t & 7;
+  float o[8];
+#pragma unroll
+  for (int b = 0; b < 8; ++b) o[b] = 0.f;
+  for (int j = 0; j < s; ++j) {
+    const float x = X[r * SMAX + j];
+#pragma unroll
+    for (int b = 0; b < 8; ++b) o[b] = fmaf(x, Ts[j * SMAX + cb + 8 * b], o[b]);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < 8; ++b) X[r * SMAX + cb + 8 * b] = (cb + 8 * b < s) ? o[b] : 0.f;
+  __syncthreads();
+}
+
+// Rows [r0, r0 + rows) of an n x s block into X[i * SMAX + j] (zero padded).
+HT_DEV void coop_load_rows(const float *src, int n, int s, int r0, int rows, float *X) {
+  for (int e = threadIdx.x; e < RBMAX * SMAX; e += 256) {
+    const int i = e % RBMAX, j = e / RBMAX;
+    X[i * SMAX + j] = (i < rows && j < s) ? __ldcg(src + (r0 + i) + static_cast<long long>(n) * j) : 0.f;
+  }
+}
+
+HT_DEV void coop_store_rows(const float *X, int n, int s, int r0, int rows, float *dst) {
+  for (int e = threadIdx.x; e < RBMAX * SMAX; e += 256) {
+    const int i = e % RBMAX, j = e / RBMAX;
+    if (i < rows && j < s) dst[(r0 + i) + static_cast<long long>(n) * j] = X[i * SMAX + j];
+  }
+}
+
+// acc[q] += partial of entry e = t + 256 q (packed upper triangle, i <= j) of L^T R.
+HT_DEV void coop_gram_partial(const float *L, const float *R, int s, Acc2 (&acc)[kMaxEntPerThread]) {
+  const int E = s * (s + 1) / 2;
+#pragma unroll
+  for (int q = 0; q < kMaxEntPerThread; ++q) {
+    const int e = threadIdx.x + 256 * q;
+    if (e < E) {
+      int i, j;
+      tri_index(e, i, j);
+#pragma unroll 8
+      for (int r = 0; r < RBMAX; ++r) acc2_add_prod(acc[q], L[r * SMAX + i], R[r * SMAX + j]);
+    }
+  }
+}
+
+HT_DEV void coop_gram_store(const Acc2 (&acc)[kMaxEntPerThread], int s, float *part) {
+  const int E = s * (s + 1) / 2;
+#pragma unroll
+  for (int q = 0; q < kMaxEntPerThread; ++q) {
+    const int e = threadIdx.x + 256 * q;
+    if (e < E) {
+      part[2 * e] = acc[q].s;
+      part[2 * e + 1] = acc[q].c;
+    }
+  }
+}
+
+// Every synchronising CTA sums a slice of all problems' entries over the
+// problem's CTA partials, in CTA order.
+HT_DEV void coop_reduce(const CoopBatch &B) {
+  for (int g = blockIdx.x * 256 + threadIdx.x; g < B.ent_total; g += B.nsync * 256) {
+    int p = 0;
+    while (g >= B.ent_off[p + 1]) ++p;
+    const CoopProb &P = B.p[p];
+    const int e = g - B.ent_off[p];
+    Acc2 acc = {0.f, 0.f};
+    for (int c0 = 0; c0 < P.ncta; c0 += GROUP) {
+      float hi[GROUP], lo[GROUP];
+#pragma unroll
+      for (int q = 0; q < GROUP; ++q) {
+        const bool ok = c0 + q < P.ncta;
+        const float *src = P.part + (static_cast<long long>(c0 + q) * ESMAX + e) * 2;
+        hi[q] = ok ? __ldcg(src) : 0.f;
+        lo[q] = ok ? __ldcg(src + 1) : 0.f;
+      }
+#pragma unroll
+      for (int q = 0; q < GROUP; ++q) acc2_add(acc, hi[q], lo[q]);
+    }
+    P.S[e] = static_cast<double>(acc.s) + static_cast<double>(acc.c);
+  }
+}
+
+HT_DEV void coop_load_S(const CoopProb &P, double *Sd) {
+  const int E = P.s * (P.s + 1) / 2;
+  for (int e = threadIdx.x; e < E; e += 256) Sd[e] = __ldcg(P.S + e);
+  __syncthreads();
+}
+
+// One CholeskyQR-type step over the CTA's rows: X = src rows (optionally
+// G * src + mu src), apply the current transform Rs (unless identity), store to dst,
+// accumulate the Gram partial.  mode 0: ITER, 1: APPLY, 2: RR (also Q rows).
+HT_DEV void coop_step(const CoopProb &P, int cl, int mode, const float *src, float *dst, float *dst2, bool ident,
+                      float mu, const float *Rs, float *Zs, float *Qr, float *ring) {
+  Acc2 acc[kMaxEntPerThread];
+#pragma unroll
+  for (int q = 0; q < kMaxEntPerThread; ++q) acc[q] = Acc2{0.f, 0.f};
+  const int rb = cl * P.rows, re = min(P.n, rb + P.rows);
+  for (int r0 = rb; r0 < re; r0 += RBMAX) {
+    const int rows = min(RBMAX, re - r0);
+    coop_load_rows(src, P.n, P.s, r0, rows, Qr);
+    if (mode != 1) {
+      coop_product(P.G, src, P.n, P.s, r0, rows, ring, Zs);
+      if (mode == 0)
+        for (int e = threadIdx.x; e < RBMAX * SMAX; e += 256) Zs[e] = fmaf(mu, Qr[e], Zs[e]);
+    } else {
+      __syncthreads();
+      for (int e = threadIdx.x; e < RBMAX * SMAX; e += 256) Zs[e] = Qr[e];
+    }
+    __syncthreads();
+    if (!ident) {
+      coop_apply(Zs, Rs, P.s);
+      if (mode == 2) coop_apply(Qr, Rs, P.s);
+    }
+    if (mode == 2) {
+      coop_store_rows(Qr, P.n, P.s, r0, rows, dst);
+      coop_store_rows(Zs, P.n, P.s, r0, rows, dst2);
+      coop_gram_partial(Qr, Zs, P.s, acc);
+    } else {
+      coop_store_rows(Zs, P.n, P.s, r0, rows, dst);
+      coop_gram_partial(Zs, Zs, P.s, acc);
+    }
+    __syncthreads();
+  }
+  coop_gram_store(acc, P.s, P.part + static_cast<long long>(cl) * ESMAX * 2);
+}
+
+// U = Q V[:, :K], GU = Y V[:, :K] on the CTA's rows, column sums of squares of
+// GU - theta U into colss[cl].
+HT_DEV void coop_final_rows(const CoopProb &P, int cl, const float *Q, const float *Y, float (*Vsm)[SMAX + 1],
+                            const float *th, float *Qr, float *Zs) {
+  const int t = threadIdx.x, n = P.n, s = P.s, K = P.K;
+  __shared__ float colsum[SMAX];
+  if (t < SMAX) colsum[t] = 0.f;
+  const int rb = cl * P.rows, re = min(n, rb + P.rows);
+  for (int r0 = rb; r0 < re; r0 += RBMAX) {
+    const int rows = min(RBMAX, re - r0);
+    coop_load_rows(Q, n, s, r0, rows, Qr);
+    coop_load_rows(Y, n, s, r0, rows, Zs);
+    __syncthreads();
+    // thread: row i = t / 8 (32 rows), columns j = t % 8 + 8 c
+    const int i = t >> 3, jb = t & 7;
+    float dsq[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int j = jb + 8 * c;
+      float u = 0.f, gu = 0.f;
+      if (j < K && i < rows) {
+        for (int k = 0; k < s; ++k) {
+          u = fmaf(Qr[i * SMAX + k], Vsm[k][j], u);
+          gu = fmaf(Zs[i * SMAX + k], Vsm[k][j], gu);
+        }
+        P.U[(r0 + i) + static_cast<long long>(n) * j] = u;
+        P.GU[(r0 + i) + static_cast<long long>(n) * j] = gu;
+      }
+      const float d = (j < K && i < rows) ? gu - th[j] * u : 0.f;
+      dsq[c] = d * d;
+    }
+    __syncthreads();
+    // column sums over the 32 rows: reuse Qr as scratch [row][col]
+#pragma unroll
+    for (int c = 0; c < 8; ++c) Qr[i * SMAX + jb + 8 * c] = dsq[c];
+    __syncthreads();
+    if (t < SMAX) {
+      float a = 0.f;
+      for (int r = 0; r < RBMAX; ++r) a += Qr[r * SMAX + t];
+      colsum[t] += a;
+    }
+    __syncthreads();
+  }
+  if (t < SMAX) P.colss[static_cast<long long>(cl) * SMAX + t] = colsum[t];
+}
+
+__global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
+  extern __shared__ __align__(16) float sm[];
+  float *Rs = sm;                           // SMAX*SMAX (upper factor, row-major)
+  float *ds = Rs + SMAX * SMAX;             // SMAX
+  float *Zs = ds + SMAX;                    // RBMAX*SMAX
+  float *Qr = Zs + RBMAX * SMAX;            // RBMAX*SMAX
+  float *ring = Qr + RBMAX * SMAX;          // product ring, or (aliased) the reducer / Jacobi scratch
+  double *Sd = reinterpret_cast<double *>(ring);
+  float (*A)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(ring + 2 * ESMAX);
+  float (*VV)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(ring + 2 * ESMAX + SMAX * (SMAX + 1));
+  float (*A2)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(ring + 2 * ESMAX + 2 * SMAX * (SMAX + 1));
+  __shared__ int s_ok;
+  __shared__ int order[SMAX];
+  __shared__ float red[256];
+  __shared__ float th_sm[SMAX];
+  __shared__ float piv[SMAX];
+  const int t = threadIdx.x;
+
+  if (static_cast<int>(blockIdx.x) >= B.nsync) {
+    // ---- direct problem (s == n <= 64): Jacobi on G itself, no barriers
+    const CoopProb &P = B.p[B.direct_idx[blockIdx.x - B.nsync]];
+    const int n = P.n, K = P.K;
+    for (int e = t; e < SMAX * SMAX; e += 256) {
+      const int i = e % SMAX, j = e / SMAX;
+      A[i][j] = (i < n && j < n) ? P.G[i + static_cast<long long>(n) * j] : 0.f;
+    }
+    __syncthreads();
+    jacobi_smem(A, A2, VV, n, order);
+    for (int r = t; r < K; r += 256) P.theta[r] = A[order[r]][order[r]];
+    // U = V[:, order[:K]], GU = G U, residual
+    for (int e = t; e < n * K; e += 256) {
+      const int i = e % n, j = e / n;
+      float gu = 0.f;
+      for (int k = 0; k < n; ++k) gu = fmaf(P.G[i + static_cast<long long>(n) * k], VV[k][order[j]], gu);
+      const float u = VV[i][order[j]];
+      P.U[i + static_cast<long long>(n) * j] = u;
+      P.GU[i + static_cast<long long>(n) * j] = gu;
+      const float d = gu - A[order[j]][order[j]] * u;
+      Zs[e] = d * d;   // n * K <= 64 * 64 fits Zs + Qr (contiguous)
+    }
+    __syncthreads();
+    if (t == 0) {
+      float m = 0.f;
+      for (int j = 0; j < K; ++j) {
+        float a = 0.f;
+        for (int i = 0; i < n; ++i) a += Zs[i + n * j];
+        m = fmaxf(m, sqrtf(a));
+      }
+      const float th = A[order[0]][order[0]];
+      P.resid[0] = th > 0.f ? m / th : m;
+    }
+    return;
+  }
+
+  int pi = 0;
+  while (!(static_cast<int>(blockIdx.x) >= B.p[pi].cta0 && static_cast<int>(blockIdx.x) < B.p[pi].cta0 + B.p[pi].ncta)) ++pi;
+  const CoopProb &P = B.p[pi];
+  const int cl = blockIdx.x - P.cta0;
+  const unsigned members = static_cast<unsigned>(B.nsync);
+
+  // mu = 1e-9 trace(G), computed identically by every CTA of the problem
+  {
+    float tr = 0.f;
+    for (int i = t; i < P.n; i += 256) tr += __ldg(P.G + i + static_cast<long long>(P.n) * i);
+    red[t] = tr;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+      if (t < w) red[t] += red[t + w];
+      __syncthreads();
+    }
+  }
+  const float mu = 1e-9f * fmaxf(red[0], 0.f);
+  // start block rows
+  {
+    const int rb = cl * P.rows, re = min(P.n, rb + P.rows);
+    for (int e = t; e < (re - rb) * P.s; e += 256) {
+      const int i = rb + e % (re - rb), j = e / (re - rb);
+      const long long idx = i + static_cast<long long>(P.n) * j;
+      P.buf[0][idx] = P.start ? P.start[idx] : gaussian(P.seed, P.stream_id, static_cast<unsigned long long>(idx));
+    }
+  }
+  if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
+
+  auto reduce_and_factor = [&](float shift) -> bool {
+    if (!grid_barrier(B.bar, members, B.err, &s_ok)) return false;
+    coop_reduce(B);
+    if (!grid_barrier(B.bar, members, B.err, &s_ok)) return false;
+    coop_load_S(P, Sd);
+    factor_transform(Sd, P.s, shift, ring + 2 * ESMAX, ds, piv, Rs);
+    return true;
+  };
+
+  int cur = 0;
+  bool ident = true;
+  for (int it = 0; it < B.iters; ++it) {
+    coop_step(P, cl, 0, P.buf[cur], P.buf[cur ^ 1], nullptr, ident, mu, Rs, Zs, Qr, ring);
+    if (!reduce_and_factor(1e-5f)) return;
+    ident = false;
+    cur ^= 1;
+  }
+  // three CholeskyQR transforms: Y_L T_L -> buffer 2, then twice in place
+  coop_step(P, cl, 1, P.buf[cur], P.buf[2], nullptr, ident, 0.f, Rs, Zs, Qr, ring);
+  if (!reduce_and_factor(1e-6f)) return;
+  coop_step(P, cl, 1, P.buf[2], P.buf[2], nullptr, false, 0.f, Rs, Zs, Qr, ring);
+  if (!reduce_and_factor(0.f)) return;
+  // Rayleigh-Ritz: Q = buf2 T -> buf3, G Q -> buf0, H = Q^T G Q
+  coop_step(P, cl, 2, P.buf[2], P.buf[3], P.buf[0], false, 0.f, Rs, Zs, Qr, ring);
+  if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
+  coop_reduce(B);
+  if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
+  if (cl == 0) {
+    coop_load_S(P, Sd);
+    const int s = P.s;
+    for (int e = t; e < SMAX * SMAX; e += 256) {
+      const int i = e % SMAX, j = e / SMAX;
+      float v = 0.f;
+      if (i < s && j < s) v = static_cast<float>(i <= j ? Sd[j * (j + 1) / 2 + i] : Sd[i * (i + 1) / 2 + j]);
+      A[i][j] = v;
+    }
+    __syncthreads();
+    jacobi_smem(A, A2, VV, s, order);
+    for (int e = t; e < s * s; e += 256) {
+      const int i = e % s, r = e / s;
+      P.V[i + s * r] = VV[i][order[r]];
+    }
+    for (int r = t; r < P.K; r += 256) P.theta[r] = A[order[r]][order[r]];
+  }
+  if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
+  // final: U, GU and the residual partials
+  {
+    float (*Vsm)[SMAX + 1] = VV;
+    const int s = P.s;
+    for (int e = t; e < SMAX * SMAX; e += 256) {
+      const int i = e % SMAX, j = e / SMAX;
+      Vsm[i][j] = (i < s && j < s) ? __ldcg(P.V + i + s * j) : 0.f;
+    }
+    for (int j = t; j < SMAX; j += 256) th_sm[j] = j < P.K ? __ldcg(P.theta + j) : 0.f;
+    __syncthreads();
+    coop_final_rows(P, cl, P.buf[3], P.buf[0], Vsm, th_sm, Qr, Zs);
+  }
+  if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
+  if (cl == 0 && t < SMAX) {
+    float a = 0.f;
+    if (t < P.K)
+      for (int c = 0; c < P.ncta; ++c) a += __ldcg(P.colss + static_cast<long long>(c) * SMAX + t);
+    red[t] = sqrtf(a);
+  }
+  __syncthreads();
+  if (cl == 0 && t == 0) {
+    float m = 0.f;
+    for (int j = 0; j < P.K; ++j) m = fmaxf(m, red[j]);
+    const float th = __ldcg(P.theta);
+    P.resid[0] = th > 0.f ? m / th : m;
+  }
+}
+
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+constexpr size_t kJacScratch = sizeof(float) * SMAX * (SMAX + 1);   // dynamic smem of the one-CTA Jacobi kernels
+
 constexpr size_t kRingFloats = NSTAGE * (RB + SMAX) * LDK;
-constexpr size_t kReducerFloats = 2 * ESMAX + SMAX * (SMAX + 1);
+constexpr size_t kReducerFloats = 2 * ESMAX + 2 * SMAX * (SMAX + 1);
 constexpr size_t kStepSmem = sizeof(float) * (SMAX * SMAX + SMAX + 2 * RB * SMAX + 64 * (RB + 1) +
                                               (kRingFloats > kReducerFloats ? kRingFloats : kReducerFloats)) +
                              64;
 
 }  // namespace
 
+namespace {
+size_t coop_workspace_bytes(const EigProblem *probs, int nprob) {
+  size_t b = align256(4 * sizeof(unsigned));
+  for (int i = 0; i < nprob; ++i) {
+    b += 4 * align256(sizeof(float) * static_cast<size_t>(probs[i].n) * SMAX);
+    b += align256(sizeof(float) * kCoopMaxCta * ESMAX * 2);
+    b += align256(sizeof(double) * ESMAX);
+    b += align256(sizeof(float) * SMAX * SMAX);
+    b += align256(sizeof(float) * kCoopMaxCta * SMAX);
+  }
+  return b;
+}
+size_t step_workspace_bytes(const EigProblem *probs, int nprob);
+}  // namespace
+
 size_t eig_workspace_bytes(const EigProblem *probs, int nprob) {
+  const size_t a = coop_workspace_bytes(probs, nprob), b = step_workspace_bytes(probs, nprob);
+  return a > b ? a : b;
+}
+
+namespace {
+size_t step_workspace_bytes(const EigProblem *probs, int nprob) {
   size_t b = 0;
   for (int i = 0; i < nprob; ++i) {
     const int nrb = (probs[i].n + RB - 1) / RB;
@@ -751,6 +1370,7 @@ size_t eig_workspace_bytes(const EigProblem *probs, int nprob) {
   }
   return b;
 }
+}  // namespace
 
 static cudaError_t build_batch(const EigProblem *probs, int nprob, void *ws, size_t ws_bytes, EigBatch &b,
                                int &max_nrb) {
@@ -792,38 +1412,104 @@ static cudaError_t launch_step(const EigBatch &b, int nprob, int max_nrb, StepAr
   return cudaGetLastError();
 }
 
+// Resources of the cooperative solver on the current device (cached).
+static int coop_max_ctas() {
+  static int cached[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  if (cached[dev]) return cached[dev];
+  int sms = 0, occ = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  if (cudaFuncSetAttribute(eig_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(kCoopSmem)) != cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, eig_coop_kernel, 256, kCoopSmem) != cudaSuccess) return 0;
+  const int m = sms * occ;
+  cached[dev] = m < kCoopMaxCta ? m : kCoopMaxCta;
+  return cached[dev];
+}
+
 cudaError_t eig_batched(EigProblem *probs, int nprob, int iters, void *ws, size_t ws_bytes, int *err, cudaStream_t st,
                         int *launches) {
   if (nprob <= 0) return cudaSuccess;
-  (void)err;
-  EigBatch b;
-  int max_nrb = 0;
-  cudaError_t e = build_batch(probs, nprob, ws, ws_bytes, b, max_nrb);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(eig_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kStepSmem));
-  if (e != cudaSuccess) return e;
-  int nl = 0;
-  eig_init_kernel<<<dim3(64, nprob), 256, 0, st>>>(b, 1); ++nl;
-  int cur = 0, tslot = 0, ident = 1;
-  for (int it = 0; it < iters; ++it) {
-    StepArgs a{STEP_ITER, cur, cur ^ 1, 0, tslot, ident, 1, 1e-5f, 1.f};
-    if ((e = launch_step(b, nprob, max_nrb, a, st)) != cudaSuccess) return e;
-    ++nl;
-    ident = 0; tslot ^= 1; cur ^= 1;
+  if (nprob > kMaxProb) return cudaErrorInvalidValue;
+  if (coop_workspace_bytes(probs, nprob) > ws_bytes) return cudaErrorInvalidValue;
+  const int budget = coop_max_ctas();
+  if (budget <= 0) return cudaErrorInvalidConfiguration;
+  CoopBatch B;
+  std::memset(&B, 0, sizeof(B));
+  char *p = static_cast<char *>(ws);
+  B.bar = reinterpret_cast<unsigned *>(p);
+  p += align256(4 * sizeof(unsigned));
+  B.err = err;
+  B.nprob = nprob;
+  B.iters = iters;
+  long long n_iter = 0;
+  int n_direct = 0, n_iterating = 0;
+  for (int i = 0; i < nprob; ++i) {
+    const EigProblem &q = probs[i];
+    if (!q.G || q.s > SMAX || q.s < 1 || q.K > q.s || q.s > q.n) return cudaErrorInvalidValue;
+    if (q.s == q.n) {
+      ++n_direct;
+    } else {
+      n_iter += q.n;
+      ++n_iterating;
+    }
   }
-  // three CholeskyQR transforms: Y_L T_L -> buffer 2, then twice in place
-  StepArgs f1{STEP_APPLY, cur, 2, 0, tslot, ident, 1, 1e-6f, 0.f};
-  if ((e = launch_step(b, nprob, max_nrb, f1, st)) != cudaSuccess) return e;
-  tslot ^= 1;
-  StepArgs f2{STEP_APPLY, 2, 2, 0, tslot, 0, 1, 0.f, 0.f};
-  if ((e = launch_step(b, nprob, max_nrb, f2, st)) != cudaSuccess) return e;
-  tslot ^= 1;
-  StepArgs rr{STEP_RR, 2, 3, 0, tslot, 0, 1, 0.f, 0.f};
-  if ((e = launch_step(b, nprob, max_nrb, rr, st)) != cudaSuccess) return e;
-  eig_final_kernel<<<dim3(max_nrb, nprob), kThreads, 0, st>>>(b, 3, 0);
-  nl += 4;
-  if (launches) *launches += nl;
-  return cudaGetLastError();
+  const int budget_it = budget - n_direct;
+  if (n_iterating > 0 && budget_it < n_iterating) return cudaErrorInvalidConfiguration;
+  int cta = 0, d = 0, ent = 0;
+  for (int i = 0; i < nprob; ++i) {
+    const EigProblem &q = probs[i];
+    CoopProb &c = B.p[i];
+    c.G = q.G; c.n = q.n; c.s = q.s; c.K = q.K;
+    c.U = q.U; c.GU = q.GU; c.theta = q.theta; c.resid = q.resid;
+    c.start = q.start; c.seed = q.seed; c.stream_id = q.stream_id;
+    for (int k = 0; k < 4; ++k) {
+      c.buf[k] = reinterpret_cast<float *>(p);
+      p += align256(sizeof(float) * static_cast<size_t>(q.n) * SMAX);
+    }
+    c.part = reinterpret_cast<float *>(p); p += align256(sizeof(float) * kCoopMaxCta * ESMAX * 2);
+    c.S = reinterpret_cast<double *>(p); p += align256(sizeof(double) * ESMAX);
+    c.V = reinterpret_cast<float *>(p); p += align256(sizeof(float) * SMAX * SMAX);
+    c.colss = reinterpret_cast<float *>(p); p += align256(sizeof(float) * kCoopMaxCta * SMAX);
+    B.ent_off[i] = ent;
+    if (q.s == q.n) {
+      c.cta0 = -1; c.ncta = 0; c.rows = 0;
+      B.direct_idx[d++] = i;
+    } else {
+      int nc = static_cast<int>(static_cast<long long>(budget_it) * q.n / n_iter);
+      nc = nc < 1 ? 1 : nc;
+      const int rows = (q.n + nc - 1) / nc;
+      c.rows = rows;
+      c.ncta = (q.n + rows - 1) / rows;
+      c.cta0 = cta;
+      cta += c.ncta;
+      ent += q.s * (q.s + 1) / 2;
+    }
+  }
+  B.ent_off[nprob] = ent;
+  B.ent_total = ent;
+  B.nsync = cta;
+  const int grid = cta + n_direct;
+  if (grid > budget) return cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaMemsetAsync(B.bar, 0, 4 * sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = kCoopSmem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, eig_coop_kernel, B);
+  if (e != cudaSuccess) return e;
+  if (launches) *launches += 1;
+  return cudaSuccess;
 }
 
 // In-place CholeskyQR3 of tall blocks (G == nullptr problems, buffer 0 = the matrix).
@@ -854,14 +1540,28 @@ cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, s
 cudaError_t svd_from_gram_launch(const float *GW, int s, int k1, int k2, float *M1, float *M2, float *Broot,
                                  cudaStream_t st) {
   if (s > SMAX || k1 > s || k2 > s) return cudaErrorInvalidValue;
-  svd_from_gram_kernel<<<1, 256, 0, st>>>(GW, s, k1, k2, M1, M2, Broot);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(svd_from_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(kJacScratch));
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  svd_from_gram_kernel<<<1, 256, kJacScratch, st>>>(GW, s, k1, k2, M1, M2, Broot);
   return cudaGetLastError();
 }
 
 cudaError_t transfer_eig_launch(const float *WG, int kw, int kt, int kc, int t_is_left, float *M, float *Broot,
                                 cudaStream_t st) {
   if (kt > SMAX || kc > kw || kt > kw) return cudaErrorInvalidValue;
-  transfer_eig_kernel<<<1, 256, 0, st>>>(WG, kw, kt, kc, t_is_left, M, Broot);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(transfer_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(kJacScratch));
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  transfer_eig_kernel<<<1, 256, kJacScratch, st>>>(WG, kw, kt, kc, t_is_left, M, Broot);
   return cudaGetLastError();
 }
 
