@@ -234,6 +234,7 @@ struct GemmReq {
   bool symmetric = false;
   bool allow_split = true;
   bool fold = false;                // tcgen05 only: b16 is a high/low split (GemmArgs::fold)
+  int mt_tc = 1;                    // tcgen05 only: 2 = 256-row tiles (GemmArgs::mt)
 };
 
 // D = A B^T over the tiles: tcgen05 on the BF16 operands when the context
@@ -247,10 +248,11 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
     if (!tc_gemm_supported(probe, q.bn_tc, &why)) use_tc = false;
   }
   const int bn = use_tc ? q.bn_tc : q.bn_simt;
+  const int mt = use_tc ? q.mt_tc : 1;
   TileGen gen;
   if (q.tiles_kind == TILES_ROWS) gen = make_rows_gen(q.t_rows, q.t_cols, bn);
   else if (q.tiles_kind == TILES_SLABS) gen = make_slabs_gen(q.t_L, q.t_R, q.t_cols, bn);
-  else if (!make_gram_gen(q.t_n, bn, &gen)) return fail(HT_ERR_UNSUPPORTED, "Gram larger than 32768");
+  else if (!make_gram_gen(q.t_n, bn, &gen, 128 * mt)) return fail(HT_ERR_UNSUPPORTED, "Gram larger than 32768");
   const int nt = gen.count;
   int splits = 1;
   if (q.allow_split && nt < sm_count()) splits = std::max(1, sm_count() / nt);
@@ -267,7 +269,7 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
   }
   const bool partial = splits > 1 || q.out_mode == OUT_PARTIAL;
   const size_t mark = c.ar.off;
-  float *part = partial ? c.ar.take<float>(static_cast<size_t>(splits) * nt * 128 * bn) : nullptr;
+  float *part = partial ? c.ar.take<float>(static_cast<size_t>(splits) * nt * gen.bm * bn) : nullptr;
   if (c.dry()) {
     c.ar.off = mark;
     return HT_OK;
@@ -284,6 +286,7 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
   g.ld_out = q.ld_out;
   g.err = c.err;
   g.fold = (use_tc && q.fold) ? 1 : 0;
+  g.mt = mt;
   if (use_tc) {
     HT_CUDA(tc_gemm_launch(g, bn, c.st));
     c.path |= 1;
@@ -307,6 +310,7 @@ ht_status_t gram(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x
   if (x16) q.a16 = q.b16 = gram_operand(v, x16);
   else q.a16.ptr = q.b16.ptr = nullptr;
   q.bn_tc = v.N >= 256 ? 256 : (v.N > 64 ? 128 : 64);
+  q.mt_tc = v.N >= 256 ? 2 : 1;   // 256 x 256 tiles, diagonal ones loading a single panel
   q.bn_simt = v.N > 64 ? 128 : 64;
   q.tiles_kind = TILES_GRAM;
   q.t_n = v.N;

@@ -53,6 +53,7 @@ enum TileKind : int {
 constexpr int kMaxGramRows = 256;   // n <= 32768
 struct TileGen {
   int kind, count, bn, cols;
+  int bm;                            // rows per tile: 128, or 256 for the paired-accumulator Gram tiles
   long long rows, L, R, n;
   int ni;                            // gram: number of 128-row blocks
   int prefix[kMaxGramRows + 1];      // gram: tiles before row block i
@@ -72,6 +73,9 @@ struct GemmArgs {
   // BN/2 rows each (a BF16 matrix split into high and low parts) and the
   // epilogue writes column j as acc[j] + acc[j + BN/2].
   int fold = 0;
+  // tcgen05 path: 2 = each CTA computes a 256-row tile as two 128-row
+  // accumulators that share every B stage (TileGen::bm must be 256)
+  int mt = 1;
 };
 
 // tcgen05 path (BF16 operands), BM = 128, BN in {64, 128, 256}.
@@ -86,13 +90,14 @@ long tc_num_kblocks(const Operand &a);
 cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s);
 long simt_k_total(const Operand &a);
 
-// Sum split-K partial tiles.  mode 0: symmetric Gram (tiles on/above the
-// diagonal, mirror into the lower triangle); mode 1: plain column-major.
+// Sum split-K partial tiles ([splits][tiles][gen.bm][bn]).  mode 0: symmetric
+// Gram (tiles on/above the diagonal, mirror into the lower triangle); mode 1:
+// plain column-major.
 cudaError_t reduce_partials_launch(const float *partial, const TileGen &gen, int splits, int bn, float *out,
                                    long long ld_out, int symmetric, cudaStream_t s);
 TileGen make_rows_gen(long long rows, int cols, int bn);
 TileGen make_slabs_gen(long long L, long long R, int cols, int bn);
-bool make_gram_gen(long long n, int bn, TileGen *g);
+bool make_gram_gen(long long n, int bn, TileGen *g, int bm = 128);
 
 // --------------------------------------------------------------- small ops
 cudaError_t convert_bf16_launch(const float *x, __nv_bfloat16 *xb, long long n, double *sumsq_partials,

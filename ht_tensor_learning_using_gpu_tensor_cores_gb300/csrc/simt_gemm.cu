@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p, const T
 // Sum partial tiles [splits][num_tiles][128][bn] in a fixed order.
 __global__ void reduce_partials_kernel(const float *__restrict__ part, const TileGen gen, int num_tiles, int splits,
                                        int bn, float *__restrict__ out, long long ld, int symmetric) {
-  const long long per_tile = 128ll * bn;
+  const long long per_tile = static_cast<long long>(gen.bm) * bn;
   const long long total = per_tile * num_tiles;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
        idx += (long long)gridDim.x * blockDim.x) {
@@ -320,7 +320,7 @@ cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s) {
 
 cudaError_t reduce_partials_launch(const float *partial, const TileGen &gen, int splits, int bn, float *out,
                                    long long ld_out, int symmetric, cudaStream_t s) {
-  const long long total = 128ll * bn * gen.count;
+  const long long total = static_cast<long long>(gen.bm) * bn * gen.count;
   int grid = static_cast<int>((total + 255) / 256);
   if (grid > 152 * 16) grid = 152 * 16;
   reduce_partials_kernel<<<grid, 256, 0, s>>>(partial, gen, gen.count, splits, bn, out, ld_out, symmetric);
@@ -330,6 +330,7 @@ cudaError_t reduce_partials_launch(const float *partial, const TileGen &gen, int
 TileGen make_rows_gen(long long rows, int cols, int bn) {
   TileGen g{};
   g.kind = TILES_ROWS;
+  g.bm = 128;
   g.rows = rows;
   g.cols = cols;
   g.bn = bn;
@@ -339,6 +340,7 @@ TileGen make_rows_gen(long long rows, int cols, int bn) {
 
 TileGen make_slabs_gen(long long L, long long R, int cols, int bn) {
   TileGen g{};
+  g.bm = 128;
   g.kind = TILES_SLABS;
   g.L = L;
   g.R = R;
@@ -348,18 +350,19 @@ TileGen make_slabs_gen(long long L, long long R, int cols, int bn) {
   return g;
 }
 
-bool make_gram_gen(long long n, int bn, TileGen *g) {
+bool make_gram_gen(long long n, int bn, TileGen *g, int bm) {
   *g = TileGen{};
   g->kind = TILES_GRAM;
   g->n = n;
   g->bn = bn;
-  const long long ni = (n + 127) / 128, nj = (n + bn - 1) / bn;
+  g->bm = bm;
+  const long long ni = (n + bm - 1) / bm, nj = (n + bn - 1) / bn;
   if (ni > kMaxGramRows) return false;
   g->ni = static_cast<int>(ni);
   int c = 0;
   for (long long i = 0; i < ni; ++i) {
-    // first column block that reaches the diagonal: bn*(j+1) - 1 >= 128*i
-    long long j0 = (128 * i + 1 + bn - 1) / bn - 1;
+    // first column block that reaches the diagonal: bn*(j+1) - 1 >= bm*i
+    long long j0 = (static_cast<long long>(bm) * i + 1 + bn - 1) / bn - 1;
     if (j0 < 0) j0 = 0;
     g->prefix[i] = c;
     g->jmin[i] = static_cast<int>(j0);

@@ -34,13 +34,17 @@ constexpr int BM = 128;
 constexpr int BK = 64;
 constexpr int kThreads = 192;
 
-template <int BN>
+// MT = 2: a 256-row tile as two 128-row accumulators (TMEM columns [0, BN)
+// and [BN, 2 BN)) that share every B stage: a third less shared-memory
+// traffic per MMA than 128-row tiles, and a deeper ring in time.
+template <int BN, int MT>
 struct TcCfg {
-  static constexpr int STAGES = BN == 256 ? 4 : (BN == 128 ? 6 : 8);
-  static constexpr uint32_t A_BYTES = BM * BK * 2;
+  static constexpr int STAGES = MT == 2 ? (BN == 256 ? 3 : 4) : (BN == 256 ? 4 : (BN == 128 ? 6 : 8));
+  static constexpr uint32_t A_BYTES = MT * BM * BK * 2;
   static constexpr uint32_t B_BYTES = BN * BK * 2;
   static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
   static constexpr size_t SMEM = 1024 + size_t(STAGES) * STAGE_BYTES + 256;
+  static constexpr uint32_t TMEM_COLS = BN * MT;
 };
 
 struct KParams {
@@ -52,6 +56,7 @@ struct KParams {
   long long ld_out;
   int *err;
   int fold;
+  int same;    // A and B are the same operand: a tile with a_row == b_row loads one panel
 };
 
 // Issue the TMA loads of one operand tile (ROWS x 64 K) for k-block kb.
@@ -77,11 +82,12 @@ HT_DEV uint64_t op_desc(int kind, uint32_t base, int kk) {
   return make_sdesc_sw128(base + kk * 32, 16, 1024);
 }
 
-template <int BN>
+template <int BN, int MT>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    const KParams p, const TileGen gen) {
-  using C = TcCfg<BN>;
+  using C = TcCfg<BN, MT>;
+  constexpr int BMT = BM * MT;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + C::STAGES * C::STAGE_BYTES);
@@ -96,6 +102,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   const Tile tile = gen_tile(gen, tile_idx);
   const int kb0 = split * p.kb_per_split;
   const int nk = max(0, min(p.num_kb, kb0 + p.kb_per_split) - kb0);
+  // a diagonal tile of a Gram with BN == BMT: A's rows are B's rows, so A is
+  // read from B's stage instead of being loaded
+  const bool a_in_b = (BN == BMT) && p.same && tile.a_row == tile.b_row;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < C::STAGES; ++s) {
@@ -109,7 +118,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     tma_prefetch_desc(&tmB);
   }
   if (warp == 1) {
-    tmem_alloc(tmem_slot, BN);
+    tmem_alloc(tmem_slot, C::TMEM_COLS);
     tmem_relinquish();
   }
   tc_fence_before();
@@ -130,8 +139,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         uint8_t *sa = smem + s * C::STAGE_BYTES;
         uint8_t *sb = sa + C::A_BYTES;
-        mbar_arrive_expect_tx(&full[s], C::STAGE_BYTES);
-        load_operand<BM>(&tmA, p.a_kind, p.a_lblocks, kb0 + i, tile.a_row, tile.a_z, sa, &full[s]);
+        mbar_arrive_expect_tx(&full[s], a_in_b ? C::B_BYTES : C::STAGE_BYTES);
+        if (!a_in_b) load_operand<BMT>(&tmA, p.a_kind, p.a_lblocks, kb0 + i, tile.a_row, tile.a_z, sa, &full[s]);
         load_operand<BN>(&tmB, p.b_kind, p.b_lblocks, kb0 + i, tile.b_row, 0, sb, &full[s]);
         issued = i + 1;
       }
@@ -155,11 +164,14 @@ __global__ void __launch_bounds__(kThreads, 1)
           break;
         }
         tc_fence_after();
-        const uint32_t sa = smem_u32(smem + s * C::STAGE_BYTES);
-        const uint32_t sb = sa + C::A_BYTES;
+        const uint32_t sb = smem_u32(smem + s * C::STAGE_BYTES) + C::A_BYTES;
+        const uint32_t sa = a_in_b ? sb : sb - C::A_BYTES;
 #pragma unroll
         for (int kk = 0; kk < BK / 16; ++kk)
-          umma_f16(tmem, op_desc(p.a_kind, sa, kk), op_desc(p.b_kind, sb, kk), idesc, (i | kk) != 0 ? 1u : 0u);
+#pragma unroll
+          for (int mt = 0; mt < MT; ++mt)   // rows mt*128.. of A start 16 KiB apart in both layouts
+            umma_f16(tmem + static_cast<uint32_t>(mt * BN), op_desc(p.a_kind, sa + mt * (BM * BK * 2), kk),
+                     op_desc(p.b_kind, sb, kk), idesc, (i | kk) != 0 ? 1u : 0u);
         umma_commit(&empty[s]);   // frees the stage once these MMAs have read it
       }
       umma_commit(done);           // accumulator complete (or abandoned)
@@ -167,7 +179,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncwarp();
   } else {
     const int q = warp & 3;        // TMEM lane quarter this warp may access
-    const int row = q * 32 + lane;
     bool ok = true;
     if (nk > 0) ok = mbar_wait_bounded(done, 0, abort_flag);
     ok = __all_sync(0xffffffffu, ok);
@@ -176,10 +187,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     const bool have = (nk > 0) && ok;
     const int cols = p.fold ? BN / 2 : BN;
 #pragma unroll 1
-    for (int c0 = 0; c0 < cols; c0 += 32) {
+    for (int it = 0; it < MT * (cols / 32); ++it) {
+      const int mt = it / (cols / 32), c0 = (it % (cols / 32)) * 32;
+      const int row = mt * BM + q * 32 + lane;
       float v[32];
       if (have) {
-        const uint32_t lane_base = tmem + (static_cast<uint32_t>(q * 32) << 16);
+        const uint32_t lane_base = tmem + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(mt * BN);
         tmem_ld_32x32b_x32(lane_base + static_cast<uint32_t>(c0), v);
         tmem_ld_wait();
         if (p.fold) {   // low half of the split B operand: add its product
@@ -194,7 +207,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int j = 0; j < 32; ++j) v[j] = 0.f;
       }
       if (p.out_mode == OUT_PARTIAL) {
-        float *dst = p.out + ((static_cast<size_t>(split) * p.num_tiles + tile_idx) * BM + row) * BN + c0;
+        float *dst = p.out + ((static_cast<size_t>(split) * p.num_tiles + tile_idx) * BMT + row) * BN + c0;
 #pragma unroll
         for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4 *>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
       } else if (row < tile.valid_rows) {
@@ -209,7 +222,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    tmem_dealloc(tmem, BN);
+    tmem_dealloc(tmem, C::TMEM_COLS);
   }
 }
 
@@ -277,12 +290,13 @@ long kblocks_of(const Operand &o) {
   return lb * (o.kind == OP_KM3 ? o.d2 : o.d1);
 }
 
-template <int BN>
+template <int BN, int MT>
 cudaError_t launch_bn(const GemmArgs &g, cudaStream_t s) {
-  using C = TcCfg<BN>;
+  using C = TcCfg<BN, MT>;
+  if (g.gen.bm != BM * MT) return cudaErrorInvalidValue;
   CUtensorMap ma, mb;
   std::string why;
-  if (!make_map(g.a, BM, &ma, &why) || !make_map(g.b, BN, &mb, &why)) return cudaErrorInvalidValue;
+  if (!make_map(g.a, BM * MT, &ma, &why) || !make_map(g.b, BN, &mb, &why)) return cudaErrorInvalidValue;
   KParams p;
   p.a_kind = g.a.kind;
   p.b_kind = g.b.kind;
@@ -297,9 +311,11 @@ cudaError_t launch_bn(const GemmArgs &g, cudaStream_t s) {
   p.ld_out = g.ld_out;
   p.err = g.err;
   p.fold = (g.fold && g.out_mode == OUT_COLMAJOR) ? 1 : 0;
-  cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(C::SMEM));
+  p.same = (g.a.ptr == g.b.ptr && g.a.kind == g.b.kind && g.a.d0 == g.b.d0 && g.a.d1 == g.b.d1 && g.a.d2 == g.b.d2) ? 1 : 0;
+  cudaError_t e =
+      cudaFuncSetAttribute(tc_gemm_kernel<BN, MT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(C::SMEM));
   if (e != cudaSuccess) return e;
-  tc_gemm_kernel<BN><<<g.num_tiles * splits, kThreads, C::SMEM, s>>>(ma, mb, p, g.gen);
+  tc_gemm_kernel<BN, MT><<<g.num_tiles * splits, kThreads, C::SMEM, s>>>(ma, mb, p, g.gen);
   return cudaGetLastError();
 }
 
@@ -330,10 +346,14 @@ bool tc_gemm_supported(const GemmArgs &g, int bn, std::string *why) {
 }
 
 cudaError_t tc_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s) {
+  if (g.mt == 2) {
+    if (bn == 256) return launch_bn<256, 2>(g, s);
+    return cudaErrorInvalidValue;
+  }
   switch (bn) {
-    case 64: return launch_bn<64>(g, s);
-    case 128: return launch_bn<128>(g, s);
-    case 256: return launch_bn<256>(g, s);
+    case 64: return launch_bn<64, 1>(g, s);
+    case 128: return launch_bn<128, 1>(g, s);
+    case 256: return launch_bn<256, 1>(g, s);
     default: return cudaErrorInvalidValue;
   }
 }

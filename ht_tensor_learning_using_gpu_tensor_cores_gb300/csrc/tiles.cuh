@@ -27,11 +27,11 @@ HT_DEV Tile gen_tile(const TileGen &g, int idx) {
     int i = 0;
     while (i + 1 < g.ni && g.prefix[i + 1] <= idx) ++i;
     const int j = g.jmin[i] + (idx - g.prefix[i]);
-    t.a_row = 128 * i;
+    t.a_row = g.bm * i;
     t.b_row = g.bn * j;
-    t.out_row = 128ll * i;
+    t.out_row = static_cast<long long>(g.bm) * i;
     t.out_col = g.bn * j;
-    t.valid_rows = static_cast<int>(min(128ll, g.n - 128ll * i));
+    t.valid_rows = static_cast<int>(min(static_cast<long long>(g.bm), g.n - static_cast<long long>(g.bm) * i));
     t.valid_cols = static_cast<int>(min(static_cast<long long>(g.bn), g.n - static_cast<long long>(g.bn) * j));
   }
   return t;
