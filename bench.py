@@ -177,6 +177,67 @@ def run_reference(args, world, rank):
 
 
 # ------------------------------------------------------------------ GPU leg
+def secondary_configs(ht, synth, torch, stream, steps=10, warmup=3):
+    """c1 (256^3, tree {1},{2,3}, ranks 16, exact HT + 1e-3 noise) and c3 (128^4,
+    balanced tree, leaf ranks 24, interior 48, exact HT + 1e-4 noise): ms per
+    decomposition of the mixed and the plain FP32 paths, device-resident input,
+    and the relative error of each (the noise level is the attainable error).
+    c4 (512 small tensors): tensors/s through the batched C ABI, wall clock per
+    call (graph replay + error readback), and the p50 / p99 relative error."""
+    cfgs = [("c1", (256, 256, 256), ht.left_first_tree_3d([1, 16, 16, 16, 16]), 1e-3),
+            ("c3", (128, 128, 128, 128), ht.balanced_tree_4d([1, 48, 48, 24, 24, 24, 24]), 1e-4)]
+    out = {}
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for name, dims, tree, noise in cfgs:
+        X = synth.exact_ht_device(dims, tree, noise, seed=21, device="cuda")
+        rec = {"dims": list(dims), "ranks": list(tree.ranks), "noise_rel": noise}
+        for prec, key in (("bf16", "mixed"), ("fp32", "plain")):
+            rec[key + "_rel_err"] = ht.decompose(X, tree, precision=prec, compute_error=True).report["rel_err"]
+            for _ in range(warmup):
+                ht.decompose(X, tree, precision=prec)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            for _ in range(steps):
+                ht.decompose(X, tree, precision=prec)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            rec[key + "_ms"] = ev0.elapsed_time(ev1) / steps
+        rec["speedup_vs_plain_fp32"] = rec["plain_ms"] / rec["mixed_ms"]
+        out[name] = rec
+        del X
+    # c4: 512 tensors, dims ~ U[32, 160], ranks ~ U[8, 16], exact HT + 1e-3 noise,
+    # through the batched C ABI (the recorded CUDA graph replayed on fixed buffers)
+    fam = synth.batch_family(512, seed=31, device="cuda")
+    trees = [t for _, t in fam]
+    xs = [x for x, _ in fam]
+    dims = [tuple(reversed(x.shape)) for x in xs]
+    rec = {"tensors": len(xs), "dims": "U[32,160]^3", "ranks": "U[8,16]", "noise_rel": 1e-3,
+           "input_bytes": int(sum(x.numel() for x in xs) * 4)}
+    for prec, key in (("bf16", "mixed"), ("fp32", "plain")):
+        bd = ht.BatchDecomposer(trees, dims, precision=prec, compute_error=True)
+        _, rep = bd(xs)                      # records the graph
+        for _ in range(2):
+            _, rep = bd(xs)
+        torch.cuda.synchronize()
+        reps = 5
+        t0 = time.perf_counter()
+        dev_ms = []
+        for _ in range(reps):
+            _, rep = bd(xs)
+            dev_ms.append(rep["ms_total"])
+        wall = (time.perf_counter() - t0) / reps
+        rec[key] = {"tensors_per_s": len(xs) / wall, "ms_per_batch": wall * 1e3,
+                    "device_ms_per_batch": statistics.median(dev_ms), "rel_err_p50": rep["rel_err_p50"],
+                    "rel_err_p99": rep["rel_err_p99"], "graph_replayed": rep["graph_replayed"],
+                    "lanes": rep["lanes"], "gpu_launches_per_batch": rep["gpu_launches"]}
+        del bd
+    ht.release_batch()
+    out["c4"] = rec
+    del fam, xs
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -260,6 +321,9 @@ def run_ours(args, world, rank, local):
     d2h = sum(int(np.asarray(a).nbytes) for a in list(res_h.U.values()) + list(res_h.B.values()))
     h2d = n * n * n * 4
 
+    # ---- the other single-tensor configurations (not the headline): c1 and c3
+    others = secondary_configs(ht, synth, torch, stream) if rank == 0 else None
+
     # ---- roofline of the dominant kernel: the BF16 Gram (3 launches per step)
     pk = peaks()
     grams_ms = statistics.median([s["grams"] for s in stage_ms])
@@ -288,6 +352,7 @@ def run_ours(args, world, rank, local):
                          "frac": achieved / pk["bf16_tflops"], "traffic": None,
                          "peak_source": pk["source"] + " bf16 burst"},
             "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
+            "other_configs": others,
         }
         print(json.dumps(line), flush=True)
 

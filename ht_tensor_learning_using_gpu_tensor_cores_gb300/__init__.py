@@ -26,14 +26,14 @@ from typing import Dict, Optional, Sequence
 import numpy as np
 
 from . import synth
-from ._lib import (FLAG_COMPUTE_ERROR, HTError, HtConfig, HtReport, HtTree, LEAF_GRAM, PREC_BF16, PREC_FP32, check,
-                   lib)
+from ._lib import (FLAG_COMPUTE_ERROR, HTError, HtBatchReport, HtConfig, HtReport, HtTree, LEAF_GRAM, PREC_BF16,
+                   PREC_FP32, check, lib)
 from .tree import (DimTree, balanced_tree_4d, left_first_tree_3d, middle_tree_3d, reference_tree_3d,
                    uniform_ranks)
 
 __all__ = ["DimTree", "reference_tree_3d", "left_first_tree_3d", "middle_tree_3d", "balanced_tree_4d",
            "uniform_ranks", "decompose", "reconstruct_error", "htd", "htd4", "HTResult", "HTError", "synth",
-           "workspace_size", "release_workspace", "kernel_launch_count"]
+           "workspace_size", "release_workspace", "kernel_launch_count", "BatchDecomposer", "release_batch"]
 
 _PREC = {"fp32": PREC_FP32, "bf16": PREC_BF16}
 
@@ -194,6 +194,83 @@ def decompose(x, tree: DimTree, dims: Optional[Sequence[int]] = None, precision:
     }
     del keep
     return HTResult(tree, dims, U, B, report)
+
+
+class BatchDecomposer:
+    """Many tensors per call through ht_decompose_batched, with output buffers
+    that stay fixed between calls so that the recorded CUDA graph is replayed.
+
+        bd = BatchDecomposer(trees, dims_list, precision="bf16", compute_error=True)
+        results, report = bd(tensors)      # tensors: contiguous float32 CUDA tensors,
+                                           # shaped dims[::-1] (column-major memory)
+
+    The input tensors must also stay the same objects (same device addresses)
+    for the graph to be replayed; new contents are fine."""
+
+    def __init__(self, trees: Sequence[DimTree], dims: Sequence[Sequence[int]], precision: str = "bf16",
+                 compute_error: bool = True, oversample: int = 16, eig_iters: int = 10, seed: int = 1234,
+                 device=None):
+        import torch
+        if len(trees) != len(dims) or not trees:
+            raise ValueError("one tree per tensor, at least one tensor")
+        order = trees[0].order
+        if any(t.order != order for t in trees):
+            raise ValueError("every tensor of a batch has the same order")
+        self.trees = list(trees)
+        self.dims = [tuple(int(v) for v in d) for d in dims]
+        for t, d in zip(self.trees, self.dims):
+            t.check_ranks(d)
+        self.order = order
+        self.count = len(trees)
+        self.compute_error = compute_error
+        flags = FLAG_COMPUTE_ERROR if compute_error else 0
+        self.cfg, self._keep = _config(precision, oversample, eig_iters, 1, seed, flags, None, 0.0)
+        dev = torch.device("cuda") if device is None else torch.device(device)
+        self.U, self.B = [], []
+        self.uptr = (c_void_p * (7 * self.count))()
+        self.bptr = (c_void_p * (7 * self.count))()
+        like = torch.empty(1, device=dev)
+        for i, (t, d) in enumerate(zip(self.trees, self.dims)):
+            U, B, up, bp = _out_buffers(t, d, like)
+            self.U.append(U)
+            self.B.append(B)
+            for k in range(7):
+                self.uptr[7 * i + k] = up[k]
+                self.bptr[7 * i + k] = bp[k]
+        self.ts = (HtTree * self.count)(*[_tree_struct(t) for t in self.trees])
+        self.cdims = (c_long * (order * self.count))(*[v for d in self.dims for v in d])
+        self.xptr = (c_void_p * self.count)()
+        self.rel = (c_double * self.count)()
+
+    def __call__(self, tensors, stream=None):
+        import torch
+        if len(tensors) != self.count:
+            raise ValueError(f"expected {self.count} tensors")
+        for i, (x, d) in enumerate(zip(tensors, self.dims)):
+            if not (_is_torch(x) and x.is_cuda and x.dtype == torch.float32 and x.is_contiguous()):
+                raise TypeError("batched inputs must be contiguous float32 CUDA tensors")
+            if tuple(reversed(x.shape)) != d and x.numel() != int(np.prod(d)):
+                raise ValueError(f"tensor {i} does not match dims {d}")
+            self.xptr[i] = x.data_ptr()
+        if stream is None:
+            stream = torch.cuda.current_stream(tensors[0].device).cuda_stream
+        rep = HtBatchReport()
+        check(lib().ht_decompose_batched(self.count, self.xptr, self.cdims, self.order, self.ts, ctypes.byref(self.cfg),
+                                         self.uptr, self.bptr, self.rel if self.compute_error else None,
+                                         ctypes.byref(rep), c_void_p(stream)))
+        results = []
+        for i in range(self.count):
+            report = {"rel_err": self.rel[i] if self.compute_error else None}
+            results.append(HTResult(self.trees[i], self.dims[i], self.U[i], self.B[i], report))
+        summary = {"rel_err_p50": rep.rel_err_p50, "rel_err_p99": rep.rel_err_p99, "rel_err_max": rep.rel_err_max,
+                   "ms_total": rep.ms_total, "gpu_launches": rep.gpu_launches, "graph_replayed": bool(rep.graph_replayed),
+                   "lanes": rep.lanes, "note": (lib().ht_last_error() or b"").decode()}
+        return results, summary
+
+
+def release_batch():
+    """Free the batched path's cached CUDA graph and workspace."""
+    check(lib().ht_release_batch())
 
 
 def reconstruct_error(x, tree: DimTree, U: Dict[int, object], B: Dict[int, object],

@@ -23,7 +23,8 @@ FLAG_COMPUTE_ERROR, FLAG_SYNC_TIMING = 1, 2
 EXPORTED = ["ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
             "ht_decompose", "ht_reconstruct_error", "ht_workspace_size", "ht_release_workspace",
             "ht_status_string", "ht_last_error", "ht_kernel_launch_count", "htd", "htd4",
-            "ht_mode_gram", "ht_mode_product", "ht_corange_product", "ht_mode_gram_noalloc"]
+            "ht_mode_gram", "ht_mode_product", "ht_corange_product", "ht_mode_gram_noalloc",
+            "ht_decompose_batched", "ht_release_batch"]
 
 
 class HtTree(Structure):
@@ -40,6 +41,11 @@ class HtConfig(Structure):
 class HtReport(Structure):
     _fields_ = [("rel_err", c_double), ("norm_x", c_double), ("ms_total", c_float), ("ms_stage", c_float * 8),
                 ("eig_residual", c_double * MAX_NODES), ("gpu_launches", c_int), ("path_flags", c_int)]
+
+
+class HtBatchReport(Structure):
+    _fields_ = [("rel_err_p50", c_double), ("rel_err_p99", c_double), ("rel_err_max", c_double),
+                ("ms_total", c_float), ("gpu_launches", c_int), ("graph_replayed", c_int), ("lanes", c_int)]
 
 
 class HTError(RuntimeError):
@@ -86,9 +92,13 @@ def lib():
     L.ht_mode_product.argtypes = [c_void_p, POINTER(c_long), c_int, c_int, c_int, c_void_p, c_int, c_int, c_void_p,
                                   c_void_p]
     L.ht_mode_gram_noalloc.argtypes = [c_void_p, POINTER(c_long), c_int, c_int, c_int, c_void_p, c_void_p]
+    L.ht_decompose_batched.argtypes = [c_int, POINTER(c_void_p), POINTER(c_long), c_int, POINTER(HtTree),
+                                       POINTER(HtConfig), POINTER(c_void_p), POINTER(c_void_p), POINTER(c_double),
+                                       POINTER(HtBatchReport), c_void_p]
+    L.ht_release_batch.argtypes = []
     L.ht_corange_product.argtypes = [c_void_p, POINTER(c_long), c_int, c_int, c_int, c_void_p, c_int, c_int,
                                      c_void_p, c_void_p]
-    for name in ("ht_mode_gram", "ht_mode_gram_noalloc", "ht_mode_product", "ht_corange_product", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
+    for name in ("ht_decompose_batched", "ht_release_batch", "ht_mode_gram", "ht_mode_gram_noalloc", "ht_mode_product", "ht_corange_product", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
                  "ht_decompose", "ht_reconstruct_error", "ht_workspace_size", "ht_release_workspace"):
         getattr(L, name).restype = c_int
     _lib = L

@@ -184,6 +184,7 @@ struct Ctx {
   int launches = 0;
   int path = 0;         // bit 0 tcgen05, bit 1 SIMT
   bool tc = false;
+  int eig_ctas = 0;     // cap on the cooperative eigen-solver's grid (0 = every SM)
   bool dry() const { return ar.dry; }
 };
 
@@ -557,7 +558,7 @@ ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const 
     const size_t eb = eig_workspace_bytes(ep, order);
     void *ews = c.ar.take<char>(eb);
     if (!ews) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (eig)");
-    if (!c.dry()) HT_CUDA(eig_batched(ep, order, iters, ews, eb, c.err, c.st, &c.launches));
+    if (!c.dry()) HT_CUDA(eig_batched(ep, order, iters, ews, eb, c.err, c.st, &c.launches, c.eig_ctas));
     c.ar.off = mark;
   }
   tl.mark(c.st);
@@ -775,6 +776,38 @@ struct CallArgs {
   bool want_err;
 };
 
+// The asynchronous part of a call, X already on the device: BF16 copy and
+// ||X||^2 (dsum[0]), the decomposition, the factors copied to the caller's
+// buffers, and the error pass (dsum[1]) when asked.  No host synchronisation,
+// so it can be captured into a CUDA graph.
+ht_status_t enqueue_body(Ctx &c, const Tree &T, const ht_config_t &cfg, const float *xd, const CallArgs &a,
+                         double *nparts, double *dsum, Timeline &tl, Result &res) {
+  long long total = 1;
+  for (int m = 0; m < a.order; ++m) total *= a.dims[m];
+  __nv_bfloat16 *xb = nullptr;
+  if (c.tc) {
+    xb = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
+    if (!xb) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (bf16 tensor)");
+    if (!c.dry()) HT_CUDA(convert_bf16_launch(xd, xb, total, nparts, 1024, c.st));
+  } else if (!c.dry()) {
+    HT_CUDA(sumsq_launch(xd, total, nparts, 1024, c.st));
+  }
+  if (!c.dry()) {
+    HT_CUDA(sumsq_finish_launch(nparts, 1024, dsum, c.st));
+    c.launches += 2;
+  }
+  tl.mark(c.st);
+  HT_TRY(decompose_core(c, T, cfg, xd, xb, a.dims, a.order, res, tl));
+  // outputs to the caller's buffers (host or device)
+  for (int t = 0; t < T.n_nodes; ++t) {
+    float *dst = T.leaf(t) ? a.U[t] : a.B[t];
+    const float *src = T.leaf(t) ? res.U[t] : res.B[t];
+    if (dst && !c.dry()) HT_CUDA(cudaMemcpyAsync(dst, src, factor_count(T, a.dims, t) * sizeof(float), cudaMemcpyDefault, c.st));
+  }
+  if (a.want_err) HT_TRY(error_core(c, T, xd, a.dims, a.order, res.U, res.B, dsum + 1));
+  return HT_OK;
+}
+
 ht_status_t run_call(Ctx &c, const Tree &T, const ht_config_t &cfg, const CallArgs &a, ht_report_t *rep) {
   long long total = 1;
   for (int m = 0; m < a.order; ++m) total *= a.dims[m];
@@ -812,28 +845,8 @@ ht_status_t run_call(Ctx &c, const Tree &T, const ht_config_t &cfg, const CallAr
   }
   if (tl.on) HT_CUDA(cudaEventRecord(h1, c.st));
   tl.mark(c.st);
-  __nv_bfloat16 *xb = nullptr;
-  if (c.tc) {
-    xb = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
-    if (!xb) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (bf16 tensor)");
-    if (!c.dry()) HT_CUDA(convert_bf16_launch(xd, xb, total, nparts, 1024, c.st));
-  } else if (!c.dry()) {
-    HT_CUDA(sumsq_launch(xd, total, nparts, 1024, c.st));
-  }
-  if (!c.dry()) {
-    HT_CUDA(sumsq_finish_launch(nparts, 1024, dsum, c.st));
-    c.launches += 2;
-  }
-  tl.mark(c.st);
   Result res;
-  HT_TRY(decompose_core(c, T, cfg, xd, xb, a.dims, a.order, res, tl));
-  // outputs to the caller's buffers (host or device)
-  for (int t = 0; t < T.n_nodes; ++t) {
-    float *dst = T.leaf(t) ? a.U[t] : a.B[t];
-    const float *src = T.leaf(t) ? res.U[t] : res.B[t];
-    if (dst && !c.dry()) HT_CUDA(cudaMemcpyAsync(dst, src, factor_count(T, a.dims, t) * sizeof(float), cudaMemcpyDefault, c.st));
-  }
-  if (a.want_err) HT_TRY(error_core(c, T, xd, a.dims, a.order, res.U, res.B, dsum + 1));
+  HT_TRY(enqueue_body(c, T, cfg, xd, a, nparts, dsum, tl, res));
   if (c.dry()) return HT_OK;
   double host_sums[2] = {0.0, 0.0};
   HT_CUDA(cudaMemcpyAsync(host_sums, dsum, sizeof(double) * (a.want_err ? 2 : 1), cudaMemcpyDeviceToHost, c.st));
@@ -882,6 +895,81 @@ size_t dry_run_bytes(const Tree &T, const ht_config_t &cfg, const CallArgs &a) {
   d.tc = cfg.precision == HT_PREC_BF16;
   run_call(d, T, cfg, a, nullptr);
   return d.ar.peak + (1 << 20);
+}
+
+// ------------------------------------------------------------ batched path
+constexpr int kLanes = 4;
+
+struct BatchState {
+  std::vector<unsigned long long> key;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  void *ws = nullptr;
+  size_t ws_bytes = 0;
+  cudaStream_t lane[kLanes] = {};
+  cudaStream_t cap = nullptr;   // capture origin (the caller's stream may be the legacy stream)
+  cudaEvent_t fork = nullptr, join[kLanes] = {}, t0 = nullptr, t1 = nullptr;
+  double *sums = nullptr;   // device: [count][2] (||X||^2, ||X - Xhat||^2)
+  int *errw = nullptr;      // device: one error word per lane
+  int launches = 0, lanes = 0;
+};
+BatchState g_batch[64];
+std::mutex g_batch_mutex;
+
+void batch_drop_graph(BatchState &b) {
+  if (b.exec) cudaGraphExecDestroy(b.exec);
+  if (b.graph) cudaGraphDestroy(b.graph);
+  b.exec = nullptr;
+  b.graph = nullptr;
+  b.key.clear();
+}
+
+ht_status_t batch_streams(BatchState &b) {
+  if (b.fork) return HT_OK;
+  for (int l = 0; l < kLanes; ++l) {
+    HT_CUDA(cudaStreamCreateWithFlags(&b.lane[l], cudaStreamNonBlocking));
+    HT_CUDA(cudaEventCreateWithFlags(&b.join[l], cudaEventDisableTiming));
+  }
+  HT_CUDA(cudaStreamCreateWithFlags(&b.cap, cudaStreamNonBlocking));
+  HT_CUDA(cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming));
+  HT_CUDA(cudaEventCreate(&b.t0));
+  HT_CUDA(cudaEventCreate(&b.t1));
+  return HT_OK;
+}
+
+// Enqueue every tensor of the batch on the lanes, forked from and joined back
+// into `st`.  Tensor i runs on lane i % lanes, after the previous tensor of
+// that lane, in the lane's workspace region.
+ht_status_t batch_enqueue(BatchState &b, cudaStream_t st, int count, const float *const *x, const long *dims,
+                          int order, const std::vector<Tree> &trees, const ht_config_t &cfg, float *const *U,
+                          float *const *B, bool want_err, size_t lane_bytes, int eig_ctas) {
+  HT_CUDA(cudaMemsetAsync(b.errw, 0, sizeof(int) * kLanes, st));
+  HT_CUDA(cudaEventRecord(b.fork, st));
+  for (int l = 0; l < b.lanes; ++l) HT_CUDA(cudaStreamWaitEvent(b.lane[l], b.fork, 0));
+  b.launches = 0;
+  for (int i = 0; i < count; ++i) {
+    const int l = i % b.lanes;
+    Ctx c;
+    c.st = b.lane[l];
+    c.tc = cfg.precision == HT_PREC_BF16;
+    c.eig_ctas = eig_ctas;
+    c.err = b.errw + l;
+    c.ar.base = static_cast<char *>(b.ws) + static_cast<size_t>(l) * lane_bytes;
+    c.ar.cap = lane_bytes;
+    double *nparts = c.ar.take<double>(1024);
+    if (!nparts) return fail(HT_ERR_OUT_OF_MEMORY, "batch workspace too small");
+    CallArgs a{x[i], true, dims + static_cast<size_t>(i) * order, order, U + static_cast<size_t>(i) * HT_MAX_NODES,
+               B + static_cast<size_t>(i) * HT_MAX_NODES, want_err};
+    Timeline tl;
+    Result res;
+    HT_TRY(enqueue_body(c, trees[i], cfg, x[i], a, nparts, b.sums + 2 * static_cast<size_t>(i), tl, res));
+    b.launches += c.launches;
+  }
+  for (int l = 0; l < b.lanes; ++l) {
+    HT_CUDA(cudaEventRecord(b.join[l], b.lane[l]));
+    HT_CUDA(cudaStreamWaitEvent(st, b.join[l], 0));
+  }
+  return HT_OK;
 }
 
 }  // namespace
@@ -1000,6 +1088,179 @@ ht_status_t ht_decompose(const float *x, const long *dims, int order, const ht_t
   c.ar.base = static_cast<char *>(ws);
   c.ar.cap = bytes;
   return run_call(c, T, cfg, a, report);
+}
+
+ht_status_t ht_decompose_batched(int count, const float *const *x, const long *dims, int order,
+                                 const ht_tree_t *trees, const ht_config_t *cfg_in, float *const *U, float *const *B,
+                                 double *rel_err, ht_batch_report_t *report, void *stream) {
+  if (count < 1 || !x || !dims || !trees || !U || !B) return fail(HT_ERR_INVALID_ARG, "NULL argument or count < 1");
+  g_last_error.clear();   // after a successful call: empty, or why no graph was recorded
+  ht_config_t cfg;
+  if (cfg_in) cfg = *cfg_in;
+  else ht_config_default(&cfg);
+  if (cfg.precision != HT_PREC_FP32 && cfg.precision != HT_PREC_BF16) return fail(HT_ERR_INVALID_ARG, "unknown precision");
+  if (cfg.leaf_method != HT_LEAF_GRAM) return fail(HT_ERR_UNSUPPORTED, "only the Gram leaf method is implemented");
+  if (cfg.oversample < 0 || cfg.eig_iters < 0) return fail(HT_ERR_INVALID_ARG, "negative oversample / eig_iters");
+  const bool want_err = (cfg.flags & HT_FLAG_COMPUTE_ERROR) != 0;
+  HT_TRY(check_device());
+  int dev = 0;
+  HT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(HT_ERR_INVALID_ARG, "device index out of range");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> lk(g_batch_mutex);
+  BatchState &b = g_batch[dev];
+  // identity of the batch: shapes, trees, config and every pointer
+  std::vector<unsigned long long> key;
+  key.reserve(static_cast<size_t>(count) * (order + 2 * HT_MAX_NODES + 2 + sizeof(ht_tree_t) / 4) + 16);
+  key.push_back(static_cast<unsigned long long>(count));
+  key.push_back(static_cast<unsigned long long>(order));
+  {
+    const unsigned char *cb = reinterpret_cast<const unsigned char *>(&cfg);
+    for (size_t q = 0; q < sizeof(cfg); ++q) key.push_back(cb[q]);
+  }
+  for (int i = 0; i < count; ++i) {
+    key.push_back(reinterpret_cast<uintptr_t>(x[i]));
+    for (int m = 0; m < order; ++m) key.push_back(static_cast<unsigned long long>(dims[static_cast<size_t>(i) * order + m]));
+    const int *tw = reinterpret_cast<const int *>(&trees[i]);
+    for (size_t q = 0; q < sizeof(ht_tree_t) / sizeof(int); ++q) key.push_back(static_cast<unsigned long long>(tw[q]));
+    for (int t = 0; t < HT_MAX_NODES; ++t) {
+      key.push_back(reinterpret_cast<uintptr_t>(U[static_cast<size_t>(i) * HT_MAX_NODES + t]));
+      key.push_back(reinterpret_cast<uintptr_t>(B[static_cast<size_t>(i) * HT_MAX_NODES + t]));
+    }
+  }
+  const bool replay = b.exec && key == b.key;
+  if (!replay) {
+    std::vector<Tree> T(count);
+    size_t lane_bytes = 0;
+    for (int i = 0; i < count; ++i) {
+      const long *di = dims + static_cast<size_t>(i) * order;
+      HT_TRY(parse_tree(&trees[i], di, order, T[i]));
+      if (!is_device_ptr(x[i])) return fail(HT_ERR_INVALID_ARG, "x[" + std::to_string(i) + "] must be device memory");
+      for (int t = 0; t < T[i].n_nodes; ++t) {
+        float *o = T[i].leaf(t) ? U[static_cast<size_t>(i) * HT_MAX_NODES + t] : B[static_cast<size_t>(i) * HT_MAX_NODES + t];
+        if (!o || !is_device_ptr(o))
+          return fail(HT_ERR_INVALID_ARG, "output of node " + std::to_string(t) + " of tensor " + std::to_string(i) +
+                                              " must be device memory");
+      }
+      CallArgs a{x[i], true, di, order, U + static_cast<size_t>(i) * HT_MAX_NODES, B + static_cast<size_t>(i) * HT_MAX_NODES,
+                 want_err};
+      lane_bytes = std::max(lane_bytes, dry_run_bytes(T[i], cfg, a) + 1024 * sizeof(double));
+    }
+    lane_bytes = (lane_bytes + 4095) & ~size_t(4095);
+    batch_drop_graph(b);
+    HT_TRY(batch_streams(b));
+    b.lanes = std::min(kLanes, count);
+    const size_t need = static_cast<size_t>(kLanes) * lane_bytes + sizeof(double) * 2 * count + 4096;
+    if (b.ws_bytes < need) {
+      if (b.ws) {
+        HT_CUDA(cudaDeviceSynchronize());
+        HT_CUDA(cudaFree(b.ws));
+        b.ws = nullptr;
+        b.ws_bytes = 0;
+      }
+      HT_CUDA(cudaMalloc(&b.ws, need));
+      b.ws_bytes = need;
+    }
+    char *tail = static_cast<char *>(b.ws) + static_cast<size_t>(kLanes) * lane_bytes;
+    b.errw = reinterpret_cast<int *>(tail);
+    b.sums = reinterpret_cast<double *>(tail + 256);
+    const int eig_ctas = std::max(8, sm_count() / b.lanes);
+    HT_CUDA(tc_prepare());   // one-time kernel attributes outside the capture
+    HT_CUDA(eig_prepare());
+    // record the batch into a graph (captured from a private stream: the
+    // caller's may be the legacy stream); if capture is refused, run it directly
+    bool captured = false;
+    std::string why;
+    cudaError_t ce = cudaStreamBeginCapture(b.cap, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+      const ht_status_t s = batch_enqueue(b, b.cap, count, x, dims, order, T, cfg, U, B, want_err, lane_bytes, eig_ctas);
+      if (s != HT_OK) why = ht_last_error();
+      cudaGraph_t g = nullptr;
+      ce = cudaStreamEndCapture(b.cap, &g);
+      cudaError_t ie = cudaErrorUnknown;
+      if (s == HT_OK && ce == cudaSuccess && g) ie = cudaGraphInstantiate(&b.exec, g, 0);
+      if (s == HT_OK && ce == cudaSuccess && g && ie == cudaSuccess) {
+        b.graph = g;
+        b.key = key;
+        captured = true;
+      } else {   // not capturable here (or a launch failed): run the batch directly below
+        if (why.empty()) why = std::string("capture: ") + cudaGetErrorString(ce != cudaSuccess ? ce : ie);
+        if (g) cudaGraphDestroy(g);
+        b.exec = nullptr;
+        cudaGetLastError();
+      }
+    } else {
+      why = std::string("begin capture: ") + cudaGetErrorString(ce);
+      cudaGetLastError();
+    }
+    if (!captured) g_last_error = "batch ran without a CUDA graph (" + why + ")";
+    if (!captured) {
+      HT_CUDA(cudaEventRecord(b.t0, st));
+      HT_TRY(batch_enqueue(b, st, count, x, dims, order, T, cfg, U, B, want_err, lane_bytes, eig_ctas));
+      HT_CUDA(cudaEventRecord(b.t1, st));
+    }
+    if (captured) {
+      HT_CUDA(cudaEventRecord(b.t0, st));
+      HT_CUDA(cudaGraphLaunch(b.exec, st));
+      HT_CUDA(cudaEventRecord(b.t1, st));
+    }
+  } else {
+    HT_CUDA(cudaEventRecord(b.t0, st));
+    HT_CUDA(cudaGraphLaunch(b.exec, st));
+    HT_CUDA(cudaEventRecord(b.t1, st));
+  }
+  std::vector<double> sums(2 * static_cast<size_t>(count));
+  int errw[kLanes] = {};
+  HT_CUDA(cudaMemcpyAsync(sums.data(), b.sums, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost, st));
+  HT_CUDA(cudaMemcpyAsync(errw, b.errw, sizeof(errw), cudaMemcpyDeviceToHost, st));
+  HT_CUDA(cudaStreamSynchronize(st));
+  HT_CUDA(cudaGetLastError());
+  for (int l = 0; l < kLanes; ++l)
+    if (errw[l] & kErrTimeout) return fail(HT_ERR_TIMEOUT, "a kernel's bounded wait expired; results are invalid");
+  std::vector<double> errs;
+  for (int i = 0; i < count; ++i) {
+    const double nx = sums[2 * static_cast<size_t>(i)], ne = sums[2 * static_cast<size_t>(i) + 1];
+    if (!std::isfinite(nx)) return fail(HT_ERR_NUMERICAL, "tensor " + std::to_string(i) + " contains NaN or Inf");
+    const double e = want_err ? (nx > 0 ? std::sqrt(std::max(ne, 0.0) / nx) : 0.0) : -1.0;
+    if (rel_err) rel_err[i] = e;
+    errs.push_back(e);
+  }
+  g_launches += static_cast<unsigned long long>(b.launches);
+  if (report) {
+    std::memset(report, 0, sizeof(*report));
+    std::vector<double> sorted = errs;
+    std::sort(sorted.begin(), sorted.end());
+    auto rank_pct = [&](double q) {
+      const size_t idx = static_cast<size_t>(std::ceil(q * sorted.size())) - 1;
+      return sorted[std::min(idx, sorted.size() - 1)];
+    };
+    report->rel_err_p50 = want_err ? rank_pct(0.50) : -1.0;
+    report->rel_err_p99 = want_err ? rank_pct(0.99) : -1.0;
+    report->rel_err_max = want_err ? sorted.back() : -1.0;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, b.t0, b.t1);
+    report->ms_total = ms;
+    report->gpu_launches = b.launches;
+    report->graph_replayed = replay ? 1 : 0;
+    report->lanes = b.lanes;
+  }
+  return HT_OK;
+}
+
+ht_status_t ht_release_batch(void) {
+  std::lock_guard<std::mutex> lk(g_batch_mutex);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return HT_OK;
+  }
+  BatchState &b = g_batch[dev];
+  HT_CUDA(cudaDeviceSynchronize());
+  batch_drop_graph(b);
+  if (b.ws) HT_CUDA(cudaFree(b.ws));
+  b.ws = nullptr;
+  b.ws_bytes = 0;
+  return HT_OK;
 }
 
 ht_status_t ht_reconstruct_error(const float *x, const long *dims, int order, const ht_tree_t *tree,

@@ -1429,12 +1429,25 @@ static int coop_max_ctas() {
   return cached[dev];
 }
 
+cudaError_t eig_prepare() {
+  if (coop_max_ctas() <= 0) return cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaFuncSetAttribute(eig_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(kStepSmem));
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(transfer_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(kJacScratch));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(svd_from_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(kJacScratch));
+}
+
 cudaError_t eig_batched(EigProblem *probs, int nprob, int iters, void *ws, size_t ws_bytes, int *err, cudaStream_t st,
-                        int *launches) {
+                        int *launches, int max_ctas) {
   if (nprob <= 0) return cudaSuccess;
   if (nprob > kMaxProb) return cudaErrorInvalidValue;
   if (coop_workspace_bytes(probs, nprob) > ws_bytes) return cudaErrorInvalidValue;
-  const int budget = coop_max_ctas();
+  int budget = coop_max_ctas();
+  if (max_ctas > 0 && max_ctas < budget) budget = max_ctas;
   if (budget <= 0) return cudaErrorInvalidConfiguration;
   CoopBatch B;
   std::memset(&B, 0, sizeof(B));
@@ -1521,8 +1534,12 @@ cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, s
   cudaError_t e = build_batch(probs, nprob, ws, ws_bytes, b, max_nrb);
   if (e != cudaSuccess) return e;
   for (int i = 0; i < nprob; ++i) b.p[i].buf[0] = probs[i].Q;   // operate on the caller's matrix in place
-  e = cudaFuncSetAttribute(eig_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kStepSmem));
-  if (e != cudaSuccess) return e;
+  static bool attr_set = false;
+  if (!attr_set) {
+    e = cudaFuncSetAttribute(eig_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kStepSmem));
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
   int nl = 0;
   eig_init_kernel<<<dim3(1, nprob), 256, 0, st>>>(b, 0);   // zeroes the tickets only
   ++nl;

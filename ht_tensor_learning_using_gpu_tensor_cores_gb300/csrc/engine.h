@@ -83,6 +83,9 @@ struct GemmArgs {
 // TMA tensor maps (strides not multiples of 16 bytes, dims too large).
 bool tc_gemm_supported(const GemmArgs &g, int bn, std::string *why);
 cudaError_t tc_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s);
+// One-time set-up (kernel attributes, the tensor-map encoder) so that later
+// launches can be recorded into a CUDA graph.
+cudaError_t tc_prepare();
 // number of 64-wide K blocks of an operand pair (tcgen05 path)
 long tc_num_kblocks(const Operand &a);
 
@@ -144,8 +147,11 @@ struct EigProblem {
   uint64_t seed, stream_id;
 };
 size_t eig_workspace_bytes(const EigProblem *probs, int nprob);
+// One-time set-up of the eigen-solver kernels (attributes, occupancy).
+cudaError_t eig_prepare();
+// max_ctas > 0 caps the cooperative grid (several batches running at once).
 cudaError_t eig_batched(EigProblem *probs, int nprob, int iters, void *ws, size_t ws_bytes, int *err,
-                        cudaStream_t s, int *launches);
+                        cudaStream_t s, int *launches, int max_ctas = 0);
 // Orthonormalise the columns of tall matrices in place (CholeskyQR, `passes`
 // times; the first pass shifted).  Uses the eigen-solver's workspace layout.
 cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, size_t ws_bytes, cudaStream_t s,

@@ -290,6 +290,19 @@ long kblocks_of(const Operand &o) {
   return lb * (o.kind == OP_KM3 ? o.d2 : o.d1);
 }
 
+// Opt-in shared memory size, set once per instantiation and device.
+template <int BN, int MT>
+cudaError_t set_smem() {
+  static bool done[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (done[dev]) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<BN, MT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(TcCfg<BN, MT>::SMEM));
+  if (e == cudaSuccess) done[dev] = true;
+  return e;
+}
+
 template <int BN, int MT>
 cudaError_t launch_bn(const GemmArgs &g, cudaStream_t s) {
   using C = TcCfg<BN, MT>;
@@ -312,8 +325,7 @@ cudaError_t launch_bn(const GemmArgs &g, cudaStream_t s) {
   p.err = g.err;
   p.fold = (g.fold && g.out_mode == OUT_COLMAJOR) ? 1 : 0;
   p.same = (g.a.ptr == g.b.ptr && g.a.kind == g.b.kind && g.a.d0 == g.b.d0 && g.a.d1 == g.b.d1 && g.a.d2 == g.b.d2) ? 1 : 0;
-  cudaError_t e =
-      cudaFuncSetAttribute(tc_gemm_kernel<BN, MT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(C::SMEM));
+  cudaError_t e = set_smem<BN, MT>();
   if (e != cudaSuccess) return e;
   tc_gemm_kernel<BN, MT><<<g.num_tiles * splits, kThreads, C::SMEM, s>>>(ma, mb, p, g.gen);
   return cudaGetLastError();
@@ -322,6 +334,15 @@ cudaError_t launch_bn(const GemmArgs &g, cudaStream_t s) {
 }  // namespace
 
 long tc_num_kblocks(const Operand &a) { return kblocks_of(a); }
+
+cudaError_t tc_prepare() {
+  if (!encode_fn()) return cudaErrorNotSupported;
+  cudaError_t e;
+  if ((e = set_smem<64, 1>()) != cudaSuccess) return e;
+  if ((e = set_smem<128, 1>()) != cudaSuccess) return e;
+  if ((e = set_smem<256, 1>()) != cudaSuccess) return e;
+  return set_smem<256, 2>();
+}
 
 bool tc_gemm_supported(const GemmArgs &g, int bn, std::string *why) {
   if (bn != 64 && bn != 128 && bn != 256) {

@@ -89,6 +89,38 @@ def exact_ht(dims: Sequence[int], tree: DimTree, noise_rel: float = 0.0, seed: i
     return np.asfortranarray(X.astype(dtype))
 
 
+def exact_ht_device(dims: Sequence[int], tree: DimTree, noise_rel: float = 0.0, seed: int = 0, device="cuda"):
+    """``exact_ht`` assembled on a torch device: the same seeded factors, the
+    noise drawn by torch's generator.  Returns the column-major tensor as a
+    contiguous torch tensor of shape ``dims[::-1]``.  Requires every interior
+    node's left modes to precede its right modes (true of the reference trees)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    U, B = {}, {}
+    for t in tree.leaves():
+        U[t] = _orth(rng, int(dims[tree.modes[t][0]]), tree.ranks[t])
+    for t in [0] + tree.interior():
+        kl, kr = tree.ranks[tree.left[t]], tree.ranks[tree.right[t]]
+        B[t] = rng.standard_normal((kl, kr, tree.ranks[t]))
+    f = lambda a: torch.as_tensor(a, dtype=torch.float32, device=device)
+
+    def basis(t):   # (prod of node dims with the lowest mode slowest) x k_t
+        if tree.is_leaf(t):
+            return f(U[t])
+        L, R = basis(tree.left[t]), basis(tree.right[t])
+        T = torch.einsum("pa,qb,abc->pqc", L, R, f(B[t]))
+        return T.reshape(-1, T.shape[-1])
+
+    l, r = tree.left[0], tree.right[0]
+    L, R = basis(l), basis(r)
+    Xc = (L @ f(B[0]).reshape(L.shape[1], R.shape[1]) @ R.T).reshape(*[int(d) for d in dims])   # X[i0, i1, ...]
+    if noise_rel > 0:
+        g = torch.Generator(device=device).manual_seed(int(seed))
+        rms = torch.sqrt(torch.mean(Xc * Xc))
+        Xc = Xc + noise_rel * rms * torch.randn(Xc.shape, generator=g, device=device)
+    return Xc.permute(*reversed(range(len(dims)))).contiguous()
+
+
 def odeco_factors(n: int, order: int = 3, decay: float = 1.5, seed: int = 0, R: Optional[int] = None):
     """Orthonormal factors A_t (n x R) and weights d_r = +-r**-decay."""
     rng = np.random.default_rng(seed)
@@ -179,8 +211,11 @@ def reference_style(n: int, seed: int = 0) -> Tuple[np.ndarray, List[int]]:
     return np.asfortranarray(X.astype(np.float32)), k
 
 
-def batch_family(count: int, seed: int = 0, dim_range=(32, 160), rank_range=(8, 16), noise_rel: float = 1e-3):
-    """``count`` exact-HT 3rd-order tensors, dims ~ U[dim_range], ranks ~ U[rank_range]."""
+def batch_family(count: int, seed: int = 0, dim_range=(32, 160), rank_range=(8, 16), noise_rel: float = 1e-3,
+                 device=None):
+    """``count`` exact-HT 3rd-order tensors, dims ~ U[dim_range], ranks ~ U[rank_range].
+    With ``device`` the tensors are assembled there (``exact_ht_device``: torch
+    tensors shaped dims[::-1], column-major memory); otherwise numpy arrays."""
     from .tree import reference_tree_3d
     rng = np.random.default_rng(seed)
     out = []
@@ -191,6 +226,8 @@ def batch_family(count: int, seed: int = 0, dim_range=(32, 160), rank_range=(8, 
         r[3] = min(r[3], dims[0]); r[4] = min(r[4], dims[1]); r[2] = min(r[2], dims[2])
         r[1] = min(r[1], r[3] * r[4], dims[2])
         tree = reference_tree_3d(r)
-        X = exact_ht(dims, tree, noise_rel, seed=int(rng.integers(0, 2**31 - 1)))
+        s_i = int(rng.integers(0, 2**31 - 1))
+        X = exact_ht(dims, tree, noise_rel, seed=s_i) if device is None else \
+            exact_ht_device(dims, tree, noise_rel, seed=s_i, device=device)
         out.append((X, tree))
     return out

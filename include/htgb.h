@@ -173,6 +173,36 @@ ht_status_t ht_corange_product(const float *x, const long *dims, int order, int 
 ht_status_t ht_mode_gram_noalloc(const float *x, const long *dims, int order, int lo, int hi, float *G,
                                  void *stream);
 
+/* ------------------------------------------------------------ batched path */
+typedef struct {
+    double rel_err_p50;      /* median relative error over the batch (HT_FLAG_COMPUTE_ERROR) */
+    double rel_err_p99;      /* 99th percentile (nearest rank)                               */
+    double rel_err_max;
+    float ms_total;          /* device time of the batch (CUDA events around the launch)     */
+    int gpu_launches;        /* kernels launched per batch                                   */
+    int graph_replayed;      /* 1 when the cached CUDA graph of an identical batch ran       */
+    int lanes;               /* concurrent streams the batch was spread over                 */
+} ht_batch_report_t;
+
+/* Decompose `count` tensors of the same order in one call.  Replaces the
+ * reference's driver loop that calls htd() once per tensor size
+ * (3D/Opt/ht_init.cu:9-47) for the many-small-tensors case.
+ *   x[i]   DEVICE pointer to tensor i (column-major, dims[i*order .. +order));
+ *   trees  count trees (trees[i] for tensor i);
+ *   U, B   count x HT_MAX_NODES tables of DEVICE output pointers: U[i*HT_MAX_NODES + t]
+ *          and B[i*HT_MAX_NODES + t] as in ht_decompose for tensor i;
+ *   rel_err host array of count (HT_FLAG_COMPUTE_ERROR) or NULL.
+ * The tensors are spread over concurrent streams, each with its own workspace.
+ * The first call records the whole batch into a CUDA graph; a later call with
+ * the same count, dims, trees, config and pointers replays it (fixed buffers,
+ * new contents).  Synchronous with respect to the host. */
+ht_status_t ht_decompose_batched(int count, const float *const *x, const long *dims, int order,
+                                 const ht_tree_t *trees, const ht_config_t *cfg,
+                                 float *const *U, float *const *B, double *rel_err,
+                                 ht_batch_report_t *report, void *stream);
+/* Free the batched path's cached graph and workspace on the current device. */
+ht_status_t ht_release_batch(void);
+
 /* Bytes of device workspace ht_decompose needs for this problem. */
 ht_status_t ht_workspace_size(const long *dims, int order, const ht_tree_t *tree,
                               const ht_config_t *cfg, unsigned long long *bytes);

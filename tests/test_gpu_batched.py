@@ -1,0 +1,90 @@
+"""The batched path (ht_decompose_batched, c4-style many small tensors) against
+single-tensor calls and the FP64 oracle, and the CUDA-graph replay: a second
+call with the same buffers replays the recorded graph and gives the same
+factors; new contents in the same buffers give the new tensors' factors.
+
+Tolerances as in the single-tensor parity tests: |err - err_fp64| <= 1e-5
+(FP32 path), <= 1e-3 (mixed BF16 path).
+"""
+import numpy as np
+import pytest
+import torch
+
+import ht_tensor_learning_using_gpu_tensor_cores_gb300 as ht
+from ht_tensor_learning_using_gpu_tensor_cores_gb300 import synth
+import ht_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp32": 1e-5, "bf16": 1e-3}
+
+
+def to_dev(X):
+    return torch.from_numpy(np.ascontiguousarray(X.transpose(tuple(range(X.ndim))[::-1]))).cuda()
+
+
+@pytest.fixture(scope="module")
+def family():
+    return synth.batch_family(12, seed=5, dim_range=(24, 72), rank_range=(4, 10))
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_batched_matches_oracle_and_single_calls(family, prec):
+    trees = [t for _, t in family]
+    dims = [X.shape for X, _ in family]
+    xs = [to_dev(X) for X, _ in family]
+    bd = ht.BatchDecomposer(trees, dims, precision=prec, compute_error=True)
+    res, rep = bd(xs)
+    torch.cuda.synchronize()
+    errs = []
+    for (X, tree), r in zip(family, res):
+        U = {t: r.U[t].cpu().numpy().astype(np.float64) for t in r.U}
+        B = {t: r.B[t].cpu().numpy().astype(np.float64) for t in r.B}
+        e = O.ht_error(X, tree, U, B)
+        Uo, Bo, _ = O.ht_decompose(X, tree)
+        e64 = O.ht_error(X, tree, Uo, Bo)
+        assert abs(e - e64) <= TOL[prec], (prec, e, e64)
+        assert abs(r.report["rel_err"] - e) <= 1e-5 + 1e-4 * e
+        single = ht.decompose(to_dev(X), tree, precision=prec, compute_error=True)
+        assert abs(single.report["rel_err"] - r.report["rel_err"]) <= (1e-6 if prec == "fp32" else 2e-4)
+        errs.append(r.report["rel_err"])
+    s = np.sort(errs)
+    assert rep["rel_err_p50"] == pytest.approx(s[int(np.ceil(0.5 * len(s))) - 1])
+    assert rep["rel_err_p99"] == pytest.approx(s[int(np.ceil(0.99 * len(s))) - 1])
+    assert rep["rel_err_max"] == pytest.approx(s[-1])
+    assert rep["gpu_launches"] > 0 and rep["lanes"] >= 1
+
+
+def test_graph_replay_same_and_new_contents(family):
+    trees = [t for _, t in family]
+    dims = [X.shape for X, _ in family]
+    xs = [to_dev(X) for X, _ in family]
+    bd = ht.BatchDecomposer(trees, dims, precision="bf16", compute_error=True)
+    r1, rep1 = bd(xs)
+    assert rep1["note"] == "", rep1["note"]   # the batch was recorded into a graph
+    U1 = [{t: r.U[t].cpu().numpy().copy() for t in r.U} for r in r1]
+    e1 = [r.report["rel_err"] for r in r1]
+    r2, rep2 = bd(xs)
+    assert rep2["graph_replayed"], "identical second call must replay the recorded graph"
+    for a, r in zip(U1, r2):
+        for t in a:
+            np.testing.assert_array_equal(a[t], r.U[t].cpu().numpy())
+    # new contents, same buffers: the replay must decompose the new tensors
+
+    for i, (x, (X, tree)) in enumerate(zip(xs, family)):
+        Y = synth.exact_ht(X.shape, tree, noise_rel=1e-2, seed=1000 + i)
+        x.copy_(to_dev(Y))
+    r3, rep3 = bd(xs)
+    assert rep3["graph_replayed"]
+    for i, (x, (X, tree)) in enumerate(zip(xs, family)):
+        single = ht.decompose(x, tree, precision="bf16", compute_error=True)
+        assert abs(single.report["rel_err"] - r3[i].report["rel_err"]) <= 2e-4
+        assert r3[i].report["rel_err"] > 5e-3 > e1[i]   # the 1e-2 noise now dominates
+
+
+
+def test_batched_rejects_host_inputs(family):
+    X, tree = family[0]
+    bd = ht.BatchDecomposer([tree], [X.shape], precision="bf16")
+    with pytest.raises(TypeError):
+        bd([X])
