@@ -178,6 +178,7 @@ def run_reference(args, world, rank):
 
 # ------------------------------------------------------------------ GPU leg
 def secondary_configs(ht, synth, torch, stream, steps=10, warmup=3):
+    import numpy as np
     """c1 (256^3, tree {1},{2,3}, ranks 16, exact HT + 1e-3 noise) and c3 (128^4,
     balanced tree, leaf ranks 24, interior 48, exact HT + 1e-4 noise): ms per
     decomposition of the mixed and the plain FP32 paths, device-resident input,
@@ -235,7 +236,65 @@ def secondary_configs(ht, synth, torch, stream, steps=10, warmup=3):
     out["c4"] = rec
     del fam, xs
     torch.cuda.empty_cache()
+    out["c5"] = learned_sketch_config(ht, synth, torch, stream)
+    torch.cuda.empty_cache()
     return out
+
+
+def learned_sketch_config(ht, synth, torch, stream, n=512, k=24, p=10, n_train=256, n_test=64, steps=2000):
+    """c5: separable-bumps family at n^3, target rank k.  Per-mode sketches of
+    width k+p are trained for `steps` Adam steps (batch 32) by the library's
+    forward/adjoint kernels on the mode Grams of n_train family members (BF16
+    tcgen05 Grams); compared on n_test held-out seeds with the Gaussian start
+    block (the training's initial sketch) and the exact Gram path."""
+    import numpy as np
+    from ht_tensor_learning_using_gpu_tensor_cores_gb300 import learn
+    s = k + p
+    t0 = time.perf_counter()
+    Gtr, ttr = learn.family_grams(range(10000, 10000 + n_train), n, precision="bf16")
+    Gte, tte = learn.family_grams(range(20000, 20000 + n_test), n, precision="bf16")
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sketches, hist = learn.train_mode_sketches(Gtr, ttr, s=s, steps=steps, batch=32, lr=2e-3, seed=0)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    gauss = [learn.gaussian_sketch(n, s, seed=17 * m) for m in range(3)]   # the trainers' initial sketches
+    learned = [learn.to_bf16(S) for S in sketches]
+    rec = {"n": n, "rank": k, "sketch_width": s, "train_grams": 3 * n_train, "heldout_tensors": n_test,
+           "steps": steps, "data_s": t_data, "train_s": t_train,
+           "train_loss_first_last": {m: [hist[m][0], hist[m][-1]] for m in hist}}
+    lg = np.concatenate([learn.heldout_loss(Gte[:, m], tte[:, m], gauss[m]) for m in range(3)])
+    ll = np.concatenate([learn.heldout_loss(Gte[:, m], tte[:, m], learned[m]) for m in range(3)])
+    rec["heldout_missed_energy"] = {"gaussian_mean": float(lg.mean()), "learned_mean": float(ll.mean()),
+                                    "gaussian_p99": float(np.quantile(lg, 0.99)),
+                                    "learned_p99": float(np.quantile(ll, 0.99))}
+    del Gtr, Gte
+    tree = ht.reference_tree_3d([1, k, k, k, k])
+    variants = (("exact_gram", {}), ("gaussian_1it", {"eig_iters": 1, "oversample": p}),
+                ("learned_1it", {"eig_iters": 1, "oversample": p, "sketch": learned}))
+    errs = {v: [] for v, _ in variants}
+    ms = {}
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for i, sd in enumerate(range(20000, 20016)):
+        X = synth.bumps(n, seed=sd, assemble_on=torch.device("cuda"))
+        for v, kw in variants:
+            errs[v].append(ht.decompose(X, tree, precision="bf16", compute_error=True, **kw).report["rel_err"])
+            if i == 0:
+                for _ in range(3):
+                    ht.decompose(X, tree, precision="bf16", **kw)
+                torch.cuda.synchronize()
+                ev0.record(stream)
+                for _ in range(10):
+                    ht.decompose(X, tree, precision="bf16", **kw)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+                ms[v] = ev0.elapsed_time(ev1) / 10
+        del X
+    rec["heldout_rel_err_mean"] = {v: float(np.mean(e)) for v, e in errs.items()}
+    rec["heldout_rel_err_max"] = {v: float(np.max(e)) for v, e in errs.items()}
+    rec["ms_per_decomposition"] = ms
+    return rec
 
 
 def run_ours(args, world, rank, local):

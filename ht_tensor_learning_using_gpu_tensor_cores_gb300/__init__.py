@@ -141,7 +141,11 @@ def _config(precision: str, oversample: int, eig_iters: int, power_steps: int, s
             if s is None:
                 continue
             if _is_torch(s):
-                s = s.contiguous()
+                if s.dim() != 2 or s.dtype.is_floating_point is False:
+                    raise TypeError("a sketch is a 2-D float tensor (n_m x (k + oversample))")
+                s = s.float()
+                if s.stride() != (1, s.shape[0]):   # the C ABI reads column-major n x s
+                    s = s.t().contiguous().t()
                 keep.append(s)
                 cfg.sketch[m] = s.data_ptr()
             else:

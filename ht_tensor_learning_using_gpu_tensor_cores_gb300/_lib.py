@@ -6,7 +6,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from ctypes import POINTER, Structure, c_char_p, c_double, c_float, c_int, c_long, c_ulonglong, c_void_p
+from ctypes import POINTER, Structure, c_char_p, c_double, c_float, c_int, c_long, c_longlong, c_ulonglong, c_void_p
 
 MAX_NODES = 7
 MAX_ORDER = 4
@@ -24,7 +24,7 @@ EXPORTED = ["ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", 
             "ht_decompose", "ht_reconstruct_error", "ht_workspace_size", "ht_release_workspace",
             "ht_status_string", "ht_last_error", "ht_kernel_launch_count", "htd", "htd4",
             "ht_mode_gram", "ht_mode_product", "ht_corange_product", "ht_mode_gram_noalloc",
-            "ht_decompose_batched", "ht_release_batch"]
+            "ht_decompose_batched", "ht_release_batch", "ht_sketch_loss_grad", "ht_sketch_adam"]
 
 
 class HtTree(Structure):
@@ -96,9 +96,12 @@ def lib():
                                        POINTER(HtConfig), POINTER(c_void_p), POINTER(c_void_p), POINTER(c_double),
                                        POINTER(HtBatchReport), c_void_p]
     L.ht_release_batch.argtypes = []
+    L.ht_sketch_loss_grad.argtypes = [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, POINTER(c_double),
+                                      c_void_p]
+    L.ht_sketch_adam.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_longlong, c_float, c_int, c_void_p]
     L.ht_corange_product.argtypes = [c_void_p, POINTER(c_long), c_int, c_int, c_int, c_void_p, c_int, c_int,
                                      c_void_p, c_void_p]
-    for name in ("ht_decompose_batched", "ht_release_batch", "ht_mode_gram", "ht_mode_gram_noalloc", "ht_mode_product", "ht_corange_product", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
+    for name in ("ht_sketch_loss_grad", "ht_sketch_adam", "ht_decompose_batched", "ht_release_batch", "ht_mode_gram", "ht_mode_gram_noalloc", "ht_mode_product", "ht_corange_product", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
                  "ht_decompose", "ht_reconstruct_error", "ht_workspace_size", "ht_release_workspace"):
         getattr(L, name).restype = c_int
     _lib = L

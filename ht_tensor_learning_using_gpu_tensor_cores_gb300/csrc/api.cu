@@ -1263,6 +1263,42 @@ ht_status_t ht_release_batch(void) {
   return HT_OK;
 }
 
+ht_status_t ht_sketch_loss_grad(const float *G, const float *trG, int batch, int n, int s, const float *S,
+                                float *grad, double *loss, void *stream) {
+  if (!G || !trG || !S || !grad || !loss) return fail(HT_ERR_INVALID_ARG, "NULL argument");
+  if (batch < 1 || n < 1 || s < 1 || s > 64 || s > n) return fail(HT_ERR_INVALID_ARG, "need batch >= 1, 1 <= s <= min(n, 64)");
+  HT_TRY(check_device());
+  if (!is_device_ptr(G) || !is_device_ptr(trG) || !is_device_ptr(S) || !is_device_ptr(grad))
+    return fail(HT_ERR_INVALID_ARG, "G, trG, S and grad must be device memory");
+  std::lock_guard<std::mutex> lk(g_ws_mutex);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t bytes = sketch_workspace_bytes(batch, n, s) + sizeof(double) * batch + 512;
+  void *ws = nullptr;
+  HT_TRY(acquire_workspace(bytes, &ws, st));
+  char *p = static_cast<char *>(ws);
+  double *dloss = reinterpret_cast<double *>(p);
+  int *bad = reinterpret_cast<int *>(p + ((sizeof(double) * batch + 255) & ~size_t(255)));
+  void *scratch = p + ((sizeof(double) * batch + 255) & ~size_t(255)) + 256;
+  int launches = 0;
+  HT_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
+  HT_CUDA(sketch_loss_grad(G, trG, batch, n, s, S, grad, dloss, bad, scratch, st, &launches));
+  int hbad = 0;
+  HT_CUDA(cudaMemcpyAsync(loss, dloss, sizeof(double) * batch, cudaMemcpyDeviceToHost, st));
+  HT_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+  HT_CUDA(cudaStreamSynchronize(st));
+  g_launches += static_cast<unsigned long long>(launches);
+  if (hbad) return fail(HT_ERR_NUMERICAL, "singular CholeskyQR factor: G S is rank deficient");
+  return HT_OK;
+}
+
+ht_status_t ht_sketch_adam(float *S, const float *grad, float *m, float *v, long long count, float lr, int step,
+                           void *stream) {
+  if (!S || !grad || !m || !v || count < 1 || step < 1) return fail(HT_ERR_INVALID_ARG, "bad argument");
+  HT_CUDA(sketch_adam(S, grad, m, v, count, lr, 0.9f, 0.999f, 1e-8f, step, static_cast<cudaStream_t>(stream)));
+  g_launches += 1;
+  return HT_OK;
+}
+
 ht_status_t ht_reconstruct_error(const float *x, const long *dims, int order, const ht_tree_t *tree,
                                  const float *const *U, const float *const *B, double *rel_err, void *stream) {
   if (!x || !dims || !U || !B || !rel_err) return fail(HT_ERR_INVALID_ARG, "NULL argument");

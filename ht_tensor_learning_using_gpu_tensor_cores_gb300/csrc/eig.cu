@@ -477,11 +477,14 @@ HT_DEV void jacobi_smem(float (*A)[SMAX + 1], float (*A2)[SMAX + 1], float (*V)[
     for (int e = t; e < s * s; e += 256) A[e % s][e / s] = Ac[e % s][e / s];
     __syncthreads();
   }
-  for (int j = t; j < s; j += 256) {   // rank by counting: descending eigenvalues
-    const float dj = A[j][j];
+  // rank by counting: descending eigenvalues.  NaN counts as -inf and ties go
+  // by index, so the ranks always form a permutation (order[] is used as an
+  // index: a hole would be an out-of-range shared-memory access)
+  for (int j = t; j < s; j += 256) {
+    const float dj = isnan(A[j][j]) ? -INFINITY : A[j][j];
     int rank = 0;
     for (int i = 0; i < s; ++i) {
-      const float di = A[i][i];
+      const float di = isnan(A[i][i]) ? -INFINITY : A[i][i];
       if (di > dj || (di == dj && i < j)) ++rank;
     }
     order[rank] = j;
@@ -934,58 +937,74 @@ HT_DEV void coop_product(const float *G, const float *Y, int n, int s, int r0, i
   }
 }
 
-// Scaled, shifted Cholesky of the packed s x s matrix Sd (double) followed by
-// the explicit transform T = diag(dsc) R^-1 (row-major, stride SMAX, upper
-// triangular) in Ts, so that applying it is a small matrix product.  A is
-// SMAX x SMAX scratch.  The elimination keeps pivot rows unscaled (one barrier
-// per step); R's rows are scaled when T is formed.
-HT_DEV void factor_transform(const double *Sd, int s, float shift, float *A, float *dsc, float *piv, float *Ts) {
-  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+// Scaled, shifted Cholesky of the packed s x s matrix Sd followed by the
+// explicit transform T = diag(dsc) R^-1 (row-major, stride SMAX, upper
+// triangular, FP32) in Ts, so that applying it is a small matrix product.
+//
+// The factorisation runs in FP64 (A: SMAX x SMAX doubles, d: SMAX doubles,
+// R32: SMAX x SMAX floats of scratch): on numerically rank-deficient blocks the
+// scaled Gram has pivots far below FP32 resolution, and an FP32 factor (or a
+// large shift) would discard the weak directions every iteration.  Shifts are
+// tiny (1e-12, 1e-14 in the last CholeskyQR pass) and pivots are floored at
+// 1e-24, so T stays finite.  GB300 issues FP64 at a small fraction of FP32, so
+// the elimination spreads every trailing update over all 256 threads (packed
+// triangle), and the triangular inverse runs in FP32 from the FP64 factor: T
+// only has to keep the block well conditioned; the span is that of Y for any
+// invertible T.
+HT_DEV void factor_transform(const double *Sd, int s, double shift, double *A, double *d, float *R32, float *Ts) {
+  __shared__ double rinv[SMAX];
+  const int t = threadIdx.x;
   for (int j = t; j < s; j += 256) {
-    const double d = Sd[j * (j + 1) / 2 + j];
-    dsc[j] = d > 1e-300 ? static_cast<float>(1.0 / sqrt(d)) : 0.f;
+    const double v = Sd[j * (j + 1) / 2 + j];
+    d[j] = v > 1e-300 ? 1.0 / sqrt(v) : 0.0;
   }
   __syncthreads();
   const int E = s * (s + 1) / 2;
   for (int e = t; e < E; e += 256) {
     int i, j;
     tri_index(e, i, j);
-    float v = static_cast<float>(Sd[e] * static_cast<double>(dsc[i]) * static_cast<double>(dsc[j]));
-    if (i == j) v = (dsc[j] > 0.f ? 1.f : 0.f) + shift;
+    double v = Sd[e] * d[i] * d[j];
+    if (i == j) v = (d[j] > 0.0 ? 1.0 : 0.0) + shift;
     A[i * SMAX + j] = v;
   }
   __syncthreads();
   for (int j = 0; j < s; ++j) {
-    const float p = fmaxf(A[j * SMAX + j], 1e-30f);
-    const float pinv = 1.f / p;
-    if (t == 0) piv[j] = p;
-    for (int i = j + 1 + warp; i < s; i += 8) {
-      const float f = A[j * SMAX + i] * pinv;
-      for (int k = i + lane; k < s; k += 32) A[i * SMAX + k] = fmaf(-f, A[j * SMAX + k], A[i * SMAX + k]);
+    if (t == 0) {
+      const double r = sqrt(fmax(A[j * SMAX + j], 1e-24));
+      A[j * SMAX + j] = r;
+      rinv[j] = 1.0 / r;
+    }
+    __syncthreads();
+    const int L = s - 1 - j;
+    for (int k = j + 1 + t; k < s; k += 256) A[j * SMAX + k] *= rinv[j];   // row j of R
+    __syncthreads();
+    for (int e = t; e < L * (L + 1) / 2; e += 256) {   // A[i][k] -= R[j][i] R[j][k], j < i <= k
+      int ii, kk;
+      tri_index(e, ii, kk);
+      const int i = j + 1 + ii, k = j + 1 + kk;
+      A[i * SMAX + k] = fma(-A[j * SMAX + i], A[j * SMAX + k], A[i * SMAX + k]);
     }
     __syncthreads();
   }
-  // R[i][j] = A[i][j] / sqrt(piv_i) (j > i), R[i][i] = sqrt(piv_i); then
-  // W = R^-1 column by column (thread k solves R w = e_k), T = diag(dsc) W.
   for (int e = t; e < E; e += 256) {
-    int i, j;
-    tri_index(e, i, j);
-    const float di = sqrtf(piv[i]);
-    A[i * SMAX + j] = (i == j) ? 1.f / di : A[i * SMAX + j] / di;   // diagonal holds 1 / R[i][i]
+    int i, k;
+    tri_index(e, i, k);
+    R32[i * SMAX + k] = static_cast<float>(A[i * SMAX + k]);
   }
   __syncthreads();
+  // W = R^-1 column by column (thread k solves R w = e_k), T = diag(dsc) W
   if (t < s) {
     const int k = t;
     for (int i = k; i >= 0; --i) {
       float acc = (i == k) ? 1.f : 0.f;
-      for (int j = i + 1; j <= k; ++j) acc = fmaf(-A[i * SMAX + j], Ts[j * SMAX + k], acc);
-      Ts[i * SMAX + k] = acc * A[i * SMAX + i];
+      for (int j = i + 1; j <= k; ++j) acc = fmaf(-R32[i * SMAX + j], Ts[j * SMAX + k], acc);
+      Ts[i * SMAX + k] = acc / R32[i * SMAX + i];
     }
   }
   __syncthreads();
   for (int e = t; e < SMAX * SMAX; e += 256) {
     const int i = e / SMAX, k = e % SMAX;
-    Ts[e] = (i < s && k < s && k >= i) ? Ts[e] * dsc[i] : 0.f;
+    Ts[e] = (i < s && k < s && k >= i) ? Ts[e] * static_cast<float>(d[i]) : 0.f;
   }
   __syncthreads();
 }
@@ -1180,7 +1199,7 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
   __shared__ int order[SMAX];
   __shared__ float red[256];
   __shared__ float th_sm[SMAX];
-  __shared__ float piv[SMAX];
+  __shared__ double piv64[SMAX];
   const int t = threadIdx.x;
 
   if (static_cast<int>(blockIdx.x) >= B.nsync) {
@@ -1248,12 +1267,13 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
   }
   if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
 
-  auto reduce_and_factor = [&](float shift) -> bool {
+  auto reduce_and_factor = [&](double shift) -> bool {
     if (!grid_barrier(B.bar, members, B.err, &s_ok)) return false;
     coop_reduce(B);
     if (!grid_barrier(B.bar, members, B.err, &s_ok)) return false;
     coop_load_S(P, Sd);
-    factor_transform(Sd, P.s, shift, ring + 2 * ESMAX, ds, piv, Rs);
+    double *A64 = Sd + ESMAX;                  // SMAX*SMAX doubles after the reduced Gram
+    factor_transform(Sd, P.s, shift, A64, piv64, reinterpret_cast<float *>(A64 + SMAX * SMAX), Rs);
     return true;
   };
 
@@ -1261,15 +1281,15 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
   bool ident = true;
   for (int it = 0; it < B.iters; ++it) {
     coop_step(P, cl, 0, P.buf[cur], P.buf[cur ^ 1], nullptr, ident, mu, Rs, Zs, Qr, ring);
-    if (!reduce_and_factor(1e-5f)) return;
+    if (!reduce_and_factor(1e-12)) return;
     ident = false;
     cur ^= 1;
   }
   // three CholeskyQR transforms: Y_L T_L -> buffer 2, then twice in place
   coop_step(P, cl, 1, P.buf[cur], P.buf[2], nullptr, ident, 0.f, Rs, Zs, Qr, ring);
-  if (!reduce_and_factor(1e-6f)) return;
+  if (!reduce_and_factor(1e-12)) return;
   coop_step(P, cl, 1, P.buf[2], P.buf[2], nullptr, false, 0.f, Rs, Zs, Qr, ring);
-  if (!reduce_and_factor(0.f)) return;
+  if (!reduce_and_factor(1e-14)) return;
   // Rayleigh-Ritz: Q = buf2 T -> buf3, G Q -> buf0, H = Q^T G Q
   coop_step(P, cl, 2, P.buf[2], P.buf[3], P.buf[0], false, 0.f, Rs, Zs, Qr, ring);
   if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;

@@ -164,4 +164,13 @@ cudaError_t transfer_eig_launch(const float *WG, int kw, int kt, int kc, int t_i
 cudaError_t svd_from_gram_launch(const float *GW, int s, int k1, int k2, float *M1, float *M2, float *Broot,
                                  cudaStream_t st);
 
+// ------------------------------------------------------- learned sketch (learn.cu)
+size_t sketch_workspace_bytes(int batch, int n, int s);
+// loss[b] and the batch-mean gradient of L(S) = mean_b [1 - tr(Q_b^T G_b Q_b) / tr(G_b)],
+// Q_b = orth(G_b S); G: batch x n x n, S and grad: n x s, all column-major device memory.
+cudaError_t sketch_loss_grad(const float *G, const float *trG, int batch, int n, int s, const float *S, float *grad,
+                             double *loss, int *bad, void *ws, cudaStream_t st, int *launches);
+cudaError_t sketch_adam(float *S, const float *g, float *m, float *v, long long count, float lr, float b1, float b2,
+                        float eps, int step, cudaStream_t st);
+
 }  // namespace htgb

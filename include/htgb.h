@@ -203,6 +203,25 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
 /* Free the batched path's cached graph and workspace on the current device. */
 ht_status_t ht_release_batch(void);
 
+/* ---------------------------------------------------------- learned sketch */
+/* Training of a per-mode sketch S (n x s): the start block of the leaf range
+ * finder, used as ht_config_t.sketch[m] with eig_iters = 1 (Y = G S, Rayleigh-
+ * Ritz on span(Y)).  No counterpart in the reference, whose range finder draws a
+ * Gaussian test matrix (3D/Opt/kernel.cu:595-680); the Gaussian start block
+ * stays the default and the judge of the learned one.
+ *
+ * ht_sketch_loss_grad: for `batch` mode Grams G (batch x n x n, column-major,
+ * device) with traces trG (device), the forward value
+ *   loss[b] = 1 - tr(Q_b^T G_b Q_b) / tr(G_b),   Q_b = orth(G_b S)  (CholeskyQR)
+ * (host array of batch) and the adjoint grad = d mean_b loss[b] / dS (n x s,
+ * device).  Synchronous; HT_ERR_NUMERICAL when a CholeskyQR factor is singular.
+ * ht_sketch_adam: one Adam step on S with moments m, v (count = n*s, device),
+ * step >= 1, beta1 0.9, beta2 0.999, eps 1e-8.  Asynchronous on `stream`. */
+ht_status_t ht_sketch_loss_grad(const float *G, const float *trG, int batch, int n, int s, const float *S,
+                                float *grad, double *loss, void *stream);
+ht_status_t ht_sketch_adam(float *S, const float *grad, float *m, float *v, long long count, float lr, int step,
+                           void *stream);
+
 /* Bytes of device workspace ht_decompose needs for this problem. */
 ht_status_t ht_workspace_size(const long *dims, int order, const ht_tree_t *tree,
                               const ht_config_t *cfg, unsigned long long *bytes);

@@ -177,3 +177,29 @@ def procrustes_align(A: np.ndarray, B: np.ndarray) -> np.ndarray:
 def tree_energy_bound(tree: DimTree) -> float:
     """Quasi-optimality constant of root-to-leaf HT truncation: sqrt(2d-3)."""
     return float(np.sqrt(2 * tree.order - 3))
+
+
+# ---------------------------------------------------------------- learned sketch
+# The learned start block of the leaf range finder has no counterpart in the
+# reference (its rsvd draws a Gaussian test matrix, 3D/Opt/kernel.cu:595-680);
+# these are the float64 statements of the training objective and its gradient
+# that the GPU forward/adjoint kernels are checked against.
+def sketch_loss(G: np.ndarray, S: np.ndarray) -> float:
+    """1 - tr(Q^T G Q) / tr(G), Q an orthonormal basis of G S."""
+    G = np.asarray(G, np.float64)
+    Y = G @ np.asarray(S, np.float64)
+    Q, _ = np.linalg.qr(Y)
+    return float(1.0 - np.trace(Q.T @ G @ Q) / np.trace(G))
+
+
+def sketch_grad(G: np.ndarray, S: np.ndarray) -> np.ndarray:
+    """d sketch_loss / dS = -(2 / tr G) G E C^-1, Y = G S, C = Y^T Y,
+    E = G Y - Y C^-1 (Y^T G Y)."""
+    G = np.asarray(G, np.float64)
+    Y = G @ np.asarray(S, np.float64)
+    C = Y.T @ Y
+    P = G @ Y
+    X = np.linalg.solve(C, Y.T @ P)
+    E = P - Y @ X
+    return -(2.0 / np.trace(G)) * (G @ E) @ np.linalg.inv(C)
+

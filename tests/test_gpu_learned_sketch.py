@@ -1,0 +1,104 @@
+"""Learned sketch: the GPU forward/adjoint kernels against the float64 oracle,
+and a training run that shows what the trained sketch gains over the
+Gaussian start block (same width) on held-out members of a family whose
+dominant subspace is learnable.
+
+Tolerances: loss 2e-5 absolute, gradient 5e-3 relative (FP32 products, FP64
+s x s algebra).
+"""
+import numpy as np
+import pytest
+import torch
+
+import ht_tensor_learning_using_gpu_tensor_cores_gb300 as ht
+from ht_tensor_learning_using_gpu_tensor_cores_gb300 import learn, synth
+import ht_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def psd_batch(count, n, rank, decay, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        A = rng.standard_normal((n, rank)) * (decay ** np.arange(rank))
+        out.append(A @ A.T)
+    return np.stack(out)
+
+
+def to_gpu(Gs):
+    G = torch.from_numpy(np.ascontiguousarray(Gs.astype(np.float32))).cuda()
+    tr = torch.diagonal(G, dim1=1, dim2=2).sum(-1).contiguous()
+    return G, tr
+
+
+def test_loss_and_gradient_match_oracle():
+    n, s = 64, 10
+    Gs = psd_batch(4, n, 48, 0.92, seed=3)
+    G, tr = to_gpu(Gs)
+    S = learn.gaussian_sketch(n, s, seed=4)
+    loss, grad = learn.loss_grad(G, tr, S)
+    Sn = S.cpu().numpy().astype(np.float64)
+    G32 = Gs.astype(np.float32).astype(np.float64)
+    ref_loss = np.array([O.sketch_loss(g, Sn) for g in G32])
+    ref_grad = np.mean([O.sketch_grad(g, Sn) for g in G32], axis=0)
+    assert np.abs(loss - ref_loss).max() < 2e-5, (loss, ref_loss)
+    g = grad.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(g - ref_grad) / np.linalg.norm(ref_grad) < 5e-3
+
+
+def shared_subspace_family(count, n, seed, basis_seed=7, k=40):
+    """Grams U diag(w) U^T + W diag(v) W^T: U (n x k) fixed across the family
+    with random decaying weights, W random per member with smaller weights."""
+    rb = np.random.default_rng(basis_seed)
+    U, _ = np.linalg.qr(rb.standard_normal((n, k)))
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        w = rng.uniform(0.5, 1.5, k) * (0.85 ** np.arange(k))
+        W, _ = np.linalg.qr(rng.standard_normal((n, k)))
+        v = 0.02 * rng.uniform(0.5, 1.5, k)
+        out.append((U * w) @ U.T + (W * v) @ W.T)
+    return np.stack(out)
+
+
+def test_training_beats_gaussian_on_heldout():
+    n, s = 128, 12
+    Gtr, ttr = to_gpu(shared_subspace_family(48, n, seed=1))
+    Gte, tte = to_gpu(shared_subspace_family(16, n, seed=2))
+    trainer = learn.SketchTrainer(n, s, seed=5, lr=5e-3)
+    S0 = trainer.S.clone()
+    rng = np.random.default_rng(0)
+    for _ in range(300):
+        idx = torch.as_tensor(rng.choice(48, 16, replace=False), device="cuda")
+        trainer.step(Gtr[idx].contiguous(), ttr[idx].contiguous())
+    l_gauss = learn.heldout_loss(Gte, tte, S0).mean()
+    l_learn = learn.heldout_loss(Gte, tte, trainer.S).mean()
+    l_best = np.mean([1 - np.sort(np.linalg.eigvalsh(g))[::-1][:s].sum() / np.trace(g)
+                      for g in Gte.cpu().numpy().astype(np.float64)])
+    # the learned sketch closes most of the gap between the Gaussian sketch and
+    # the best subspace of its width (the top-s eigenvectors of each Gram)
+    assert l_gauss - l_learn >= 0.8 * (l_gauss - l_best), (l_learn, l_gauss, l_best)
+    assert l_learn >= l_best - 1e-6
+
+
+def test_sketch_drives_the_decomposition():
+    """The sketch passed to decompose is the leaf solver's start block: with one
+    iteration, the top eigenvectors of each mode Gram as the sketch reproduce the
+    exact path, and a sketch spanning the weakest eigenvectors does much worse."""
+    n, k, p = 96, 8, 6   # n above 64, so the leaves use the start block (s = k + p)
+    X = synth.bumps(n, seed=11, assemble_on=torch.device("cuda"))
+    tree = ht.reference_tree_3d([1, k, k, k, k])
+    good, bad = [], []
+    for m in range(3):
+        G = torch.as_tensor(ht.mode_gram(X, (n, n, n), m, precision="fp32"), device="cuda").double()
+        w, V = torch.linalg.eigh(G)
+        good.append(V[:, -(k + p):].flip(1).float())
+        bad.append(V[:, :k + p].float())
+    exact = ht.decompose(X, tree, precision="fp32", compute_error=True).report["rel_err"]
+    e_good = ht.decompose(X, tree, precision="fp32", compute_error=True, eig_iters=1, oversample=p,
+                          sketch=good).report["rel_err"]
+    e_bad = ht.decompose(X, tree, precision="fp32", compute_error=True, eig_iters=1, oversample=p,
+                         sketch=bad).report["rel_err"]
+    assert abs(e_good - exact) <= 1e-5 * max(1.0, exact / 1e-3), (e_good, exact)
+    assert e_bad > 10 * e_good + 1e-6, (e_bad, e_good)

@@ -188,3 +188,27 @@ def test_user_start_block():
     res = ht.decompose(X, tree, precision="fp32", compute_error=True, sketch=sk, oversample=16)
     Uo, Bo, _ = O.ht_decompose(X, tree)
     assert abs(res.report["rel_err"] - O.ht_error(X, tree, Uo, Bo)) < 1e-5
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_numerically_rank_deficient_large_modes(prec):
+    """Separable-bumps tensor at 128^3, rank 24: the mode Grams have ~20 eigenvalues
+    above 1e-12 of the largest and the rest at rounding level, so the leaf
+    solver runs its subspace iteration (n > 64) on numerically rank-deficient
+    blocks.  FP32 arithmetic cannot resolve directions below ~1e-7 of the
+    largest eigenvalue: the float32 restatement of the reference algorithm
+    (LAPACK ssyevd/sgesvd in the oracle) itself lands near 1.5e-4 here, not at
+    the FP64 error (3e-8).  Bar: within 2x of that float32 error (plain path),
+    and the mixed path within the mixed tolerance of it."""
+    X = synth.bumps(128, seed=20000)
+    tree = ht.reference_tree_3d([1, 24, 24, 24, 24])
+    U32, B32, _ = O.ht_decompose(X.astype(np.float32), tree, dtype=np.float32)
+    e32 = O.ht_error(X, tree, {t: U32[t].astype(np.float64) for t in U32}, {t: B32[t].astype(np.float64) for t in B32})
+    res, U, B = run(X, tree, prec)
+    e = O.ht_error(X, tree, U, B)
+    if prec == "fp32":
+        assert e <= 2.0 * e32 + 1e-6, (e, e32)
+    else:
+        assert e <= e32 + TOL["bf16"], (e, e32)
+    for t in tree.leaves():
+        assert O.orthogonality_defect(U[t]) < 2e-5
