@@ -937,6 +937,18 @@ HT_DEV void coop_product(const float *G, const float *Y, int n, int s, int r0, i
   }
 }
 
+// 1 / sqrt(max(x, 1e-24)) in FP64 from an FP32 seed and two Newton steps
+// y <- y (3 - x y^2) / 2 (each squares the relative error): a few FP64
+// multiplies instead of the FP64 square-root and division sequences, which
+// are long on GB300's narrow FP64 pipe.
+HT_DEV double frsqrt_fp64(double x) {
+  x = fmax(x, 1e-24);
+  double y = static_cast<double>(rsqrtf(static_cast<float>(x)));
+  y = y * fma(-0.5 * x, y * y, 1.5);
+  y = y * fma(-0.5 * x, y * y, 1.5);
+  return y;
+}
+
 // Scaled, shifted Cholesky of the packed s x s matrix Sd followed by the
 // explicit transform T = diag(dsc) R^-1 (row-major, stride SMAX, upper
 // triangular, FP32) in Ts, so that applying it is a small matrix product.
@@ -952,7 +964,6 @@ HT_DEV void coop_product(const float *G, const float *Y, int n, int s, int r0, i
 // only has to keep the block well conditioned; the span is that of Y for any
 // invertible T.
 HT_DEV void factor_transform(const double *Sd, int s, double shift, double *A, double *d, float *R32, float *Ts) {
-  __shared__ double rinv[SMAX];
   const int t = threadIdx.x;
   for (int j = t; j < s; j += 256) {
     const double v = Sd[j * (j + 1) / 2 + j];
@@ -969,15 +980,15 @@ HT_DEV void factor_transform(const double *Sd, int s, double shift, double *A, d
   }
   __syncthreads();
   for (int j = 0; j < s; ++j) {
-    if (t == 0) {
-      const double r = sqrt(fmax(A[j * SMAX + j], 1e-24));
-      A[j * SMAX + j] = r;
-      rinv[j] = 1.0 / r;
+    // warp 0 forms the pivot (every lane, no extra barrier) and scales row j
+    if (t < 32) {
+      const double piv = fmax(A[j * SMAX + j], 1e-24);
+      const double ri = frsqrt_fp64(piv);
+      for (int k = j + 1 + t; k < s; k += 32) A[j * SMAX + k] *= ri;   // row j of R
+      if (t == 0) A[j * SMAX + j] = piv * ri;
     }
     __syncthreads();
     const int L = s - 1 - j;
-    for (int k = j + 1 + t; k < s; k += 256) A[j * SMAX + k] *= rinv[j];   // row j of R
-    __syncthreads();
     for (int e = t; e < L * (L + 1) / 2; e += 256) {   // A[i][k] -= R[j][i] R[j][k], j < i <= k
       int ii, kk;
       tri_index(e, ii, kk);
