@@ -25,14 +25,14 @@ from typing import Dict, Optional, Sequence
 
 import numpy as np
 
-from . import synth
+from . import htformat, synth
 from ._lib import (FLAG_COMPUTE_ERROR, HTError, HtBatchReport, HtConfig, HtReport, HtTree, LEAF_GRAM, PREC_BF16,
                    PREC_FP32, check, lib)
 from .tree import (DimTree, balanced_tree_4d, left_first_tree_3d, middle_tree_3d, reference_tree_3d,
                    uniform_ranks)
 
 __all__ = ["DimTree", "reference_tree_3d", "left_first_tree_3d", "middle_tree_3d", "balanced_tree_4d",
-           "uniform_ranks", "decompose", "reconstruct_error", "htd", "htd4", "HTResult", "HTError", "synth",
+           "uniform_ranks", "decompose", "reconstruct_error", "reconstruct", "evaluate", "htformat", "htd", "htd4", "HTResult", "HTError", "synth",
            "workspace_size", "release_workspace", "kernel_launch_count", "BatchDecomposer", "release_batch"]
 
 _PREC = {"fp32": PREC_FP32, "bf16": PREC_BF16}
@@ -277,21 +277,8 @@ def release_batch():
     check(lib().ht_release_batch())
 
 
-def reconstruct_error(x, tree: DimTree, U: Dict[int, object], B: Dict[int, object],
-                      dims: Optional[Sequence[int]] = None, stream=None) -> float:
-    """||X - Xhat||_F / ||X||_F computed on the GPU without materialising Xhat."""
-    dims = _dims_of(x, tree, dims)
-    ts = _tree_struct(tree)
-    cdims = (c_long * 4)(*dims)
-    keep = []
-    if _is_torch(x):
-        import torch
-        xptr = x.data_ptr()
-        if stream is None:
-            stream = torch.cuda.current_stream(x.device).cuda_stream
-    else:
-        xa, xptr = _host_input(x, dims)
-        keep.append(xa)
+def _factor_ptrs(U: Dict[int, object], B: Dict[int, object], keep: list):
+    """C pointer tables of column-major factors (numpy or torch; copies are kept alive in keep)."""
     uptr = (c_void_p * 7)()
     bptr = (c_void_p * 7)()
 
@@ -312,6 +299,90 @@ def reconstruct_error(x, tree: DimTree, U: Dict[int, object], B: Dict[int, objec
         if _is_torch(a) and a.dim() == 3:
             a = a.permute(2, 1, 0).contiguous().permute(2, 1, 0)
         bptr[t] = p(a)
+    return uptr, bptr
+
+
+def _factor_device(U: Dict[int, object], B: Dict[int, object]):
+    """The CUDA device of torch factors, or None for host factors."""
+    for a in list(U.values()) + list(B.values()):
+        if _is_torch(a) and a.is_cuda:
+            return a.device
+    return None
+
+
+def reconstruct(tree: DimTree, U: Dict[int, object], B: Dict[int, object], dims: Sequence[int], stream=None):
+    """The full tensor Xhat of an HT representation, computed on the GPU.
+
+    Torch CUDA factors give a torch tensor shaped ``dims[::-1]`` (its memory is
+    the column-major tensor); host factors give a Fortran-ordered numpy array
+    of shape ``dims``.  The reference forms Xhat only to measure the error
+    (3D/Opt/htd_tensorcore.cu:295-331)."""
+    dims = tuple(int(d) for d in dims)
+    ts = _tree_struct(tree)
+    keep = []
+    uptr, bptr = _factor_ptrs(U, B, keep)
+    dev = _factor_device(U, B)
+    if dev is not None:
+        import torch
+        out = torch.empty(tuple(reversed(dims)), dtype=torch.float32, device=dev)
+        optr = out.data_ptr()
+        if stream is None:
+            stream = torch.cuda.current_stream(dev).cuda_stream
+    else:
+        out = np.empty(dims, dtype=np.float32, order="F")
+        optr = out.ctypes.data
+    check(lib().ht_reconstruct((c_long * 4)(*dims), len(dims), ctypes.byref(ts), uptr, bptr, c_void_p(optr),
+                               c_void_p(stream) if stream else None))
+    return out
+
+
+def evaluate(tree: DimTree, U: Dict[int, object], B: Dict[int, object], dims: Sequence[int], idx, stream=None):
+    """Entries Xhat[idx[e, 0], ..., idx[e, order-1]] (0-based) of an HT
+    representation without forming Xhat.  idx: (count, order) integers, numpy or
+    torch; the result matches idx's library (numpy float32 or torch float32 on
+    idx's device)."""
+    dims = tuple(int(d) for d in dims)
+    ts = _tree_struct(tree)
+    keep = []
+    uptr, bptr = _factor_ptrs(U, B, keep)
+    if _is_torch(idx):
+        import torch
+        ix = idx.to(torch.int64).contiguous()
+        if ix.dim() != 2 or ix.shape[1] != len(dims):
+            raise ValueError("idx must be (count, order)")
+        count = ix.shape[0]
+        out = torch.empty(count, dtype=torch.float32, device=ix.device)
+        iptr, optr = ix.data_ptr(), out.data_ptr()
+        if stream is None and ix.is_cuda:
+            stream = torch.cuda.current_stream(ix.device).cuda_stream
+    else:
+        ix = np.ascontiguousarray(np.asarray(idx, dtype=np.int64))
+        if ix.ndim != 2 or ix.shape[1] != len(dims):
+            raise ValueError("idx must be (count, order)")
+        count = ix.shape[0]
+        out = np.empty(count, dtype=np.float32)
+        iptr, optr = ix.ctypes.data, out.ctypes.data
+    check(lib().ht_evaluate((c_long * 4)(*dims), len(dims), ctypes.byref(ts), uptr, bptr, c_void_p(iptr),
+                            count, c_void_p(optr), c_void_p(stream) if stream else None))
+    return out
+
+
+def reconstruct_error(x, tree: DimTree, U: Dict[int, object], B: Dict[int, object],
+                      dims: Optional[Sequence[int]] = None, stream=None) -> float:
+    """||X - Xhat||_F / ||X||_F computed on the GPU without materialising Xhat."""
+    dims = _dims_of(x, tree, dims)
+    ts = _tree_struct(tree)
+    cdims = (c_long * 4)(*dims)
+    keep = []
+    if _is_torch(x):
+        import torch
+        xptr = x.data_ptr()
+        if stream is None:
+            stream = torch.cuda.current_stream(x.device).cuda_stream
+    else:
+        xa, xptr = _host_input(x, dims)
+        keep.append(xa)
+    uptr, bptr = _factor_ptrs(U, B, keep)
     out = c_double(0.0)
     check(lib().ht_reconstruct_error(c_void_p(xptr), cdims, len(dims), ctypes.byref(ts), uptr, bptr,
                                      ctypes.byref(out), c_void_p(stream) if stream else None))

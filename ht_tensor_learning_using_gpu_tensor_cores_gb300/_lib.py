@@ -24,7 +24,8 @@ EXPORTED = ["ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", 
             "ht_decompose", "ht_reconstruct_error", "ht_workspace_size", "ht_release_workspace",
             "ht_status_string", "ht_last_error", "ht_kernel_launch_count", "htd", "htd4",
             "ht_mode_gram", "ht_mode_product", "ht_corange_product", "ht_mode_gram_noalloc",
-            "ht_decompose_batched", "ht_release_batch", "ht_sketch_loss_grad", "ht_sketch_adam"]
+            "ht_decompose_batched", "ht_release_batch", "ht_sketch_loss_grad", "ht_sketch_adam",
+            "ht_reconstruct", "ht_evaluate"]
 
 
 class HtTree(Structure):
@@ -76,6 +77,10 @@ def lib():
                                POINTER(c_void_p), POINTER(c_void_p), POINTER(HtReport), c_void_p]
     L.ht_reconstruct_error.argtypes = [c_void_p, POINTER(c_long), c_int, POINTER(HtTree), POINTER(c_void_p),
                                        POINTER(c_void_p), POINTER(c_double), c_void_p]
+    L.ht_reconstruct.argtypes = [POINTER(c_long), c_int, POINTER(HtTree), POINTER(c_void_p), POINTER(c_void_p),
+                                 c_void_p, c_void_p]
+    L.ht_evaluate.argtypes = [POINTER(c_long), c_int, POINTER(HtTree), POINTER(c_void_p), POINTER(c_void_p),
+                              c_void_p, c_longlong, c_void_p, c_void_p]
     L.ht_workspace_size.argtypes = [POINTER(c_long), c_int, POINTER(HtTree), POINTER(HtConfig), POINTER(c_ulonglong)]
     L.ht_release_workspace.argtypes = []
     L.ht_status_string.argtypes = [c_int]
@@ -101,7 +106,7 @@ def lib():
     L.ht_sketch_adam.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_longlong, c_float, c_int, c_void_p]
     L.ht_corange_product.argtypes = [c_void_p, POINTER(c_long), c_int, c_int, c_int, c_void_p, c_int, c_int,
                                      c_void_p, c_void_p]
-    for name in ("ht_sketch_loss_grad", "ht_sketch_adam", "ht_decompose_batched", "ht_release_batch", "ht_mode_gram", "ht_mode_gram_noalloc", "ht_mode_product", "ht_corange_product", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
+    for name in ("ht_reconstruct", "ht_evaluate", "ht_sketch_loss_grad", "ht_sketch_adam", "ht_decompose_batched", "ht_release_batch", "ht_mode_gram", "ht_mode_gram_noalloc", "ht_mode_product", "ht_corange_product", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
                  "ht_decompose", "ht_reconstruct_error", "ht_workspace_size", "ht_release_workspace"):
         getattr(L, name).restype = c_int
     _lib = L

@@ -1364,6 +1364,195 @@ ht_status_t ht_reconstruct_error(const float *x, const long *dims, int order, co
   return HT_OK;
 }
 
+// Factors on the device: host factors are staged into the arena.
+static ht_status_t stage_factors(Ctx &c, const Tree &T, const long *dims, const float *const *U, const float *const *B,
+                                 const float **Ud, const float **Bd) {
+  for (int t = 0; t < T.n_nodes; ++t) {
+    const float *src = T.leaf(t) ? U[t] : B[t];
+    const size_t count = factor_count(T, dims, t);
+    const float *d = src;
+    if (!is_device_ptr(src)) {
+      float *tmp = c.ar.take<float>(count);
+      if (!tmp) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small");
+      if (!c.dry()) HT_CUDA(cudaMemcpyAsync(tmp, src, count * sizeof(float), cudaMemcpyHostToDevice, c.st));
+      d = tmp;
+    }
+    (T.leaf(t) ? Ud : Bd)[t] = d;
+  }
+  return HT_OK;
+}
+
+// Xhat into out (device, column-major).  3rd order: X_(t) = W U_c^T with
+// W = (U_p x U_q) (B_t B_root'), the unfolding chosen by which mode c holds;
+// 4th order: X_(12) = (W12 B_root) W34^T.  Interior children list their modes
+// in increasing order, so W's rows are the column-major (i_p, i_q) pairs.
+static ht_status_t reconstruct_core(Ctx &c, const Tree &T, const long *dims, int order, const float *const *U,
+                                    const float *const *B, float *out) {
+  const size_t mark = c.ar.off;
+  if (order == 3) {
+    const Plan3 P = plan3(T);
+    const long long np_ = dims[P.mp], nq_ = dims[P.mq], nc_ = dims[P.mc];
+    float *Bkt = c.ar.take<float>(static_cast<size_t>(P.kt) * P.kc);
+    float *core = c.ar.take<float>(static_cast<size_t>(P.kp) * P.kq * P.kc);
+    float *Tm = c.ar.take<float>(static_cast<size_t>(np_) * P.kq * P.kc);
+    float *Wm = c.ar.take<float>(static_cast<size_t>(np_) * nq_ * P.kc);
+    if (!Bkt || !core || !Tm || !Wm) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (reconstruct)");
+    if (!c.dry()) {
+      if (P.t_is_left) HT_CUDA(cudaMemcpyAsync(Bkt, B[0], sizeof(float) * P.kt * P.kc, cudaMemcpyDeviceToDevice, c.st));
+      else HT_CUDA(transpose_small_launch(B[0], P.kc, P.kt, Bkt, c.st));
+      const long long kpq = static_cast<long long>(P.kp) * P.kq;
+      HT_CUDA(matmul_nn_launch(B[P.t], kpq, Bkt, P.kt, core, kpq, kpq, P.kc, P.kt, c.st));
+      HT_CUDA(expand2_launch(U[P.p], static_cast<int>(np_), P.kp, core, U[P.q], static_cast<int>(nq_), P.kq, P.kc, Tm,
+                             Wm, c.st));
+      if (P.mc == 2)        // X_(01) = W U_2^T
+        HT_CUDA(gemm_nt_launch(Wm, np_ * nq_, 0, U[P.c], nc_, out, np_ * nq_, 0, np_ * nq_, nc_, P.kc, 1, c.st));
+      else if (P.mc == 0)   // X_(0) = U_0 W^T
+        HT_CUDA(gemm_nt_launch(U[P.c], nc_, 0, Wm, np_ * nq_, out, nc_, 0, nc_, np_ * nq_, P.kc, 1, c.st));
+      else                  // slab i2: X(:, :, i2) = W[(:, i2), :] U_1^T
+        HT_CUDA(gemm_nt_launch(Wm, np_ * nq_, np_, U[P.c], nc_, out, np_, np_ * nc_, np_, nc_, P.kc, nq_, c.st));
+      c.launches += 4;
+    }
+  } else {
+    const int t1 = T.left[0], t2 = T.right[0];
+    const int k1 = T.rank[t1], k2 = T.rank[t2];
+    const int a1 = T.left[t1], b1 = T.right[t1], a2 = T.left[t2], b2 = T.right[t2];
+    const long long R = static_cast<long long>(dims[0]) * dims[1], Cn = static_cast<long long>(dims[2]) * dims[3];
+    float *T1 = c.ar.take<float>(static_cast<size_t>(dims[0]) * T.rank[b1] * k1);
+    float *W12 = c.ar.take<float>(static_cast<size_t>(R) * k1);
+    float *A12 = c.ar.take<float>(static_cast<size_t>(R) * k2);
+    float *T2 = c.ar.take<float>(static_cast<size_t>(dims[2]) * T.rank[b2] * k2);
+    float *W34 = c.ar.take<float>(static_cast<size_t>(Cn) * k2);
+    if (!T1 || !W12 || !A12 || !T2 || !W34) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (reconstruct)");
+    if (!c.dry()) {
+      HT_CUDA(expand2_launch(U[a1], static_cast<int>(dims[0]), T.rank[a1], B[t1], U[b1], static_cast<int>(dims[1]),
+                             T.rank[b1], k1, T1, W12, c.st));
+      HT_CUDA(expand2_launch(U[a2], static_cast<int>(dims[2]), T.rank[a2], B[t2], U[b2], static_cast<int>(dims[3]),
+                             T.rank[b2], k2, T2, W34, c.st));
+      HT_CUDA(matmul_nn_launch(W12, R, B[0], k1, A12, R, R, k2, k1, c.st));
+      HT_CUDA(gemm_nt_launch(A12, R, 0, W34, Cn, out, R, 0, R, Cn, k2, 1, c.st));
+      c.launches += 6;
+    }
+  }
+  c.ar.off = mark;
+  return HT_OK;
+}
+
+ht_status_t ht_reconstruct(const long *dims, int order, const ht_tree_t *tree, const float *const *U,
+                           const float *const *B, float *x_out, void *stream) {
+  if (!dims || !U || !B || !x_out) return fail(HT_ERR_INVALID_ARG, "NULL argument");
+  Tree T;
+  HT_TRY(parse_tree(tree, dims, order, T));
+  for (int t = 0; t < T.n_nodes; ++t)
+    if (!(T.leaf(t) ? U[t] : B[t])) return fail(HT_ERR_INVALID_ARG, "missing factor for node " + std::to_string(t));
+  HT_TRY(check_device());
+  std::lock_guard<std::mutex> lk(g_ws_mutex);
+  long long total = 1;
+  for (int m = 0; m < order; ++m) total *= dims[m];
+  const bool out_dev = is_device_ptr(x_out);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  auto plan = [&](Ctx &c) -> ht_status_t {
+    const float *Ud[HT_MAX_NODES] = {}, *Bd[HT_MAX_NODES] = {};
+    HT_TRY(stage_factors(c, T, dims, U, B, Ud, Bd));
+    float *o = out_dev ? x_out : c.ar.take<float>(static_cast<size_t>(total));
+    if (!o) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small");
+    HT_TRY(reconstruct_core(c, T, dims, order, Ud, Bd, o));
+    if (!out_dev && !c.dry())
+      HT_CUDA(cudaMemcpyAsync(x_out, o, sizeof(float) * total, cudaMemcpyDeviceToHost, c.st));
+    return HT_OK;
+  };
+  Ctx d;
+  d.ar.dry = true;
+  HT_TRY(plan(d));
+  const size_t bytes = d.ar.peak + (1 << 20);
+  void *ws = nullptr;
+  HT_TRY(acquire_workspace(bytes, &ws, st));
+  Ctx c;
+  c.st = st;
+  c.ar.base = static_cast<char *>(ws);
+  c.ar.cap = bytes;
+  HT_TRY(plan(c));
+  HT_CUDA(cudaStreamSynchronize(c.st));
+  g_launches += static_cast<unsigned long long>(c.launches);
+  return HT_OK;
+}
+
+ht_status_t ht_evaluate(const long *dims, int order, const ht_tree_t *tree, const float *const *U,
+                        const float *const *B, const long long *idx, long long count, float *out, void *stream) {
+  if (!dims || !U || !B || count < 0) return fail(HT_ERR_INVALID_ARG, "NULL argument or negative count");
+  if (count == 0) return HT_OK;
+  if (!idx || !out) return fail(HT_ERR_INVALID_ARG, "NULL argument");
+  Tree T;
+  HT_TRY(parse_tree(tree, dims, order, T));
+  for (int t = 0; t < T.n_nodes; ++t)
+    if (!(T.leaf(t) ? U[t] : B[t])) return fail(HT_ERR_INVALID_ARG, "missing factor for node " + std::to_string(t));
+  HT_TRY(check_device());
+  std::lock_guard<std::mutex> lk(g_ws_mutex);
+  const bool idx_dev = is_device_ptr(idx), out_dev = is_device_ptr(out);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // children before parents: node ids carry no order, so sort by depth, deepest first
+  EvalTree et{};
+  et.order = order;
+  et.n_nodes = T.n_nodes;
+  int depth[HT_MAX_NODES] = {};
+  for (int t = 1; t < T.n_nodes; ++t)
+    for (int p = T.parent[t]; p >= 0; p = T.parent[p]) ++depth[t];
+  int q = 0;
+  for (int dpt = order; dpt >= 0; --dpt)
+    for (int t = 0; t < T.n_nodes; ++t)
+      if (depth[t] == dpt) et.post[q++] = t;
+  for (int t = 0; t < T.n_nodes; ++t) {
+    et.left[t] = T.left[t];
+    et.right[t] = T.right[t];
+    et.rank[t] = T.rank[t];
+    et.mode[t] = T.leaf(t) ? T.mode_of_leaf(t) : -1;
+  }
+  for (int m = 0; m < order; ++m) et.dim[m] = dims[m];
+  auto plan = [&](Ctx &c) -> ht_status_t {
+    const float *Ud[HT_MAX_NODES] = {}, *Bd[HT_MAX_NODES] = {};
+    c.err = c.ar.take<int>(64);
+    if (!c.err) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small");
+    HT_TRY(stage_factors(c, T, dims, U, B, Ud, Bd));
+    const long long *ix = idx;
+    if (!idx_dev) {
+      long long *tmp = c.ar.take<long long>(static_cast<size_t>(count) * order);
+      if (!tmp) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small");
+      if (!c.dry())
+        HT_CUDA(cudaMemcpyAsync(tmp, idx, sizeof(long long) * count * order, cudaMemcpyHostToDevice, c.st));
+      ix = tmp;
+    }
+    float *o = out_dev ? out : c.ar.take<float>(static_cast<size_t>(count));
+    if (!o) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small");
+    if (!c.dry()) {
+      for (int t = 0; t < T.n_nodes; ++t) {
+        et.U[t] = Ud[t];
+        et.B[t] = Bd[t];
+      }
+      HT_CUDA(cudaMemsetAsync(c.err, 0, sizeof(int), c.st));
+      HT_CUDA(evaluate_launch(et, ix, count, o, c.err, c.st));
+      ++c.launches;
+      if (!out_dev) HT_CUDA(cudaMemcpyAsync(out, o, sizeof(float) * count, cudaMemcpyDeviceToHost, c.st));
+    }
+    return HT_OK;
+  };
+  Ctx d;
+  d.ar.dry = true;
+  HT_TRY(plan(d));
+  const size_t bytes = d.ar.peak + (1 << 20);
+  void *ws = nullptr;
+  HT_TRY(acquire_workspace(bytes, &ws, st));
+  Ctx c;
+  c.st = st;
+  c.ar.base = static_cast<char *>(ws);
+  c.ar.cap = bytes;
+  HT_TRY(plan(c));
+  int errword = 0;
+  HT_CUDA(cudaMemcpyAsync(&errword, c.err, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+  HT_CUDA(cudaStreamSynchronize(c.st));
+  g_launches += static_cast<unsigned long long>(c.launches);
+  if (errword) return fail(HT_ERR_INVALID_ARG, "an index lies outside its mode");
+  return HT_OK;
+}
+
 // Shared driver of the three unfolding primitives.  op 0: Gram, 1: mode product, 2: co-range product.
 static ht_status_t unfolding_op(int op, const float *x, const long *dims, int order, int lo, int hi, const float *Mat,
                                 int k, int precision, float *out, void *stream) {

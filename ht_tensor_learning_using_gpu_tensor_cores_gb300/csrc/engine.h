@@ -173,4 +173,24 @@ cudaError_t sketch_loss_grad(const float *G, const float *trG, int batch, int n,
 cudaError_t sketch_adam(float *S, const float *g, float *m, float *v, long long count, float lr, float b1, float b2,
                         float eps, int step, cudaStream_t st);
 
+// ------------------------------------------------ HT-format operations (htops.cu)
+// Slab z < batch: C + z sC (m x n, ldc) = (A + z sA) (m x k, lda) B^T (n x k, ldb),
+// column-major, k <= 64.
+cudaError_t gemm_nt_launch(const float *A, long long lda, long long sA, const float *B, long long ldb, float *C,
+                           long long ldc, long long sC, long long m, long long n, int k, long long batch,
+                           cudaStream_t s);
+constexpr int kEvalNodes = 7;
+struct EvalTree {
+  int order, n_nodes;
+  int left[kEvalNodes], right[kEvalNodes], rank[kEvalNodes], mode[kEvalNodes];
+  int post[kEvalNodes];              // nodes in post order (children before parents, root last)
+  long long dim[4];
+  const float *U[kEvalNodes];        // leaves: dim x rank, column-major
+  const float *B[kEvalNodes];        // interior nodes and root: k_l x k_r x k_t
+};
+// out[e] = the HT tensor's entry at indices idx[e*order .. e*order + order);
+// an index out of range sets *err to 1.
+cudaError_t evaluate_launch(const EvalTree &et, const long long *idx, long long count, float *out, int *err,
+                            cudaStream_t s);
+
 }  // namespace htgb

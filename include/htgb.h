@@ -126,6 +126,25 @@ ht_status_t ht_reconstruct_error(const float *x, const long *dims, int order,
                                  const float *const *U, const float *const *B,
                                  double *rel_err, void *stream);
 
+/* ------------------------------------------------------ HT-format operations */
+/* Full tensor Xhat (column-major, dims[0..order)) of an HT representation.
+ * Replaces the reference's reconstruction by node bases
+ * (third_order_tensor_decompsition/CUDA/Optimized/htd_tensorcore.cu:295-331,
+ * htd_batch.cu:196-244), which it only uses to measure the error.  Factors and
+ * x_out may be host or device memory; returns after the result is complete. */
+ht_status_t ht_reconstruct(const long *dims, int order, const ht_tree_t *tree,
+                           const float *const *U, const float *const *B,
+                           float *x_out, void *stream);
+
+/* Entries of an HT representation at count index tuples, without forming the
+ * tensor: out[e] = Xhat(idx[e*order], ..., idx[e*order + order - 1]), 0-based.
+ * Each entry is contracted from the leaf rows to the root (cost
+ * sum_t k_l k_r k_t per entry).  An index outside its mode returns
+ * HT_ERR_INVALID_ARG.  idx and out may be host or device memory. */
+ht_status_t ht_evaluate(const long *dims, int order, const ht_tree_t *tree,
+                        const float *const *U, const float *const *B,
+                        const long long *idx, long long count, float *out, void *stream);
+
 /* ---------------------------------------------------- unfolding primitives */
 /* The three matricisation products the decomposition is built from, exposed
  * for direct use.  Modes lo..hi (0-based, contiguous) form the group g; with

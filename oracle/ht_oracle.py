@@ -143,6 +143,23 @@ def ht_reconstruct(tree: DimTree, dims: Sequence[int], U: Dict[int, np.ndarray],
     return fold(M, tree.modes[l], dims)
 
 
+def ht_entries(tree: DimTree, U: Dict[int, np.ndarray], B: Dict[int, np.ndarray], idx: np.ndarray) -> np.ndarray:
+    """Entries Xhat[idx[e]] contracted leaf-to-root without forming Xhat: a leaf
+    contributes the row U_t[i_m, :], an interior node
+    v_t[c] = sum_{a,b} B_t[a, b, c] v_l[a] v_r[b], and the root's v_0[0] is the
+    entry.  The same contraction as ht_reconstruct's node bases
+    (htd_batch.cu:196-224), restricted to one row of each."""
+    idx = np.asarray(idx, dtype=np.int64)
+
+    def vec(t):
+        if tree.is_leaf(t):
+            return U[t][idx[:, tree.modes[t][0]], :].astype(np.float64)
+        vl, vr = vec(tree.left[t]), vec(tree.right[t])
+        return np.einsum("ea,eb,abc->ec", vl, vr, np.asarray(B[t], np.float64), optimize=True)
+
+    return vec(0)[:, 0]
+
+
 def rel_error(X: np.ndarray, Xh: np.ndarray) -> float:
     """||X - Xhat||_F / ||X||_F in float64 (htd_batch.cu:237-244)."""
     X = np.asarray(X, dtype=np.float64)
