@@ -25,7 +25,8 @@ EXPORTED = ["ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", 
             "ht_status_string", "ht_last_error", "ht_kernel_launch_count", "htd", "htd4",
             "ht_mode_gram", "ht_mode_product", "ht_corange_product", "ht_mode_gram_noalloc",
             "ht_decompose_batched", "ht_release_batch", "ht_sketch_loss_grad", "ht_sketch_adam",
-            "ht_reconstruct", "ht_evaluate"]
+            "ht_reconstruct", "ht_evaluate", "ht_layer_weight", "ht_layer_forward", "ht_layer_backward",
+            "ht_layer_check", "ht_layer_release"]
 
 
 class HtTree(Structure):
@@ -47,6 +48,10 @@ class HtReport(Structure):
 class HtBatchReport(Structure):
     _fields_ = [("rel_err_p50", c_double), ("rel_err_p99", c_double), ("rel_err_max", c_double),
                 ("ms_total", c_float), ("gpu_launches", c_int), ("graph_replayed", c_int), ("lanes", c_int)]
+
+
+class HtLayerShape(Structure):
+    _fields_ = [("n", c_int * 3), ("m", c_int * 3), ("r", c_int * 4)]
 
 
 class HTError(RuntimeError):
@@ -81,6 +86,13 @@ def lib():
                                  c_void_p, c_void_p]
     L.ht_evaluate.argtypes = [POINTER(c_long), c_int, POINTER(HtTree), POINTER(c_void_p), POINTER(c_void_p),
                               c_void_p, c_longlong, c_void_p, c_void_p]
+    L.ht_layer_weight.argtypes = [POINTER(HtLayerShape)] + [c_void_p] * 7
+    L.ht_layer_forward.argtypes = [POINTER(HtLayerShape)] + [c_void_p] * 6 + [c_int, c_int, c_void_p, c_longlong,
+                                                                              c_void_p, c_void_p]
+    L.ht_layer_backward.argtypes = [POINTER(HtLayerShape)] + [c_void_p] * 5 + [c_int, c_void_p, c_void_p, c_longlong] \
+        + [c_void_p] * 8
+    L.ht_layer_check.argtypes = []
+    L.ht_layer_release.argtypes = []
     L.ht_workspace_size.argtypes = [POINTER(c_long), c_int, POINTER(HtTree), POINTER(HtConfig), POINTER(c_ulonglong)]
     L.ht_release_workspace.argtypes = []
     L.ht_status_string.argtypes = [c_int]
@@ -106,7 +118,8 @@ def lib():
     L.ht_sketch_adam.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_longlong, c_float, c_int, c_void_p]
     L.ht_corange_product.argtypes = [c_void_p, POINTER(c_long), c_int, c_int, c_int, c_void_p, c_int, c_int,
                                      c_void_p, c_void_p]
-    for name in ("ht_reconstruct", "ht_evaluate", "ht_sketch_loss_grad", "ht_sketch_adam", "ht_decompose_batched", "ht_release_batch", "ht_mode_gram", "ht_mode_gram_noalloc", "ht_mode_product", "ht_corange_product", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
+    for name in ("ht_layer_weight", "ht_layer_forward", "ht_layer_backward", "ht_layer_check", "ht_layer_release",
+                 "ht_reconstruct", "ht_evaluate", "ht_sketch_loss_grad", "ht_sketch_adam", "ht_decompose_batched", "ht_release_batch", "ht_mode_gram", "ht_mode_gram_noalloc", "ht_mode_product", "ht_corange_product", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
                  "ht_decompose", "ht_reconstruct_error", "ht_workspace_size", "ht_release_workspace"):
         getattr(L, name).restype = c_int
     _lib = L

@@ -253,7 +253,9 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
   TileGen gen;
   if (q.tiles_kind == TILES_ROWS) gen = make_rows_gen(q.t_rows, q.t_cols, bn);
   else if (q.tiles_kind == TILES_SLABS) gen = make_slabs_gen(q.t_L, q.t_R, q.t_cols, bn);
-  else if (!make_gram_gen(q.t_n, bn, &gen, 128 * mt)) return fail(HT_ERR_UNSUPPORTED, "Gram larger than 32768");
+  else if (q.tiles_kind == TILES_GRID) {
+    if (!make_grid_gen(q.t_rows, q.t_n, bn, &gen)) return fail(HT_ERR_UNSUPPORTED, "product too large for one grid");
+  } else if (!make_gram_gen(q.t_n, bn, &gen, 128 * mt)) return fail(HT_ERR_UNSUPPORTED, "Gram larger than 32768");
   const int nt = gen.count;
   int splits = 1;
   if (q.allow_split && nt < sm_count()) splits = std::max(1, sm_count() / nt);
@@ -1803,6 +1805,293 @@ void htd4(float *x, long a, long b, long c, long d, int *k, void *cublas_handle,
     return;
   }
   std::printf("error rate %g\n", rep.rel_err);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ HT tensor layer
+// Forward:  P, Q from the factors; W (Nout x Nin) from P, Q; one GEMM
+//           y^T = W x^T (rows o, columns z, i.e. y row-major); bias + activation.
+// Backward: P, Q, T1 and W again; dx = dy W and dW = dy^T x as GEMMs; dbias as
+//           column sums of dy; dP, dQ from dW; the factor gradients from dP, dQ.
+namespace {
+
+std::mutex g_layer_mutex;
+DeviceWorkspace g_layer_ws[64];
+int *g_layer_err[64];   // first 256 bytes of each device's layer workspace
+
+ht_status_t layer_shape(const ht_layer_shape_t *in, LayerShape *sh) {
+  if (!in) return fail(HT_ERR_INVALID_ARG, "shape is NULL");
+  long long nin = 1, nout = 1;
+  for (int j = 0; j < 3; ++j) {
+    if (in->n[j] < 1 || in->m[j] < 1) return fail(HT_ERR_INVALID_ARG, "mode sizes must be positive");
+    sh->n[j] = in->n[j];
+    sh->m[j] = in->m[j];
+    nin *= in->n[j];
+    nout *= in->m[j];
+  }
+  for (int j = 0; j < 4; ++j)
+    if (in->r[j] < 1 || in->r[j] > kLayerMaxRank) return fail(HT_ERR_UNSUPPORTED, "layer ranks must lie in [1, 64]");
+  if (nin > (1ll << 28) || nout > (1ll << 28) || nin * nout > (1ll << 34))
+    return fail(HT_ERR_UNSUPPORTED, "layer too large");
+  const long long A = static_cast<long long>(in->n[0]) * in->m[0], B = static_cast<long long>(in->n[1]) * in->m[1],
+                  C = static_cast<long long>(in->n[2]) * in->m[2];
+  if (A * B > (1ll << 31) - 1 || C * 4 > 48 * 1024)
+    return fail(HT_ERR_UNSUPPORTED, "layer mode products too large (n[2]*m[2] <= 12288)");
+  sh->r3 = in->r[0];
+  sh->r4 = in->r[1];
+  sh->r2 = in->r[2];
+  sh->r1 = in->r[3];
+  return HT_OK;
+}
+
+long long layer_nin(const LayerShape &s) { return static_cast<long long>(s.n[0]) * s.n[1] * s.n[2]; }
+long long layer_nout(const LayerShape &s) { return static_cast<long long>(s.m[0]) * s.m[1] * s.m[2]; }
+size_t layer_p_count(const LayerShape &s) {
+  return static_cast<size_t>(s.n[0]) * s.m[0] * s.n[1] * s.m[1] * s.r1;
+}
+size_t layer_q_count(const LayerShape &s) { return static_cast<size_t>(s.n[2]) * s.m[2] * s.r1; }
+size_t layer_t1_count(const LayerShape &s) { return static_cast<size_t>(s.n[0]) * s.m[0] * s.r4 * s.r1; }
+
+ht_status_t layer_check_ptrs(std::initializer_list<const void *> ptrs) {
+  for (const void *p : ptrs)
+    if (p && !is_device_ptr(p)) return fail(HT_ERR_INVALID_ARG, "HT layer arguments must be device memory");
+  return HT_OK;
+}
+
+// Run plan() as a dry run to size the workspace, grow the device's layer
+// workspace if needed (synchronising only then) and run it for real.
+template <class F>
+ht_status_t layer_run(cudaStream_t st, bool tc, F &&plan) {
+  int dev = 0;
+  HT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(HT_ERR_INVALID_ARG, "device index out of range");
+  Ctx d;
+  d.ar.dry = true;
+  d.tc = tc;
+  HT_TRY(plan(d));
+  const size_t bytes = d.ar.peak + 256 + (1 << 16);
+  std::lock_guard<std::mutex> lk(g_layer_mutex);
+  DeviceWorkspace &w = g_layer_ws[dev];
+  if (w.bytes < bytes) {
+    if (w.ptr) {
+      HT_CUDA(cudaDeviceSynchronize());
+      HT_CUDA(cudaFree(w.ptr));
+      w.ptr = nullptr;
+      w.bytes = 0;
+    }
+    HT_CUDA(cudaMalloc(&w.ptr, bytes));
+    HT_CUDA(cudaMemset(w.ptr, 0, 256));
+    HT_CUDA(cudaDeviceSynchronize());
+    w.bytes = bytes;
+    g_layer_err[dev] = static_cast<int *>(w.ptr);
+  }
+  Ctx c;
+  c.st = st;
+  c.tc = tc;
+  c.err = g_layer_err[dev];
+  c.ar.base = static_cast<char *>(w.ptr) + 256;
+  c.ar.cap = w.bytes - 256;
+  HT_TRY(plan(c));
+  g_launches += static_cast<unsigned long long>(c.launches);
+  return HT_OK;
+}
+
+// D (rows x cols, column-major, ld = rows) = A B^T over the two operand pairs.
+ht_status_t layer_gemm(Ctx &c, const Operand &a32, const Operand &b32, const Operand &a16, const Operand &b16,
+                       long long rows, long long cols, float *D) {
+  GemmReq q;
+  q.a32 = a32;
+  q.b32 = b32;
+  q.a16 = a16;
+  q.b16 = b16;
+  q.bn_tc = cols >= 256 ? 256 : (cols > 64 ? 128 : 64);
+  q.bn_simt = cols > 64 ? 128 : 64;
+  q.tiles_kind = TILES_GRID;
+  q.t_rows = rows;
+  q.t_n = cols;
+  q.out_mode = OUT_COLMAJOR;
+  q.out = D;
+  q.ld_out = rows;
+  if (c.tc) {   // the FP32 operands may be absent here: no SIMT fallback
+    GemmArgs probe;
+    probe.a = a16;
+    probe.b = b16;
+    probe.splits = 1;
+    std::string why;
+    if (!a16.ptr || !b16.ptr || !tc_gemm_supported(probe, q.bn_tc, &why))
+      return fail(HT_ERR_UNSUPPORTED, "BF16 layer product not expressible as TMA tiles: " + why);
+  }
+  return run_gemm(c, q);
+}
+
+Operand op_of(int kind, const void *p, long d0, long d1) {
+  Operand o;
+  o.kind = kind;
+  o.ptr = p;
+  o.d0 = d0;
+  o.d1 = d1;
+  o.d2 = 1;
+  return o;
+}
+
+}  // namespace
+
+extern "C" {
+
+ht_status_t ht_layer_weight(const ht_layer_shape_t *shape, const float *u1, const float *u2, const float *u3,
+                            const float *b2, const float *b1, float *W, void *stream) {
+  LayerShape sh;
+  HT_TRY(layer_shape(shape, &sh));
+  if (!u1 || !u2 || !u3 || !b2 || !b1 || !W) return fail(HT_ERR_INVALID_ARG, "NULL argument");
+  HT_TRY(check_device());
+  HT_TRY(layer_check_ptrs({u1, u2, u3, b2, b1, W}));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  return layer_run(st, false, [&](Ctx &c) -> ht_status_t {
+    float *P = c.ar.take<float>(layer_p_count(sh));
+    float *Q = c.ar.take<float>(layer_q_count(sh));
+    if (!P || !Q) return fail(HT_ERR_OUT_OF_MEMORY, "layer workspace too small");
+    if (c.dry()) return HT_OK;
+    HT_CUDA(layer_pq_launch(sh, u1, u2, u3, b2, b1, P, Q, nullptr, c.st));
+    HT_CUDA(layer_weight_launch(sh, P, Q, W, nullptr, c.st));
+    c.launches += 2;
+    return HT_OK;
+  });
+}
+
+ht_status_t ht_layer_forward(const ht_layer_shape_t *shape, const float *u1, const float *u2, const float *u3,
+                             const float *b2, const float *b1, const float *bias, int activation, int precision,
+                             const float *x, long long batch, float *y, void *stream) {
+  LayerShape sh;
+  HT_TRY(layer_shape(shape, &sh));
+  if (!u1 || !u2 || !u3 || !b2 || !b1 || !x || !y) return fail(HT_ERR_INVALID_ARG, "NULL argument");
+  if (batch < 1 || batch > (1ll << 31) - 256) return fail(HT_ERR_INVALID_ARG, "batch must lie in [1, 2^31)");
+  if (activation != 0 && activation != 1) return fail(HT_ERR_INVALID_ARG, "activation must be 0 or 1");
+  if (precision != HT_PREC_FP32 && precision != HT_PREC_BF16) return fail(HT_ERR_INVALID_ARG, "bad precision");
+  const long long nin = layer_nin(sh), nout = layer_nout(sh);
+  const bool tc = precision == HT_PREC_BF16;
+  if (tc && (nin % 8 || nout % 8))
+    return fail(HT_ERR_UNSUPPORTED, "the BF16 layer needs n0*n1*n2 and m0*m1*m2 divisible by 8");
+  HT_TRY(check_device());
+  HT_TRY(layer_check_ptrs({u1, u2, u3, b2, b1, bias, x, y}));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  return layer_run(st, tc, [&](Ctx &c) -> ht_status_t {
+    float *P = c.ar.take<float>(layer_p_count(sh));
+    float *Q = c.ar.take<float>(layer_q_count(sh));
+    float *W32 = tc ? nullptr : c.ar.take<float>(static_cast<size_t>(nin * nout));
+    __nv_bfloat16 *W16 = tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(nin * nout)) : nullptr;
+    __nv_bfloat16 *x16 = tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(batch * nin)) : nullptr;
+    if (!P || !Q || !(W32 || W16) || (tc && !x16)) return fail(HT_ERR_OUT_OF_MEMORY, "layer workspace too small");
+    if (!c.dry()) {
+      HT_CUDA(layer_pq_launch(sh, u1, u2, u3, b2, b1, P, Q, nullptr, c.st));
+      HT_CUDA(layer_weight_launch(sh, P, Q, W32, W16, c.st));
+      if (tc) HT_CUDA(f32_to_bf16_launch(x, x16, batch * nin, c.st));
+      c.launches += tc ? 3 : 2;
+    }
+    // y^T (nout x batch, column-major) = W x^T: A = W (rows o, K-major), B = x (rows z, K-major)
+    HT_TRY(layer_gemm(c, op_of(OP_KM3, W32, nin, nout), op_of(OP_KM3, x, nin, batch),
+                      op_of(OP_KM3, W16, nin, nout), op_of(OP_KM3, x16, nin, batch), nout, batch, y));
+    if (!c.dry() && (bias || activation)) {
+      HT_CUDA(bias_act_launch(y, bias, batch, nout, activation, c.st));
+      ++c.launches;
+    }
+    return HT_OK;
+  });
+}
+
+ht_status_t ht_layer_backward(const ht_layer_shape_t *shape, const float *u1, const float *u2, const float *u3,
+                              const float *b2, const float *b1, int precision, const float *x, const float *dy,
+                              long long batch, float *dx, float *du1, float *du2, float *du3, float *db2,
+                              float *db1, float *dbias, void *stream) {
+  LayerShape sh;
+  HT_TRY(layer_shape(shape, &sh));
+  if (!u1 || !u2 || !u3 || !b2 || !b1 || !x || !dy || !du1 || !du2 || !du3 || !db2 || !db1)
+    return fail(HT_ERR_INVALID_ARG, "NULL argument");
+  if (batch < 1 || batch > (1ll << 31) - 256) return fail(HT_ERR_INVALID_ARG, "batch must lie in [1, 2^31)");
+  if (precision != HT_PREC_FP32 && precision != HT_PREC_BF16) return fail(HT_ERR_INVALID_ARG, "bad precision");
+  const long long nin = layer_nin(sh), nout = layer_nout(sh);
+  const bool tc = precision == HT_PREC_BF16;
+  if (tc && (nin % 8 || nout % 8))
+    return fail(HT_ERR_UNSUPPORTED, "the BF16 layer needs n0*n1*n2 and m0*m1*m2 divisible by 8");
+  HT_TRY(check_device());
+  HT_TRY(layer_check_ptrs({u1, u2, u3, b2, b1, x, dy, dx, du1, du2, du3, db2, db1, dbias}));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  return layer_run(st, tc, [&](Ctx &c) -> ht_status_t {
+    float *P = c.ar.take<float>(layer_p_count(sh));
+    float *Q = c.ar.take<float>(layer_q_count(sh));
+    float *T1 = c.ar.take<float>(layer_t1_count(sh));
+    float *dP = c.ar.take<float>(layer_p_count(sh));
+    float *dQ = c.ar.take<float>(layer_q_count(sh));
+    float *dT1 = c.ar.take<float>(layer_t1_count(sh));
+    float *dW = c.ar.take<float>(static_cast<size_t>(nin * nout));
+    float *W32 = (!tc && dx) ? c.ar.take<float>(static_cast<size_t>(nin * nout)) : nullptr;
+    __nv_bfloat16 *W16 = (tc && dx) ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(nin * nout)) : nullptr;
+    __nv_bfloat16 *x16 = tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(batch * nin)) : nullptr;
+    __nv_bfloat16 *dy16 = tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(batch * nout)) : nullptr;
+    float *part = dbias ? c.ar.take<float>(static_cast<size_t>(layer_colsum_chunks(batch)) * nout) : nullptr;
+    if (!P || !Q || !T1 || !dP || !dQ || !dT1 || !dW || (dx && !(W32 || W16)) || (tc && (!x16 || !dy16)) ||
+        (dbias && !part))
+      return fail(HT_ERR_OUT_OF_MEMORY, "layer workspace too small");
+    if (!c.dry()) {
+      HT_CUDA(layer_pq_launch(sh, u1, u2, u3, b2, b1, P, Q, T1, c.st));
+      ++c.launches;
+      if (dx) {
+        HT_CUDA(layer_weight_launch(sh, P, Q, W32, W16, c.st));
+        ++c.launches;
+      }
+      if (tc) {
+        HT_CUDA(f32_to_bf16_launch(x, x16, batch * nin, c.st));
+        HT_CUDA(f32_to_bf16_launch(dy, dy16, batch * nout, c.st));
+        c.launches += 2;
+      }
+    }
+    if (dx)   // dx^T (nin x batch) = W^T dy^T: A = W^T (rows i, MN-major), B = dy (rows z, K-major)
+      HT_TRY(layer_gemm(c, op_of(OP_MN3, W32, nin, nout), op_of(OP_KM3, dy, nout, batch),
+                        op_of(OP_MN3, W16, nin, nout), op_of(OP_KM3, dy16, nout, batch), nin, batch, dx));
+    // dW^T (nin x nout, column-major = dW row-major) = x^T dy: A = x^T (rows i), B = dy^T (rows o), K = z
+    HT_TRY(layer_gemm(c, op_of(OP_MN3, x, nin, batch), op_of(OP_MN3, dy, nout, batch),
+                      op_of(OP_MN3, x16, nin, batch), op_of(OP_MN3, dy16, nout, batch), nin, nout, dW));
+    if (!c.dry()) {
+      if (dbias) {
+        HT_CUDA(layer_colsum_launch(dy, batch, nout, part, dbias, c.st));
+        c.launches += 2;
+      }
+      HT_CUDA(layer_factor_grads_launch(sh, dW, u1, u2, u3, b2, b1, P, Q, T1, dP, dQ, dT1, du1, du2, du3, db2, db1,
+                                        c.st));
+      c.launches += 4;
+    }
+    return HT_OK;
+  });
+}
+
+ht_status_t ht_layer_check(void) {
+  int dev = 0;
+  HT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(HT_ERR_INVALID_ARG, "device index out of range");
+  HT_CUDA(cudaDeviceSynchronize());
+  std::lock_guard<std::mutex> lk(g_layer_mutex);
+  if (!g_layer_err[dev]) return HT_OK;
+  int w = 0;
+  HT_CUDA(cudaMemcpy(&w, g_layer_err[dev], sizeof(int), cudaMemcpyDeviceToHost));
+  HT_CUDA(cudaMemset(g_layer_err[dev], 0, sizeof(int)));
+  if (w & kErrTimeout) return fail(HT_ERR_TIMEOUT, "a wait inside an HT layer kernel timed out");
+  return HT_OK;
+}
+
+ht_status_t ht_layer_release(void) {
+  int dev = 0;
+  HT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(HT_ERR_INVALID_ARG, "device index out of range");
+  std::lock_guard<std::mutex> lk(g_layer_mutex);
+  DeviceWorkspace &w = g_layer_ws[dev];
+  if (w.ptr) {
+    HT_CUDA(cudaDeviceSynchronize());
+    HT_CUDA(cudaFree(w.ptr));
+  }
+  w.ptr = nullptr;
+  w.bytes = 0;
+  g_layer_err[dev] = nullptr;
+  return HT_OK;
 }
 
 }  // extern "C"

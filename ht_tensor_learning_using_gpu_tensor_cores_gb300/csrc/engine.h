@@ -48,7 +48,8 @@ enum OutMode : int { OUT_PARTIAL = 0, OUT_COLMAJOR = 1 };
 enum TileKind : int {
   TILES_ROWS = 0,   // rows [0, rows) in blocks of 128, one column block
   TILES_SLABS = 1,  // (l-block, r) blocks of a (L, *, R) view, out_row = l + L*r
-  TILES_GRAM = 2    // blocks of an n x n symmetric matrix on or above the diagonal
+  TILES_GRAM = 2,   // blocks of an n x n symmetric matrix on or above the diagonal
+  TILES_GRID = 3    // bm x bn blocks of a rows x n output, row block fastest
 };
 constexpr int kMaxGramRows = 256;   // n <= 32768
 struct TileGen {
@@ -100,6 +101,8 @@ cudaError_t reduce_partials_launch(const float *partial, const TileGen &gen, int
                                    long long ld_out, int symmetric, cudaStream_t s);
 TileGen make_rows_gen(long long rows, int cols, int bn);
 TileGen make_slabs_gen(long long L, long long R, int cols, int bn);
+// rows x cols output in 128 x bn tiles (TILES_GRID); false when the tile count overflows
+bool make_grid_gen(long long rows, long long cols, int bn, TileGen *g);
 bool make_gram_gen(long long n, int bn, TileGen *g, int bm = 128);
 
 // --------------------------------------------------------------- small ops
@@ -192,5 +195,31 @@ struct EvalTree {
 // an index out of range sets *err to 1.
 cudaError_t evaluate_launch(const EvalTree &et, const long long *idx, long long count, float *out, int *err,
                             cudaStream_t s);
+
+// ------------------------------------------------------ HT tensor layer (layer.cu)
+constexpr int kLayerMaxRank = 64;
+// u1 (n0, m0, r3), u2 (n1, m1, r4), u3 (n2, m2, r2), b2 (r3, r4, r1), b1 (r1, r2), C-order
+struct LayerShape {
+  int n[3], m[3];
+  int r1, r2, r3, r4;
+};
+// P[a, b, r1] (A x B x r1), Q[c, r1] (C x r1) and, when T1 is non-null,
+// T1[a, r4, r1] = sum_r3 u1[a, r3] b2[r3, r4, r1]
+cudaError_t layer_pq_launch(const LayerShape &sh, const float *u1, const float *u2, const float *u3, const float *b2,
+                            const float *b1, float *P, float *Q, float *T1, cudaStream_t s);
+// W (Nout x Nin, row-major) from P and Q, into W32 (FP32) or, when W32 is null, W16 (BF16)
+cudaError_t layer_weight_launch(const LayerShape &sh, const float *P, const float *Q, float *W32, __nv_bfloat16 *W16,
+                                cudaStream_t s);
+// y[z, o] = act(y[z, o] + bias[o]) (bias may be null; act 0 identity, 1 ReLU)
+cudaError_t bias_act_launch(float *y, const float *bias, long long batch, long long nout, int act, cudaStream_t s);
+// out[o] = sum_z dy[z, o]; part holds layer_colsum_chunks(batch) * nout floats
+int layer_colsum_chunks(long long batch);
+cudaError_t layer_colsum_launch(const float *dy, long long batch, long long nout, float *part, float *out,
+                                cudaStream_t s);
+// du1, du2, du3, db2, db1 from dW (Nout x Nin, row-major), via dP, dQ, dT1 (scratch of P, Q, T1's sizes)
+cudaError_t layer_factor_grads_launch(const LayerShape &sh, const float *dW, const float *u1, const float *u2,
+                                      const float *u3, const float *b2, const float *b1, const float *P,
+                                      const float *Q, const float *T1, float *dP, float *dQ, float *dT1, float *du1,
+                                      float *du2, float *du3, float *db2, float *db1, cudaStream_t s);
 
 }  // namespace htgb

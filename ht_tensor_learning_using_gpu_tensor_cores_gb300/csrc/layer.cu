@@ -1,0 +1,330 @@
+// HT tensor layer: a fully connected layer whose weight is held in HT format.
+//
+// The reference's layer (HT_tensor_layer/FC_MNIST/mnist_ht.py:232-245 and
+// Alex_ImageNet/model/alexnet.py:157-170) maps x[z, n0, n1, n2] to
+// y[z, m0, m1, m2] through the einsum chain
+//   x u1[n0,m0,r3] -> b2[r3,r4,r1] -> u2[n1,m1,r4] -> b1[r1,r2] -> u3[n2,m2,r2],
+// i.e. y = x W^T with
+//   W[(m0,m1,m2), (n0,n1,n2)] = sum_{r1} P[a, b, r1] Q[c, r1],
+//   P[a, b, r1] = sum_{r3,r4} u1[a, r3] u2[b, r4] b2[r3, r4, r1],   a = n0 M0 + m0, b = n1 M1 + m1
+//   Q[c, r1]    = sum_{r2} b1[r1, r2] u3[c, r2],                     c = n2 M2 + m2.
+// The chain costs more multiply-adds per sample than the dense product at the
+// reference's shapes (rank 16 on 8 x 8 x 16 modes), so here the weight is formed
+// once per call from the factors (batch-independent, L2-resident) and the batch
+// goes through one GEMM; the kernels in this file form P, Q and W, add the
+// bias, and carry the gradients back from dW to the factors.
+//
+// All parameter tensors use the reference's C-order layouts:
+// u_j (N_j, M_j, r_j), b2 (r3, r4, r1), b1 (r1, r2), bias (M0, M1, M2).
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+#include "engine.h"
+
+namespace htgb {
+namespace {
+
+constexpr int kLayerThreads = 256;
+
+int grid_for_layer(long long n) {
+  long long g = (n + kLayerThreads - 1) / kLayerThreads;
+  if (g > 152 * 32) g = 152 * 32;
+  return static_cast<int>(g < 1 ? 1 : g);
+}
+
+// Blocks [0, A): T1[a] = u1[a, :] b2 (r4 x r1, in shared memory, also written to
+// T1g when non-null), then P[a, b, r1] for every b.  Blocks [A, A + qb): Q.
+__global__ void __launch_bounds__(kLayerThreads) layer_pq_kernel(const LayerShape sh, const float *__restrict__ u1,
+                                                                 const float *__restrict__ u2,
+                                                                 const float *__restrict__ u3,
+                                                                 const float *__restrict__ b2,
+                                                                 const float *__restrict__ b1, float *__restrict__ P,
+                                                                 float *__restrict__ Q, float *__restrict__ T1g) {
+  __shared__ float T1[kLayerMaxRank * kLayerMaxRank];
+  const int A = sh.n[0] * sh.m[0], B = sh.n[1] * sh.m[1], C = sh.n[2] * sh.m[2];
+  const int R1 = sh.r1, R2 = sh.r2, R3 = sh.r3, R4 = sh.r4;
+  if (static_cast<int>(blockIdx.x) < A) {
+    const int a = blockIdx.x;
+    for (int e = threadIdx.x; e < R4 * R1; e += kLayerThreads) {
+      const int r4 = e / R1, r1 = e - r4 * R1;
+      float s = 0.f;
+      for (int r3 = 0; r3 < R3; ++r3) s = fmaf(u1[a * R3 + r3], b2[(r3 * R4 + r4) * R1 + r1], s);
+      T1[e] = s;
+      if (T1g) T1g[static_cast<long long>(a) * R4 * R1 + e] = s;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < B * R1; e += kLayerThreads) {
+      const int b = e / R1, r1 = e - b * R1;
+      float s = 0.f;
+      for (int r4 = 0; r4 < R4; ++r4) s = fmaf(T1[r4 * R1 + r1], u2[b * R4 + r4], s);
+      P[(static_cast<long long>(a) * B + b) * R1 + r1] = s;
+    }
+  } else {
+    const long long e = static_cast<long long>(blockIdx.x - A) * kLayerThreads + threadIdx.x;
+    if (e >= static_cast<long long>(C) * R1) return;
+    const int c = static_cast<int>(e / R1), r1 = static_cast<int>(e - static_cast<long long>(c) * R1);
+    float s = 0.f;
+    for (int r2 = 0; r2 < R2; ++r2) s = fmaf(b1[r1 * R2 + r2], u3[c * R2 + r2], s);
+    Q[e] = s;
+  }
+}
+
+template <class T>
+HT_DEV T from_f32(float v);
+template <>
+HT_DEV float from_f32<float>(float v) { return v; }
+template <>
+HT_DEV __nv_bfloat16 from_f32<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+
+// W[o * Nin + i] = sum_r1 P[a, b, r1] Q[c, r1]; i = (n0 N1 + n1) N2 + n2 runs
+// fastest, so consecutive threads share (a, b) and read P's row once.
+template <class T>
+__global__ void __launch_bounds__(kLayerThreads) layer_weight_kernel(const LayerShape sh, const float *__restrict__ P,
+                                                                     const float *__restrict__ Q, T *__restrict__ W) {
+  const int N1 = sh.n[1], N2 = sh.n[2], M0 = sh.m[0], M1 = sh.m[1], M2 = sh.m[2];
+  const long long Nin = static_cast<long long>(sh.n[0]) * N1 * N2, Nout = static_cast<long long>(M0) * M1 * M2;
+  const int B = N1 * M1, R1 = sh.r1;
+  for (long long e = blockIdx.x * static_cast<long long>(kLayerThreads) + threadIdx.x; e < Nin * Nout;
+       e += static_cast<long long>(gridDim.x) * kLayerThreads) {
+    const long long o = e / Nin, i = e - o * Nin;
+    const int n2 = static_cast<int>(i % N2), n1 = static_cast<int>((i / N2) % N1), n0 = static_cast<int>(i / N2 / N1);
+    const int m2 = static_cast<int>(o % M2), m1 = static_cast<int>((o / M2) % M1), m0 = static_cast<int>(o / M2 / M1);
+    const int a = n0 * M0 + m0, b = n1 * M1 + m1, c = n2 * M2 + m2;
+    const float *p = P + (static_cast<long long>(a) * B + b) * R1;
+    const float *q = Q + static_cast<long long>(c) * R1;
+    float s = 0.f;
+    for (int r = 0; r < R1; ++r) s = fmaf(p[r], q[r], s);
+    W[e] = from_f32<T>(s);
+  }
+}
+
+// y[z, o] = act(y[z, o] + bias[o]), act 0 = identity, 1 = ReLU
+__global__ void bias_act_kernel(float *__restrict__ y, const float *__restrict__ bias, long long batch, long long nout,
+                                int act) {
+  for (long long e = blockIdx.x * static_cast<long long>(kLayerThreads) + threadIdx.x; e < batch * nout;
+       e += static_cast<long long>(gridDim.x) * kLayerThreads) {
+    float v = y[e];
+    if (bias) v += bias[e % nout];
+    if (act == 1) v = fmaxf(v, 0.f);
+    y[e] = v;
+  }
+}
+
+// dbias[o] = sum_z dy[z, o]: one thread per o, the batch split over blockIdx.y
+// partials summed in a fixed order by layer_colsum_finish_kernel.
+__global__ void layer_colsum_kernel(const float *__restrict__ dy, long long batch, long long nout, int chunks,
+                                    float *__restrict__ part) {
+  const long long o = blockIdx.x * static_cast<long long>(kLayerThreads) + threadIdx.x;
+  if (o >= nout) return;
+  const long long per = (batch + chunks - 1) / chunks;
+  const long long z0 = per * blockIdx.y, z1 = min(batch, z0 + per);
+  float s = 0.f;
+  for (long long z = z0; z < z1; ++z) s += dy[z * nout + o];
+  part[static_cast<long long>(blockIdx.y) * nout + o] = s;
+}
+
+__global__ void layer_colsum_finish_kernel(const float *__restrict__ part, long long nout, int chunks,
+                                           float *__restrict__ out) {
+  const long long o = blockIdx.x * static_cast<long long>(kLayerThreads) + threadIdx.x;
+  if (o >= nout) return;
+  float s = 0.f;
+  for (int c = 0; c < chunks; ++c) s += part[static_cast<long long>(c) * nout + o];
+  out[o] = s;
+}
+
+// dP[a, b, r1] = sum_{n2, m2} dW[o, i] Q[c, r1] and, in the same pass over dW,
+// per-(a, b) block contributions to dQ.  One block per (a, b): the M2 x N2
+// sub-block of dW it owns is staged in shared memory.
+//   dQpart[(a, b), c, r1] is not formed: dQ is summed by layer_dq_kernel.
+__global__ void __launch_bounds__(kLayerThreads) layer_dp_kernel(const LayerShape sh, const float *__restrict__ dW,
+                                                                 const float *__restrict__ Q, float *__restrict__ dP) {
+  extern __shared__ float sm[];
+  const int N1 = sh.n[1], N2 = sh.n[2], M0 = sh.m[0], M1 = sh.m[1], M2 = sh.m[2];
+  const long long Nin = static_cast<long long>(sh.n[0]) * N1 * N2;
+  const int B = N1 * M1, C = N2 * M2, R1 = sh.r1;
+  const int ab = blockIdx.x, a = ab / B, b = ab - a * B;
+  const int n0 = a / M0, m0 = a - n0 * M0, n1 = b / M1, m1 = b - n1 * M1;
+  float *blk = sm;   // [c = n2 M2 + m2]
+  for (int e = threadIdx.x; e < C; e += kLayerThreads) {
+    const int n2 = e / M2, m2 = e - n2 * M2;
+    const long long o = (static_cast<long long>(m0) * M1 + m1) * M2 + m2;
+    const long long i = (static_cast<long long>(n0) * N1 + n1) * N2 + n2;
+    blk[e] = dW[o * Nin + i];
+  }
+  __syncthreads();
+  for (int r1 = threadIdx.x; r1 < R1; r1 += kLayerThreads) {
+    float s = 0.f;
+    for (int c = 0; c < C; ++c) s = fmaf(blk[c], Q[static_cast<long long>(c) * R1 + r1], s);
+    dP[static_cast<long long>(ab) * R1 + r1] = s;
+  }
+}
+
+// dQ[c, r1] = sum_{a, b} dW[o, i] P[a, b, r1]: one block per c, the (a, b)
+// range split over the threads, a fixed-order tree reduction at the end.
+__global__ void __launch_bounds__(kLayerThreads) layer_dq_kernel(const LayerShape sh, const float *__restrict__ dW,
+                                                                 const float *__restrict__ P, float *__restrict__ dQ) {
+  __shared__ float red[kLayerThreads / 32][kLayerMaxRank];
+  const int N1 = sh.n[1], N2 = sh.n[2], M0 = sh.m[0], M1 = sh.m[1], M2 = sh.m[2];
+  const long long Nin = static_cast<long long>(sh.n[0]) * N1 * N2;
+  const int A = sh.n[0] * M0, B = N1 * M1, R1 = sh.r1;
+  const int c = blockIdx.x, n2 = c / M2, m2 = c - n2 * M2;
+  float acc[kLayerMaxRank];
+#pragma unroll
+  for (int r = 0; r < kLayerMaxRank; ++r) acc[r] = 0.f;
+  for (int ab = threadIdx.x; ab < A * B; ab += kLayerThreads) {
+    const int a = ab / B, b = ab - a * B;
+    const int n0 = a / M0, m0 = a - n0 * M0, n1 = b / M1, m1 = b - n1 * M1;
+    const long long o = (static_cast<long long>(m0) * M1 + m1) * M2 + m2;
+    const long long i = (static_cast<long long>(n0) * N1 + n1) * N2 + n2;
+    const float g = dW[o * Nin + i];
+    const float *p = P + static_cast<long long>(ab) * R1;
+#pragma unroll
+    for (int r = 0; r < kLayerMaxRank; ++r)
+      if (r < R1) acc[r] = fmaf(g, p[r], acc[r]);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int r = 0; r < kLayerMaxRank; ++r) {
+    float v = acc[r];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) red[warp][r] = v;
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < R1; r += kLayerThreads) {
+    float s = 0.f;
+    for (int w = 0; w < kLayerThreads / 32; ++w) s += red[w][r];
+    dQ[static_cast<long long>(c) * R1 + r] = s;
+  }
+}
+
+// The factor gradients from dP, dQ (all small):
+//   du3[c, r2] = sum_r1 dQ[c, r1] b1[r1, r2]        db1[r1, r2] = sum_c dQ[c, r1] u3[c, r2]
+//   dT1[a, r4, r1] = sum_b dP[a, b, r1] u2[b, r4]   du2[b, r4] = sum_{a, r1} dP[a, b, r1] T1[a, r4, r1]
+//   du1[a, r3] = sum_{r4, r1} dT1[a, r4, r1] b2[r3, r4, r1]
+//   db2[r3, r4, r1] = sum_a u1[a, r3] dT1[a, r4, r1]
+// Stage 1 (one thread per output entry): dT1, du2, du3, db1.
+__global__ void layer_grad1_kernel(const LayerShape sh, const float *__restrict__ u2, const float *__restrict__ u3,
+                                   const float *__restrict__ b1, const float *__restrict__ T1,
+                                   const float *__restrict__ dP, const float *__restrict__ dQ,
+                                   float *__restrict__ dT1, float *__restrict__ du2, float *__restrict__ du3,
+                                   float *__restrict__ db1) {
+  const int A = sh.n[0] * sh.m[0], B = sh.n[1] * sh.m[1], C = sh.n[2] * sh.m[2];
+  const int R1 = sh.r1, R2 = sh.r2, R4 = sh.r4;
+  const long long n_dt1 = static_cast<long long>(A) * R4 * R1, n_du2 = static_cast<long long>(B) * R4,
+                  n_du3 = static_cast<long long>(C) * R2, n_db1 = static_cast<long long>(R1) * R2;
+  const long long total = n_dt1 + n_du2 + n_du3 + n_db1;
+  for (long long e = blockIdx.x * static_cast<long long>(kLayerThreads) + threadIdx.x; e < total;
+       e += static_cast<long long>(gridDim.x) * kLayerThreads) {
+    if (e < n_dt1) {
+      const int a = static_cast<int>(e / (R4 * R1)), rem = static_cast<int>(e - static_cast<long long>(a) * R4 * R1);
+      const int r4 = rem / R1, r1 = rem - r4 * R1;
+      float s = 0.f;
+      for (int b = 0; b < B; ++b) s = fmaf(dP[(static_cast<long long>(a) * B + b) * R1 + r1], u2[b * R4 + r4], s);
+      dT1[e] = s;
+    } else if (e < n_dt1 + n_du2) {
+      const long long f = e - n_dt1;
+      const int b = static_cast<int>(f / R4), r4 = static_cast<int>(f - static_cast<long long>(b) * R4);
+      float s = 0.f;
+      for (int a = 0; a < A; ++a)
+        for (int r1 = 0; r1 < R1; ++r1)
+          s = fmaf(dP[(static_cast<long long>(a) * B + b) * R1 + r1], T1[(static_cast<long long>(a) * R4 + r4) * R1 + r1],
+                   s);
+      du2[f] = s;
+    } else if (e < n_dt1 + n_du2 + n_du3) {
+      const long long f = e - n_dt1 - n_du2;
+      const int c = static_cast<int>(f / R2), r2 = static_cast<int>(f - static_cast<long long>(c) * R2);
+      float s = 0.f;
+      for (int r1 = 0; r1 < R1; ++r1) s = fmaf(dQ[static_cast<long long>(c) * R1 + r1], b1[r1 * R2 + r2], s);
+      du3[f] = s;
+    } else {
+      const long long f = e - n_dt1 - n_du2 - n_du3;
+      const int r1 = static_cast<int>(f / R2), r2 = static_cast<int>(f - static_cast<long long>(r1) * R2);
+      float s = 0.f;
+      for (int c = 0; c < C; ++c) s = fmaf(dQ[static_cast<long long>(c) * R1 + r1], u3[c * R2 + r2], s);
+      db1[f] = s;
+    }
+  }
+}
+
+// Stage 2: du1, db2 from dT1.
+__global__ void layer_grad2_kernel(const LayerShape sh, const float *__restrict__ u1, const float *__restrict__ b2,
+                                   const float *__restrict__ dT1, float *__restrict__ du1, float *__restrict__ db2) {
+  const int A = sh.n[0] * sh.m[0];
+  const int R1 = sh.r1, R3 = sh.r3, R4 = sh.r4;
+  const long long n_du1 = static_cast<long long>(A) * R3, n_db2 = static_cast<long long>(R3) * R4 * R1;
+  for (long long e = blockIdx.x * static_cast<long long>(kLayerThreads) + threadIdx.x; e < n_du1 + n_db2;
+       e += static_cast<long long>(gridDim.x) * kLayerThreads) {
+    if (e < n_du1) {
+      const int a = static_cast<int>(e / R3), r3 = static_cast<int>(e - static_cast<long long>(a) * R3);
+      float s = 0.f;
+      for (int q = 0; q < R4 * R1; ++q)
+        s = fmaf(dT1[static_cast<long long>(a) * R4 * R1 + q], b2[static_cast<long long>(r3) * R4 * R1 + q], s);
+      du1[e] = s;
+    } else {
+      const long long f = e - n_du1;
+      const int r3 = static_cast<int>(f / (R4 * R1)), q = static_cast<int>(f - static_cast<long long>(r3) * R4 * R1);
+      float s = 0.f;
+      for (int a = 0; a < A; ++a)
+        s = fmaf(u1[a * R3 + r3], dT1[static_cast<long long>(a) * R4 * R1 + q], s);
+      db2[f] = s;
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t layer_pq_launch(const LayerShape &sh, const float *u1, const float *u2, const float *u3, const float *b2,
+                            const float *b1, float *P, float *Q, float *T1, cudaStream_t s) {
+  const int A = sh.n[0] * sh.m[0], C = sh.n[2] * sh.m[2];
+  const long long qb = (static_cast<long long>(C) * sh.r1 + kLayerThreads - 1) / kLayerThreads;
+  layer_pq_kernel<<<static_cast<unsigned>(A + qb), kLayerThreads, 0, s>>>(sh, u1, u2, u3, b2, b1, P, Q, T1);
+  return cudaGetLastError();
+}
+
+cudaError_t layer_weight_launch(const LayerShape &sh, const float *P, const float *Q, float *W32, __nv_bfloat16 *W16,
+                                cudaStream_t s) {
+  const long long total = static_cast<long long>(sh.n[0]) * sh.n[1] * sh.n[2] * sh.m[0] * sh.m[1] * sh.m[2];
+  if (W32) layer_weight_kernel<float><<<grid_for_layer(total), kLayerThreads, 0, s>>>(sh, P, Q, W32);
+  else layer_weight_kernel<__nv_bfloat16><<<grid_for_layer(total), kLayerThreads, 0, s>>>(sh, P, Q, W16);
+  return cudaGetLastError();
+}
+
+cudaError_t bias_act_launch(float *y, const float *bias, long long batch, long long nout, int act, cudaStream_t s) {
+  bias_act_kernel<<<grid_for_layer(batch * nout), kLayerThreads, 0, s>>>(y, bias, batch, nout, act);
+  return cudaGetLastError();
+}
+
+int layer_colsum_chunks(long long batch) {
+  long long c = batch / 256;
+  if (c < 1) c = 1;
+  if (c > 64) c = 64;
+  return static_cast<int>(c);
+}
+
+cudaError_t layer_colsum_launch(const float *dy, long long batch, long long nout, float *part, float *out,
+                                cudaStream_t s) {
+  const int chunks = layer_colsum_chunks(batch);
+  const unsigned gx = static_cast<unsigned>((nout + kLayerThreads - 1) / kLayerThreads);
+  layer_colsum_kernel<<<dim3(gx, chunks), kLayerThreads, 0, s>>>(dy, batch, nout, chunks, part);
+  layer_colsum_finish_kernel<<<gx, kLayerThreads, 0, s>>>(part, nout, chunks, out);
+  return cudaGetLastError();
+}
+
+cudaError_t layer_factor_grads_launch(const LayerShape &sh, const float *dW, const float *u1, const float *u2,
+                                      const float *u3, const float *b2, const float *b1, const float *P,
+                                      const float *Q, const float *T1, float *dP, float *dQ, float *dT1, float *du1,
+                                      float *du2, float *du3, float *db2, float *db1, cudaStream_t s) {
+  const int A = sh.n[0] * sh.m[0], B = sh.n[1] * sh.m[1], C = sh.n[2] * sh.m[2];
+  const size_t smem = sizeof(float) * static_cast<size_t>(C);
+  if (smem > 48 * 1024) return cudaErrorInvalidValue;
+  layer_dp_kernel<<<static_cast<unsigned>(A * B), kLayerThreads, smem, s>>>(sh, dW, Q, dP);
+  layer_dq_kernel<<<static_cast<unsigned>(C), kLayerThreads, 0, s>>>(sh, dW, P, dQ);
+  const long long n1 = static_cast<long long>(A) * sh.r4 * sh.r1 + static_cast<long long>(B) * sh.r4 +
+                       static_cast<long long>(C) * sh.r2 + static_cast<long long>(sh.r1) * sh.r2;
+  layer_grad1_kernel<<<grid_for_layer(n1), kLayerThreads, 0, s>>>(sh, u2, u3, b1, T1, dP, dQ, dT1, du2, du3, db1);
+  const long long n2 = static_cast<long long>(A) * sh.r3 + static_cast<long long>(sh.r3) * sh.r4 * sh.r1;
+  layer_grad2_kernel<<<grid_for_layer(n2), kLayerThreads, 0, s>>>(sh, u1, b2, dT1, du1, db2);
+  return cudaGetLastError();
+}
+
+}  // namespace htgb

@@ -350,6 +350,20 @@ TileGen make_slabs_gen(long long L, long long R, int cols, int bn) {
   return g;
 }
 
+bool make_grid_gen(long long rows, long long cols, int bn, TileGen *g) {
+  *g = TileGen{};
+  g->kind = TILES_GRID;
+  g->bm = 128;
+  g->bn = bn;
+  g->rows = rows;
+  g->n = cols;
+  g->cols = bn;
+  const long long count = ((rows + 127) / 128) * ((cols + bn - 1) / bn);
+  if (rows < 1 || cols < 1 || count > (1ll << 30) || rows > (1ll << 31) - 256 || cols > (1ll << 31) - 256) return false;
+  g->count = static_cast<int>(count);
+  return true;
+}
+
 bool make_gram_gen(long long n, int bn, TileGen *g, int bm) {
   *g = TileGen{};
   g->kind = TILES_GRAM;

@@ -23,6 +23,15 @@ HT_DEV Tile gen_tile(const TileGen &g, int idx) {
     t.out_row = 128 * lb + g.L * r;
     t.valid_rows = static_cast<int>(min(128ll, g.L - 128 * lb));
     t.valid_cols = min(g.cols, g.bn);
+  } else if (g.kind == TILES_GRID) {
+    const long long nrb = (g.rows + g.bm - 1) / g.bm;
+    const long long cb = idx / nrb, rb = idx - cb * nrb;
+    t.a_row = static_cast<int>(g.bm * rb);
+    t.b_row = static_cast<int>(g.bn * cb);
+    t.out_row = g.bm * rb;
+    t.out_col = static_cast<int>(g.bn * cb);
+    t.valid_rows = static_cast<int>(min(static_cast<long long>(g.bm), g.rows - g.bm * rb));
+    t.valid_cols = static_cast<int>(min(static_cast<long long>(g.bn), g.n - g.bn * cb));
   } else {
     int i = 0;
     while (i + 1 < g.ni && g.prefix[i + 1] <= idx) ++i;

@@ -241,6 +241,47 @@ ht_status_t ht_sketch_loss_grad(const float *G, const float *trG, int batch, int
 ht_status_t ht_sketch_adam(float *S, const float *grad, float *m, float *v, long long count, float lr, int step,
                            void *stream);
 
+/* -------------------------------------------------------- HT tensor layer */
+/* A fully connected layer whose weight is an HT tensor, as the reference's
+ * tNet / AlexNet_ht layers (HT_tensor_layer/FC_MNIST/mnist_ht.py:199-245,
+ * Alex_ImageNet/model/alexnet.py:157-170).  x is (batch, n[0], n[1], n[2]) and
+ * y is (batch, m[0], m[1], m[2]), both C-order; the parameters keep the
+ * reference's C-order layouts:
+ *   u1 (n[0], m[0], r[0])   u2 (n[1], m[1], r[1])   u3 (n[2], m[2], r[2])
+ *   b2 (r[0], r[1], r[3])   b1 (r[3], r[2])         bias (m[0], m[1], m[2])
+ * and y[z, m0, m1, m2] = sum x[z, n0, n1, n2] u1[n0, m0, e] b2[e, f, g]
+ *   u2[n1, m1, f] b1[g, h] u3[n2, m2, h]  (+ bias), the reference's einsum chain.
+ * Ranks <= 64.  All pointers are device memory.  The calls are asynchronous on
+ * `stream` and use a per-device workspace of their own: calls that may overlap
+ * on the GPU (different streams) must be ordered by the caller.
+ * precision: HT_PREC_FP32 (FP32 SIMT products) or HT_PREC_BF16 (tcgen05
+ * products on BF16 operands, FP32 accumulation; needs n and m products that are
+ * multiples of 8). */
+typedef struct {
+    int n[3];   /* input modes  */
+    int m[3];   /* output modes */
+    int r[4];   /* ranks of u1, u2, u3 and the third dimension of b2 */
+} ht_layer_shape_t;
+
+/* W (m0*m1*m2 x n0*n1*n2, row-major: an nn.Linear weight) from the factors. */
+ht_status_t ht_layer_weight(const ht_layer_shape_t *shape, const float *u1, const float *u2, const float *u3,
+                            const float *b2, const float *b1, float *W, void *stream);
+/* y = act(x W^T + bias); bias may be NULL; activation 0 = none, 1 = ReLU. */
+ht_status_t ht_layer_forward(const ht_layer_shape_t *shape, const float *u1, const float *u2, const float *u3,
+                             const float *b2, const float *b1, const float *bias, int activation, int precision,
+                             const float *x, long long batch, float *y, void *stream);
+/* Gradients of sum(dy * y) for y = x W^T + bias: dx (may be NULL), the five
+ * factor gradients (same layouts as the factors) and dbias (may be NULL). */
+ht_status_t ht_layer_backward(const ht_layer_shape_t *shape, const float *u1, const float *u2, const float *u3,
+                              const float *b2, const float *b1, int precision, const float *x, const float *dy,
+                              long long batch, float *dx, float *du1, float *du2, float *du3, float *db2,
+                              float *db1, float *dbias, void *stream);
+/* Synchronise the device and report (then clear) a wait that timed out inside
+ * an earlier layer call on this device: HT_ERR_TIMEOUT, else HT_OK. */
+ht_status_t ht_layer_check(void);
+/* Free the layer workspace of the current device. */
+ht_status_t ht_layer_release(void);
+
 /* Bytes of device workspace ht_decompose needs for this problem. */
 ht_status_t ht_workspace_size(const long *dims, int order, const ht_tree_t *tree,
                               const ht_config_t *cfg, unsigned long long *bytes);

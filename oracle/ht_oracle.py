@@ -220,3 +220,48 @@ def sketch_grad(G: np.ndarray, S: np.ndarray) -> np.ndarray:
     E = P - Y @ X
     return -(2.0 / np.trace(G)) * (G @ E) @ np.linalg.inv(C)
 
+
+# ------------------------------------------------------------- HT tensor layer
+def ht_layer_chain(x: np.ndarray, u1, u2, u3, b2, b1, bias=None) -> np.ndarray:
+    """The reference's HT layer forward, step for step
+    (HT_tensor_layer/FC_MNIST/mnist_ht.py:233-241): x (batch, N0*N1*N2) ->
+    y (batch, M0*M1*M2), float64."""
+    f = lambda a: np.asarray(a, dtype=np.float64)
+    u1, u2, u3, b2, b1 = f(u1), f(u2), f(u3), f(b2), f(b1)
+    batch = x.shape[0]
+    t = f(x).reshape(batch, u1.shape[0], u2.shape[0], u3.shape[0])
+    t = np.einsum("zabc,ade->zbcde", t, u1)
+    t = np.einsum("zabcd,def->zabcef", t, b2)
+    t = np.einsum("zabcde,afd->zbcef", t, u2)
+    t = np.einsum("zabcd,ce->zabde", t, b1)
+    t = np.einsum("zabcd,aed->zbce", t, u3)
+    if bias is not None:
+        t = t + f(bias).reshape(t.shape[1:])
+    return t.reshape(batch, -1)
+
+
+def ht_layer_weight(u1, u2, u3, b2, b1) -> np.ndarray:
+    """Dense weight W (M0*M1*M2, N0*N1*N2) with chain(x) = x W^T: the chain applied
+    to the identity."""
+    nin = u1.shape[0] * u2.shape[0] * u3.shape[0]
+    return ht_layer_chain(np.eye(nin), u1, u2, u3, b2, b1).T.copy()
+
+
+def ht_layer_init(weight: np.ndarray, rank: int, N: Sequence[int], M: Sequence[int]):
+    """The reference's ``ht(data, rank, N, M)`` (mnist_ht.py:167-197) in float64:
+    leaves 3, 4, 2 from the top eigenvectors of the unfolding Grams (descending
+    order; the reference takes torch.eig's unsorted first columns), node 1 from
+    the SVD of the (a*b) x c unfolding, then the two ncon contractions."""
+    a, b, c = N[0] * M[0], N[1] * M[1], N[2] * M[2]
+    X = np.asarray(weight, dtype=np.float64).reshape(a, b, c)
+    U3m = X.reshape(a, b * c)
+    U4m = X.transpose(1, 0, 2).reshape(b, a * c)
+    U2m = X.transpose(2, 0, 1).reshape(c, a * b)
+    U1m = X.reshape(a * b, c)
+    leaf = lambda A: top_eigvecs(A @ A.T, rank)[1]
+    U3, U4, U2 = leaf(U3m), leaf(U4m), leaf(U2m)
+    U1 = np.linalg.svd(U1m, full_matrices=False)[0][:, :rank].reshape(a, b, rank)
+    B1 = np.einsum("abk,ai,bj->ijk", U1, U3, U4)
+    B0 = np.einsum("abc,abi,cj->ij", X, U1, U2)
+    return (U3.reshape(N[0], M[0], rank), U4.reshape(N[1], M[1], rank), U2.reshape(N[2], M[2], rank), B1, B0)
+
