@@ -238,7 +238,104 @@ def secondary_configs(ht, synth, torch, stream, steps=10, warmup=3):
     torch.cuda.empty_cache()
     out["c5"] = learned_sketch_config(ht, synth, torch, stream)
     torch.cuda.empty_cache()
+    out["ht_format"] = ht_format_config(ht, synth, torch, stream)
+    torch.cuda.empty_cache()
+    out["ht_layer"] = ht_layer_config(torch, stream)
+    torch.cuda.empty_cache()
     return out
+
+
+def _event_ms(torch, stream, fn, iters, warmup=3):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(iters):
+        fn()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / iters
+
+
+def _reference_chain(torch, x, u1, u2, u3, b2, b1, bias):
+    """The reference's HT layer forward (HT_tensor_layer/FC_MNIST/mnist_ht.py:233-241),
+    PyTorch einsum on the same GPU, FP32 (TF32 off)."""
+    batch = x.shape[0]
+    t = x.reshape(batch, u1.shape[0], u2.shape[0], u3.shape[0])
+    t = torch.einsum("zabc,ade->zbcde", t, u1)
+    t = torch.einsum("zabcd,def->zabcef", t, b2)
+    t = torch.einsum("zabcde,afd->zbcef", t, u2)
+    t = torch.einsum("zabcd,ce->zabde", t, b1)
+    t = torch.einsum("zabcd,aed->zbce", t, u3)
+    return (t + bias).reshape(batch, -1)
+
+
+def ht_layer_config(torch, stream):
+    """HT tensor layer (the reference's tNet / AlexNet_ht layer): ms per forward and
+    per forward+backward through ht_layer_forward / ht_layer_backward (BF16 tcgen05
+    and FP32 products), beside the reference's own einsum chain run by PyTorch on
+    the same GPU.  Random factors of the reference's shapes; device-resident batch."""
+    import numpy as np
+    from ht_tensor_learning_using_gpu_tensor_cores_gb300 import htlayer
+    out = {}
+    allow = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    for name, N, M, r, batches in (("mnist_fc1", (8, 8, 16), (8, 8, 16), 16, (128, 65536)),
+                                   ("alexnet_fc6", (16, 16, 25), (16, 16, 16), 16, (256, 8192))):
+        g = torch.Generator(device="cuda").manual_seed(0)
+        mk = lambda *s: (torch.randn(*s, device="cuda", generator=g) / np.sqrt(s[0] * s[-1])).contiguous()
+        f = [mk(N[0], M[0], r), mk(N[1], M[1], r), mk(N[2], M[2], r), mk(r, r, r), mk(r, r)]
+        bias = torch.randn(*M, device="cuda")
+        for B in batches:
+            x = torch.randn(B, int(np.prod(N)), device="cuda")
+            rec = {"N": list(N), "M": list(M), "rank": r, "batch": B}
+            it = 20 if B <= 1024 else 5
+            rec["reference_chain_fwd_ms"] = _event_ms(torch, stream, lambda: _reference_chain(torch, x, *f, bias), it)
+            for prec in ("bf16", "fp32"):
+                rec[f"{prec}_fwd_ms"] = _event_ms(
+                    torch, stream, lambda: htlayer.layer_forward(x, *f, bias=bias, precision=prec), it)
+            ps = [t.clone().requires_grad_(True) for t in f]
+            bs = bias.clone().requires_grad_(True)
+
+            def ref_step():
+                _reference_chain(torch, x, *ps, bs).sum().backward()
+
+            def our_step(prec):
+                htlayer.ht_layer(x, *ps, bs, prec).sum().backward()
+
+            rec["reference_chain_fwdbwd_ms"] = _event_ms(torch, stream, ref_step, it)
+            for prec in ("bf16", "fp32"):
+                rec[f"{prec}_fwdbwd_ms"] = _event_ms(torch, stream, lambda: our_step(prec), it)
+            rec["samples_per_s_bf16_fwd"] = B / (rec["bf16_fwd_ms"] * 1e-3)
+            rec["speedup_bf16_fwd_vs_reference_chain"] = rec["reference_chain_fwd_ms"] / rec["bf16_fwd_ms"]
+            rec["speedup_fp32_fwd_vs_reference_chain"] = rec["reference_chain_fwd_ms"] / rec["fp32_fwd_ms"]
+            rec["speedup_bf16_fwdbwd_vs_reference_chain"] = rec["reference_chain_fwdbwd_ms"] / rec["bf16_fwdbwd_ms"]
+            out[f"{name}_b{B}"] = rec
+            del x, ps, bs
+    torch.backends.cuda.matmul.allow_tf32 = allow
+    htlayer.release()
+    return out
+
+
+def ht_format_config(ht, synth, torch, stream, n=1024, k=32):
+    """HT-format operations on the headline's factors (1024^3, rank 32):
+    ht_reconstruct (the full 4 GiB tensor, GB/s of output) and ht_evaluate
+    (entries/s for 2^20 random index tuples)."""
+    tree = ht.reference_tree_3d([1, k, k, k, k])
+    X = synth.exact_ht_device((n, n, n), tree, noise_rel=1e-3, seed=3)
+    res = ht.decompose(X, tree, precision="bf16")
+    del X
+    torch.cuda.empty_cache()
+    out = torch.empty((n, n, n), dtype=torch.float32, device="cuda")
+    rec_ms = _event_ms(torch, stream, lambda: ht.reconstruct(tree, res.U, res.B, (n, n, n), out=out), 5)
+    del out
+    cnt = 1 << 20
+    idx = torch.randint(0, n, (cnt, 3), device="cuda", dtype=torch.int64)
+    ev_ms = _event_ms(torch, stream, lambda: ht.evaluate(tree, res.U, res.B, (n, n, n), idx), 5)
+    return {"n": n, "rank": k, "reconstruct_ms": rec_ms,
+            "reconstruct_write_GBps": n ** 3 * 4 / (rec_ms * 1e-3) / 1e9,
+            "evaluate_entries": cnt, "evaluate_ms": ev_ms, "evaluate_entries_per_s": cnt / (ev_ms * 1e-3)}
 
 
 def learned_sketch_config(ht, synth, torch, stream, n=512, k=24, p=10, n_train=256, n_test=64, steps=2000):

@@ -310,19 +310,28 @@ def _factor_device(U: Dict[int, object], B: Dict[int, object]):
     return None
 
 
-def reconstruct(tree: DimTree, U: Dict[int, object], B: Dict[int, object], dims: Sequence[int], stream=None):
+def reconstruct(tree: DimTree, U: Dict[int, object], B: Dict[int, object], dims: Sequence[int], stream=None,
+                out=None):
     """The full tensor Xhat of an HT representation, computed on the GPU.
 
     Torch CUDA factors give a torch tensor shaped ``dims[::-1]`` (its memory is
     the column-major tensor); host factors give a Fortran-ordered numpy array
-    of shape ``dims``.  The reference forms Xhat only to measure the error
-    (3D/Opt/htd_tensorcore.cu:295-331)."""
+    of shape ``dims``.  ``out`` (a contiguous float32 CUDA tensor of prod(dims)
+    elements) receives the result instead of a new tensor.  The reference forms
+    Xhat only to measure the error (3D/Opt/htd_tensorcore.cu:295-331)."""
     dims = tuple(int(d) for d in dims)
     ts = _tree_struct(tree)
     keep = []
     uptr, bptr = _factor_ptrs(U, B, keep)
     dev = _factor_device(U, B)
-    if dev is not None:
+    if out is not None:
+        if not (_is_torch(out) and out.is_cuda and out.is_contiguous() and out.numel() == int(np.prod(dims))):
+            raise ValueError("out must be a contiguous CUDA tensor with prod(dims) elements")
+        optr = out.data_ptr()
+        if stream is None:
+            import torch
+            stream = torch.cuda.current_stream(out.device).cuda_stream
+    elif dev is not None:
         import torch
         out = torch.empty(tuple(reversed(dims)), dtype=torch.float32, device=dev)
         optr = out.data_ptr()

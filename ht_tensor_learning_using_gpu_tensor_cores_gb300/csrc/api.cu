@@ -1491,24 +1491,13 @@ ht_status_t ht_evaluate(const long *dims, int order, const ht_tree_t *tree, cons
   std::lock_guard<std::mutex> lk(g_ws_mutex);
   const bool idx_dev = is_device_ptr(idx), out_dev = is_device_ptr(out);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // children before parents: node ids carry no order, so sort by depth, deepest first
-  EvalTree et{};
-  et.order = order;
-  et.n_nodes = T.n_nodes;
-  int depth[HT_MAX_NODES] = {};
-  for (int t = 1; t < T.n_nodes; ++t)
-    for (int p = T.parent[t]; p >= 0; p = T.parent[p]) ++depth[t];
-  int q = 0;
-  for (int dpt = order; dpt >= 0; --dpt)
-    for (int t = 0; t < T.n_nodes; ++t)
-      if (depth[t] == dpt) et.post[q++] = t;
-  for (int t = 0; t < T.n_nodes; ++t) {
-    et.left[t] = T.left[t];
-    et.right[t] = T.right[t];
-    et.rank[t] = T.rank[t];
-    et.mode[t] = T.leaf(t) ? T.mode_of_leaf(t) : -1;
-  }
-  for (int m = 0; m < order; ++m) et.dim[m] = dims[m];
+  // Precontracted rows (3rd order, root -> t = {p, q}, c):
+  //   Wp[i_p][(y = r_c) + k_c b] = sum_{a, r_t} U_p[i_p, a] B_t[a, b, r_t] B_root'[r_t, r_c],
+  //   entry = sum_y (sum_b Wp[i_p][y, b] U_q[i_q, b]) U_c[i_c, y];
+  // 4th order (root -> t1 = {0, 1}, t2 = {2, 3}):
+  //   W12[i0][r1 + k1 b] = sum_a U_a1[i0, a] B_t1[a, b, r1]
+  //   W34[i2][r1 + k1 d] = sum_{c, r2} U_a2[i2, c] B_t2[c, d, r2] B_root[r1, r2]
+  //   entry = sum_r1 (sum_b W12[i0][r1, b] U_b1[i1, b]) (sum_d W34[i2][r1, d] U_b2[i3, d]).
   auto plan = [&](Ctx &c) -> ht_status_t {
     const float *Ud[HT_MAX_NODES] = {}, *Bd[HT_MAX_NODES] = {};
     c.err = c.ar.take<int>(64);
@@ -1524,13 +1513,53 @@ ht_status_t ht_evaluate(const long *dims, int order, const ht_tree_t *tree, cons
     }
     float *o = out_dev ? out : c.ar.take<float>(static_cast<size_t>(count));
     if (!o) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small");
-    if (!c.dry()) {
-      for (int t = 0; t < T.n_nodes; ++t) {
-        et.U[t] = Ud[t];
-        et.B[t] = Bd[t];
+    EvalPlan ep{};
+    ep.order = order;
+    if (order == 3) {
+      const Plan3 P = plan3(T);
+      float *Bkt = c.ar.take<float>(static_cast<size_t>(P.kt) * P.kc);
+      float *core = c.ar.take<float>(static_cast<size_t>(P.kc) * P.kq * P.kp);
+      float *Wp = c.ar.take<float>(static_cast<size_t>(dims[P.mp]) * P.kq * P.kc);
+      if (!Bkt || !core || !Wp) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small");
+      if (!c.dry()) {
+        if (P.t_is_left)
+          HT_CUDA(cudaMemcpyAsync(Bkt, Bd[0], sizeof(float) * P.kt * P.kc, cudaMemcpyDeviceToDevice, c.st));
+        else HT_CUDA(transpose_small_launch(Bd[0], P.kc, P.kt, Bkt, c.st));
+        HT_CUDA(eval_core_launch(Bd[P.t], P.kp, P.kq, P.kt, Bkt, P.kc, core, c.st));
+        const long long rw = static_cast<long long>(P.kc) * P.kq;
+        HT_CUDA(gemm_nt_launch(core, rw, 0, Ud[P.p], dims[P.mp], Wp, rw, 0, rw, dims[P.mp], P.kp, 1, c.st));
+        c.launches += 3;
       }
+      ep.ky = P.kc;
+      ep.side[0] = EvalSide{Wp, Ud[P.q], dims[P.mp], dims[P.mq], P.mp, P.mq, P.kq};
+      ep.side[1] = EvalSide{nullptr, Ud[P.c], 0, dims[P.mc], 0, P.mc, 0};
+    } else {
+      const int t1 = T.left[0], t2 = T.right[0];
+      const int k1 = T.rank[t1], k2 = T.rank[t2];
+      const int a1 = T.left[t1], b1 = T.right[t1], a2 = T.left[t2], b2 = T.right[t2];
+      const int ka1 = T.rank[a1], kb1 = T.rank[b1], ka2 = T.rank[a2], kb2 = T.rank[b2];
+      float *c12 = c.ar.take<float>(static_cast<size_t>(k1) * kb1 * ka1);
+      float *B0T = c.ar.take<float>(static_cast<size_t>(k2) * k1);
+      float *c34 = c.ar.take<float>(static_cast<size_t>(k1) * kb2 * ka2);
+      float *W12 = c.ar.take<float>(static_cast<size_t>(dims[0]) * k1 * kb1);
+      float *W34 = c.ar.take<float>(static_cast<size_t>(dims[2]) * k1 * kb2);
+      if (!c12 || !B0T || !c34 || !W12 || !W34) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small");
+      if (!c.dry()) {
+        HT_CUDA(eval_core_launch(Bd[t1], ka1, kb1, k1, nullptr, k1, c12, c.st));
+        HT_CUDA(transpose_small_launch(Bd[0], k1, k2, B0T, c.st));
+        HT_CUDA(eval_core_launch(Bd[t2], ka2, kb2, k2, B0T, k1, c34, c.st));
+        const long long r12 = static_cast<long long>(k1) * kb1, r34 = static_cast<long long>(k1) * kb2;
+        HT_CUDA(gemm_nt_launch(c12, r12, 0, Ud[a1], dims[0], W12, r12, 0, r12, dims[0], ka1, 1, c.st));
+        HT_CUDA(gemm_nt_launch(c34, r34, 0, Ud[a2], dims[2], W34, r34, 0, r34, dims[2], ka2, 1, c.st));
+        c.launches += 5;
+      }
+      ep.ky = k1;
+      ep.side[0] = EvalSide{W12, Ud[b1], dims[0], dims[1], 0, 1, kb1};
+      ep.side[1] = EvalSide{W34, Ud[b2], dims[2], dims[3], 2, 3, kb2};
+    }
+    if (!c.dry()) {
       HT_CUDA(cudaMemsetAsync(c.err, 0, sizeof(int), c.st));
-      HT_CUDA(evaluate_launch(et, ix, count, o, c.err, c.st));
+      HT_CUDA(evaluate_launch(ep, ix, count, o, c.err, c.st));
       ++c.launches;
       if (!out_dev) HT_CUDA(cudaMemcpyAsync(out, o, sizeof(float) * count, cudaMemcpyDeviceToHost, c.st));
     }
@@ -2029,8 +2058,10 @@ ht_status_t ht_layer_backward(const ht_layer_shape_t *shape, const float *u1, co
     __nv_bfloat16 *x16 = tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(batch * nin)) : nullptr;
     __nv_bfloat16 *dy16 = tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(batch * nout)) : nullptr;
     float *part = dbias ? c.ar.take<float>(static_cast<size_t>(layer_colsum_chunks(batch)) * nout) : nullptr;
+    const size_t nqp = layer_dq_part_count(sh);
+    float *dQpart = nqp ? c.ar.take<float>(nqp) : nullptr;
     if (!P || !Q || !T1 || !dP || !dQ || !dT1 || !dW || (dx && !(W32 || W16)) || (tc && (!x16 || !dy16)) ||
-        (dbias && !part))
+        (dbias && !part) || (nqp && !dQpart))
       return fail(HT_ERR_OUT_OF_MEMORY, "layer workspace too small");
     if (!c.dry()) {
       HT_CUDA(layer_pq_launch(sh, u1, u2, u3, b2, b1, P, Q, T1, c.st));
@@ -2056,8 +2087,8 @@ ht_status_t ht_layer_backward(const ht_layer_shape_t *shape, const float *u1, co
         HT_CUDA(layer_colsum_launch(dy, batch, nout, part, dbias, c.st));
         c.launches += 2;
       }
-      HT_CUDA(layer_factor_grads_launch(sh, dW, u1, u2, u3, b2, b1, P, Q, T1, dP, dQ, dT1, du1, du2, du3, db2, db1,
-                                        c.st));
+      HT_CUDA(layer_factor_grads_launch(sh, dW, u1, u2, u3, b2, b1, P, Q, T1, dP, dQ, dT1, dQpart, du1, du2, du3,
+                                        db2, db1, c.st));
       c.launches += 4;
     }
     return HT_OK;

@@ -182,18 +182,24 @@ cudaError_t sketch_adam(float *S, const float *g, float *m, float *v, long long 
 cudaError_t gemm_nt_launch(const float *A, long long lda, long long sA, const float *B, long long ldb, float *C,
                            long long ldc, long long sC, long long m, long long n, int k, long long batch,
                            cudaStream_t s);
-constexpr int kEvalNodes = 7;
-struct EvalTree {
-  int order, n_nodes;
-  int left[kEvalNodes], right[kEvalNodes], rank[kEvalNodes], mode[kEvalNodes];
-  int post[kEvalNodes];              // nodes in post order (children before parents, root last)
-  long long dim[4];
-  const float *U[kEvalNodes];        // leaves: dim x rank, column-major
-  const float *B[kEvalNodes];        // interior nodes and root: k_l x k_r x k_t
+// out[(c + kc b) + kc kq a] = sum_rt Bt[a + kp b + kp kq rt] M[rt + kt c]; M null: identity (kc = kt)
+cudaError_t eval_core_launch(const float *Bt, int kp, int kq, int kt, const float *M, int kc, float *out,
+                             cudaStream_t s);
+// One side of an entry: with W, a[y] = sum_x W[i_row (ky kx) + y + ky x] Uv[i_vec + n_vec x];
+// without W, a[y] = Uv[i_vec + n_vec y].
+struct EvalSide {
+  const float *W;
+  const float *Uv;
+  long long n_row, n_vec;
+  int mode_row, mode_vec, kx;
 };
-// out[e] = the HT tensor's entry at indices idx[e*order .. e*order + order);
+struct EvalPlan {
+  int order, ky;
+  EvalSide side[2];
+};
+// out[e] = sum_y a0[y] a1[y] at the index tuple idx[e*order .. e*order + order);
 // an index out of range sets *err to 1.
-cudaError_t evaluate_launch(const EvalTree &et, const long long *idx, long long count, float *out, int *err,
+cudaError_t evaluate_launch(const EvalPlan &ep, const long long *idx, long long count, float *out, int *err,
                             cudaStream_t s);
 
 // ------------------------------------------------------ HT tensor layer (layer.cu)
@@ -216,10 +222,13 @@ cudaError_t bias_act_launch(float *y, const float *bias, long long batch, long l
 int layer_colsum_chunks(long long batch);
 cudaError_t layer_colsum_launch(const float *dy, long long batch, long long nout, float *part, float *out,
                                 cudaStream_t s);
+// Floats of the dQ partial buffer layer_factor_grads_launch wants (0: the shape
+// takes the unfused path, which needs none).
+size_t layer_dq_part_count(const LayerShape &sh);
 // du1, du2, du3, db2, db1 from dW (Nout x Nin, row-major), via dP, dQ, dT1 (scratch of P, Q, T1's sizes)
 cudaError_t layer_factor_grads_launch(const LayerShape &sh, const float *dW, const float *u1, const float *u2,
                                       const float *u3, const float *b2, const float *b1, const float *P,
-                                      const float *Q, const float *T1, float *dP, float *dQ, float *dT1, float *du1,
-                                      float *du2, float *du3, float *db2, float *db1, cudaStream_t s);
+                                      const float *Q, const float *T1, float *dP, float *dQ, float *dT1, float *dQpart,
+                                      float *du1, float *du2, float *du3, float *db2, float *db1, cudaStream_t s);
 
 }  // namespace htgb

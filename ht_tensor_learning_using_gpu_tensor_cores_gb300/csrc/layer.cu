@@ -98,6 +98,54 @@ __global__ void __launch_bounds__(kLayerThreads) layer_weight_kernel(const Layer
   }
 }
 
+// The same W, a block per (m0, m1, group of kWeightG m2 rows): the P slice
+// Ps[(n0, n1)][r] = P[n0 M0 + m0, n1 M1 + m1, r] and Qt[r][g][n2] =
+// Q[n2 M2 + m2_0 + g, r] sit in shared memory, each thread keeps kWeightG
+// accumulators for one input index i and writes kWeightG rows of W, consecutive
+// threads on consecutive i (coalesced rows).
+constexpr int kWeightG = 8;
+template <class T>
+__global__ void __launch_bounds__(kLayerThreads) layer_weight_tiled_kernel(const LayerShape sh,
+                                                                           const float *__restrict__ P,
+                                                                           const float *__restrict__ Q,
+                                                                           T *__restrict__ W) {
+  extern __shared__ float sm[];
+  const int N0 = sh.n[0], N1 = sh.n[1], N2 = sh.n[2], M0 = sh.m[0], M1 = sh.m[1], M2 = sh.m[2];
+  const int R1 = sh.r1, B = N1 * M1, NP = N0 * N1;
+  const long long Nin = static_cast<long long>(NP) * N2;
+  const int groups = (M2 + kWeightG - 1) / kWeightG;
+  const int gi = blockIdx.x % groups, mm = blockIdx.x / groups, m1 = mm % M1, m0 = mm / M1;
+  const int m2_0 = gi * kWeightG, G = min(kWeightG, M2 - m2_0);
+  float *Ps = sm;                                    // NP x R1
+  float *Qt = sm + static_cast<size_t>(NP) * R1;     // R1 x kWeightG x N2
+  for (int e = threadIdx.x; e < NP * R1; e += kLayerThreads) {
+    const int pr = e / R1, r = e - pr * R1, n0 = pr / N1, n1 = pr - n0 * N1;
+    Ps[e] = P[(static_cast<long long>(n0 * M0 + m0) * B + (n1 * M1 + m1)) * R1 + r];
+  }
+  for (int e = threadIdx.x; e < R1 * kWeightG * N2; e += kLayerThreads) {
+    const int n2 = e % N2, g = (e / N2) % kWeightG, r = e / (N2 * kWeightG);
+    Qt[e] = g < G ? Q[static_cast<long long>(n2 * M2 + m2_0 + g) * R1 + r] : 0.f;
+  }
+  __syncthreads();
+  const long long o0 = (static_cast<long long>(m0) * M1 + m1) * M2 + m2_0;
+  for (long long i = threadIdx.x; i < Nin; i += kLayerThreads) {
+    const int pr = static_cast<int>(i / N2), n2 = static_cast<int>(i - static_cast<long long>(pr) * N2);
+    float acc[kWeightG];
+#pragma unroll
+    for (int g = 0; g < kWeightG; ++g) acc[g] = 0.f;
+    const float *ps = Ps + static_cast<size_t>(pr) * R1;
+    for (int r = 0; r < R1; ++r) {
+      const float pv = ps[r];
+      const float *q = Qt + static_cast<size_t>(r) * kWeightG * N2 + n2;
+#pragma unroll
+      for (int g = 0; g < kWeightG; ++g) acc[g] = fmaf(pv, q[g * N2], acc[g]);
+    }
+#pragma unroll
+    for (int g = 0; g < kWeightG; ++g)
+      if (g < G) W[(o0 + g) * Nin + i] = from_f32<T>(acc[g]);
+  }
+}
+
 // y[z, o] = act(y[z, o] + bias[o]), act 0 = identity, 1 = ReLU
 __global__ void bias_act_kernel(float *__restrict__ y, const float *__restrict__ bias, long long batch, long long nout,
                                 int act) {
@@ -197,6 +245,73 @@ __global__ void __launch_bounds__(kLayerThreads) layer_dq_kernel(const LayerShap
   }
 }
 
+// dP and per-block dQ partials in one pass over dW, a block per (m0, m1): the
+// block reads the M2 rows o = (m0 M1 + m1) M2 + m2 of dW (coalesced, staged in
+// shared memory with an odd pair stride), and with Q (C x R1) and the P slice
+// Ps[(n0, n1)][r] resident accumulates
+//   dPs[(n0, n1)][r] += sum_n2 dW[o, (n0, n1, n2)] Q[n2 M2 + m2, r]
+//   dQpart[blk][n2 M2 + m2][r] = sum_(n0, n1) dW[o, (n0, n1, n2)] Ps[(n0, n1)][r].
+// Every accumulator has one owning thread, so the sums are deterministic.
+__global__ void __launch_bounds__(kLayerThreads) layer_dpq_kernel(const LayerShape sh, const float *__restrict__ dW,
+                                                                  const float *__restrict__ P,
+                                                                  const float *__restrict__ Q,
+                                                                  float *__restrict__ dP,
+                                                                  float *__restrict__ dQpart) {
+  extern __shared__ float sm[];
+  const int N0 = sh.n[0], N1 = sh.n[1], N2 = sh.n[2], M0 = sh.m[0], M1 = sh.m[1], M2 = sh.m[2];
+  const int R1 = sh.r1, B = N1 * M1, NP = N0 * N1, C = N2 * M2;
+  const int rs = N2 | 1;                             // odd stride between pairs: conflict-free column reads
+  const long long Nin = static_cast<long long>(NP) * N2;
+  const int blk = blockIdx.x, m1 = blk % M1, m0 = blk / M1;
+  float *row = sm;                                   // NP x rs
+  float *Qs = row + static_cast<size_t>(NP) * rs;    // C x R1
+  float *Ps = Qs + static_cast<size_t>(C) * R1;      // NP x R1
+  float *dPs = Ps + static_cast<size_t>(NP) * R1;    // NP x R1
+  for (int e = threadIdx.x; e < C * R1; e += kLayerThreads) Qs[e] = Q[e];
+  for (int e = threadIdx.x; e < NP * R1; e += kLayerThreads) {
+    const int pr = e / R1, r = e - pr * R1, n0 = pr / N1, n1 = pr - n0 * N1;
+    Ps[e] = P[(static_cast<long long>(n0 * M0 + m0) * B + (n1 * M1 + m1)) * R1 + r];
+    dPs[e] = 0.f;
+  }
+  for (int m2 = 0; m2 < M2; ++m2) {
+    __syncthreads();   // previous row fully consumed (and Qs / Ps written on the first pass)
+    const float *src = dW + ((static_cast<long long>(m0) * M1 + m1) * M2 + m2) * Nin;
+    for (long long i = threadIdx.x; i < Nin; i += kLayerThreads) {
+      const int pr = static_cast<int>(i / N2), n2 = static_cast<int>(i - static_cast<long long>(pr) * N2);
+      row[pr * rs + n2] = src[i];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < NP * R1; e += kLayerThreads) {
+      const int pr = e / R1, r = e - pr * R1;
+      const float *rw = row + pr * rs;
+      float s = dPs[e];
+      for (int n2 = 0; n2 < N2; ++n2) s = fmaf(rw[n2], Qs[(n2 * M2 + m2) * R1 + r], s);
+      dPs[e] = s;
+    }
+    for (int e = threadIdx.x; e < N2 * R1; e += kLayerThreads) {
+      const int r = e / N2, n2 = e - r * N2;
+      float s = 0.f;
+      for (int pr = 0; pr < NP; ++pr) s = fmaf(row[pr * rs + n2], Ps[pr * R1 + r], s);
+      dQpart[(static_cast<long long>(blk) * C + (n2 * M2 + m2)) * R1 + r] = s;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < NP * R1; e += kLayerThreads) {
+    const int pr = e / R1, r = e - pr * R1, n0 = pr / N1, n1 = pr - n0 * N1;
+    dP[(static_cast<long long>(n0 * M0 + m0) * B + (n1 * M1 + m1)) * R1 + r] = dPs[e];
+  }
+}
+
+// dQ[c, r] = sum over the (m0, m1) blocks of dQpart, in block order.
+__global__ void layer_dq_reduce_kernel(const float *__restrict__ dQpart, int blocks, long long count,
+                                       float *__restrict__ dQ) {
+  const long long e = blockIdx.x * static_cast<long long>(kLayerThreads) + threadIdx.x;
+  if (e >= count) return;
+  float s = 0.f;
+  for (int b = 0; b < blocks; ++b) s += dQpart[static_cast<long long>(b) * count + e];
+  dQ[e] = s;
+}
+
 // The factor gradients from dP, dQ (all small):
 //   du3[c, r2] = sum_r1 dQ[c, r1] b1[r1, r2]        db1[r1, r2] = sum_c dQ[c, r1] u3[c, r2]
 //   dT1[a, r4, r1] = sum_b dP[a, b, r1] u2[b, r4]   du2[b, r4] = sum_{a, r1} dP[a, b, r1] T1[a, r4, r1]
@@ -281,9 +396,41 @@ cudaError_t layer_pq_launch(const LayerShape &sh, const float *u1, const float *
   return cudaGetLastError();
 }
 
+size_t layer_weight_smem(const LayerShape &sh) {
+  return sizeof(float) * (static_cast<size_t>(sh.n[0]) * sh.n[1] * sh.r1 +
+                          static_cast<size_t>(sh.r1) * kWeightG * sh.n[2]);
+}
+
+size_t layer_dpq_smem(const LayerShape &sh) {
+  const size_t NP = static_cast<size_t>(sh.n[0]) * sh.n[1], C = static_cast<size_t>(sh.n[2]) * sh.m[2];
+  return sizeof(float) * (NP * (sh.n[2] | 1) + C * sh.r1 + 2 * NP * sh.r1);
+}
+
+constexpr size_t kLayerSmemMax = 200 * 1024;
+
+template <class K>
+cudaError_t allow_smem(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+}
+
 cudaError_t layer_weight_launch(const LayerShape &sh, const float *P, const float *Q, float *W32, __nv_bfloat16 *W16,
                                 cudaStream_t s) {
   const long long total = static_cast<long long>(sh.n[0]) * sh.n[1] * sh.n[2] * sh.m[0] * sh.m[1] * sh.m[2];
+  const size_t smem = layer_weight_smem(sh);
+  if (smem <= kLayerSmemMax) {
+    const unsigned grid =
+        static_cast<unsigned>(sh.m[0]) * sh.m[1] * ((sh.m[2] + kWeightG - 1) / kWeightG);
+    cudaError_t e;
+    if (W32) {
+      if ((e = allow_smem(layer_weight_tiled_kernel<float>, smem)) != cudaSuccess) return e;
+      layer_weight_tiled_kernel<float><<<grid, kLayerThreads, smem, s>>>(sh, P, Q, W32);
+    } else {
+      if ((e = allow_smem(layer_weight_tiled_kernel<__nv_bfloat16>, smem)) != cudaSuccess) return e;
+      layer_weight_tiled_kernel<__nv_bfloat16><<<grid, kLayerThreads, smem, s>>>(sh, P, Q, W16);
+    }
+    return cudaGetLastError();
+  }
   if (W32) layer_weight_kernel<float><<<grid_for_layer(total), kLayerThreads, 0, s>>>(sh, P, Q, W32);
   else layer_weight_kernel<__nv_bfloat16><<<grid_for_layer(total), kLayerThreads, 0, s>>>(sh, P, Q, W16);
   return cudaGetLastError();
@@ -310,15 +457,31 @@ cudaError_t layer_colsum_launch(const float *dy, long long batch, long long nout
   return cudaGetLastError();
 }
 
+size_t layer_dq_part_count(const LayerShape &sh) {
+  if (layer_dpq_smem(sh) > kLayerSmemMax) return 0;
+  return static_cast<size_t>(sh.m[0]) * sh.m[1] * sh.n[2] * sh.m[2] * sh.r1;
+}
+
 cudaError_t layer_factor_grads_launch(const LayerShape &sh, const float *dW, const float *u1, const float *u2,
                                       const float *u3, const float *b2, const float *b1, const float *P,
-                                      const float *Q, const float *T1, float *dP, float *dQ, float *dT1, float *du1,
-                                      float *du2, float *du3, float *db2, float *db1, cudaStream_t s) {
+                                      const float *Q, const float *T1, float *dP, float *dQ, float *dT1, float *dQpart,
+                                      float *du1, float *du2, float *du3, float *db2, float *db1, cudaStream_t s) {
   const int A = sh.n[0] * sh.m[0], B = sh.n[1] * sh.m[1], C = sh.n[2] * sh.m[2];
-  const size_t smem = sizeof(float) * static_cast<size_t>(C);
-  if (smem > 48 * 1024) return cudaErrorInvalidValue;
-  layer_dp_kernel<<<static_cast<unsigned>(A * B), kLayerThreads, smem, s>>>(sh, dW, Q, dP);
-  layer_dq_kernel<<<static_cast<unsigned>(C), kLayerThreads, 0, s>>>(sh, dW, P, dQ);
+  const size_t smem_dpq = layer_dpq_smem(sh);
+  if (smem_dpq <= kLayerSmemMax && dQpart) {
+    cudaError_t e = allow_smem(layer_dpq_kernel, smem_dpq);
+    if (e != cudaSuccess) return e;
+    const int blocks = sh.m[0] * sh.m[1];
+    layer_dpq_kernel<<<static_cast<unsigned>(blocks), kLayerThreads, smem_dpq, s>>>(sh, dW, P, Q, dP, dQpart);
+    const long long cnt = static_cast<long long>(C) * sh.r1;
+    layer_dq_reduce_kernel<<<static_cast<unsigned>((cnt + kLayerThreads - 1) / kLayerThreads), kLayerThreads, 0, s>>>(
+        dQpart, blocks, cnt, dQ);
+  } else {
+    const size_t smem = sizeof(float) * static_cast<size_t>(C);
+    if (smem > 48 * 1024) return cudaErrorInvalidValue;
+    layer_dp_kernel<<<static_cast<unsigned>(A * B), kLayerThreads, smem, s>>>(sh, dW, Q, dP);
+    layer_dq_kernel<<<static_cast<unsigned>(C), kLayerThreads, 0, s>>>(sh, dW, P, dQ);
+  }
   const long long n1 = static_cast<long long>(A) * sh.r4 * sh.r1 + static_cast<long long>(B) * sh.r4 +
                        static_cast<long long>(C) * sh.r2 + static_cast<long long>(sh.r1) * sh.r2;
   layer_grad1_kernel<<<grid_for_layer(n1), kLayerThreads, 0, s>>>(sh, u2, u3, b1, T1, dP, dQ, dT1, du2, du3, db1);

@@ -61,6 +61,11 @@ def _stream(t):
     return c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
 
 
+def release() -> None:
+    """Free the layer workspace of the current device."""
+    check(lib().ht_layer_release())
+
+
 def layer_weight(u1, u2, u3, b2, b1):
     """The dense weight (M0*M1*M2, N0*N1*N2) of the layer (an ``nn.Linear``
     weight: y = x W^T)."""

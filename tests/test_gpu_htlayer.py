@@ -140,7 +140,7 @@ def test_autograd_module_trains():
             first = float(loss.detach())
             assert all(p.grad is not None and torch.isfinite(p.grad).all() for p in layer.parameters())
         opt.step()
-    assert float(loss) < 0.05 * first
+    assert loss.item() < 0.05 * first
 
 
 def test_ht_init_matches_reference_init():
