@@ -324,6 +324,39 @@ ht_status_t gram(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x
   return run_gemm(c, q);
 }
 
+// l-block exponent of the last mode's second BF16 copy (0: no copy).
+int last_mode_block(const long *dims, int order) {
+  if (order != 3) return 0;
+  const long long N = dims[2], L = static_cast<long long>(dims[0]) * dims[1];
+  if (N < 256 || L < 65536) return 0;
+  if (N % 16 == 0 && L % 256 == 0) return 8;   // 256-element l-blocks: 512-byte rows, 16-column tiles
+  if (N % 64 == 0 && L % 64 == 0) return 6;    // 64-element l-blocks: 128-byte rows, 64-column tiles
+  return 0;
+}
+
+// Gram of the last mode (v.R == 1) from the l-blocked BF16 copy x16t
+// (x16t[((l/B) N + n) B + l%B], B = 2^lb): a K-major operand whose rows are 2B
+// bytes apart.  Read in place, the last mode's K-major rows are 2L bytes apart,
+// so every 256-row TMA box touches 256 different 2 MiB pages; at 1024^3 that
+// Gram read X three times from DRAM and ran at half the speed of the other two.
+ht_status_t gram_transposed(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x16t, int lb, float *G) {
+  GemmReq q;
+  q.a32 = q.b32 = gram_operand(v, x32);
+  Operand o;
+  o.kind = OP_KM3; o.ptr = x16t; o.d0 = 1l << lb; o.d1 = v.N; o.d2 = v.L >> lb;
+  q.a16 = q.b16 = o;
+  q.bn_tc = v.N >= 256 ? 256 : (v.N > 64 ? 128 : 64);
+  q.mt_tc = v.N >= 256 ? 2 : 1;
+  q.bn_simt = v.N > 64 ? 128 : 64;
+  q.tiles_kind = TILES_GRAM;
+  q.t_n = v.N;
+  q.out_mode = OUT_PARTIAL;
+  q.out = G;
+  q.ld_out = v.N;
+  q.symmetric = true;
+  return run_gemm(c, q);
+}
+
 // Z ((L*R) x k, column-major) = contraction of the middle index of view v with W (v.N x k)
 // fold_h > 0: W16 is the split_bf16 form of W32 (v.N x 2*fold_h, high part in
 // columns [0, k), low part in [fold_h, fold_h + k)), so the tcgen05 product
@@ -504,7 +537,8 @@ struct Timeline {
 };
 
 ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const float *x32,
-                           const __nv_bfloat16 *x16, const long *dims, int order, Result &res, Timeline &tl) {
+                           const __nv_bfloat16 *x16, const __nv_bfloat16 *x16t, int lb, const long *dims,
+                           int order, Result &res, Timeline &tl) {
   const int p_over = cfg.oversample > 0 ? cfg.oversample : 16;
   const int iters = cfg.eig_iters > 0 ? cfg.eig_iters : 10;
   const bool d3 = order == 3;
@@ -517,7 +551,11 @@ ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const 
     G[m] = c.ar.take<float>(static_cast<size_t>(dims[m]) * dims[m]);
     if (!G[m]) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (Gram)");
   }
-  for (int m = 0; m < order; ++m) HT_TRY(gram(c, view_of_group(dims, order, m, m), x32, x16, G[m]));
+  for (int m = 0; m < order; ++m) {
+    const View v = view_of_group(dims, order, m, m);
+    if (m == order - 1 && x16t) HT_TRY(gram_transposed(c, v, x32, x16t, lb, G[m]));
+    else HT_TRY(gram(c, v, x32, x16, G[m]));
+  }
   tl.mark(c.st);
 
   // 2. top-K eigenvectors of every leaf Gram, one batch
@@ -786,11 +824,19 @@ ht_status_t enqueue_body(Ctx &c, const Tree &T, const ht_config_t &cfg, const fl
                          double *nparts, double *dsum, Timeline &tl, Result &res) {
   long long total = 1;
   for (int m = 0; m < a.order; ++m) total *= a.dims[m];
-  __nv_bfloat16 *xb = nullptr;
+  __nv_bfloat16 *xb = nullptr, *xbt = nullptr;
+  int lb = c.tc ? last_mode_block(a.dims, a.order) : 0;
   if (c.tc) {
     xb = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
     if (!xb) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (bf16 tensor)");
-    if (!c.dry()) HT_CUDA(convert_bf16_launch(xd, xb, total, nparts, 1024, c.st));
+    if (lb && (reinterpret_cast<uintptr_t>(xd) & 15u) == 0) {
+      const long long N = a.dims[a.order - 1], L = total / N;
+      xbt = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
+      if (!xbt) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (bf16 tensor)");
+      if (!c.dry()) HT_CUDA(convert_bf16_dual_launch(xd, xb, xbt, L, N, lb, nparts, 1024, c.st));
+    } else if (!c.dry()) {
+      HT_CUDA(convert_bf16_launch(xd, xb, total, nparts, 1024, c.st));
+    }
   } else if (!c.dry()) {
     HT_CUDA(sumsq_launch(xd, total, nparts, 1024, c.st));
   }
@@ -799,7 +845,8 @@ ht_status_t enqueue_body(Ctx &c, const Tree &T, const ht_config_t &cfg, const fl
     c.launches += 2;
   }
   tl.mark(c.st);
-  HT_TRY(decompose_core(c, T, cfg, xd, xb, a.dims, a.order, res, tl));
+  if (!xbt) lb = 0;
+  HT_TRY(decompose_core(c, T, cfg, xd, xb, xbt, lb, a.dims, a.order, res, tl));
   // outputs to the caller's buffers (host or device)
   for (int t = 0; t < T.n_nodes; ++t) {
     float *dst = T.leaf(t) ? a.U[t] : a.B[t];

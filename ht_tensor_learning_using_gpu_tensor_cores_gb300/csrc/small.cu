@@ -45,6 +45,61 @@ __global__ void __launch_bounds__(256) convert_bf16_kernel(const float *__restri
   if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
 }
 
+// X (L x N, l fastest, FP32) -> xb (the same layout, BF16) and xbt, a second
+// BF16 copy in l-blocks of B = 2^lb elements: xbt[((l / B) N + n) B + l % B],
+// plus the compensated sum of squares per block.  Work goes in tiles of B l by
+// TN n (TN = 2^(12 - lb), 4096 elements a tile), l-blocks fastest: the grid's blocks
+// then read and write xb inside TN columns at a time, and each tile's xbt part
+// is one contiguous run of 2 B TN bytes (8 KiB), so all three streams stay
+// within a few hundred 2 MiB pages.  In xbt the rows of the last mode's Gram
+// (rows n, K = l) are 2B bytes apart inside each l-block, where in xb they lie
+// 2L bytes apart (one 2 MiB page per row at 1024^3).  Needs L % B == 0 and
+// N % TN == 0.
+__global__ void __launch_bounds__(256) convert_bf16_dual_kernel(const float *__restrict__ x,
+                                                                __nv_bfloat16 *__restrict__ xb,
+                                                                __nv_bfloat16 *__restrict__ xbt, long long L,
+                                                                long long N, int lb, double *partials) {
+  Acc2 a = {0.f, 0.f};
+  const int TN = 1 << (12 - lb);
+  const long long B = 1ll << lb, nlb = L >> lb, tiles = nlb * (N / TN);
+  const int row4 = static_cast<int>(B / 4);          // float4 per tile column
+  // every tile holds B * TN = 4096 elements: 4 float4 per thread, loaded together
+  for (long long ti = blockIdx.x; ti < tiles; ti += gridDim.x) {
+    const long long lblk = ti % nlb, n0 = (ti / nlb) * TN;
+    float4 v[4];
+    long long off[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int q = threadIdx.x + 256 * j, nn = q / row4, l4 = q - nn * row4;
+      off[j] = (lblk << lb) + 4 * l4 + L * (n0 + nn);
+      v[j] = __ldcs(reinterpret_cast<const float4 *>(x + off[j]));
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      acc2_add_prod(a, v[j].x, v[j].x);
+      acc2_add_prod(a, v[j].y, v[j].y);
+      acc2_add_prod(a, v[j].z, v[j].z);
+      acc2_add_prod(a, v[j].w, v[j].w);
+      __nv_bfloat162 lo = __floats2bfloat162_rn(v[j].x, v[j].y);
+      __nv_bfloat162 hi = __floats2bfloat162_rn(v[j].z, v[j].w);
+      uint2 pk;
+      pk.x = *reinterpret_cast<uint32_t *>(&lo);
+      pk.y = *reinterpret_cast<uint32_t *>(&hi);
+      *reinterpret_cast<uint2 *>(xb + off[j]) = pk;
+      // the tile's xbt part is contiguous and in the same element order as q
+      *reinterpret_cast<uint2 *>(xbt + ((lblk * N + n0) << lb) + 4 * (threadIdx.x + 256 * j)) = pk;
+    }
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = static_cast<double>(a.s) + static_cast<double>(a.c);
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
+}
+
 __global__ void sumsq_kernel(const float *__restrict__ x, long long n, double *partials) {
   Acc2 a = {0.f, 0.f};
   for (long long i = blockIdx.x * 256ll + threadIdx.x; i < n; i += gridDim.x * 256ll) {
@@ -283,6 +338,17 @@ cudaError_t convert_bf16_launch(const float *x, __nv_bfloat16 *xb, long long n, 
     convert_bf16_kernel<<<num_partials, 256, 0, s>>>(x, xb, n, partials);
   else
     return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t convert_bf16_dual_launch(const float *x, __nv_bfloat16 *xb, __nv_bfloat16 *xbt, long long L, long long N,
+                                     int lb, double *partials, int num_partials, cudaStream_t s) {
+  const int TN = 1 << (12 - lb);
+  if (lb < 6 || lb > 12 || L % (1ll << lb) || N < TN || N % TN || num_partials < 1 || num_partials > 4096 ||
+      (reinterpret_cast<uintptr_t>(x) & 15u) || (reinterpret_cast<uintptr_t>(xb) & 7u) ||
+      (reinterpret_cast<uintptr_t>(xbt) & 7u))
+    return cudaErrorInvalidValue;
+  convert_bf16_dual_kernel<<<num_partials, 256, 0, s>>>(x, xb, xbt, L, N, lb, partials);
   return cudaGetLastError();
 }
 
