@@ -38,6 +38,11 @@ sys.path.insert(0, ROOT)
 N_FULL, RANK, DECAY = 1024, 32, 1.5
 CPU_SAMPLE_N = 512
 METRIC = "HT-decomp ms @1024^3 r32, err<=1e-3 vs FP64: mixed/learned vs plain FP32"
+# DRAM bytes (read + write) of one leaf-Gram launch at 1024^3, from a one-pass ncu capture:
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none
+#       -k 'regex:tc_gemm_kernel|convert_bf16' -c 8 python bench.py --steps 2 --warmup 1 --mixed-only --no-cpu
+# (2.149e9 read + ~0 written per Gram launch; X in BF16 is 2.147e9 bytes)
+GRAM_DRAM_BYTES_PER_LAUNCH = 2.149e9
 
 
 def peaks():
@@ -503,9 +508,13 @@ def run_ours(args, world, rank, local):
                         "mixed_minus_fp64": err_mixed - e_opt, "plain_minus_fp64": err_plain - e_opt},
             "stage_ms": stage_med,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "roofline": {"bound": "tensor", "kernel": "tc_gemm_kernel<256> (leaf Grams, 3 launches + reduce)",
+            "roofline": {"bound": "tensor", "kernel": "tc_gemm_kernel<256,2> (leaf Grams, 3 launches + reduce)",
                          "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
-                         "frac": achieved / pk["bf16_tflops"], "traffic": None,
+                         "frac": achieved / pk["bf16_tflops"],
+                         "traffic": GRAM_DRAM_BYTES_PER_LAUNCH if n == N_FULL else None,
+                         "traffic_unit": "bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)",
+                         "algorithmic_bytes_per_launch": 2 * float(n) ** 3,
+                         "flop_per_launch": float(n) ** 4,
                          "peak_source": pk["source"] + " bf16 burst"},
             "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
             "other_configs": others,
