@@ -32,7 +32,7 @@ from .tree import (DimTree, balanced_tree_4d, left_first_tree_3d, middle_tree_3d
                    uniform_ranks)
 
 __all__ = ["DimTree", "reference_tree_3d", "left_first_tree_3d", "middle_tree_3d", "balanced_tree_4d",
-           "uniform_ranks", "decompose", "reconstruct_error", "reconstruct", "evaluate", "htformat", "htd", "htd4", "HTResult", "HTError", "synth",
+           "uniform_ranks", "decompose", "decompose_streaming", "reconstruct_error", "reconstruct", "evaluate", "htformat", "htd", "htd4", "HTResult", "HTError", "synth",
            "workspace_size", "release_workspace", "kernel_launch_count", "BatchDecomposer", "release_batch"]
 
 _PREC = {"fp32": PREC_FP32, "bf16": PREC_BF16}
@@ -197,6 +197,50 @@ def decompose(x, tree: DimTree, dims: Optional[Sequence[int]] = None, precision:
         "path": {"tcgen05": bool(rep.path_flags & 1), "simt": bool(rep.path_flags & 2)},
     }
     del keep
+    return HTResult(tree, dims, U, B, report)
+
+
+def decompose_streaming(x, tree: DimTree, slab_bytes: int, dims: Optional[Sequence[int]] = None,
+                        precision: str = "bf16", oversample: int = 16, eig_iters: int = 10, seed: int = 1234,
+                        compute_error: bool = False, stream=None) -> HTResult:
+    """Out-of-core HT decomposition of a 3rd-order float32 tensor that stays in
+    host memory (a Fortran-ordered numpy array of shape dims, or a flat buffer
+    with dims=): X is streamed through two device slab buffers of at most
+    slab_bytes together (ht_decompose_streaming).  Factors come back as numpy
+    arrays.  Page-locked host memory (e.g. from torch's pin_memory) gives the
+    full copy bandwidth."""
+    if _is_torch(x):   # a contiguous CPU tensor shaped dims[::-1] (its memory is the column-major tensor)
+        import torch
+        if x.is_cuda or x.dtype != torch.float32 or not x.is_contiguous():
+            raise TypeError("decompose_streaming reads a contiguous float32 host tensor; use decompose for device "
+                            "tensors")
+        dims = tuple(int(d) for d in (dims if dims is not None else reversed(x.shape)))
+        keep, xptr = [x], x.data_ptr()
+    else:
+        dims = _dims_of(x, tree, dims)
+        arr, xptr = _host_input(x, dims)
+        keep = [arr]
+    if len(dims) != 3:
+        raise ValueError("decompose_streaming handles 3rd-order tensors")
+    tree.check_ranks(dims)
+    flags = FLAG_COMPUTE_ERROR if compute_error else 0
+    cfg, keep2 = _config(precision, oversample, eig_iters, 1, seed, flags)
+    ts = _tree_struct(tree)
+    U, B, uptr, bptr = _out_buffers(tree, dims, None)
+    rep = HtReport()
+    check(lib().ht_decompose_streaming(c_void_p(xptr), (c_long * 4)(*dims), 3, ctypes.byref(ts), ctypes.byref(cfg),
+                                       uptr, bptr, ctypes.c_ulonglong(int(slab_bytes)), ctypes.byref(rep),
+                                       c_void_p(stream) if stream else None))
+    report = {
+        "rel_err": rep.rel_err if compute_error else None,
+        "norm_x": rep.norm_x,
+        "ms_total": rep.ms_total,
+        "ms_stage": {name: rep.ms_stage[i] for i, name in
+                     enumerate(["pass_grams_12", "pass_gram_3", "eig", "core_pass", "transfer", "error_pass"])},
+        "gpu_launches": rep.gpu_launches,
+        "path": {"tcgen05": bool(rep.path_flags & 1), "simt": bool(rep.path_flags & 2)},
+    }
+    del keep, keep2
     return HTResult(tree, dims, U, B, report)
 
 

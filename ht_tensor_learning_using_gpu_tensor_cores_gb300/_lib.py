@@ -26,7 +26,7 @@ EXPORTED = ["ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", 
             "ht_mode_gram", "ht_mode_product", "ht_corange_product", "ht_mode_gram_noalloc",
             "ht_decompose_batched", "ht_release_batch", "ht_sketch_loss_grad", "ht_sketch_adam",
             "ht_reconstruct", "ht_evaluate", "ht_layer_weight", "ht_layer_forward", "ht_layer_backward",
-            "ht_layer_check", "ht_layer_release"]
+            "ht_layer_check", "ht_layer_release", "ht_decompose_streaming"]
 
 
 class HtTree(Structure):
@@ -86,6 +86,9 @@ def lib():
                                  c_void_p, c_void_p]
     L.ht_evaluate.argtypes = [POINTER(c_long), c_int, POINTER(HtTree), POINTER(c_void_p), POINTER(c_void_p),
                               c_void_p, c_longlong, c_void_p, c_void_p]
+    L.ht_decompose_streaming.argtypes = [c_void_p, POINTER(c_long), c_int, POINTER(HtTree), POINTER(HtConfig),
+                                         POINTER(c_void_p), POINTER(c_void_p), c_ulonglong, POINTER(HtReport),
+                                         c_void_p]
     L.ht_layer_weight.argtypes = [POINTER(HtLayerShape)] + [c_void_p] * 7
     L.ht_layer_forward.argtypes = [POINTER(HtLayerShape)] + [c_void_p] * 6 + [c_int, c_int, c_void_p, c_longlong,
                                                                               c_void_p, c_void_p]
@@ -118,7 +121,7 @@ def lib():
     L.ht_sketch_adam.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_longlong, c_float, c_int, c_void_p]
     L.ht_corange_product.argtypes = [c_void_p, POINTER(c_long), c_int, c_int, c_int, c_void_p, c_int, c_int,
                                      c_void_p, c_void_p]
-    for name in ("ht_layer_weight", "ht_layer_forward", "ht_layer_backward", "ht_layer_check", "ht_layer_release",
+    for name in ("ht_decompose_streaming", "ht_layer_weight", "ht_layer_forward", "ht_layer_backward", "ht_layer_check", "ht_layer_release",
                  "ht_reconstruct", "ht_evaluate", "ht_sketch_loss_grad", "ht_sketch_adam", "ht_decompose_batched", "ht_release_batch", "ht_mode_gram", "ht_mode_gram_noalloc", "ht_mode_product", "ht_corange_product", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
                  "ht_decompose", "ht_reconstruct_error", "ht_workspace_size", "ht_release_workspace"):
         getattr(L, name).restype = c_int

@@ -536,30 +536,15 @@ struct Timeline {
   }
 };
 
-ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const float *x32,
-                           const __nv_bfloat16 *x16, const __nv_bfloat16 *x16t, int lb, const long *dims,
-                           int order, Result &res, Timeline &tl) {
+// 2. top-K eigenvectors of every leaf Gram G[m], one batched launch; the leaf
+// bases land in res.U (arena memory taken here).
+ht_status_t leaf_eigs(Ctx &c, const Tree &T, const ht_config_t &cfg, const long *dims, int order, float *const *G,
+                      EigProblem *ep, Result &res) {
   const int p_over = cfg.oversample > 0 ? cfg.oversample : 16;
   const int iters = cfg.eig_iters > 0 ? cfg.eig_iters : 10;
   const bool d3 = order == 3;
   Plan3 P3{};
   if (d3) P3 = plan3(T);
-
-  // 1. leaf Grams
-  float *G[4] = {};
-  for (int m = 0; m < order; ++m) {
-    G[m] = c.ar.take<float>(static_cast<size_t>(dims[m]) * dims[m]);
-    if (!G[m]) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (Gram)");
-  }
-  for (int m = 0; m < order; ++m) {
-    const View v = view_of_group(dims, order, m, m);
-    if (m == order - 1 && x16t) HT_TRY(gram_transposed(c, v, x32, x16t, lb, G[m]));
-    else HT_TRY(gram(c, v, x32, x16, G[m]));
-  }
-  tl.mark(c.st);
-
-  // 2. top-K eigenvectors of every leaf Gram, one batch
-  EigProblem ep[4];
   for (int m = 0; m < order; ++m) {
     const int leaf = T.leaf_of_mode(m);
     const int K = (d3 && leaf == P3.c) ? P3.kw : T.rank[leaf];
@@ -601,6 +586,72 @@ ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const 
     if (!c.dry()) HT_CUDA(eig_batched(ep, order, iters, ews, eb, c.err, c.st, &c.launches, c.eig_ctas));
     c.ar.off = mark;
   }
+  return HT_OK;
+}
+
+// Buffers of the 3rd-order transfer step (taken before the core pass's scratch).
+struct Transfer3 {
+  float *C, *WG, *M, *Bkt, *Broot, *Bt;
+};
+
+ht_status_t take_transfer3(Ctx &c, const Plan3 &P, Transfer3 &tr) {
+  tr.C = c.ar.take<float>(static_cast<size_t>(P.kp) * P.kq * P.kt);
+  tr.WG = c.ar.take<float>(static_cast<size_t>(P.kw) * P.kw);
+  tr.M = c.ar.take<float>(static_cast<size_t>(P.kt) * P.kt);
+  tr.Bkt = c.ar.take<float>(static_cast<size_t>(P.kt) * P.kc);
+  tr.Broot = c.ar.take<float>(static_cast<size_t>(P.kt) * P.kc);
+  tr.Bt = c.ar.take<float>(static_cast<size_t>(P.kp) * P.kq * P.kt);
+  if (!tr.C || !tr.WG || !tr.M || !tr.Bkt || !tr.Broot || !tr.Bt)
+    return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (transfer)");
+  return HT_OK;
+}
+
+// 4. transfer tensors from the core-pass product Z = X_(t) V (3rd order).
+ht_status_t transfer3_from_z(Ctx &c, const Plan3 &P, const long *dims, const EigProblem *ep, const float *Z,
+                             const Transfer3 &tr, Result &res) {
+  const EigProblem &ec = ep[P.mc];
+  HT_TRY(core_contract(c, Z, static_cast<int>(dims[P.mp]), static_cast<int>(dims[P.mq]), P.kt, ep[P.mp].U, P.kp,
+                       ep[P.mq].U, P.kq, tr.C));
+  if (!c.dry()) {
+    const int nc = static_cast<int>(dims[P.mc]);
+    HT_CUDA(gemm_tn_small_launch(ec.U, nc, ec.GU, nc, tr.WG, P.kw, P.kw, P.kw, nc, c.st));
+    HT_CUDA(transfer_eig_launch(tr.WG, P.kw, P.kt, P.kc, 1, tr.M, tr.Bkt, c.st));
+    const long long kpq = static_cast<long long>(P.kp) * P.kq;
+    HT_CUDA(matmul_nn_launch(tr.C, kpq, tr.M, P.kt, tr.Bt, kpq, kpq, P.kt, P.kt, c.st));
+    c.launches += 3;
+    if (!P.t_is_left) {
+      HT_CUDA(transpose_small_launch(tr.Bkt, P.kt, P.kc, tr.Broot, c.st));
+      ++c.launches;
+    }
+  }
+  res.B[P.t] = tr.Bt;
+  res.B[0] = P.t_is_left ? tr.Bkt : tr.Broot;
+  return HT_OK;
+}
+
+ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const float *x32,
+                           const __nv_bfloat16 *x16, const __nv_bfloat16 *x16t, int lb, const long *dims,
+                           int order, Result &res, Timeline &tl) {
+  const int p_over = cfg.oversample > 0 ? cfg.oversample : 16;
+  const bool d3 = order == 3;
+  Plan3 P3{};
+  if (d3) P3 = plan3(T);
+
+  // 1. leaf Grams
+  float *G[4] = {};
+  for (int m = 0; m < order; ++m) {
+    G[m] = c.ar.take<float>(static_cast<size_t>(dims[m]) * dims[m]);
+    if (!G[m]) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (Gram)");
+  }
+  for (int m = 0; m < order; ++m) {
+    const View v = view_of_group(dims, order, m, m);
+    if (m == order - 1 && x16t) HT_TRY(gram_transposed(c, v, x32, x16t, lb, G[m]));
+    else HT_TRY(gram(c, v, x32, x16, G[m]));
+  }
+  tl.mark(c.st);
+
+  EigProblem ep[4];
+  HT_TRY(leaf_eigs(c, T, cfg, dims, order, G, ep, res));
   tl.mark(c.st);
 
   if (d3) {
@@ -608,13 +659,8 @@ ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const 
     const View vc = view_of_group(dims, 3, P.mc, P.mc);
     const long long zrows = vc.L * vc.R;
     const EigProblem &ec = ep[P.mc];
-    float *C = c.ar.take<float>(static_cast<size_t>(P.kp) * P.kq * P.kt);
-    float *WG = c.ar.take<float>(static_cast<size_t>(P.kw) * P.kw);
-    float *M = c.ar.take<float>(static_cast<size_t>(P.kt) * P.kt);
-    float *Bkt = c.ar.take<float>(static_cast<size_t>(P.kt) * P.kc);
-    float *Broot = c.ar.take<float>(static_cast<size_t>(P.kt) * P.kc);
-    float *Bt = c.ar.take<float>(static_cast<size_t>(P.kp) * P.kq * P.kt);
-    if (!C || !WG || !M || !Bkt || !Broot || !Bt) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (transfer)");
+    Transfer3 tr;
+    HT_TRY(take_transfer3(c, P, tr));
     const size_t mark = c.ar.off;
     float *Z = c.ar.take<float>(static_cast<size_t>(zrows) * P.kt);
     // V enters the BF16 product as high + low BF16 parts (one MMA tile of
@@ -632,24 +678,8 @@ ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const 
     }
     HT_TRY(mode_product(c, vc, x32, x16, ec.U, V16, P.kt, Z, fold_h));
     tl.mark(c.st);
-    // 4. transfer tensors
-    HT_TRY(core_contract(c, Z, static_cast<int>(dims[P.mp]), static_cast<int>(dims[P.mq]), P.kt, ep[P.mp].U, P.kp,
-                         ep[P.mq].U, P.kq, C));
+    HT_TRY(transfer3_from_z(c, P, dims, ep, Z, tr, res));
     c.ar.off = mark;
-    if (!c.dry()) {
-      const int nc = static_cast<int>(dims[P.mc]);
-      HT_CUDA(gemm_tn_small_launch(ec.U, nc, ec.GU, nc, WG, P.kw, P.kw, P.kw, nc, c.st));
-      HT_CUDA(transfer_eig_launch(WG, P.kw, P.kt, P.kc, 1, M, Bkt, c.st));
-      const long long kpq = static_cast<long long>(P.kp) * P.kq;
-      HT_CUDA(matmul_nn_launch(C, kpq, M, P.kt, Bt, kpq, kpq, P.kt, P.kt, c.st));
-      c.launches += 3;
-      if (!P.t_is_left) {
-        HT_CUDA(transpose_small_launch(Bkt, P.kt, P.kc, Broot, c.st));
-        ++c.launches;
-      }
-    }
-    res.B[P.t] = Bt;
-    res.B[0] = P.t_is_left ? Bkt : Broot;
     tl.mark(c.st);
     return HT_OK;
   }
@@ -802,6 +832,262 @@ ht_status_t error_core(Ctx &c, const Tree &T, const float *x32, const long *dims
 size_t factor_count(const Tree &T, const long *dims, int t) {
   if (T.leaf(t)) return static_cast<size_t>(dims[T.mode_of_leaf(t)]) * T.rank[t];
   return static_cast<size_t>(T.rank[T.left[t]]) * T.rank[T.right[t]] * T.rank[t];
+}
+
+// ------------------------------------------------------------ out-of-core path
+// A 3rd-order tensor that stays in host memory (the reference's 3D/TSQR variant
+// streams four slabs of frontal slices: htd_tensorcore.cu:58-111).  Passes over
+// host X, each through two device slab buffers (the copy of slab s+1 on its own
+// stream overlaps the work on slab s):
+//   A  slabs along mode 2 (contiguous):    ||X||^2, G_0 += X_s(0) X_s(0)^T, G_1 likewise
+//   B  slabs along mode 1 (2-D copies):    G_2 += X_s(2) X_s(2)^T
+//      (a Gram accumulates over slabs along any mode but its own)
+//   -  leaf eigen-solver on the three Grams, in core
+//   C  slabs along mode 2:                 Z = X_(t) V, accumulated (c = mode 2) or
+//                                          written by row blocks (c = mode 0 or 1)
+//   -  transfer tensors from Z, in core
+//   D  (error) slabs along mode 2:         ||X_s - Xhat_s||^2 from the fused error kernel
+struct StreamArgs {
+  const float *xh;
+  const long *dims;
+  float *const *U;
+  float *const *B;
+  bool want_err;
+  long long slab2, slab1;   // slab lengths along modes 2 and 1
+};
+
+struct SlabIo {
+  cudaStream_t cs = nullptr;
+  cudaEvent_t copied[2] = {}, freed[2] = {};
+  float *buf[2] = {};
+};
+
+// Streams `count` slabs through io.buf: copy(s, dst, cs) issues slab s's copy
+// on the copy stream, compute(s, src) enqueues its work on c.st.  In a dry run
+// only slab 0's work is sized.
+template <class Copy, class Compute>
+ht_status_t stream_slabs(Ctx &c, SlabIo &io, long long count, Copy copy, Compute compute) {
+  if (c.dry()) return count > 0 ? compute(0, io.buf[0]) : HT_OK;
+  // the buffers may still be read by an earlier pass's work on c.st
+  HT_CUDA(cudaEventRecord(io.freed[0], c.st));
+  HT_CUDA(cudaStreamWaitEvent(io.cs, io.freed[0], 0));
+  auto issue = [&](long long s) -> ht_status_t {
+    const int b = static_cast<int>(s & 1);
+    if (s >= 2) HT_CUDA(cudaStreamWaitEvent(io.cs, io.freed[b], 0));
+    HT_TRY(copy(s, io.buf[b], io.cs));
+    HT_CUDA(cudaEventRecord(io.copied[b], io.cs));
+    return HT_OK;
+  };
+  HT_TRY(issue(0));
+  for (long long s = 0; s < count; ++s) {
+    if (s + 1 < count) HT_TRY(issue(s + 1));
+    const int b = static_cast<int>(s & 1);
+    HT_CUDA(cudaStreamWaitEvent(c.st, io.copied[b], 0));
+    HT_TRY(compute(s, io.buf[b]));
+    HT_CUDA(cudaEventRecord(io.freed[b], c.st));
+  }
+  return HT_OK;
+}
+
+ht_status_t stream_call(Ctx &c, const Tree &T, const ht_config_t &cfg, const StreamArgs &a, SlabIo &io,
+                        Timeline &tl, double *dsum) {
+  const long n0 = a.dims[0], n1 = a.dims[1], n2 = a.dims[2];
+  const long long s2 = a.slab2, s1 = a.slab1;
+  const long long cnt2 = (n2 + s2 - 1) / s2, cnt1 = (n1 + s1 - 1) / s1;
+  const long long slab_floats = std::max(s2 * n0 * n1, s1 * n0 * n2);
+  const Plan3 P = plan3(T);
+  const long nmax = std::max({n0, n1, n2});
+  io.buf[0] = c.ar.take<float>(static_cast<size_t>(slab_floats));
+  io.buf[1] = c.ar.take<float>(static_cast<size_t>(slab_floats));
+  __nv_bfloat16 *b16 = c.tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(slab_floats) + 64) : nullptr;
+  __nv_bfloat16 *b16t = c.tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(slab_floats) + 64) : nullptr;
+  double *nparts = c.ar.take<double>(static_cast<size_t>(cnt2) * 1024);
+  double *scratch_parts = c.ar.take<double>(1024);
+  float *G[3];
+  for (int m = 0; m < 3; ++m) G[m] = c.ar.take<float>(static_cast<size_t>(a.dims[m]) * a.dims[m]);
+  float *Gt = c.ar.take<float>(static_cast<size_t>(nmax) * nmax);
+  if (!io.buf[0] || !io.buf[1] || (c.tc && (!b16 || !b16t)) || !nparts || !scratch_parts || !G[0] || !G[1] ||
+      !G[2] || !Gt)
+    return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (streaming buffers)");
+  const size_t slab_row_bytes2 = sizeof(float) * static_cast<size_t>(n0) * n1;
+  auto copy2 = [&](long long s, float *dst, cudaStream_t cs) -> ht_status_t {   // X[:, :, c0:c0+len]
+    const long long c0 = s * s2, len = std::min(s2, n2 - c0);
+    HT_CUDA(cudaMemcpyAsync(dst, a.xh + static_cast<size_t>(n0) * n1 * c0, slab_row_bytes2 * len,
+                            cudaMemcpyHostToDevice, cs));
+    return HT_OK;
+  };
+  auto copy1 = [&](long long s, float *dst, cudaStream_t cs) -> ht_status_t {   // X[:, j0:j0+len, :]
+    const long long j0 = s * s1, len = std::min(s1, n1 - j0);
+    const size_t w = sizeof(float) * static_cast<size_t>(n0) * len;
+    HT_CUDA(cudaMemcpy2DAsync(dst, w, a.xh + static_cast<size_t>(n0) * j0, sizeof(float) * n0 * n1, w, n2,
+                              cudaMemcpyHostToDevice, cs));
+    return HT_OK;
+  };
+  auto bf16_of = [&](const float *x, long long count, double *parts) -> ht_status_t {
+    if (c.dry()) return HT_OK;
+    if (c.tc) HT_CUDA(convert_bf16_launch(x, b16, count, parts, 1024, c.st));
+    else HT_CUDA(sumsq_launch(x, count, parts, 1024, c.st));
+    ++c.launches;
+    return HT_OK;
+  };
+  auto accumulate = [&](float *dst, const float *src, long long count, bool first) -> ht_status_t {
+    if (!c.dry()) {
+      HT_CUDA(accumulate_launch(dst, src, count, first ? 1 : 0, c.st));
+      ++c.launches;
+    }
+    return HT_OK;
+  };
+
+  // pass A: ||X||^2, G_0, G_1
+  HT_TRY(stream_slabs(c, io, cnt2, copy2, [&](long long s, const float *x) -> ht_status_t {
+    const long long len = std::min(s2, n2 - s * s2);
+    const long dd[3] = {n0, n1, static_cast<long>(len)};
+    HT_TRY(bf16_of(x, n0 * n1 * len, nparts + s * 1024));
+    for (int m = 0; m < 2; ++m) {
+      HT_TRY(gram(c, view_of_group(dd, 3, m, m), x, b16, Gt));
+      HT_TRY(accumulate(G[m], Gt, static_cast<long long>(a.dims[m]) * a.dims[m], s == 0));
+    }
+    return HT_OK;
+  }));
+  if (!c.dry()) {
+    HT_CUDA(sumsq_finish_launch(nparts, static_cast<int>(cnt2 * 1024), dsum, c.st));
+    ++c.launches;
+  }
+  tl.mark(c.st);
+  // pass B: G_2
+  HT_TRY(stream_slabs(c, io, cnt1, copy1, [&](long long s, const float *x) -> ht_status_t {
+    const long long len = std::min(s1, n1 - s * s1);
+    const long dd[3] = {n0, static_cast<long>(len), n2};
+    const View v = view_of_group(dd, 3, 2, 2);
+    const int lb = c.tc ? last_mode_block(dd, 3) : 0;
+    if (lb && !c.dry()) {
+      HT_CUDA(convert_bf16_dual_launch(x, b16, b16t, v.L, v.N, lb, scratch_parts, 1024, c.st));
+      ++c.launches;
+    } else {
+      HT_TRY(bf16_of(x, n0 * len * n2, scratch_parts));
+    }
+    if (lb) HT_TRY(gram_transposed(c, v, x, b16t, lb, Gt));
+    else HT_TRY(gram(c, v, x, b16, Gt));
+    return accumulate(G[2], Gt, static_cast<long long>(n2) * n2, s == 0);
+  }));
+  tl.mark(c.st);
+
+  // leaf eigen-solver
+  Result res;
+  EigProblem ep[4];
+  HT_TRY(leaf_eigs(c, T, cfg, a.dims, 3, G, ep, res));
+  tl.mark(c.st);
+
+  // pass C: Z = X_(t) V
+  const EigProblem &ec = ep[P.mc];
+  const View vc = view_of_group(a.dims, 3, P.mc, P.mc);
+  const long long zrows = vc.L * vc.R;
+  Transfer3 tr;
+  HT_TRY(take_transfer3(c, P, tr));
+  const size_t mark = c.ar.off;
+  const int fold_h = P.kt <= 32 ? 32 : 64;
+  float *Z = c.ar.take<float>(static_cast<size_t>(zrows) * P.kt);
+  const long long zs_rows = P.mc == 2 ? zrows : (P.mc == 0 ? static_cast<long long>(n1) * s2 : static_cast<long long>(n0) * s2);
+  float *Zs = c.ar.take<float>(static_cast<size_t>(zs_rows) * P.kt);
+  const long vrows = P.mc == 2 ? static_cast<long>(s2) : static_cast<long>(a.dims[P.mc]);
+  float *Vs = c.ar.take<float>(static_cast<size_t>(vrows) * P.kt);
+  __nv_bfloat16 *V16 = c.tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(vrows) * 2 * fold_h + 64) : nullptr;
+  if (!Z || !Zs || !Vs || (c.tc && !V16)) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (core pass)");
+  if (P.mc != 2 && !c.dry()) {   // V is used whole by every slab
+    HT_CUDA(cudaMemcpyAsync(Vs, ec.U, sizeof(float) * a.dims[P.mc] * P.kt, cudaMemcpyDeviceToDevice, c.st));
+    if (V16) {
+      HT_CUDA(split_bf16_launch(Vs, a.dims[P.mc], P.kt, fold_h, V16, c.st));
+      ++c.launches;
+    }
+  }
+  HT_TRY(stream_slabs(c, io, cnt2, copy2, [&](long long s, const float *x) -> ht_status_t {
+    const long long c0 = s * s2, len = std::min(s2, n2 - c0);
+    const long dd[3] = {n0, n1, static_cast<long>(len)};
+    if (c.tc) HT_TRY(bf16_of(x, n0 * n1 * len, scratch_parts));
+    const View v = view_of_group(dd, 3, P.mc, P.mc);
+    if (P.mc == 2) {   // V rows of this slab
+      if (!c.dry()) {
+        HT_CUDA(cudaMemcpy2DAsync(Vs, sizeof(float) * len, ec.U + c0, sizeof(float) * n2, sizeof(float) * len, P.kt,
+                                  cudaMemcpyDeviceToDevice, c.st));
+        if (V16) {
+          HT_CUDA(split_bf16_launch(Vs, len, P.kt, fold_h, V16, c.st));
+          ++c.launches;
+        }
+      }
+      HT_TRY(mode_product(c, v, x, c.tc ? b16 : nullptr, Vs, V16, P.kt, Zs, fold_h));
+      return accumulate(Z, Zs, zrows * P.kt, s == 0);
+    }
+    HT_TRY(mode_product(c, v, x, c.tc ? b16 : nullptr, Vs, V16, P.kt, Zs, fold_h));
+    if (!c.dry()) {   // rows (i1 or i0, i2 in the slab) of Z
+      const long long per = P.mc == 0 ? n1 : n0;
+      HT_CUDA(cudaMemcpy2DAsync(Z + per * c0, sizeof(float) * zrows, Zs, sizeof(float) * per * len,
+                                sizeof(float) * per * len, P.kt, cudaMemcpyDeviceToDevice, c.st));
+    }
+    return HT_OK;
+  }));
+  tl.mark(c.st);
+  HT_TRY(transfer3_from_z(c, P, a.dims, ep, Z, tr, res));
+  c.ar.off = mark;
+  tl.mark(c.st);
+
+  // outputs
+  for (int t = 0; t < T.n_nodes; ++t) {
+    float *dst = T.leaf(t) ? a.U[t] : a.B[t];
+    const float *src = T.leaf(t) ? res.U[t] : res.B[t];
+    if (dst && !c.dry())
+      HT_CUDA(cudaMemcpyAsync(dst, src, factor_count(T, a.dims, t) * sizeof(float), cudaMemcpyDefault, c.st));
+  }
+
+  // pass D: ||X - Xhat||^2
+  if (a.want_err) {
+    const long np_ = a.dims[P.mp], nq_ = a.dims[P.mq], nc_ = a.dims[P.mc];
+    float *Bkt = c.ar.take<float>(static_cast<size_t>(P.kt) * P.kc);
+    float *core = c.ar.take<float>(static_cast<size_t>(P.kp) * P.kq * P.kc);
+    float *Tm = c.ar.take<float>(static_cast<size_t>(np_) * P.kq * P.kc);
+    float *Wm = c.ar.take<float>(static_cast<size_t>(np_) * nq_ * P.kc);
+    long long nb = 0;
+    if (P.mc == 2) nb = error_fused_blocks(static_cast<long long>(n0) * n1, s2);
+    else if (P.mc == 0) nb = error_fused_blocks(n0, static_cast<long long>(n1) * s2);
+    else nb = static_cast<long long>(error_fused_blocks(n0, n1)) * s2;
+    double *eparts = c.ar.take<double>(static_cast<size_t>(nb * cnt2) + 8);
+    if (!Bkt || !core || !Tm || !Wm || !eparts) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (error)");
+    if (!c.dry()) {
+      HT_CUDA(cudaMemsetAsync(eparts, 0, sizeof(double) * nb * cnt2, c.st));
+      if (P.t_is_left)
+        HT_CUDA(cudaMemcpyAsync(Bkt, res.B[0], sizeof(float) * P.kt * P.kc, cudaMemcpyDeviceToDevice, c.st));
+      else HT_CUDA(transpose_small_launch(res.B[0], P.kc, P.kt, Bkt, c.st));
+      const long long kpq = static_cast<long long>(P.kp) * P.kq;
+      HT_CUDA(matmul_nn_launch(res.B[P.t], kpq, Bkt, P.kt, core, kpq, kpq, P.kc, P.kt, c.st));
+      HT_CUDA(expand2_launch(res.U[P.p], static_cast<int>(np_), P.kp, core, res.U[P.q], static_cast<int>(nq_), P.kq,
+                             P.kc, Tm, Wm, c.st));
+      c.launches += 4;
+    }
+    HT_TRY(stream_slabs(c, io, cnt2, copy2, [&](long long s, const float *x) -> ht_status_t {
+      if (c.dry()) return HT_OK;
+      const long long c0 = s * s2, len = std::min(s2, n2 - c0);
+      double *pp = eparts + s * nb;
+      if (P.mc == 2) {   // X_s (n0 n1 x len) = W U_2[c0:c0+len]^T
+        const long long R = static_cast<long long>(n0) * n1;
+        HT_CUDA(error_fused_launch(x, R, 0, Wm, R, 0, res.U[P.c] + c0, nc_, R, len, P.kc, 1, pp, c.st));
+      } else if (P.mc == 0) {   // X_s (n0 x n1 len) = U_0 W[rows (i1, i2 in slab)]^T
+        HT_CUDA(error_fused_launch(x, n0, 0, res.U[P.c], n0, 0, Wm + static_cast<long long>(n1) * c0,
+                                   static_cast<long long>(np_) * nq_, n0, static_cast<long long>(n1) * len, P.kc, 1,
+                                   pp, c.st));
+      } else {   // slice i2 of X_s (n0 x n1) = W[rows (i0, i2)] U_1^T
+        HT_CUDA(error_fused_launch(x, n0, static_cast<long long>(n0) * n1, Wm + static_cast<long long>(n0) * c0,
+                                   static_cast<long long>(np_) * nq_, n0, res.U[P.c], nc_, n0, n1, P.kc,
+                                   static_cast<int>(len), pp, c.st));
+      }
+      ++c.launches;
+      return HT_OK;
+    }));
+    if (!c.dry()) {
+      HT_CUDA(sumsq_finish_launch(eparts, static_cast<int>(nb * cnt2), dsum + 1, c.st));
+      ++c.launches;
+    }
+    tl.mark(c.st);
+  }
+  return HT_OK;
 }
 
 // One full call (decomposition, outputs, optional error), used both as the
@@ -1137,6 +1423,126 @@ ht_status_t ht_decompose(const float *x, const long *dims, int order, const ht_t
   c.ar.base = static_cast<char *>(ws);
   c.ar.cap = bytes;
   return run_call(c, T, cfg, a, report);
+}
+
+ht_status_t ht_decompose_streaming(const float *x, const long *dims, int order, const ht_tree_t *tree,
+                                   const ht_config_t *cfg_in, float *const *U, float *const *B,
+                                   unsigned long long slab_bytes, ht_report_t *report, void *stream) {
+  if (!x || !dims || !U || !B) return fail(HT_ERR_INVALID_ARG, "NULL argument");
+  if (order != 3) return fail(HT_ERR_UNSUPPORTED, "the streaming path handles 3rd-order tensors");
+  Tree T;
+  HT_TRY(parse_tree(tree, dims, order, T));
+  ht_config_t cfg;
+  if (cfg_in) cfg = *cfg_in;
+  else ht_config_default(&cfg);
+  if (cfg.precision != HT_PREC_FP32 && cfg.precision != HT_PREC_BF16) return fail(HT_ERR_INVALID_ARG, "unknown precision");
+  if (cfg.leaf_method != HT_LEAF_GRAM) return fail(HT_ERR_UNSUPPORTED, "only the Gram leaf method is implemented");
+  if (cfg.oversample < 0 || cfg.eig_iters < 0) return fail(HT_ERR_INVALID_ARG, "negative oversample / eig_iters");
+  for (int t = 0; t < T.n_nodes; ++t) {
+    if (T.leaf(t) && !U[t]) return fail(HT_ERR_INVALID_ARG, "U[t] is NULL for leaf " + std::to_string(t));
+    if (!T.leaf(t) && !B[t]) return fail(HT_ERR_INVALID_ARG, "B[t] is NULL for interior node " + std::to_string(t));
+  }
+  HT_TRY(check_device());
+  if (is_device_ptr(x)) return fail(HT_ERR_INVALID_ARG, "the streaming path reads x from host memory; use ht_decompose");
+  // slab lengths: two FP32 slab buffers within slab_bytes, multiples of 8 where possible
+  auto slab_len = [&](long long per_index, long long extent) {
+    long long len = static_cast<long long>(slab_bytes / (2ull * sizeof(float) * static_cast<unsigned long long>(per_index)));
+    if (len >= 8) len -= len % 8;
+    return std::max(1ll, std::min(len, extent));
+  };
+  StreamArgs a;
+  a.xh = x;
+  a.dims = dims;
+  a.U = U;
+  a.B = B;
+  a.want_err = (cfg.flags & HT_FLAG_COMPUTE_ERROR) != 0;
+  a.slab2 = slab_len(static_cast<long long>(dims[0]) * dims[1], dims[2]);
+  a.slab1 = slab_len(static_cast<long long>(dims[0]) * dims[2], dims[1]);
+  std::lock_guard<std::mutex> lk(g_ws_mutex);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  auto plan = [&](Ctx &c, SlabIo &io, Timeline &tl, double **dsum) -> ht_status_t {
+    c.err = c.ar.take<int>(64);
+    *dsum = c.ar.take<double>(8);
+    if (!c.err || !*dsum) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small");
+    if (!c.dry()) HT_CUDA(cudaMemsetAsync(c.err, 0, sizeof(int), c.st));
+    tl.mark(c.st);
+    return stream_call(c, T, cfg, a, io, tl, *dsum);
+  };
+  size_t bytes = 0;
+  {
+    Ctx d;
+    d.ar.dry = true;
+    d.tc = cfg.precision == HT_PREC_BF16;
+    SlabIo io;
+    Timeline tl;
+    double *ds = nullptr;
+    HT_TRY(plan(d, io, tl, &ds));
+    bytes = d.ar.peak + (1 << 20);
+  }
+  void *ws = nullptr;
+  HT_TRY(acquire_workspace(bytes, &ws, st));
+  Ctx c;
+  c.st = st;
+  c.tc = cfg.precision == HT_PREC_BF16;
+  c.ar.base = static_cast<char *>(ws);
+  c.ar.cap = bytes;
+  SlabIo io;
+  Timeline tl;
+  tl.on = report != nullptr;
+  struct Cleanup {
+    SlabIo &io;
+    Timeline &tl;
+    ~Cleanup() {
+      if (io.cs) {
+        cudaStreamSynchronize(io.cs);
+        cudaStreamDestroy(io.cs);
+      }
+      for (int b = 0; b < 2; ++b) {
+        if (io.copied[b]) cudaEventDestroy(io.copied[b]);
+        if (io.freed[b]) cudaEventDestroy(io.freed[b]);
+      }
+      if (tl.on)
+        for (int i = 0; i < 8; ++i)
+          if (tl.ev[i]) cudaEventDestroy(tl.ev[i]);
+    }
+  } cleanup{io, tl};
+  HT_CUDA(cudaStreamCreateWithFlags(&io.cs, cudaStreamNonBlocking));
+  for (int b = 0; b < 2; ++b) {
+    HT_CUDA(cudaEventCreateWithFlags(&io.copied[b], cudaEventDisableTiming));
+    HT_CUDA(cudaEventCreateWithFlags(&io.freed[b], cudaEventDisableTiming));
+  }
+  if (tl.on)
+    for (int i = 0; i < 8; ++i) HT_CUDA(cudaEventCreate(&tl.ev[i]));
+  double *dsum = nullptr;
+  HT_TRY(plan(c, io, tl, &dsum));
+  double host_sums[2] = {0.0, 0.0};
+  HT_CUDA(cudaMemcpyAsync(host_sums, dsum, sizeof(double) * (a.want_err ? 2 : 1), cudaMemcpyDeviceToHost, c.st));
+  int errword = 0;
+  HT_CUDA(cudaMemcpyAsync(&errword, c.err, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+  HT_CUDA(cudaStreamSynchronize(c.st));
+  HT_CUDA(cudaGetLastError());
+  g_launches += static_cast<unsigned long long>(c.launches);
+  if (errword & kErrTimeout) return fail(HT_ERR_TIMEOUT, "a kernel's bounded wait expired; results are invalid");
+  if (!std::isfinite(host_sums[0])) return fail(HT_ERR_NUMERICAL, "input tensor contains NaN or Inf");
+  if (report) {
+    std::memset(report, 0, sizeof(*report));
+    report->norm_x = std::sqrt(host_sums[0]);
+    report->rel_err =
+        a.want_err ? (host_sums[0] > 0 ? std::sqrt(std::max(host_sums[1], 0.0) / host_sums[0]) : 0.0) : -1.0;
+    // marks: 0 start, 1 pass A, 2 pass B, 3 eig, 4 pass C, 5 transfer, 6 error pass
+    float ms = 0.f;
+    for (int i = 1; i < tl.n && i <= 6; ++i) {
+      cudaEventElapsedTime(&ms, tl.ev[i - 1], tl.ev[i]);
+      report->ms_stage[i - 1] = ms;
+    }
+    if (tl.n >= 2) {
+      cudaEventElapsedTime(&ms, tl.ev[0], tl.ev[tl.n - 1]);
+      report->ms_total = ms;
+    }
+    report->gpu_launches = c.launches;
+    report->path_flags = c.path;
+  }
+  return HT_OK;
 }
 
 ht_status_t ht_decompose_batched(int count, const float *const *x, const long *dims, int order,

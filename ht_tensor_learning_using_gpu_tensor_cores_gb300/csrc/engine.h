@@ -109,6 +109,8 @@ bool make_gram_gen(long long n, int bn, TileGen *g, int bm = 128);
 cudaError_t convert_bf16_launch(const float *x, __nv_bfloat16 *xb, long long n, double *sumsq_partials,
                                 int num_partials, cudaStream_t s);
 cudaError_t sumsq_launch(const float *x, long long n, double *partials, int num_partials, cudaStream_t s);
+// dst = src (first != 0) or dst += src, n floats
+cudaError_t accumulate_launch(float *dst, const float *src, long long n, int first, cudaStream_t s);
 // X (L x N) -> xb (same layout) and xbt (l-blocks of B = 2^lb: xbt[((l/B) N + n) B + l%B])
 // in BF16 + sum-of-squares partials; 6 <= lb <= 12, L % B == 0, x 16-byte aligned
 cudaError_t convert_bf16_dual_launch(const float *x, __nv_bfloat16 *xb, __nv_bfloat16 *xbt, long long L, long long N,

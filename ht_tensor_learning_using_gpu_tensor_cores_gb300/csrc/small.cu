@@ -100,6 +100,12 @@ __global__ void __launch_bounds__(256) convert_bf16_dual_kernel(const float *__r
   if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
 }
 
+// dst = src (first) or dst + src, n floats
+__global__ void accumulate_kernel(float *__restrict__ dst, const float *__restrict__ src, long long n, int first) {
+  for (long long i = blockIdx.x * 256ll + threadIdx.x; i < n; i += gridDim.x * 256ll)
+    dst[i] = first ? src[i] : dst[i] + src[i];
+}
+
 __global__ void sumsq_kernel(const float *__restrict__ x, long long n, double *partials) {
   Acc2 a = {0.f, 0.f};
   for (long long i = blockIdx.x * 256ll + threadIdx.x; i < n; i += gridDim.x * 256ll) {
@@ -349,6 +355,11 @@ cudaError_t convert_bf16_dual_launch(const float *x, __nv_bfloat16 *xb, __nv_bfl
       (reinterpret_cast<uintptr_t>(xbt) & 7u))
     return cudaErrorInvalidValue;
   convert_bf16_dual_kernel<<<num_partials, 256, 0, s>>>(x, xb, xbt, L, N, lb, partials);
+  return cudaGetLastError();
+}
+
+cudaError_t accumulate_launch(float *dst, const float *src, long long n, int first, cudaStream_t s) {
+  accumulate_kernel<<<grid_for(n), 256, 0, s>>>(dst, src, n, first);
   return cudaGetLastError();
 }
 

@@ -119,6 +119,24 @@ ht_status_t ht_decompose(const float *x, const long *dims, int order,
                          float *const *U, float *const *B,
                          ht_report_t *report, void *stream);
 
+/* Out-of-core variant for 3rd-order tensors that stay in host memory (pinned
+ * memory gives the full copy bandwidth; pageable memory works through the
+ * driver's staging).  The reference's 3D/TSQR variant streams the tensor in
+ * four slabs of frontal slices (third_order_tensor_decompsition/CUDA/TSQR/
+ * htd_tensorcore.cu:58-111).  Here X goes through two device slab buffers of at
+ * most slab_bytes together, three times (four with HT_FLAG_COMPUTE_ERROR):
+ * slabs along mode 3 for the mode-1 and mode-2 Grams, slabs along mode 2 for
+ * the mode-3 Gram, slabs along mode 3 for the core pass (and the error); each
+ * copy overlaps the work on the previous slab.  Same outputs and
+ * configuration as ht_decompose.  report->ms_stage: 0 first pass (Grams 1, 2),
+ * 1 second pass (Gram 3), 2 eigen-solver, 3 core pass, 4 transfer tensors,
+ * 5 error pass. */
+ht_status_t ht_decompose_streaming(const float *x, const long *dims, int order,
+                                   const ht_tree_t *tree, const ht_config_t *cfg,
+                                   float *const *U, float *const *B,
+                                   unsigned long long slab_bytes,
+                                   ht_report_t *report, void *stream);
+
 /* Relative reconstruction error ||X - Xhat||_F / ||X||_F of an HT
  * representation (one fused pass over x on the GPU; htd_batch.cu:196-244). */
 ht_status_t ht_reconstruct_error(const float *x, const long *dims, int order,
