@@ -245,6 +245,8 @@ def secondary_configs(ht, synth, torch, stream, steps=10, warmup=3):
     torch.cuda.empty_cache()
     out["ht_format"] = ht_format_config(ht, synth, torch, stream)
     torch.cuda.empty_cache()
+    out["out_of_core"] = out_of_core_config(ht, synth, torch)
+    torch.cuda.empty_cache()
     out["ht_layer"] = ht_layer_config(torch, stream)
     torch.cuda.empty_cache()
     return out
@@ -341,6 +343,35 @@ def ht_format_config(ht, synth, torch, stream, n=1024, k=32):
     return {"n": n, "rank": k, "reconstruct_ms": rec_ms,
             "reconstruct_write_GBps": n ** 3 * 4 / (rec_ms * 1e-3) / 1e9,
             "evaluate_entries": cnt, "evaluate_ms": ev_ms, "evaluate_entries_per_s": cnt / (ev_ms * 1e-3)}
+
+
+def out_of_core_config(ht, synth, torch, n=1024, k=32, slab_gib=1.0):
+    """The headline tensor (1024^3, rank 32) decomposed from page-locked host memory
+    through ht_decompose_streaming with 1 GiB of device slab buffers (a quarter of
+    the tensor): three passes over host X, BF16 products.  Reports ms per
+    decomposition (wall clock around the synchronous call), the host bytes
+    streamed and the effective host->device rate, and the error against the
+    in-core path on the same tensor."""
+    tree = ht.reference_tree_3d([1, k, k, k, k])
+    Xd = synth.odeco(n, decay=DECAY, seed=1, assemble_on=torch.device("cuda"))
+    e_in = ht.decompose(Xd, tree, precision="bf16", compute_error=True).report["rel_err"]
+    Xh = Xd.cpu().pin_memory()
+    del Xd
+    torch.cuda.empty_cache()
+    slab = int(slab_gib * (1 << 30))
+    r = ht.decompose_streaming(Xh, tree, slab_bytes=slab, precision="bf16", compute_error=True)
+    ht.decompose_streaming(Xh, tree, slab_bytes=slab, precision="bf16")
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        rr = ht.decompose_streaming(Xh, tree, slab_bytes=slab, precision="bf16")
+    ms = (time.perf_counter() - t0) * 1e3 / reps
+    streamed = 3 * n ** 3 * 4
+    del Xh
+    ht.release_workspace()
+    return {"n": n, "rank": k, "slab_buffer_bytes": slab, "passes": 3, "ms": ms,
+            "host_bytes_streamed": streamed, "effective_h2d_GBps": streamed / (ms * 1e-3) / 1e9,
+            "stage_ms": rr.report["ms_stage"], "rel_err": r.report["rel_err"], "rel_err_in_core": e_in}
 
 
 def learned_sketch_config(ht, synth, torch, stream, n=512, k=24, p=10, n_train=256, n_test=64, steps=2000):
