@@ -629,9 +629,10 @@ ht_status_t transfer3_from_z(Ctx &c, const Plan3 &P, const long *dims, const Eig
   return HT_OK;
 }
 
+// G_pre[m] non-null: the mode-m Gram is already there (the pipelined input path).
 ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const float *x32,
                            const __nv_bfloat16 *x16, const __nv_bfloat16 *x16t, int lb, const long *dims,
-                           int order, Result &res, Timeline &tl) {
+                           int order, Result &res, Timeline &tl, float *const *G_pre = nullptr) {
   const int p_over = cfg.oversample > 0 ? cfg.oversample : 16;
   const bool d3 = order == 3;
   Plan3 P3{};
@@ -640,10 +641,11 @@ ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const 
   // 1. leaf Grams
   float *G[4] = {};
   for (int m = 0; m < order; ++m) {
-    G[m] = c.ar.take<float>(static_cast<size_t>(dims[m]) * dims[m]);
+    G[m] = (G_pre && G_pre[m]) ? G_pre[m] : c.ar.take<float>(static_cast<size_t>(dims[m]) * dims[m]);
     if (!G[m]) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (Gram)");
   }
   for (int m = 0; m < order; ++m) {
+    if (G_pre && G_pre[m]) continue;
     const View v = view_of_group(dims, order, m, m);
     if (m == order - 1 && x16t) HT_TRY(gram_transposed(c, v, x32, x16t, lb, G[m]));
     else HT_TRY(gram(c, v, x32, x16, G[m]));
@@ -1143,6 +1145,98 @@ ht_status_t enqueue_body(Ctx &c, const Tree &T, const ht_config_t &cfg, const fl
   return HT_OK;
 }
 
+// Host input, mixed path, 3rd order with the l-blocked copy: the host->device
+// copy goes in slabs along mode 3 on its own stream, and each slab's BF16
+// conversion and its share of the mode-1 and mode-2 Grams run as soon as it
+// lands, so that only the last slab's work, the mode-3 Gram and the rest of the
+// decomposition follow the copy.  The whole tensor ends up resident as in the
+// plain host-input path.
+constexpr int kPipeSlabs = 8;
+
+bool pipelined_input(const Ctx &c, const CallArgs &a) {
+  if (a.x_dev || !c.tc || a.order != 3) return false;
+  const int lb = last_mode_block(a.dims, a.order);
+  if (lb != 8) return false;   // 16-column conversion tiles: slabs of multiples of 16 columns
+  const long long total = static_cast<long long>(a.dims[0]) * a.dims[1] * a.dims[2];
+  return total * 4 >= (256ll << 20) && a.dims[2] >= 16 * kPipeSlabs;
+}
+
+ht_status_t enqueue_pipelined(Ctx &c, const Tree &T, const ht_config_t &cfg, const CallArgs &a, double *dsum,
+                              Timeline &tl, Result &res, cudaEvent_t h2d_done) {
+  const long n0 = a.dims[0], n1 = a.dims[1], n2 = a.dims[2];
+  const long long L = static_cast<long long>(n0) * n1, total = L * n2;
+  const int lb = last_mode_block(a.dims, a.order);
+  long long len = (n2 + kPipeSlabs - 1) / kPipeSlabs;
+  len = (len + 15) / 16 * 16;
+  const long long S = (n2 + len - 1) / len;
+  float *xd = c.ar.take<float>(static_cast<size_t>(total));
+  __nv_bfloat16 *xb = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
+  __nv_bfloat16 *xbt = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
+  double *parts = c.ar.take<double>(static_cast<size_t>(S) * 1024);
+  float *G[4] = {};
+  G[0] = c.ar.take<float>(static_cast<size_t>(n0) * n0);
+  G[1] = c.ar.take<float>(static_cast<size_t>(n1) * n1);
+  float *Gt = c.ar.take<float>(static_cast<size_t>(std::max(n0, n1)) * std::max(n0, n1));
+  if (!xd || !xb || !xbt || !parts || !G[0] || !G[1] || !Gt)
+    return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (pipelined input)");
+  cudaStream_t cs = nullptr;
+  cudaEvent_t ev[kPipeSlabs + 1] = {};
+  struct Cleanup {
+    cudaStream_t &cs;
+    cudaEvent_t *ev;
+    ~Cleanup() {
+      if (cs) {
+        cudaStreamSynchronize(cs);
+        cudaStreamDestroy(cs);
+      }
+      for (int i = 0; i <= kPipeSlabs; ++i)
+        if (ev[i]) cudaEventDestroy(ev[i]);
+    }
+  } cleanup{cs, ev};
+  if (!c.dry()) {
+    HT_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    for (long long s = 0; s <= S; ++s) HT_CUDA(cudaEventCreateWithFlags(&ev[s], cudaEventDisableTiming));
+    // the copy may start only after earlier work on c.st (the workspace is shared)
+    HT_CUDA(cudaEventRecord(ev[S], c.st));
+    HT_CUDA(cudaStreamWaitEvent(cs, ev[S], 0));
+    for (long long s = 0; s < S; ++s) {
+      const long long c0 = s * len, w = std::min(len, n2 - c0);
+      HT_CUDA(cudaMemcpyAsync(xd + L * c0, a.x + L * c0, sizeof(float) * L * w, cudaMemcpyHostToDevice, cs));
+      HT_CUDA(cudaEventRecord(ev[s], cs));
+    }
+    if (h2d_done) HT_CUDA(cudaEventRecord(h2d_done, cs));
+  }
+  for (long long s = 0; s < S; ++s) {
+    const long long c0 = s * len, w = std::min(len, n2 - c0);
+    if (!c.dry()) {
+      HT_CUDA(cudaStreamWaitEvent(c.st, ev[s], 0));
+      HT_CUDA(convert_bf16_dual_launch(xd, xb, xbt, L, n2, lb, parts + s * 1024, 1024, c.st, c0, w));
+      ++c.launches;
+    }
+    const long dd[3] = {n0, n1, static_cast<long>(w)};
+    for (int m = 0; m < 2; ++m) {
+      HT_TRY(gram(c, view_of_group(dd, 3, m, m), xd + L * c0, xb + L * c0, Gt));
+      if (!c.dry()) {
+        HT_CUDA(accumulate_launch(G[m], Gt, static_cast<long long>(a.dims[m]) * a.dims[m], s == 0 ? 1 : 0, c.st));
+        ++c.launches;
+      }
+    }
+  }
+  if (!c.dry()) {
+    HT_CUDA(sumsq_finish_launch(parts, static_cast<int>(S * 1024), dsum, c.st));
+    ++c.launches;
+  }
+  tl.mark(c.st);
+  HT_TRY(decompose_core(c, T, cfg, xd, xb, xbt, lb, a.dims, a.order, res, tl, G));
+  for (int t = 0; t < T.n_nodes; ++t) {
+    float *dst = T.leaf(t) ? a.U[t] : a.B[t];
+    const float *src = T.leaf(t) ? res.U[t] : res.B[t];
+    if (dst && !c.dry()) HT_CUDA(cudaMemcpyAsync(dst, src, factor_count(T, a.dims, t) * sizeof(float), cudaMemcpyDefault, c.st));
+  }
+  if (a.want_err) HT_TRY(error_core(c, T, xd, a.dims, a.order, res.U, res.B, dsum + 1));
+  return HT_OK;
+}
+
 ht_status_t run_call(Ctx &c, const Tree &T, const ht_config_t &cfg, const CallArgs &a, ht_report_t *rep) {
   long long total = 1;
   for (int m = 0; m < a.order; ++m) total *= a.dims[m];
@@ -1171,17 +1265,22 @@ ht_status_t run_call(Ctx &c, const Tree &T, const ht_config_t &cfg, const CallAr
   } guard{tl, h0, h1};
   if (!c.dry()) HT_CUDA(cudaMemsetAsync(c.err, 0, sizeof(int), c.st));
   if (tl.on) HT_CUDA(cudaEventRecord(h0, c.st));
-  const float *xd = a.x;
-  if (!a.x_dev) {
-    float *t = c.ar.take<float>(static_cast<size_t>(total));
-    if (!t) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (tensor)");
-    if (!c.dry()) HT_CUDA(cudaMemcpyAsync(t, a.x, sizeof(float) * total, cudaMemcpyHostToDevice, c.st));
-    xd = t;
-  }
-  if (tl.on) HT_CUDA(cudaEventRecord(h1, c.st));
-  tl.mark(c.st);
   Result res;
-  HT_TRY(enqueue_body(c, T, cfg, xd, a, nparts, dsum, tl, res));
+  if (pipelined_input(c, a)) {
+    tl.mark(c.st);
+    HT_TRY(enqueue_pipelined(c, T, cfg, a, dsum, tl, res, tl.on ? h1 : nullptr));
+  } else {
+    const float *xd = a.x;
+    if (!a.x_dev) {
+      float *t = c.ar.take<float>(static_cast<size_t>(total));
+      if (!t) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (tensor)");
+      if (!c.dry()) HT_CUDA(cudaMemcpyAsync(t, a.x, sizeof(float) * total, cudaMemcpyHostToDevice, c.st));
+      xd = t;
+    }
+    if (tl.on) HT_CUDA(cudaEventRecord(h1, c.st));
+    tl.mark(c.st);
+    HT_TRY(enqueue_body(c, T, cfg, xd, a, nparts, dsum, tl, res));
+  }
   if (c.dry()) return HT_OK;
   double host_sums[2] = {0.0, 0.0};
   HT_CUDA(cudaMemcpyAsync(host_sums, dsum, sizeof(double) * (a.want_err ? 2 : 1), cudaMemcpyDeviceToHost, c.st));

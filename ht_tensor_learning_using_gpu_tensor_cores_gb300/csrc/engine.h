@@ -113,8 +113,11 @@ cudaError_t sumsq_launch(const float *x, long long n, double *partials, int num_
 cudaError_t accumulate_launch(float *dst, const float *src, long long n, int first, cudaStream_t s);
 // X (L x N) -> xb (same layout) and xbt (l-blocks of B = 2^lb: xbt[((l/B) N + n) B + l%B])
 // in BF16 + sum-of-squares partials; 6 <= lb <= 12, L % B == 0, x 16-byte aligned
+// Only the columns n in [n_begin, n_begin + n_count) (n_count < 0: to the end; both
+// multiples of 2^(12 - lb)).
 cudaError_t convert_bf16_dual_launch(const float *x, __nv_bfloat16 *xb, __nv_bfloat16 *xbt, long long L, long long N,
-                                     int lb, double *partials, int num_partials, cudaStream_t s);
+                                     int lb, double *partials, int num_partials, cudaStream_t s,
+                                     long long n_begin = 0, long long n_count = -1);
 cudaError_t f32_to_bf16_launch(const float *x, __nv_bfloat16 *y, long long n, cudaStream_t s);
 // W (rows x k, column-major FP32) -> Y (rows x 2h BF16): columns [0, k) the
 // BF16 rounding hi(W), columns [h, h + k) the rounding of W - hi(W), the rest 0.

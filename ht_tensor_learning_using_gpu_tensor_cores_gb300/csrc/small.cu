@@ -47,7 +47,8 @@ __global__ void __launch_bounds__(256) convert_bf16_kernel(const float *__restri
 
 // X (L x N, l fastest, FP32) -> xb (the same layout, BF16) and xbt, a second
 // BF16 copy in l-blocks of B = 2^lb elements: xbt[((l / B) N + n) B + l % B],
-// plus the compensated sum of squares per block.  Work goes in tiles of B l by
+// plus the compensated sum of squares per block, over the columns n in
+// [n_begin, n_begin + n_count).  Work goes in tiles of B l by
 // TN n (TN = 2^(12 - lb), 4096 elements a tile), l-blocks fastest: the grid's blocks
 // then read and write xb inside TN columns at a time, and each tile's xbt part
 // is one contiguous run of 2 B TN bytes (8 KiB), so all three streams stay
@@ -58,14 +59,15 @@ __global__ void __launch_bounds__(256) convert_bf16_kernel(const float *__restri
 __global__ void __launch_bounds__(256) convert_bf16_dual_kernel(const float *__restrict__ x,
                                                                 __nv_bfloat16 *__restrict__ xb,
                                                                 __nv_bfloat16 *__restrict__ xbt, long long L,
-                                                                long long N, int lb, double *partials) {
+                                                                long long N, long long n_begin, long long n_count,
+                                                                int lb, double *partials) {
   Acc2 a = {0.f, 0.f};
   const int TN = 1 << (12 - lb);
-  const long long B = 1ll << lb, nlb = L >> lb, tiles = nlb * (N / TN);
+  const long long B = 1ll << lb, nlb = L >> lb, tiles = nlb * (n_count / TN);
   const int row4 = static_cast<int>(B / 4);          // float4 per tile column
   // every tile holds B * TN = 4096 elements: 4 float4 per thread, loaded together
   for (long long ti = blockIdx.x; ti < tiles; ti += gridDim.x) {
-    const long long lblk = ti % nlb, n0 = (ti / nlb) * TN;
+    const long long lblk = ti % nlb, n0 = n_begin + (ti / nlb) * TN;
     float4 v[4];
     long long off[4];
 #pragma unroll
@@ -348,13 +350,16 @@ cudaError_t convert_bf16_launch(const float *x, __nv_bfloat16 *xb, long long n, 
 }
 
 cudaError_t convert_bf16_dual_launch(const float *x, __nv_bfloat16 *xb, __nv_bfloat16 *xbt, long long L, long long N,
-                                     int lb, double *partials, int num_partials, cudaStream_t s) {
+                                     int lb, double *partials, int num_partials, cudaStream_t s, long long n_begin,
+                                     long long n_count) {
   const int TN = 1 << (12 - lb);
-  if (lb < 6 || lb > 12 || L % (1ll << lb) || N < TN || N % TN || num_partials < 1 || num_partials > 4096 ||
+  if (n_count < 0) n_count = N - n_begin;
+  if (lb < 6 || lb > 12 || L % (1ll << lb) || N < TN || N % TN || n_begin < 0 || n_begin % TN || n_count % TN ||
+      n_begin + n_count > N || num_partials < 1 || num_partials > 4096 ||
       (reinterpret_cast<uintptr_t>(x) & 15u) || (reinterpret_cast<uintptr_t>(xb) & 7u) ||
       (reinterpret_cast<uintptr_t>(xbt) & 7u))
     return cudaErrorInvalidValue;
-  convert_bf16_dual_kernel<<<num_partials, 256, 0, s>>>(x, xb, xbt, L, N, lb, partials);
+  convert_bf16_dual_kernel<<<num_partials, 256, 0, s>>>(x, xb, xbt, L, N, n_begin, n_count, lb, partials);
   return cudaGetLastError();
 }
 

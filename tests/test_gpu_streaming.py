@@ -85,3 +85,19 @@ def test_streaming_rejects_device_input_and_4th_order():
     t4 = ht.balanced_tree_4d([1, 2, 2, 2, 2, 2, 2])
     with pytest.raises((ValueError, HTError)):
         ht.decompose_streaming(np.zeros((4, 4, 4, 4), np.float32, order="F"), t4, slab_bytes=1 << 20)
+
+
+def test_pipelined_host_input_matches_device_input():
+    """Host input of a large 3rd-order tensor goes through the pipelined copy
+    (slabs along mode 3, conversion and mode-1/2 Gram shares as each lands): the
+    result equals the device-input path's."""
+    n, k = 512, 24
+    tree = ht.reference_tree_3d([1, k, k, k, k])
+    Xd = synth.exact_ht_device((n, n, n), tree, noise_rel=1e-3, seed=13)
+    ref = ht.decompose(Xd, tree, precision="bf16", compute_error=True)
+    Xh = Xd.cpu().pin_memory().numpy().reshape(-1)
+    res = ht.decompose(Xh, tree, dims=(n, n, n), precision="bf16", compute_error=True)
+    assert abs(res.report["rel_err"] - ref.report["rel_err"]) <= 2e-6, (res.report["rel_err"], ref.report["rel_err"])
+    assert abs(res.report["norm_x"] - ref.report["norm_x"]) <= 1e-6 * ref.report["norm_x"]
+    for t in tree.leaves():
+        assert O.principal_angles(np.asarray(res.U[t], np.float64), ref.U[t].cpu().numpy().astype(np.float64)).max() < 1e-3
