@@ -245,8 +245,9 @@ __global__ void __launch_bounds__(kLayerThreads) layer_dq_kernel(const LayerShap
   }
 }
 
-// dP and per-block dQ partials in one pass over dW, a block per (m0, m1): the
-// block reads the M2 rows o = (m0 M1 + m1) M2 + m2 of dW (coalesced, staged in
+// dP and per-block dQ partials in one pass over dW, a block per (m0, m1) and
+// range of m2 (several ranges give dP partials, summed afterwards): the block
+// reads its rows o = (m0 M1 + m1) M2 + m2 of dW (coalesced, staged in
 // shared memory with an odd pair stride), and with Q (C x R1) and the P slice
 // Ps[(n0, n1)][r] resident accumulates
 //   dPs[(n0, n1)][r] += sum_n2 dW[o, (n0, n1, n2)] Q[n2 M2 + m2, r]
@@ -262,7 +263,9 @@ __global__ void __launch_bounds__(kLayerThreads) layer_dpq_kernel(const LayerSha
   const int R1 = sh.r1, B = N1 * M1, NP = N0 * N1, C = N2 * M2;
   const int rs = N2 | 1;                             // odd stride between pairs: conflict-free column reads
   const long long Nin = static_cast<long long>(NP) * N2;
-  const int blk = blockIdx.x, m1 = blk % M1, m0 = blk / M1;
+  const int chunks = gridDim.x / (M0 * M1);          // m2 ranges per (m0, m1): dP partials per range
+  const int blk = blockIdx.x / chunks, ch = blockIdx.x - blk * chunks, m1 = blk % M1, m0 = blk / M1;
+  const int mg = (M2 + chunks - 1) / chunks, m2_lo = ch * mg, m2_hi = min(M2, m2_lo + mg);
   float *row = sm;                                   // NP x rs
   float *Qs = row + static_cast<size_t>(NP) * rs;    // C x R1
   float *Ps = Qs + static_cast<size_t>(C) * R1;      // NP x R1
@@ -273,7 +276,7 @@ __global__ void __launch_bounds__(kLayerThreads) layer_dpq_kernel(const LayerSha
     Ps[e] = P[(static_cast<long long>(n0 * M0 + m0) * B + (n1 * M1 + m1)) * R1 + r];
     dPs[e] = 0.f;
   }
-  for (int m2 = 0; m2 < M2; ++m2) {
+  for (int m2 = m2_lo; m2 < m2_hi; ++m2) {
     __syncthreads();   // previous row fully consumed (and Qs / Ps written on the first pass)
     const float *src = dW + ((static_cast<long long>(m0) * M1 + m1) * M2 + m2) * Nin;
     for (long long i = threadIdx.x; i < Nin; i += kLayerThreads) {
@@ -296,9 +299,11 @@ __global__ void __launch_bounds__(kLayerThreads) layer_dpq_kernel(const LayerSha
     }
   }
   __syncthreads();
+  // chunks > 1: dP points at the partial buffer [chunks][A B R1]
+  float *dPo = dP + static_cast<long long>(ch) * (static_cast<long long>(sh.n[0]) * M0 * B * R1);
   for (int e = threadIdx.x; e < NP * R1; e += kLayerThreads) {
     const int pr = e / R1, r = e - pr * R1, n0 = pr / N1, n1 = pr - n0 * N1;
-    dP[(static_cast<long long>(n0 * M0 + m0) * B + (n1 * M1 + m1)) * R1 + r] = dPs[e];
+    dPo[(static_cast<long long>(n0 * M0 + m0) * B + (n1 * M1 + m1)) * R1 + r] = dPs[e];
   }
 }
 
@@ -317,7 +322,8 @@ __global__ void layer_dq_reduce_kernel(const float *__restrict__ dQpart, int blo
 //   dT1[a, r4, r1] = sum_b dP[a, b, r1] u2[b, r4]   du2[b, r4] = sum_{a, r1} dP[a, b, r1] T1[a, r4, r1]
 //   du1[a, r3] = sum_{r4, r1} dT1[a, r4, r1] b2[r3, r4, r1]
 //   db2[r3, r4, r1] = sum_a u1[a, r3] dT1[a, r4, r1]
-// Stage 1 (one thread per output entry): dT1, du2, du3, db1.
+// Stage 1 (one thread per output entry): dT1, du3 and, when non-null, du2 and
+// db1 (layer_du2_kernel and layer_db1_kernel do those two faster).
 __global__ void layer_grad1_kernel(const LayerShape sh, const float *__restrict__ u2, const float *__restrict__ u3,
                                    const float *__restrict__ b1, const float *__restrict__ T1,
                                    const float *__restrict__ dP, const float *__restrict__ dQ,
@@ -325,8 +331,8 @@ __global__ void layer_grad1_kernel(const LayerShape sh, const float *__restrict_
                                    float *__restrict__ db1) {
   const int A = sh.n[0] * sh.m[0], B = sh.n[1] * sh.m[1], C = sh.n[2] * sh.m[2];
   const int R1 = sh.r1, R2 = sh.r2, R4 = sh.r4;
-  const long long n_dt1 = static_cast<long long>(A) * R4 * R1, n_du2 = static_cast<long long>(B) * R4,
-                  n_du3 = static_cast<long long>(C) * R2, n_db1 = static_cast<long long>(R1) * R2;
+  const long long n_dt1 = static_cast<long long>(A) * R4 * R1, n_du2 = du2 ? static_cast<long long>(B) * R4 : 0,
+                  n_du3 = static_cast<long long>(C) * R2, n_db1 = db1 ? static_cast<long long>(R1) * R2 : 0;
   const long long total = n_dt1 + n_du2 + n_du3 + n_db1;
   for (long long e = blockIdx.x * static_cast<long long>(kLayerThreads) + threadIdx.x; e < total;
        e += static_cast<long long>(gridDim.x) * kLayerThreads) {
@@ -358,6 +364,71 @@ __global__ void layer_grad1_kernel(const LayerShape sh, const float *__restrict_
       for (int c = 0; c < C; ++c) s = fmaf(dQ[static_cast<long long>(c) * R1 + r1], u3[c * R2 + r2], s);
       db1[f] = s;
     }
+  }
+}
+
+// du2[b, r4] = sum_{a, r1} dP[a, b, r1] T1[a, r4, r1]: a block per b, the
+// (a, r1) pairs split over the threads with R4 accumulators each, then a
+// fixed-order reduction (deterministic).
+__global__ void __launch_bounds__(kLayerThreads) layer_du2_kernel(const LayerShape sh, const float *__restrict__ dP,
+                                                                  const float *__restrict__ T1, float *__restrict__ du2) {
+  __shared__ float red[kLayerThreads / 32][kLayerMaxRank];
+  const int A = sh.n[0] * sh.m[0], B = sh.n[1] * sh.m[1];
+  const int R1 = sh.r1, R4 = sh.r4, b = blockIdx.x;
+  float acc[kLayerMaxRank];
+#pragma unroll
+  for (int r = 0; r < kLayerMaxRank; ++r) acc[r] = 0.f;
+  for (int e = threadIdx.x; e < A * R1; e += kLayerThreads) {
+    const int a = e / R1, r1 = e - a * R1;
+    const float g = dP[(static_cast<long long>(a) * B + b) * R1 + r1];
+    const float *t = T1 + static_cast<long long>(a) * R4 * R1 + r1;
+#pragma unroll
+    for (int r = 0; r < kLayerMaxRank; ++r)
+      if (r < R4) acc[r] = fmaf(g, t[r * R1], acc[r]);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int r = 0; r < kLayerMaxRank; ++r) {
+    float v = acc[r];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) red[warp][r] = v;
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < R4; r += kLayerThreads) {
+    float v = 0.f;
+    for (int w = 0; w < kLayerThreads / 32; ++w) v += red[w][r];
+    du2[static_cast<long long>(b) * R4 + r] = v;
+  }
+}
+
+// db1[r1, r2] = sum_c dQ[c, r1] u3[c, r2]: a block per r1, c split over the
+// threads with R2 accumulators each, fixed-order reduction.
+__global__ void __launch_bounds__(kLayerThreads) layer_db1_kernel(const LayerShape sh, const float *__restrict__ dQ,
+                                                                  const float *__restrict__ u3, float *__restrict__ db1) {
+  __shared__ float red[kLayerThreads / 32][kLayerMaxRank];
+  const int C = sh.n[2] * sh.m[2], R1 = sh.r1, R2 = sh.r2, r1 = blockIdx.x;
+  float acc[kLayerMaxRank];
+#pragma unroll
+  for (int r = 0; r < kLayerMaxRank; ++r) acc[r] = 0.f;
+  for (int c = threadIdx.x; c < C; c += kLayerThreads) {
+    const float g = dQ[static_cast<long long>(c) * R1 + r1];
+    const float *u = u3 + static_cast<long long>(c) * R2;
+#pragma unroll
+    for (int r = 0; r < kLayerMaxRank; ++r)
+      if (r < R2) acc[r] = fmaf(g, u[r], acc[r]);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int r = 0; r < kLayerMaxRank; ++r) {
+    float v = acc[r];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) red[warp][r] = v;
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < R2; r += kLayerThreads) {
+    float v = 0.f;
+    for (int w = 0; w < kLayerThreads / 32; ++w) v += red[w][r];
+    db1[static_cast<long long>(r1) * R2 + r] = v;
   }
 }
 
@@ -457,9 +528,18 @@ cudaError_t layer_colsum_launch(const float *dy, long long batch, long long nout
   return cudaGetLastError();
 }
 
+int layer_dpq_chunks(const LayerShape &sh) {
+  const int blocks = sh.m[0] * sh.m[1];
+  int ch = (2 * 152 + blocks - 1) / blocks;
+  return ch < 1 ? 1 : (ch > sh.m[2] ? sh.m[2] : ch);
+}
+
 size_t layer_dq_part_count(const LayerShape &sh) {
   if (layer_dpq_smem(sh) > kLayerSmemMax) return 0;
-  return static_cast<size_t>(sh.m[0]) * sh.m[1] * sh.n[2] * sh.m[2] * sh.r1;
+  const size_t dq = static_cast<size_t>(sh.m[0]) * sh.m[1] * sh.n[2] * sh.m[2] * sh.r1;
+  const int ch = layer_dpq_chunks(sh);
+  const size_t dp = ch > 1 ? static_cast<size_t>(ch) * sh.n[0] * sh.m[0] * sh.n[1] * sh.m[1] * sh.r1 : 0;
+  return dq + dp;   // dQ partials, then dP partials
 }
 
 cudaError_t layer_factor_grads_launch(const LayerShape &sh, const float *dW, const float *u1, const float *u2,
@@ -471,20 +551,29 @@ cudaError_t layer_factor_grads_launch(const LayerShape &sh, const float *dW, con
   if (smem_dpq <= kLayerSmemMax && dQpart) {
     cudaError_t e = allow_smem(layer_dpq_kernel, smem_dpq);
     if (e != cudaSuccess) return e;
-    const int blocks = sh.m[0] * sh.m[1];
-    layer_dpq_kernel<<<static_cast<unsigned>(blocks), kLayerThreads, smem_dpq, s>>>(sh, dW, P, Q, dP, dQpart);
+    const int blocks = sh.m[0] * sh.m[1], ch = layer_dpq_chunks(sh);
+    float *dPpart = dQpart + static_cast<size_t>(blocks) * C * sh.r1;
+    layer_dpq_kernel<<<static_cast<unsigned>(blocks * ch), kLayerThreads, smem_dpq, s>>>(sh, dW, P, Q,
+                                                                                         ch > 1 ? dPpart : dP, dQpart);
     const long long cnt = static_cast<long long>(C) * sh.r1;
     layer_dq_reduce_kernel<<<static_cast<unsigned>((cnt + kLayerThreads - 1) / kLayerThreads), kLayerThreads, 0, s>>>(
         dQpart, blocks, cnt, dQ);
+    if (ch > 1) {
+      const long long pc = static_cast<long long>(A) * B * sh.r1;
+      layer_dq_reduce_kernel<<<static_cast<unsigned>((pc + kLayerThreads - 1) / kLayerThreads), kLayerThreads, 0,
+                               s>>>(dPpart, ch, pc, dP);
+    }
   } else {
     const size_t smem = sizeof(float) * static_cast<size_t>(C);
     if (smem > 48 * 1024) return cudaErrorInvalidValue;
     layer_dp_kernel<<<static_cast<unsigned>(A * B), kLayerThreads, smem, s>>>(sh, dW, Q, dP);
     layer_dq_kernel<<<static_cast<unsigned>(C), kLayerThreads, 0, s>>>(sh, dW, P, dQ);
   }
-  const long long n1 = static_cast<long long>(A) * sh.r4 * sh.r1 + static_cast<long long>(B) * sh.r4 +
-                       static_cast<long long>(C) * sh.r2 + static_cast<long long>(sh.r1) * sh.r2;
-  layer_grad1_kernel<<<grid_for_layer(n1), kLayerThreads, 0, s>>>(sh, u2, u3, b1, T1, dP, dQ, dT1, du2, du3, db1);
+  const long long n1 = static_cast<long long>(A) * sh.r4 * sh.r1 + static_cast<long long>(C) * sh.r2;
+  layer_grad1_kernel<<<grid_for_layer(n1), kLayerThreads, 0, s>>>(sh, u2, u3, b1, T1, dP, dQ, dT1, nullptr, du3,
+                                                                   nullptr);
+  layer_du2_kernel<<<static_cast<unsigned>(B), kLayerThreads, 0, s>>>(sh, dP, T1, du2);
+  layer_db1_kernel<<<static_cast<unsigned>(sh.r1), kLayerThreads, 0, s>>>(sh, dQ, u3, db1);
   const long long n2 = static_cast<long long>(A) * sh.r3 + static_cast<long long>(sh.r3) * sh.r4 * sh.r1;
   layer_grad2_kernel<<<grid_for_layer(n2), kLayerThreads, 0, s>>>(sh, u1, b2, dT1, du1, db2);
   return cudaGetLastError();
