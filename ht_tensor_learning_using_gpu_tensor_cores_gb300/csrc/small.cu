@@ -12,7 +12,7 @@
 namespace htgb {
 namespace {
 
-__global__ void __launch_bounds__(256) convert_bf16_kernel(const float *__restrict__ x, __nv_bfloat16 *__restrict__ xb,
+__global__ void __launch_bounds__(256, 8) convert_bf16_kernel(const float *__restrict__ x, __nv_bfloat16 *__restrict__ xb,
                                                            long long n, double *partials) {
   Acc2 a = {0.f, 0.f};
   const long long n4 = n / 4;
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(256) convert_bf16_kernel(const float *__restri
 // (rows n, K = l) are 2B bytes apart inside each l-block, where in xb they lie
 // 2L bytes apart (one 2 MiB page per row at 1024^3).  Needs L % B == 0 and
 // N % TN == 0.
-__global__ void __launch_bounds__(256) convert_bf16_dual_kernel(const float *__restrict__ x,
+__global__ void __launch_bounds__(256, 8) convert_bf16_dual_kernel(const float *__restrict__ x,
                                                                 __nv_bfloat16 *__restrict__ xb,
                                                                 __nv_bfloat16 *__restrict__ xbt, long long L,
                                                                 long long N, long long n_begin, long long n_count,
