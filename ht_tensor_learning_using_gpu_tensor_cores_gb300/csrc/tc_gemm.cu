@@ -39,7 +39,7 @@ constexpr int kThreads = 192;
 // traffic per MMA than 128-row tiles, and a deeper ring in time.
 template <int BN, int MT>
 struct TcCfg {
-  static constexpr int STAGES = MT == 2 ? (BN == 256 ? 3 : 4) : (BN == 256 ? 4 : (BN == 128 ? 6 : 8));
+  static constexpr int STAGES = MT == 2 ? (BN == 256 ? 3 : 4) : (BN == 256 ? 4 : (BN == 128 ? 6 : 3));
   static constexpr uint32_t A_BYTES = MT * BM * BK * 2;
   static constexpr uint32_t B_BYTES = BN * BK * 2;
   static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
