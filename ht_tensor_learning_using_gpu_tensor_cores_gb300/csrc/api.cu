@@ -426,7 +426,9 @@ ht_status_t core_contract(Ctx &c, const float *Z, int np, int nq, int ku, const 
   const size_t mark = c.ar.off;
   const long long rows = static_cast<long long>(nq) * ku;
   float *T1 = c.ar.take<float>(static_cast<size_t>(rows) * kp);
-  if (!T1) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (core)");
+  const int ranges = core_step2_ranges(nq, ku);
+  float *parts = ranges > 1 ? c.ar.take<float>(static_cast<size_t>(ranges) * kp * kq * ku) : nullptr;
+  if (!T1 || (ranges > 1 && !parts)) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (core)");
   // T1[(j + nq*u) + rows*a] = sum_i Z[i + np*(j + nq*u)] Up[i + np*a]
   GemmReq q;
   q.a32.kind = OP_KM3; q.a32.ptr = Z; q.a32.d0 = np; q.a32.d1 = rows; q.a32.d2 = 1;
@@ -439,8 +441,8 @@ ht_status_t core_contract(Ctx &c, const float *Z, int np, int nq, int ku, const 
   q.ld_out = rows;
   HT_TRY(run_gemm(c, q));
   if (!c.dry()) {
-    HT_CUDA(core_step2_launch(T1, rows, nq, kp, Uq, kq, ku, C, c.st));
-    ++c.launches;
+    HT_CUDA(core_step2_launch(T1, rows, nq, kp, Uq, kq, ku, C, parts, c.st));
+    c.launches += ranges > 1 ? 2 : 1;
   }
   c.ar.off = mark;
   return HT_OK;

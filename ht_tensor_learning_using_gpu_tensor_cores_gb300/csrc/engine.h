@@ -126,9 +126,12 @@ cudaError_t sumsq_finish_launch(const double *partials, int n, double *out, cuda
 // C (m x n) = A^T B with A (K x m), B (K x n), column-major, compensated FP32.
 cudaError_t gemm_tn_small_launch(const float *A, int lda, const float *B, int ldb, float *C, int ldc, int m, int n,
                                  int K, cudaStream_t s);
-// C[a + kp*b + kp*kq*c] = sum_j T1[(j + nq*c) + ldt*a] * Uq[j + nq*b]
+// C[a + kp*b + kp*kq*c] = sum_j T1[(j + nq*c) + ldt*a] * Uq[j + nq*b].  scratch (or
+// null: one CTA per c) holds core_step2_ranges(nq, kc) * kp*kq*kc floats of partial
+// sums over ranges of j, summed in order afterwards.
+int core_step2_ranges(int nq, int kc);
 cudaError_t core_step2_launch(const float *T1, long long ldt, int nq, int kp, const float *Uq, int kq, int kc, float *C,
-                              cudaStream_t s);
+                              float *scratch, cudaStream_t s);
 // W[i0 + n0*i1 + n0*n1*c] = sum_{a,b} U0[i0,a] U1[i1,b] core[a + k0*b + k0*k1*c]  (T: n0*k1*k2 scratch)
 cudaError_t expand2_launch(const float *U0, int n0, int k0, const float *core, const float *U1, int n1, int k1, int k2,
                            float *T, float *W, cudaStream_t s);

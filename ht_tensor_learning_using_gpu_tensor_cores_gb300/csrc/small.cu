@@ -174,10 +174,12 @@ __global__ void gemm_tn_small_kernel(const float *__restrict__ A, int lda, const
   if (lane == 0) C[i + static_cast<long long>(ldc) * j] = static_cast<float>(v);
 }
 
-// C[a, b, c] = sum_j T1[(j + nq*c) + ldt*a] * Uq[j + nq*b]   (one CTA per c)
+// C[a, b, c] = sum_j T1[(j + nq*c) + ldt*a] * Uq[j + nq*b]: a CTA per (c, range
+// of jc values of j); with several ranges C points at partials [range][kp kq kc].
 __global__ void __launch_bounds__(256) core_step2_kernel(const float *__restrict__ T1, long long ldt, int nq, int kp,
-                                                         const float *__restrict__ Uq, int kq, float *__restrict__ C) {
-  const int c = blockIdx.x;
+                                                         const float *__restrict__ Uq, int kq, int jc,
+                                                         float *__restrict__ C) {
+  const int c = blockIdx.x, j_lo = blockIdx.y * jc, j_hi = min(nq, j_lo + jc);
   __shared__ float Ts[64][65];
   __shared__ float Us[64][65];
   const int t = threadIdx.x;
@@ -185,12 +187,12 @@ __global__ void __launch_bounds__(256) core_step2_kernel(const float *__restrict
   float acc[16];
 #pragma unroll
   for (int q = 0; q < 16; ++q) acc[q] = 0.f;
-  for (int j0 = 0; j0 < nq; j0 += 64) {
+  for (int j0 = j_lo; j0 < j_hi; j0 += 64) {
     __syncthreads();
     for (int e = t; e < 64 * 64; e += 256) {
       const int jj = e % 64, a = e / 64;
-      Ts[jj][a] = (j0 + jj < nq && a < kp) ? T1[(j0 + jj + static_cast<long long>(nq) * c) + ldt * a] : 0.f;
-      Us[jj][a] = (j0 + jj < nq && a < kq) ? Uq[(j0 + jj) + static_cast<long long>(nq) * a] : 0.f;
+      Ts[jj][a] = (j0 + jj < j_hi && a < kp) ? T1[(j0 + jj + static_cast<long long>(nq) * c) + ldt * a] : 0.f;
+      Us[jj][a] = (j0 + jj < j_hi && a < kq) ? Uq[(j0 + jj) + static_cast<long long>(nq) * a] : 0.f;
     }
     __syncthreads();
 #pragma unroll
@@ -204,10 +206,20 @@ __global__ void __launch_bounds__(256) core_step2_kernel(const float *__restrict
       }
     }
   }
+  float *Co = C + static_cast<long long>(blockIdx.y) * npair * gridDim.x;
 #pragma unroll
   for (int q = 0; q < 16; ++q) {
     const int pr = t + 256 * q;
-    if (pr < npair) C[pr + static_cast<long long>(npair) * c] = acc[q];
+    if (pr < npair) Co[pr + static_cast<long long>(npair) * c] = acc[q];
+  }
+}
+
+// out[e] = sum_r part[r * count + e], r in order
+__global__ void sum_parts_kernel(const float *__restrict__ part, int nparts, long long count, float *__restrict__ out) {
+  for (long long e = blockIdx.x * 256ll + threadIdx.x; e < count; e += gridDim.x * 256ll) {
+    float v = 0.f;
+    for (int r = 0; r < nparts; ++r) v += part[static_cast<long long>(r) * count + e];
+    out[e] = v;
   }
 }
 
@@ -396,10 +408,26 @@ cudaError_t gemm_tn_small_launch(const float *A, int lda, const float *B, int ld
   return cudaGetLastError();
 }
 
+int core_step2_ranges(int nq, int kc) {
+  const int chunks64 = (nq + 63) / 64;
+  int want = (2 * 152 + kc - 1) / kc;
+  if (want > chunks64) want = chunks64;
+  if (want < 1) want = 1;
+  const int per = (chunks64 + want - 1) / want;   // 64-blocks of j per range
+  return (chunks64 + per - 1) / per;
+}
+
 cudaError_t core_step2_launch(const float *T1, long long ldt, int nq, int kp, const float *Uq, int kq, int kc, float *C,
-                              cudaStream_t s) {
+                              float *scratch, cudaStream_t s) {
   if (kp > 64 || kq > 64 || kp * kq > 16 * 256) return cudaErrorInvalidValue;
-  core_step2_kernel<<<kc, 256, 0, s>>>(T1, ldt, nq, kp, Uq, kq, C);
+  const int ranges = scratch ? core_step2_ranges(nq, kc) : 1;
+  const int chunks64 = (nq + 63) / 64;
+  const int jc = 64 * ((chunks64 + ranges - 1) / ranges);
+  core_step2_kernel<<<dim3(kc, ranges), 256, 0, s>>>(T1, ldt, nq, kp, Uq, kq, jc, ranges > 1 ? scratch : C);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || ranges == 1) return e;
+  const long long count = static_cast<long long>(kp) * kq * kc;
+  sum_parts_kernel<<<grid_for(count), 256, 0, s>>>(scratch, ranges, count, C);
   return cudaGetLastError();
 }
 
