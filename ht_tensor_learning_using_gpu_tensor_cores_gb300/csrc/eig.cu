@@ -472,6 +472,19 @@ HT_DEV void jacobi_smem(float (*A)[SMAX + 1], float (*A2)[SMAX + 1], float (*V)[
     float (*tmp)[SMAX + 1] = Ac;
     Ac = An;
     An = tmp;
+    // first quiet round: if no pair of the whole matrix would rotate (the
+    // criterion of jac_choose), the remaining quiet rounds of the sweep would
+    // change nothing
+    if (quiet == 1) {
+      int bad = 0;
+      for (int e = t; e < s * (s + 1) / 2; e += 256) {
+        int i, j;
+        tri_index(e, i, j);
+        const float apq = Ac[i][j];
+        if (i != j && fabsf(apq) > 1e-30f && fabsf(apq) > 2.4e-7f * sqrtf(fabsf(Ac[i][i] * Ac[j][j]))) bad = 1;
+      }
+      if (!__syncthreads_or(bad)) break;
+    }
   }
   if (Ac != A) {
     for (int e = t; e < s * s; e += 256) A[e % s][e / s] = Ac[e % s][e / s];
