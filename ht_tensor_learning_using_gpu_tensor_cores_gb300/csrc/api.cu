@@ -1334,7 +1334,7 @@ size_t dry_run_bytes(const Tree &T, const ht_config_t &cfg, const CallArgs &a) {
 }
 
 // ------------------------------------------------------------ batched path
-constexpr int kLanes = 4;
+constexpr int kLanes = 16;
 
 struct BatchState {
   std::vector<unsigned long long> key;
