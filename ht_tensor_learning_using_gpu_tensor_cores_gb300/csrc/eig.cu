@@ -1003,9 +1003,12 @@ HT_DEV void factor_transform(const double *Sd, int s, double shift, double *A, d
     __syncthreads();
     const int L = s - 1 - j;
     for (int e = t; e < L * (L + 1) / 2; e += 256) {   // A[i][k] -= R[j][i] R[j][k], j < i <= k
-      int ii, kk;
-      tri_index(e, ii, kk);
-      const int i = j + 1 + ii, k = j + 1 + kk;
+      // tri_index varies its first index fastest; mapping it to the column k
+      // (reversed) makes consecutive threads touch consecutive words of a row
+      // instead of one bank SMAX doubles apart
+      int a, b;
+      tri_index(e, a, b);
+      const int i = s - 1 - b, k = s - 1 - a;
       A[i * SMAX + k] = fma(-A[j * SMAX + i], A[j * SMAX + k], A[i * SMAX + k]);
     }
     __syncthreads();
