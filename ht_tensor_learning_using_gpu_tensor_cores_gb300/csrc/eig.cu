@@ -962,25 +962,70 @@ HT_DEV double frsqrt_fp64(double x) {
   return y;
 }
 
+// Pairs of floats (hi + lo, |lo| <= ulp(hi)/2) as a ~48-bit format: sums by
+// Knuth's two-sum, products by the FMA two-product (Dekker's double-float
+// arithmetic).  The rounded intrinsics keep the compiler from contracting or
+// reordering the error terms.
+struct DF {
+  float h, l;
+};
+HT_DEV DF df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+  return DF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+HT_DEV DF df_quick(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+HT_DEV DF df_add(DF x, DF y) {
+  DF s = df_two_sum(x.h, y.h);
+  const DF t = df_two_sum(x.l, y.l);
+  s = df_quick(s.h, __fadd_rn(s.l, t.h));
+  return df_quick(s.h, __fadd_rn(s.l, t.l));
+}
+HT_DEV DF df_mul(DF x, DF y) {
+  const float p = __fmul_rn(x.h, y.h);
+  float e = __fmaf_rn(x.h, y.h, -p);
+  e = __fmaf_rn(x.h, y.l, __fmaf_rn(x.l, y.h, e));
+  return df_quick(p, e);
+}
+HT_DEV DF df_of(double v) {
+  const float h = static_cast<float>(v);
+  return DF{h, static_cast<float>(v - static_cast<double>(h))};
+}
+// 1 / sqrt(x) from the FP32 estimate and one Newton step y + y (1 - x y^2) / 2
+// in pair arithmetic (the step squares the estimate's ~2^-23 relative error).
+HT_DEV DF df_rsqrt(DF x) {
+  const float y0 = rsqrtf(x.h);
+  const DF y = DF{y0, 0.f};
+  const DF r = df_mul(x, df_mul(y, y));
+  const DF e = df_add(DF{1.f, 0.f}, DF{-r.h, -r.l});
+  return df_add(y, df_mul(y, DF{__fmul_rn(0.5f, e.h), __fmul_rn(0.5f, e.l)}));
+}
+
 // Scaled, shifted Cholesky of the packed s x s matrix Sd followed by the
 // explicit transform T = diag(dsc) R^-1 (row-major, stride SMAX, upper
 // triangular, FP32) in Ts, so that applying it is a small matrix product.
 //
-// The factorisation runs in FP64 (A: SMAX x SMAX doubles, d: SMAX doubles,
-// R32: SMAX x SMAX floats of scratch): on numerically rank-deficient blocks the
-// scaled Gram has pivots far below FP32 resolution, and an FP32 factor (or a
-// large shift) would discard the weak directions every iteration.  Shifts are
+// On numerically rank-deficient blocks the scaled Gram has pivots far below
+// FP32 resolution, and an FP32 factor (or a large shift) would discard the weak
+// directions every iteration.  The elimination therefore runs in float-pair
+// arithmetic (~48 bits) on the unit-diagonal scaled matrix: A's storage (SMAX x
+// SMAX doubles) holds the high and the low floats.  GB300 issues FP64 at a
+// small fraction of the FP32 rate and with long latency (measured with clock64
+// on the FP64 version of this loop: ~1000 cycles a step for the pivot alone,
+// ~1900 a step in all); pair arithmetic runs on the FP32 pipe.  Shifts are
 // tiny (1e-12, 1e-14 in the last CholeskyQR pass) and pivots are floored at
-// 1e-24, so T stays finite.  GB300 issues FP64 at a small fraction of FP32, so
-// the elimination spreads every trailing update over all 256 threads (packed
-// triangle), and the triangular inverse runs in FP32 from the FP64 factor: T
-// only has to keep the block well conditioned; the span is that of Y for any
-// invertible T.
+// 1e-24, so T stays finite.  Every trailing update is spread over all 256
+// threads (packed triangle, consecutive threads on consecutive words of a
+// row), and the triangular inverse runs in FP32 from the factor: T only has to
+// keep the block well conditioned; the span is that of Y for any invertible T.
 HT_DEV void factor_transform(const double *Sd, int s, double shift, double *A, double *d, float *R32, float *Ts) {
   const int t = threadIdx.x;
+  float *Ah = reinterpret_cast<float *>(A), *Al = Ah + SMAX * SMAX;   // the pair's high and low floats
   for (int j = t; j < s; j += 256) {
     const double v = Sd[j * (j + 1) / 2 + j];
-    d[j] = v > 1e-300 ? 1.0 / sqrt(v) : 0.0;
+    d[j] = v > 1e-300 ? (v >= 1e-24 ? frsqrt_fp64(v) : 1.0 / sqrt(v)) : 0.0;
   }
   __syncthreads();
   const int E = s * (s + 1) / 2;
@@ -989,34 +1034,47 @@ HT_DEV void factor_transform(const double *Sd, int s, double shift, double *A, d
     tri_index(e, i, j);
     double v = Sd[e] * d[i] * d[j];
     if (i == j) v = (d[j] > 0.0 ? 1.0 : 0.0) + shift;
-    A[i * SMAX + j] = v;
+    const DF p = df_of(v);
+    Ah[i * SMAX + j] = p.h;
+    Al[i * SMAX + j] = p.l;
   }
   __syncthreads();
   for (int j = 0; j < s; ++j) {
     // warp 0 forms the pivot (every lane, no extra barrier) and scales row j
     if (t < 32) {
-      const double piv = fmax(A[j * SMAX + j], 1e-24);
-      const double ri = frsqrt_fp64(piv);
-      for (int k = j + 1 + t; k < s; k += 32) A[j * SMAX + k] *= ri;   // row j of R
-      if (t == 0) A[j * SMAX + j] = piv * ri;
+      DF piv = DF{Ah[j * SMAX + j], Al[j * SMAX + j]};
+      if (!(piv.h >= 1e-24f)) piv = DF{1e-24f, 0.f};
+      const DF ri = df_rsqrt(piv);
+      for (int k = j + 1 + t; k < s; k += 32) {   // row j of R
+        const DF r = df_mul(DF{Ah[j * SMAX + k], Al[j * SMAX + k]}, ri);
+        Ah[j * SMAX + k] = r.h;
+        Al[j * SMAX + k] = r.l;
+      }
+      if (t == 0) {
+        const DF r = df_mul(piv, ri);
+        Ah[j * SMAX + j] = r.h;
+        Al[j * SMAX + j] = r.l;
+      }
     }
     __syncthreads();
     const int L = s - 1 - j;
     for (int e = t; e < L * (L + 1) / 2; e += 256) {   // A[i][k] -= R[j][i] R[j][k], j < i <= k
       // tri_index varies its first index fastest; mapping it to the column k
       // (reversed) makes consecutive threads touch consecutive words of a row
-      // instead of one bank SMAX doubles apart
       int a, b;
       tri_index(e, a, b);
       const int i = s - 1 - b, k = s - 1 - a;
-      A[i * SMAX + k] = fma(-A[j * SMAX + i], A[j * SMAX + k], A[i * SMAX + k]);
+      const DF p = df_mul(DF{Ah[j * SMAX + i], Al[j * SMAX + i]}, DF{Ah[j * SMAX + k], Al[j * SMAX + k]});
+      const DF r = df_add(DF{Ah[i * SMAX + k], Al[i * SMAX + k]}, DF{-p.h, -p.l});
+      Ah[i * SMAX + k] = r.h;
+      Al[i * SMAX + k] = r.l;
     }
     __syncthreads();
   }
   for (int e = t; e < E; e += 256) {
     int i, k;
     tri_index(e, i, k);
-    R32[i * SMAX + k] = static_cast<float>(A[i * SMAX + k]);
+    R32[i * SMAX + k] = __fadd_rn(Ah[i * SMAX + k], Al[i * SMAX + k]);
   }
   __syncthreads();
   // W = R^-1 column by column (thread k solves R w = e_k), T = diag(dsc) W
