@@ -1077,21 +1077,61 @@ HT_DEV void factor_transform(const double *Sd, int s, double shift, double *A, d
     R32[i * SMAX + k] = __fadd_rn(Ah[i * SMAX + k], Al[i * SMAX + k]);
   }
   __syncthreads();
-  // W = R^-1 column by column (thread k solves R w = e_k), T = diag(dsc) W
-  if (t < s) {
-    const int k = t;
-    for (int i = k; i >= 0; --i) {
-      float acc = (i == k) ? 1.f : 0.f;
-      for (int j = i + 1; j <= k; ++j) acc = fmaf(-R32[i * SMAX + j], Ts[j * SMAX + k], acc);
-      Ts[i * SMAX + k] = acc / R32[i * SMAX + i];
+  // W = R^-1 in 32 x 32 blocks, R = [R11 R12; 0 R22]:
+  //   W11 = R11^-1, W22 = R22^-1  (warp 0 / warp 1: lane = column, back substitution
+  //                                 with the column in registers, R rows broadcast)
+  //   W12 = -W11 (R12 W22)        (two 32 x 32 products over all threads)
+  // then T = diag(dsc) W.  W lives in A's storage (free once R is formed).
+  {
+    __shared__ float rinv[SMAX];
+    constexpr int WS = SMAX + 1;
+    float *W = Ah;
+    const int n1 = s < 32 ? s : 32, n2 = s - n1;
+    for (int i = t; i < s; i += 256) rinv[i] = 1.f / R32[i * SMAX + i];
+    for (int e = t; e < SMAX * WS; e += 256) W[e] = 0.f;
+    __syncthreads();
+    if (t < 64) {
+      const int w = t >> 5, lane = t & 31, base = 32 * w, nb = w == 0 ? n1 : n2;
+      if (lane < nb) {
+        float wv[32];
+#pragma unroll
+        for (int ii = 31; ii >= 0; --ii) {
+          float acc = ii == lane ? 1.f : 0.f;
+#pragma unroll
+          for (int jj = ii + 1; jj < 32; ++jj)
+            if (jj <= lane) acc = fmaf(-R32[(base + ii) * SMAX + base + jj], wv[jj], acc);
+          wv[ii] = (ii <= lane) ? acc * rinv[base + (ii < nb ? ii : 0)] : 0.f;
+        }
+#pragma unroll
+        for (int ii = 0; ii < 32; ++ii)
+          if (ii <= lane) W[(base + ii) * WS + base + lane] = wv[ii];
+      }
     }
+    __syncthreads();
+    if (n2 > 0) {
+      // P = R12 W22 (n1 x n2) into the strictly lower part's rows (W[32 + i][*] is free below the diagonal)
+      float *Pm = Ts;   // Ts is written last: use it as scratch (n1 rows, stride SMAX)
+      for (int e = t; e < n1 * n2; e += 256) {
+        const int i = e / n2, k = e % n2;
+        float acc = 0.f;
+        for (int j = 0; j <= k; ++j) acc = fmaf(R32[i * SMAX + 32 + j], W[(32 + j) * WS + 32 + k], acc);
+        Pm[i * SMAX + k] = acc;
+      }
+      __syncthreads();
+      for (int e = t; e < n1 * n2; e += 256) {
+        const int i = e / n2, k = e % n2;
+        float acc = 0.f;
+        for (int j = i; j < n1; ++j) acc = fmaf(W[i * WS + j], Pm[j * SMAX + k], acc);
+        W[i * WS + 32 + k] = -acc;
+      }
+      __syncthreads();
+    }
+    for (int e = t; e < SMAX * SMAX; e += 256) {
+      const int i = e / SMAX, k = e % SMAX;
+      Ts[e] = (i < s && k < s && k >= i) ? W[i * WS + k] * static_cast<float>(d[i]) : 0.f;
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  for (int e = t; e < SMAX * SMAX; e += 256) {
-    const int i = e / SMAX, k = e % SMAX;
-    Ts[e] = (i < s && k < s && k >= i) ? Ts[e] * static_cast<float>(d[i]) : 0.f;
-  }
-  __syncthreads();
 }
 
 // X (RBMAX x SMAX rows) <- X T for the upper-triangular T (s x s): thread
