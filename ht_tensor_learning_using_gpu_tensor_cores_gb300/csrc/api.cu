@@ -585,7 +585,11 @@ ht_status_t leaf_eigs(Ctx &c, const Tree &T, const ht_config_t &cfg, const long 
     const size_t eb = eig_workspace_bytes(ep, order);
     void *ews = c.ar.take<char>(eb);
     if (!ews) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (eig)");
-    if (!c.dry()) HT_CUDA(eig_batched(ep, order, iters, ews, eb, c.err, c.st, &c.launches, c.eig_ctas));
+    // the FP32 path keeps two CholeskyQR refinement passes (its error sits at
+    // FP32 rounding, where the last pass still moves it); the mixed path's
+    // BF16 Gram error is four orders above what they change
+    const int refine = cfg.precision == HT_PREC_FP32 ? 2 : 0;
+    if (!c.dry()) HT_CUDA(eig_batched(ep, order, iters, ews, eb, c.err, c.st, &c.launches, c.eig_ctas, refine));
     c.ar.off = mark;
   }
   return HT_OK;

@@ -8,7 +8,7 @@
 //
 //   Q_0 = Gaussian (or a supplied start block)
 //   Y_i = (G + mu I) Q_i,  Q_{i+1} = Y_i T_i   (T_i: shifted CholeskyQR factor of Y_i)
-//   three more CholeskyQR transforms (orthonormal to FP32 rounding)
+//   (the float-pair factor leaves Q_L = Y_L T_L orthonormal to ~1e-7)
 //   Rayleigh-Ritz: H = Q^T G Q, Jacobi eigen-decomposition of H (s x s),
 //   U = Q V[:, top K], GU = G U, residual max_j ||G u_j - theta_j u_j|| / theta_1.
 //
@@ -804,7 +804,7 @@ struct CoopProb {
 
 struct CoopBatch {
   CoopProb p[kMaxProb];
-  int nprob, iters, nsync, ent_total;
+  int nprob, iters, refine, nsync, ent_total;
   int ent_off[kMaxProb + 1];
   int direct_idx[kMaxProb];               // problem index of direct CTA d (blockIdx.x - nsync)
   unsigned *bar;                          // [2]: arrivals, generation (zero at launch)
@@ -1015,7 +1015,7 @@ HT_DEV DF df_rsqrt(DF x) {
 // small fraction of the FP32 rate and with long latency (measured with clock64
 // on the FP64 version of this loop: ~1000 cycles a step for the pivot alone,
 // ~1900 a step in all); pair arithmetic runs on the FP32 pipe.  Shifts are
-// tiny (1e-12, 1e-14 in the last CholeskyQR pass) and pivots are floored at
+// tiny (1e-12; 1e-14 in a second refinement pass) and pivots are floored at
 // 1e-24, so T stays finite.  Every trailing update is spread over all 256
 // threads (packed triangle, consecutive threads on consecutive words of a
 // row), and the triangular inverse runs in FP32 from the factor: T only has to
@@ -1410,13 +1410,27 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
     ident = false;
     cur ^= 1;
   }
-  // three CholeskyQR transforms: Y_L T_L -> buffer 2, then twice in place
+  // Q_L = Y_L T_L -> buffer 2.  The float-pair factor leaves Q_L orthonormal
+  // to ~1e-7 (scaled off-diagonal of Q_L^T Q_L, 1e-6 on clustered spectra), so
+  // Rayleigh-Ritz takes it as it is: no further CholeskyQR pass.  G Q is formed
+  // from Q_L itself, not as (G Y_L) T_L, whose sum over the ill-scaled columns of
+  // Y_L loses digits to cancellation.
+  // The FP32 path asks for `refine` CholeskyQR passes on Q_L all the same
+  // (orthonormal to FP32 rounding, the last digit of its error).
   coop_step(P, cl, 1, P.buf[cur], P.buf[2], nullptr, ident, 0.f, Rs, Zs, Qr, ring);
-  if (!reduce_and_factor(1e-12)) return;
-  coop_step(P, cl, 1, P.buf[2], P.buf[2], nullptr, false, 0.f, Rs, Zs, Qr, ring);
-  if (!reduce_and_factor(1e-14)) return;
-  // Rayleigh-Ritz: Q = buf2 T -> buf3, G Q -> buf0, H = Q^T G Q
-  coop_step(P, cl, 2, P.buf[2], P.buf[3], P.buf[0], false, 0.f, Rs, Zs, Qr, ring);
+  bool rr_ident = true;
+  if (ident || B.refine > 0) {   // ident: no iteration ran, orthonormalise the start block
+    if (!reduce_and_factor(1e-12)) return;
+    rr_ident = false;
+    for (int r = 1; r < B.refine; ++r) {   // row-local, so in place
+      coop_step(P, cl, 1, P.buf[2], P.buf[2], nullptr, false, 0.f, Rs, Zs, Qr, ring);
+      if (!reduce_and_factor(1e-14)) return;
+    }
+  } else if (!grid_barrier(B.bar, members, B.err, &s_ok)) {
+    return;
+  }
+  // Rayleigh-Ritz: Q -> buf3, G Q -> buf0, H = Q^T G Q
+  coop_step(P, cl, 2, P.buf[2], P.buf[3], P.buf[0], rr_ident, 0.f, Rs, Zs, Qr, ring);
   if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
   coop_reduce(B);
   if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
@@ -1587,7 +1601,7 @@ cudaError_t eig_prepare() {
 }
 
 cudaError_t eig_batched(EigProblem *probs, int nprob, int iters, void *ws, size_t ws_bytes, int *err, cudaStream_t st,
-                        int *launches, int max_ctas) {
+                        int *launches, int max_ctas, int refine) {
   if (nprob <= 0) return cudaSuccess;
   if (nprob > kMaxProb) return cudaErrorInvalidValue;
   if (coop_workspace_bytes(probs, nprob) > ws_bytes) return cudaErrorInvalidValue;
@@ -1602,6 +1616,7 @@ cudaError_t eig_batched(EigProblem *probs, int nprob, int iters, void *ws, size_
   B.err = err;
   B.nprob = nprob;
   B.iters = iters;
+  B.refine = refine < 0 ? 0 : (refine > 2 ? 2 : refine);
   long long n_iter = 0;
   int n_direct = 0, n_iterating = 0;
   for (int i = 0; i < nprob; ++i) {

@@ -165,8 +165,9 @@ size_t eig_workspace_bytes(const EigProblem *probs, int nprob);
 // One-time set-up of the eigen-solver kernels (attributes, occupancy).
 cudaError_t eig_prepare();
 // max_ctas > 0 caps the cooperative grid (several batches running at once).
+// refine (0-2): CholeskyQR passes on the last block before Rayleigh-Ritz.
 cudaError_t eig_batched(EigProblem *probs, int nprob, int iters, void *ws, size_t ws_bytes, int *err,
-                        cudaStream_t s, int *launches, int max_ctas = 0);
+                        cudaStream_t s, int *launches, int max_ctas = 0, int refine = 0);
 // Orthonormalise the columns of tall matrices in place (CholeskyQR, `passes`
 // times; the first pass shifted).  Uses the eigen-solver's workspace layout.
 cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, size_t ws_bytes, cudaStream_t s,
