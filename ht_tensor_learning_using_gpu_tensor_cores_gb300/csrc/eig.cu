@@ -1039,35 +1039,66 @@ HT_DEV void factor_transform(const double *Sd, int s, double shift, double *A, d
     Al[i * SMAX + j] = p.l;
   }
   __syncthreads();
-  for (int j = 0; j < s; ++j) {
-    // warp 0 forms the pivot (every lane, no extra barrier) and scales row j
+  // Row 0 of R: warp 0 forms the pivot (every lane) and scales the row.
+  if (t < 32) {
+    DF piv = DF{Ah[0], Al[0]};
+    if (!(piv.h >= 1e-24f)) piv = DF{1e-24f, 0.f};
+    const DF ri = df_rsqrt(piv);
+    for (int k = 1 + t; k < s; k += 32) {
+      const DF r = df_mul(DF{Ah[k], Al[k]}, ri);
+      Ah[k] = r.h;
+      Al[k] = r.l;
+    }
+    if (t == 0) {
+      const DF r = df_mul(piv, ri);
+      Ah[0] = r.h;
+      Al[0] = r.l;
+    }
+  }
+  __syncthreads();
+  // Step j (row j of R final): warp 0 applies row j to row j + 1, forms its
+  // pivot from registers and scales it -- the next step's row -- while warps
+  // 1-7 apply row j to rows j + 2 .. s - 1.  One barrier a step, and the
+  // pivot's dependent chain overlaps the bulk of the update.  Every entry sees
+  // the same operations in the same order as a plain right-looking sweep.
+  for (int j = 0; j + 1 < s; ++j) {
+    const int j1 = j + 1;
     if (t < 32) {
-      DF piv = DF{Ah[j * SMAX + j], Al[j * SMAX + j]};
+      const DF rj = DF{Ah[j * SMAX + j1], Al[j * SMAX + j1]};
+      DF v[2] = {DF{0.f, 0.f}, DF{0.f, 0.f}};
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int k = j1 + t + 32 * q;
+        if (k < s) {
+          const DF p = df_mul(rj, DF{Ah[j * SMAX + k], Al[j * SMAX + k]});
+          v[q] = df_add(DF{Ah[j1 * SMAX + k], Al[j1 * SMAX + k]}, DF{-p.h, -p.l});
+        }
+      }
+      DF piv = DF{__shfl_sync(0xffffffffu, v[0].h, 0), __shfl_sync(0xffffffffu, v[0].l, 0)};
       if (!(piv.h >= 1e-24f)) piv = DF{1e-24f, 0.f};
       const DF ri = df_rsqrt(piv);
-      for (int k = j + 1 + t; k < s; k += 32) {   // row j of R
-        const DF r = df_mul(DF{Ah[j * SMAX + k], Al[j * SMAX + k]}, ri);
-        Ah[j * SMAX + k] = r.h;
-        Al[j * SMAX + k] = r.l;
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int k = j1 + t + 32 * q;
+        if (k < s) {
+          const DF r = df_mul(k == j1 ? piv : v[q], ri);
+          Ah[j1 * SMAX + k] = r.h;
+          Al[j1 * SMAX + k] = r.l;
+        }
       }
-      if (t == 0) {
-        const DF r = df_mul(piv, ri);
-        Ah[j * SMAX + j] = r.h;
-        Al[j * SMAX + j] = r.l;
+    } else {
+      const int L = s - 2 - j;   // A[i][k] -= R[j][i] R[j][k], j + 1 < i <= k
+      for (int e = t - 32; e < L * (L + 1) / 2; e += 224) {
+        // tri_index varies its first index fastest; mapping it to the column
+        // k (reversed) makes consecutive threads touch consecutive words of a row
+        int a, b;
+        tri_index(e, a, b);
+        const int i = s - 1 - b, k = s - 1 - a;
+        const DF p = df_mul(DF{Ah[j * SMAX + i], Al[j * SMAX + i]}, DF{Ah[j * SMAX + k], Al[j * SMAX + k]});
+        const DF r = df_add(DF{Ah[i * SMAX + k], Al[i * SMAX + k]}, DF{-p.h, -p.l});
+        Ah[i * SMAX + k] = r.h;
+        Al[i * SMAX + k] = r.l;
       }
-    }
-    __syncthreads();
-    const int L = s - 1 - j;
-    for (int e = t; e < L * (L + 1) / 2; e += 256) {   // A[i][k] -= R[j][i] R[j][k], j < i <= k
-      // tri_index varies its first index fastest; mapping it to the column k
-      // (reversed) makes consecutive threads touch consecutive words of a row
-      int a, b;
-      tri_index(e, a, b);
-      const int i = s - 1 - b, k = s - 1 - a;
-      const DF p = df_mul(DF{Ah[j * SMAX + i], Al[j * SMAX + i]}, DF{Ah[j * SMAX + k], Al[j * SMAX + k]});
-      const DF r = df_add(DF{Ah[i * SMAX + k], Al[i * SMAX + k]}, DF{-p.h, -p.l});
-      Ah[i * SMAX + k] = r.h;
-      Al[i * SMAX + k] = r.l;
     }
     __syncthreads();
   }
