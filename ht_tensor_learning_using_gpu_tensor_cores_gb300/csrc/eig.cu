@@ -12,12 +12,13 @@
 //   Rayleigh-Ritz: H = Q^T G Q, Jacobi eigen-decomposition of H (s x s),
 //   U = Q V[:, top K], GU = G U, residual max_j ||G u_j - theta_j u_j|| / theta_1.
 //
-// One launch per iteration: since Q_{i+1} = Y_i T_i, a CTA computes its rows
-// of Y_{i+1} = (G Y_i + mu Y_i) T_i from the complete Y_i of the previous
-// launch, applies T_i by forward substitution, and writes its partial of the
-// s x s Gram Y_{i+1}^T Y_{i+1}.  The last CTA to finish (a two-level
-// "last block" reduction: atomic tickets, no waiting) sums the partials in a
-// fixed order and factors T_{i+1} for the next launch.
+// All iterations of every problem run in ONE cooperative launch
+// (eig_coop_kernel): since Q_{i+1} = Y_i T_i, a CTA computes its rows of
+// Y_{i+1} = (G Y_i + mu Y_i) T_i from the complete Y_i and writes its partial
+// of the s x s Gram Y_{i+1}^T Y_{i+1}; after a grid barrier all CTAs reduce
+// the partials in a fixed order, and after a second one every CTA of the
+// problem factors T_{i+1} itself.  The same kernel, in its CholeskyQR mode,
+// orthonormalises tall blocks without a Gram (the 4th-order range finder).
 //
 // Precision: G and the n x s blocks are FP32; the s x s Gram matrices are
 // accumulated with compensated FP32 (TwoProduct/TwoSum), as accurate as FP64
@@ -38,38 +39,8 @@ namespace {
 
 constexpr int SMAX = 64;
 constexpr int ESMAX = SMAX * (SMAX + 1) / 2;   // packed upper triangle
-constexpr int RB = 16;                          // rows per CTA
-constexpr int GROUP = 8;                        // CTAs per first-level reduction group
+constexpr int GROUP = 8;                        // partials loaded at once by the reduction
 constexpr int kMaxProb = 8;
-constexpr int kThreads = 256;
-
-enum StepMode : int { STEP_ITER = 0, STEP_APPLY = 1, STEP_RR = 2 };
-
-struct EigDev {
-  const float *G;
-  int n, s, K, nrb, ngroups, direct;
-  float *buf[4];            // n x s work blocks
-  float *U, *GU, *theta, *resid;
-  const float *start;
-  unsigned long long seed, stream_id;
-  float *part;              // [nrb][ESMAX][2]
-  float *gpart;             // [ngroups][ESMAX][2]
-  int *cnt;                 // [ngroups + 1] tickets, zero between launches
-  float *R[2];              // [SMAX*SMAX] upper factors, row-major, ping-pong slots
-  float *dsc[2];            // [SMAX] column scaling
-  float *V;                 // [SMAX*SMAX] Ritz vectors of H, descending
-  float *mu;                // [1]
-  float *colss;             // [nrb][SMAX]
-};
-
-struct EigBatch {
-  EigDev p[kMaxProb];
-};
-
-struct StepArgs {
-  int mode, src, dst, dst2, tslot, t_identity, want_s;
-  float shift, mu_scale;
-};
 
 // packed upper triangle, column-major: e = j(j+1)/2 + i, i <= j
 HT_DEV void tri_index(int e, int &i, int &j) {
@@ -80,68 +51,6 @@ HT_DEV void tri_index(int e, int &i, int &j) {
   i = e - jj * (jj + 1) / 2;
 }
 
-// fill = 0: only reset the bookkeeping (tickets), for in-place CholeskyQR.
-__global__ void eig_init_kernel(const EigBatch probs, int fill) {
-  const EigDev &P = probs.p[blockIdx.y];
-  const long long total = fill ? static_cast<long long>(P.n) * P.s : 0;
-  // direct problems start the Rayleigh-Ritz step from Q = I in buffer 2
-  float *dst = P.direct ? P.buf[2] : P.buf[0];
-  for (long long idx = blockIdx.x * 256ll + threadIdx.x; idx < total; idx += gridDim.x * 256ll) {
-    float v;
-    if (P.direct) v = (idx % P.n == idx / P.n) ? 1.f : 0.f;
-    else if (P.start) v = P.start[idx];
-    else v = gaussian(P.seed, P.stream_id, static_cast<unsigned long long>(idx));
-    dst[idx] = v;
-  }
-  if (blockIdx.x == 0) {
-    __shared__ float red[256];
-    float t = 0.f;
-    for (int i = threadIdx.x; i < P.n; i += 256) t += P.G ? P.G[i + static_cast<long long>(P.n) * i] : 0.f;
-    red[threadIdx.x] = t;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) P.mu[0] = 1e-9f * fmaxf(red[0], 0.f);
-    for (int i = threadIdx.x; i <= P.ngroups; i += 256) P.cnt[i] = 0;
-  }
-}
-
-// Forward substitution of one row (one half-warp): x <- (x .* dsc) R^-1 with R
-// upper triangular (row-major, stride SMAX) in shared memory.  Lane l owns
-// columns l, l+16, l+32, l+48.
-HT_DEV void apply_factor_row(float *row, const float *Rs, const float *ds, int s, int l, unsigned mask) {
-  float tv[4], q[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    const int j = l + 16 * c;
-    tv[c] = j < s ? row[j] * ds[j] : 0.f;
-  }
-  for (int j = 0; j < s; ++j) {
-    const int owner = j & 15, cj = j >> 4;
-    float qj = 0.f;
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-      if (l == owner && c == cj) {
-        qj = tv[c] / Rs[j * SMAX + j];
-        q[c] = qj;
-      }
-    qj = __shfl_sync(mask, qj, owner, 16);
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const int k = l + 16 * c;
-      if (k > j && k < s) tv[c] = fmaf(-qj, Rs[j * SMAX + k], tv[c]);
-    }
-  }
-  __syncwarp(mask);
-#pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    const int j = l + 16 * c;
-    if (j < s) row[j] = q[c];
-  }
-}
-
 // 16-byte asynchronous global->shared copy; src_bytes < 16 zero-fills the rest.
 HT_DEV void cp_async16(void *smem_dst, const void *gsrc, int src_bytes) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(smem_dst)), "l"(gsrc), "r"(src_bytes)
@@ -150,146 +59,6 @@ HT_DEV void cp_async16(void *smem_dst, const void *gsrc, int src_bytes) {
 HT_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 HT_DEV void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
-constexpr int KC = 64;       // k chunk of the G * src product
-constexpr int NSTAGE = 3;    // cp.async pipeline depth
-constexpr int LDK = KC + 4;  // padded row length (keeps float4 alignment)
-
-// Z[i][j] (16 x s, in Zs) = sum_k G[r0+i, k] src[k, j], G symmetric so row
-// r0+i of G is read as column r0+i (contiguous).  Thread t owns rows
-// 4*(t>>6)..+3 of column t&63.  Chunks of KC rows of src stream through a
-// NSTAGE-deep cp.async ring.  Requires n % 4 == 0 and 16-byte aligned bases.
-HT_DEV void gsrc_product_async(const float *G, const float *src, int n, int s, int r0, int rows, float *ring,
-                               float (&acc)[4]) {
-  const int t = threadIdx.x;
-  const int nchunks = (n + KC - 1) / KC;
-  auto issue = [&](int c) {
-    const int kc = c * KC;
-    float *Gd = ring + (c % NSTAGE) * (RB + SMAX) * LDK, *Sd_ = Gd + RB * LDK;
-    // G: RB rows x KC/4 float4 = 256 copies
-    {
-      const int i = t >> 4, k4 = (t & 15) * 4;
-      const int kk = kc + k4;
-      const int bytes = (i < rows && kk < n) ? 4 * min(4, n - kk) : 0;
-      const float *g = G + (bytes ? (static_cast<long long>(kk) + static_cast<long long>(n) * (r0 + i)) : 0);
-      cp_async16(Gd + i * LDK + k4, g, bytes);
-    }
-    // src: SMAX columns x KC/4 float4 = 1024 copies, 4 per thread
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int idx = t + 256 * q;
-      const int j = idx >> 4, k4 = (idx & 15) * 4;
-      const int kk = kc + k4;
-      const int bytes = (j < s && kk < n) ? 4 * min(4, n - kk) : 0;
-      const float *g = src + (bytes ? (static_cast<long long>(kk) + static_cast<long long>(n) * j) : 0);
-      cp_async16(Sd_ + j * LDK + k4, g, bytes);
-    }
-  };
-  for (int c = 0; c < NSTAGE - 1; ++c) {
-    if (c < nchunks) issue(c);
-    cp_async_commit();
-  }
-  const int ig = t >> 6, j = t & 63;
-#pragma unroll
-  for (int c4 = 0; c4 < 4; ++c4) acc[c4] = 0.f;
-  for (int c = 0; c < nchunks; ++c) {
-    if (c + NSTAGE - 1 < nchunks) issue(c + NSTAGE - 1);
-    cp_async_commit();
-    cp_async_wait<NSTAGE - 1>();   // chunk c has landed
-    __syncthreads();
-    const float *Gd = ring + (c % NSTAGE) * (RB + SMAX) * LDK, *Sd_ = Gd + RB * LDK;
-#pragma unroll 4
-    for (int kk = 0; kk < KC; kk += 4) {
-      const float4 q = *reinterpret_cast<const float4 *>(Sd_ + j * LDK + kk);
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const float4 g = *reinterpret_cast<const float4 *>(Gd + (4 * ig + r) * LDK + kk);
-        acc[r] = fmaf(g.x, q.x, fmaf(g.y, q.y, fmaf(g.z, q.z, fmaf(g.w, q.w, acc[r]))));
-      }
-    }
-    __syncthreads();   // the stage is refilled NSTAGE-1 chunks later
-  }
-  cp_async_wait<0>();
-}
-
-// Last-block bookkeeping: returns true in exactly one CTA of the group /
-// of the whole problem once every member has published its partial.
-HT_DEV bool arrive(int *counter, int members, int *s_flag) {
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const int tk = atomicAdd(counter, 1);
-    const int last = (tk == members - 1) ? 1 : 0;
-    if (last) *counter = 0;   // every member has arrived: reset for the next launch
-    *s_flag = last;
-  }
-  __syncthreads();
-  const bool last = *s_flag != 0;
-  if (last) __threadfence();
-  return last;
-}
-
-// acc += sum of the (hi, lo) pairs of entry e in partials [first, first+count),
-// in order; loads are issued GROUP at a time so their latencies overlap.
-HT_DEV void sum_pairs(Acc2 &acc, const float *base, int first, int count, int e) {
-  for (int r0 = 0; r0 < count; r0 += GROUP) {
-    float hi[GROUP], lo[GROUP];
-#pragma unroll
-    for (int q = 0; q < GROUP; ++q) {
-      if (r0 + q < count) {
-        const float *p = base + (static_cast<long long>(first + r0 + q) * ESMAX + e) * 2;
-        hi[q] = __ldcg(p);
-        lo[q] = __ldcg(p + 1);
-      } else {
-        hi[q] = 0.f;
-        lo[q] = 0.f;
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < GROUP; ++q) acc2_add(acc, hi[q], lo[q]);
-  }
-}
-
-// Scaled, shifted Cholesky of the packed s x s matrix Sd (double): the upper
-// factor R (row-major, stride SMAX) in A and the scaling in dsc_sm, copied to
-// global memory when Rout is not null.
-HT_DEV void factor_and_store(const double *Sd, int s, float shift, float *A, float *dsc_sm, float *Rout, float *dout) {
-  const int t = threadIdx.x;
-  for (int j = t; j < s; j += kThreads) {
-    const double d = Sd[j * (j + 1) / 2 + j];
-    dsc_sm[j] = d > 1e-300 ? static_cast<float>(1.0 / sqrt(d)) : 0.f;
-  }
-  __syncthreads();
-  const int E = s * (s + 1) / 2;
-  for (int e = t; e < E; e += kThreads) {
-    int i, j;
-    tri_index(e, i, j);
-    float v = static_cast<float>(Sd[e] * static_cast<double>(dsc_sm[i]) * static_cast<double>(dsc_sm[j]));
-    if (i == j) v = (dsc_sm[j] > 0.f ? 1.f : 0.f) + shift;
-    A[i * SMAX + j] = v;
-  }
-  __syncthreads();
-  // right-looking Cholesky A = R^T R on the upper triangle; step j updates rows
-  // > j from the unscaled row j, then scales row j (never touched again)
-  const int warp = t >> 5, lane = t & 31;
-  for (int j = 0; j < s; ++j) {
-    const float d = sqrtf(fmaxf(A[j * SMAX + j], 1e-30f));
-    const float inv = 1.f / d;
-    for (int i = j + 1 + warp; i < s; i += kThreads / 32) {
-      const float rji = A[j * SMAX + i] * inv;
-      for (int k = i + lane; k < s; k += 32) A[i * SMAX + k] = fmaf(-rji, A[j * SMAX + k] * inv, A[i * SMAX + k]);
-    }
-    __syncthreads();
-    for (int k = j + t; k < s; k += kThreads) A[j * SMAX + k] = (k == j) ? d : A[j * SMAX + k] * inv;
-  }
-  __syncthreads();
-  if (!Rout) return;   // the caller keeps the factor in shared memory
-  for (int e = t; e < s * SMAX; e += kThreads) {
-    const int i = e / SMAX, k = e % SMAX;
-    Rout[e] = (k >= i && k < s) ? A[e] : 0.f;
-  }
-  for (int j = t; j < s; j += kThreads) dout[j] = dsc_sm[j];
-}
 
 // Cyclic Jacobi on a symmetric s x s matrix held in shared memory (s <= SMAX),
 // 256 threads, round-robin ("circle method") ordering: every round rotates up
@@ -505,175 +274,6 @@ HT_DEV void jacobi_smem(float (*A)[SMAX + 1], float (*A2)[SMAX + 1], float (*V)[
   __syncthreads();
 }
 
-// One step of the eigen-solver for every problem of the batch (see the file
-// comment).  ITER: dst = (G src + mu src) T; APPLY: dst = src T (in place
-// allowed); RR: dst = src T, dst2 = (G src) T and the Rayleigh quotient.
-__global__ void __launch_bounds__(kThreads) eig_step_kernel(const EigBatch probs, const StepArgs a) {
-  const EigDev &P = probs.p[blockIdx.y];
-  const int rb = blockIdx.x;
-  if (rb >= P.nrb) return;
-  if (P.direct && a.mode != STEP_RR) return;
-  extern __shared__ __align__(16) float sm[];
-  float *Rs = sm;                                   // SMAX*SMAX
-  float *ds = Rs + SMAX * SMAX;                     // SMAX
-  float *Zs = ds + SMAX;                            // RB*SMAX  (rows of the result)
-  float *Qr = Zs + RB * SMAX;                       // RB*SMAX  (RR: rows of Q)
-  float *Gs = Qr + RB * SMAX;                       // 64*(RB+1)   (scalar path)
-  float *Ss = Gs + 64 * (RB + 1);                   // ring of NSTAGE*(RB+SMAX)*LDK floats (async path),
-                                                    // or 64*68 (scalar path); 16-byte aligned
-  // the final reducer's scratch aliases the ring (dead once the product is done)
-  double *Sd = reinterpret_cast<double *>(Ss);              // ESMAX
-  float *Vs = reinterpret_cast<float *>(Sd + ESMAX);        // SMAX*(SMAX+1) (RR Jacobi)
-  __shared__ int s_flag;
-  __shared__ int order[SMAX];
-  const int n = P.n, s = P.s, t = threadIdx.x;
-  const int r0 = rb * RB;
-  const int rows = min(RB, n - r0);
-  const float *src = P.buf[a.src];
-  const bool ident = a.t_identity || P.direct;
-
-  if (!ident) {
-    for (int e = t; e < SMAX * SMAX; e += kThreads) Rs[e] = P.R[a.tslot][e];
-    for (int j = t; j < SMAX; j += kThreads) ds[j] = P.dsc[a.tslot][j];
-  }
-  // rows of src owned by this CTA
-  for (int e = t; e < RB * SMAX; e += kThreads) {
-    const int i = e % RB, j = e / RB;
-    const float v = (i < rows && j < s) ? src[(r0 + i) + static_cast<long long>(n) * j] : 0.f;
-    if (a.mode == STEP_APPLY) Zs[i * SMAX + j] = v;
-    else Qr[i * SMAX + j] = v;
-  }
-  if (a.mode != STEP_APPLY) {
-    const float mu = (a.mode == STEP_ITER) ? P.mu[0] * a.mu_scale : 0.f;
-    const bool vec = (n % 4 == 0) && ((reinterpret_cast<uintptr_t>(P.G) | reinterpret_cast<uintptr_t>(src)) & 15u) == 0;
-    if (vec) {
-      float acc[4];
-      gsrc_product_async(P.G, src, n, s, r0, rows, Ss, acc);
-      const int ig = t >> 6, j = t & 63;
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const int i = 4 * ig + r;
-        Zs[i * SMAX + j] = (i < rows && j < s) ? acc[r] + mu * Qr[i * SMAX + j] : 0.f;
-      }
-    } else {
-      // Z = G[rows, :] src, scalar loads (unaligned shapes)
-      const int i = t >> 4, cg = t & 15;
-      float acc[4] = {0.f, 0.f, 0.f, 0.f};
-      for (int kc = 0; kc < n; kc += 64) {
-        __syncthreads();
-        for (int e = t; e < 64 * RB; e += kThreads) {
-          const int kk = e % 64, ii = e / 64;
-          Gs[kk * (RB + 1) + ii] =
-              (kc + kk < n && ii < rows) ? P.G[(kc + kk) + static_cast<long long>(n) * (r0 + ii)] : 0.f;
-        }
-        for (int e = t; e < 64 * SMAX; e += kThreads) {
-          const int kk = e % 64, jj = e / 64;
-          Ss[kk * 68 + jj] = (kc + kk < n && jj < s) ? src[(kc + kk) + static_cast<long long>(n) * jj] : 0.f;
-        }
-        __syncthreads();
-#pragma unroll 8
-        for (int kk = 0; kk < 64; ++kk) {
-          const float g = Gs[kk * (RB + 1) + i];
-          const float4 q4 = *reinterpret_cast<const float4 *>(&Ss[kk * 68 + 4 * cg]);
-          acc[0] = fmaf(g, q4.x, acc[0]);
-          acc[1] = fmaf(g, q4.y, acc[1]);
-          acc[2] = fmaf(g, q4.z, acc[2]);
-          acc[3] = fmaf(g, q4.w, acc[3]);
-        }
-      }
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const int j = 4 * cg + c;
-        Zs[i * SMAX + j] = (i < rows && j < s) ? acc[c] + mu * Qr[i * SMAX + j] : 0.f;
-      }
-    }
-  }
-  __syncthreads();
-  // apply the previous factor: one half-warp per row
-  if (!ident) {
-    const int half = t >> 4, l = t & 15;
-    const unsigned mask = 0xFFFFu << (16 * (half & 1));
-    apply_factor_row(Zs + half * SMAX, Rs, ds, s, l, mask);
-    if (a.mode == STEP_RR) apply_factor_row(Qr + half * SMAX, Rs, ds, s, l, mask);
-  }
-  __syncthreads();
-  float *dst = P.buf[a.dst];
-  if (a.mode == STEP_RR) {
-    float *dst2 = P.buf[a.dst2];
-    for (int e = t; e < RB * SMAX; e += kThreads) {
-      const int i = e % RB, j = e / RB;
-      if (i < rows && j < s) {
-        dst[(r0 + i) + static_cast<long long>(n) * j] = Qr[i * SMAX + j];
-        dst2[(r0 + i) + static_cast<long long>(n) * j] = Zs[i * SMAX + j];
-      }
-    }
-  } else {
-    for (int e = t; e < RB * SMAX; e += kThreads) {
-      const int i = e % RB, j = e / RB;
-      if (i < rows && j < s) dst[(r0 + i) + static_cast<long long>(n) * j] = Zs[i * SMAX + j];
-    }
-  }
-  if (!a.want_s) return;
-  // partial of the s x s Gram (ITER/APPLY: Y^T Y, RR: Q^T Y), packed upper triangle
-  const int E = s * (s + 1) / 2;
-  const float *L = (a.mode == STEP_RR) ? Qr : Zs;
-  {
-    const int j = t & 63, ib = t >> 6;   // column j, rows ib, ib+4, ... <= j
-    if (j < s) {
-      float zc[RB];
-#pragma unroll
-      for (int r = 0; r < RB; ++r) zc[r] = Zs[r * SMAX + j];
-      for (int i = ib; i <= j; i += 4) {
-        Acc2 acc = {0.f, 0.f};
-#pragma unroll
-        for (int r = 0; r < RB; ++r) acc2_add_prod(acc, L[r * SMAX + i], zc[r]);   // rows >= `rows` are zero
-        float *d = P.part + (static_cast<long long>(rb) * ESMAX + j * (j + 1) / 2 + i) * 2;
-        d[0] = acc.s;
-        d[1] = acc.c;
-      }
-    }
-  }
-  // two-level deterministic reduction by the last CTAs to arrive
-  const int g = rb / GROUP;
-  const int gsize = min(GROUP, P.nrb - g * GROUP);
-  if (!arrive(&P.cnt[g], gsize, &s_flag)) return;
-  for (int e = t; e < E; e += kThreads) {
-    Acc2 acc = {0.f, 0.f};
-    sum_pairs(acc, P.part, g * GROUP, gsize, e);
-    float *d = P.gpart + (static_cast<long long>(g) * ESMAX + e) * 2;
-    d[0] = acc.s;
-    d[1] = acc.c;
-  }
-  if (!arrive(&P.cnt[P.ngroups], P.ngroups, &s_flag)) return;
-  for (int e = t; e < E; e += kThreads) {
-    Acc2 acc = {0.f, 0.f};
-    sum_pairs(acc, P.gpart, 0, P.ngroups, e);
-    Sd[e] = static_cast<double>(acc.s) + static_cast<double>(acc.c);
-  }
-  __syncthreads();
-  if (a.mode != STEP_RR) {
-    factor_and_store(Sd, s, a.shift, Rs, ds, P.R[a.tslot ^ 1], P.dsc[a.tslot ^ 1]);
-    return;
-  }
-  // Rayleigh-Ritz: Jacobi on H (symmetrised from the upper triangle)
-  float (*A)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(Rs);
-  float (*VV)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(Vs);
-  float (*AA2)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(Vs + SMAX * (SMAX + 1));
-  for (int e = t; e < SMAX * SMAX; e += kThreads) {
-    const int i = e % SMAX, j = e / SMAX;
-    float v = 0.f;
-    if (i < s && j < s) v = static_cast<float>(i <= j ? Sd[j * (j + 1) / 2 + i] : Sd[i * (i + 1) / 2 + j]);
-    A[i][j] = v;
-  }
-  __syncthreads();
-  jacobi_smem(A, AA2, VV, s, order);
-  for (int e = t; e < s * s; e += kThreads) {
-    const int i = e % s, r = e / s;
-    P.V[i + s * r] = VV[i][order[r]];
-  }
-  for (int r = t; r < P.K; r += kThreads) P.theta[r] = A[order[r]][order[r]];
-}
-
 // Transfer-tensor step of the complementary-leaf construction.  WG = W^T G_c W
 // (kw x kw, leading dimension kw) for the complementary leaf's Ritz block W;
 // V = W[:, :kt].  With GV = V^T G_c V = P diag(lam) P^T:
@@ -760,15 +360,27 @@ __global__ void __launch_bounds__(256) svd_from_gram_kernel(const float *GW, int
     const int i = e % s, r = e / s;
     M2[i + s * r] = V[i][order[r]] * inv[r];
   }
+  // Broot = M1^T (GW_sym V[:, order[:k2]]) diag(inv): the symmetrised Gram in
+  // the Jacobi scratch, the product P = GW_sym V_k2 in A (its diagonal is read
+  // above), both in shared memory
+  for (int e = t; e < s * s; e += 256) {
+    const int a = e % s, c = e / s;
+    A2[a][c] = 0.5f * (GW[a + s * c] + GW[c + s * a]);
+  }
+  __syncthreads();
+  for (int e = t; e < s * k2; e += 256) {
+    const int a = e % s, j = e / s;
+    const int oj = order[j];
+    float g = 0.f;
+    for (int c = 0; c < s; ++c) g = fmaf(A2[a][c], V[c][oj], g);
+    A[a][j] = g;
+  }
+  __syncthreads();
   for (int e = t; e < k1 * k2; e += 256) {
     const int i = e % k1, j = e / k1;
-    const int oi = order[i], oj = order[j];
+    const int oi = order[i];
     float acc = 0.f;
-    for (int a = 0; a < s; ++a) {
-      float g = 0.f;
-      for (int c = 0; c < s; ++c) g = fmaf(0.5f * (GW[a + s * c] + GW[c + s * a]), V[c][oj], g);
-      acc = fmaf(V[a][oi], g, acc);
-    }
+    for (int a = 0; a < s; ++a) acc = fmaf(V[a][oi], A[a][j], acc);
     Broot[i + k1 * j] = acc * inv[j];
   }
 }
@@ -804,7 +416,7 @@ struct CoopProb {
 
 struct CoopBatch {
   CoopProb p[kMaxProb];
-  int nprob, iters, refine, nsync, ent_total;
+  int nprob, iters, refine, orth_passes, nsync, ent_total;
   int ent_off[kMaxProb + 1];
   int direct_idx[kMaxProb];               // problem index of direct CTA d (blockIdx.x - nsync)
   unsigned *bar;                          // [2]: arrivals, generation (zero at launch)
@@ -1400,6 +1012,26 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
   const int cl = blockIdx.x - P.cta0;
   const unsigned members = static_cast<unsigned>(B.nsync);
 
+  if (B.orth_passes > 0) {
+    // In-place shifted CholeskyQR of buffer 0 (problems without a Gram): each
+    // pass applies the previous transform to the CTA's rows and accumulates
+    // their Gram partial, all CTAs reduce, every CTA factors (float pairs).
+    // The first pass is shifted by 1e-6 of the unit diagonal so that it cannot
+    // break down; the later ones clean up the orthogonality.
+    float *Q = P.buf[0];
+    double *A64 = Sd + ESMAX;
+    for (int pass = 0; pass <= B.orth_passes; ++pass) {
+      coop_step(P, cl, 1, Q, Q, nullptr, pass == 0, 0.f, Rs, Zs, Qr, ring);   // row-local: in place
+      if (pass == B.orth_passes) break;
+      if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
+      coop_reduce(B);
+      if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
+      coop_load_S(P, Sd);
+      factor_transform(Sd, P.s, pass == 0 ? 1e-6 : 0.0, A64, piv64, reinterpret_cast<float *>(A64 + SMAX * SMAX), Rs);
+    }
+    return;
+  }
+
   // mu = 1e-9 trace(G), computed identically by every CTA of the problem
   {
     float tr = 0.f;
@@ -1515,12 +1147,6 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 constexpr size_t kJacScratch = sizeof(float) * SMAX * (SMAX + 1);   // dynamic smem of the one-CTA Jacobi kernels
 
-constexpr size_t kRingFloats = NSTAGE * (RB + SMAX) * LDK;
-constexpr size_t kReducerFloats = 2 * ESMAX + 2 * SMAX * (SMAX + 1);
-constexpr size_t kStepSmem = sizeof(float) * (SMAX * SMAX + SMAX + 2 * RB * SMAX + 64 * (RB + 1) +
-                                              (kRingFloats > kReducerFloats ? kRingFloats : kReducerFloats)) +
-                             64;
-
 }  // namespace
 
 namespace {
@@ -1535,72 +1161,9 @@ size_t coop_workspace_bytes(const EigProblem *probs, int nprob) {
   }
   return b;
 }
-size_t step_workspace_bytes(const EigProblem *probs, int nprob);
 }  // namespace
 
-size_t eig_workspace_bytes(const EigProblem *probs, int nprob) {
-  const size_t a = coop_workspace_bytes(probs, nprob), b = step_workspace_bytes(probs, nprob);
-  return a > b ? a : b;
-}
-
-namespace {
-size_t step_workspace_bytes(const EigProblem *probs, int nprob) {
-  size_t b = 0;
-  for (int i = 0; i < nprob; ++i) {
-    const int nrb = (probs[i].n + RB - 1) / RB;
-    const int ng = (nrb + GROUP - 1) / GROUP;
-    b += 4 * align256(sizeof(float) * static_cast<size_t>(probs[i].n) * SMAX);
-    b += align256(sizeof(float) * nrb * ESMAX * 2);
-    b += align256(sizeof(float) * ng * ESMAX * 2);
-    b += align256(sizeof(int) * (ng + 1));
-    b += 2 * align256(sizeof(float) * SMAX * SMAX) + 2 * align256(sizeof(float) * SMAX);
-    b += align256(sizeof(float) * SMAX * SMAX);
-    b += align256(sizeof(float) * 4);
-    b += align256(sizeof(float) * nrb * SMAX);
-  }
-  return b;
-}
-}  // namespace
-
-static cudaError_t build_batch(const EigProblem *probs, int nprob, void *ws, size_t ws_bytes, EigBatch &b,
-                               int &max_nrb) {
-  if (nprob > kMaxProb) return cudaErrorInvalidValue;
-  if (eig_workspace_bytes(probs, nprob) > ws_bytes) return cudaErrorInvalidValue;
-  char *p = static_cast<char *>(ws);
-  max_nrb = 0;
-  for (int i = 0; i < nprob; ++i) {
-    const EigProblem &q = probs[i];
-    if (q.s > SMAX || q.s < 1 || q.K > q.s || q.s > q.n) return cudaErrorInvalidValue;
-    EigDev &d = b.p[i];
-    d.G = q.G; d.n = q.n; d.s = q.s; d.K = q.K;
-    d.nrb = (q.n + RB - 1) / RB;
-    d.ngroups = (d.nrb + GROUP - 1) / GROUP;
-    d.direct = (q.G != nullptr && q.s == q.n) ? 1 : 0;
-    max_nrb = d.nrb > max_nrb ? d.nrb : max_nrb;
-    d.U = q.U; d.GU = q.GU; d.theta = q.theta; d.resid = q.resid;
-    d.start = q.start; d.seed = q.seed; d.stream_id = q.stream_id;
-    for (int k = 0; k < 4; ++k) {
-      d.buf[k] = reinterpret_cast<float *>(p);
-      p += align256(sizeof(float) * static_cast<size_t>(q.n) * SMAX);
-    }
-    d.part = reinterpret_cast<float *>(p); p += align256(sizeof(float) * d.nrb * ESMAX * 2);
-    d.gpart = reinterpret_cast<float *>(p); p += align256(sizeof(float) * d.ngroups * ESMAX * 2);
-    d.cnt = reinterpret_cast<int *>(p); p += align256(sizeof(int) * (d.ngroups + 1));
-    for (int k = 0; k < 2; ++k) {
-      d.R[k] = reinterpret_cast<float *>(p); p += align256(sizeof(float) * SMAX * SMAX);
-      d.dsc[k] = reinterpret_cast<float *>(p); p += align256(sizeof(float) * SMAX);
-    }
-    d.V = reinterpret_cast<float *>(p); p += align256(sizeof(float) * SMAX * SMAX);
-    d.mu = reinterpret_cast<float *>(p); p += align256(sizeof(float) * 4);
-    d.colss = reinterpret_cast<float *>(p); p += align256(sizeof(float) * d.nrb * SMAX);
-  }
-  return cudaSuccess;
-}
-
-static cudaError_t launch_step(const EigBatch &b, int nprob, int max_nrb, StepArgs a, cudaStream_t st) {
-  eig_step_kernel<<<dim3(max_nrb, nprob), kThreads, kStepSmem, st>>>(b, a);
-  return cudaGetLastError();
-}
+size_t eig_workspace_bytes(const EigProblem *probs, int nprob) { return coop_workspace_bytes(probs, nprob); }
 
 // Resources of the cooperative solver on the current device (cached).
 static int coop_max_ctas() {
@@ -1621,10 +1184,7 @@ static int coop_max_ctas() {
 
 cudaError_t eig_prepare() {
   if (coop_max_ctas() <= 0) return cudaErrorInvalidConfiguration;
-  cudaError_t e = cudaFuncSetAttribute(eig_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(kStepSmem));
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(transfer_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(transfer_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            static_cast<int>(kJacScratch));
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(svd_from_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1716,33 +1276,75 @@ cudaError_t eig_batched(EigProblem *probs, int nprob, int iters, void *ws, size_
   return cudaSuccess;
 }
 
-// In-place CholeskyQR3 of tall blocks (G == nullptr problems, buffer 0 = the matrix).
-cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, size_t ws_bytes, cudaStream_t st,
+// In-place CholeskyQR (`passes` factorisations, the first shifted) of tall
+// blocks: G == nullptr problems, Q = the matrix.  One cooperative launch of the
+// eigen-solver's kernel in its CholeskyQR mode.
+cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, size_t ws_bytes, int *err, cudaStream_t st,
                            int *launches) {
   if (nprob <= 0) return cudaSuccess;
-  EigBatch b;
-  int max_nrb = 0;
-  cudaError_t e = build_batch(probs, nprob, ws, ws_bytes, b, max_nrb);
+  if (nprob > kMaxProb || passes < 1) return cudaErrorInvalidValue;
+  if (coop_workspace_bytes(probs, nprob) > ws_bytes) return cudaErrorInvalidValue;
+  const int budget = coop_max_ctas();
+  if (budget < nprob) return cudaErrorInvalidConfiguration;
+  CoopBatch B;
+  std::memset(&B, 0, sizeof(B));
+  char *p = static_cast<char *>(ws);
+  B.bar = reinterpret_cast<unsigned *>(p);
+  p += align256(4 * sizeof(unsigned));
+  B.err = err;
+  B.nprob = nprob;
+  B.orth_passes = passes;
+  long long n_all = 0;
+  for (int i = 0; i < nprob; ++i) {
+    const EigProblem &q = probs[i];
+    if (q.G || !q.Q || q.s > SMAX || q.s < 1 || q.s > q.n) return cudaErrorInvalidValue;
+    n_all += q.n;
+  }
+  int cta = 0, ent = 0;
+  for (int i = 0; i < nprob; ++i) {
+    const EigProblem &q = probs[i];
+    CoopProb &c = B.p[i];
+    c.G = nullptr; c.n = q.n; c.s = q.s; c.K = q.s;
+    for (int k = 0; k < 4; ++k) {
+      c.buf[k] = reinterpret_cast<float *>(p);
+      p += align256(sizeof(float) * static_cast<size_t>(q.n) * SMAX);
+    }
+    c.buf[0] = q.Q;   // operate on the caller's matrix in place
+    c.part = reinterpret_cast<float *>(p); p += align256(sizeof(float) * kCoopMaxCta * ESMAX * 2);
+    c.S = reinterpret_cast<double *>(p); p += align256(sizeof(double) * ESMAX);
+    c.V = reinterpret_cast<float *>(p); p += align256(sizeof(float) * SMAX * SMAX);
+    c.colss = reinterpret_cast<float *>(p); p += align256(sizeof(float) * kCoopMaxCta * SMAX);
+    B.ent_off[i] = ent;
+    int nc = static_cast<int>(static_cast<long long>(budget) * q.n / n_all);
+    nc = nc < 1 ? 1 : nc;
+    const int rows = (q.n + nc - 1) / nc;
+    c.rows = rows;
+    c.ncta = (q.n + rows - 1) / rows;
+    c.cta0 = cta;
+    cta += c.ncta;
+    ent += q.s * (q.s + 1) / 2;
+  }
+  B.ent_off[nprob] = ent;
+  B.ent_total = ent;
+  B.nsync = cta;
+  if (cta > budget) return cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaMemsetAsync(B.bar, 0, 4 * sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
-  for (int i = 0; i < nprob; ++i) b.p[i].buf[0] = probs[i].Q;   // operate on the caller's matrix in place
-  static bool attr_set = false;
-  if (!attr_set) {
-    e = cudaFuncSetAttribute(eig_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kStepSmem));
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
-  int nl = 0;
-  eig_init_kernel<<<dim3(1, nprob), 256, 0, st>>>(b, 0);   // zeroes the tickets only
-  ++nl;
-  int tslot = 0;
-  for (int pass = 0; pass <= passes; ++pass) {
-    StepArgs a{STEP_APPLY, 0, 0, 0, tslot, pass == 0 ? 1 : 0, pass < passes ? 1 : 0, pass == 0 ? 1e-6f : 0.f, 0.f};
-    if ((e = launch_step(b, nprob, max_nrb, a, st)) != cudaSuccess) return e;
-    ++nl;
-    if (pass < passes) tslot ^= 1;
-  }
-  if (launches) *launches += nl;
-  return cudaGetLastError();
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(cta);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = kCoopSmem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, eig_coop_kernel, B);
+  if (e != cudaSuccess) return e;
+  if (launches) *launches += 1;
+  return cudaSuccess;
 }
 
 cudaError_t svd_from_gram_launch(const float *GW, int s, int k1, int k2, float *M1, float *M2, float *Broot,

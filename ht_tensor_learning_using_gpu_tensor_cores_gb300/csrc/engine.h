@@ -169,8 +169,9 @@ cudaError_t eig_prepare();
 cudaError_t eig_batched(EigProblem *probs, int nprob, int iters, void *ws, size_t ws_bytes, int *err,
                         cudaStream_t s, int *launches, int max_ctas = 0, int refine = 0);
 // Orthonormalise the columns of tall matrices in place (CholeskyQR, `passes`
-// times; the first pass shifted).  Uses the eigen-solver's workspace layout.
-cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, size_t ws_bytes, cudaStream_t s,
+// times; the first pass shifted).  Uses the eigen-solver's workspace layout;
+// a wait that runs out sets bits in *err.
+cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, size_t ws_bytes, int *err, cudaStream_t s,
                            int *launches);
 // Transfer-tensor eigen step (see eig.cu).  WG: kw x kw.  M: kt x kt, Bkt: kt x kc.
 cudaError_t transfer_eig_launch(const float *WG, int kw, int kt, int kc, int t_is_left, float *M, float *Broot,
