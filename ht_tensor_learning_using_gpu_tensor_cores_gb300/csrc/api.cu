@@ -725,7 +725,7 @@ ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const 
     EigProblem e;
     e.G = nullptr; e.n = static_cast<int>(rows); e.s = s; e.K = s; e.Q = Qm; e.Y = nullptr;
     e.U = e.GU = e.theta = e.resid = nullptr; e.start = nullptr; e.seed = 0; e.stream_id = 0;
-    HT_CUDA(cholqr_batched(&e, 1, 3, cws, cbytes, c.err, c.st, &c.launches));
+    HT_CUDA(cholqr_batched(&e, 1, 2, cws, cbytes, c.err, c.st, &c.launches));
     return HT_OK;
   };
   auto to16 = [&](const float *src, long long count) -> const __nv_bfloat16 * {

@@ -1013,11 +1013,13 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
   const unsigned members = static_cast<unsigned>(B.nsync);
 
   if (B.orth_passes > 0) {
-    // In-place shifted CholeskyQR of buffer 0 (problems without a Gram): each
-    // pass applies the previous transform to the CTA's rows and accumulates
-    // their Gram partial, all CTAs reduce, every CTA factors (float pairs).
-    // The first pass is shifted by 1e-6 of the unit diagonal so that it cannot
-    // break down; the later ones clean up the orthogonality.
+    // In-place CholeskyQR of buffer 0 (problems without a Gram): each pass
+    // applies the previous transform to the CTA's rows and accumulates their
+    // Gram partial, all CTAs reduce, every CTA factors (float pairs, pivots
+    // floored, so it cannot break down; the first pass shifted by 1e-12 of the
+    // unit diagonal, as the eigen-solver's iterations).  The Gram and the
+    // factor carry ~48 bits, so after one pass only the FP32 rounding of the
+    // applied transform remains (~u * cond(Y)); a second pass removes it.
     float *Q = P.buf[0];
     double *A64 = Sd + ESMAX;
     for (int pass = 0; pass <= B.orth_passes; ++pass) {
@@ -1027,7 +1029,7 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
       coop_reduce(B);
       if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
       coop_load_S(P, Sd);
-      factor_transform(Sd, P.s, pass == 0 ? 1e-6 : 0.0, A64, piv64, reinterpret_cast<float *>(A64 + SMAX * SMAX), Rs);
+      factor_transform(Sd, P.s, pass == 0 ? 1e-12 : 0.0, A64, piv64, reinterpret_cast<float *>(A64 + SMAX * SMAX), Rs);
     }
     return;
   }
