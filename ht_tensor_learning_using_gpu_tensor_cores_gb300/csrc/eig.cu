@@ -872,7 +872,7 @@ HT_DEV void coop_load_S(const CoopProb &P, double *Sd) {
 // G * src + mu src), apply the current transform Rs (unless identity), store to dst,
 // accumulate the Gram partial.  mode 0: ITER, 1: APPLY, 2: RR (also Q rows).
 HT_DEV void coop_step(const CoopProb &P, int cl, int mode, const float *src, float *dst, float *dst2, bool ident,
-                      float mu, const float *Rs, float *Zs, float *Qr, float *ring) {
+                      float mu, const float *Rs, float *Zs, float *Qr, float *ring, bool want_s = true) {
   Acc2 acc[kMaxEntPerThread];
 #pragma unroll
   for (int q = 0; q < kMaxEntPerThread; ++q) acc[q] = Acc2{0.f, 0.f};
@@ -899,11 +899,11 @@ HT_DEV void coop_step(const CoopProb &P, int cl, int mode, const float *src, flo
       coop_gram_partial(Qr, Zs, P.s, acc);
     } else {
       coop_store_rows(Zs, P.n, P.s, r0, rows, dst);
-      coop_gram_partial(Zs, Zs, P.s, acc);
+      if (want_s) coop_gram_partial(Zs, Zs, P.s, acc);
     }
     __syncthreads();
   }
-  coop_gram_store(acc, P.s, P.part + static_cast<long long>(cl) * ESMAX * 2);
+  if (want_s) coop_gram_store(acc, P.s, P.part + static_cast<long long>(cl) * ESMAX * 2);
 }
 
 // U = Q V[:, :K], GU = Y V[:, :K] on the CTA's rows, column sums of squares of
@@ -1023,7 +1023,8 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
     float *Q = P.buf[0];
     double *A64 = Sd + ESMAX;
     for (int pass = 0; pass <= B.orth_passes; ++pass) {
-      coop_step(P, cl, 1, Q, Q, nullptr, pass == 0, 0.f, Rs, Zs, Qr, ring);   // row-local: in place
+      // row-local: in place; the last pass only applies the transform
+      coop_step(P, cl, 1, Q, Q, nullptr, pass == 0, 0.f, Rs, Zs, Qr, ring, pass < B.orth_passes);
       if (pass == B.orth_passes) break;
       if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
       coop_reduce(B);
@@ -1082,7 +1083,7 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
   // Y_L loses digits to cancellation.
   // The FP32 path asks for `refine` CholeskyQR passes on Q_L all the same
   // (orthonormal to FP32 rounding, the last digit of its error).
-  coop_step(P, cl, 1, P.buf[cur], P.buf[2], nullptr, ident, 0.f, Rs, Zs, Qr, ring);
+  coop_step(P, cl, 1, P.buf[cur], P.buf[2], nullptr, ident, 0.f, Rs, Zs, Qr, ring, ident || B.refine > 0);
   bool rr_ident = true;
   if (ident || B.refine > 0) {   // ident: no iteration ran, orthonormalise the start block
     if (!reduce_and_factor(1e-12)) return;

@@ -235,35 +235,55 @@ __global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p, const T
   }
 }
 
-// Sum partial tiles [splits][num_tiles][128][bn] in a fixed order.
-__global__ void reduce_partials_kernel(const float *__restrict__ part, const TileGen gen, int num_tiles, int splits,
-                                       int bn, float *__restrict__ out, long long ld, int symmetric) {
+// Sum partial tiles [splits][num_tiles][128][bn] in a fixed order.  A block
+// is (256 / G) consecutive outputs x G split groups: thread (o, g) sums the
+// partials of group g in order (8 loads in flight), then the G group sums are
+// added in group order.  Splitting the split range keeps enough loads in
+// flight when there are few outputs and many splits (small Grams).
+__global__ void __launch_bounds__(256) reduce_partials_kernel(const float *__restrict__ part, const TileGen gen,
+                                                              int num_tiles, int splits, int bn, int groups,
+                                                              float *__restrict__ out, long long ld, int symmetric) {
+  __shared__ float red[256];
+  const int nout = 256 / groups;
+  const int o = threadIdx.x % nout, g = threadIdx.x / nout;
+  const int per = (splits + groups - 1) / groups;
+  const int k_begin = g * per, k_end = min(splits, k_begin + per);
   const long long per_tile = static_cast<long long>(gen.bm) * bn;
   const long long total = per_tile * num_tiles;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int t = static_cast<int>(idx / per_tile);
-    const int within = static_cast<int>(idx - t * per_tile);
-    const int row = within / bn, col = within % bn;
-    const Tile tl = gen_tile(gen, t);
-    if (row >= tl.valid_rows || col >= tl.valid_cols) continue;
+  for (long long base = static_cast<long long>(blockIdx.x) * nout; base < total;
+       base += static_cast<long long>(gridDim.x) * nout) {
+    const long long idx = base + o;
+    const bool live = idx < total;
+    const int t = live ? static_cast<int>(idx / per_tile) : 0;
+    const int within = live ? static_cast<int>(idx - t * per_tile) : 0;
     float s = 0.f;
-    for (int k0 = 0; k0 < splits; k0 += 8) {   // 8 loads in flight, summed in order
-      float v[8];
+    if (live) {
+      for (int k0 = k_begin; k0 < k_end; k0 += 8) {   // 8 loads in flight, summed in order
+        float v[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q)
-        v[q] = (k0 + q < splits) ? part[(static_cast<long long>(k0 + q) * num_tiles + t) * per_tile + within] : 0.f;
+        for (int q = 0; q < 8; ++q)
+          v[q] = (k0 + q < k_end) ? part[(static_cast<long long>(k0 + q) * num_tiles + t) * per_tile + within] : 0.f;
 #pragma unroll
-      for (int q = 0; q < 8; ++q) s += v[q];
+        for (int q = 0; q < 8; ++q) s += v[q];
+      }
     }
-    const long long gr = tl.out_row + row, gc = tl.out_col + col;
-    if (symmetric) {
-      if (gc < gr) continue;   // the mirror element is produced by the tile holding (gc, gr)
-      out[gr + ld * gc] = s;
-      out[gc + ld * gr] = s;
-    } else {
-      out[gr + ld * gc] = s;
+    red[threadIdx.x] = s;
+    __syncthreads();
+    if (g == 0 && live) {
+      for (int q = 1; q < groups; ++q) s += red[q * nout + o];
+      const int row = within / bn, col = within % bn;
+      const Tile tl = gen_tile(gen, t);
+      if (row < tl.valid_rows && col < tl.valid_cols) {
+        const long long gr = tl.out_row + row, gc = tl.out_col + col;
+        if (!symmetric) {
+          out[gr + ld * gc] = s;
+        } else if (gc >= gr) {   // the mirror element is produced by the tile holding (gc, gr)
+          out[gr + ld * gc] = s;
+          out[gc + ld * gr] = s;
+        }
+      }
     }
+    __syncthreads();
   }
 }
 
@@ -321,9 +341,13 @@ cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s) {
 cudaError_t reduce_partials_launch(const float *partial, const TileGen &gen, int splits, int bn, float *out,
                                    long long ld_out, int symmetric, cudaStream_t s) {
   const long long total = static_cast<long long>(gen.bm) * bn * gen.count;
-  int grid = static_cast<int>((total + 255) / 256);
-  if (grid > 152 * 16) grid = 152 * 16;
-  reduce_partials_kernel<<<grid, 256, 0, s>>>(partial, gen, gen.count, splits, bn, out, ld_out, symmetric);
+  // split groups: about 8 partials per thread, at most 8 groups
+  int groups = 1;
+  while (groups < 8 && splits > 8 * groups) groups *= 2;
+  const int nout = 256 / groups;
+  long long blocks = (total + nout - 1) / nout;
+  const int grid = static_cast<int>(blocks < 152 * 16 ? blocks : 152 * 16);
+  reduce_partials_kernel<<<grid, 256, 0, s>>>(partial, gen, gen.count, splits, bn, groups, out, ld_out, symmetric);
   return cudaGetLastError();
 }
 
