@@ -437,6 +437,17 @@ def run_ours(args, world, rank, local):
     from ht_tensor_learning_using_gpu_tensor_cores_gb300 import synth
 
     torch.cuda.set_device(local)
+    if args.fourth_order_only:
+        # profiling mode: only the 128^4 mixed-path decomposition (leaf ranks 24,
+        # interior 48, exact HT + 1e-4 noise), warm-up + timed steps, no other work
+        tree4 = ht.balanced_tree_4d([1, 48, 48, 24, 24, 24, 24])
+        X4 = synth.exact_ht_device((128,) * 4, tree4, 1e-4, seed=21, device="cuda")
+        for _ in range(args.warmup + args.steps):
+            ht.decompose(X4, tree4, precision="bf16")
+        torch.cuda.synchronize()
+        if rank == 0:
+            print(json.dumps({"fourth_order_only": True, "steps": args.steps, "warmup": args.warmup}), flush=True)
+        return
     n, k = args.n, RANK
     tree = ht.reference_tree_3d([1, k, k, k, k])
     X = synth.odeco(n, decay=DECAY, seed=1 + rank, assemble_on=torch.device("cuda", local))   # column-major memory
@@ -575,6 +586,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--mixed-only", action="store_true",
                     help="run only the headline mixed-path steps (for profiler launch lists)")
+    ap.add_argument("--fourth-order-only", action="store_true",
+                    help="run only the 128^4 mixed-path steps (for profiler launch lists)")
     args = ap.parse_args()
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
