@@ -16,6 +16,18 @@ constexpr uint64_t kWaitLimitNs = 2000000000ull;   // 2 s
 // Error bits written to the per-call device error word.
 enum : int { kErrTimeout = 1, kErrNonFinite = 2, kErrBreakdown = 4 };
 
+// Opt-in dynamic shared memory above 48 KB for `func`, once per device
+// (`done` holds 64 per-device flags owned by the caller).
+template <typename F>
+inline cudaError_t opt_in_smem(F *func, int bytes, bool *done) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (done[dev]) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) done[dev] = true;
+  return e;
+}
+
 HT_DEV uint32_t smem_u32(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
 
 HT_DEV uint64_t global_timer_ns() {

@@ -1353,13 +1353,9 @@ cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, s
 cudaError_t svd_from_gram_launch(const float *GW, int s, int k1, int k2, float *M1, float *M2, float *Broot,
                                  cudaStream_t st) {
   if (s > SMAX || k1 > s || k2 > s) return cudaErrorInvalidValue;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(svd_from_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(kJacScratch));
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  static bool attr_set[64] = {};
+  const cudaError_t e = opt_in_smem(svd_from_gram_kernel, static_cast<int>(kJacScratch), attr_set);
+  if (e != cudaSuccess) return e;
   svd_from_gram_kernel<<<1, 256, kJacScratch, st>>>(GW, s, k1, k2, M1, M2, Broot);
   return cudaGetLastError();
 }
@@ -1367,13 +1363,9 @@ cudaError_t svd_from_gram_launch(const float *GW, int s, int k1, int k2, float *
 cudaError_t transfer_eig_launch(const float *WG, int kw, int kt, int kc, int t_is_left, float *M, float *Broot,
                                 cudaStream_t st) {
   if (kt > SMAX || kc > kw || kt > kw) return cudaErrorInvalidValue;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(transfer_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(kJacScratch));
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  static bool attr_set[64] = {};
+  const cudaError_t e = opt_in_smem(transfer_eig_kernel, static_cast<int>(kJacScratch), attr_set);
+  if (e != cudaSuccess) return e;
   transfer_eig_kernel<<<1, 256, kJacScratch, st>>>(WG, kw, kt, kc, t_is_left, M, Broot);
   return cudaGetLastError();
 }

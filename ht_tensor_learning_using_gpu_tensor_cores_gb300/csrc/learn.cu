@@ -215,12 +215,11 @@ cudaError_t sketch_loss_grad(const float *G, const float *trG, int batch, int n,
   const dim3 grid((n + LT_ROWS - 1) / LT_ROWS, batch);
   ls_bgemm_kernel<<<grid, 256, 0, st>>>(G, S, 0, Y, n, s);                                   // Y = G S
   ls_bgemm_kernel<<<grid, 256, 0, st>>>(G, Y, static_cast<long long>(n) * s, P, n, s);       // P = G Y
-  static bool attr_set = false;
+  static bool attr_set[64] = {};
   constexpr int kSmallSmem = 2 * LS_MAX * LS_MAX * sizeof(double);
-  if (!attr_set) {
-    const cudaError_t e = cudaFuncSetAttribute(ls_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmallSmem);
+  {
+    const cudaError_t e = opt_in_smem(ls_small_kernel, kSmallSmem, attr_set);
     if (e != cudaSuccess) return e;
-    attr_set = true;
   }
   ls_small_kernel<<<batch, 256, kSmallSmem, st>>>(Y, P, trG, n, s, E, Ci, loss, bad);     // E, C^-1, loss
   ls_bgemm_kernel<<<grid, 256, 0, st>>>(G, E, static_cast<long long>(n) * s, GE, n, s);      // G E
