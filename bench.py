@@ -163,12 +163,13 @@ def cpu_baseline(sample_n=CPU_SAMPLE_N, reps=1):
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        pass
+    # warm-up: the same path on a small sample (imports, BLAS thread pools), untimed
+    for _ in range(max(0, args.warmup)):
+        cpu_baseline(min(64, args.cpu_sample), reps=1)
     vals = []
     cb = None
     for _ in range(max(1, args.steps)):
-        cb = cpu_baseline(CPU_SAMPLE_N, reps=1)
+        cb = cpu_baseline(args.cpu_sample, reps=1)
         vals.append(cb["value"])
     v = statistics.median(vals)
     cb["value"] = v
@@ -537,7 +538,7 @@ def run_ours(args, world, rank, local):
     tiles = -(-n // 256)
     issued = tiles * (tiles + 1) / 2 * 256.0 * 256.0 * 2.0 * float(n) ** 2   # per launch
     stage_med = {kk: statistics.median([s[kk] for s in stage_ms]) for kk in stage_ms[0]}
-    cpu = cpu_baseline(CPU_SAMPLE_N) if (rank == 0 and not args.no_cpu) else None
+    cpu = cpu_baseline(args.cpu_sample) if (rank == 0 and not args.no_cpu) else None
 
     if rank == 0:
         line = {
@@ -584,6 +585,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=N_FULL)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE_N,
+                    help="edge of the cubic sample the CPU path decomposes (its time is scaled by n^4 to 1024^3)")
     ap.add_argument("--mixed-only", action="store_true",
                     help="run only the headline mixed-path steps (for profiler launch lists)")
     ap.add_argument("--fourth-order-only", action="store_true",
