@@ -253,15 +253,29 @@ def ht_layer_init(weight: np.ndarray, rank: int, N: Sequence[int], M: Sequence[i
     order; the reference takes torch.eig's unsorted first columns), node 1 from
     the SVD of the (a*b) x c unfolding, then the two ncon contractions."""
     a, b, c = N[0] * M[0], N[1] * M[1], N[2] * M[2]
-    X = np.asarray(weight, dtype=np.float64).reshape(a, b, c)
-    U3m = X.reshape(a, b * c)
-    U4m = X.transpose(1, 0, 2).reshape(b, a * c)
-    U2m = X.transpose(2, 0, 1).reshape(c, a * b)
-    U1m = X.reshape(a * b, c)
+    X, U3m, U4m, U2m, U1m = ht_layer_unfoldings(weight, N, M)
     leaf = lambda A: top_eigvecs(A @ A.T, rank)[1]
     U3, U4, U2 = leaf(U3m), leaf(U4m), leaf(U2m)
     U1 = np.linalg.svd(U1m, full_matrices=False)[0][:, :rank].reshape(a, b, rank)
+    B1, B0 = ht_layer_transfers(X, U1, U2, U3, U4)
+    return (U3.reshape(N[0], M[0], rank), U4.reshape(N[1], M[1], rank), U2.reshape(N[2], M[2], rank), B1, B0)
+
+
+def ht_layer_unfoldings(weight: np.ndarray, N: Sequence[int], M: Sequence[int]):
+    """The tensor view X (a, b, c) of the weight and its four unfoldings as the
+    reference's ``ht()`` forms them (mnist_ht.py:168-177): nodes 3 (a x bc),
+    4 (b x ac), 2 (c x ab) and 1 (ab x c), float64."""
+    a, b, c = N[0] * M[0], N[1] * M[1], N[2] * M[2]
+    X = np.asarray(weight, dtype=np.float64).reshape(a, b, c)
+    return X, X.reshape(a, b * c), X.transpose(1, 0, 2).reshape(b, a * c), X.transpose(2, 0, 1).reshape(c, a * b), \
+        X.reshape(a * b, c)
+
+
+def ht_layer_transfers(X: np.ndarray, U1: np.ndarray, U2: np.ndarray, U3: np.ndarray, U4: np.ndarray):
+    """The two ncon contractions of ``ht()`` (mnist_ht.py:195-196): B1 (r3, r4, r1)
+    from node 1's basis U1 (a, b, r1) and the leaves U3 (a, r3), U4 (b, r4); B0
+    (r1, r2) from X, U1 and U2 (c, r2)."""
     B1 = np.einsum("abk,ai,bj->ijk", U1, U3, U4)
     B0 = np.einsum("abc,abi,cj->ij", X, U1, U2)
-    return (U3.reshape(N[0], M[0], rank), U4.reshape(N[1], M[1], rank), U2.reshape(N[2], M[2], rank), B1, B0)
+    return B1, B0
 

@@ -10,7 +10,9 @@ The reference scripts
   third_order_tensor_decompsition/Python/HT_TensorNetwork.py
   fourth_order_tensor_decomposition/single_GPU/Python/HT_4d_TensorNetwork.py
 are executed unmodified except for the problem size line ``n=...`` (the
-shipped sizes, 160 / 560 / 120, give fixtures of many MB).  Their third-party
+shipped sizes, 160 / 560 / 120, give fixtures of many MB).  For the HT tensor
+layer (HT_tensor_layer/FC_MNIST/mnist_ht.py) the ``ht()`` function and the
+einsum chain of ``tNet.forward`` are executed as written (``make_ht_layer``).  Their third-party
 dependencies are not installed here, so this script supplies small stand-ins
 that restate the published semantics of the calls the scripts make:
 
@@ -184,6 +186,50 @@ def make_tensornetwork_4d(n, seed):
     return out
 
 
+def make_ht_layer(seed, N=(4, 4, 6), M=(4, 5, 4), rank=4, batch=5):
+    """The HT tensor layer of HT_tensor_layer/FC_MNIST/mnist_ht.py: its ``ht()``
+    initialisation (lines 167-197) run as written on a seeded weight, and the
+    einsum chain of ``tNet.forward`` (lines 233-240) on a seeded input, with the
+    gradients torch autograd gives that chain for a seeded output cotangent.  The
+    module's other lines (datasets, training loop, thop/torchvision imports) are
+    not executed; the reshape to the layer's (N0, N1, N2) input is restated for
+    these small sizes."""
+    rel = "HT_tensor_layer/FC_MNIST/mnist_ht.py"
+    src = open(os.path.join(REF, rel), encoding="utf-8").read()
+    i = src.index("def ht(data,rank,N,M):")
+    j = src.index("# ht tensor layer", i)
+    ns = {"torch": torch, "tn": sys.modules["tensornetwork"]}
+    exec(compile(src[i:j], rel, "exec"), ns)
+    k = src.index("def forward(self, x):", src.index("class tNet"))
+    body = src[k:src.index("x = x + self.b1", k) + len("x = x + self.b1")]
+    chain = [l.strip() for l in body.splitlines() if l.strip().startswith("x = torch.einsum(")]
+    assert len(chain) == 5, chain
+    torch.manual_seed(seed)
+    nin, nout = int(np.prod(N)), int(np.prod(M))
+    W = torch.randn(nout, nin) / np.sqrt(nin)
+    u1, u2, u3, b2, b1 = ns["ht"](W, rank, list(N), list(M))
+    x0 = torch.randn(batch, nin)
+    bias0 = torch.randn(*M)
+    dy = torch.randn(batch, nout)
+    params = [t.detach().clone().float().requires_grad_(True) for t in (u1, u2, u3, b2, b1, bias0, x0)]
+    self_ = types.SimpleNamespace(u1_1=params[0], u2_1=params[1], u3_1=params[2], b2_1=params[3], b1_1=params[4],
+                                  b1=params[5])
+    loc = {"torch": torch, "self": self_, "x": torch.reshape(params[6], (batch, *N))}
+    for line in chain:
+        exec(line, {}, loc)
+    exec("x = x + self.b1", {}, loc)
+    y = torch.reshape(loc["x"], (batch, nout))
+    y.backward(dy)
+    names = ["u1", "u2", "u3", "b2", "b1", "bias", "x"]
+    out = dict(W=_np(W), N=np.array(N, dtype=np.int32), M=np.array(M, dtype=np.int32), rank=np.int32(rank),
+               y=_np(y), dy=_np(dy), seed=np.int32(seed))
+    for nm, t in zip(names, params):
+        out[nm] = _np(t)
+        out["g_" + nm] = _np(t.grad)
+    np.savez_compressed(os.path.join(OUT, f"ref_htlayer_s{seed}.npz"), **out)
+    return out
+
+
 if __name__ == "__main__":
     _install_shims()
     torch.set_num_threads(4)
@@ -196,3 +242,6 @@ if __name__ == "__main__":
     for n, seed in [(20, 6)]:
         o = make_tensornetwork_4d(n, seed)
         print("tensornetwork 4d", n, seed, "k", o["k"].tolist())
+    for seed in (7,):
+        o = make_ht_layer(seed)
+        print("ht layer", seed, "y", o["y"].shape)
