@@ -35,6 +35,16 @@ Documented deviations from the reference (both are fixes, not choices):
 
 Tensors are column-major numpy arrays (Fortran order) as in the reference's
 CUDA code (``htd_tensorcore.cu:12``).
+
+Pinned to the reference's own outputs (tests/golden/, made by
+tests/golden/make_golden.py, which runs the reference's Python as written):
+the decomposition and its error by tests/test_oracle_golden.py (HT_TensorLy.py,
+HT_TensorNetwork.py, HT_4d_TensorNetwork.py); the HT tensor layer
+(``ht_layer_chain``, ``ht_layer_weight``, ``ht_layer_unfoldings``,
+``ht_layer_transfers``) by tests/test_oracle_htlayer_golden.py
+(HT_tensor_layer/FC_MNIST/mnist_ht.py).  The learned-sketch objective and its
+adjoint have no counterpart in the reference; they are checked against finite
+differences (tests/test_sketch_oracle.py).
 """
 from __future__ import annotations
 
