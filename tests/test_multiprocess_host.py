@@ -1,0 +1,57 @@
+"""The N > 1 host path of bench.py on CPU: two ranks over gloo (127.0.0.1).
+
+Each rank of a multi-GPU run decomposes its own tensor (replicas, no collective
+on the data path); the host side only synchronises (barrier) and takes the max
+of the per-rank times (allmax) before rank 0 prints.  These tests run that host
+logic with world_size 2 on the gloo backend, and the reference arm under
+torch.distributed.run, where rank 0 alone measures and prints."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+import torch.multiprocessing as mp
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, out_dir):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    sys.path.insert(0, ROOT)
+    import bench
+    bench.barrier(world)
+    v = bench.allmax(1.5 * (rank + 1), world)
+    bench.barrier(world)
+    with open(os.path.join(out_dir, f"rank{rank}.txt"), "w") as f:
+        f.write(repr(v))
+    dist.destroy_process_group()
+
+
+def test_allmax_and_barrier_over_gloo(tmp_path):
+    world = 2
+    mp.spawn(_rank_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True)
+    vals = [float(open(tmp_path / f"rank{r}.txt").read()) for r in range(world)]
+    assert vals == [3.0, 3.0]
+
+
+def test_reference_arm_under_torchrun_two_ranks():
+    port = _free_port()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.join(ROOT, "bench.py"),
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--cpu-sample", "32"]
+    out = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-3000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, out.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
