@@ -179,3 +179,36 @@ def test_bumps_and_batch_family():
     for X, tree in fam:
         tree.check_ranks(X.shape)
         assert 32 <= min(X.shape) and max(X.shape) <= 160
+
+
+@pytest.mark.parametrize("lang,compiler,flags", [("c", "gcc", ["-std=c99"]), ("c++", "g++", ["-std=c++17"])])
+def test_header_compiles_and_links_from_c_and_cpp(tmp_path, lang, compiler, flags):
+    """A caller of the reference's entry points, in C or C++, compiles against
+    include/htgb.h alone (no CUDA headers) and links against libhtgb.so."""
+    import shutil
+    import subprocess
+    if shutil.which(compiler) is None:
+        pytest.skip(f"{compiler} not installed")
+    src = tmp_path / ("caller.c" if lang == "c" else "caller.cpp")
+    src.write_text(
+        '#include "htgb.h"\n'
+        "#include <stdio.h>\n"
+        "int main(void) {\n"
+        "  ht_config_t cfg; ht_tree_t tree; int k[5] = {1, 4, 4, 4, 4}; long dims[3] = {8, 8, 8};\n"
+        "  if (ht_config_default(&cfg) != HT_OK) return 1;\n"
+        "  if (ht_tree_reference_3d(&tree, k) != HT_OK) return 2;\n"
+        "  if (ht_tree_validate(&tree, dims, 3) != HT_OK) return 3;\n"
+        "  float (*f3)(float *, long, long, long, int *) = htd;\n"
+        "  void (*f4)(float *, long, long, long, long, int *, void *, void *) = htd4;\n"
+        "  printf(\"%s %d\\n\", ht_status_string(HT_OK), f3 != 0 && f4 != 0);\n"
+        "  return 0;\n"
+        "}\n")
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    cmd = [compiler, *flags, "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+           "-L", libdir, "-lhtgb", f"-Wl,-rpath,{libdir}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0, (run.returncode, run.stderr)
+    assert run.stdout.split()[-1] == "1"
