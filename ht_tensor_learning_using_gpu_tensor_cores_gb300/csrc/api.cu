@@ -26,6 +26,7 @@
 //
 // Workspace: one cached device buffer per device, carved by a bump arena.
 // The whole pipeline first runs as a dry run (no launches) to size it.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -210,16 +211,7 @@ Operand gram_operand(const View &v, const void *x) {
   return o;
 }
 
-int g_sms = 0;
-int sm_count() {
-  if (!g_sms) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaGetLastError();
-    if (g_sms <= 0) g_sms = 148;
-  }
-  return g_sms;
-}
+int sm_count() { return device_sm_count(); }
 
 struct GemmReq {
   Operand a32, b32;                 // FP32 operands (SIMT path)
@@ -587,8 +579,15 @@ ht_status_t leaf_eigs(Ctx &c, const Tree &T, const ht_config_t &cfg, const long 
     if (!ews) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (eig)");
     // the FP32 path keeps two CholeskyQR refinement passes (its error sits at
     // FP32 rounding, where the last pass still moves it); the mixed path's
-    // BF16 Gram error is four orders above what they change
-    const int refine = cfg.precision == HT_PREC_FP32 ? 2 : 0;
+    // BF16 Gram error is four orders above what they change once the block has
+    // converged.  With few iterations, or a caller's start block, the last
+    // block need not be: Y = G S is rank deficient whenever the Gram's rank is
+    // below s (the separable-bumps family: rank <= 32 < 34), and one shifted
+    // CholeskyQR of it leaves noise columns that are not orthogonal to the
+    // rest.  Those paths refine on both precisions.
+    bool sketched = false;
+    for (int m = 0; m < order; ++m) sketched = sketched || cfg.sketch[m] != nullptr;
+    const int refine = (cfg.precision == HT_PREC_FP32 || iters < 4 || sketched) ? 2 : 0;
     if (!c.dry()) HT_CUDA(eig_batched(ep, order, iters, ews, eb, c.err, c.st, &c.launches, c.eig_ctas, refine));
     c.ar.off = mark;
   }
@@ -1299,6 +1298,11 @@ ht_status_t run_call(Ctx &c, const Tree &T, const ht_config_t &cfg, const CallAr
   HT_CUDA(cudaGetLastError());
   if (errword & kErrTimeout) return fail(HT_ERR_TIMEOUT, "a kernel's bounded wait expired; results are invalid");
   if (!std::isfinite(host_sums[0])) return fail(HT_ERR_NUMERICAL, "input tensor contains NaN or Inf");
+  if (errword & kErrBreakdown) return fail(HT_ERR_NUMERICAL, "a factorisation broke down (non-orthonormal basis)");
+  // X^ is X projected onto the tensor product of orthonormal node bases, so
+  // ||X - X^|| <= ||X||: a larger error means a basis is not orthonormal
+  if (a.want_err && host_sums[0] > 0 && !(host_sums[1] <= host_sums[0] * (1.0 + 1e-3)))
+    return fail(HT_ERR_NUMERICAL, "relative error above 1: a node basis is not orthonormal");
   if (rep) {
     std::memset(rep, 0, sizeof(*rep));
     rep->norm_x = std::sqrt(host_sums[0]);
@@ -1629,6 +1633,11 @@ ht_status_t ht_decompose_streaming(const float *x, const long *dims, int order, 
   g_launches += static_cast<unsigned long long>(c.launches);
   if (errword & kErrTimeout) return fail(HT_ERR_TIMEOUT, "a kernel's bounded wait expired; results are invalid");
   if (!std::isfinite(host_sums[0])) return fail(HT_ERR_NUMERICAL, "input tensor contains NaN or Inf");
+  if (errword & kErrBreakdown) return fail(HT_ERR_NUMERICAL, "a factorisation broke down (non-orthonormal basis)");
+  // X^ is X projected onto the tensor product of orthonormal node bases, so
+  // ||X - X^|| <= ||X||: a larger error means a basis is not orthonormal
+  if (a.want_err && host_sums[0] > 0 && !(host_sums[1] <= host_sums[0] * (1.0 + 1e-3)))
+    return fail(HT_ERR_NUMERICAL, "relative error above 1: a node basis is not orthonormal");
   if (report) {
     std::memset(report, 0, sizeof(*report));
     report->norm_x = std::sqrt(host_sums[0]);
@@ -1847,7 +1856,10 @@ ht_status_t ht_sketch_loss_grad(const float *G, const float *trG, int batch, int
   HT_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
   HT_CUDA(cudaStreamSynchronize(st));
   g_launches += static_cast<unsigned long long>(launches);
-  if (hbad) return fail(HT_ERR_NUMERICAL, "singular CholeskyQR factor: G S is rank deficient");
+  if (hbad) return fail(HT_ERR_NUMERICAL, "non-finite value in a Gram, the sketch or its CholeskyQR factor");
+  for (int b = 0; b < batch; ++b)
+    if (!(loss[b] >= -1e-4 && loss[b] <= 1.0 + 1e-4))
+      return fail(HT_ERR_NUMERICAL, "sketch loss of Gram " + std::to_string(b) + " outside [0, 1]");
   return HT_OK;
 }
 
@@ -2248,26 +2260,62 @@ __device__ __align__(256) float g_noalloc_scratch[HT_NOALLOC_SCRATCH_BYTES / siz
 namespace {
 
 std::mutex g_noalloc_mutex;
-float *g_noalloc_ptr[64];   // device address of g_noalloc_scratch, per device
+struct NoallocSlot {
+  float *ptr = nullptr;            // device address of g_noalloc_scratch
+  unsigned long long ctx = 0;      // id of the context it was looked up in
+};
+NoallocSlot g_noalloc_slot[64];
+
+// Id of the current context (0 when the driver cannot say).  A device's
+// primary context is destroyed by cudaDeviceReset and a new one gets a new id,
+// so an address looked up in the old one is not reused.
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext *);
+  using GetId = CUresult (*)(CUcontext, unsigned long long *);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+    cudaGetLastError();
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
 
 // The host-side symbol g_noalloc_scratch is not a device address; look the
-// real address up once per device, with that device current.
+// real address up once per device (and again in a new context), with that
+// device current.
 ht_status_t noalloc_scratch(float **out) {
   int dev = 0;
   HT_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return fail(HT_ERR_INVALID_ARG, "device index out of range");
   std::lock_guard<std::mutex> lk(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
+  NoallocSlot &slot = g_noalloc_slot[dev];
+  const unsigned long long ctx = current_context_id();
+  if (!slot.ptr || ctx == 0 || slot.ctx != ctx) {
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
       cudaGetLastError();
+      slot.ptr = nullptr;
       return fail(HT_ERR_CUDA, std::string("ht_mode_gram_noalloc: cudaGetSymbolAddress failed: ") +
                                    cudaGetErrorString(e));
     }
-    g_noalloc_ptr[dev] = static_cast<float *>(p);
+    slot.ptr = static_cast<float *>(p);
+    slot.ctx = ctx;
   }
-  *out = g_noalloc_ptr[dev];
+  *out = slot.ptr;
   return HT_OK;
 }
 

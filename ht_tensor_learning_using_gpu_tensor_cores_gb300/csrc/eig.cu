@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(256) svd_from_gram_kernel(const float *GW, int
 constexpr int RBMAX = 32;                 // rows per sub-block
 constexpr int CNS = 4;                    // cp.async stages of the G * Y product
 constexpr int CLD = 68;                   // padded k length of a staged row
-constexpr int kCoopMaxCta = 160;          // >= SMs of the device
+constexpr int kCoopMaxCta = 160;          // cap on the cooperative grid (sizes the per-CTA partials)
 constexpr int kMaxEntPerThread = (ESMAX + 255) / 256;
 
 struct CoopProb {

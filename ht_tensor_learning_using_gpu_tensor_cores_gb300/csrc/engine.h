@@ -94,9 +94,9 @@ long tc_num_kblocks(const Operand &a);
 cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s);
 long simt_k_total(const Operand &a);
 
-// Sum split-K partial tiles ([splits][tiles][gen.bm][bn]).  mode 0: symmetric
-// Gram (tiles on/above the diagonal, mirror into the lower triangle); mode 1:
-// plain column-major.
+// Sum split-K partial tiles ([splits][tiles][gen.bm][bn]) into out.
+// symmetric = 0: plain column-major tiles; symmetric != 0: a symmetric Gram
+// (tiles on/above the diagonal, mirrored into the lower triangle).
 cudaError_t reduce_partials_launch(const float *partial, const TileGen &gen, int splits, int bn, float *out,
                                    long long ld_out, int symmetric, cudaStream_t s);
 TileGen make_rows_gen(long long rows, int cols, int bn);
@@ -104,6 +104,9 @@ TileGen make_slabs_gen(long long L, long long R, int cols, int bn);
 // rows x cols output in 128 x bn tiles (TILES_GRID); false when the tile count overflows
 bool make_grid_gen(long long rows, long long cols, int bn, TileGen *g);
 bool make_gram_gen(long long n, int bn, TileGen *g, int bm = 128);
+
+// Multiprocessor count of the current device (cached per device).
+int device_sm_count();
 
 // --------------------------------------------------------------- small ops
 cudaError_t convert_bf16_launch(const float *x, __nv_bfloat16 *xb, long long n, double *sumsq_partials,

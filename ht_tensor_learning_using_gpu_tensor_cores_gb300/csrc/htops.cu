@@ -169,7 +169,7 @@ cudaError_t eval_core_launch(const float *Bt, int kp, int kq, int kt, const floa
                              cudaStream_t s) {
   const int total = kc * kq * kp;
   int grid = (total + 255) / 256;
-  if (grid > 152 * 8) grid = 152 * 8;
+  if (grid > 8 * device_sm_count()) grid = 8 * device_sm_count();
   eval_core_kernel<<<grid < 1 ? 1 : grid, 256, 0, s>>>(Bt, kp, kq, kt, M, kc, out);
   return cudaGetLastError();
 }
@@ -178,7 +178,7 @@ cudaError_t evaluate_launch(const EvalPlan &ep, const long long *idx, long long 
                             cudaStream_t s) {
   if (ep.ky < 1 || ep.ky > 64) return cudaErrorInvalidValue;
   long long grid = (count + 7) / 8;
-  if (grid > 152 * 16) grid = 152 * 16;
+  if (grid > 16ll * device_sm_count()) grid = 16ll * device_sm_count();
   if (grid < 1) grid = 1;
   evaluate_kernel<<<static_cast<unsigned>(grid), 256, 0, s>>>(ep, idx, count, out, err);
   return cudaGetLastError();

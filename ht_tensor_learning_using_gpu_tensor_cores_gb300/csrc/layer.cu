@@ -28,7 +28,7 @@ constexpr int kLayerThreads = 256;
 
 int grid_for_layer(long long n) {
   long long g = (n + kLayerThreads - 1) / kLayerThreads;
-  if (g > 152 * 32) g = 152 * 32;
+  if (g > 32ll * device_sm_count()) g = 32ll * device_sm_count();
   return static_cast<int>(g < 1 ? 1 : g);
 }
 
@@ -530,7 +530,7 @@ cudaError_t layer_colsum_launch(const float *dy, long long batch, long long nout
 
 int layer_dpq_chunks(const LayerShape &sh) {
   const int blocks = sh.m[0] * sh.m[1];
-  int ch = (2 * 152 + blocks - 1) / blocks;
+  int ch = (2 * device_sm_count() + blocks - 1) / blocks;
   return ch < 1 ? 1 : (ch > sh.m[2] ? sh.m[2] : ch);
 }
 

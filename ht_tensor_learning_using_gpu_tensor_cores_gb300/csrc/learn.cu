@@ -7,7 +7,10 @@
 // Grams, the energy the subspace misses:
 //
 //   L(S) = mean_b [ 1 - tr(Q_b^T G_b Q_b) / tr(G_b) ]
-//        = mean_b [ 1 - tr(C_b^-1 H_b) / tr(G_b) ],   C = Y^T Y = R^T R,  H = Y^T G Y.
+//        = mean_b [ 1 - tr(C_b^-1 H_b) / tr(G_b) ],   C = Y^T Y = R^T R,  H = Y^T G Y,
+//
+// with C and H restricted to the columns of Y that the CholeskyQR keeps (a
+// column in the span of the earlier ones to rounding is left out, see kDrop).
 //
 // Its adjoint through CholeskyQR (dC, dH back to dY, then dS = G dY):
 //
@@ -70,34 +73,47 @@ __global__ void __launch_bounds__(256) ls_bgemm_kernel(const float *__restrict__
   }
 }
 
+// A column of Y whose pivot (Schur complement) is below kDrop times its
+// squared norm lies in the span of the earlier columns to rounding and is left
+// out of Q: Y = G S is rank deficient whenever the Gram's rank is below the
+// sketch width (the separable-bumps family: rank <= 32 < 34), and keeping such
+// a column would turn rounding noise into a basis vector (and the loss
+// negative).  The oracle (sketch_loss) applies the same rule.
+constexpr double kDrop = 1e-8;
+
 // In-place Cholesky C = R^T R of an s x s FP64 matrix (upper triangle of A,
-// row-major stride LS_MAX) by one CTA; returns false on a non-positive pivot.
-__device__ bool ls_cholesky(double *A, int s, int *s_bad) {
+// row-major stride LS_MAX) by one CTA, dropping dependent columns: a dropped
+// column j gets R[j, j] = 1 and a zero row, and keep[j] = 0.  *s_bad is set
+// on a non-finite pivot.
+__device__ void ls_cholesky(double *A, int s, int *keep, double *d0, int *s_bad) {
   const int t = threadIdx.x;
   if (t == 0) *s_bad = 0;
+  for (int j = t; j < s; j += 256) d0[j] = A[j * LS_MAX + j];
   __syncthreads();
   for (int j = 0; j < s; ++j) {
     if (t == 0) {
       const double d = A[j * LS_MAX + j];
-      if (!(d > 0.0)) *s_bad = 1;
-      A[j * LS_MAX + j] = d > 0.0 ? sqrt(d) : 1.0;
+      if (!isfinite(d)) *s_bad = 1;
+      keep[j] = d > kDrop * d0[j] ? 1 : 0;
+      A[j * LS_MAX + j] = keep[j] ? sqrt(d) : 1.0;
     }
     __syncthreads();
-    const double inv = 1.0 / A[j * LS_MAX + j];
+    const double inv = keep[j] ? 1.0 / A[j * LS_MAX + j] : 0.0;
     for (int k = j + 1 + t; k < s; k += 256) A[j * LS_MAX + k] *= inv;
     __syncthreads();
-    for (int e = t; e < (s - j - 1) * (s - j - 1); e += 256) {
-      const int i = j + 1 + e / (s - j - 1), k = j + 1 + e % (s - j - 1);
-      if (k >= i) A[i * LS_MAX + k] -= A[j * LS_MAX + i] * A[j * LS_MAX + k];
-    }
+    if (keep[j])
+      for (int e = t; e < (s - j - 1) * (s - j - 1); e += 256) {
+        const int i = j + 1 + e / (s - j - 1), k = j + 1 + e % (s - j - 1);
+        if (k >= i) A[i * LS_MAX + k] -= A[j * LS_MAX + i] * A[j * LS_MAX + k];
+      }
     __syncthreads();
   }
-  return *s_bad == 0;
 }
 
-// Per Gram b: C = Y^T Y, H = Y^T P (FP64 accumulation), X = C^-1 H,
-// loss_b = 1 - tr(X) / trG_b, E = P - Y X, and Ci = C^-1 (FP64) for the
-// gradient.  One CTA per Gram.
+// Per Gram b: C = Y^T Y, H = Y^T P (FP64 accumulation), X = C_KK^-1 H_KK on the
+// kept columns K (zero rows and columns elsewhere), loss_b = 1 - tr(X) / trG_b,
+// E = P - Y X, and Ci = C_KK^-1 (FP64, zero outside K) for the gradient.  One
+// CTA per Gram.
 __global__ void __launch_bounds__(256) ls_small_kernel(const float *__restrict__ Y, const float *__restrict__ P,
                                                        const float *__restrict__ trG, int n, int s,
                                                        float *__restrict__ E, double *__restrict__ Ci,
@@ -106,6 +122,8 @@ __global__ void __launch_bounds__(256) ls_small_kernel(const float *__restrict__
   double *C = ls_sm;                        // LS_MAX x LS_MAX
   double *W = ls_sm + LS_MAX * LS_MAX;      // H, then X = C^-1 H
   __shared__ int s_bad;
+  __shared__ int keep[LS_MAX];
+  __shared__ double d0[LS_MAX];
   const int b = blockIdx.x, t = threadIdx.x;
   const float *Yb = Y + static_cast<long long>(b) * n * s;
   const float *Pb = P + static_cast<long long>(b) * n * s;
@@ -121,35 +139,40 @@ __global__ void __launch_bounds__(256) ls_small_kernel(const float *__restrict__
     W[i * LS_MAX + j] = h;
   }
   __syncthreads();
-  const bool ok = ls_cholesky(C, s, &s_bad);
-  if (!ok && t == 0) atomicOr(bad, 1);
-  // X = R^-1 R^-T H: forward substitution with R^T, then back substitution with R (column per thread)
+  ls_cholesky(C, s, keep, d0, &s_bad);
+  if (s_bad && t == 0) atomicOr(bad, 1);
+  // X = R^-1 R^-T H on K: forward substitution with R^T, then back substitution
+  // with R (column per thread); dropped rows and columns are zero
   for (int j = t; j < s; j += 256) {
     for (int i = 0; i < s; ++i) {   // R^T z = h
-      double v = W[i * LS_MAX + j];
-      for (int k = 0; k < i; ++k) v -= C[k * LS_MAX + i] * W[k * LS_MAX + j];
-      W[i * LS_MAX + j] = v / C[i * LS_MAX + i];
+      double v = (keep[i] && keep[j]) ? W[i * LS_MAX + j] : 0.0;
+      if (keep[i])
+        for (int k = 0; k < i; ++k) v -= C[k * LS_MAX + i] * W[k * LS_MAX + j];
+      W[i * LS_MAX + j] = keep[i] ? v / C[i * LS_MAX + i] : 0.0;
     }
     for (int i = s - 1; i >= 0; --i) {   // R x = z
       double v = W[i * LS_MAX + j];
-      for (int k = i + 1; k < s; ++k) v -= C[i * LS_MAX + k] * W[k * LS_MAX + j];
-      W[i * LS_MAX + j] = v / C[i * LS_MAX + i];
+      if (keep[i])
+        for (int k = i + 1; k < s; ++k) v -= C[i * LS_MAX + k] * W[k * LS_MAX + j];
+      W[i * LS_MAX + j] = keep[i] ? v / C[i * LS_MAX + i] : 0.0;
     }
   }
   __syncthreads();
-  // C^-1 = R^-1 R^-T, column j by thread j
+  // C_KK^-1 = R^-1 R^-T on K, column j by thread j
   double *Cib = Ci + static_cast<long long>(b) * LS_MAX * LS_MAX;
   for (int j = t; j < s; j += 256) {
     double z[LS_MAX];
     for (int i = 0; i < s; ++i) {   // R^T z = e_j
-      double v = (i == j) ? 1.0 : 0.0;
-      for (int k = 0; k < i; ++k) v -= C[k * LS_MAX + i] * z[k];
-      z[i] = v / C[i * LS_MAX + i];
+      double v = (i == j && keep[j]) ? 1.0 : 0.0;
+      if (keep[i])
+        for (int k = 0; k < i; ++k) v -= C[k * LS_MAX + i] * z[k];
+      z[i] = keep[i] ? v / C[i * LS_MAX + i] : 0.0;
     }
     for (int i = s - 1; i >= 0; --i) {   // R x = z
       double v = z[i];
-      for (int k = i + 1; k < s; ++k) v -= C[i * LS_MAX + k] * Cib[k * LS_MAX + j];
-      Cib[i * LS_MAX + j] = v / C[i * LS_MAX + i];
+      if (keep[i])
+        for (int k = i + 1; k < s; ++k) v -= C[i * LS_MAX + k] * Cib[k * LS_MAX + j];
+      Cib[i * LS_MAX + j] = keep[i] ? v / C[i * LS_MAX + i] : 0.0;
     }
   }
   if (t == 0) {
@@ -157,7 +180,7 @@ __global__ void __launch_bounds__(256) ls_small_kernel(const float *__restrict__
     for (int i = 0; i < s; ++i) tr += W[i * LS_MAX + i];
     loss[b] = 1.0 - tr / static_cast<double>(trG[b]);
   }
-  // E = P - Y X
+  // E = P - Y X (columns outside K are multiplied by zero rows of Ci later)
   float *Eb = E + static_cast<long long>(b) * n * s;
   for (int e = t; e < n * s; e += 256) {
     const int r = e % n, j = e / n;

@@ -346,7 +346,8 @@ cudaError_t reduce_partials_launch(const float *partial, const TileGen &gen, int
   while (groups < 8 && splits > 8 * groups) groups *= 2;
   const int nout = 256 / groups;
   long long blocks = (total + nout - 1) / nout;
-  const int grid = static_cast<int>(blocks < 152 * 16 ? blocks : 152 * 16);
+  const long long cap = 16ll * device_sm_count();
+  const int grid = static_cast<int>(blocks < cap ? blocks : cap);
   reduce_partials_kernel<<<grid, 256, 0, s>>>(partial, gen, gen.count, splits, bn, groups, out, ld_out, symmetric);
   return cudaGetLastError();
 }

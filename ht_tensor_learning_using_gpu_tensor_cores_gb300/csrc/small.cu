@@ -343,7 +343,31 @@ __global__ void transpose_small_kernel(const float *A, int m, int n, float *AT) 
   }
 }
 
-int grid_for(long long n, int cap = 152 * 8) {
+}  // namespace
+
+// Multiprocessor count of the current device (cached per device).
+int device_sm_count() {
+  static int cached[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return 1;
+  }
+  if (cached[dev] <= 0) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+      cudaGetLastError();
+      v = 1;
+    }
+    cached[dev] = v;
+  }
+  return cached[dev];
+}
+
+namespace {
+
+int grid_for(long long n, int cap = 0) {
+  if (cap <= 0) cap = 8 * device_sm_count();
   long long g = (n + 255) / 256;
   if (g < 1) g = 1;
   if (g > cap) g = cap;
@@ -410,7 +434,7 @@ cudaError_t gemm_tn_small_launch(const float *A, int lda, const float *B, int ld
 
 int core_step2_ranges(int nq, int kc) {
   const int chunks64 = (nq + 63) / 64;
-  int want = (2 * 152 + kc - 1) / kc;
+  int want = (2 * device_sm_count() + kc - 1) / kc;
   if (want > chunks64) want = chunks64;
   if (want < 1) want = 1;
   const int per = (chunks64 + want - 1) / want;   // 64-blocks of j per range

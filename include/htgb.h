@@ -251,7 +251,9 @@ ht_status_t ht_release_batch(void);
  * device) with traces trG (device), the forward value
  *   loss[b] = 1 - tr(Q_b^T G_b Q_b) / tr(G_b),   Q_b = orth(G_b S)  (CholeskyQR)
  * (host array of batch) and the adjoint grad = d mean_b loss[b] / dS (n x s,
- * device).  Synchronous; HT_ERR_NUMERICAL when a CholeskyQR factor is singular.
+ * device).  A column of G_b S in the span of the earlier columns to rounding
+ * (a Gram of rank below s) is left out of Q_b, so loss[b] stays in [0, 1].
+ * Synchronous; HT_ERR_NUMERICAL when a Gram, S or a factor holds NaN/Inf.
  * ht_sketch_adam: one Adam step on S with moments m, v (count = n*s, device),
  * step >= 1, beta1 0.9, beta2 0.999, eps 1e-8.  Asynchronous on `stream`. */
 ht_status_t ht_sketch_loss_grad(const float *G, const float *trG, int batch, int n, int s, const float *S,

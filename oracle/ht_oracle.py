@@ -48,18 +48,51 @@ differences (tests/test_sketch_oracle.py).
 """
 from __future__ import annotations
 
-import os
-import sys
 from typing import Dict, Sequence, Tuple
 
 import numpy as np
 
-_HERE = os.path.dirname(os.path.abspath(__file__))
-if os.path.dirname(_HERE) not in sys.path:
-    sys.path.insert(0, os.path.dirname(_HERE))
 
-from ht_tensor_learning_using_gpu_tensor_cores_gb300.tree import DimTree  # noqa: E402
-from ht_tensor_learning_using_gpu_tensor_cores_gb300.synth import fold  # noqa: E402
+class OTree:
+    """The oracle's own description of a dimension tree: per node the sorted
+    modes, the children (-1 for leaves) and the rank; node 0 is the root.  It
+    is built from plain lists or copied out of any object carrying ``order``,
+    ``modes``, ``left``, ``right`` and ``ranks`` (the product's tree class), so
+    the oracle shares no mapping code with the product."""
+
+    def __init__(self, order, modes, left, right, ranks):
+        self.order = int(order)
+        self.modes = [tuple(sorted(int(m) for m in ms)) for ms in modes]
+        self.left = [int(v) for v in left]
+        self.right = [int(v) for v in right]
+        self.ranks = [int(v) for v in ranks]
+        self.n_nodes = len(self.modes)
+        if self.n_nodes != 2 * self.order - 1 or self.modes[0] != tuple(range(self.order)):
+            raise ValueError("not a binary dimension tree with node 0 the root")
+
+    def is_leaf(self, t: int) -> bool:
+        return self.left[t] < 0
+
+    def leaves(self):
+        return [t for t in range(self.n_nodes) if self.is_leaf(t)]
+
+    def interior(self):
+        return [t for t in range(1, self.n_nodes) if not self.is_leaf(t)]
+
+
+def as_tree(tree) -> OTree:
+    if isinstance(tree, OTree):
+        return tree
+    return OTree(tree.order, tree.modes, tree.left, tree.right, tree.ranks)
+
+
+def fold(M: np.ndarray, row_modes: Sequence[int], dims: Sequence[int]) -> np.ndarray:
+    """Inverse of ``unfold``: the column-major tensor of shape ``dims`` whose
+    matricisation with rows over ``row_modes`` is M."""
+    rest = [m for m in range(len(dims)) if m not in row_modes]
+    perm = list(row_modes) + rest
+    T = np.reshape(M, [int(dims[m]) for m in perm], order="F")
+    return np.asfortranarray(np.transpose(T, np.argsort(perm)))
 
 
 def unfold(X: np.ndarray, row_modes: Sequence[int]) -> np.ndarray:
@@ -88,13 +121,14 @@ def top_eigvecs(G: np.ndarray, k: int, eig_order: str = "desc") -> Tuple[np.ndar
     return w[idx], V[:, idx]
 
 
-def ht_decompose(X: np.ndarray, tree: DimTree, dtype=np.float64, eig_order: str = "desc",
+def ht_decompose(X: np.ndarray, tree, dtype=np.float64, eig_order: str = "desc",
                  interior_svd: bool = True):
     """Root-to-leaf HT decomposition (the reference algorithm).
 
     Returns (U, B, info): U[t] for every non-root node (leaves and interior
     nodes), B[t] (k_l x k_r x k_t, Fortran order) for interior nodes and the
     root (k_l x k_r x 1)."""
+    tree = as_tree(tree)
     X = np.asarray(X, dtype=dtype)
     if not X.flags.f_contiguous:
         X = np.asfortranarray(X)
@@ -132,8 +166,9 @@ def transfer_tensor(Ut: np.ndarray, Ul: np.ndarray, Ur: np.ndarray) -> np.ndarra
     return np.asfortranarray(Bt)
 
 
-def node_basis(tree: DimTree, U: Dict[int, np.ndarray], B: Dict[int, np.ndarray], t: int) -> np.ndarray:
+def node_basis(tree, U: Dict[int, np.ndarray], B: Dict[int, np.ndarray], t: int) -> np.ndarray:
     """Reconstructed basis of node t: U_t for leaves, (U_r kron U_l) B_t above."""
+    tree = as_tree(tree)
     if tree.is_leaf(t):
         return U[t]
     l, r = tree.left[t], tree.right[t]
@@ -144,8 +179,9 @@ def node_basis(tree: DimTree, U: Dict[int, np.ndarray], B: Dict[int, np.ndarray]
     return T.reshape(Ul.shape[0] * Ur.shape[0], kt, order="F")
 
 
-def ht_reconstruct(tree: DimTree, dims: Sequence[int], U: Dict[int, np.ndarray], B: Dict[int, np.ndarray]) -> np.ndarray:
+def ht_reconstruct(tree, dims: Sequence[int], U: Dict[int, np.ndarray], B: Dict[int, np.ndarray]) -> np.ndarray:
     """Full tensor from (U_leaf, B_t) (htd_batch.cu:196-224, HT_TensorLy.py:76-81)."""
+    tree = as_tree(tree)
     l, r = tree.left[0], tree.right[0]
     Ul = node_basis(tree, U, B, l)
     Ur = node_basis(tree, U, B, r)
@@ -153,12 +189,13 @@ def ht_reconstruct(tree: DimTree, dims: Sequence[int], U: Dict[int, np.ndarray],
     return fold(M, tree.modes[l], dims)
 
 
-def ht_entries(tree: DimTree, U: Dict[int, np.ndarray], B: Dict[int, np.ndarray], idx: np.ndarray) -> np.ndarray:
+def ht_entries(tree, U: Dict[int, np.ndarray], B: Dict[int, np.ndarray], idx: np.ndarray) -> np.ndarray:
     """Entries Xhat[idx[e]] contracted leaf-to-root without forming Xhat: a leaf
     contributes the row U_t[i_m, :], an interior node
     v_t[c] = sum_{a,b} B_t[a, b, c] v_l[a] v_r[b], and the root's v_0[0] is the
     entry.  The same contraction as ht_reconstruct's node bases
     (htd_batch.cu:196-224), restricted to one row of each."""
+    tree = as_tree(tree)
     idx = np.asarray(idx, dtype=np.int64)
 
     def vec(t):
@@ -176,7 +213,8 @@ def rel_error(X: np.ndarray, Xh: np.ndarray) -> float:
     return float(np.linalg.norm((X - np.asarray(Xh, dtype=np.float64)).ravel()) / np.linalg.norm(X.ravel()))
 
 
-def ht_error(X: np.ndarray, tree: DimTree, U, B) -> float:
+def ht_error(X: np.ndarray, tree, U, B) -> float:
+    tree = as_tree(tree)
     return rel_error(X, ht_reconstruct(tree, X.shape, U, B))
 
 
@@ -201,8 +239,9 @@ def procrustes_align(A: np.ndarray, B: np.ndarray) -> np.ndarray:
     return u @ vt
 
 
-def tree_energy_bound(tree: DimTree) -> float:
+def tree_energy_bound(tree) -> float:
     """Quasi-optimality constant of root-to-leaf HT truncation: sqrt(2d-3)."""
+    tree = as_tree(tree)
     return float(np.sqrt(2 * tree.order - 3))
 
 
@@ -211,24 +250,56 @@ def tree_energy_bound(tree: DimTree) -> float:
 # reference (its rsvd draws a Gaussian test matrix, 3D/Opt/kernel.cu:595-680);
 # these are the float64 statements of the training objective and its gradient
 # that the GPU forward/adjoint kernels are checked against.
-def sketch_loss(G: np.ndarray, S: np.ndarray) -> float:
-    """1 - tr(Q^T G Q) / tr(G), Q an orthonormal basis of G S."""
-    G = np.asarray(G, np.float64)
-    Y = G @ np.asarray(S, np.float64)
-    Q, _ = np.linalg.qr(Y)
-    return float(1.0 - np.trace(Q.T @ G @ Q) / np.trace(G))
+# A column of Y = G S whose CholeskyQR pivot (Schur complement) falls below
+# SKETCH_DROP times its squared norm lies in the span of the earlier columns
+# to rounding: it is left out of Q (rank-deficient Y, e.g. a Gram of rank
+# below the sketch width).  The GPU kernel (csrc/learn.cu) applies the same rule.
+SKETCH_DROP = 1e-8
 
 
-def sketch_grad(G: np.ndarray, S: np.ndarray) -> np.ndarray:
-    """d sketch_loss / dS = -(2 / tr G) G E C^-1, Y = G S, C = Y^T Y,
-    E = G Y - Y C^-1 (Y^T G Y)."""
+def _sketch_parts(G: np.ndarray, S: np.ndarray):
+    """Y = G S, C = Y^T Y, the kept columns K of the pivot-dropping Cholesky."""
     G = np.asarray(G, np.float64)
     Y = G @ np.asarray(S, np.float64)
     C = Y.T @ Y
-    P = G @ Y
-    X = np.linalg.solve(C, Y.T @ P)
-    E = P - Y @ X
-    return -(2.0 / np.trace(G)) * (G @ E) @ np.linalg.inv(C)
+    s = C.shape[0]
+    A = C.copy()
+    keep = np.ones(s, dtype=bool)
+    d0 = np.diag(C).copy()
+    for j in range(s):
+        d = A[j, j]
+        if not d > SKETCH_DROP * d0[j]:
+            keep[j] = False
+            continue
+        r = A[j, j + 1:] / np.sqrt(d)
+        A[j + 1:, j + 1:] -= np.outer(r, r)
+    return G, Y, C, keep
+
+
+def sketch_loss(G: np.ndarray, S: np.ndarray) -> float:
+    """1 - tr(Q^T G Q) / tr(G), Q an orthonormal basis of G S (of its kept
+    columns when G S is rank deficient)."""
+    G, Y, C, K = _sketch_parts(G, S)
+    if not K.any():
+        return 1.0
+    H = Y[:, K].T @ G @ Y[:, K]
+    return float(1.0 - np.trace(np.linalg.solve(C[np.ix_(K, K)], H)) / np.trace(G))
+
+
+def sketch_grad(G: np.ndarray, S: np.ndarray) -> np.ndarray:
+    """d sketch_loss / dS: on the kept columns K, -(2 / tr G) G E C^-1 with
+    Y = G S, C = Y_K^T Y_K, E = G Y_K - Y_K C^-1 (Y_K^T G Y_K); zero elsewhere."""
+    G, Y, C, K = _sketch_parts(G, S)
+    out = np.zeros((G.shape[0], C.shape[0]))
+    if not K.any():
+        return out
+    YK = Y[:, K]
+    CK = C[np.ix_(K, K)]
+    P = G @ YK
+    X = np.linalg.solve(CK, YK.T @ P)
+    E = P - YK @ X
+    out[:, K] = -(2.0 / np.trace(G)) * (G @ E) @ np.linalg.inv(CK)
+    return out
 
 
 # ------------------------------------------------------------- HT tensor layer

@@ -1,9 +1,9 @@
 """Generate golden vectors by running the reference's own Python HT statements.
 
-Run in a container where the reference checkout is mounted (default path
-/root/reference, override with HT_REFERENCE_DIR):
+Run where a checkout of the reference is available, naming its root in
+HT_REFERENCE_DIR (required; there is no default):
 
-    python tests/golden/make_golden.py
+    HT_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 
 The reference scripts
   third_order_tensor_decompsition/Python/HT_TensorLy.py
@@ -43,7 +43,7 @@ import types
 import numpy as np
 import torch
 
-REF = os.environ.get("HT_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("HT_REFERENCE_DIR", "")
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -231,6 +231,8 @@ def make_ht_layer(seed, N=(4, 4, 6), M=(4, 5, 4), rank=4, batch=5):
 
 
 if __name__ == "__main__":
+    if not REF or not os.path.isdir(REF):
+        sys.exit("set HT_REFERENCE_DIR to the root of a reference checkout")
     _install_shims()
     torch.set_num_threads(4)
     for n, seed in [(24, 1), (32, 2)]:

@@ -102,3 +102,33 @@ def test_sketch_drives_the_decomposition():
                          sketch=bad).report["rel_err"]
     assert abs(e_good - exact) <= 1e-5 * max(1.0, exact / 1e-3), (e_good, exact)
     assert e_bad > 10 * e_good + 1e-6, (e_bad, e_good)
+
+
+def test_one_iteration_paths_on_the_bump_family_bf16():
+    """The learned-sketch configuration on its own tensor family (separable
+    bumps, rank 24, sketch width 34 = 24 + 10), mixed path, one iteration:
+    with a Gaussian and with a trained start block the error stays within
+    1e-3 of the exact-Gram path's against the FP64 oracle.  Every mode Gram of
+    this family has rank <= 32 < 34, so Y = G S is rank deficient; the call
+    must still return orthonormal bases (it once returned errors of 4-44 with
+    HT_OK), and training must keep its losses in [0, 1]."""
+    n, k, p = 256, 24, 10
+    tree = ht.reference_tree_3d([1, k, k, k, k])
+    X = synth.bumps(n, seed=901, assemble_on=torch.device("cuda"))
+    Xnp = np.asfortranarray(X.cpu().numpy().transpose(2, 1, 0))
+    Uo, Bo, _ = O.ht_decompose(Xnp, tree, dtype=np.float64)
+    err64 = O.ht_error(Xnp, tree, Uo, Bo)
+    exact = ht.decompose(X, tree, precision="bf16", compute_error=True)
+    assert exact.report["rel_err"] - err64 <= 1e-3
+    G, trg = learn.family_grams(range(910, 918), n, precision="bf16")
+    sketches, hist = learn.train_mode_sketches(G, trg, s=k + p, steps=60, batch=8, lr=2e-3, seed=3)
+    assert min(min(h) for h in hist.values()) >= -1e-6, "sketch losses must stay non-negative"
+    for name, sk in (("gaussian", None), ("learned", [learn.to_bf16(S) for S in sketches])):
+        res = ht.decompose(X, tree, precision="bf16", compute_error=True, eig_iters=1, oversample=p, sketch=sk)
+        U = {t: res.U[t].cpu().numpy() for t in res.U}
+        B = {t: res.B[t].cpu().numpy() for t in res.B}
+        for t, u in U.items():
+            assert O.orthogonality_defect(u) < 1e-4, (name, t)
+        e = O.ht_error(Xnp, tree, U, B)
+        assert abs(e - res.report["rel_err"]) <= 1e-5 + 1e-3 * e, (name, e, res.report["rel_err"])
+        assert e <= exact.report["rel_err"] + 1e-3, (name, e, exact.report["rel_err"], err64)

@@ -37,3 +37,22 @@ def test_sketch_loss_invariances():
     w, V = np.linalg.eigh(G)
     best = 1 - w[::-1][:s].sum() / w.sum()
     assert abs(O.sketch_loss(G, V[:, ::-1][:, :s]) - best) < 1e-12
+
+
+def test_sketch_loss_rank_deficient_gram_stays_in_range():
+    """A Gram of rank below the sketch width (the separable-bumps family: rank
+    <= 32 < 34) makes Y = G S rank deficient.  The dependent columns are left
+    out of Q, so the loss stays in [0, 1] and equals the exact value 0 (the
+    kept columns span the whole range)."""
+    rng = np.random.default_rng(2)
+    n, r, s = 40, 6, 9
+    A = rng.standard_normal((n, r)) * (0.5 ** np.arange(r))
+    G = A @ A.T
+    S = rng.standard_normal((n, s))
+    loss = O.sketch_loss(G, S)
+    assert 0.0 <= loss < 1e-9, loss
+    _, _, _, keep = O._sketch_parts(G, S)
+    assert keep.sum() == r
+    g = O.sketch_grad(G, S)
+    assert np.isfinite(g).all()
+    assert np.abs(g[:, ~keep]).max() == 0.0

@@ -1,6 +1,7 @@
-"""The allocation-free Gram entry point (ht_mode_gram_noalloc) against the
-allocating one (ht_mode_gram, FP32), both called through the C ABI on device
-buffers.  FP32 tolerance as elsewhere: 1e-5 relative (Frobenius).
+"""The allocation-free Gram entry point (ht_mode_gram_noalloc), called through
+the C ABI on device buffers, against numpy's float64 X_(g) X_(g)^T and against
+the allocating entry point (ht_mode_gram, FP32).  FP32 tolerance as elsewhere:
+1e-5 relative (Frobenius).
 
 Two calls in a row on different shapes share the one static scratch array;
 the second must not see the first's leftovers.  The file is named so that
@@ -35,6 +36,16 @@ def n_of(dims, lo, hi):
     return int(np.prod(dims[lo:hi + 1]))
 
 
+def gram_fp64(x, dims, lo, hi):
+    """X_(g) X_(g)^T in float64: rows over modes lo..hi, columns over the rest."""
+    L = int(np.prod(dims[:lo]))
+    N = n_of(dims, lo, hi)
+    R = int(np.prod(dims[hi + 1:]))
+    X3 = x.cpu().numpy().astype(np.float64).reshape((L, N, R), order="F")
+    Xg = X3.transpose(1, 0, 2).reshape(N, L * R)
+    return Xg @ Xg.T
+
+
 def call_noalloc(L, x, dims, lo, hi, G, stream):
     return L.ht_mode_gram_noalloc(ctypes.c_void_p(x.data_ptr()), (ctypes.c_long * 4)(*dims), len(dims), lo, hi,
                                   ctypes.c_void_p(G.data_ptr()), ctypes.c_void_p(stream))
@@ -64,16 +75,18 @@ def test_noalloc_gram_matches_allocating_gram_twice():
         assert rc == 0, L.ht_last_error()
     torch.cuda.synchronize()
     assert torch.cuda.mem_get_info()[0] == free_before, "the no-alloc call changed free device memory"
-    for (d, lo, hi), G, R in zip(cases, outs, refs):
+    for (d, lo, hi), x, G, R in zip(cases, inputs, outs, refs):
         g, r = G.cpu().numpy(), R.cpu().numpy()
         assert np.isfinite(g).all()
         assert np.array_equal(g, g.T)
+        assert rel(g, gram_fp64(x, d, lo, hi)) < TOL, (d, lo, hi, rel(g, gram_fp64(x, d, lo, hi)))
         assert rel(g, r) < TOL, (d, lo, hi, rel(g, r))
     # the first shape again, after the second call left its partials in the scratch
     d, lo, hi = cases[0]
     G = torch.full_like(outs[0], float("nan"))
     assert call_noalloc(L, inputs[0], d, lo, hi, G, stream) == 0
     torch.cuda.synchronize()
+    assert rel(G.cpu().numpy(), gram_fp64(inputs[0], d, lo, hi)) < TOL
     assert rel(G.cpu().numpy(), refs[0].cpu().numpy()) < TOL
 
 
