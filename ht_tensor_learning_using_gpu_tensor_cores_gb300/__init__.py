@@ -26,7 +26,7 @@ from typing import Dict, Optional, Sequence
 import numpy as np
 
 from . import htformat, synth
-from ._lib import (FLAG_COMPUTE_ERROR, HTError, HtBatchReport, HtConfig, HtReport, HtTree, LEAF_GRAM, PREC_BF16,
+from ._lib import (FLAG_COMPUTE_ERROR, HTError, HtBatchReport, HtConfig, HtReport, HtTree, LEAF_GRAM, LEAF_SKETCH, PREC_BF16,
                    PREC_FP32, check, lib)
 from .tree import (DimTree, balanced_tree_4d, left_first_tree_3d, middle_tree_3d, reference_tree_3d,
                    uniform_ranks)
@@ -121,14 +121,19 @@ def _out_buffers(tree: DimTree, dims, like):
     return U, B, uptr, bptr
 
 
+_LEAF = {"gram": LEAF_GRAM, "sketch": LEAF_SKETCH}
+
+
 def _config(precision: str, oversample: int, eig_iters: int, power_steps: int, seed: int, flags: int,
-            sketch=None, eig_tol: float = 0.0) -> tuple:
+            sketch=None, eig_tol: float = 0.0, leaf_method: str = "gram") -> tuple:
     cfg = HtConfig()
     check(lib().ht_config_default(ctypes.byref(cfg)))
     if precision not in _PREC:
         raise ValueError(f"precision must be one of {sorted(_PREC)}")
+    if leaf_method not in _LEAF:
+        raise ValueError(f"leaf_method must be one of {sorted(_LEAF)}")
     cfg.precision = _PREC[precision]
-    cfg.leaf_method = LEAF_GRAM
+    cfg.leaf_method = _LEAF[leaf_method]
     cfg.oversample = int(oversample)
     cfg.eig_iters = int(eig_iters)
     cfg.power_steps = int(power_steps)
@@ -157,17 +162,22 @@ def _config(precision: str, oversample: int, eig_iters: int, power_steps: int, s
 
 def decompose(x, tree: DimTree, dims: Optional[Sequence[int]] = None, precision: str = "bf16", oversample: int = 16,
               eig_iters: int = 10, power_steps: int = 1, seed: int = 1234, compute_error: bool = False,
-              sketch=None, eig_tol: float = 0.0, stream=None) -> HTResult:
+              sketch=None, eig_tol: float = 0.0, stream=None, leaf_method: str = "gram") -> HTResult:
     """HT decomposition of a column-major 3rd/4th-order float32 tensor.
 
     precision="bf16": BF16 tcgen05 GEMMs with FP32 accumulation (the mixed path);
     precision="fp32": every product in FP32 on CUDA cores (the plain path).
-    sketch: optional per-mode start blocks (n_m x (k+p)) for the leaf eigen-solver.
+    leaf_method="gram": leaf bases from the mode Grams (subspace iteration,
+    eig_iters); "sketch": from the Gram-free range finder on X_(t)
+    (power_steps applications of X_(t) X_(t)^T as streaming products, a
+    Nystrom core; the interior node from a Householder TSQR).
+    sketch: optional per-mode blocks (n_m x (k+p)): the eigen-solver's start
+    block ("gram") or the range finder's block S ("sketch").
     """
     dims = _dims_of(x, tree, dims)
     tree.check_ranks(dims)
     flags = FLAG_COMPUTE_ERROR if compute_error else 0
-    cfg, keep = _config(precision, oversample, eig_iters, power_steps, seed, flags, sketch, eig_tol)
+    cfg, keep = _config(precision, oversample, eig_iters, power_steps, seed, flags, sketch, eig_tol, leaf_method)
     ts = _tree_struct(tree)
     cdims = (c_long * 4)(*dims)
     if _is_torch(x):
@@ -560,4 +570,26 @@ def corange_product(x, dims: Sequence[int], lo: int, Q, hi: Optional[int] = None
     return out
 
 
-__all__ += ["mode_gram", "mode_product", "corange_product"]
+def tsqr(A):
+    """R factor (k x k, upper triangular, non-negative diagonal) of a tall-skinny
+    float32 matrix A (m x k, k <= 64) by the GPU Householder TSQR (ht_tsqr).
+    A: a numpy array (any order) or a float32 CUDA tensor of shape (m, k) whose
+    columns are contiguous (e.g. the transpose of a contiguous (k, m) tensor).
+    Returns the same kind as A."""
+    if _is_torch(A):
+        import torch
+        if not A.is_cuda or A.dtype != torch.float32 or A.dim() != 2 or A.stride(0) != 1:
+            raise TypeError("A must be a float32 CUDA tensor (m, k) with contiguous columns")
+        m, k = int(A.shape[0]), int(A.shape[1])
+        R = torch.empty((k, k), dtype=torch.float32, device=A.device).t()   # column-major storage
+        check(lib().ht_tsqr(c_void_p(A.data_ptr()), m, k, max(int(A.stride(1)), m), c_void_p(R.data_ptr()),
+                            c_void_p(torch.cuda.current_stream(A.device).cuda_stream)))
+        return R
+    a = np.asfortranarray(np.asarray(A, dtype=np.float32))
+    m, k = a.shape
+    R = np.zeros((k, k), dtype=np.float32, order="F")
+    check(lib().ht_tsqr(c_void_p(a.ctypes.data), m, k, m, c_void_p(R.ctypes.data), None))
+    return R
+
+
+__all__ += ["mode_gram", "mode_product", "corange_product", "tsqr"]

@@ -20,7 +20,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libhtgb.so")
-SOURCES = ["api.cu", "tc_gemm.cu", "simt_gemm.cu", "eig.cu", "small.cu", "learn.cu", "htops.cu", "layer.cu"]
+SOURCES = ["api.cu", "tc_gemm.cu", "simt_gemm.cu", "eig.cu", "small.cu", "learn.cu", "htops.cu", "layer.cu", "tsqr.cu", "sketch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
 

@@ -121,8 +121,9 @@ def lib():
     L.ht_sketch_adam.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_longlong, c_float, c_int, c_void_p]
     L.ht_corange_product.argtypes = [c_void_p, POINTER(c_long), c_int, c_int, c_int, c_void_p, c_int, c_int,
                                      c_void_p, c_void_p]
+    L.ht_tsqr.argtypes = [c_void_p, c_longlong, c_int, c_longlong, c_void_p, c_void_p]
     for name in ("ht_decompose_streaming", "ht_layer_weight", "ht_layer_forward", "ht_layer_backward", "ht_layer_check", "ht_layer_release",
-                 "ht_reconstruct", "ht_evaluate", "ht_sketch_loss_grad", "ht_sketch_adam", "ht_decompose_batched", "ht_release_batch", "ht_mode_gram", "ht_mode_gram_noalloc", "ht_mode_product", "ht_corange_product", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
+                 "ht_reconstruct", "ht_evaluate", "ht_sketch_loss_grad", "ht_sketch_adam", "ht_decompose_batched", "ht_release_batch", "ht_mode_gram", "ht_mode_gram_noalloc", "ht_mode_product", "ht_corange_product", "ht_tsqr", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
                  "ht_decompose", "ht_reconstruct_error", "ht_workspace_size", "ht_release_workspace"):
         getattr(L, name).restype = c_int
     _lib = L

@@ -388,8 +388,10 @@ ht_status_t mode_product(Ctx &c, const View &v, const float *x32, const __nv_bfl
 }
 
 // Z (v.N x k, column-major) = X_(group) Q with Q ((L*R) x k): contract every index but the middle one
+// a16: optional BF16 A operand in place of X_(group) read from x16 (the
+// l-blocked copy of the last mode, see gram_transposed)
 ht_status_t corange_product(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x16, const float *Q32,
-                            const __nv_bfloat16 *Q16, int k, float *Z) {
+                            const __nv_bfloat16 *Q16, int k, float *Z, const Operand *a16 = nullptr) {
   GemmReq q;
   auto opB = [&](const void *p) {
     Operand o;
@@ -402,7 +404,7 @@ ht_status_t corange_product(Ctx &c, const View &v, const float *x32, const __nv_
     return o;
   };
   q.a32 = gram_operand(v, x32); q.b32 = opB(Q32);
-  if (x16 && Q16) { q.a16 = gram_operand(v, x16); q.b16 = opB(Q16); }
+  if ((x16 || a16) && Q16) { q.a16 = a16 ? *a16 : gram_operand(v, x16); q.b16 = opB(Q16); }
   else q.a16.ptr = q.b16.ptr = nullptr;
   q.bn_tc = 64; q.bn_simt = 64;
   q.tiles_kind = TILES_ROWS; q.t_rows = v.N; q.t_cols = k;
@@ -594,6 +596,154 @@ ht_status_t leaf_eigs(Ctx &c, const Tree &T, const ht_config_t &cfg, const long 
   return HT_OK;
 }
 
+// 2'. Leaf bases without the mode Grams (HT_LEAF_SKETCH): a randomized range
+// finder on X_(m) whose test matrix is Omega = X_(m)^T Q for a per-mode block
+// Q (n_m x s, s = k + oversample): the caller's sketch[m] or a Gaussian one.
+// Each application Y = G Q = X_(m) (X_(m)^T Q) is two streaming products
+// over the tensor (mode product, then co-range product); G is never formed.
+//   Q = orth(S);  power_steps times: Q = orth(G Q);  Y = G Q
+// and the leaf basis is Q1 times the top-k eigenvectors of the Nystrom core
+// H = R1 (Q^T Y + nu I)^-1 R1^T, Y + nu Q = Q1 R1 (sketch.cu).  Orthonormal
+// blocks come from the eigen-solver's cooperative CholeskyQR2 (float-pair
+// factor).  The reference's range finder (rsvd, 3D/Opt/kernel.cu:595-680)
+// draws a Gaussian Omega for X_(12) and SVDs the projected B = Q^T A; no
+// residual is reported on this path (there is no Gram to measure it on).
+constexpr float kNystromShift = 1e-7f;   // nu / tr(Q^T G Q)
+
+ht_status_t leaf_sketch(Ctx &c, const Tree &T, const ht_config_t &cfg, const long *dims, int order,
+                        const float *x32, const __nv_bfloat16 *x16, const __nv_bfloat16 *x16t, int lb,
+                        EigProblem *ep, Result &res) {
+  const int p_over = cfg.oversample > 0 ? cfg.oversample : 16;
+  const int qsteps = cfg.power_steps >= 0 ? cfg.power_steps : 1;
+  const bool d3 = order == 3;
+  Plan3 P3{};
+  if (d3) P3 = plan3(T);
+  int K[4], S[4];
+  long long LRmax = 0, nmax = 0;
+  int smax = 1;
+  for (int m = 0; m < order; ++m) {
+    const int leaf = T.leaf_of_mode(m);
+    K[m] = (d3 && leaf == P3.c) ? P3.kw : T.rank[leaf];
+    const int n = static_cast<int>(dims[m]);
+    S[m] = std::max(K[m], std::min({n, K[m] + p_over, 64}));
+    if (S[m] > 64) return fail(HT_ERR_UNSUPPORTED, "sketch width above 64");
+    const View v = view_of_group(dims, order, m, m);
+    LRmax = std::max(LRmax, static_cast<long long>(v.L * v.R));
+    nmax = std::max(nmax, static_cast<long long>(n));
+    smax = std::max(smax, S[m]);
+  }
+  // results (kept): U per leaf; work (released at the end)
+  for (int m = 0; m < order; ++m) {
+    const int leaf = T.leaf_of_mode(m);
+    EigProblem &e = ep[m];
+    e = EigProblem{};
+    e.n = static_cast<int>(dims[m]); e.s = S[m]; e.K = K[m];
+    e.U = c.ar.take<float>(static_cast<size_t>(e.n) * K[m]);
+    if (!e.U) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (sketch bases)");
+    res.U[leaf] = e.U;
+    res.resid[leaf] = nullptr;
+  }
+  const size_t mark = c.ar.off;
+  const int hmax = smax <= 32 ? 32 : 64;
+  float *Z32 = c.ar.take<float>(static_cast<size_t>(LRmax) * smax);
+  __nv_bfloat16 *Z16 = c.tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(LRmax) * smax + 64) : nullptr;
+  __nv_bfloat16 *Q16 = c.tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(nmax) * 2 * hmax + 64) : nullptr;
+  if (!Z32 || (c.tc && (!Z16 || !Q16))) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (sketch products)");
+  float *Qm[4], *Ym[4], *Q1[4], *Wm[4], *R1[4], *Hm[4], *Tm[4], *M2[4], *Br[4];
+  for (int m = 0; m < order; ++m) {
+    const size_t ns = static_cast<size_t>(dims[m]) * S[m], ss = static_cast<size_t>(S[m]) * S[m];
+    Qm[m] = c.ar.take<float>(ns);
+    Ym[m] = c.ar.take<float>(ns);
+    Q1[m] = c.ar.take<float>(ns);
+    Wm[m] = c.ar.take<float>(ss);
+    R1[m] = c.ar.take<float>(ss);
+    Hm[m] = c.ar.take<float>(ss);
+    Tm[m] = c.ar.take<float>(static_cast<size_t>(S[m]) * K[m]);
+    M2[m] = c.ar.take<float>(static_cast<size_t>(S[m]) * K[m]);
+    Br[m] = c.ar.take<float>(static_cast<size_t>(K[m]) * K[m]);
+    if (!Qm[m] || !Ym[m] || !Q1[m] || !Wm[m] || !R1[m] || !Hm[m] || !Tm[m] || !M2[m] || !Br[m])
+      return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (sketch)");
+  }
+  EigProblem cq[4];
+  for (int m = 0; m < order; ++m) {
+    cq[m] = EigProblem{};
+    cq[m].n = static_cast<int>(dims[m]); cq[m].s = S[m]; cq[m].K = S[m];
+  }
+  const size_t cbytes = eig_workspace_bytes(cq, order);
+  void *cws = c.ar.take<char>(cbytes);
+  if (!cws) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (sketch CholeskyQR)");
+  if (c.dry()) {
+    c.ar.off = mark;
+    return HT_OK;
+  }
+  auto orth_all = [&](float *const *M) -> ht_status_t {   // CholeskyQR2 of every mode's block, one launch
+    for (int m = 0; m < order; ++m) {
+      cq[m].Q = M[m];
+      cq[m].G = nullptr; cq[m].Y = cq[m].U = cq[m].GU = cq[m].theta = cq[m].resid = nullptr;
+      cq[m].start = nullptr;
+    }
+    HT_CUDA(cholqr_batched(cq, order, 2, cws, cbytes, c.err, c.st, &c.launches));
+    return HT_OK;
+  };
+  // Y = G Q for mode m, as X_(m) (X_(m)^T Q)
+  auto apply_gram = [&](int m, const float *Qsrc, float *Ydst) -> ht_status_t {
+    const View v = view_of_group(dims, order, m, m);
+    const long long LR = v.L * v.R;
+    const int s = S[m], h = s <= 32 ? 32 : 64;
+    if (c.tc) {
+      HT_CUDA(split_bf16_launch(Qsrc, dims[m], s, h, Q16, c.st));
+      ++c.launches;
+    }
+    HT_TRY(mode_product(c, v, x32, x16, Qsrc, Q16, s, Z32, c.tc ? h : 0));
+    if (c.tc) {
+      HT_CUDA(f32_to_bf16_launch(Z32, Z16, LR * s, c.st));
+      ++c.launches;
+    }
+    if (c.tc && m == order - 1 && x16t) {
+      Operand o;
+      o.kind = OP_KM3; o.ptr = x16t; o.d0 = 1l << lb; o.d1 = v.N; o.d2 = v.L >> lb;
+      return corange_product(c, v, x32, x16, Z32, Z16, s, Ydst, &o);
+    }
+    return corange_product(c, v, x32, x16, Z32, Z16, s, Ydst);
+  };
+  // start blocks
+  for (int m = 0; m < order; ++m) {
+    const size_t ns = static_cast<size_t>(dims[m]) * S[m];
+    if (cfg.sketch[m]) {
+      HT_CUDA(cudaMemcpyAsync(Qm[m], cfg.sketch[m], sizeof(float) * ns, cudaMemcpyDefault, c.st));
+    } else {
+      HT_CUDA(gaussian_fill_launch(Qm[m], static_cast<long long>(ns), cfg.seed, 200 + m, c.st));
+      ++c.launches;
+    }
+  }
+  HT_TRY(orth_all(Qm));
+  for (int it = 0; it < qsteps; ++it) {
+    for (int m = 0; m < order; ++m) HT_TRY(apply_gram(m, Qm[m], Ym[m]));
+    for (int m = 0; m < order; ++m) std::swap(Qm[m], Ym[m]);
+    HT_TRY(orth_all(Qm));
+  }
+  for (int m = 0; m < order; ++m) HT_TRY(apply_gram(m, Qm[m], Ym[m]));
+  // Nystrom: W = Q^T Y, Y_nu = Y + nu Q -> Q1 R1, H = R1 (W + nu I)^-1 R1^T, U = Q1 * top-K(H)
+  for (int m = 0; m < order; ++m) {
+    const int n = static_cast<int>(dims[m]), s = S[m];
+    HT_CUDA(gemm_tn_small_launch(Qm[m], n, Ym[m], n, Wm[m], s, s, s, n, c.st));
+    HT_CUDA(nystrom_shift_launch(Ym[m], Qm[m], n, s, Wm[m], kNystromShift, Q1[m], c.st));
+    HT_CUDA(cudaMemcpyAsync(Ym[m], Q1[m], sizeof(float) * n * s, cudaMemcpyDeviceToDevice, c.st));   // Y_nu
+    c.launches += 2;
+  }
+  HT_TRY(orth_all(Q1));
+  for (int m = 0; m < order; ++m) {
+    const int n = static_cast<int>(dims[m]), s = S[m];
+    HT_CUDA(gemm_tn_small_launch(Q1[m], n, Ym[m], n, R1[m], s, s, s, n, c.st));
+    HT_CUDA(nystrom_core_launch(Wm[m], R1[m], s, kNystromShift, Hm[m], c.err, c.st));
+    HT_CUDA(svd_from_gram_launch(Hm[m], s, K[m], K[m], Tm[m], M2[m], Br[m], c.st));
+    HT_CUDA(matmul_nn_launch(Q1[m], n, Tm[m], s, ep[m].U, n, n, K[m], s, c.st));
+    c.launches += 4;
+  }
+  c.ar.off = mark;
+  return HT_OK;
+}
+
 // Buffers of the 3rd-order transfer step (taken before the core pass's scratch).
 struct Transfer3 {
   float *C, *WG, *M, *Bkt, *Broot, *Bt;
@@ -612,18 +762,22 @@ ht_status_t take_transfer3(Ctx &c, const Plan3 &P, Transfer3 &tr) {
 }
 
 // 4. transfer tensors from the core-pass product Z = X_(t) V (3rd order).
+// WG_ready: W^T G_c W is already in tr.WG (the sketch path's TSQR of Z).
 ht_status_t transfer3_from_z(Ctx &c, const Plan3 &P, const long *dims, const EigProblem *ep, const float *Z,
-                             const Transfer3 &tr, Result &res) {
+                             const Transfer3 &tr, Result &res, bool WG_ready = false) {
   const EigProblem &ec = ep[P.mc];
   HT_TRY(core_contract(c, Z, static_cast<int>(dims[P.mp]), static_cast<int>(dims[P.mq]), P.kt, ep[P.mp].U, P.kp,
                        ep[P.mq].U, P.kq, tr.C));
   if (!c.dry()) {
     const int nc = static_cast<int>(dims[P.mc]);
-    HT_CUDA(gemm_tn_small_launch(ec.U, nc, ec.GU, nc, tr.WG, P.kw, P.kw, P.kw, nc, c.st));
+    if (!WG_ready) {
+      HT_CUDA(gemm_tn_small_launch(ec.U, nc, ec.GU, nc, tr.WG, P.kw, P.kw, P.kw, nc, c.st));
+      ++c.launches;
+    }
     HT_CUDA(transfer_eig_launch(tr.WG, P.kw, P.kt, P.kc, 1, tr.M, tr.Bkt, c.st));
     const long long kpq = static_cast<long long>(P.kp) * P.kq;
     HT_CUDA(matmul_nn_launch(tr.C, kpq, tr.M, P.kt, tr.Bt, kpq, kpq, P.kt, P.kt, c.st));
-    c.launches += 3;
+    c.launches += 2;
     if (!P.t_is_left) {
       HT_CUDA(transpose_small_launch(tr.Bkt, P.kt, P.kc, tr.Broot, c.st));
       ++c.launches;
@@ -643,23 +797,31 @@ ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const 
   Plan3 P3{};
   if (d3) P3 = plan3(T);
 
-  // 1. leaf Grams
-  float *G[4] = {};
-  for (int m = 0; m < order; ++m) {
-    G[m] = (G_pre && G_pre[m]) ? G_pre[m] : c.ar.take<float>(static_cast<size_t>(dims[m]) * dims[m]);
-    if (!G[m]) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (Gram)");
-  }
-  for (int m = 0; m < order; ++m) {
-    if (G_pre && G_pre[m]) continue;
-    const View v = view_of_group(dims, order, m, m);
-    if (m == order - 1 && x16t) HT_TRY(gram_transposed(c, v, x32, x16t, lb, G[m]));
-    else HT_TRY(gram(c, v, x32, x16, G[m]));
-  }
-  tl.mark(c.st);
-
+  const bool sketch = cfg.leaf_method == HT_LEAF_SKETCH;
   EigProblem ep[4];
-  HT_TRY(leaf_eigs(c, T, cfg, dims, order, G, ep, res));
-  tl.mark(c.st);
+  if (sketch) {
+    // 1'-2'. leaf bases from the Gram-free range finder (stage "grams" holds
+    // all of it, stage "eig" is empty)
+    HT_TRY(leaf_sketch(c, T, cfg, dims, order, x32, x16, x16t, lb, ep, res));
+    tl.mark(c.st);
+    tl.mark(c.st);
+  } else {
+    // 1. leaf Grams
+    float *G[4] = {};
+    for (int m = 0; m < order; ++m) {
+      G[m] = (G_pre && G_pre[m]) ? G_pre[m] : c.ar.take<float>(static_cast<size_t>(dims[m]) * dims[m]);
+      if (!G[m]) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (Gram)");
+    }
+    for (int m = 0; m < order; ++m) {
+      if (G_pre && G_pre[m]) continue;
+      const View v = view_of_group(dims, order, m, m);
+      if (m == order - 1 && x16t) HT_TRY(gram_transposed(c, v, x32, x16t, lb, G[m]));
+      else HT_TRY(gram(c, v, x32, x16, G[m]));
+    }
+    tl.mark(c.st);
+    HT_TRY(leaf_eigs(c, T, cfg, dims, order, G, ep, res));
+    tl.mark(c.st);
+  }
 
   if (d3) {
     const Plan3 &P = P3;
@@ -669,23 +831,32 @@ ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const 
     Transfer3 tr;
     HT_TRY(take_transfer3(c, P, tr));
     const size_t mark = c.ar.off;
-    float *Z = c.ar.take<float>(static_cast<size_t>(zrows) * P.kt);
+    // the sketch path has no Gram of the complementary mode: Z gets all kw
+    // columns of its basis W and W^T G_c W = Z^T Z comes from the Householder
+    // TSQR of Z (R^T R)
+    const int kz = sketch ? P.kw : P.kt;
+    float *Z = c.ar.take<float>(static_cast<size_t>(zrows) * kz);
     // V enters the BF16 product as high + low BF16 parts (one MMA tile of
     // 2*fold_h columns): rounding V itself to BF16 would tilt every column of
     // Z = X_(t) V by ~2^-9 of X's energy, which dominates the error of nearly
     // exact low-rank inputs.
-    const int fold_h = P.kt <= 32 ? 32 : 64;
+    const int fold_h = kz <= 32 ? 32 : 64;
     __nv_bfloat16 *V16 =
         c.tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(dims[P.mc]) * 2 * fold_h + 64) : nullptr;
-    if (!Z || (c.tc && !V16)) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (core pass)");
-    // 3. core pass: Z = X_(t) V, V = leading kt columns of the complementary leaf's Ritz block
+    float *Rz = sketch ? c.ar.take<float>(static_cast<size_t>(kz) * kz) : nullptr;
+    const size_t qbytes = sketch ? tsqr_workspace_bytes(zrows, kz) : 0;
+    void *qws = sketch ? c.ar.take<char>(qbytes) : nullptr;
+    if (!Z || (c.tc && !V16) || (sketch && (!Rz || !qws)))
+      return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (core pass)");
+    // 3. core pass: Z = X_(t) V, V = leading kz columns of the complementary leaf's basis
     if (V16 && !c.dry()) {
-      HT_CUDA(split_bf16_launch(ec.U, dims[P.mc], P.kt, fold_h, V16, c.st));
+      HT_CUDA(split_bf16_launch(ec.U, dims[P.mc], kz, fold_h, V16, c.st));
       ++c.launches;
     }
-    HT_TRY(mode_product(c, vc, x32, x16, ec.U, V16, P.kt, Z, fold_h));
+    HT_TRY(mode_product(c, vc, x32, x16, ec.U, V16, kz, Z, fold_h));
+    if (sketch && !c.dry()) HT_CUDA(tsqr_launch(Z, zrows, kz, zrows, Rz, tr.WG, qws, qbytes, c.st, &c.launches));
     tl.mark(c.st);
-    HT_TRY(transfer3_from_z(c, P, dims, ep, Z, tr, res));
+    HT_TRY(transfer3_from_z(c, P, dims, ep, Z, tr, res, sketch));
     c.ar.off = mark;
     tl.mark(c.st);
     return HT_OK;
@@ -1513,7 +1684,8 @@ ht_status_t ht_decompose(const float *x, const long *dims, int order, const ht_t
   if (cfg_in) cfg = *cfg_in;
   else ht_config_default(&cfg);
   if (cfg.precision != HT_PREC_FP32 && cfg.precision != HT_PREC_BF16) return fail(HT_ERR_INVALID_ARG, "unknown precision");
-  if (cfg.leaf_method != HT_LEAF_GRAM) return fail(HT_ERR_UNSUPPORTED, "only the Gram leaf method is implemented");
+  if (cfg.leaf_method != HT_LEAF_GRAM && cfg.leaf_method != HT_LEAF_SKETCH)
+    return fail(HT_ERR_INVALID_ARG, "unknown leaf method");
   if (cfg.oversample < 0 || cfg.eig_iters < 0) return fail(HT_ERR_INVALID_ARG, "negative oversample / eig_iters");
   for (int t = 0; t < T.n_nodes; ++t) {
     if (T.leaf(t) && !U[t]) return fail(HT_ERR_INVALID_ARG, "U[t] is NULL for leaf " + std::to_string(t));
@@ -1545,7 +1717,9 @@ ht_status_t ht_decompose_streaming(const float *x, const long *dims, int order, 
   if (cfg_in) cfg = *cfg_in;
   else ht_config_default(&cfg);
   if (cfg.precision != HT_PREC_FP32 && cfg.precision != HT_PREC_BF16) return fail(HT_ERR_INVALID_ARG, "unknown precision");
-  if (cfg.leaf_method != HT_LEAF_GRAM) return fail(HT_ERR_UNSUPPORTED, "only the Gram leaf method is implemented");
+  if (cfg.leaf_method == HT_LEAF_SKETCH)
+    return fail(HT_ERR_UNSUPPORTED, "the streaming path computes leaf Grams; HT_LEAF_SKETCH runs in ht_decompose");
+  if (cfg.leaf_method != HT_LEAF_GRAM) return fail(HT_ERR_INVALID_ARG, "unknown leaf method");
   if (cfg.oversample < 0 || cfg.eig_iters < 0) return fail(HT_ERR_INVALID_ARG, "negative oversample / eig_iters");
   for (int t = 0; t < T.n_nodes; ++t) {
     if (T.leaf(t) && !U[t]) return fail(HT_ERR_INVALID_ARG, "U[t] is NULL for leaf " + std::to_string(t));
@@ -1668,7 +1842,9 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
   if (cfg_in) cfg = *cfg_in;
   else ht_config_default(&cfg);
   if (cfg.precision != HT_PREC_FP32 && cfg.precision != HT_PREC_BF16) return fail(HT_ERR_INVALID_ARG, "unknown precision");
-  if (cfg.leaf_method != HT_LEAF_GRAM) return fail(HT_ERR_UNSUPPORTED, "only the Gram leaf method is implemented");
+  if (cfg.leaf_method == HT_LEAF_SKETCH)
+    return fail(HT_ERR_UNSUPPORTED, "the batched path computes leaf Grams; HT_LEAF_SKETCH runs in ht_decompose");
+  if (cfg.leaf_method != HT_LEAF_GRAM) return fail(HT_ERR_INVALID_ARG, "unknown leaf method");
   if (cfg.oversample < 0 || cfg.eig_iters < 0) return fail(HT_ERR_INVALID_ARG, "negative oversample / eig_iters");
   const bool want_err = (cfg.flags & HT_FLAG_COMPUTE_ERROR) != 0;
   HT_TRY(check_device());
@@ -2247,6 +2423,55 @@ ht_status_t ht_mode_product(const float *x, const long *dims, int order, int lo,
 ht_status_t ht_corange_product(const float *x, const long *dims, int order, int lo, int hi, const float *Q, int k,
                                int precision, float *Z, void *stream) {
   return unfolding_op(2, x, dims, order, lo, hi, Q, k, precision, Z, stream);
+}
+
+ht_status_t ht_tsqr(const float *A, long long m, int k, long long lda, float *R, void *stream) {
+  if (!A || !R) return fail(HT_ERR_INVALID_ARG, "NULL argument");
+  if (m < 1 || k < 1 || lda < m) return fail(HT_ERR_INVALID_ARG, "need m >= 1, k >= 1 and lda >= m");
+  if (k > 64) return fail(HT_ERR_UNSUPPORTED, "k above 64");
+  HT_TRY(check_device());
+  std::lock_guard<std::mutex> lk(g_ws_mutex);
+  const bool a_dev = is_device_ptr(A), r_dev = is_device_ptr(R);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  auto body = [&](Ctx &c) -> ht_status_t {
+    const float *Ad = A;
+    long long ld = lda;
+    if (!a_dev) {
+      float *t = c.ar.take<float>(static_cast<size_t>(m) * k);
+      if (!t) return fail(HT_ERR_OUT_OF_MEMORY, "workspace");
+      if (!c.dry())
+        HT_CUDA(cudaMemcpy2DAsync(t, sizeof(float) * m, A, sizeof(float) * lda, sizeof(float) * m, k,
+                                  cudaMemcpyHostToDevice, c.st));
+      Ad = t;
+      ld = m;
+    }
+    float *Rd = R;
+    if (!r_dev) {
+      Rd = c.ar.take<float>(static_cast<size_t>(k) * k);
+      if (!Rd) return fail(HT_ERR_OUT_OF_MEMORY, "workspace");
+    }
+    const size_t qb = tsqr_workspace_bytes(m, k);
+    void *qws = c.ar.take<char>(qb);
+    if (!qws) return fail(HT_ERR_OUT_OF_MEMORY, "workspace");
+    if (c.dry()) return HT_OK;
+    HT_CUDA(tsqr_launch(Ad, m, k, ld, Rd, nullptr, qws, qb, c.st, &c.launches));
+    if (!r_dev) HT_CUDA(cudaMemcpyAsync(R, Rd, sizeof(float) * k * k, cudaMemcpyDeviceToHost, c.st));
+    HT_CUDA(cudaStreamSynchronize(c.st));
+    HT_CUDA(cudaGetLastError());
+    g_launches += static_cast<unsigned long long>(c.launches);
+    return HT_OK;
+  };
+  Ctx d;
+  d.ar.dry = true;
+  body(d);
+  const size_t bytes = d.ar.peak + (1 << 20);
+  void *ws = nullptr;
+  HT_TRY(acquire_workspace(bytes, &ws, st));
+  Ctx c;
+  c.st = st;
+  c.ar.base = static_cast<char *>(ws);
+  c.ar.cap = bytes;
+  return body(c);
 }
 
 }  // extern "C"

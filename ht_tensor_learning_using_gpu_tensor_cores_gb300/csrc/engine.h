@@ -184,6 +184,22 @@ cudaError_t transfer_eig_launch(const float *WG, int kw, int kt, int kc, int t_i
 cudaError_t svd_from_gram_launch(const float *GW, int s, int k1, int k2, float *M1, float *M2, float *Broot,
                                  cudaStream_t st);
 
+// ------------------------------------------------------- Householder TSQR (tsqr.cu)
+size_t tsqr_workspace_bytes(long long m, int k);
+// R (k x k, column-major, upper triangular, diagonal >= 0) of A = Q R for A
+// (m x k, column-major, leading dimension lda), k <= 64; RtR (optional, may be
+// null) = R^T R in compensated FP32.  ws holds tsqr_workspace_bytes(m, k).
+cudaError_t tsqr_launch(const float *A, long long m, int k, long long lda, float *R, float *RtR, void *ws,
+                        size_t ws_bytes, cudaStream_t st, int *launches);
+
+// ------------------------------------------- Gram-free leaf range finder (sketch.cu)
+// Yn = Y + nu Q (n x s), nu = nu_rel * tr(W) for the s x s matrix W.
+cudaError_t nystrom_shift_launch(const float *Y, const float *Q, long long n, int s, const float *W, float nu_rel,
+                                 float *Yn, cudaStream_t st);
+// H (s x s) = R1 (sym(W) + nu I)^-1 R1^T, nu as above (FP64, one CTA).
+cudaError_t nystrom_core_launch(const float *W, const float *R1, int s, float nu_rel, float *H, int *err,
+                                cudaStream_t st);
+
 // ------------------------------------------------------- learned sketch (learn.cu)
 size_t sketch_workspace_bytes(int batch, int n, int s);
 // loss[b] and the batch-mean gradient of L(S) = mean_b [1 - tr(Q_b^T G_b Q_b) / tr(G_b)],

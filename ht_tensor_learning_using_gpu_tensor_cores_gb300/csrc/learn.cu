@@ -14,12 +14,14 @@
 //
 // Its adjoint through CholeskyQR (dC, dH back to dY, then dS = G dY):
 //
-//   dL/dS = -(2 / B) sum_b G_b E_b C_b^-1 / tr(G_b),   E = G Y - Y C^-1 H = (I - Q Q^T) G Q R.
+//   dL/dS = -(2 / B) sum_b G_b E_b C_b^-1 / tr(G_b),   E = G Y - Y C^-1 H = (I - Q Q^T) G Q R,
+//         = -(2 / B) sum_b G_b (I - Q_b Q_b^T) G_b Q_b R_b^-T / tr(G_b).
 //
-// Kernels: a batched n x n by n x s product (FP32, the three large products),
-// a per-Gram kernel for the s x s algebra (C and H accumulated in FP64, FP64
-// Cholesky and solves, E formed in FP64), and a deterministic batch reduction
-// of the gradient, plus an Adam step.  The reference has no learned component;
+// Kernels: a batched n x n by n x s product (FP32, the three large products
+// Y = G S, P = G Q, G E), a per-Gram factor kernel (C in FP64, the
+// column-dropping Cholesky, R^-1 and Q = Y R^-1 in FP64), a per-Gram loss
+// kernel (H = Q^T P, E = P - Q H in FP64), a deterministic batch reduction of
+// the gradient, plus an Adam step.  The reference has no learned component;
 // the Gaussian start block it would use (the rsvd test matrix,
 // 3D/Opt/kernel.cu:595-680) is what the learned sketch replaces.
 #include "common.cuh"
@@ -110,88 +112,94 @@ __device__ void ls_cholesky(double *A, int s, int *keep, double *d0, int *s_bad)
   }
 }
 
-// Per Gram b: C = Y^T Y, H = Y^T P (FP64 accumulation), X = C_KK^-1 H_KK on the
-// kept columns K (zero rows and columns elsewhere), loss_b = 1 - tr(X) / trG_b,
-// E = P - Y X, and Ci = C_KK^-1 (FP64, zero outside K) for the gradient.  One
-// CTA per Gram.
-__global__ void __launch_bounds__(256) ls_small_kernel(const float *__restrict__ Y, const float *__restrict__ P,
-                                                       const float *__restrict__ trG, int n, int s,
-                                                       float *__restrict__ E, double *__restrict__ Ci,
-                                                       double *__restrict__ loss, int *__restrict__ bad) {
+// Per Gram b: C = Y^T Y (FP64 accumulation), the column-dropping Cholesky
+// C_KK = R^T R, Rinv = R^-1 (FP64, zero outside K) and the orthonormal basis
+// Q = Y Rinv (FP64 sums, stored FP32; dropped columns zero).  Forming Q keeps
+// the loss well conditioned: tr(Q^T G Q) from a fresh product G Q cannot
+// exceed tr(G), whereas tr(C^-1 Y^T G Y) carries the rounding of G Y through
+// C^-1.  One CTA per Gram.
+__global__ void __launch_bounds__(256) ls_factor_kernel(const float *__restrict__ Y, int n, int s,
+                                                        float *__restrict__ Q, double *__restrict__ Rinv,
+                                                        int *__restrict__ bad) {
   extern __shared__ double ls_sm[];
-  double *C = ls_sm;                        // LS_MAX x LS_MAX
-  double *W = ls_sm + LS_MAX * LS_MAX;      // H, then X = C^-1 H
+  double *C = ls_sm;                        // LS_MAX x LS_MAX: C, then R (upper triangle)
+  double *Ri = ls_sm + LS_MAX * LS_MAX;     // LS_MAX x LS_MAX: R^-1
   __shared__ int s_bad;
   __shared__ int keep[LS_MAX];
   __shared__ double d0[LS_MAX];
   const int b = blockIdx.x, t = threadIdx.x;
   const float *Yb = Y + static_cast<long long>(b) * n * s;
-  const float *Pb = P + static_cast<long long>(b) * n * s;
   for (int e = t; e < s * s; e += 256) {
     const int i = e / s, j = e % s;
-    double c = 0.0, h = 0.0;
-    for (int r = 0; r < n; ++r) {
-      const double yi = Yb[r + static_cast<long long>(n) * i];
-      c = fma(yi, static_cast<double>(Yb[r + static_cast<long long>(n) * j]), c);
-      h = fma(yi, static_cast<double>(Pb[r + static_cast<long long>(n) * j]), h);
-    }
+    double c = 0.0;
+    for (int r = 0; r < n; ++r)
+      c = fma(static_cast<double>(Yb[r + static_cast<long long>(n) * i]),
+              static_cast<double>(Yb[r + static_cast<long long>(n) * j]), c);
     C[i * LS_MAX + j] = c;
-    W[i * LS_MAX + j] = h;
   }
   __syncthreads();
   ls_cholesky(C, s, keep, d0, &s_bad);
   if (s_bad && t == 0) atomicOr(bad, 1);
-  // X = R^-1 R^-T H on K: forward substitution with R^T, then back substitution
-  // with R (column per thread); dropped rows and columns are zero
+  // R^-1, column j by thread j (back substitution; zero rows/columns off K)
   for (int j = t; j < s; j += 256) {
-    for (int i = 0; i < s; ++i) {   // R^T z = h
-      double v = (keep[i] && keep[j]) ? W[i * LS_MAX + j] : 0.0;
-      if (keep[i])
-        for (int k = 0; k < i; ++k) v -= C[k * LS_MAX + i] * W[k * LS_MAX + j];
-      W[i * LS_MAX + j] = keep[i] ? v / C[i * LS_MAX + i] : 0.0;
-    }
-    for (int i = s - 1; i >= 0; --i) {   // R x = z
-      double v = W[i * LS_MAX + j];
-      if (keep[i])
-        for (int k = i + 1; k < s; ++k) v -= C[i * LS_MAX + k] * W[k * LS_MAX + j];
-      W[i * LS_MAX + j] = keep[i] ? v / C[i * LS_MAX + i] : 0.0;
+    for (int i = s - 1; i >= 0; --i) {
+      double v = (i == j) ? 1.0 : 0.0;
+      if (keep[i] && keep[j]) {
+        for (int k = i + 1; k <= j; ++k) v -= C[i * LS_MAX + k] * Ri[k * LS_MAX + j];
+        v /= C[i * LS_MAX + i];
+      } else {
+        v = 0.0;
+      }
+      Ri[i * LS_MAX + j] = v;
     }
   }
   __syncthreads();
-  // C_KK^-1 = R^-1 R^-T on K, column j by thread j
-  double *Cib = Ci + static_cast<long long>(b) * LS_MAX * LS_MAX;
-  for (int j = t; j < s; j += 256) {
-    double z[LS_MAX];
-    for (int i = 0; i < s; ++i) {   // R^T z = e_j
-      double v = (i == j && keep[j]) ? 1.0 : 0.0;
-      if (keep[i])
-        for (int k = 0; k < i; ++k) v -= C[k * LS_MAX + i] * z[k];
-      z[i] = keep[i] ? v / C[i * LS_MAX + i] : 0.0;
-    }
-    for (int i = s - 1; i >= 0; --i) {   // R x = z
-      double v = z[i];
-      if (keep[i])
-        for (int k = i + 1; k < s; ++k) v -= C[i * LS_MAX + k] * Cib[k * LS_MAX + j];
-      Cib[i * LS_MAX + j] = keep[i] ? v / C[i * LS_MAX + i] : 0.0;
-    }
+  double *Rb = Rinv + static_cast<long long>(b) * LS_MAX * LS_MAX;
+  for (int e = t; e < LS_MAX * LS_MAX; e += 256) Rb[e] = Ri[e];
+  float *Qb = Q + static_cast<long long>(b) * n * s;
+  for (int e = t; e < n * s; e += 256) {
+    const int r = e % n, j = e / n;
+    double v = 0.0;
+    for (int k = 0; k <= j; ++k) v = fma(static_cast<double>(Yb[r + static_cast<long long>(n) * k]), Ri[k * LS_MAX + j], v);
+    Qb[e] = static_cast<float>(v);
   }
+}
+
+// Per Gram b, with P = G Q: H = Q^T P (FP64), loss_b = 1 - tr(H) / trG_b and
+// E = P - Q H (the part of G Q outside span(Q)).  One CTA per Gram.
+__global__ void __launch_bounds__(256) ls_loss_kernel(const float *__restrict__ Q, const float *__restrict__ P,
+                                                      const float *__restrict__ trG, int n, int s,
+                                                      float *__restrict__ E, double *__restrict__ loss) {
+  __shared__ double H[LS_MAX * LS_MAX];
+  const int b = blockIdx.x, t = threadIdx.x;
+  const float *Qb = Q + static_cast<long long>(b) * n * s;
+  const float *Pb = P + static_cast<long long>(b) * n * s;
+  for (int e = t; e < s * s; e += 256) {
+    const int i = e / s, j = e % s;
+    double h = 0.0;
+    for (int r = 0; r < n; ++r)
+      h = fma(static_cast<double>(Qb[r + static_cast<long long>(n) * i]),
+              static_cast<double>(Pb[r + static_cast<long long>(n) * j]), h);
+    H[i * LS_MAX + j] = h;
+  }
+  __syncthreads();
   if (t == 0) {
     double tr = 0.0;
-    for (int i = 0; i < s; ++i) tr += W[i * LS_MAX + i];
+    for (int i = 0; i < s; ++i) tr += H[i * LS_MAX + i];
     loss[b] = 1.0 - tr / static_cast<double>(trG[b]);
   }
-  // E = P - Y X (columns outside K are multiplied by zero rows of Ci later)
   float *Eb = E + static_cast<long long>(b) * n * s;
   for (int e = t; e < n * s; e += 256) {
     const int r = e % n, j = e / n;
     double v = Pb[r + static_cast<long long>(n) * j];
-    for (int k = 0; k < s; ++k) v -= static_cast<double>(Yb[r + static_cast<long long>(n) * k]) * W[k * LS_MAX + j];
+    for (int k = 0; k < s; ++k) v -= static_cast<double>(Qb[r + static_cast<long long>(n) * k]) * H[k * LS_MAX + j];
     Eb[e] = static_cast<float>(v);
   }
 }
 
-// grad[r, j] = -(2 / B) sum_b (1 / trG_b) sum_k GE_b[r, k] Ci_b[k, j], batch summed in order.
-__global__ void __launch_bounds__(256) ls_grad_kernel(const float *__restrict__ GE, const double *__restrict__ Ci,
+// grad[r, j] = -(2 / B) sum_b (1 / trG_b) sum_k GE_b[r, k] Rinv_b[j, k], batch
+// summed in order (dL/dS = -(2 / tr G) G (I - Q Q^T) G Q R^-T).
+__global__ void __launch_bounds__(256) ls_grad_kernel(const float *__restrict__ GE, const double *__restrict__ Rinv,
                                                       const float *__restrict__ trG, int batch, int n, int s,
                                                       float *__restrict__ grad) {
   const long long e = blockIdx.x * 256ll + threadIdx.x;
@@ -200,9 +208,9 @@ __global__ void __launch_bounds__(256) ls_grad_kernel(const float *__restrict__ 
   double acc = 0.0;
   for (int b = 0; b < batch; ++b) {
     const float *GEb = GE + static_cast<long long>(b) * n * s;
-    const double *Cib = Ci + static_cast<long long>(b) * LS_MAX * LS_MAX;
+    const double *Rb = Rinv + static_cast<long long>(b) * LS_MAX * LS_MAX;
     double v = 0.0;
-    for (int k = 0; k < s; ++k) v = fma(static_cast<double>(GEb[r + static_cast<long long>(n) * k]), Cib[k * LS_MAX + j], v);
+    for (int k = j; k < s; ++k) v = fma(static_cast<double>(GEb[r + static_cast<long long>(n) * k]), Rb[j * LS_MAX + k], v);
     acc += v / static_cast<double>(trG[b]);
   }
   grad[e] = static_cast<float>(-2.0 * acc / batch);
@@ -225,7 +233,7 @@ __global__ void ls_adam_kernel(float *__restrict__ S, const float *__restrict__ 
 
 size_t sketch_workspace_bytes(int batch, int n, int s) {
   const size_t ns = static_cast<size_t>(n) * s * batch;
-  return 4 * ns * sizeof(float) + static_cast<size_t>(batch) * LS_MAX * LS_MAX * sizeof(double) +
+  return 5 * ns * sizeof(float) + static_cast<size_t>(batch) * LS_MAX * LS_MAX * sizeof(double) +
          static_cast<size_t>(batch) * sizeof(double) + 256;
 }
 
@@ -233,22 +241,23 @@ cudaError_t sketch_loss_grad(const float *G, const float *trG, int batch, int n,
                              double *loss, int *bad, void *ws, cudaStream_t st, int *launches) {
   if (s < 1 || s > LS_MAX || n < s || batch < 1) return cudaErrorInvalidValue;
   const size_t ns = static_cast<size_t>(n) * s * batch;
-  float *Y = static_cast<float *>(ws), *P = Y + ns, *E = P + ns, *GE = E + ns;
-  double *Ci = reinterpret_cast<double *>(GE + ns);
+  float *Y = static_cast<float *>(ws), *Q = Y + ns, *P = Q + ns, *E = P + ns, *GE = E + ns;
+  double *Rinv = reinterpret_cast<double *>(GE + ns);
   const dim3 grid((n + LT_ROWS - 1) / LT_ROWS, batch);
-  ls_bgemm_kernel<<<grid, 256, 0, st>>>(G, S, 0, Y, n, s);                                   // Y = G S
-  ls_bgemm_kernel<<<grid, 256, 0, st>>>(G, Y, static_cast<long long>(n) * s, P, n, s);       // P = G Y
   static bool attr_set[64] = {};
-  constexpr int kSmallSmem = 2 * LS_MAX * LS_MAX * sizeof(double);
+  constexpr int kFactorSmem = 2 * LS_MAX * LS_MAX * sizeof(double);
   {
-    const cudaError_t e = opt_in_smem(ls_small_kernel, kSmallSmem, attr_set);
+    const cudaError_t e = opt_in_smem(ls_factor_kernel, kFactorSmem, attr_set);
     if (e != cudaSuccess) return e;
   }
-  ls_small_kernel<<<batch, 256, kSmallSmem, st>>>(Y, P, trG, n, s, E, Ci, loss, bad);     // E, C^-1, loss
+  ls_bgemm_kernel<<<grid, 256, 0, st>>>(G, S, 0, Y, n, s);                                   // Y = G S
+  ls_factor_kernel<<<batch, 256, kFactorSmem, st>>>(Y, n, s, Q, Rinv, bad);                 // Q = Y R^-1
+  ls_bgemm_kernel<<<grid, 256, 0, st>>>(G, Q, static_cast<long long>(n) * s, P, n, s);       // P = G Q
+  ls_loss_kernel<<<batch, 256, 0, st>>>(Q, P, trG, n, s, E, loss);                          // loss, E
   ls_bgemm_kernel<<<grid, 256, 0, st>>>(G, E, static_cast<long long>(n) * s, GE, n, s);      // G E
   const long long cnt = static_cast<long long>(n) * s;
-  ls_grad_kernel<<<static_cast<int>((cnt + 255) / 256), 256, 0, st>>>(GE, Ci, trG, batch, n, s, grad);
-  if (launches) *launches += 5;
+  ls_grad_kernel<<<static_cast<int>((cnt + 255) / 256), 256, 0, st>>>(GE, Rinv, trG, batch, n, s, grad);
+  if (launches) *launches += 6;
   return cudaGetLastError();
 }
 

@@ -53,7 +53,13 @@ typedef enum {
 
 typedef enum {
     HT_LEAF_GRAM = 0,   /* leaf bases from the mode Gram X_(t) X_(t)^T               */
-    HT_LEAF_SKETCH = 1  /* leaf bases from a randomized range finder on X_(t)        */
+    HT_LEAF_SKETCH = 1  /* leaf bases from a randomized range finder on X_(t) that
+                           never forms the Gram: test matrix X_(t)^T S for a per-mode
+                           block S (n_t x (k_t + oversample): sketch[t] or Gaussian),
+                           power_steps applications of X_(t) X_(t)^T as two streaming
+                           products each, CholeskyQR2 between them, a Nystrom core
+                           for the leaf basis; 3rd order: the interior node from the
+                           Householder TSQR of X_(t) V (ht_decompose only)          */
 } ht_leaf_method_t;
 
 /* Flags */
@@ -78,7 +84,9 @@ typedef struct {
     int power_steps;      /* power steps of the range finder (default 1)         */
     unsigned long long seed;  /* Gaussian start / test matrices (default 1234)   */
     const float *sketch[HT_MAX_ORDER]; /* optional start matrices per mode, n_m x (k+p),
-                                          column-major, host or device; NULL = Gaussian */
+                                          column-major, host or device; NULL = Gaussian.
+                                          HT_LEAF_GRAM: the eigen-solver's start block;
+                                          HT_LEAF_SKETCH: the range finder's block S   */
     int flags;            /* HT_FLAG_*                                           */
     double eig_tol;       /* residual tolerance reported as HT_ERR_NOT_CONVERGED
                              when exceeded (0 = do not check)                    */
@@ -182,6 +190,18 @@ ht_status_t ht_mode_product(const float *x, const long *dims, int order, int lo,
                             int precision, float *Z, void *stream);
 ht_status_t ht_corange_product(const float *x, const long *dims, int order, int lo, int hi, const float *Q, int k,
                                int precision, float *Z, void *stream);
+
+/* R factor of A = Q R for a tall-skinny A (m x k, column-major, leading
+ * dimension lda >= m, 1 <= k <= 64) by Householder TSQR on the GPU: every
+ * row block folded into per-warp R factors with Householder reflections
+ * (warp-shuffle reductions), the warps' factors combined in a shared-memory
+ * tree and the CTAs' in a fan-in-8 tree across the grid, in one launch.
+ * Replaces the reference's tsqr_svd / tsqr_svd_half row-block QR
+ * (third_order_tensor_decompsition/CUDA/TSQR/kernel.cu:500-949, geqrf at
+ * :326-350), which factors four host-split blocks with cuSOLVER.
+ * R (k x k, column-major) is upper triangular with a non-negative diagonal.
+ * A and R may be host or device memory; returns after R is written. */
+ht_status_t ht_tsqr(const float *A, long long m, int k, long long lda, float *R, void *stream);
 
 /* ht_mode_gram_noalloc: the FP32 mode Gram G (N x N) = X_(g) X_(g)^T with no
  * memory allocation at all.  It has no counterpart in the reference.

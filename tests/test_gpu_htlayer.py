@@ -136,9 +136,10 @@ def test_backward_matches_autograd(N, M, r, batch, prec):
     for name, got, want in zip(("u1", "u2", "u3", "b2", "b1"), gr, gf):
         assert got.shape == want.shape
         assert rel(got.cpu().numpy(), want.numpy()) <= 1e-4, name
-    # dbias = column sums of dy in FP32 on both paths
+    # dbias = column sums of the FP32 dy on both paths
     assert rel(dbias.cpu().numpy(), dy.sum(0).numpy()) <= 1e-5
-    assert rel(dbias.cpu().numpy(), gb.reshape(-1).numpy()) <= 1e-5
+    if prec == "fp32":
+        assert rel(dbias.cpu().numpy(), gb.reshape(-1).numpy()) <= 1e-5
 
 
 def test_autograd_module_trains():
