@@ -19,7 +19,9 @@ numpy restatement of the reference's HT_TensorLy.py on the host cores.
 
 --impl reference: times the reference's CPU implementation of the path (the
 numpy port of HT_TensorLy.py; the Python statement itself needs tensorly and
-torch.eig, neither available) on this machine's host cores.
+torch.eig, neither available) on this machine's host cores, on the full
+1024^3 tensor (one decomposition, a few minutes; the line's `steps` counts the
+full-size decompositions timed).
 """
 from __future__ import annotations
 
@@ -127,57 +129,91 @@ def allmax(v, world):
 
 
 # ------------------------------------------------------------------ CPU leg
-def cpu_baseline(sample_n=CPU_SAMPLE_N, reps=1):
-    """The reference's CPU path (numpy port of HT_TensorLy.py, FP32, timed region
-    = decomposition + reconstruction + error as in the Python statement) on a
-    sample_n^3 tensor of the same family, scaled by (N/sample_n)^4 -- the
-    operation count of the Gram GEMMs and the n^2 x n SVD -- to the full size."""
-    import numpy as np
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import ht_oracle as O
-    from ht_tensor_learning_using_gpu_tensor_cores_gb300 import synth, tree as T
-    X = synth.odeco(sample_n, decay=DECAY, seed=1)
-    tr = T.reference_tree_3d([1, RANK, RANK, RANK, RANK])
-    times = []
-    for _ in range(reps):
-        t0 = time.perf_counter()
-        U, B, _ = O.ht_decompose(X, tr, dtype=np.float32)
-        err = O.ht_error(X, tr, U, B)
-        times.append(time.perf_counter() - t0)
-    t = min(times)
-    scale = (N_FULL / sample_n) ** 4
+def blas_info():
+    """(threads, BLAS library) numpy uses: threadpoolctl when present, else
+    numpy's build configuration and the host's core count."""
     try:
         import threadpoolctl
         info = threadpoolctl.threadpool_info()
         threads = max((i.get("num_threads", 1) for i in info), default=os.cpu_count())
-        blas = ",".join(sorted({i.get("internal_api", "?") for i in info}))
+        blas = ",".join(sorted({f"{i.get('internal_api', '?')} {i.get('version', '')}".strip() for i in info}))
+        return int(threads), blas
     except Exception:
-        threads, blas = os.cpu_count(), "unknown"
-    return {"value": t * scale * 1e3, "unit": "ms", "cores": int(threads), "kind": "port",
-            "sample": f"full FP32 decomposition+reconstruction+error of a {sample_n}^3 tensor of the same family "
-                      f"(numpy port of HT_TensorLy.py), {t:.2f} s measured, scaled x{scale:.0f} by the n^4 "
-                      f"operation count to {N_FULL}^3",
-            "blas": blas, "sample_seconds": t, "sample_err": err}
+        pass
+    try:
+        import numpy as np
+        b = np.show_config(mode="dicts")["Build Dependencies"]["blas"]
+        blas = f"{b.get('name', '?')} {b.get('version', '')}".strip()
+    except Exception:
+        blas = "unknown"
+    threads = int(os.environ.get("OPENBLAS_NUM_THREADS", os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)))
+    return threads, blas
+
+
+def cpu_decompose(n):
+    """The reference's CPU path, the numpy port of HT_TensorLy.py (FP32: leaf
+    Grams + eigh, SVD of the n^2 x n unfolding for node {1,2}, transfer
+    contractions), on an n^3 tensor of the headline family.  Timed region: the
+    decomposition, X -> (U_t, B_t), the region the GPU headline times.
+    Returns (seconds, rel_err or None); the error pass runs after the timed
+    region and only for n <= 512 (the full-size reconstruction would double
+    the CPU time)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ht_oracle as O
+    from ht_tensor_learning_using_gpu_tensor_cores_gb300 import synth, tree as T
+    X = synth.odeco(n, decay=DECAY, seed=1)
+    tr = T.reference_tree_3d([1, RANK, RANK, RANK, RANK])
+    t0 = time.perf_counter()
+    U, B, _ = O.ht_decompose(X, tr, dtype=np.float32)
+    t = time.perf_counter() - t0
+    err = O.ht_error(X, tr, U, B) if n <= 512 else None
+    return t, err
+
+
+def cpu_baseline(sample_n=CPU_SAMPLE_N):
+    """Bounded sample for the GPU line: the CPU path on a sample_n^3 tensor of the
+    same family, scaled by (N/sample_n)^4 (the operation count of the Gram GEMMs
+    and of the n^2 x n SVD) to the full size.  The reference arm
+    (--impl reference) measures the full size instead."""
+    t, err = cpu_decompose(sample_n)
+    scale = (N_FULL / sample_n) ** 4
+    threads, blas = blas_info()
+    return {"value": t * scale * 1e3, "unit": "ms", "cores": threads, "kind": "port",
+            "sample": f"FP32 decomposition of a {sample_n}^3 tensor of the same family (numpy port of "
+                      f"HT_TensorLy.py), {t:.2f} s measured, scaled x{scale:.0f} by the n^4 operation count to "
+                      f"{N_FULL}^3 (extrapolated; --impl reference measures {N_FULL}^3)",
+            "blas": blas, "sample_seconds": t, "sample_err": err, "extrapolated": True}
 
 
 def run_reference(args, world, rank):
+    """The reference's CPU implementation at the benchmark configuration itself:
+    one full 1024^3 rank-32 decomposition (a few minutes of host time), after
+    `warmup` untimed runs on a 64^3 sample (imports, BLAS thread pools).  Each
+    full-size run is one step; --ref-steps sets how many (default 1, so the
+    whole run stays within a few minutes); the line's `steps` is the number
+    actually timed."""
     if rank != 0:
         return
-    # warm-up: the same path on a small sample (imports, BLAS thread pools), untimed
     for _ in range(max(0, args.warmup)):
-        cpu_baseline(min(64, args.cpu_sample), reps=1)
-    vals = []
-    cb = None
-    for _ in range(max(1, args.steps)):
-        cb = cpu_baseline(args.cpu_sample, reps=1)
-        vals.append(cb["value"])
-    v = statistics.median(vals)
-    cb["value"] = v
+        cpu_decompose(64)
+    n = args.ref_n
+    secs = []
+    for _ in range(max(1, args.ref_steps)):
+        t, _ = cpu_decompose(n)
+        secs.append(t)
+    v = statistics.median(secs) * 1e3
+    threads, blas = blas_info()
+    cb = {"value": v, "unit": "ms", "cores": threads, "kind": "port",
+          "sample": f"{len(secs)} full FP32 decomposition(s) of the {n}^3 rank-{RANK} tensor (numpy port of "
+                    f"HT_TensorLy.py), measured, not scaled",
+          "blas": blas, "seconds": secs}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"HT decomposition {N_FULL}^3 rank {RANK}, reference tree, r^-1.5 spectrum",
-                       "path": "numpy port of HT_TensorLy.py on host cores"},
+            "steps": len(secs), "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": v,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"HT decomposition {n}^3 rank {RANK}, reference tree, r^-1.5 spectrum",
+                       "path": "numpy port of HT_TensorLy.py on host cores",
+                       "timed_region": "decomposition X -> (U_t, B_t), as the GPU headline"},
             "cpu_baseline": cb, "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -527,6 +563,37 @@ def run_ours(args, world, rank, local):
     d2h = sum(int(np.asarray(a).nbytes) for a in list(res_h.U.values()) + list(res_h.B.values()))
     h2d = n * n * n * 4
 
+    # ---- Gram-free leaf range finder (HT_LEAF_SKETCH) on the same tensor: the
+    # configuration's oversampling 10 and one power step, BF16 products
+    sk_kw = {"leaf_method": "sketch", "oversample": 10, "power_steps": 1}
+    sk_res = ht.decompose(X, tree, precision="bf16", compute_error=True, **sk_kw)
+    for _ in range(max(3, args.warmup)):
+        ht.decompose(X, tree, precision="bf16", **sk_kw)
+    torch.cuda.synchronize()
+    sk_steps = max(1, min(args.steps, 10))
+    sk_stage = []
+    ev0.record(stream)
+    for _ in range(sk_steps):
+        sk_stage.append(ht.decompose(X, tree, precision="bf16", **sk_kw).report["ms_stage"])
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms_sketch = ev0.elapsed_time(ev1) / sk_steps
+
+    # ---- leaf principal angles against the exact subspaces (the family's
+    # leading factor columns, closed form), per path
+    A_true, _ = synth.odeco_factors(n, 3, DECAY, seed=1 + rank)
+
+    def max_angles(res):
+        out = {}
+        for t in tree.leaves():
+            m = tree.modes[t][0]
+            At = torch.as_tensor(A_true[m][:, :k], dtype=torch.float64, device=X.device)
+            sv = torch.linalg.svdvals(At.T @ res.U[t].double())
+            out[f"mode{m}"] = float(torch.arccos(sv.clamp(max=1.0)).max())
+        return out
+
+    angles = {"mixed": max_angles(mixed), "plain_fp32": max_angles(plain), "sketch": max_angles(sk_res)}
+
     # ---- the other single-tensor configurations (not the headline): c1 and c3
     others = secondary_configs(ht, synth, torch, stream) if rank == 0 else None
 
@@ -571,6 +638,20 @@ def run_ours(args, world, rank, local):
                          "issued_note": "tcgen05 work actually issued: the upper triangle of 256 x 256 tiles, "
                                         "diagonal tiles in full",
                          "peak_source": pk["source"] + " bf16 burst"},
+            "leaf_principal_angles_rad": angles,
+            "sketch_path": {
+                "what": "leaf bases from the Gram-free range finder (block width k+10, one power step, Nystrom "
+                        "core), interior node from the Householder TSQR of X_(12) V; BF16 products",
+                "ms": ms_sketch, "rel_err": sk_res.report["rel_err"],
+                "rel_err_minus_fp64": sk_res.report["rel_err"] - e_opt,
+                "speedup_vs_plain_fp32": ms_plain / ms_sketch,
+                "stage_ms": {kk: statistics.median([s_[kk] for s_ in sk_stage]) for kk in sk_stage[0]},
+                "streaming_products": 12,
+                "products_GBps": 12 * 2.0 * float(n) ** 3 / (statistics.median([s_["grams"] for s_ in sk_stage])
+                                                              * 1e-3) / 1e9,
+                "products_GBps_note": "12 passes over BF16 X (2 applications of X X^T per mode, 2 products each) "
+                                      "over the whole range-finder stage, CholeskyQR and Nystrom included",
+                "hbm_peak_GBps": pk["hbm_gbs"]},
             "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
             "other_configs": others,
         }
@@ -586,7 +667,9 @@ def main():
     ap.add_argument("--n", type=int, default=N_FULL)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE_N,
-                    help="edge of the cubic sample the CPU path decomposes (its time is scaled by n^4 to 1024^3)")
+                    help="edge of the cubic sample the GPU line's CPU baseline decomposes (scaled by n^4 to 1024^3)")
+    ap.add_argument("--ref-n", type=int, default=N_FULL, help="--impl reference: edge of the decomposed tensor")
+    ap.add_argument("--ref-steps", type=int, default=1, help="--impl reference: full-size decompositions timed")
     ap.add_argument("--mixed-only", action="store_true",
                     help="run only the headline mixed-path steps (for profiler launch lists)")
     ap.add_argument("--fourth-order-only", action="store_true",

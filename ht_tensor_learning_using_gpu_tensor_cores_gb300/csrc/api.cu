@@ -672,10 +672,6 @@ ht_status_t leaf_sketch(Ctx &c, const Tree &T, const ht_config_t &cfg, const lon
   const size_t cbytes = eig_workspace_bytes(cq, order);
   void *cws = c.ar.take<char>(cbytes);
   if (!cws) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (sketch CholeskyQR)");
-  if (c.dry()) {
-    c.ar.off = mark;
-    return HT_OK;
-  }
   auto orth_all = [&](float *const *M) -> ht_status_t {   // CholeskyQR2 of every mode's block, one launch
     for (int m = 0; m < order; ++m) {
       cq[m].Q = M[m];
@@ -690,12 +686,12 @@ ht_status_t leaf_sketch(Ctx &c, const Tree &T, const ht_config_t &cfg, const lon
     const View v = view_of_group(dims, order, m, m);
     const long long LR = v.L * v.R;
     const int s = S[m], h = s <= 32 ? 32 : 64;
-    if (c.tc) {
+    if (c.tc && !c.dry()) {
       HT_CUDA(split_bf16_launch(Qsrc, dims[m], s, h, Q16, c.st));
       ++c.launches;
     }
     HT_TRY(mode_product(c, v, x32, x16, Qsrc, Q16, s, Z32, c.tc ? h : 0));
-    if (c.tc) {
+    if (c.tc && !c.dry()) {
       HT_CUDA(f32_to_bf16_launch(Z32, Z16, LR * s, c.st));
       ++c.launches;
     }
@@ -706,6 +702,11 @@ ht_status_t leaf_sketch(Ctx &c, const Tree &T, const ht_config_t &cfg, const lon
     }
     return corange_product(c, v, x32, x16, Z32, Z16, s, Ydst);
   };
+  if (c.dry()) {   // size the products' split-K scratch
+    for (int m = 0; m < order; ++m) HT_TRY(apply_gram(m, Qm[m], Ym[m]));
+    c.ar.off = mark;
+    return HT_OK;
+  }
   // start blocks
   for (int m = 0; m < order; ++m) {
     const size_t ns = static_cast<size_t>(dims[m]) * S[m];

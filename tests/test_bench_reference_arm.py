@@ -1,6 +1,7 @@
 """The reference arm of bench.py (the numpy port of the reference's CPU path on
 the host cores) prints one JSON line with the keys the benchmark contract asks
-for.  Runs on a 48^3 sample so that it finishes in seconds without a GPU."""
+for.  Runs with a 48^3 tensor (--ref-n) so that it finishes in seconds without a
+GPU; by default the arm decomposes the full 1024^3 tensor."""
 import json
 import os
 import subprocess
@@ -11,7 +12,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def test_reference_arm_json_line():
     out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "2",
-                          "--warmup", "1", "--cpu-sample", "48"], capture_output=True, text=True, timeout=300,
+                          "--warmup", "1", "--ref-n", "48", "--ref-steps", "2"], capture_output=True, text=True, timeout=300,
                          cwd=ROOT)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
@@ -21,9 +22,9 @@ def test_reference_arm_json_line():
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
                 "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert key in d, key
-    assert d["steps"] == 2 and d["warmup"] == 1 and d["n_gpus"] == 1
+    assert d["steps"] == 2 and d["steps_requested"] == 2 and d["warmup"] == 1 and d["n_gpus"] == 1
     assert d["higher_is_better"] is False and d["unit"] == "ms" and d["value"] > 0
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
-    assert "48^3" in cb["sample"]
+    assert "48^3" in cb["sample"] and len(cb["seconds"]) == 2 and cb["blas"]
     assert d["e2e"] == {"value": d["value"], "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
