@@ -2426,6 +2426,27 @@ ht_status_t ht_corange_product(const float *x, const long *dims, int order, int 
   return unfolding_op(2, x, dims, order, lo, hi, Q, k, precision, Z, stream);
 }
 
+ht_status_t ht_selftest_wait_timeout(int ctas, double limit_ms, void *stream) {
+  if (ctas < 1 || !(limit_ms > 0.0) || limit_ms > 2000.0)
+    return fail(HT_ERR_INVALID_ARG, "need ctas >= 1 and 0 < limit_ms <= 2000");
+  HT_TRY(check_device());
+  if (ctas > sm_count()) return fail(HT_ERR_INVALID_ARG, "ctas above the device's multiprocessor count");
+  std::lock_guard<std::mutex> lk(g_ws_mutex);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  void *ws = nullptr;
+  HT_TRY(acquire_workspace(1 << 20, &ws, st));
+  int *err = reinterpret_cast<int *>(static_cast<char *>(ws) + 256);
+  HT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+  HT_CUDA(wait_probe_launch(ctas, static_cast<uint64_t>(limit_ms * 1e6), ws, err, st));
+  int h = 0;
+  HT_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  HT_CUDA(cudaStreamSynchronize(st));
+  HT_CUDA(cudaGetLastError());
+  ++g_launches;
+  if (h & kErrTimeout) return fail(HT_ERR_TIMEOUT, "the probe's grid barrier wait ran out, as intended");
+  return fail(HT_ERR_CUDA, "the probe's wait did not report a timeout");
+}
+
 ht_status_t ht_tsqr(const float *A, long long m, int k, long long lda, float *R, void *stream) {
   if (!A || !R) return fail(HT_ERR_INVALID_ARG, "NULL argument");
   if (m < 1 || k < 1 || lda < m) return fail(HT_ERR_INVALID_ARG, "need m >= 1, k >= 1 and lda >= m");

@@ -429,8 +429,8 @@ constexpr size_t kCoopSmem =
     sizeof(float) * (SMAX * SMAX + SMAX + 2 * RBMAX * SMAX + (kCoopRing > kCoopAlias ? kCoopRing : kCoopAlias)) + 64;
 
 // Bounded grid barrier over the first `members` CTAs.  False (and the error
-// word set) when the wait ran past the limit; the caller then returns.
-HT_DEV bool grid_barrier(unsigned *bar, unsigned members, int *err, int *s_ok) {
+// word set) when the wait ran past limit_ns; the caller then returns.
+HT_DEV bool grid_barrier(unsigned *bar, unsigned members, int *err, int *s_ok, uint64_t limit_ns = kWaitLimitNs) {
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned *gen = bar + 1;
@@ -445,7 +445,7 @@ HT_DEV bool grid_barrier(unsigned *bar, unsigned members, int *err, int *s_ok) {
       const uint64_t t0 = global_timer_ns();
       while (*gen == g) {
         __nanosleep(64);
-        if (global_timer_ns() - t0 > kWaitLimitNs) {
+        if (global_timer_ns() - t0 > limit_ns) {
           ok = 0;
           break;
         }
@@ -1368,6 +1368,35 @@ cudaError_t transfer_eig_launch(const float *WG, int kw, int kt, int kc, int t_i
   if (e != cudaSuccess) return e;
   transfer_eig_kernel<<<1, 256, kJacScratch, st>>>(WG, kw, kt, kc, t_is_left, M, Broot);
   return cudaGetLastError();
+}
+
+// Self-test of the bounded waits: a cooperative grid whose barrier expects one
+// more member than the grid holds, so it can never complete.  Every CTA gives
+// up after limit_ns, sets kErrTimeout in *err and returns; nothing hangs and
+// the context stays usable.  Used by the failure-detection tests.
+namespace {
+__global__ void wait_probe_kernel(unsigned *bar, unsigned members, uint64_t limit_ns, int *err) {
+  __shared__ int s_ok;
+  grid_barrier(bar, members, err, &s_ok, limit_ns);
+}
+}  // namespace
+
+cudaError_t wait_probe_launch(int ctas, uint64_t limit_ns, void *ws, int *err, cudaStream_t st) {
+  if (ctas < 1 || ctas > device_sm_count() || limit_ns > kWaitLimitNs) return cudaErrorInvalidValue;
+  unsigned *bar = static_cast<unsigned *>(ws);
+  cudaError_t e = cudaMemsetAsync(bar, 0, 4 * sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(ctas);
+  cfg.blockDim = dim3(32);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, wait_probe_kernel, bar, static_cast<unsigned>(ctas) + 1u, limit_ns, err);
 }
 
 }  // namespace htgb

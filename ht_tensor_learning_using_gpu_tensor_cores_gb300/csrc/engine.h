@@ -176,6 +176,10 @@ cudaError_t eig_batched(EigProblem *probs, int nprob, int iters, void *ws, size_
 // a wait that runs out sets bits in *err.
 cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, size_t ws_bytes, int *err, cudaStream_t s,
                            int *launches);
+// Self-test of the bounded waits: a cooperative grid of `ctas` CTAs (<= SMs)
+// whose barrier expects ctas + 1 members; every CTA gives up after limit_ns
+// (<= the library's 2 s wait limit) and sets kErrTimeout in *err.  ws: 16 bytes.
+cudaError_t wait_probe_launch(int ctas, uint64_t limit_ns, void *ws, int *err, cudaStream_t st);
 // Transfer-tensor eigen step (see eig.cu).  WG: kw x kw.  M: kt x kt, Bkt: kt x kc.
 cudaError_t transfer_eig_launch(const float *WG, int kw, int kt, int kc, int t_is_left, float *M, float *Broot,
                                 cudaStream_t st);

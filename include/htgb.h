@@ -230,6 +230,15 @@ ht_status_t ht_tsqr(const float *A, long long m, int k, long long lda, float *R,
 ht_status_t ht_mode_gram_noalloc(const float *x, const long *dims, int order, int lo, int hi, float *G,
                                  void *stream);
 
+/* Self-test of failure detection (no counterpart in the reference): launches a
+ * cooperative grid of `ctas` CTAs (at most the device's multiprocessor count)
+ * whose grid barrier waits for ctas + 1 members, so the wait can only run
+ * out.  Every CTA gives up after limit_ms (0 < limit_ms <= 2000; the library's
+ * own waits give up after 2000 ms) and the call returns HT_ERR_TIMEOUT, as a
+ * decomposition does when one of its waits runs out; nothing hangs and the
+ * device stays usable for the next call. */
+ht_status_t ht_selftest_wait_timeout(int ctas, double limit_ms, void *stream);
+
 /* ------------------------------------------------------------ batched path */
 typedef struct {
     double rel_err_p50;      /* median relative error over the batch (HT_FLAG_COMPUTE_ERROR) */

@@ -48,3 +48,24 @@ def test_non_finite_tensor_in_a_batch_is_reported():
     assert "tensor 3" in str(e.value)
     del bd
     ht.release_batch()
+
+
+@pytest.mark.parametrize("ctas", [1, 8])
+def test_bounded_wait_runs_out_and_the_device_stays_usable(ctas):
+    """A grid barrier that waits for one CTA more than its grid holds can only
+    run out (ht_selftest_wait_timeout, a 20 ms limit instead of the library's
+    2 s): every CTA gives up, the call returns HT_ERR_TIMEOUT, and the next
+    decomposition on the same context succeeds with the usual error."""
+    import time
+    from ht_tensor_learning_using_gpu_tensor_cores_gb300._lib import lib
+    HT_ERR_TIMEOUT = 5
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rc = lib().ht_selftest_wait_timeout(ctas, 20.0, None)
+    dt = time.perf_counter() - t0
+    assert rc == HT_ERR_TIMEOUT, lib().ht_last_error()
+    assert b"ran out" in lib().ht_last_error()
+    assert 0.02 <= dt < 5.0, dt
+    tree, X = _tensor()
+    ref = ht.decompose(X, tree, precision="bf16", compute_error=True)
+    assert abs(ref.report["rel_err"] - 1e-3) < 1e-4
