@@ -439,10 +439,27 @@ def learned_sketch_config(ht, synth, torch, stream, n=512, k=24, p=10, n_train=2
     rec["heldout_missed_energy"] = {"gaussian_mean": float(lg.mean()), "learned_mean": float(ll.mean()),
                                     "gaussian_p99": float(np.quantile(lg, 0.99)),
                                     "learned_p99": float(np.quantile(ll, 0.99))}
+    # below the family's rank the sketch is a choice: width 6, trained on the same
+    # Grams, held-out missed energy against the Gaussian start and the best
+    # subspace of that width (top-6 eigenvectors of each Gram)
+    sn = 6
+    narrow, _ = learn.train_mode_sketches(Gtr, ttr, s=sn, steps=400, batch=16, lr=2e-3, seed=1)
+    g0 = [learn.gaussian_sketch(n, sn, seed=1 + 17 * m) for m in range(3)]
+    lgn = np.concatenate([learn.heldout_loss(Gte[:, m], tte[:, m], g0[m]) for m in range(3)])
+    lln = np.concatenate([learn.heldout_loss(Gte[:, m], tte[:, m], narrow[m]) for m in range(3)])
+    ev = torch.linalg.eigvalsh(Gte.double()).flip(-1)
+    best = (1.0 - ev[..., :sn].sum(-1) / ev.sum(-1)).reshape(-1).cpu().numpy()
+    rec["below_rank_width6"] = {"gaussian_missed_energy_mean": float(lgn.mean()),
+                                "learned_missed_energy_mean": float(lln.mean()),
+                                "best_subspace_missed_energy_mean": float(best.mean()),
+                                "gap_closed": float((lgn.mean() - lln.mean()) / max(lgn.mean() - best.mean(), 1e-30))}
     del Gtr, Gte
     tree = ht.reference_tree_3d([1, k, k, k, k])
     variants = (("exact_gram", {}), ("gaussian_1it", {"eig_iters": 1, "oversample": p}),
-                ("learned_1it", {"eig_iters": 1, "oversample": p, "sketch": learned}))
+                ("learned_1it", {"eig_iters": 1, "oversample": p, "sketch": learned}),
+                ("gaussian_range_finder", {"leaf_method": "sketch", "oversample": p, "power_steps": 0}),
+                ("learned_range_finder", {"leaf_method": "sketch", "oversample": p, "power_steps": 0,
+                                          "sketch": learned}))
     errs = {v: [] for v, _ in variants}
     ms = {}
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -463,6 +480,10 @@ def learned_sketch_config(ht, synth, torch, stream, n=512, k=24, p=10, n_train=2
         del X
     rec["heldout_rel_err_mean"] = {v: float(np.mean(e)) for v, e in errs.items()}
     rec["heldout_rel_err_max"] = {v: float(np.max(e)) for v, e in errs.items()}
+    rec["heldout_rel_err_max_minus_exact_gram"] = {v: float(np.max(np.array(e) - np.array(errs["exact_gram"])))
+                                                   for v, e in errs.items()}
+    rec["variants"] = {"gram_1it": "leaf solver on the mode Gram, one iteration from the start block",
+                       "range_finder": "Gram-free range finder (Y = X (X^T S), Nystrom core), no power step"}
     rec["ms_per_decomposition"] = ms
     return rec
 
