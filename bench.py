@@ -516,13 +516,16 @@ def run_ours(args, world, rank, local):
     def one(prec, compute_error=False):
         return ht.decompose(X, tree, precision=prec, compute_error=compute_error)
 
-    if args.mixed_only:
-        # profiling mode: only the headline step (warm-up + timed steps), no other work
+    if args.mixed_only or args.sketch_only:
+        # profiling modes: only the headline step (or the Gram-free range-finder
+        # path on the same tensor), warm-up + timed steps, no other work
+        kw = {"leaf_method": "sketch", "oversample": 10, "power_steps": 1} if args.sketch_only else {}
         for _ in range(args.warmup + args.steps):
-            one("bf16")
+            ht.decompose(X, tree, precision="bf16", **kw)
         torch.cuda.synchronize()
         if rank == 0:
-            print(json.dumps({"mixed_only": True, "steps": args.steps, "warmup": args.warmup}), flush=True)
+            print(json.dumps({"mixed_only": bool(args.mixed_only), "sketch_only": bool(args.sketch_only),
+                              "steps": args.steps, "warmup": args.warmup}), flush=True)
         return
 
     # correctness of both paths against the FP64 optimum (not timed)
@@ -693,6 +696,8 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=1, help="--impl reference: full-size decompositions timed")
     ap.add_argument("--mixed-only", action="store_true",
                     help="run only the headline mixed-path steps (for profiler launch lists)")
+    ap.add_argument("--sketch-only", action="store_true",
+                    help="run only the Gram-free range-finder path on the headline tensor (for profiler launch lists)")
     ap.add_argument("--fourth-order-only", action="store_true",
                     help="run only the 128^4 mixed-path steps (for profiler launch lists)")
     args = ap.parse_args()

@@ -44,46 +44,80 @@ HT_DEV float warp_sum_bcast(float v) {
   return __shfl_sync(0xffffffffu, v, 0);
 }
 
+// Sum of v[i] over the warp for 32 columns i at once (reduce-scatter): lane l
+// returns the total of column l.  31 shuffles, all independent per level.
+HT_DEV float warp_reduce_scatter32(float (&v)[32]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < o; ++i) {
+      const float send = up ? v[i] : v[i + o];
+      const float keep = up ? v[i + o] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+  return v[0];
+}
+
 // [R; P] -> R' with R' upper triangular and R'^T R' = R^T R + P^T P: k
 // Householder reflections.  R: k x k row-major (stride LD), P: prow x k
 // row-major (stride LD, prow <= 64, destroyed).  One warp; lane l holds panel
-// rows l and l + 32, and, while column j is reduced, entries l and l + 32 of
-// R's row j in registers (the only row of R the reflector changes).
-template <int LD>
+// rows l and l + 32 and, while column j is reduced, entries l + 32 b of R's row
+// j (the only row of R the reflector changes, R being upper triangular).  For
+// each column j the dot products of the reflector with all later columns are
+// formed together, 32 columns per reduce-scatter, so the shuffles of different
+// columns overlap instead of forming one long dependent chain per column.
+template <int KM, int LD>
 HT_DEV void warp_qr_fold(float *R, float *P, int prow, int k) {
+  constexpr int NB = KM / 32;
   const int lane = threadIdx.x & 31;
   const bool h0 = lane < prow, h1 = lane + 32 < prow;
   float *p0 = P + lane * LD, *p1 = P + (lane + 32) * LD;
   for (int j = 0; j < k; ++j) {
-    float ra = lane < k ? R[j * LD + lane] : 0.f;
-    float rb = lane + 32 < k ? R[j * LD + lane + 32] : 0.f;
+    float r[NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) r[b] = lane + 32 * b < k ? R[j * LD + lane + 32 * b] : 0.f;
     const float x0 = h0 ? p0[j] : 0.f, x1 = h1 ? p1[j] : 0.f;
     const float sig = warp_sum_bcast(fmaf(x0, x0, x1 * x1));
-    const float rjj = __shfl_sync(0xffffffffu, j < 32 ? ra : rb, j & 31);
-    if (sig == 0.f) continue;   // the column below the pivot is already zero
-    const float nrm = sqrtf(fmaf(rjj, rjj, sig));
-    const float alpha = rjj > 0.f ? -nrm : nrm;
-    const float v0 = rjj - alpha;            // reflector v = [v0; x], tau = 2 / v^T v
-    const float tau = -1.f / (alpha * v0);
-    for (int c = j + 1; c < k; ++c) {
-      const float a0 = h0 ? p0[c] : 0.f, a1 = h1 ? p1[c] : 0.f;
-      const float rjc = __shfl_sync(0xffffffffu, c < 32 ? ra : rb, c & 31);
-      const float w = fmaf(v0, rjc, warp_sum_bcast(fmaf(x0, a0, x1 * a1)));
-      const float tw = tau * w;
-      if (h0) p0[c] = fmaf(-tw, x0, a0);
-      if (h1) p1[c] = fmaf(-tw, x1, a1);
-      if (lane == (c & 31)) {
-        const float nv = fmaf(-tw, v0, rjc);
-        if (c < 32) ra = nv;
-        else rb = nv;
+    const float rjj = __shfl_sync(0xffffffffu, NB == 1 || j < 32 ? r[0] : r[NB - 1], j & 31);
+    if (sig != 0.f) {   // else the column below the pivot is already zero
+      const float nrm = sqrtf(fmaf(rjj, rjj, sig));
+      const float alpha = rjj > 0.f ? -nrm : nrm;
+      const float v0 = rjj - alpha;            // reflector v = [v0; x], tau = 2 / v^T v
+      const float tau = -1.f / (alpha * v0);
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        if (32 * b + 31 <= j) continue;        // every column of this block is done
+        float a0[32], a1[32], v[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          const int c = 32 * b + i;
+          const bool live = c > j && c < k;
+          a0[i] = (live && h0) ? p0[c] : 0.f;
+          a1[i] = (live && h1) ? p1[c] : 0.f;
+          v[i] = fmaf(x0, a0[i], x1 * a1[i]);
+        }
+        const int cl = 32 * b + lane;        // this lane's column
+        const float w = fmaf(v0, r[b], warp_reduce_scatter32(v));
+        const float tw = (cl > j && cl < k) ? tau * w : 0.f;
+        r[b] = fmaf(-tw, v0, r[b]);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          const int c = 32 * b + i;
+          const float twi = __shfl_sync(0xffffffffu, tw, i);
+          if (c > j && c < k) {
+            if (h0) p0[c] = fmaf(-twi, x0, a0[i]);
+            if (h1) p1[c] = fmaf(-twi, x1, a1[i]);
+          }
+        }
       }
+      if (lane == (j & 31)) r[NB == 1 ? 0 : j / 32] = alpha;
     }
-    if (lane == (j & 31)) {
-      if (j < 32) ra = alpha;
-      else rb = alpha;
-    }
-    if (lane < k) R[j * LD + lane] = ra;
-    if (lane + 32 < k) R[j * LD + lane + 32] = rb;
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+      if (lane + 32 * b < k) R[j * LD + lane + 32 * b] = r[b];
     __syncwarp();
   }
 }
@@ -127,14 +161,14 @@ __global__ void __launch_bounds__(TqCfg<KM>::THREADS, 1) tsqr_kernel(const TqPar
       P[(lane + 32) * LD + c] = lane + 32 < prow ? __ldg(col + lane + 32) : 0.f;
     }
     __syncwarp();
-    warp_qr_fold<LD>(R, P, prow, k);
+    warp_qr_fold<KM, LD>(R, P, prow, k);
   }
   __syncthreads();
 
   // 2. the warps' R factors, combined pairwise in shared memory
   auto tree = [&]() {
     for (int half = C::WARPS / 2; half >= 1; half >>= 1) {
-      if (warp < half) warp_qr_fold<LD>(R, tq_sm + (warp + half) * C::WARP_FLOATS, k, k);
+      if (warp < half) warp_qr_fold<KM, LD>(R, tq_sm + (warp + half) * C::WARP_FLOATS, k, k);
       __syncthreads();
     }
   };
@@ -173,7 +207,7 @@ __global__ void __launch_bounds__(TqCfg<KM>::THREADS, 1) tsqr_kernel(const TqPar
     }
     for (int w = warp + C::WARPS; w < gsize; w += C::WARPS) {
       load_member(P, group * TQ_FAN + w);
-      warp_qr_fold<LD>(R, P, k, k);
+      warp_qr_fold<KM, LD>(R, P, k, k);
     }
     __syncthreads();
     tree();
