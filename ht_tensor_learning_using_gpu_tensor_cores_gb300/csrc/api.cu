@@ -644,10 +644,9 @@ ht_status_t leaf_sketch(Ctx &c, const Tree &T, const ht_config_t &cfg, const lon
     res.resid[leaf] = nullptr;
   }
   const size_t mark = c.ar.off;
-  const int hmax = smax <= 32 ? 32 : 64;
   float *Z32 = c.ar.take<float>(static_cast<size_t>(LRmax) * smax);
   __nv_bfloat16 *Z16 = c.tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(LRmax) * smax + 64) : nullptr;
-  __nv_bfloat16 *Q16 = c.tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(nmax) * 2 * hmax + 64) : nullptr;
+  __nv_bfloat16 *Q16 = c.tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(nmax) * smax + 64) : nullptr;
   if (!Z32 || (c.tc && (!Z16 || !Q16))) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (sketch products)");
   float *Qm[4], *Ym[4], *Q1[4], *Wm[4], *R1[4], *Hm[4], *Tm[4], *M2[4], *Br[4];
   for (int m = 0; m < order; ++m) {
@@ -681,16 +680,18 @@ ht_status_t leaf_sketch(Ctx &c, const Tree &T, const ht_config_t &cfg, const lon
     HT_CUDA(cholqr_batched(cq, order, 2, cws, cbytes, c.err, c.st, &c.launches));
     return HT_OK;
   };
-  // Y = G Q for mode m, as X_(m) (X_(m)^T Q)
-  auto apply_gram = [&](int m, const float *Qsrc, float *Ydst) -> ht_status_t {
+  // Y = G Q for mode m, as X_(m) (X_(m)^T Q).  On the mixed path Q is first
+  // rounded to BF16 in place, so the products see exactly the block that the
+  // Nystrom core later pairs with Y (any block serves as a test matrix).
+  auto apply_gram = [&](int m, float *Qsrc, float *Ydst) -> ht_status_t {
     const View v = view_of_group(dims, order, m, m);
     const long long LR = v.L * v.R;
-    const int s = S[m], h = s <= 32 ? 32 : 64;
+    const int s = S[m];
     if (c.tc && !c.dry()) {
-      HT_CUDA(split_bf16_launch(Qsrc, dims[m], s, h, Q16, c.st));
+      HT_CUDA(round_bf16_launch(Qsrc, Q16, dims[m] * s, c.st));
       ++c.launches;
     }
-    HT_TRY(mode_product(c, v, x32, x16, Qsrc, Q16, s, Z32, c.tc ? h : 0));
+    HT_TRY(mode_product(c, v, x32, x16, Qsrc, Q16, s, Z32));
     if (c.tc && !c.dry()) {
       HT_CUDA(f32_to_bf16_launch(Z32, Z16, LR * s, c.st));
       ++c.launches;
@@ -733,13 +734,22 @@ ht_status_t leaf_sketch(Ctx &c, const Tree &T, const ht_config_t &cfg, const lon
     c.launches += 2;
   }
   HT_TRY(orth_all(Q1));
+  NystromProb np_[4];
+  SvdGramProb sp[4];
   for (int m = 0; m < order; ++m) {
     const int n = static_cast<int>(dims[m]), s = S[m];
     HT_CUDA(gemm_tn_small_launch(Q1[m], n, Ym[m], n, R1[m], s, s, s, n, c.st));
-    HT_CUDA(nystrom_core_launch(Wm[m], R1[m], s, kNystromShift, Hm[m], c.err, c.st));
-    HT_CUDA(svd_from_gram_launch(Hm[m], s, K[m], K[m], Tm[m], M2[m], Br[m], c.st));
+    ++c.launches;
+    np_[m] = NystromProb{Wm[m], R1[m], s, Hm[m]};
+    sp[m] = SvdGramProb{Hm[m], s, K[m], K[m], Tm[m], M2[m], Br[m]};
+  }
+  HT_CUDA(nystrom_core_launch(np_, order, kNystromShift, c.err, c.st));       // all modes, a CTA each
+  HT_CUDA(svd_from_gram_batched_launch(sp, order, c.st));                     // top-K eigenvectors of each H
+  c.launches += 2;
+  for (int m = 0; m < order; ++m) {
+    const int n = static_cast<int>(dims[m]), s = S[m];
     HT_CUDA(matmul_nn_launch(Q1[m], n, Tm[m], s, ep[m].U, n, n, K[m], s, c.st));
-    c.launches += 4;
+    ++c.launches;
   }
   c.ar.off = mark;
   return HT_OK;

@@ -329,8 +329,16 @@ __global__ void __launch_bounds__(256) transfer_eig_kernel(const float *WG, int 
 // SVD of a tall W from its Gram GW = W^T W (s x s): GW = U diag(sigma^2) U^T.
 // M1 = U[:, :k1], M2 = U[:, :k2] diag(1/sigma) (zero where sigma <= 1e-6 sigma_1),
 // Broot = M1^T GW M2 (k1 x k2).
-__global__ void __launch_bounds__(256) svd_from_gram_kernel(const float *GW, int s, int k1, int k2, float *M1,
-                                                            float *M2, float *Broot) {
+// Up to four independent problems, one CTA each (blockIdx.x).
+struct SvdGramBatch {
+  SvdGramProb p[4];
+};
+
+__global__ void __launch_bounds__(256) svd_from_gram_kernel(const SvdGramBatch batch) {
+  const SvdGramProb &pb = batch.p[blockIdx.x];
+  const float *GW = pb.GW;
+  const int s = pb.s, k1 = pb.k1, k2 = pb.k2;
+  float *M1 = pb.M1, *M2 = pb.M2, *Broot = pb.Broot;
   __shared__ float A[SMAX][SMAX + 1];
   __shared__ float V[SMAX][SMAX + 1];
   extern __shared__ float jac_scratch[];   // SMAX * (SMAX + 1) floats
@@ -1350,14 +1358,26 @@ cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, s
   return cudaSuccess;
 }
 
-cudaError_t svd_from_gram_launch(const float *GW, int s, int k1, int k2, float *M1, float *M2, float *Broot,
-                                 cudaStream_t st) {
-  if (s > SMAX || k1 > s || k2 > s) return cudaErrorInvalidValue;
+cudaError_t svd_from_gram_batched_launch(const SvdGramProb *probs, int nprob, cudaStream_t st) {
+  if (nprob < 1 || nprob > 4) return cudaErrorInvalidValue;
+  SvdGramBatch b;
+  std::memset(&b, 0, sizeof(b));
+  for (int i = 0; i < nprob; ++i) {
+    const SvdGramProb &q = probs[i];
+    if (q.s > SMAX || q.s < 1 || q.k1 > q.s || q.k2 > q.s) return cudaErrorInvalidValue;
+    b.p[i] = q;
+  }
   static bool attr_set[64] = {};
   const cudaError_t e = opt_in_smem(svd_from_gram_kernel, static_cast<int>(kJacScratch), attr_set);
   if (e != cudaSuccess) return e;
-  svd_from_gram_kernel<<<1, 256, kJacScratch, st>>>(GW, s, k1, k2, M1, M2, Broot);
+  svd_from_gram_kernel<<<nprob, 256, kJacScratch, st>>>(b);
   return cudaGetLastError();
+}
+
+cudaError_t svd_from_gram_launch(const float *GW, int s, int k1, int k2, float *M1, float *M2, float *Broot,
+                                 cudaStream_t st) {
+  SvdGramProb q{GW, s, k1, k2, M1, M2, Broot};
+  return svd_from_gram_batched_launch(&q, 1, st);
 }
 
 cudaError_t transfer_eig_launch(const float *WG, int kw, int kt, int kc, int t_is_left, float *M, float *Broot,

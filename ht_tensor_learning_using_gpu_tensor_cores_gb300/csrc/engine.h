@@ -122,6 +122,8 @@ cudaError_t convert_bf16_dual_launch(const float *x, __nv_bfloat16 *xb, __nv_bfl
                                      int lb, double *partials, int num_partials, cudaStream_t s,
                                      long long n_begin = 0, long long n_count = -1);
 cudaError_t f32_to_bf16_launch(const float *x, __nv_bfloat16 *y, long long n, cudaStream_t s);
+// x <- bf16(x) in place (values kept in FP32) and y = the BF16 copy.
+cudaError_t round_bf16_launch(float *x, __nv_bfloat16 *y, long long n, cudaStream_t s);
 // W (rows x k, column-major FP32) -> Y (rows x 2h BF16): columns [0, k) the
 // BF16 rounding hi(W), columns [h, h + k) the rounding of W - hi(W), the rest 0.
 cudaError_t split_bf16_launch(const float *W, long long rows, int k, int h, __nv_bfloat16 *Y, cudaStream_t s);
@@ -187,6 +189,13 @@ cudaError_t transfer_eig_launch(const float *WG, int kw, int kt, int kc, int t_i
 // M2 (s x k2) = top-k2 eigenvectors scaled by sigma^-1, Broot (k1 x k2) = M1^T GW M2.
 cudaError_t svd_from_gram_launch(const float *GW, int s, int k1, int k2, float *M1, float *M2, float *Broot,
                                  cudaStream_t st);
+// The same for up to four independent problems in one launch (a CTA each).
+struct SvdGramProb {
+  const float *GW;
+  int s, k1, k2;
+  float *M1, *M2, *Broot;
+};
+cudaError_t svd_from_gram_batched_launch(const SvdGramProb *probs, int nprob, cudaStream_t st);
 
 // ------------------------------------------------------- Householder TSQR (tsqr.cu)
 size_t tsqr_workspace_bytes(long long m, int k);
@@ -200,9 +209,14 @@ cudaError_t tsqr_launch(const float *A, long long m, int k, long long lda, float
 // Yn = Y + nu Q (n x s), nu = nu_rel * tr(W) for the s x s matrix W.
 cudaError_t nystrom_shift_launch(const float *Y, const float *Q, long long n, int s, const float *W, float nu_rel,
                                  float *Yn, cudaStream_t st);
-// H (s x s) = R1 (sym(W) + nu I)^-1 R1^T, nu as above (FP64, one CTA).
-cudaError_t nystrom_core_launch(const float *W, const float *R1, int s, float nu_rel, float *H, int *err,
-                                cudaStream_t st);
+// H (s x s) = R1 (sym(W) + nu I)^-1 R1^T, nu as above (FP64, one CTA per
+// problem; up to four problems in one launch).
+struct NystromProb {
+  const float *W, *R1;
+  int s;
+  float *H;
+};
+cudaError_t nystrom_core_launch(const NystromProb *probs, int nprob, float nu_rel, int *err, cudaStream_t st);
 
 // ------------------------------------------------------- learned sketch (learn.cu)
 size_t sketch_workspace_bytes(int batch, int n, int s);

@@ -42,9 +42,16 @@ __global__ void nystrom_shift_kernel(const float *__restrict__ Y, const float *_
 
 // H = R1 (sym(W) + nu I)^-1 R1^T in FP64 (Cholesky of the shifted W; a pivot
 // that rounding drove to or below zero is floored at nu).  One CTA.
-__global__ void __launch_bounds__(256) nystrom_core_kernel(const float *__restrict__ W, const float *__restrict__ R1,
-                                                           int s, float nu_rel, float *__restrict__ H,
+struct NystromBatch {
+  NystromProb p[4];
+};
+
+__global__ void __launch_bounds__(256) nystrom_core_kernel(const NystromBatch batch, float nu_rel,
                                                            int *__restrict__ err) {
+  const float *__restrict__ W = batch.p[blockIdx.x].W;
+  const float *__restrict__ R1 = batch.p[blockIdx.x].R1;
+  const int s = batch.p[blockIdx.x].s;
+  float *__restrict__ H = batch.p[blockIdx.x].H;
   extern __shared__ double ny_sm[];
   double *L = ny_sm;                       // upper Cholesky factor, row-major: (W + nu I) = L^T L
   double *F = ny_sm + NY_MAX * NY_MAX;     // F = R1 L^-1, row-major
@@ -105,14 +112,19 @@ cudaError_t nystrom_shift_launch(const float *Y, const float *Q, long long n, in
   return cudaGetLastError();
 }
 
-cudaError_t nystrom_core_launch(const float *W, const float *R1, int s, float nu_rel, float *H, int *err,
-                                cudaStream_t st) {
-  if (s < 1 || s > NY_MAX) return cudaErrorInvalidValue;
+cudaError_t nystrom_core_launch(const NystromProb *probs, int nprob, float nu_rel, int *err, cudaStream_t st) {
+  if (nprob < 1 || nprob > 4) return cudaErrorInvalidValue;
+  NystromBatch b;
+  for (int i = 0; i < 4; ++i) b.p[i] = NystromProb{nullptr, nullptr, 0, nullptr};
+  for (int i = 0; i < nprob; ++i) {
+    if (probs[i].s < 1 || probs[i].s > NY_MAX) return cudaErrorInvalidValue;
+    b.p[i] = probs[i];
+  }
   constexpr int kSmem = 2 * NY_MAX * NY_MAX * sizeof(double);
   static bool attr_set[64] = {};
   const cudaError_t e = opt_in_smem(nystrom_core_kernel, kSmem, attr_set);
   if (e != cudaSuccess) return e;
-  nystrom_core_kernel<<<1, 256, kSmem, st>>>(W, R1, s, nu_rel, H, err);
+  nystrom_core_kernel<<<nprob, 256, kSmem, st>>>(b, nu_rel, err);
   return cudaGetLastError();
 }
 

@@ -124,6 +124,15 @@ __global__ void sumsq_kernel(const float *__restrict__ x, long long n, double *p
   if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
 }
 
+// x[i] = the BF16 rounding of x[i] (kept in FP32), and the BF16 copy in y.
+__global__ void round_bf16_kernel(float *__restrict__ x, __nv_bfloat16 *__restrict__ y, long long n) {
+  for (long long i = blockIdx.x * 256ll + threadIdx.x; i < n; i += gridDim.x * 256ll) {
+    const __nv_bfloat16 b = __float2bfloat16_rn(x[i]);
+    y[i] = b;
+    x[i] = __bfloat162float(b);
+  }
+}
+
 __global__ void f32_to_bf16_kernel(const float *__restrict__ x, __nv_bfloat16 *__restrict__ y, long long n) {
   for (long long i = blockIdx.x * 256ll + threadIdx.x; i < n; i += gridDim.x * 256ll) y[i] = __float2bfloat16_rn(x[i]);
 }
@@ -411,6 +420,11 @@ cudaError_t sumsq_launch(const float *x, long long n, double *partials, int num_
 
 cudaError_t f32_to_bf16_launch(const float *x, __nv_bfloat16 *y, long long n, cudaStream_t s) {
   f32_to_bf16_kernel<<<grid_for(n), 256, 0, s>>>(x, y, n);
+  return cudaGetLastError();
+}
+
+cudaError_t round_bf16_launch(float *x, __nv_bfloat16 *y, long long n, cudaStream_t s) {
+  round_bf16_kernel<<<grid_for(n), 256, 0, s>>>(x, y, n);
   return cudaGetLastError();
 }
 

@@ -122,6 +122,66 @@ HT_DEV void warp_qr_fold(float *R, float *P, int prow, int k) {
   }
 }
 
+// The same fold for k <= 32 with the panel in registers (lane l: rows l and
+// l + 32, all 32 columns): no shared-memory traffic for the panel, and the
+// column extraction is a select over the unrolled register array.
+template <int LD>
+HT_DEV void warp_qr_fold32(float *R, float (&p0)[32], float (&p1)[32], int k) {
+  const int lane = threadIdx.x & 31;
+  for (int j = 0; j < k; ++j) {
+    float r = lane < k ? R[j * LD + lane] : 0.f;
+    float x0 = 0.f, x1 = 0.f;
+#pragma unroll
+    for (int c = 0; c < 32; ++c)
+      if (c == j) {
+        x0 = p0[c];
+        x1 = p1[c];
+      }
+    const float sig = warp_sum_bcast(fmaf(x0, x0, x1 * x1));
+    const float rjj = __shfl_sync(0xffffffffu, r, j);
+    if (sig != 0.f) {   // else the column below the pivot is already zero
+      const float nrm = sqrtf(fmaf(rjj, rjj, sig));
+      const float alpha = rjj > 0.f ? -nrm : nrm;
+      const float v0 = rjj - alpha;
+      const float tau = -1.f / (alpha * v0);
+      float v[32];
+#pragma unroll
+      for (int c = 0; c < 32; ++c) v[c] = c > j ? fmaf(x0, p0[c], x1 * p1[c]) : 0.f;
+      const float w = fmaf(v0, r, warp_reduce_scatter32(v));
+      const float tw = (lane > j && lane < k) ? tau * w : 0.f;
+      r = fmaf(-tw, v0, r);
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        const float twc = __shfl_sync(0xffffffffu, tw, c);
+        if (c > j) {
+          p0[c] = fmaf(-twc, x0, p0[c]);
+          p1[c] = fmaf(-twc, x1, p1[c]);
+        }
+      }
+      if (lane == j) r = alpha;
+    }
+    if (lane < k) R[j * LD + lane] = r;
+    __syncwarp();
+  }
+}
+
+// Fold a row-major panel in shared memory (prow <= 64 rows, stride LD) into R.
+template <int KM, int LD>
+HT_DEV void warp_fold_smem(float *R, float *P, int prow, int k) {
+  if constexpr (KM == 32) {
+    const int lane = threadIdx.x & 31;
+    float p0[32], p1[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) {
+      p0[c] = (lane < prow && c < k) ? P[lane * LD + c] : 0.f;
+      p1[c] = (lane + 32 < prow && c < k) ? P[(lane + 32) * LD + c] : 0.f;
+    }
+    warp_qr_fold32<LD>(R, p0, p1, k);
+  } else {
+    warp_qr_fold<KM, LD>(R, P, prow, k);
+  }
+}
+
 struct TqParams {
   const float *A;
   long long m, lda;
@@ -154,21 +214,32 @@ __global__ void __launch_bounds__(TqCfg<KM>::THREADS, 1) tsqr_kernel(const TqPar
   for (long long r0 = r_begin + static_cast<long long>(warp) * TQ_PROWS; r0 < r_end;
        r0 += static_cast<long long>(C::WARPS) * TQ_PROWS) {
     const int prow = static_cast<int>(min(static_cast<long long>(TQ_PROWS), r_end - r0));
+    if constexpr (KM == 32) {   // the panel straight into registers
+      float p0[32], p1[32];
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        const float *col = p.A + r0 + p.lda * c;
+        p0[c] = (c < k && lane < prow) ? __ldg(col + lane) : 0.f;
+        p1[c] = (c < k && lane + 32 < prow) ? __ldg(col + lane + 32) : 0.f;
+      }
+      warp_qr_fold32<LD>(R, p0, p1, k);
+    } else {
 #pragma unroll 4
-    for (int c = 0; c < k; ++c) {
-      const float *col = p.A + r0 + p.lda * c;
-      P[lane * LD + c] = lane < prow ? __ldg(col + lane) : 0.f;
-      P[(lane + 32) * LD + c] = lane + 32 < prow ? __ldg(col + lane + 32) : 0.f;
+      for (int c = 0; c < k; ++c) {
+        const float *col = p.A + r0 + p.lda * c;
+        P[lane * LD + c] = lane < prow ? __ldg(col + lane) : 0.f;
+        P[(lane + 32) * LD + c] = lane + 32 < prow ? __ldg(col + lane + 32) : 0.f;
+      }
+      __syncwarp();
+      warp_qr_fold<KM, LD>(R, P, prow, k);
     }
-    __syncwarp();
-    warp_qr_fold<KM, LD>(R, P, prow, k);
   }
   __syncthreads();
 
   // 2. the warps' R factors, combined pairwise in shared memory
   auto tree = [&]() {
     for (int half = C::WARPS / 2; half >= 1; half >>= 1) {
-      if (warp < half) warp_qr_fold<KM, LD>(R, tq_sm + (warp + half) * C::WARP_FLOATS, k, k);
+      if (warp < half) warp_fold_smem<KM, LD>(R, tq_sm + (warp + half) * C::WARP_FLOATS, k, k);
       __syncthreads();
     }
   };
@@ -207,7 +278,7 @@ __global__ void __launch_bounds__(TqCfg<KM>::THREADS, 1) tsqr_kernel(const TqPar
     }
     for (int w = warp + C::WARPS; w < gsize; w += C::WARPS) {
       load_member(P, group * TQ_FAN + w);
-      warp_qr_fold<KM, LD>(R, P, k, k);
+      warp_fold_smem<KM, LD>(R, P, k, k);
     }
     __syncthreads();
     tree();
