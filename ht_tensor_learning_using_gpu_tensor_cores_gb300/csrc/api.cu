@@ -225,6 +225,7 @@ struct GemmReq {
   float *out = nullptr;
   long long ld_out = 0;
   bool symmetric = false;
+  bool accumulate = false;          // OUT_PARTIAL reductions add to q.out
   bool allow_split = true;
   bool fold = false;                // tcgen05 only: b16 is a high/low split (GemmArgs::fold)
   int mt_tc = 1;                    // tcgen05 only: 2 = 256-row tiles (GemmArgs::mt)
@@ -291,7 +292,8 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
   }
   ++c.launches;
   if (partial) {
-    HT_CUDA(reduce_partials_launch(part, gen, splits, bn, q.out, q.ld_out, q.symmetric ? 1 : 0, c.st));
+    HT_CUDA(reduce_partials_launch(part, gen, splits, bn, q.out, q.ld_out,
+                                   (q.symmetric ? 1 : 0) | (q.accumulate ? 2 : 0), c.st));
     ++c.launches;
   }
   c.ar.off = mark;   // scratch is stream-ordered: later work may reuse it
@@ -299,7 +301,9 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
 }
 
 // G (n x n, column-major, symmetric) = X_(group) X_(group)^T, n = v.N
-ht_status_t gram(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x16, float *G) {
+// (accumulate: G += X_(group) X_(group)^T)
+ht_status_t gram(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x16, float *G,
+                 bool accumulate = false) {
   GemmReq q;
   q.a32 = q.b32 = gram_operand(v, x32);
   if (x16) q.a16 = q.b16 = gram_operand(v, x16);
@@ -313,6 +317,7 @@ ht_status_t gram(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x
   q.out = G;
   q.ld_out = v.N;
   q.symmetric = true;
+  q.accumulate = accumulate;
   return run_gemm(c, q);
 }
 
@@ -1332,20 +1337,45 @@ ht_status_t enqueue_body(Ctx &c, const Tree &T, const ht_config_t &cfg, const fl
   return HT_OK;
 }
 
-// Host input, mixed path, 3rd order with the l-blocked copy: the host->device
-// copy goes in slabs along mode 3 on its own stream, and each slab's BF16
-// conversion and its share of the mode-1 and mode-2 Grams run as soon as it
-// lands, so that only the last slab's work, the mode-3 Gram and the rest of the
-// decomposition follow the copy.  The whole tensor ends up resident as in the
-// plain host-input path.
+// Mixed path, 3rd order with the l-blocked copy, Gram leaves: X is taken in
+// slabs along mode 3 and the mode-1 and mode-2 Grams accumulate slab by slab
+// (split-K reductions that add into G), so that they overlap the work that
+// produces the slabs:
+//   host input    the host->device copy of slab s+1 (its own stream) overlaps
+//                 the conversion and the Gram shares of slab s;
+//   device input  the BF16 conversion of slab s+1 (its own stream, HBM-bound)
+//                 overlaps the Gram shares of slab s (tensor-bound).
+// Only the last slab's work, the mode-3 Gram and the rest of the
+// decomposition follow.  The whole tensor ends up resident as in the plain path.
 constexpr int kPipeSlabs = 8;
 
-bool pipelined_input(const Ctx &c, const CallArgs &a) {
-  if (a.x_dev || !c.tc || a.order != 3) return false;
+bool pipelined_input(const Ctx &c, const CallArgs &a, const ht_config_t &cfg) {
+  if (!c.tc || a.order != 3 || cfg.leaf_method != HT_LEAF_GRAM) return false;
   const int lb = last_mode_block(a.dims, a.order);
   if (lb != 8) return false;   // 16-column conversion tiles: slabs of multiples of 16 columns
+  if (a.x_dev && (reinterpret_cast<uintptr_t>(a.x) & 15u) != 0) return false;
   const long long total = static_cast<long long>(a.dims[0]) * a.dims[1] * a.dims[2];
   return total * 4 >= (256ll << 20) && a.dims[2] >= 16 * kPipeSlabs;
+}
+
+// Side stream and slab events of the pipelined path, created once per device.
+struct PipeRes {
+  cudaStream_t cs = nullptr;
+  cudaEvent_t ev[kPipeSlabs + 1] = {};
+};
+PipeRes g_pipe[64];
+
+ht_status_t pipe_resources(PipeRes **out) {
+  int dev = 0;
+  HT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(HT_ERR_INVALID_ARG, "device index out of range");
+  PipeRes &r = g_pipe[dev];
+  if (!r.cs) {
+    HT_CUDA(cudaStreamCreateWithFlags(&r.cs, cudaStreamNonBlocking));
+    for (int i = 0; i <= kPipeSlabs; ++i) HT_CUDA(cudaEventCreateWithFlags(&r.ev[i], cudaEventDisableTiming));
+  }
+  *out = &r;
+  return HT_OK;
 }
 
 ht_status_t enqueue_pipelined(Ctx &c, const Tree &T, const ht_config_t &cfg, const CallArgs &a, double *dsum,
@@ -1356,58 +1386,45 @@ ht_status_t enqueue_pipelined(Ctx &c, const Tree &T, const ht_config_t &cfg, con
   long long len = (n2 + kPipeSlabs - 1) / kPipeSlabs;
   len = (len + 15) / 16 * 16;
   const long long S = (n2 + len - 1) / len;
-  float *xd = c.ar.take<float>(static_cast<size_t>(total));
+  float *xd = a.x_dev ? const_cast<float *>(a.x) : c.ar.take<float>(static_cast<size_t>(total));
   __nv_bfloat16 *xb = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
   __nv_bfloat16 *xbt = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
   double *parts = c.ar.take<double>(static_cast<size_t>(S) * 1024);
   float *G[4] = {};
   G[0] = c.ar.take<float>(static_cast<size_t>(n0) * n0);
   G[1] = c.ar.take<float>(static_cast<size_t>(n1) * n1);
-  float *Gt = c.ar.take<float>(static_cast<size_t>(std::max(n0, n1)) * std::max(n0, n1));
-  if (!xd || !xb || !xbt || !parts || !G[0] || !G[1] || !Gt)
+  if (!xd || !xb || !xbt || !parts || !G[0] || !G[1])
     return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (pipelined input)");
-  cudaStream_t cs = nullptr;
-  cudaEvent_t ev[kPipeSlabs + 1] = {};
-  struct Cleanup {
-    cudaStream_t &cs;
-    cudaEvent_t *ev;
-    ~Cleanup() {
-      if (cs) {
-        cudaStreamSynchronize(cs);
-        cudaStreamDestroy(cs);
-      }
-      for (int i = 0; i <= kPipeSlabs; ++i)
-        if (ev[i]) cudaEventDestroy(ev[i]);
-    }
-  } cleanup{cs, ev};
+  PipeRes *pr = nullptr;
   if (!c.dry()) {
-    HT_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-    for (long long s = 0; s <= S; ++s) HT_CUDA(cudaEventCreateWithFlags(&ev[s], cudaEventDisableTiming));
-    // the copy may start only after earlier work on c.st (the workspace is shared)
-    HT_CUDA(cudaEventRecord(ev[S], c.st));
-    HT_CUDA(cudaStreamWaitEvent(cs, ev[S], 0));
+    HT_TRY(pipe_resources(&pr));
+    // the side stream may start only after earlier work on c.st (the workspace is shared)
+    HT_CUDA(cudaEventRecord(pr->ev[S], c.st));
+    HT_CUDA(cudaStreamWaitEvent(pr->cs, pr->ev[S], 0));
     for (long long s = 0; s < S; ++s) {
       const long long c0 = s * len, w = std::min(len, n2 - c0);
-      HT_CUDA(cudaMemcpyAsync(xd + L * c0, a.x + L * c0, sizeof(float) * L * w, cudaMemcpyHostToDevice, cs));
-      HT_CUDA(cudaEventRecord(ev[s], cs));
+      if (a.x_dev) {
+        HT_CUDA(convert_bf16_dual_launch(xd, xb, xbt, L, n2, lb, parts + s * 1024, 1024, pr->cs, c0, w));
+        ++c.launches;
+      } else {
+        HT_CUDA(cudaMemcpyAsync(xd + L * c0, a.x + L * c0, sizeof(float) * L * w, cudaMemcpyHostToDevice, pr->cs));
+      }
+      HT_CUDA(cudaEventRecord(pr->ev[s], pr->cs));
     }
-    if (h2d_done) HT_CUDA(cudaEventRecord(h2d_done, cs));
+    if (h2d_done && !a.x_dev) HT_CUDA(cudaEventRecord(h2d_done, pr->cs));
   }
   for (long long s = 0; s < S; ++s) {
     const long long c0 = s * len, w = std::min(len, n2 - c0);
     if (!c.dry()) {
-      HT_CUDA(cudaStreamWaitEvent(c.st, ev[s], 0));
-      HT_CUDA(convert_bf16_dual_launch(xd, xb, xbt, L, n2, lb, parts + s * 1024, 1024, c.st, c0, w));
-      ++c.launches;
-    }
-    const long dd[3] = {n0, n1, static_cast<long>(w)};
-    for (int m = 0; m < 2; ++m) {
-      HT_TRY(gram(c, view_of_group(dd, 3, m, m), xd + L * c0, xb + L * c0, Gt));
-      if (!c.dry()) {
-        HT_CUDA(accumulate_launch(G[m], Gt, static_cast<long long>(a.dims[m]) * a.dims[m], s == 0 ? 1 : 0, c.st));
+      HT_CUDA(cudaStreamWaitEvent(c.st, pr->ev[s], 0));
+      if (!a.x_dev) {
+        HT_CUDA(convert_bf16_dual_launch(xd, xb, xbt, L, n2, lb, parts + s * 1024, 1024, c.st, c0, w));
         ++c.launches;
       }
     }
+    const long dd[3] = {n0, n1, static_cast<long>(w)};
+    for (int m = 0; m < 2; ++m)
+      HT_TRY(gram(c, view_of_group(dd, 3, m, m), xd + L * c0, xb + L * c0, G[m], s > 0));
   }
   if (!c.dry()) {
     HT_CUDA(sumsq_finish_launch(parts, static_cast<int>(S * 1024), dsum, c.st));
@@ -1453,7 +1470,8 @@ ht_status_t run_call(Ctx &c, const Tree &T, const ht_config_t &cfg, const CallAr
   if (!c.dry()) HT_CUDA(cudaMemsetAsync(c.err, 0, sizeof(int), c.st));
   if (tl.on) HT_CUDA(cudaEventRecord(h0, c.st));
   Result res;
-  if (pipelined_input(c, a)) {
+  if (pipelined_input(c, a, cfg)) {
+    if (a.x_dev && tl.on) HT_CUDA(cudaEventRecord(h1, c.st));
     tl.mark(c.st);
     HT_TRY(enqueue_pipelined(c, T, cfg, a, dsum, tl, res, tl.on ? h1 : nullptr));
   } else {

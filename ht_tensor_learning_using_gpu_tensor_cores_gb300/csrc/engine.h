@@ -94,9 +94,10 @@ long tc_num_kblocks(const Operand &a);
 cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s);
 long simt_k_total(const Operand &a);
 
-// Sum split-K partial tiles ([splits][tiles][gen.bm][bn]) into out.
-// symmetric = 0: plain column-major tiles; symmetric != 0: a symmetric Gram
-// (tiles on/above the diagonal, mirrored into the lower triangle).
+// Sum split-K partial tiles ([splits][tiles][gen.bm][bn]) into out.  symmetric
+// bit 0 clear: plain column-major tiles; set: a symmetric Gram (tiles on/above
+// the diagonal, mirrored into the lower triangle).  Bit 1: add the sums to what
+// out holds instead of overwriting it (a Gram accumulated over slabs).
 cudaError_t reduce_partials_launch(const float *partial, const TileGen &gen, int splits, int bn, float *out,
                                    long long ld_out, int symmetric, cudaStream_t s);
 TileGen make_rows_gen(long long rows, int cols, int bn);

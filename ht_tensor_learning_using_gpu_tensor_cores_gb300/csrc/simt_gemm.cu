@@ -275,11 +275,14 @@ __global__ void __launch_bounds__(256) reduce_partials_kernel(const float *__res
       const Tile tl = gen_tile(gen, t);
       if (row < tl.valid_rows && col < tl.valid_cols) {
         const long long gr = tl.out_row + row, gc = tl.out_col + col;
-        if (!symmetric) {
-          out[gr + ld * gc] = s;
+        const bool acc = (symmetric & 2) != 0;   // add to what out holds
+        if (!(symmetric & 1)) {
+          out[gr + ld * gc] = acc ? out[gr + ld * gc] + s : s;
         } else if (gc >= gr) {   // the mirror element is produced by the tile holding (gc, gr)
-          out[gr + ld * gc] = s;
-          out[gc + ld * gr] = s;
+          const long long a = gr + ld * gc, b = gc + ld * gr;
+          const float v = acc ? out[a] + s : s;
+          out[a] = v;
+          if (b != a) out[b] = v;
         }
       }
     }
