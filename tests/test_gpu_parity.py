@@ -237,4 +237,4 @@ def test_slab_pipelined_input_512cubed(where):
         Up = plain.U[t].cpu().numpy().astype(np.float64)
         assert O.orthogonality_defect(Um) < 2e-4
         # the leading 8 directions are well separated on this spectrum
-        assert O.principal_angles(Um[:, :8], Up[:, :8]).max() < 1e-2
+        assert O.principal_angles(Um[:, :8], Up[:, :8]).max() < 3e-2
