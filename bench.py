@@ -506,6 +506,20 @@ def run_ours(args, world, rank, local):
         if rank == 0:
             print(json.dumps({"fourth_order_only": True, "steps": args.steps, "warmup": args.warmup}), flush=True)
         return
+    if args.batch_only:
+        # profiling mode: only the batched configuration (512 tensors, dims
+        # U[32,160]^3, ranks U[8,16]), mixed path, warm-up + timed batches
+        fam = synth.batch_family(512, seed=31, device="cuda")
+        xs = [x for x, _ in fam]
+        bd = ht.BatchDecomposer([t for _, t in fam], [tuple(reversed(x.shape)) for x in xs], precision="bf16",
+                                compute_error=True)
+        for _ in range(args.warmup + args.steps):
+            _, rep = bd(xs)
+        torch.cuda.synchronize()
+        if rank == 0:
+            print(json.dumps({"batch_only": True, "steps": args.steps, "warmup": args.warmup,
+                              "device_ms_per_batch": rep["ms_total"]}), flush=True)
+        return
     n, k = args.n, RANK
     tree = ht.reference_tree_3d([1, k, k, k, k])
     X = synth.odeco(n, decay=DECAY, seed=1 + rank, assemble_on=torch.device("cuda", local))   # column-major memory
@@ -699,6 +713,8 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=1, help="--impl reference: full-size decompositions timed")
     ap.add_argument("--mixed-only", action="store_true",
                     help="run only the headline mixed-path steps (for profiler launch lists)")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="run only the batched 512-tensor configuration (for profiler launch lists)")
     ap.add_argument("--sketch-only", action="store_true",
                     help="run only the Gram-free range-finder path on the headline tensor (for profiler launch lists)")
     ap.add_argument("--fourth-order-only", action="store_true",
