@@ -229,6 +229,7 @@ struct GemmReq {
   bool allow_split = true;
   bool fold = false;                // tcgen05 only: b16 is a high/low split (GemmArgs::fold)
   int mt_tc = 1;                    // tcgen05 only: 2 = 256-row tiles (GemmArgs::mt)
+  __nv_bfloat16 *out16 = nullptr;   // column-major output wanted in BF16 here (q.out may then be scratch)
 };
 
 // D = A B^T over the tiles: tcgen05 on the BF16 operands when the context
@@ -283,6 +284,10 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
   g.err = c.err;
   g.fold = (use_tc && q.fold) ? 1 : 0;
   g.mt = mt;
+  // a BF16 column-major output comes straight from the tcgen05 epilogue, else
+  // from the FP32 result converted afterwards
+  const bool direct16 = q.out16 && use_tc && !partial;
+  g.out16 = direct16 ? q.out16 : nullptr;
   if (use_tc) {
     HT_CUDA(tc_gemm_launch(g, bn, c.st));
     c.path |= 1;
@@ -294,6 +299,10 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
   if (partial) {
     HT_CUDA(reduce_partials_launch(part, gen, splits, bn, q.out, q.ld_out,
                                    (q.symmetric ? 1 : 0) | (q.accumulate ? 2 : 0), c.st));
+    ++c.launches;
+  }
+  if (q.out16 && !direct16) {   // rows x cols column-major, ld = rows
+    HT_CUDA(f32_to_bf16_launch(q.out, q.out16, q.ld_out * q.t_cols, c.st));
     ++c.launches;
   }
   c.ar.off = mark;   // scratch is stream-ordered: later work may reuse it
@@ -358,8 +367,9 @@ ht_status_t gram_transposed(Ctx &c, const View &v, const float *x32, const __nv_
 // fold_h > 0: W16 is the split_bf16 form of W32 (v.N x 2*fold_h, high part in
 // columns [0, k), low part in [fold_h, fold_h + k)), so the tcgen05 product
 // carries W to about 16 significant bits instead of BF16's 8.
+// Z16 non-null: the product is wanted in BF16 there (Z is then FP32 scratch).
 ht_status_t mode_product(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x16, const float *W32,
-                         const __nv_bfloat16 *W16, int k, float *Z, int fold_h = 0) {
+                         const __nv_bfloat16 *W16, int k, float *Z, int fold_h = 0, __nv_bfloat16 *Z16 = nullptr) {
   GemmReq q;
   auto opA = [&](const void *x) {
     Operand o;
@@ -388,6 +398,7 @@ ht_status_t mode_product(Ctx &c, const View &v, const float *x32, const __nv_bfl
   }
   q.out_mode = OUT_COLMAJOR;
   q.out = Z;
+  q.out16 = Z16;
   q.ld_out = v.L * v.R;
   return run_gemm(c, q);
 }
@@ -690,17 +701,12 @@ ht_status_t leaf_sketch(Ctx &c, const Tree &T, const ht_config_t &cfg, const lon
   // Nystrom core later pairs with Y (any block serves as a test matrix).
   auto apply_gram = [&](int m, float *Qsrc, float *Ydst) -> ht_status_t {
     const View v = view_of_group(dims, order, m, m);
-    const long long LR = v.L * v.R;
     const int s = S[m];
     if (c.tc && !c.dry()) {
       HT_CUDA(round_bf16_launch(Qsrc, Q16, dims[m] * s, c.st));
       ++c.launches;
     }
-    HT_TRY(mode_product(c, v, x32, x16, Qsrc, Q16, s, Z32));
-    if (c.tc && !c.dry()) {
-      HT_CUDA(f32_to_bf16_launch(Z32, Z16, LR * s, c.st));
-      ++c.launches;
-    }
+    HT_TRY(mode_product(c, v, x32, x16, Qsrc, Q16, s, Z32, 0, c.tc ? Z16 : nullptr));
     if (c.tc && m == order - 1 && x16t) {
       Operand o;
       o.kind = OP_KM3; o.ptr = x16t; o.d0 = 1l << lb; o.d1 = v.N; o.d2 = v.L >> lb;

@@ -77,6 +77,9 @@ struct GemmArgs {
   // tcgen05 path: 2 = each CTA computes a 256-row tile as two 128-row
   // accumulators that share every B stage (TileGen::bm must be 256)
   int mt = 1;
+  // tcgen05 path, column-major output only: non-null = write the output in
+  // BF16 here instead of FP32 to `out`
+  __nv_bfloat16 *out16 = nullptr;
 };
 
 // tcgen05 path (BF16 operands), BM = 128, BN in {64, 128, 256}.

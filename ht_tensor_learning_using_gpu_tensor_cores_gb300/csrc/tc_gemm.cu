@@ -57,6 +57,7 @@ struct KParams {
   int *err;
   int fold;
   int same;    // A and B are the same operand: a tile with a_row == b_row loads one panel
+  __nv_bfloat16 *out16;   // OUT_COLMAJOR only: write the tile in BF16 here instead of FP32 to out
 };
 
 // Issue the TMA loads of one operand tile (ROWS x 64 K) for k-block kb.
@@ -211,10 +212,18 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
         for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4 *>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
       } else if (row < tile.valid_rows) {
-        float *dst = p.out + tile.out_row + row + p.ld_out * static_cast<long long>(tile.out_col + c0);
+        const long long off = tile.out_row + row + p.ld_out * static_cast<long long>(tile.out_col + c0);
+        if (p.out16) {
+          __nv_bfloat16 *dst = p.out16 + off;
 #pragma unroll
-        for (int j = 0; j < 32; ++j)
-          if (c0 + j < tile.valid_cols) dst[p.ld_out * j] = v[j];
+          for (int j = 0; j < 32; ++j)
+            if (c0 + j < tile.valid_cols) dst[p.ld_out * j] = __float2bfloat16_rn(v[j]);
+        } else {
+          float *dst = p.out + off;
+#pragma unroll
+          for (int j = 0; j < 32; ++j)
+            if (c0 + j < tile.valid_cols) dst[p.ld_out * j] = v[j];
+        }
       }
     }
   }
@@ -324,6 +333,7 @@ cudaError_t launch_bn(const GemmArgs &g, cudaStream_t s) {
   p.ld_out = g.ld_out;
   p.err = g.err;
   p.fold = (g.fold && g.out_mode == OUT_COLMAJOR) ? 1 : 0;
+  p.out16 = g.out_mode == OUT_COLMAJOR ? g.out16 : nullptr;
   p.same = (g.a.ptr == g.b.ptr && g.a.kind == g.b.kind && g.a.d0 == g.b.d0 && g.a.d1 == g.b.d1 && g.a.d2 == g.b.d2) ? 1 : 0;
   cudaError_t e = set_smem<BN, MT>();
   if (e != cudaSuccess) return e;

@@ -35,6 +35,8 @@ struct TqCfg {
   static constexpr int LD = KM + 1;                                  // row stride (floats): conflict-free rows
   static constexpr int WARP_FLOATS = (KM + TQ_PROWS) * LD;           // R (KM rows) + panel (64 rows)
   static constexpr size_t SMEM = size_t(WARPS) * WARP_FLOATS * sizeof(float);
+  static constexpr int RPL = KM == 32 ? 4 : 2;                       // panel rows per lane in the main loop
+  static constexpr int PANEL = 32 * RPL;                             // main-loop panel height
 };
 
 // Sum over the warp, the same value in every lane (lane 0's reduction order).
@@ -122,22 +124,28 @@ HT_DEV void warp_qr_fold(float *R, float *P, int prow, int k) {
   }
 }
 
-// The same fold for k <= 32 with the panel in registers (lane l: rows l and
-// l + 32, all 32 columns): no shared-memory traffic for the panel, and the
-// column extraction is a select over the unrolled register array.
-template <int LD>
-HT_DEV void warp_qr_fold32(float *R, float (&p0)[32], float (&p1)[32], int k) {
+// The same fold for k <= 32 with the panel in registers: lane l holds rows
+// l + 32 q (q < RPL) of all 32 columns.  The column extraction is a select over
+// the unrolled register array; the shuffles of one column step (the column
+// norm, the 32-column reduce-scatter and the broadcast of the 32 updates) are
+// shared by all 32 RPL rows of the panel, so taller panels amortise them.
+template <int LD, int RPL>
+HT_DEV void warp_qr_fold32(float *R, float (&p)[RPL][32], int k) {
   const int lane = threadIdx.x & 31;
   for (int j = 0; j < k; ++j) {
     float r = lane < k ? R[j * LD + lane] : 0.f;
-    float x0 = 0.f, x1 = 0.f;
+    float x[RPL];
 #pragma unroll
-    for (int c = 0; c < 32; ++c)
-      if (c == j) {
-        x0 = p0[c];
-        x1 = p1[c];
-      }
-    const float sig = warp_sum_bcast(fmaf(x0, x0, x1 * x1));
+    for (int q = 0; q < RPL; ++q) {
+      x[q] = 0.f;
+#pragma unroll
+      for (int c = 0; c < 32; ++c)
+        if (c == j) x[q] = p[q][c];
+    }
+    float ss = 0.f;
+#pragma unroll
+    for (int q = 0; q < RPL; ++q) ss = fmaf(x[q], x[q], ss);
+    const float sig = warp_sum_bcast(ss);
     const float rjj = __shfl_sync(0xffffffffu, r, j);
     if (sig != 0.f) {   // else the column below the pivot is already zero
       const float nrm = sqrtf(fmaf(rjj, rjj, sig));
@@ -146,7 +154,12 @@ HT_DEV void warp_qr_fold32(float *R, float (&p0)[32], float (&p1)[32], int k) {
       const float tau = -1.f / (alpha * v0);
       float v[32];
 #pragma unroll
-      for (int c = 0; c < 32; ++c) v[c] = c > j ? fmaf(x0, p0[c], x1 * p1[c]) : 0.f;
+      for (int c = 0; c < 32; ++c) {
+        float a = 0.f;
+#pragma unroll
+        for (int q = 0; q < RPL; ++q) a = fmaf(x[q], p[q][c], a);
+        v[c] = c > j ? a : 0.f;
+      }
       const float w = fmaf(v0, r, warp_reduce_scatter32(v));
       const float tw = (lane > j && lane < k) ? tau * w : 0.f;
       r = fmaf(-tw, v0, r);
@@ -154,8 +167,8 @@ HT_DEV void warp_qr_fold32(float *R, float (&p0)[32], float (&p1)[32], int k) {
       for (int c = 0; c < 32; ++c) {
         const float twc = __shfl_sync(0xffffffffu, tw, c);
         if (c > j) {
-          p0[c] = fmaf(-twc, x0, p0[c]);
-          p1[c] = fmaf(-twc, x1, p1[c]);
+#pragma unroll
+          for (int q = 0; q < RPL; ++q) p[q][c] = fmaf(-twc, x[q], p[q][c]);
         }
       }
       if (lane == j) r = alpha;
@@ -170,13 +183,13 @@ template <int KM, int LD>
 HT_DEV void warp_fold_smem(float *R, float *P, int prow, int k) {
   if constexpr (KM == 32) {
     const int lane = threadIdx.x & 31;
-    float p0[32], p1[32];
+    float p[2][32];
 #pragma unroll
     for (int c = 0; c < 32; ++c) {
-      p0[c] = (lane < prow && c < k) ? P[lane * LD + c] : 0.f;
-      p1[c] = (lane + 32 < prow && c < k) ? P[(lane + 32) * LD + c] : 0.f;
+      p[0][c] = (lane < prow && c < k) ? P[lane * LD + c] : 0.f;
+      p[1][c] = (lane + 32 < prow && c < k) ? P[(lane + 32) * LD + c] : 0.f;
     }
-    warp_qr_fold32<LD>(R, p0, p1, k);
+    warp_qr_fold32<LD, 2>(R, p, k);
   } else {
     warp_qr_fold<KM, LD>(R, P, prow, k);
   }
@@ -211,18 +224,19 @@ __global__ void __launch_bounds__(TqCfg<KM>::THREADS, 1) tsqr_kernel(const TqPar
   // 1. this CTA's rows, in 64-row panels dealt round-robin to the warps
   const long long r_begin = static_cast<long long>(blockIdx.x) * p.rows_per_cta;
   const long long r_end = min(p.m, r_begin + p.rows_per_cta);
-  for (long long r0 = r_begin + static_cast<long long>(warp) * TQ_PROWS; r0 < r_end;
-       r0 += static_cast<long long>(C::WARPS) * TQ_PROWS) {
-    const int prow = static_cast<int>(min(static_cast<long long>(TQ_PROWS), r_end - r0));
+  for (long long r0 = r_begin + static_cast<long long>(warp) * C::PANEL; r0 < r_end;
+       r0 += static_cast<long long>(C::WARPS) * C::PANEL) {
+    const int prow = static_cast<int>(min(static_cast<long long>(C::PANEL), r_end - r0));
     if constexpr (KM == 32) {   // the panel straight into registers
-      float p0[32], p1[32];
+      float pr[TqCfg<KM>::RPL][32];
 #pragma unroll
       for (int c = 0; c < 32; ++c) {
         const float *col = p.A + r0 + p.lda * c;
-        p0[c] = (c < k && lane < prow) ? __ldg(col + lane) : 0.f;
-        p1[c] = (c < k && lane + 32 < prow) ? __ldg(col + lane + 32) : 0.f;
+#pragma unroll
+        for (int q = 0; q < TqCfg<KM>::RPL; ++q)
+          pr[q][c] = (c < k && lane + 32 * q < prow) ? __ldg(col + lane + 32 * q) : 0.f;
       }
-      warp_qr_fold32<LD>(R, p0, p1, k);
+      warp_qr_fold32<LD, TqCfg<KM>::RPL>(R, pr, k);
     } else {
 #pragma unroll 4
       for (int c = 0; c < k; ++c) {
