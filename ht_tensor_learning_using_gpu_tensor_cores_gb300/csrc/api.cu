@@ -230,6 +230,10 @@ struct GemmReq {
   bool fold = false;                // tcgen05 only: b16 is a high/low split (GemmArgs::fold)
   int mt_tc = 1;                    // tcgen05 only: 2 = 256-row tiles (GemmArgs::mt)
   __nv_bfloat16 *out16 = nullptr;   // column-major output wanted in BF16 here (q.out may then be scratch)
+  // split-K partials into the caller's buffer with exactly force_splits
+  // splits, no reduction (the caller reduces several launches' partials at once)
+  float *part_ext = nullptr;
+  int force_splits = 0;
 };
 
 // D = A B^T over the tiles: tcgen05 on the BF16 operands when the context
@@ -253,7 +257,9 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
   const int nt = gen.count;
   int splits = 1;
   if (q.allow_split && nt < sm_count()) splits = std::max(1, sm_count() / nt);
-  if (use_tc) {
+  if (q.force_splits > 0) {
+    splits = q.force_splits;
+  } else if (use_tc) {
     const long nkb = tc_num_kblocks(q.a16);
     long per = (nkb + splits - 1) / splits;
     per = std::max<long>(per, std::min<long>(nkb, 16));   // keep the smem pipeline busy
@@ -266,7 +272,8 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
   }
   const bool partial = splits > 1 || q.out_mode == OUT_PARTIAL;
   const size_t mark = c.ar.off;
-  float *part = partial ? c.ar.take<float>(static_cast<size_t>(splits) * nt * gen.bm * bn) : nullptr;
+  float *part = q.part_ext ? q.part_ext
+                           : (partial ? c.ar.take<float>(static_cast<size_t>(splits) * nt * gen.bm * bn) : nullptr);
   if (c.dry()) {
     c.ar.off = mark;
     return HT_OK;
@@ -296,7 +303,7 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
     c.path |= 2;
   }
   ++c.launches;
-  if (partial) {
+  if (partial && !q.part_ext) {
     HT_CUDA(reduce_partials_launch(part, gen, splits, bn, q.out, q.ld_out,
                                    (q.symmetric ? 1 : 0) | (q.accumulate ? 2 : 0), c.st));
     ++c.launches;
@@ -309,16 +316,23 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
   return HT_OK;
 }
 
+// tcgen05 tile of an n x n Gram: 256 x 256 (two M = 128 accumulators) from n = 256 up
+int gram_bn_tc(long n) { return n >= 256 ? 256 : (n > 64 ? 128 : 64); }
+int gram_mt_tc(long n) { return n >= 256 ? 2 : 1; }
+
 // G (n x n, column-major, symmetric) = X_(group) X_(group)^T, n = v.N
-// (accumulate: G += X_(group) X_(group)^T)
+// (accumulate: G += X_(group) X_(group)^T).  part_ext: leave the split-K
+// partials (force_splits of them) in that buffer unreduced.
 ht_status_t gram(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x16, float *G,
-                 bool accumulate = false) {
+                 bool accumulate = false, float *part_ext = nullptr, int force_splits = 0) {
   GemmReq q;
   q.a32 = q.b32 = gram_operand(v, x32);
   if (x16) q.a16 = q.b16 = gram_operand(v, x16);
   else q.a16.ptr = q.b16.ptr = nullptr;
-  q.bn_tc = v.N >= 256 ? 256 : (v.N > 64 ? 128 : 64);
-  q.mt_tc = v.N >= 256 ? 2 : 1;   // 256 x 256 tiles, diagonal ones loading a single panel
+  q.part_ext = part_ext;
+  q.force_splits = force_splits;
+  q.bn_tc = gram_bn_tc(v.N);
+  q.mt_tc = gram_mt_tc(v.N);   // 256 x 256 tiles, diagonal ones loading a single panel
   q.bn_simt = v.N > 64 ? 128 : 64;
   q.tiles_kind = TILES_GRAM;
   q.t_n = v.N;
@@ -1395,10 +1409,32 @@ ht_status_t enqueue_pipelined(Ctx &c, const Tree &T, const ht_config_t &cfg, con
   float *xd = a.x_dev ? const_cast<float *>(a.x) : c.ar.take<float>(static_cast<size_t>(total));
   __nv_bfloat16 *xb = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
   __nv_bfloat16 *xbt = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
-  double *parts = c.ar.take<double>(static_cast<size_t>(S) * 1024);
+  // device input: the conversion runs beside the Grams, so it takes 5 CTAs per
+  // SM (32 registers x 256 threads each), which leaves an SM's registers and
+  // threads for one Gram CTA (192 threads x 80 registers)
+  const int np_conv = a.x_dev ? std::min(1024, 5 * sm_count()) : 1024;
+  double *parts = c.ar.take<double>(static_cast<size_t>(S) * np_conv);
   float *G[4] = {};
   G[0] = c.ar.take<float>(static_cast<size_t>(n0) * n0);
   G[1] = c.ar.take<float>(static_cast<size_t>(n1) * n1);
+  // the slab Grams of modes 1 and 2 leave their split-K partials side by side
+  // (slab-major) and each mode is reduced once after the last slab
+  TileGen ggen[2];
+  int gsplits[2];
+  float *gpart[2];
+  for (int m = 0; m < 2; ++m) {
+    const long nm = a.dims[m];
+    const int bn = gram_bn_tc(nm), mt = gram_mt_tc(nm);
+    if (!make_gram_gen(nm, bn, &ggen[m], 128 * mt)) return fail(HT_ERR_UNSUPPORTED, "Gram larger than 32768");
+    const int nt = ggen[m].count;
+    int sp = nt < sm_count() ? std::max(1, sm_count() / nt) : 1;
+    const long long kb = (static_cast<long long>(a.dims[1 - m]) * len + 63) / 64;   // K blocks of a full slab
+    long long per = (kb + sp - 1) / sp;
+    per = std::max<long long>(per, std::min<long long>(kb, 16));
+    gsplits[m] = static_cast<int>((kb + per - 1) / per);
+    gpart[m] = c.ar.take<float>(static_cast<size_t>(S) * gsplits[m] * nt * ggen[m].bm * bn);
+    if (!gpart[m]) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (pipelined Gram partials)");
+  }
   if (!xd || !xb || !xbt || !parts || !G[0] || !G[1])
     return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (pipelined input)");
   PipeRes *pr = nullptr;
@@ -1410,7 +1446,7 @@ ht_status_t enqueue_pipelined(Ctx &c, const Tree &T, const ht_config_t &cfg, con
     for (long long s = 0; s < S; ++s) {
       const long long c0 = s * len, w = std::min(len, n2 - c0);
       if (a.x_dev) {
-        HT_CUDA(convert_bf16_dual_launch(xd, xb, xbt, L, n2, lb, parts + s * 1024, 1024, pr->cs, c0, w));
+        HT_CUDA(convert_bf16_dual_launch(xd, xb, xbt, L, n2, lb, parts + s * np_conv, np_conv, pr->cs, c0, w));
         ++c.launches;
       } else {
         HT_CUDA(cudaMemcpyAsync(xd + L * c0, a.x + L * c0, sizeof(float) * L * w, cudaMemcpyHostToDevice, pr->cs));
@@ -1424,16 +1460,24 @@ ht_status_t enqueue_pipelined(Ctx &c, const Tree &T, const ht_config_t &cfg, con
     if (!c.dry()) {
       HT_CUDA(cudaStreamWaitEvent(c.st, pr->ev[s], 0));
       if (!a.x_dev) {
-        HT_CUDA(convert_bf16_dual_launch(xd, xb, xbt, L, n2, lb, parts + s * 1024, 1024, c.st, c0, w));
+        HT_CUDA(convert_bf16_dual_launch(xd, xb, xbt, L, n2, lb, parts + s * np_conv, np_conv, c.st, c0, w));
         ++c.launches;
       }
     }
     const long dd[3] = {n0, n1, static_cast<long>(w)};
-    for (int m = 0; m < 2; ++m)
-      HT_TRY(gram(c, view_of_group(dd, 3, m, m), xd + L * c0, xb + L * c0, G[m], s > 0));
+    for (int m = 0; m < 2; ++m) {
+      const size_t slab_part = static_cast<size_t>(gsplits[m]) * ggen[m].count * ggen[m].bm * ggen[m].bn;
+      HT_TRY(gram(c, view_of_group(dd, 3, m, m), xd + L * c0, xb + L * c0, G[m], false, gpart[m] + s * slab_part,
+                  gsplits[m]));
+    }
   }
   if (!c.dry()) {
-    HT_CUDA(sumsq_finish_launch(parts, static_cast<int>(S * 1024), dsum, c.st));
+    for (int m = 0; m < 2; ++m) {
+      HT_CUDA(reduce_partials_launch(gpart[m], ggen[m], static_cast<int>(S) * gsplits[m], ggen[m].bn, G[m], a.dims[m],
+                                     1, c.st));
+      ++c.launches;
+    }
+    HT_CUDA(sumsq_finish_launch(parts, static_cast<int>(S * np_conv), dsum, c.st));
     ++c.launches;
   }
   tl.mark(c.st);
