@@ -344,6 +344,26 @@ ht_status_t gram(Ctx &c, const View &v, const float *x32, const __nv_bfloat16 *x
   return run_gemm(c, q);
 }
 
+// The Gram of view v (FP32 operands from x32) with its BF16 operands read from
+// the first-mode-padded copy x16p, whose view of the same mode group is vp
+// (vp.N = n1p for the first mode; rows beyond v.N are zero and clipped).
+ht_status_t gram_padded(Ctx &c, const View &v, const View &vp, const float *x32, const __nv_bfloat16 *x16p,
+                        float *G) {
+  GemmReq q;
+  q.a32 = q.b32 = gram_operand(v, x32);
+  q.a16 = q.b16 = gram_operand(vp, x16p);
+  q.bn_tc = gram_bn_tc(v.N);
+  q.mt_tc = gram_mt_tc(v.N);
+  q.bn_simt = v.N > 64 ? 128 : 64;
+  q.tiles_kind = TILES_GRAM;
+  q.t_n = v.N;
+  q.out_mode = OUT_PARTIAL;
+  q.out = G;
+  q.ld_out = v.N;
+  q.symmetric = true;
+  return run_gemm(c, q);
+}
+
 // l-block exponent of the last mode's second BF16 copy (0: no copy).
 int last_mode_block(const long *dims, int order) {
   if (order != 3) return 0;
@@ -825,9 +845,12 @@ ht_status_t transfer3_from_z(Ctx &c, const Plan3 &P, const long *dims, const Eig
 }
 
 // G_pre[m] non-null: the mode-m Gram is already there (the pipelined input path).
+// x16p: a BF16 copy with the first mode padded to n1p rows (zeros), used by the
+// leaf Grams when n1 is not a multiple of 8 (TMA needs 16-byte rows).
 ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const float *x32,
                            const __nv_bfloat16 *x16, const __nv_bfloat16 *x16t, int lb, const long *dims,
-                           int order, Result &res, Timeline &tl, float *const *G_pre = nullptr) {
+                           int order, Result &res, Timeline &tl, float *const *G_pre = nullptr,
+                           const __nv_bfloat16 *x16p = nullptr, long n1p = 0) {
   const int p_over = cfg.oversample > 0 ? cfg.oversample : 16;
   const bool d3 = order == 3;
   Plan3 P3{};
@@ -848,10 +871,13 @@ ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const 
       G[m] = (G_pre && G_pre[m]) ? G_pre[m] : c.ar.take<float>(static_cast<size_t>(dims[m]) * dims[m]);
       if (!G[m]) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (Gram)");
     }
+    long pdims[HT_MAX_ORDER];
+    for (int m = 0; m < order; ++m) pdims[m] = (m == 0 && x16p) ? n1p : dims[m];
     for (int m = 0; m < order; ++m) {
       if (G_pre && G_pre[m]) continue;
       const View v = view_of_group(dims, order, m, m);
-      if (m == order - 1 && x16t) HT_TRY(gram_transposed(c, v, x32, x16t, lb, G[m]));
+      if (x16p) HT_TRY(gram_padded(c, v, view_of_group(pdims, order, m, m), x32, x16p, G[m]));
+      else if (m == order - 1 && x16t) HT_TRY(gram_transposed(c, v, x32, x16t, lb, G[m]));
       else HT_TRY(gram(c, v, x32, x16, G[m]));
     }
     tl.mark(c.st);
@@ -1324,9 +1350,18 @@ ht_status_t enqueue_body(Ctx &c, const Tree &T, const ht_config_t &cfg, const fl
                          double *nparts, double *dsum, Timeline &tl, Result &res) {
   long long total = 1;
   for (int m = 0; m < a.order; ++m) total *= a.dims[m];
-  __nv_bfloat16 *xb = nullptr, *xbt = nullptr;
+  __nv_bfloat16 *xb = nullptr, *xbt = nullptr, *xp = nullptr;
   int lb = c.tc ? last_mode_block(a.dims, a.order) : 0;
-  if (c.tc) {
+  // first mode not a multiple of 8: the Grams read a copy padded to n1p rows
+  // (the tcgen05 path's TMA rows must be 16-byte multiples); the other products
+  // of such a tensor run on the FP32 operands
+  const long n1 = a.dims[0], n1p = (n1 + 7) / 8 * 8;
+  if (c.tc && n1 % 8 != 0 && cfg.leaf_method == HT_LEAF_GRAM) {
+    xp = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total / n1 * n1p) + 64);
+    if (!xp) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (padded bf16 tensor)");
+    if (!c.dry()) HT_CUDA(convert_bf16_pad_launch(xd, xp, n1, n1p, total / n1, nparts, 1024, c.st));
+    lb = 0;
+  } else if (c.tc) {
     xb = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
     if (!xb) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (bf16 tensor)");
     if (lb && (reinterpret_cast<uintptr_t>(xd) & 15u) == 0) {
@@ -1346,7 +1381,7 @@ ht_status_t enqueue_body(Ctx &c, const Tree &T, const ht_config_t &cfg, const fl
   }
   tl.mark(c.st);
   if (!xbt) lb = 0;
-  HT_TRY(decompose_core(c, T, cfg, xd, xb, xbt, lb, a.dims, a.order, res, tl));
+  HT_TRY(decompose_core(c, T, cfg, xd, xb, xbt, lb, a.dims, a.order, res, tl, nullptr, xp, n1p));
   // outputs to the caller's buffers (host or device)
   for (int t = 0; t < T.n_nodes; ++t) {
     float *dst = T.leaf(t) ? a.U[t] : a.B[t];

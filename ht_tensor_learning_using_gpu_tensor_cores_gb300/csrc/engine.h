@@ -116,6 +116,9 @@ int device_sm_count();
 cudaError_t convert_bf16_launch(const float *x, __nv_bfloat16 *xb, long long n, double *sumsq_partials,
                                 int num_partials, cudaStream_t s);
 cudaError_t sumsq_launch(const float *x, long long n, double *partials, int num_partials, cudaStream_t s);
+// X (n1 x rest, FP32) -> xp (n1p x rest, BF16, rows n1..n1p-1 zero) + sum-of-squares partials
+cudaError_t convert_bf16_pad_launch(const float *x, __nv_bfloat16 *xp, long long n1, long long n1p, long long rest,
+                                    double *partials, int num_partials, cudaStream_t s);
 // dst = src (first != 0) or dst += src, n floats
 cudaError_t accumulate_launch(float *dst, const float *src, long long n, int first, cudaStream_t s);
 // X (L x N) -> xb (same layout) and xbt (l-blocks of B = 2^lb: xbt[((l/B) N + n) B + l%B])

@@ -45,6 +45,31 @@ __global__ void __launch_bounds__(256, 8) convert_bf16_kernel(const float *__res
   if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
 }
 
+// X (n1 x rest, FP32, first index fastest) -> xp (n1p x rest, BF16, zero rows
+// n1 <= i < n1p) and the compensated sum of squares per block.  The padded copy
+// gives every matricisation a leading dimension that TMA can address (a
+// multiple of 8 BF16 elements) when n1 itself is not one.
+__global__ void __launch_bounds__(256) convert_bf16_pad_kernel(const float *__restrict__ x, __nv_bfloat16 *__restrict__ xp,
+                                                             long long n1, long long n1p, long long rest,
+                                                             double *partials) {
+  Acc2 a = {0.f, 0.f};
+  const long long total = n1p * rest;
+  for (long long e = blockIdx.x * 256ll + threadIdx.x; e < total; e += gridDim.x * 256ll) {
+    const long long r = e / n1p, i = e - r * n1p;
+    const float v = i < n1 ? __ldcs(x + i + n1 * r) : 0.f;
+    acc2_add_prod(a, v, v);
+    xp[e] = __float2bfloat16_rn(v);
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = static_cast<double>(a.s) + static_cast<double>(a.c);
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
+}
+
 // X (L x N, l fastest, FP32) -> xb (the same layout, BF16) and xbt, a second
 // BF16 copy in l-blocks of B = 2^lb elements: xbt[((l / B) N + n) B + l % B],
 // plus the compensated sum of squares per block, over the columns n in
@@ -384,6 +409,13 @@ int grid_for(long long n, int cap = 0) {
 }
 
 }  // namespace
+
+cudaError_t convert_bf16_pad_launch(const float *x, __nv_bfloat16 *xp, long long n1, long long n1p, long long rest,
+                                    double *partials, int num_partials, cudaStream_t s) {
+  if (n1 < 1 || n1p < n1 || rest < 1 || num_partials < 1) return cudaErrorInvalidValue;
+  convert_bf16_pad_kernel<<<num_partials, 256, 0, s>>>(x, xp, n1, n1p, rest, partials);
+  return cudaGetLastError();
+}
 
 cudaError_t convert_bf16_launch(const float *x, __nv_bfloat16 *xb, long long n, double *partials, int num_partials,
                                 cudaStream_t s) {

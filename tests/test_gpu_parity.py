@@ -238,3 +238,17 @@ def test_slab_pipelined_input_512cubed(where):
         assert O.orthogonality_defect(Um) < 2e-4
         # the leading 8 directions are well separated on this spectrum
         assert O.principal_angles(Um[:, :8], Up[:, :8]).max() < 3e-2
+
+
+@pytest.mark.parametrize("dims", [(37, 45, 51), (61, 64, 40), (45, 32, 24, 17)])
+def test_unaligned_first_mode_uses_padded_bf16_grams(dims):
+    """A first mode that is not a multiple of 8 cannot be addressed by TMA in
+    place; the mixed path then reads its leaf Grams from a zero-padded BF16
+    copy and still runs them on tcgen05, within the BF16 bar of the oracle."""
+    if len(dims) == 3:
+        tree = ht.reference_tree_3d([1, 8, 6, 7, 6])
+    else:
+        tree = ht.balanced_tree_4d([1, 10, 10, 5, 5, 5, 5])
+    X = synth.exact_ht(dims, tree, noise_rel=1e-3, seed=17)
+    res, e, e64 = check_against_oracle(X, tree, "bf16")
+    assert res.report["path"]["tcgen05"]
