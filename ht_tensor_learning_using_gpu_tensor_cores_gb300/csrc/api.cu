@@ -1405,7 +1405,9 @@ ht_status_t enqueue_body(Ctx &c, const Tree &T, const ht_config_t &cfg, const fl
 constexpr int kPipeSlabs = 8;
 
 bool pipelined_input(const Ctx &c, const CallArgs &a, const ht_config_t &cfg) {
-  if (!c.tc || a.order != 3 || cfg.leaf_method != HT_LEAF_GRAM) return false;
+  // device input stays on the plain path: measured at 1024^3, the conversion on
+  // a side stream did not overlap the slab Grams (5.63 ms against 5.38 ms)
+  if (a.x_dev || !c.tc || a.order != 3 || cfg.leaf_method != HT_LEAF_GRAM) return false;
   const int lb = last_mode_block(a.dims, a.order);
   if (lb != 8) return false;   // 16-column conversion tiles: slabs of multiples of 16 columns
   if (a.x_dev && (reinterpret_cast<uintptr_t>(a.x) & 15u) != 0) return false;

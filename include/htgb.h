@@ -98,11 +98,11 @@ typedef struct {
     float ms_total;          /* device time of the decomposition (CUDA events)    */
     float ms_stage[8];       /* 0 input/convert, 1 grams, 2 eig, 3 core pass,
                                 4 transfer tensors, 5 error, 6 h2d, 7 d2h.  When a
-                                3rd-order BF16 Gram-path call takes X in slabs
-                                (tensors of 256 MiB and more), stage 0 also holds
-                                the mode-1/2 Grams, which overlap the conversion
-                                (device input) or the copy (host input), and
-                                stage 1 the last mode's Gram alone.  With
+                                3rd-order BF16 Gram-path call with host input
+                                takes X in slabs (tensors of 256 MiB and more),
+                                stage 0 also holds the mode-1/2 Grams, which
+                                overlap the copy, and stage 1 the last mode's
+                                Gram alone.  With
                                 HT_LEAF_SKETCH stage 1 is the whole range finder
                                 and stage 2 is empty.                             */
     double eig_residual[HT_MAX_NODES]; /* max_j ||G u_j - theta_j u_j|| / theta_1   */

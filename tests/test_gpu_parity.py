@@ -216,9 +216,9 @@ def test_numerically_rank_deficient_large_modes(prec):
 
 @pytest.mark.parametrize("where", ["device", "host"])
 def test_slab_pipelined_input_512cubed(where):
-    """3rd-order BF16 Gram-path inputs of 256 MiB and more run slab by slab: the
-    mode-1/2 Grams accumulate over 8 slabs along mode 3 while the next slab is
-    converted (device input) or copied (host input).  At 512^3 on the r^-1.5
+    """3rd-order BF16 Gram-path host inputs of 256 MiB and more run slab by slab:
+    the mode-1/2 Grams accumulate over 8 slabs along mode 3 while the next slab
+    is copied (device inputs take the plain path).  At 512^3 on the r^-1.5
     family the error matches the closed-form FP64 optimum within 1e-3 and the
     plain path's (not pipelined) within 1e-3, the leaf bases are orthonormal, and
     the leading leaf subspaces agree with the plain path's."""
