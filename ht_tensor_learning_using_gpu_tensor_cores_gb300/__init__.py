@@ -267,10 +267,20 @@ class BatchDecomposer:
 
     def __init__(self, trees: Sequence[DimTree], dims: Sequence[Sequence[int]], precision: str = "bf16",
                  compute_error: bool = True, oversample: int = 16, eig_iters: int = 10, seed: int = 1234,
-                 device=None):
+                 device=None, tuning=None):
+        """tuning: None keeps the default launch shape and the given eig_iters /
+        oversample; "auto" takes them from the autotuner's table for the bucket
+        of the batch's largest dimension (autotune.lookup); a dict with keys
+        lanes, eig_ctas, eig_iters, oversample sets them explicitly."""
         import torch
+        from . import autotune
         if len(trees) != len(dims) or not trees:
             raise ValueError("one tree per tensor, at least one tensor")
+        if tuning == "auto":
+            tuning = autotune.lookup(dims, precision=precision)
+        self.tuning = dict(tuning) if tuning is not None else None
+        if self.tuning is not None:
+            eig_iters, oversample = int(self.tuning["eig_iters"]), int(self.tuning["oversample"])
         order = trees[0].order
         if any(t.order != order for t in trees):
             raise ValueError("every tensor of a batch has the same order")
@@ -312,6 +322,8 @@ class BatchDecomposer:
             self.xptr[i] = x.data_ptr()
         if stream is None:
             stream = torch.cuda.current_stream(tensors[0].device).cuda_stream
+        t = self.tuning or {"lanes": 0, "eig_ctas": 0}
+        check(lib().ht_batch_set_tuning(int(t["lanes"]), int(t["eig_ctas"])))
         rep = HtBatchReport()
         check(lib().ht_decompose_batched(self.count, self.xptr, self.cdims, self.order, self.ts, ctypes.byref(self.cfg),
                                          self.uptr, self.bptr, self.rel if self.compute_error else None,

@@ -24,7 +24,7 @@ EXPORTED = ["ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", 
             "ht_decompose", "ht_reconstruct_error", "ht_workspace_size", "ht_release_workspace",
             "ht_status_string", "ht_last_error", "ht_kernel_launch_count", "htd", "htd4",
             "ht_mode_gram", "ht_mode_product", "ht_corange_product", "ht_tsqr", "ht_selftest_wait_timeout", "ht_mode_gram_noalloc",
-            "ht_decompose_batched", "ht_release_batch", "ht_sketch_loss_grad", "ht_sketch_adam",
+            "ht_decompose_batched", "ht_release_batch", "ht_batch_set_tuning", "ht_sketch_loss_grad", "ht_sketch_adam",
             "ht_reconstruct", "ht_evaluate", "ht_layer_weight", "ht_layer_forward", "ht_layer_backward",
             "ht_layer_check", "ht_layer_release", "ht_decompose_streaming"]
 
@@ -123,8 +123,9 @@ def lib():
                                      c_void_p, c_void_p]
     L.ht_tsqr.argtypes = [c_void_p, c_longlong, c_int, c_longlong, c_void_p, c_void_p]
     L.ht_selftest_wait_timeout.argtypes = [c_int, c_double, c_void_p]
+    L.ht_batch_set_tuning.argtypes = [c_int, c_int]
     for name in ("ht_decompose_streaming", "ht_layer_weight", "ht_layer_forward", "ht_layer_backward", "ht_layer_check", "ht_layer_release",
-                 "ht_reconstruct", "ht_evaluate", "ht_sketch_loss_grad", "ht_sketch_adam", "ht_decompose_batched", "ht_release_batch", "ht_mode_gram", "ht_mode_gram_noalloc", "ht_mode_product", "ht_corange_product", "ht_tsqr", "ht_selftest_wait_timeout", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
+                 "ht_reconstruct", "ht_evaluate", "ht_sketch_loss_grad", "ht_sketch_adam", "ht_decompose_batched", "ht_release_batch", "ht_mode_gram", "ht_mode_gram_noalloc", "ht_mode_product", "ht_corange_product", "ht_tsqr", "ht_selftest_wait_timeout", "ht_batch_set_tuning", "ht_config_default", "ht_tree_reference_3d", "ht_tree_balanced_4d", "ht_tree_validate",
                  "ht_decompose", "ht_reconstruct_error", "ht_workspace_size", "ht_release_workspace"):
         getattr(L, name).restype = c_int
     _lib = L

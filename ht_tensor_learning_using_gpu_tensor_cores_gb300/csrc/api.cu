@@ -1629,7 +1629,17 @@ size_t dry_run_bytes(const Tree &T, const ht_config_t &cfg, const CallArgs &a) {
 }
 
 // ------------------------------------------------------------ batched path
-constexpr int kLanes = 16;
+constexpr int kLanes = 32;          // streams a batch may be spread over (at most)
+constexpr int kDefaultLanes = 16;
+
+// Launch shape of the batched path, per device: lanes (concurrent streams) and
+// the cap on each lane's cooperative eigen-solver grid (0: SMs / lanes, at
+// least 8).  Set by ht_batch_set_tuning (an autotuner's table), read per call.
+struct BatchTuning {
+  int lanes = kDefaultLanes;
+  int eig_ctas = 0;
+};
+BatchTuning g_batch_tuning[64];
 
 struct BatchState {
   std::vector<unsigned long long> key;
@@ -1970,11 +1980,14 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   std::lock_guard<std::mutex> lk(g_batch_mutex);
   BatchState &b = g_batch[dev];
-  // identity of the batch: shapes, trees, config and every pointer
+  const BatchTuning tune = g_batch_tuning[dev];
+  // identity of the batch: shapes, trees, config, launch shape and every pointer
   std::vector<unsigned long long> key;
   key.reserve(static_cast<size_t>(count) * (order + 2 * HT_MAX_NODES + 2 + sizeof(ht_tree_t) / 4) + 16);
   key.push_back(static_cast<unsigned long long>(count));
   key.push_back(static_cast<unsigned long long>(order));
+  key.push_back(static_cast<unsigned long long>(tune.lanes));
+  key.push_back(static_cast<unsigned long long>(tune.eig_ctas));
   {
     const unsigned char *cb = reinterpret_cast<const unsigned char *>(&cfg);
     for (size_t q = 0; q < sizeof(cfg); ++q) key.push_back(cb[q]);
@@ -2010,8 +2023,8 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
     lane_bytes = (lane_bytes + 4095) & ~size_t(4095);
     batch_drop_graph(b);
     HT_TRY(batch_streams(b));
-    b.lanes = std::min(kLanes, count);
-    const size_t need = static_cast<size_t>(kLanes) * lane_bytes + sizeof(double) * 2 * count + 4096;
+    b.lanes = std::min(tune.lanes, count);
+    const size_t need = static_cast<size_t>(b.lanes) * lane_bytes + sizeof(double) * 2 * count + 4096;
     if (b.ws_bytes < need) {
       if (b.ws) {
         HT_CUDA(cudaDeviceSynchronize());
@@ -2022,10 +2035,10 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
       HT_CUDA(cudaMalloc(&b.ws, need));
       b.ws_bytes = need;
     }
-    char *tail = static_cast<char *>(b.ws) + static_cast<size_t>(kLanes) * lane_bytes;
+    char *tail = static_cast<char *>(b.ws) + static_cast<size_t>(b.lanes) * lane_bytes;
     b.errw = reinterpret_cast<int *>(tail);
     b.sums = reinterpret_cast<double *>(tail + 256);
-    const int eig_ctas = std::max(8, sm_count() / b.lanes);
+    const int eig_ctas = tune.eig_ctas > 0 ? tune.eig_ctas : std::max(8, sm_count() / b.lanes);
     HT_CUDA(tc_prepare());   // one-time kernel attributes outside the capture
     HT_CUDA(eig_prepare());
     // record the batch into a graph (captured from a private stream: the
@@ -2105,6 +2118,18 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
     report->graph_replayed = replay ? 1 : 0;
     report->lanes = b.lanes;
   }
+  return HT_OK;
+}
+
+ht_status_t ht_batch_set_tuning(int lanes, int eig_ctas) {
+  if (lanes < 0 || lanes > kLanes || eig_ctas < 0)
+    return fail(HT_ERR_INVALID_ARG, "lanes must lie in [0, " + std::to_string(kLanes) + "], eig_ctas >= 0");
+  int dev = 0;
+  HT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(HT_ERR_INVALID_ARG, "device index out of range");
+  std::lock_guard<std::mutex> lk(g_batch_mutex);
+  g_batch_tuning[dev].lanes = lanes > 0 ? lanes : kDefaultLanes;
+  g_batch_tuning[dev].eig_ctas = eig_ctas;
   return HT_OK;
 }
 

@@ -275,6 +275,12 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
                                  ht_batch_report_t *report, void *stream);
 /* Free the batched path's cached graph and workspace on the current device. */
 ht_status_t ht_release_batch(void);
+/* Launch shape of later ht_decompose_batched calls on the current device:
+ * lanes = concurrent streams (1..32, 0 = the default 16) and eig_ctas = cap on
+ * each lane's cooperative eigen-solver grid (0 = SMs / lanes, at least 8).  The
+ * library's autotuner (autotune.tune_batched) picks them per size bucket; no
+ * counterpart in the reference, which has no batched path. */
+ht_status_t ht_batch_set_tuning(int lanes, int eig_ctas);
 
 /* ---------------------------------------------------------- learned sketch */
 /* Training of a per-mode sketch S (n x s): the start block of the leaf range
