@@ -256,8 +256,10 @@ def secondary_configs(ht, synth, torch, stream, steps=10, warmup=3):
     dims = [tuple(reversed(x.shape)) for x in xs]
     rec = {"tensors": len(xs), "dims": "U[32,160]^3", "ranks": "U[8,16]", "noise_rel": 1e-3,
            "input_bytes": int(sum(x.numel() for x in xs) * 4)}
-    for prec, key in (("bf16", "mixed"), ("fp32", "plain")):
-        bd = ht.BatchDecomposer(trees, dims, precision=prec, compute_error=True)
+    from ht_tensor_learning_using_gpu_tensor_cores_gb300 import autotune
+    rec["tuned_config"] = autotune.lookup(dims, precision="bf16")
+    for prec, key, tuning in (("bf16", "mixed_tuned", "auto"), ("bf16", "mixed", None), ("fp32", "plain", None)):
+        bd = ht.BatchDecomposer(trees, dims, precision=prec, compute_error=True, tuning=tuning)
         _, rep = bd(xs)                      # records the graph
         for _ in range(2):
             _, rep = bd(xs)
