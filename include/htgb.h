@@ -80,7 +80,8 @@ typedef struct {
     int precision;        /* ht_precision_t                                      */
     int leaf_method;      /* ht_leaf_method_t                                    */
     int oversample;       /* subspace size = k + oversample (default 16)         */
-    int eig_iters;        /* subspace iterations per leaf Gram (default 10)      */
+    int eig_iters;        /* subspace iterations per leaf Gram (default 0 =
+                             10 on the FP32 path, 6 on the mixed path)           */
     int power_steps;      /* power steps of the range finder (default 1)         */
     unsigned long long seed;  /* Gaussian start / test matrices (default 1234)   */
     const float *sketch[HT_MAX_ORDER]; /* optional start matrices per mode, n_m x (k+p),

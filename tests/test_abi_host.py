@@ -140,7 +140,7 @@ def test_compute_fails_loudly_without_device():
 def test_config_defaults():
     cfg = _lib.HtConfig()
     assert _lib.lib().ht_config_default(ctypes.byref(cfg)) == 0
-    assert cfg.precision == _lib.PREC_BF16 and cfg.oversample == 16 and cfg.eig_iters == 10
+    assert cfg.precision == _lib.PREC_BF16 and cfg.oversample == 16 and cfg.eig_iters == 0   # 0: per-precision default
     assert cfg.seed == 1234 and cfg.power_steps == 1
     assert _lib.lib().ht_status_string(5) == b"kernel wait timed out"
 
