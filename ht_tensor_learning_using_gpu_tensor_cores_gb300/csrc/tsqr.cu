@@ -199,7 +199,7 @@ struct TqParams {
   const float *A;
   long long m, lda;
   int k;
-  long long rows_per_cta;   // multiple of 64
+  long long rows_per_cta;   // a multiple of warps x panel rows
   float *slots;             // per level: count_l x k x k floats (row-major R)
   long long slot_off[8];    // float offset of level l's slots
   int cnt_off[8];           // offset of level l's group counters
@@ -357,7 +357,10 @@ cudaError_t tsqr_launch(const float *A, long long m, int k, long long lda, float
   p.lda = lda;
   p.k = k;
   const long long grid = tq_grid(m);
-  p.rows_per_cta = ((m + grid - 1) / grid + TQ_PROWS - 1) / TQ_PROWS * TQ_PROWS;
+  // a CTA's rows are a whole number of rounds of panels over its warps, so the
+  // warps finish together (the tree that follows waits for the slowest)
+  const long long round = k <= 32 ? TqCfg<32>::WARPS * TqCfg<32>::PANEL : TqCfg<64>::WARPS * TqCfg<64>::PANEL;
+  p.rows_per_cta = ((m + grid - 1) / grid + round - 1) / round * round;
   const long long g = (m + p.rows_per_cta - 1) / p.rows_per_cta;   // CTAs that own rows
   long long counts[8];
   const int L = tq_levels(g, counts);
