@@ -38,7 +38,23 @@ __all__ = ["DimTree", "reference_tree_3d", "left_first_tree_3d", "middle_tree_3d
 _PREC = {"fp32": PREC_FP32, "bf16": PREC_BF16}
 
 
+_TREE_STRUCTS: Dict[tuple, HtTree] = {}
+
+
 def _tree_struct(tree: DimTree) -> HtTree:
+    """The C struct of a tree (cached by the tree's contents: the C side only
+    reads it)."""
+    key = (tree.order, tuple(tree.left), tuple(tree.right), tuple(tree.ranks), tuple(map(tuple, tree.modes)))
+    t = _TREE_STRUCTS.get(key)
+    if t is None:
+        t = _make_tree_struct(tree)
+        if len(_TREE_STRUCTS) >= 256:
+            _TREE_STRUCTS.clear()
+        _TREE_STRUCTS[key] = t
+    return t
+
+
+def _make_tree_struct(tree: DimTree) -> HtTree:
     f = tree.as_struct_fields()
     t = HtTree()
     t.order, t.n_nodes = f["order"], f["n_nodes"]
@@ -103,14 +119,16 @@ def _out_buffers(tree: DimTree, dims, like):
             B[t] = np.zeros((kl, kr, tree.ranks[t]), dtype=np.float32, order="F")
         ptr = lambda a: a.ctypes.data
     else:
+        # column-major factors allocated directly (one torch call each); the
+        # call writes every element, so they are not cleared
         import torch
         dev = like.device
         for t in tree.leaves():
             n, k = dims[tree.modes[t][0]], tree.ranks[t]
-            U[t] = torch.zeros((k, n), dtype=torch.float32, device=dev).t()
+            U[t] = torch.empty_strided((n, k), (1, n), dtype=torch.float32, device=dev)
         for t in [0] + tree.interior():
-            kl, kr = tree.ranks[tree.left[t]], tree.ranks[tree.right[t]]
-            B[t] = torch.zeros((tree.ranks[t], kr, kl), dtype=torch.float32, device=dev).permute(2, 1, 0)
+            kl, kr, kt = tree.ranks[tree.left[t]], tree.ranks[tree.right[t]], tree.ranks[t]
+            B[t] = torch.empty_strided((kl, kr, kt), (1, kl, kl * kr), dtype=torch.float32, device=dev)
         ptr = lambda a: a.data_ptr()
     uptr = (c_void_p * 7)()
     bptr = (c_void_p * 7)()
@@ -124,8 +142,28 @@ def _out_buffers(tree: DimTree, dims, like):
 _LEAF = {"gram": LEAF_GRAM, "sketch": LEAF_SKETCH}
 
 
+_CONFIGS: Dict[tuple, HtConfig] = {}
+
+
 def _config(precision: str, oversample: int, eig_iters: int, power_steps: int, seed: int, flags: int,
             sketch=None, eig_tol: float = 0.0, leaf_method: str = "gram") -> tuple:
+    """(ht_config_t, objects to keep alive during the call).  Configurations
+    without sketch blocks are cached: the C side only reads them."""
+    if sketch is None:
+        key = (precision, oversample, eig_iters, power_steps, seed, flags, eig_tol, leaf_method)
+        cfg = _CONFIGS.get(key)
+        if cfg is None:
+            cfg, _ = _make_config(precision, oversample, eig_iters, power_steps, seed, flags, None, eig_tol,
+                                  leaf_method)
+            if len(_CONFIGS) >= 256:
+                _CONFIGS.clear()
+            _CONFIGS[key] = cfg
+        return cfg, []
+    return _make_config(precision, oversample, eig_iters, power_steps, seed, flags, sketch, eig_tol, leaf_method)
+
+
+def _make_config(precision: str, oversample: int, eig_iters: int, power_steps: int, seed: int, flags: int,
+                 sketch=None, eig_tol: float = 0.0, leaf_method: str = "gram") -> tuple:
     cfg = HtConfig()
     check(lib().ht_config_default(ctypes.byref(cfg)))
     if precision not in _PREC:

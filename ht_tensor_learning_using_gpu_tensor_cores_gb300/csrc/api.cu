@@ -76,6 +76,20 @@ struct DeviceWorkspace {
 std::mutex g_ws_mutex;
 DeviceWorkspace g_ws[64];
 
+// Per-device host state of the single-tensor call, guarded by g_ws_mutex:
+// a page-locked block that receives the call's status words in one copy (a
+// pageable copy costs a full host round trip each), the timing events (made
+// once, not per call), and the workspace sizes of recent call signatures (the
+// dry run that sizes a call plans every launch on the host).
+struct CallHostState {
+  char *status = nullptr;      // cudaHostAlloc'd, kStatusBytes
+  cudaEvent_t ev[10] = {};
+  bool ev_made = false;
+  std::vector<std::pair<std::string, size_t>> sizes;
+};
+CallHostState g_call[64];
+constexpr size_t kStatusBytes = 352;
+
 // Bump allocator over one device buffer.  In dry-run mode it only counts.
 struct Arena {
   char *base = nullptr;
@@ -181,12 +195,23 @@ ht_status_t parse_tree(const ht_tree_t *in, const long *dims, int order, Tree &t
 struct Ctx {
   cudaStream_t st = nullptr;
   int *err = nullptr;   // device error word
+  float *resid_slots = nullptr;   // per-leaf eigen residuals inside the call's status block (or null)
   Arena ar;
   int launches = 0;
   int path = 0;         // bit 0 tcgen05, bit 1 SIMT
   bool tc = false;
   int eig_ctas = 0;     // cap on the cooperative eigen-solver's grid (0 = every SM)
-  bool dry() const { return ar.dry; }
+  // Two-phase enqueue of the batched path.  eig_mode 0: leaf_eigs launches
+  // the cooperative solver; 1: it appends its problems to eig_table (the
+  // grouped solver's entries) and launches nothing; 2: it launches nothing
+  // (the batch launches the grouped solver).  Launches before the leaf
+  // solver (mute_pre) or after it (mute_post) are skipped while the arena
+  // still hands out the same real pointers, so the phases of one tensor agree.
+  int eig_mode = 0;
+  std::vector<unsigned char> *eig_table = nullptr;
+  int eig_iters_used = 0, eig_refine_used = 0;
+  bool mute_pre = false, mute_post = false, past_eig = false;
+  bool dry() const { return ar.dry || (past_eig ? mute_post : mute_pre); }
 };
 
 View view_of_group(const long *dims, int order, int lo, int hi) {   // modes [lo, hi]
@@ -609,7 +634,7 @@ ht_status_t leaf_eigs(Ctx &c, const Tree &T, const ht_config_t &cfg, const long 
     e.U = c.ar.take<float>(static_cast<size_t>(n) * K);
     e.GU = c.ar.take<float>(static_cast<size_t>(n) * K);
     e.theta = c.ar.take<float>(64);
-    e.resid = c.ar.take<float>(4);
+    e.resid = c.resid_slots ? c.resid_slots + leaf : c.ar.take<float>(4);
     e.seed = cfg.seed;
     e.stream_id = static_cast<uint64_t>(m);
     e.start = nullptr;
@@ -629,7 +654,7 @@ ht_status_t leaf_eigs(Ctx &c, const Tree &T, const ht_config_t &cfg, const long 
   }
   {
     const size_t mark = c.ar.off;
-    const size_t eb = eig_workspace_bytes(ep, order);
+    const size_t eb = c.eig_mode ? eig_grouped_workspace_bytes(ep, order) : eig_workspace_bytes(ep, order);
     void *ews = c.ar.take<char>(eb);
     if (!ews) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (eig)");
     // the FP32 path keeps two CholeskyQR refinement passes (its error sits at
@@ -643,7 +668,11 @@ ht_status_t leaf_eigs(Ctx &c, const Tree &T, const ht_config_t &cfg, const long 
     bool sketched = false;
     for (int m = 0; m < order; ++m) sketched = sketched || cfg.sketch[m] != nullptr;
     const int refine = (cfg.precision == HT_PREC_FP32 || iters < 4 || sketched) ? 2 : 0;
-    if (!c.dry()) HT_CUDA(eig_batched(ep, order, iters, ews, eb, c.err, c.st, &c.launches, c.eig_ctas, refine));
+    c.past_eig = true;
+    c.eig_iters_used = iters;
+    c.eig_refine_used = refine;
+    if (c.eig_mode == 1 && !c.ar.dry) HT_CUDA(eig_grouped_fill(ep, order, ews, eb, *c.eig_table));
+    if (c.eig_mode == 0 && !c.dry()) HT_CUDA(eig_batched(ep, order, iters, ews, eb, c.err, c.st, &c.launches, c.eig_ctas, refine));
     c.ar.off = mark;
   }
   return HT_OK;
@@ -1534,29 +1563,35 @@ ht_status_t enqueue_pipelined(Ctx &c, const Tree &T, const ht_config_t &cfg, con
 ht_status_t run_call(Ctx &c, const Tree &T, const ht_config_t &cfg, const CallArgs &a, ht_report_t *rep) {
   long long total = 1;
   for (int m = 0; m < a.order; ++m) total *= a.dims[m];
-  c.err = c.ar.take<int>(64);
+  // the call's status block, read back in one copy: ||X||^2 and the error
+  // pass's sum (8 doubles, bytes 0-63), the error word (64 ints, 64-319) and
+  // the leaf eigen residuals (8 floats, 320-351)
+  char *status = reinterpret_cast<char *>(c.ar.take<double>(kStatusBytes / sizeof(double)));
   double *nparts = c.ar.take<double>(1024);
-  double *dsum = c.ar.take<double>(8);
-  if (!c.err || !nparts || !dsum) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small");
+  if (!status || !nparts) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small");
+  double *dsum = reinterpret_cast<double *>(status);
+  c.err = reinterpret_cast<int *>(status + 64);
+  c.resid_slots = reinterpret_cast<float *>(status + 320);
   Timeline tl;
   tl.on = rep != nullptr && !c.dry();
   cudaEvent_t h0 = nullptr, h1 = nullptr;
-  if (tl.on) {
-    for (int i = 0; i < 8; ++i) HT_CUDA(cudaEventCreate(&tl.ev[i]));
-    HT_CUDA(cudaEventCreate(&h0));
-    HT_CUDA(cudaEventCreate(&h1));
-  }
-  struct Guard {
-    Timeline &tl;
-    cudaEvent_t a, b;
-    ~Guard() {
-      if (tl.on) {
-        for (int i = 0; i < 8; ++i) cudaEventDestroy(tl.ev[i]);
-        cudaEventDestroy(a);
-        cudaEventDestroy(b);
-      }
+  CallHostState *hs = nullptr;
+  if (!c.dry()) {
+    int dev = 0;
+    HT_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(HT_ERR_INVALID_ARG, "device index out of range");
+    hs = &g_call[dev];
+    if (!hs->status) HT_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&hs->status), kStatusBytes, cudaHostAllocDefault));
+    if (tl.on && !hs->ev_made) {
+      for (int i = 0; i < 10; ++i) HT_CUDA(cudaEventCreate(&hs->ev[i]));
+      hs->ev_made = true;
     }
-  } guard{tl, h0, h1};
+    if (tl.on) {
+      for (int i = 0; i < 8; ++i) tl.ev[i] = hs->ev[i];
+      h0 = hs->ev[8];
+      h1 = hs->ev[9];
+    }
+  }
   if (!c.dry()) HT_CUDA(cudaMemsetAsync(c.err, 0, sizeof(int), c.st));
   if (tl.on) HT_CUDA(cudaEventRecord(h0, c.st));
   Result res;
@@ -1577,15 +1612,16 @@ ht_status_t run_call(Ctx &c, const Tree &T, const ht_config_t &cfg, const CallAr
     HT_TRY(enqueue_body(c, T, cfg, xd, a, nparts, dsum, tl, res));
   }
   if (c.dry()) return HT_OK;
-  double host_sums[2] = {0.0, 0.0};
-  HT_CUDA(cudaMemcpyAsync(host_sums, dsum, sizeof(double) * (a.want_err ? 2 : 1), cudaMemcpyDeviceToHost, c.st));
-  int errword = 0;
-  HT_CUDA(cudaMemcpyAsync(&errword, c.err, sizeof(int), cudaMemcpyDeviceToHost, c.st));
-  float resid[HT_MAX_NODES] = {};
-  for (int t = 0; t < T.n_nodes; ++t)
-    if (T.leaf(t) && res.resid[t]) HT_CUDA(cudaMemcpyAsync(&resid[t], res.resid[t], sizeof(float), cudaMemcpyDeviceToHost, c.st));
+  HT_CUDA(cudaMemcpyAsync(hs->status, status, kStatusBytes, cudaMemcpyDeviceToHost, c.st));
   HT_CUDA(cudaStreamSynchronize(c.st));
   HT_CUDA(cudaGetLastError());
+  double host_sums[2] = {0.0, 0.0};
+  std::memcpy(host_sums, hs->status, sizeof(double) * (a.want_err ? 2 : 1));
+  int errword = 0;
+  std::memcpy(&errword, hs->status + 64, sizeof(int));
+  float resid[HT_MAX_NODES] = {};
+  for (int t = 0; t < T.n_nodes; ++t)
+    if (T.leaf(t) && res.resid[t]) std::memcpy(&resid[t], hs->status + 320 + sizeof(float) * t, sizeof(float));
   if (errword & kErrTimeout) return fail(HT_ERR_TIMEOUT, "a kernel's bounded wait expired; results are invalid");
   if (!std::isfinite(host_sums[0])) return fail(HT_ERR_NUMERICAL, "input tensor contains NaN or Inf");
   if (errword & kErrBreakdown) return fail(HT_ERR_NUMERICAL, "a factorisation broke down (non-orthonormal basis)");
@@ -1623,9 +1659,10 @@ ht_status_t run_call(Ctx &c, const Tree &T, const ht_config_t &cfg, const CallAr
   return HT_OK;
 }
 
-size_t dry_run_bytes(const Tree &T, const ht_config_t &cfg, const CallArgs &a) {
+size_t dry_run_bytes(const Tree &T, const ht_config_t &cfg, const CallArgs &a, int eig_mode = 0) {
   Ctx d;
   d.ar.dry = true;
+  d.eig_mode = eig_mode;
   d.tc = cfg.precision == HT_PREC_BF16;
   run_call(d, T, cfg, a, nullptr);
   return d.ar.peak + (1 << 20);
@@ -1656,7 +1693,24 @@ struct BatchState {
   double *sums = nullptr;   // device: [count][2] (||X||^2, ||X - Xhat||^2)
   int *errw = nullptr;      // device: one error word per lane
   int launches = 0, lanes = 0;
+  void *table = nullptr;    // device: the grouped leaf solver's problem table
+  size_t table_bytes = 0;
 };
+
+// Workspace layout of one batch.  Per-lane mode: tensor i runs in lane
+// i % lanes's region (lane_bytes each), after the previous tensor of that
+// lane.  Grouped mode: tensor i has the region [off[i], off[i + 1]) of its
+// own, so that its state survives between the two phases around the grouped
+// leaf solver (nprob problems, iters / refine as every tensor's leaf_eigs).
+struct BatchLayout {
+  bool grouped = false;
+  size_t lane_bytes = 0;
+  std::vector<size_t> off;
+  int nprob = 0, iters = 0, refine = 0;
+};
+// Leaves of at most this size go through the grouped solver (one CTA each);
+// batches with larger modes keep the per-lane cooperative solver.
+constexpr long kGroupedMaxN = 512;
 BatchState g_batch[64];
 std::mutex g_batch_mutex;
 
@@ -1681,16 +1735,18 @@ ht_status_t batch_streams(BatchState &b) {
   return HT_OK;
 }
 
-// Enqueue every tensor of the batch on the lanes, forked from and joined back
-// into `st`.  Tensor i runs on lane i % lanes, after the previous tensor of
-// that lane, in the lane's workspace region.
-ht_status_t batch_enqueue(BatchState &b, cudaStream_t st, int count, const float *const *x, const long *dims,
-                          int order, const std::vector<Tree> &trees, const ht_config_t &cfg, float *const *U,
-                          float *const *B, bool want_err, size_t lane_bytes, int eig_ctas) {
-  HT_CUDA(cudaMemsetAsync(b.errw, 0, sizeof(int) * kLanes, st));
-  HT_CUDA(cudaEventRecord(b.fork, st));
-  for (int l = 0; l < b.lanes; ++l) HT_CUDA(cudaStreamWaitEvent(b.lane[l], b.fork, 0));
-  b.launches = 0;
+// One pass over every tensor of the batch.  phase 0: the whole chain of each
+// tensor; 1: its launches up to the leaf Grams; 2: its launches after the leaf
+// solver; 3: no launches, the grouped solver's table is filled (host only).
+// Phases 0-2 run on the lanes, forked from and joined back into `st`.
+ht_status_t batch_pass(BatchState &b, const BatchLayout &L, int phase, cudaStream_t st, int count,
+                       const float *const *x, const long *dims, int order, const std::vector<Tree> &trees,
+                       const ht_config_t &cfg, float *const *U, float *const *B, bool want_err, int eig_ctas,
+                       std::vector<unsigned char> *table, int *iters_used, int *refine_used) {
+  if (phase != 3) {
+    HT_CUDA(cudaEventRecord(b.fork, st));
+    for (int l = 0; l < b.lanes; ++l) HT_CUDA(cudaStreamWaitEvent(b.lane[l], b.fork, 0));
+  }
   for (int i = 0; i < count; ++i) {
     const int l = i % b.lanes;
     Ctx c;
@@ -1698,8 +1754,17 @@ ht_status_t batch_enqueue(BatchState &b, cudaStream_t st, int count, const float
     c.tc = cfg.precision == HT_PREC_BF16;
     c.eig_ctas = eig_ctas;
     c.err = b.errw + l;
-    c.ar.base = static_cast<char *>(b.ws) + static_cast<size_t>(l) * lane_bytes;
-    c.ar.cap = lane_bytes;
+    if (L.grouped) {
+      c.ar.base = static_cast<char *>(b.ws) + L.off[i];
+      c.ar.cap = L.off[i + 1] - L.off[i];
+      c.eig_mode = phase == 3 ? 1 : 2;
+      c.eig_table = table;
+      c.mute_pre = phase == 2 || phase == 3;
+      c.mute_post = phase == 1 || phase == 3;
+    } else {
+      c.ar.base = static_cast<char *>(b.ws) + static_cast<size_t>(l) * L.lane_bytes;
+      c.ar.cap = L.lane_bytes;
+    }
     double *nparts = c.ar.take<double>(1024);
     if (!nparts) return fail(HT_ERR_OUT_OF_MEMORY, "batch workspace too small");
     CallArgs a{x[i], true, dims + static_cast<size_t>(i) * order, order, U + static_cast<size_t>(i) * HT_MAX_NODES,
@@ -1708,11 +1773,59 @@ ht_status_t batch_enqueue(BatchState &b, cudaStream_t st, int count, const float
     Result res;
     HT_TRY(enqueue_body(c, trees[i], cfg, x[i], a, nparts, b.sums + 2 * static_cast<size_t>(i), tl, res));
     b.launches += c.launches;
+    if (iters_used) *iters_used = c.eig_iters_used;
+    if (refine_used) *refine_used = c.eig_refine_used;
   }
-  for (int l = 0; l < b.lanes; ++l) {
-    HT_CUDA(cudaEventRecord(b.join[l], b.lane[l]));
-    HT_CUDA(cudaStreamWaitEvent(st, b.join[l], 0));
+  if (phase != 3) {
+    for (int l = 0; l < b.lanes; ++l) {
+      HT_CUDA(cudaEventRecord(b.join[l], b.lane[l]));
+      HT_CUDA(cudaStreamWaitEvent(st, b.join[l], 0));
+    }
   }
+  return HT_OK;
+}
+
+// Enqueue the whole batch on `st`.  Grouped mode: the lanes run every
+// tensor's conversion and leaf Grams, ONE launch of the grouped leaf solver
+// covers every leaf of every tensor (its table uploaded beforehand by
+// batch_plan_grouped), then the lanes run the rest of every tensor.
+ht_status_t batch_enqueue(BatchState &b, const BatchLayout &L, cudaStream_t st, int count, const float *const *x,
+                          const long *dims, int order, const std::vector<Tree> &trees, const ht_config_t &cfg,
+                          float *const *U, float *const *B, bool want_err, int eig_ctas) {
+  HT_CUDA(cudaMemsetAsync(b.errw, 0, sizeof(int) * kLanes, st));
+  b.launches = 0;
+  if (!L.grouped)
+    return batch_pass(b, L, 0, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas, nullptr, nullptr,
+                      nullptr);
+  HT_TRY(batch_pass(b, L, 1, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas, nullptr, nullptr,
+                    nullptr));
+  HT_CUDA(eig_grouped_launch(b.table, L.nprob, L.iters, L.refine, st));
+  b.launches += 1;
+  return batch_pass(b, L, 2, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas, nullptr, nullptr,
+                    nullptr);
+}
+
+// Host-only pass that lays out every leaf problem of the batch for the
+// grouped solver and copies the table to the device (outside any capture).
+ht_status_t batch_plan_grouped(BatchState &b, BatchLayout &L, int count, const float *const *x, const long *dims,
+                               int order, const std::vector<Tree> &trees, const ht_config_t &cfg, float *const *U,
+                               float *const *B, bool want_err) {
+  std::vector<unsigned char> table;
+  int iters = 0, refine = 0;
+  const int launches = b.launches;
+  HT_TRY(batch_pass(b, L, 3, nullptr, count, x, dims, order, trees, cfg, U, B, want_err, 0, &table, &iters, &refine));
+  b.launches = launches;
+  L.nprob = static_cast<int>(table.size() / eig_grouped_entry_bytes());
+  L.iters = iters;
+  L.refine = refine;
+  if (table.size() > b.table_bytes) {
+    if (b.table) HT_CUDA(cudaFree(b.table));
+    b.table = nullptr;
+    b.table_bytes = 0;
+    HT_CUDA(cudaMalloc(&b.table, table.size()));
+    b.table_bytes = table.size();
+  }
+  if (!table.empty()) HT_CUDA(cudaMemcpy(b.table, table.data(), table.size(), cudaMemcpyHostToDevice));
   return HT_OK;
 }
 
@@ -1804,6 +1917,47 @@ ht_status_t ht_release_workspace(void) {
   return HT_OK;
 }
 
+// Workspace bytes of a single-tensor call, from the cache of recent call
+// signatures on this device or a dry run.  The signature holds everything the
+// dry run's plan depends on: the device, the dims, the tree, the configuration
+// (its sketch blocks as absent / host / device), where X lives and its 16-byte
+// alignment, and whether the error pass runs.  Call with g_ws_mutex held.
+ht_status_t sized_call_bytes(const Tree &T, const ht_config_t &cfg, const CallArgs &a, size_t *bytes) {
+  int dev = 0;
+  HT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(HT_ERR_INVALID_ARG, "device index out of range");
+  long long key[64];
+  int n = 0;
+  key[n++] = dev;
+  key[n++] = a.order;
+  for (int m = 0; m < a.order; ++m) key[n++] = a.dims[m];
+  key[n++] = T.n_nodes;
+  for (int t = 0; t < T.n_nodes; ++t)
+    key[n++] = (static_cast<long long>(T.left[t] + 1) << 48) | (static_cast<long long>(T.right[t] + 1) << 40) |
+               (static_cast<long long>(T.mask[t]) << 32) | static_cast<unsigned>(T.rank[t]);
+  key[n++] = cfg.precision;
+  key[n++] = cfg.leaf_method;
+  key[n++] = cfg.oversample;
+  key[n++] = cfg.eig_iters;
+  key[n++] = cfg.power_steps;
+  key[n++] = cfg.flags;
+  for (int m = 0; m < a.order; ++m) key[n++] = cfg.sketch[m] ? (is_device_ptr(cfg.sketch[m]) ? 2 : 1) : 0;
+  key[n++] = a.x_dev;
+  key[n++] = static_cast<long long>(reinterpret_cast<uintptr_t>(a.x) & 15u);
+  key[n++] = a.want_err;
+  const std::string k(reinterpret_cast<const char *>(key), sizeof(long long) * n);
+  auto &cache = g_call[dev].sizes;
+  for (const auto &e : cache)
+    if (e.first == k) {
+      *bytes = e.second;
+      return HT_OK;
+    }
+  *bytes = dry_run_bytes(T, cfg, a);
+  if (cache.size() >= 64) cache.erase(cache.begin());
+  cache.emplace_back(k, *bytes);
+  return HT_OK;
+}
+
 ht_status_t ht_decompose(const float *x, const long *dims, int order, const ht_tree_t *tree, const ht_config_t *cfg_in,
                          float *const *U, float *const *B, ht_report_t *report, void *stream) {
   if (!x || !dims || !U || !B) return fail(HT_ERR_INVALID_ARG, "NULL argument");
@@ -1823,7 +1977,8 @@ ht_status_t ht_decompose(const float *x, const long *dims, int order, const ht_t
   HT_TRY(check_device());
   std::lock_guard<std::mutex> lk(g_ws_mutex);
   CallArgs a{x, is_device_ptr(x), dims, order, U, B, (cfg.flags & HT_FLAG_COMPUTE_ERROR) != 0};
-  const size_t bytes = dry_run_bytes(T, cfg, a);
+  size_t bytes = 0;
+  HT_TRY(sized_call_bytes(T, cfg, a, &bytes));
   void *ws = nullptr;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   HT_TRY(acquire_workspace(bytes, &ws, st));
@@ -2008,7 +2163,11 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
   const bool replay = b.exec && key == b.key;
   if (!replay) {
     std::vector<Tree> T(count);
-    size_t lane_bytes = 0;
+    BatchLayout L;
+    L.grouped = true;
+    for (int i = 0; i < count; ++i)
+      for (int m = 0; m < order; ++m) L.grouped = L.grouped && dims[static_cast<size_t>(i) * order + m] <= kGroupedMaxN;
+    L.off.assign(static_cast<size_t>(count) + 1, 0);
     for (int i = 0; i < count; ++i) {
       const long *di = dims + static_cast<size_t>(i) * order;
       HT_TRY(parse_tree(&trees[i], di, order, T[i]));
@@ -2021,13 +2180,15 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
       }
       CallArgs a{x[i], true, di, order, U + static_cast<size_t>(i) * HT_MAX_NODES, B + static_cast<size_t>(i) * HT_MAX_NODES,
                  want_err};
-      lane_bytes = std::max(lane_bytes, dry_run_bytes(T[i], cfg, a) + 1024 * sizeof(double));
+      const size_t bi = (dry_run_bytes(T[i], cfg, a, L.grouped ? 1 : 0) + 1024 * sizeof(double) + 4095) & ~size_t(4095);
+      L.lane_bytes = std::max(L.lane_bytes, bi);
+      L.off[i + 1] = L.off[i] + bi;
     }
-    lane_bytes = (lane_bytes + 4095) & ~size_t(4095);
     batch_drop_graph(b);
     HT_TRY(batch_streams(b));
     b.lanes = std::min(tune.lanes, count);
-    const size_t need = static_cast<size_t>(b.lanes) * lane_bytes + sizeof(double) * 2 * count + 4096;
+    const size_t regions = L.grouped ? L.off[count] : static_cast<size_t>(b.lanes) * L.lane_bytes;
+    const size_t need = regions + sizeof(double) * 2 * count + 4096;
     if (b.ws_bytes < need) {
       if (b.ws) {
         HT_CUDA(cudaDeviceSynchronize());
@@ -2038,19 +2199,20 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
       HT_CUDA(cudaMalloc(&b.ws, need));
       b.ws_bytes = need;
     }
-    char *tail = static_cast<char *>(b.ws) + static_cast<size_t>(b.lanes) * lane_bytes;
+    char *tail = static_cast<char *>(b.ws) + regions;
     b.errw = reinterpret_cast<int *>(tail);
     b.sums = reinterpret_cast<double *>(tail + 256);
     const int eig_ctas = tune.eig_ctas > 0 ? tune.eig_ctas : std::max(8, sm_count() / b.lanes);
     HT_CUDA(tc_prepare());   // one-time kernel attributes outside the capture
     HT_CUDA(eig_prepare());
+    if (L.grouped) HT_TRY(batch_plan_grouped(b, L, count, x, dims, order, T, cfg, U, B, want_err));
     // record the batch into a graph (captured from a private stream: the
     // caller's may be the legacy stream); if capture is refused, run it directly
     bool captured = false;
     std::string why;
     cudaError_t ce = cudaStreamBeginCapture(b.cap, cudaStreamCaptureModeThreadLocal);
     if (ce == cudaSuccess) {
-      const ht_status_t s = batch_enqueue(b, b.cap, count, x, dims, order, T, cfg, U, B, want_err, lane_bytes, eig_ctas);
+      const ht_status_t s = batch_enqueue(b, L, b.cap, count, x, dims, order, T, cfg, U, B, want_err, eig_ctas);
       if (s != HT_OK) why = ht_last_error();
       cudaGraph_t g = nullptr;
       ce = cudaStreamEndCapture(b.cap, &g);
@@ -2073,7 +2235,7 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
     if (!captured) g_last_error = "batch ran without a CUDA graph (" + why + ")";
     if (!captured) {
       HT_CUDA(cudaEventRecord(b.t0, st));
-      HT_TRY(batch_enqueue(b, st, count, x, dims, order, T, cfg, U, B, want_err, lane_bytes, eig_ctas));
+      HT_TRY(batch_enqueue(b, L, st, count, x, dims, order, T, cfg, U, B, want_err, eig_ctas));
       HT_CUDA(cudaEventRecord(b.t1, st));
     }
     if (captured) {
@@ -2149,6 +2311,9 @@ ht_status_t ht_release_batch(void) {
   if (b.ws) HT_CUDA(cudaFree(b.ws));
   b.ws = nullptr;
   b.ws_bytes = 0;
+  if (b.table) HT_CUDA(cudaFree(b.table));
+  b.table = nullptr;
+  b.table_bytes = 0;
   return HT_OK;
 }
 

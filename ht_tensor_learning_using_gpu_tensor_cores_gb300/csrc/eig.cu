@@ -960,89 +960,120 @@ HT_DEV void coop_final_rows(const CoopProb &P, int cl, const float *Q, const flo
   if (t < SMAX) P.colss[static_cast<long long>(cl) * SMAX + t] = colsum[t];
 }
 
-__global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
-  extern __shared__ __align__(16) float sm[];
-  float *Rs = sm;                           // SMAX*SMAX (upper factor, row-major)
-  float *ds = Rs + SMAX * SMAX;             // SMAX
-  float *Zs = ds + SMAX;                    // RBMAX*SMAX
-  float *Qr = Zs + RBMAX * SMAX;            // RBMAX*SMAX
-  float *ring = Qr + RBMAX * SMAX;          // product ring, or (aliased) the reducer / Jacobi scratch
-  double *Sd = reinterpret_cast<double *>(ring);
-  float (*A)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(ring + 2 * ESMAX);
-  float (*VV)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(ring + 2 * ESMAX + SMAX * (SMAX + 1));
-  float (*A2)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(ring + 2 * ESMAX + 2 * SMAX * (SMAX + 1));
+// Shared memory of the eigen-solver kernels: the dynamic block (kCoopSmem)
+// carved as the cooperative kernel always has, plus small static arrays.
+struct EigSmem {
+  float *Rs;                    // SMAX*SMAX (upper factor, row-major)
+  float *Zs, *Qr;               // RBMAX*SMAX each
+  float *ring;                  // product ring, or (aliased) the reducer / Jacobi scratch
+  double *Sd;
+  float (*A)[SMAX + 1], (*VV)[SMAX + 1], (*A2)[SMAX + 1];
+  int *s_ok, *order;
+  float *red, *th_sm;
+  double *piv64;
+};
+
+HT_DEV EigSmem eig_smem(float *sm) {
   __shared__ int s_ok;
   __shared__ int order[SMAX];
   __shared__ float red[256];
   __shared__ float th_sm[SMAX];
   __shared__ double piv64[SMAX];
+  EigSmem m;
+  m.Rs = sm;
+  m.Zs = m.Rs + SMAX * SMAX + SMAX;   // SMAX floats after the factor are reserved
+  m.Qr = m.Zs + RBMAX * SMAX;
+  m.ring = m.Qr + RBMAX * SMAX;
+  m.Sd = reinterpret_cast<double *>(m.ring);
+  m.A = reinterpret_cast<float (*)[SMAX + 1]>(m.ring + 2 * ESMAX);
+  m.VV = reinterpret_cast<float (*)[SMAX + 1]>(m.ring + 2 * ESMAX + SMAX * (SMAX + 1));
+  m.A2 = reinterpret_cast<float (*)[SMAX + 1]>(m.ring + 2 * ESMAX + 2 * SMAX * (SMAX + 1));
+  m.s_ok = &s_ok;
+  m.order = order;
+  m.red = red;
+  m.th_sm = th_sm;
+  m.piv64 = piv64;
+  return m;
+}
+
+// Direct problem (s == n <= 64): Jacobi eigen-decomposition of G itself.
+HT_DEV void eig_direct(const CoopProb &P, const EigSmem &m) {
+  const int t = threadIdx.x, n = P.n, K = P.K;
+  float (*A)[SMAX + 1] = m.A;
+  float (*VV)[SMAX + 1] = m.VV;
+  const int *order = m.order;
+  for (int e = t; e < SMAX * SMAX; e += 256) {
+    const int i = e % SMAX, j = e / SMAX;
+    A[i][j] = (i < n && j < n) ? P.G[i + static_cast<long long>(n) * j] : 0.f;
+  }
+  __syncthreads();
+  jacobi_smem(A, m.A2, VV, n, m.order);
+  for (int r = t; r < K; r += 256) P.theta[r] = A[order[r]][order[r]];
+  // U = V[:, order[:K]], GU = G U, residual
+  for (int e = t; e < n * K; e += 256) {
+    const int i = e % n, j = e / n;
+    float gu = 0.f;
+    for (int k = 0; k < n; ++k) gu = fmaf(P.G[i + static_cast<long long>(n) * k], VV[k][order[j]], gu);
+    const float u = VV[i][order[j]];
+    P.U[i + static_cast<long long>(n) * j] = u;
+    P.GU[i + static_cast<long long>(n) * j] = gu;
+    const float d = gu - A[order[j]][order[j]] * u;
+    m.Zs[e] = d * d;   // n * K <= 64 * 64 fits Zs + Qr (contiguous)
+  }
+  __syncthreads();
+  if (t == 0) {
+    float mx = 0.f;
+    for (int j = 0; j < K; ++j) {
+      float a = 0.f;
+      for (int i = 0; i < n; ++i) a += m.Zs[i + n * j];
+      mx = fmaxf(mx, sqrtf(a));
+    }
+    const float th = A[order[0]][order[0]];
+    P.resid[0] = th > 0.f ? mx / th : mx;
+  }
+}
+
+// Synchronisation of the phases of one problem.  Cooperative: the problem's
+// rows are spread over several CTAs of a cooperative grid -- bounded grid
+// barriers, and the Gram partials reduced by all CTAs of the grid.  Local:
+// the problem is one CTA's (the grouped solver) -- block barriers, and the
+// CTA reduces its own partials.
+struct CoopSync {
+  const CoopBatch *B;
+  unsigned members;
+  int *s_ok;
+  HT_DEV bool bar() const { return grid_barrier(B->bar, members, B->err, s_ok); }
+  HT_DEV void reduce() const { coop_reduce(*B); }
+};
+
+HT_DEV void coop_reduce_one(const CoopProb &P) {
+  const int E = P.s * (P.s + 1) / 2;
+  for (int e = threadIdx.x; e < E; e += 256) {
+    Acc2 acc = {0.f, 0.f};
+    for (int c = 0; c < P.ncta; ++c) {
+      const float *src = P.part + (static_cast<long long>(c) * ESMAX + e) * 2;
+      acc2_add(acc, __ldcg(src), __ldcg(src + 1));
+    }
+    P.S[e] = static_cast<double>(acc.s) + static_cast<double>(acc.c);
+  }
+}
+
+struct LocalSync {
+  const CoopProb *P;
+  HT_DEV bool bar() const {
+    __syncthreads();
+    return true;
+  }
+  HT_DEV void reduce() const { coop_reduce_one(*P); }
+};
+
+// Subspace iteration, Rayleigh-Ritz and the final U / GU / residual of one
+// problem; CTA `cl` of the problem's P.ncta owns rows [cl * P.rows, ...).
+template <class Sync>
+HT_DEV void eig_iterate(const CoopProb &P, int cl, const Sync &sy, int iters, int refine, const EigSmem &m) {
   const int t = threadIdx.x;
-
-  if (static_cast<int>(blockIdx.x) >= B.nsync) {
-    // ---- direct problem (s == n <= 64): Jacobi on G itself, no barriers
-    const CoopProb &P = B.p[B.direct_idx[blockIdx.x - B.nsync]];
-    const int n = P.n, K = P.K;
-    for (int e = t; e < SMAX * SMAX; e += 256) {
-      const int i = e % SMAX, j = e / SMAX;
-      A[i][j] = (i < n && j < n) ? P.G[i + static_cast<long long>(n) * j] : 0.f;
-    }
-    __syncthreads();
-    jacobi_smem(A, A2, VV, n, order);
-    for (int r = t; r < K; r += 256) P.theta[r] = A[order[r]][order[r]];
-    // U = V[:, order[:K]], GU = G U, residual
-    for (int e = t; e < n * K; e += 256) {
-      const int i = e % n, j = e / n;
-      float gu = 0.f;
-      for (int k = 0; k < n; ++k) gu = fmaf(P.G[i + static_cast<long long>(n) * k], VV[k][order[j]], gu);
-      const float u = VV[i][order[j]];
-      P.U[i + static_cast<long long>(n) * j] = u;
-      P.GU[i + static_cast<long long>(n) * j] = gu;
-      const float d = gu - A[order[j]][order[j]] * u;
-      Zs[e] = d * d;   // n * K <= 64 * 64 fits Zs + Qr (contiguous)
-    }
-    __syncthreads();
-    if (t == 0) {
-      float m = 0.f;
-      for (int j = 0; j < K; ++j) {
-        float a = 0.f;
-        for (int i = 0; i < n; ++i) a += Zs[i + n * j];
-        m = fmaxf(m, sqrtf(a));
-      }
-      const float th = A[order[0]][order[0]];
-      P.resid[0] = th > 0.f ? m / th : m;
-    }
-    return;
-  }
-
-  int pi = 0;
-  while (!(static_cast<int>(blockIdx.x) >= B.p[pi].cta0 && static_cast<int>(blockIdx.x) < B.p[pi].cta0 + B.p[pi].ncta)) ++pi;
-  const CoopProb &P = B.p[pi];
-  const int cl = blockIdx.x - P.cta0;
-  const unsigned members = static_cast<unsigned>(B.nsync);
-
-  if (B.orth_passes > 0) {
-    // In-place CholeskyQR of buffer 0 (problems without a Gram): each pass
-    // applies the previous transform to the CTA's rows and accumulates their
-    // Gram partial, all CTAs reduce, every CTA factors (float pairs, pivots
-    // floored, so it cannot break down; the first pass shifted by 1e-12 of the
-    // unit diagonal, as the eigen-solver's iterations).  The Gram and the
-    // factor carry ~48 bits, so after one pass only the FP32 rounding of the
-    // applied transform remains (~u * cond(Y)); a second pass removes it.
-    float *Q = P.buf[0];
-    double *A64 = Sd + ESMAX;
-    for (int pass = 0; pass <= B.orth_passes; ++pass) {
-      // row-local: in place; the last pass only applies the transform
-      coop_step(P, cl, 1, Q, Q, nullptr, pass == 0, 0.f, Rs, Zs, Qr, ring, pass < B.orth_passes);
-      if (pass == B.orth_passes) break;
-      if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
-      coop_reduce(B);
-      if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
-      coop_load_S(P, Sd);
-      factor_transform(Sd, P.s, pass == 0 ? 1e-12 : 0.0, A64, piv64, reinterpret_cast<float *>(A64 + SMAX * SMAX), Rs);
-    }
-    return;
-  }
-
+  float *Rs = m.Rs, *Zs = m.Zs, *Qr = m.Qr, *ring = m.ring, *red = m.red;
+  double *Sd = m.Sd;
   // mu = 1e-9 trace(G), computed identically by every CTA of the problem
   {
     float tr = 0.f;
@@ -1064,21 +1095,21 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
       P.buf[0][idx] = P.start ? P.start[idx] : gaussian(P.seed, P.stream_id, static_cast<unsigned long long>(idx));
     }
   }
-  if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
+  if (!sy.bar()) return;
 
   auto reduce_and_factor = [&](double shift) -> bool {
-    if (!grid_barrier(B.bar, members, B.err, &s_ok)) return false;
-    coop_reduce(B);
-    if (!grid_barrier(B.bar, members, B.err, &s_ok)) return false;
+    if (!sy.bar()) return false;
+    sy.reduce();
+    if (!sy.bar()) return false;
     coop_load_S(P, Sd);
     double *A64 = Sd + ESMAX;                  // SMAX*SMAX doubles after the reduced Gram
-    factor_transform(Sd, P.s, shift, A64, piv64, reinterpret_cast<float *>(A64 + SMAX * SMAX), Rs);
+    factor_transform(Sd, P.s, shift, A64, m.piv64, reinterpret_cast<float *>(A64 + SMAX * SMAX), Rs);
     return true;
   };
 
   int cur = 0;
   bool ident = true;
-  for (int it = 0; it < B.iters; ++it) {
+  for (int it = 0; it < iters; ++it) {
     coop_step(P, cl, 0, P.buf[cur], P.buf[cur ^ 1], nullptr, ident, mu, Rs, Zs, Qr, ring);
     if (!reduce_and_factor(1e-12)) return;
     ident = false;
@@ -1091,23 +1122,23 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
   // Y_L loses digits to cancellation.
   // The FP32 path asks for `refine` CholeskyQR passes on Q_L all the same
   // (orthonormal to FP32 rounding, the last digit of its error).
-  coop_step(P, cl, 1, P.buf[cur], P.buf[2], nullptr, ident, 0.f, Rs, Zs, Qr, ring, ident || B.refine > 0);
+  coop_step(P, cl, 1, P.buf[cur], P.buf[2], nullptr, ident, 0.f, Rs, Zs, Qr, ring, ident || refine > 0);
   bool rr_ident = true;
-  if (ident || B.refine > 0) {   // ident: no iteration ran, orthonormalise the start block
+  if (ident || refine > 0) {   // ident: no iteration ran, orthonormalise the start block
     if (!reduce_and_factor(1e-12)) return;
     rr_ident = false;
-    for (int r = 1; r < B.refine; ++r) {   // row-local, so in place
+    for (int r = 1; r < refine; ++r) {   // row-local, so in place
       coop_step(P, cl, 1, P.buf[2], P.buf[2], nullptr, false, 0.f, Rs, Zs, Qr, ring);
       if (!reduce_and_factor(1e-14)) return;
     }
-  } else if (!grid_barrier(B.bar, members, B.err, &s_ok)) {
+  } else if (!sy.bar()) {
     return;
   }
   // Rayleigh-Ritz: Q -> buf3, G Q -> buf0, H = Q^T G Q
   coop_step(P, cl, 2, P.buf[2], P.buf[3], P.buf[0], rr_ident, 0.f, Rs, Zs, Qr, ring);
-  if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
-  coop_reduce(B);
-  if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
+  if (!sy.bar()) return;
+  sy.reduce();
+  if (!sy.bar()) return;
   if (cl == 0) {
     coop_load_S(P, Sd);
     const int s = P.s;
@@ -1115,30 +1146,30 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
       const int i = e % SMAX, j = e / SMAX;
       float v = 0.f;
       if (i < s && j < s) v = static_cast<float>(i <= j ? Sd[j * (j + 1) / 2 + i] : Sd[i * (i + 1) / 2 + j]);
-      A[i][j] = v;
+      m.A[i][j] = v;
     }
     __syncthreads();
-    jacobi_smem(A, A2, VV, s, order);
+    jacobi_smem(m.A, m.A2, m.VV, s, m.order);
     for (int e = t; e < s * s; e += 256) {
       const int i = e % s, r = e / s;
-      P.V[i + s * r] = VV[i][order[r]];
+      P.V[i + s * r] = m.VV[i][m.order[r]];
     }
-    for (int r = t; r < P.K; r += 256) P.theta[r] = A[order[r]][order[r]];
+    for (int r = t; r < P.K; r += 256) P.theta[r] = m.A[m.order[r]][m.order[r]];
   }
-  if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
+  if (!sy.bar()) return;
   // final: U, GU and the residual partials
   {
-    float (*Vsm)[SMAX + 1] = VV;
+    float (*Vsm)[SMAX + 1] = m.VV;
     const int s = P.s;
     for (int e = t; e < SMAX * SMAX; e += 256) {
       const int i = e % SMAX, j = e / SMAX;
       Vsm[i][j] = (i < s && j < s) ? __ldcg(P.V + i + s * j) : 0.f;
     }
-    for (int j = t; j < SMAX; j += 256) th_sm[j] = j < P.K ? __ldcg(P.theta + j) : 0.f;
+    for (int j = t; j < SMAX; j += 256) m.th_sm[j] = j < P.K ? __ldcg(P.theta + j) : 0.f;
     __syncthreads();
-    coop_final_rows(P, cl, P.buf[3], P.buf[0], Vsm, th_sm, Qr, Zs);
+    coop_final_rows(P, cl, P.buf[3], P.buf[0], Vsm, m.th_sm, Qr, Zs);
   }
-  if (!grid_barrier(B.bar, members, B.err, &s_ok)) return;
+  if (!sy.bar()) return;
   if (cl == 0 && t < SMAX) {
     float a = 0.f;
     if (t < P.K)
@@ -1147,11 +1178,72 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const CoopBatch B) {
   }
   __syncthreads();
   if (cl == 0 && t == 0) {
-    float m = 0.f;
-    for (int j = 0; j < P.K; ++j) m = fmaxf(m, red[j]);
+    float mx = 0.f;
+    for (int j = 0; j < P.K; ++j) mx = fmaxf(mx, red[j]);
     const float th = __ldcg(P.theta);
-    P.resid[0] = th > 0.f ? m / th : m;
+    P.resid[0] = th > 0.f ? mx / th : mx;
   }
+}
+
+__global__ void __launch_bounds__(256, 1) eig_coop_kernel(const __grid_constant__ CoopBatch B) {
+  extern __shared__ __align__(16) float sm[];
+  const EigSmem m = eig_smem(sm);
+
+  if (static_cast<int>(blockIdx.x) >= B.nsync) {
+    // ---- direct problem (s == n <= 64): Jacobi on G itself, no barriers
+    eig_direct(B.p[B.direct_idx[blockIdx.x - B.nsync]], m);
+    return;
+  }
+
+  int pi = 0;
+  while (!(static_cast<int>(blockIdx.x) >= B.p[pi].cta0 && static_cast<int>(blockIdx.x) < B.p[pi].cta0 + B.p[pi].ncta)) ++pi;
+  const CoopProb &P = B.p[pi];
+  const int cl = blockIdx.x - P.cta0;
+  const unsigned members = static_cast<unsigned>(B.nsync);
+
+  if (B.orth_passes > 0) {
+    // In-place CholeskyQR of buffer 0 (problems without a Gram): each pass
+    // applies the previous transform to the CTA's rows and accumulates their
+    // Gram partial, all CTAs reduce, every CTA factors (float pairs, pivots
+    // floored, so it cannot break down; the first pass shifted by 1e-12 of the
+    // unit diagonal, as the eigen-solver's iterations).  The Gram and the
+    // factor carry ~48 bits, so after one pass only the FP32 rounding of the
+    // applied transform remains (~u * cond(Y)); a second pass removes it.
+    float *Q = P.buf[0];
+    double *A64 = m.Sd + ESMAX;
+    for (int pass = 0; pass <= B.orth_passes; ++pass) {
+      // row-local: in place; the last pass only applies the transform
+      coop_step(P, cl, 1, Q, Q, nullptr, pass == 0, 0.f, m.Rs, m.Zs, m.Qr, m.ring, pass < B.orth_passes);
+      if (pass == B.orth_passes) break;
+      if (!grid_barrier(B.bar, members, B.err, m.s_ok)) return;
+      coop_reduce(B);
+      if (!grid_barrier(B.bar, members, B.err, m.s_ok)) return;
+      coop_load_S(P, m.Sd);
+      factor_transform(m.Sd, P.s, pass == 0 ? 1e-12 : 0.0, A64, m.piv64, reinterpret_cast<float *>(A64 + SMAX * SMAX),
+                       m.Rs);
+    }
+    return;
+  }
+  const CoopSync sy{&B, members, m.s_ok};
+  eig_iterate(P, cl, sy, B.iters, B.refine, m);
+}
+
+// Grouped solver of the batched path: CTA b solves problem tab[b] alone (all
+// of its rows, block barriers only), so one ordinary launch covers every leaf
+// of every tensor of a batch and no CTA waits on another.
+__global__ void __launch_bounds__(256, 1) eig_grouped_kernel(const CoopProb *__restrict__ tab, int iters, int refine) {
+  extern __shared__ __align__(16) float sm[];
+  const EigSmem m = eig_smem(sm);
+  __shared__ CoopProb sP;
+  if (threadIdx.x == 0) sP = tab[blockIdx.x];
+  __syncthreads();
+  const CoopProb &P = sP;
+  if (P.s == P.n) {
+    eig_direct(P, m);
+    return;
+  }
+  const LocalSync sy{&P};
+  eig_iterate(P, 0, sy, iters, refine, m);
 }
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -1197,6 +1289,8 @@ cudaError_t eig_prepare() {
   if (coop_max_ctas() <= 0) return cudaErrorInvalidConfiguration;
   cudaError_t e = cudaFuncSetAttribute(transfer_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            static_cast<int>(kJacScratch));
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(eig_grouped_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kCoopSmem));
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(svd_from_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               static_cast<int>(kJacScratch));
@@ -1285,6 +1379,58 @@ cudaError_t eig_batched(EigProblem *probs, int nprob, int iters, void *ws, size_
   if (e != cudaSuccess) return e;
   if (launches) *launches += 1;
   return cudaSuccess;
+}
+
+// ---- grouped solver (batched path): one CTA per problem, so a problem's
+// workspace holds one CTA's Gram and residual partials
+namespace {
+size_t grouped_prob_bytes(const EigProblem &q) {
+  return 4 * align256(sizeof(float) * static_cast<size_t>(q.n) * SMAX) + align256(sizeof(float) * ESMAX * 2) +
+         align256(sizeof(double) * ESMAX) + align256(sizeof(float) * SMAX * SMAX) + align256(sizeof(float) * SMAX);
+}
+}  // namespace
+
+size_t eig_grouped_workspace_bytes(const EigProblem *probs, int nprob) {
+  size_t b = 0;
+  for (int i = 0; i < nprob; ++i) b += grouped_prob_bytes(probs[i]);
+  return b;
+}
+
+size_t eig_grouped_entry_bytes() { return sizeof(CoopProb); }
+
+cudaError_t eig_grouped_fill(const EigProblem *probs, int nprob, void *ws, size_t ws_bytes,
+                             std::vector<unsigned char> &table) {
+  if (eig_grouped_workspace_bytes(probs, nprob) > ws_bytes) return cudaErrorInvalidValue;
+  char *p = static_cast<char *>(ws);
+  for (int i = 0; i < nprob; ++i) {
+    const EigProblem &q = probs[i];
+    if (!q.G || q.s > SMAX || q.s < 1 || q.K > q.s || q.s > q.n) return cudaErrorInvalidValue;
+    CoopProb c;
+    std::memset(&c, 0, sizeof(c));
+    c.G = q.G; c.n = q.n; c.s = q.s; c.K = q.K;
+    c.cta0 = 0; c.ncta = 1; c.rows = q.n;
+    c.U = q.U; c.GU = q.GU; c.theta = q.theta; c.resid = q.resid;
+    c.start = q.start; c.seed = q.seed; c.stream_id = q.stream_id;
+    for (int k = 0; k < 4; ++k) {
+      c.buf[k] = reinterpret_cast<float *>(p);
+      p += align256(sizeof(float) * static_cast<size_t>(q.n) * SMAX);
+    }
+    c.part = reinterpret_cast<float *>(p); p += align256(sizeof(float) * ESMAX * 2);
+    c.S = reinterpret_cast<double *>(p); p += align256(sizeof(double) * ESMAX);
+    c.V = reinterpret_cast<float *>(p); p += align256(sizeof(float) * SMAX * SMAX);
+    c.colss = reinterpret_cast<float *>(p); p += align256(sizeof(float) * SMAX);
+    const unsigned char *raw = reinterpret_cast<const unsigned char *>(&c);
+    table.insert(table.end(), raw, raw + sizeof(c));
+  }
+  return cudaSuccess;
+}
+
+cudaError_t eig_grouped_launch(const void *table_dev, int nprob, int iters, int refine, cudaStream_t st) {
+  if (nprob <= 0) return cudaSuccess;
+  if (!table_dev || (reinterpret_cast<uintptr_t>(table_dev) % alignof(CoopProb)) != 0) return cudaErrorInvalidValue;
+  eig_grouped_kernel<<<nprob, 256, kCoopSmem, st>>>(static_cast<const CoopProb *>(table_dev), iters,
+                                                    refine < 0 ? 0 : (refine > 2 ? 2 : refine));
+  return cudaGetLastError();
 }
 
 // In-place CholeskyQR (`passes` factorisations, the first shifted) of tall

@@ -180,6 +180,16 @@ cudaError_t eig_prepare();
 // refine (0-2): CholeskyQR passes on the last block before Rayleigh-Ritz.
 cudaError_t eig_batched(EigProblem *probs, int nprob, int iters, void *ws, size_t ws_bytes, int *err,
                         cudaStream_t s, int *launches, int max_ctas = 0, int refine = 0);
+// Grouped solver of the batched path: every problem of a batch in one launch,
+// one CTA per problem (no cooperative launch, no CTA waits on another).
+// eig_grouped_fill appends one table entry per problem (entry_bytes each) to
+// `table`, carving the problems' buffers from ws; the table is copied to
+// device memory (16-byte aligned) before eig_grouped_launch reads it.
+size_t eig_grouped_workspace_bytes(const EigProblem *probs, int nprob);
+size_t eig_grouped_entry_bytes();
+cudaError_t eig_grouped_fill(const EigProblem *probs, int nprob, void *ws, size_t ws_bytes,
+                             std::vector<unsigned char> &table);
+cudaError_t eig_grouped_launch(const void *table_dev, int nprob, int iters, int refine, cudaStream_t st);
 // Orthonormalise the columns of tall matrices in place (CholeskyQR, `passes`
 // times; the first pass shifted).  Uses the eigen-solver's workspace layout;
 // a wait that runs out sets bits in *err.

@@ -88,3 +88,42 @@ def test_batched_rejects_host_inputs(family):
     bd = ht.BatchDecomposer([tree], [X.shape], precision="bf16")
     with pytest.raises(TypeError):
         bd([X])
+
+
+def _check_batch(pairs, prec):
+    trees = [t for _, t in pairs]
+    dims = [X.shape for X, _ in pairs]
+    bd = ht.BatchDecomposer(trees, dims, precision=prec, compute_error=True)
+    res, rep = bd([to_dev(X) for X, _ in pairs])
+    for (X, tree), r in zip(pairs, res):
+        U = {t: r.U[t].cpu().numpy().astype(np.float64) for t in r.U}
+        B = {t: r.B[t].cpu().numpy().astype(np.float64) for t in r.B}
+        e = O.ht_error(X, tree, U, B)
+        Uo, Bo, _ = O.ht_decompose(X, tree)
+        assert abs(e - O.ht_error(X, tree, Uo, Bo)) <= TOL[prec], (prec, X.shape, e)
+        assert abs(r.report["rel_err"] - e) <= 1e-5 + 1e-4 * e
+        for t in tree.leaves():
+            assert O.orthogonality_defect(U[t]) < 1e-4
+    return rep
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_batched_large_mode_uses_per_lane_solver(prec):
+    """A batch with a mode above the grouped solver's 512 runs every tensor's
+    leaf solver as a cooperative launch of its own; results as before."""
+    pairs = []
+    for i, d in enumerate([(520, 24, 20), (40, 36, 32), (33, 47, 61)]):
+        tree = ht.reference_tree_3d([1, 8, 6, 5, 7])
+        pairs.append((synth.exact_ht(d, tree, noise_rel=1e-3, seed=300 + i), tree))
+    _check_batch(pairs, prec)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_batched_4d_and_direct_leaves(prec):
+    """4th-order tensors (four leaves each, the root's range finder after the
+    grouped leaf solver) and leaves of size <= 64 solved directly, in one batch."""
+    pairs = []
+    for i, d in enumerate([(20, 24, 18, 22), (30, 16, 26, 20), (12, 28, 20, 24)]):
+        tree = ht.balanced_tree_4d([1, 12, 12, 6, 6, 6, 6])
+        pairs.append((synth.exact_ht(d, tree, noise_rel=1e-3, seed=400 + i), tree))
+    _check_batch(pairs, prec)
