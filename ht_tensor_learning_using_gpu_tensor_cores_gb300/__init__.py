@@ -373,7 +373,10 @@ class BatchDecomposer:
             results.append(HTResult(self.trees[i], self.dims[i], self.U[i], self.B[i], report))
         summary = {"rel_err_p50": rep.rel_err_p50, "rel_err_p99": rep.rel_err_p99, "rel_err_max": rep.rel_err_max,
                    "ms_total": rep.ms_total, "gpu_launches": rep.gpu_launches, "graph_replayed": bool(rep.graph_replayed),
-                   "lanes": rep.lanes, "note": (lib().ht_last_error() or b"").decode()}
+                   "lanes": rep.lanes, "grouped": bool(rep.grouped),
+                   "ms_phase": {"lanes_to_grams": rep.ms_phase[0], "grouped_leaf_solver": rep.ms_phase[1],
+                                "lanes_after": rep.ms_phase[2]},
+                   "note": (lib().ht_last_error() or b"").decode()}
         return results, summary
 
 

@@ -1690,6 +1690,8 @@ struct BatchState {
   cudaStream_t lane[kLanes] = {};
   cudaStream_t cap = nullptr;   // capture origin (the caller's stream may be the legacy stream)
   cudaEvent_t fork = nullptr, join[kLanes] = {}, t0 = nullptr, t1 = nullptr;
+  cudaEvent_t tp[2] = {};   // grouped mode: after the lanes' first phase, after the grouped solver
+  bool grouped = false;
   double *sums = nullptr;   // device: [count][2] (||X||^2, ||X - Xhat||^2)
   int *errw = nullptr;      // device: one error word per lane
   int launches = 0, lanes = 0;
@@ -1732,6 +1734,8 @@ ht_status_t batch_streams(BatchState &b) {
   HT_CUDA(cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming));
   HT_CUDA(cudaEventCreate(&b.t0));
   HT_CUDA(cudaEventCreate(&b.t1));
+  HT_CUDA(cudaEventCreate(&b.tp[0]));
+  HT_CUDA(cudaEventCreate(&b.tp[1]));
   return HT_OK;
 }
 
@@ -1799,7 +1803,10 @@ ht_status_t batch_enqueue(BatchState &b, const BatchLayout &L, cudaStream_t st, 
                       nullptr);
   HT_TRY(batch_pass(b, L, 1, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas, nullptr, nullptr,
                     nullptr));
+  // external records: inside a capture they become event-record nodes of the graph
+  HT_CUDA(cudaEventRecordWithFlags(b.tp[0], st, cudaEventRecordExternal));
   HT_CUDA(eig_grouped_launch(b.table, L.nprob, L.iters, L.refine, st));
+  HT_CUDA(cudaEventRecordWithFlags(b.tp[1], st, cudaEventRecordExternal));
   b.launches += 1;
   return batch_pass(b, L, 2, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas, nullptr, nullptr,
                     nullptr);
@@ -1815,6 +1822,7 @@ ht_status_t batch_plan_grouped(BatchState &b, BatchLayout &L, int count, const f
   const int launches = b.launches;
   HT_TRY(batch_pass(b, L, 3, nullptr, count, x, dims, order, trees, cfg, U, B, want_err, 0, &table, &iters, &refine));
   b.launches = launches;
+  eig_grouped_order(table);
   L.nprob = static_cast<int>(table.size() / eig_grouped_entry_bytes());
   L.iters = iters;
   L.refine = refine;
@@ -2187,6 +2195,7 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
     batch_drop_graph(b);
     HT_TRY(batch_streams(b));
     b.lanes = std::min(tune.lanes, count);
+    b.grouped = L.grouped;
     const size_t regions = L.grouped ? L.off[count] : static_cast<size_t>(b.lanes) * L.lane_bytes;
     const size_t need = regions + sizeof(double) * 2 * count + 4096;
     if (b.ws_bytes < need) {
@@ -2282,6 +2291,14 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
     report->gpu_launches = b.launches;
     report->graph_replayed = replay ? 1 : 0;
     report->lanes = b.lanes;
+    report->grouped = b.grouped ? 1 : 0;
+    if (b.grouped &&
+        (cudaEventElapsedTime(&report->ms_phase[0], b.t0, b.tp[0]) != cudaSuccess ||
+         cudaEventElapsedTime(&report->ms_phase[1], b.tp[0], b.tp[1]) != cudaSuccess ||
+         cudaEventElapsedTime(&report->ms_phase[2], b.tp[1], b.t1) != cudaSuccess)) {
+      cudaGetLastError();   // timing unavailable: report zeros, leave no error behind
+      report->ms_phase[0] = report->ms_phase[1] = report->ms_phase[2] = 0.f;
+    }
   }
   return HT_OK;
 }

@@ -28,6 +28,7 @@
 // nonzero on exactly null directions without moving any eigenvector or
 // slowing convergence.  Modes with n <= 64 (s == n) skip the iteration: Q = I
 // and the Rayleigh-Ritz step is a Jacobi eigen-decomposition of G itself.
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -1423,6 +1424,20 @@ cudaError_t eig_grouped_fill(const EigProblem *probs, int nprob, void *ws, size_
     table.insert(table.end(), raw, raw + sizeof(c));
   }
   return cudaSuccess;
+}
+
+void eig_grouped_order(std::vector<unsigned char> &table) {
+  // CTAs start in index order, so the longest problems go first and the short
+  // ones fill the last wave: Jacobi sweeps on the whole Gram (s == n, cost
+  // ~n^3 per sweep) before iterating problems (~n^2 s per iteration)
+  const size_t nb = sizeof(CoopProb), np = table.size() / nb;
+  std::vector<CoopProb> v(np);
+  std::memcpy(v.data(), table.data(), np * nb);
+  auto cost = [](const CoopProb &q) {
+    return q.s == q.n ? 4.0 * q.n * q.n * q.n : static_cast<double>(q.n) * q.n * q.s + 64.0 * q.s * q.s * q.s;
+  };
+  std::stable_sort(v.begin(), v.end(), [&](const CoopProb &a, const CoopProb &b) { return cost(a) > cost(b); });
+  std::memcpy(table.data(), v.data(), np * nb);
 }
 
 cudaError_t eig_grouped_launch(const void *table_dev, int nprob, int iters, int refine, cudaStream_t st) {

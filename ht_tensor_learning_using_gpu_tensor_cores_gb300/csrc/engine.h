@@ -189,6 +189,8 @@ size_t eig_grouped_workspace_bytes(const EigProblem *probs, int nprob);
 size_t eig_grouped_entry_bytes();
 cudaError_t eig_grouped_fill(const EigProblem *probs, int nprob, void *ws, size_t ws_bytes,
                              std::vector<unsigned char> &table);
+// Longest problems first (CTAs start in index order).
+void eig_grouped_order(std::vector<unsigned char> &table);
 cudaError_t eig_grouped_launch(const void *table_dev, int nprob, int iters, int refine, cudaStream_t st);
 // Orthonormalise the columns of tall matrices in place (CholeskyQR, `passes`
 // times; the first pass shifted).  Uses the eigen-solver's workspace layout;

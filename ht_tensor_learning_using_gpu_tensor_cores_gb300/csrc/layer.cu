@@ -293,9 +293,13 @@ __global__ void __launch_bounds__(kLayerThreads) layer_dpq_kernel(const LayerSha
     }
     for (int e = threadIdx.x; e < N2 * R1; e += kLayerThreads) {
       const int r = e / N2, n2 = e - r * N2;
-      float s = 0.f;
-      for (int pr = 0; pr < NP; ++pr) s = fmaf(row[pr * rs + n2], Ps[pr * R1 + r], s);
-      dQpart[(static_cast<long long>(blk) * C + (n2 * M2 + m2)) * R1 + r] = s;
+      float s[4] = {0.f, 0.f, 0.f, 0.f};   // four independent chains, combined in a fixed order
+      int pr = 0;
+      for (; pr + 4 <= NP; pr += 4)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) s[j] = fmaf(row[(pr + j) * rs + n2], Ps[(pr + j) * R1 + r], s[j]);
+      for (; pr < NP; ++pr) s[0] = fmaf(row[pr * rs + n2], Ps[pr * R1 + r], s[0]);
+      dQpart[(static_cast<long long>(blk) * C + (n2 * M2 + m2)) * R1 + r] = (s[0] + s[1]) + (s[2] + s[3]);
     }
   }
   __syncthreads();
@@ -312,9 +316,101 @@ __global__ void layer_dq_reduce_kernel(const float *__restrict__ dQpart, int blo
                                        float *__restrict__ dQ) {
   const long long e = blockIdx.x * static_cast<long long>(kLayerThreads) + threadIdx.x;
   if (e >= count) return;
-  float s = 0.f;
-  for (int b = 0; b < blocks; ++b) s += dQpart[static_cast<long long>(b) * count + e];
-  dQ[e] = s;
+  float s[4] = {0.f, 0.f, 0.f, 0.f};   // four independent chains, combined in a fixed order
+  int b = 0;
+  for (; b + 4 <= blocks; b += 4)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) s[q] += dQpart[static_cast<long long>(b + q) * count + e];
+  for (; b < blocks; ++b) s[0] += dQpart[static_cast<long long>(b) * count + e];
+  dQ[e] = (s[0] + s[1]) + (s[2] + s[3]);
+}
+
+// dT1[a, r4, r1] = sum_b u2[b, r4] dP[a, b, r1]: a block per a, the b range
+// staged through shared memory in chunks of kDtChunk rows of dP[a] and u2,
+// each thread owning fixed (r4, r1) outputs.  Blocks [A, A + du3 blocks):
+// du3[c, r2] = sum_r1 dQ[c, r1] b1[r1, r2], a thread per entry.
+constexpr int kDtChunk = 64;
+__global__ void __launch_bounds__(kLayerThreads) layer_dt1_kernel(const LayerShape sh, const float *__restrict__ u2,
+                                                                  const float *__restrict__ b1,
+                                                                  const float *__restrict__ dP,
+                                                                  const float *__restrict__ dQ,
+                                                                  float *__restrict__ dT1, float *__restrict__ du3) {
+  const int A = sh.n[0] * sh.m[0], B = sh.n[1] * sh.m[1], C = sh.n[2] * sh.m[2];
+  const int R1 = sh.r1, R2 = sh.r2, R4 = sh.r4, t = threadIdx.x;
+  if (static_cast<int>(blockIdx.x) >= A) {
+    const long long f = (blockIdx.x - A) * static_cast<long long>(kLayerThreads) + t;
+    if (f >= static_cast<long long>(C) * R2) return;
+    const int c = static_cast<int>(f / R2), r2 = static_cast<int>(f - static_cast<long long>(c) * R2);
+    float v = 0.f;
+    for (int r1 = 0; r1 < R1; ++r1) v = fmaf(dQ[static_cast<long long>(c) * R1 + r1], b1[r1 * R2 + r2], v);
+    du3[f] = v;
+    return;
+  }
+  __shared__ float sP[kDtChunk * kLayerMaxRank];   // [b][r1]
+  __shared__ float sU[kDtChunk * kLayerMaxRank];   // [b][r4]
+  constexpr int kOut = kLayerMaxRank * kLayerMaxRank / kLayerThreads;
+  const int a = blockIdx.x, nout = R4 * R1;
+  float acc[kOut];
+#pragma unroll
+  for (int q = 0; q < kOut; ++q) acc[q] = 0.f;
+  for (int b0 = 0; b0 < B; b0 += kDtChunk) {
+    const int nb = min(kDtChunk, B - b0);
+    __syncthreads();
+    for (int e = t; e < nb * R1; e += kLayerThreads) sP[e] = dP[(static_cast<long long>(a) * B + b0) * R1 + e];
+    for (int e = t; e < nb * R4; e += kLayerThreads) sU[e] = u2[static_cast<long long>(b0) * R4 + e];
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < kOut; ++q) {
+      const int o = t + q * kLayerThreads;
+      if (o < nout) {
+        const int r4 = o / R1, r1 = o - r4 * R1;
+        float v = acc[q];
+        for (int b = 0; b < nb; ++b) v = fmaf(sU[b * R4 + r4], sP[b * R1 + r1], v);
+        acc[q] = v;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kOut; ++q) {
+    const int o = t + q * kLayerThreads;
+    if (o < nout) dT1[static_cast<long long>(a) * nout + o] = acc[q];
+  }
+}
+
+// du1[a, r3] = sum_q dT1[a, q] b2[r3, q] (q = (r4, r1)): a warp per entry,
+// lanes striding q, a fixed shuffle tree.  Blocks past the du1 ones:
+// db2[r3, q] = sum_a u1[a, r3] dT1[a, q], a thread per entry with four
+// independent chains over a combined in a fixed order.
+__global__ void __launch_bounds__(kLayerThreads) layer_dt1_back_kernel(const LayerShape sh, const float *__restrict__ u1,
+                                                                       const float *__restrict__ b2,
+                                                                       const float *__restrict__ dT1,
+                                                                       float *__restrict__ du1,
+                                                                       float *__restrict__ db2, int du1_blocks) {
+  const int A = sh.n[0] * sh.m[0];
+  const int R1 = sh.r1, R3 = sh.r3, R4 = sh.r4, Qn = R4 * R1;
+  if (static_cast<int>(blockIdx.x) < du1_blocks) {
+    const long long w = blockIdx.x * static_cast<long long>(kLayerThreads / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= static_cast<long long>(A) * R3) return;
+    const int a = static_cast<int>(w / R3), r3 = static_cast<int>(w - static_cast<long long>(a) * R3);
+    const float *d = dT1 + static_cast<long long>(a) * Qn;
+    const float *g = b2 + static_cast<long long>(r3) * Qn;
+    float v = 0.f;
+    for (int q = lane; q < Qn; q += 32) v = fmaf(d[q], g[q], v);
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) du1[w] = v;
+    return;
+  }
+  const long long f = (blockIdx.x - du1_blocks) * static_cast<long long>(kLayerThreads) + threadIdx.x;
+  if (f >= static_cast<long long>(R3) * Qn) return;
+  const int r3 = static_cast<int>(f / Qn), q = static_cast<int>(f - static_cast<long long>(r3) * Qn);
+  float s[4] = {0.f, 0.f, 0.f, 0.f};
+  int a = 0;
+  for (; a + 4 <= A; a += 4)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) s[j] = fmaf(u1[(a + j) * R3 + r3], dT1[static_cast<long long>(a + j) * Qn + q], s[j]);
+  for (; a < A; ++a) s[0] = fmaf(u1[a * R3 + r3], dT1[static_cast<long long>(a) * Qn + q], s[0]);
+  db2[f] = (s[0] + s[1]) + (s[2] + s[3]);
 }
 
 // The factor gradients from dP, dQ (all small):
@@ -322,73 +418,31 @@ __global__ void layer_dq_reduce_kernel(const float *__restrict__ dQpart, int blo
 //   dT1[a, r4, r1] = sum_b dP[a, b, r1] u2[b, r4]   du2[b, r4] = sum_{a, r1} dP[a, b, r1] T1[a, r4, r1]
 //   du1[a, r3] = sum_{r4, r1} dT1[a, r4, r1] b2[r3, r4, r1]
 //   db2[r3, r4, r1] = sum_a u1[a, r3] dT1[a, r4, r1]
-// Stage 1 (one thread per output entry): dT1, du3 and, when non-null, du2 and
-// db1 (layer_du2_kernel and layer_db1_kernel do those two faster).
-__global__ void layer_grad1_kernel(const LayerShape sh, const float *__restrict__ u2, const float *__restrict__ u3,
-                                   const float *__restrict__ b1, const float *__restrict__ T1,
-                                   const float *__restrict__ dP, const float *__restrict__ dQ,
-                                   float *__restrict__ dT1, float *__restrict__ du2, float *__restrict__ du3,
-                                   float *__restrict__ db1) {
-  const int A = sh.n[0] * sh.m[0], B = sh.n[1] * sh.m[1], C = sh.n[2] * sh.m[2];
-  const int R1 = sh.r1, R2 = sh.r2, R4 = sh.r4;
-  const long long n_dt1 = static_cast<long long>(A) * R4 * R1, n_du2 = du2 ? static_cast<long long>(B) * R4 : 0,
-                  n_du3 = static_cast<long long>(C) * R2, n_db1 = db1 ? static_cast<long long>(R1) * R2 : 0;
-  const long long total = n_dt1 + n_du2 + n_du3 + n_db1;
-  for (long long e = blockIdx.x * static_cast<long long>(kLayerThreads) + threadIdx.x; e < total;
-       e += static_cast<long long>(gridDim.x) * kLayerThreads) {
-    if (e < n_dt1) {
-      const int a = static_cast<int>(e / (R4 * R1)), rem = static_cast<int>(e - static_cast<long long>(a) * R4 * R1);
-      const int r4 = rem / R1, r1 = rem - r4 * R1;
-      float s = 0.f;
-      for (int b = 0; b < B; ++b) s = fmaf(dP[(static_cast<long long>(a) * B + b) * R1 + r1], u2[b * R4 + r4], s);
-      dT1[e] = s;
-    } else if (e < n_dt1 + n_du2) {
-      const long long f = e - n_dt1;
-      const int b = static_cast<int>(f / R4), r4 = static_cast<int>(f - static_cast<long long>(b) * R4);
-      float s = 0.f;
-      for (int a = 0; a < A; ++a)
-        for (int r1 = 0; r1 < R1; ++r1)
-          s = fmaf(dP[(static_cast<long long>(a) * B + b) * R1 + r1], T1[(static_cast<long long>(a) * R4 + r4) * R1 + r1],
-                   s);
-      du2[f] = s;
-    } else if (e < n_dt1 + n_du2 + n_du3) {
-      const long long f = e - n_dt1 - n_du2;
-      const int c = static_cast<int>(f / R2), r2 = static_cast<int>(f - static_cast<long long>(c) * R2);
-      float s = 0.f;
-      for (int r1 = 0; r1 < R1; ++r1) s = fmaf(dQ[static_cast<long long>(c) * R1 + r1], b1[r1 * R2 + r2], s);
-      du3[f] = s;
-    } else {
-      const long long f = e - n_dt1 - n_du2 - n_du3;
-      const int r1 = static_cast<int>(f / R2), r2 = static_cast<int>(f - static_cast<long long>(r1) * R2);
-      float s = 0.f;
-      for (int c = 0; c < C; ++c) s = fmaf(dQ[static_cast<long long>(c) * R1 + r1], u3[c * R2 + r2], s);
-      db1[f] = s;
-    }
-  }
-}
-
+// dT1 and du3 come from layer_dt1_kernel, du1 and db2 from
+// layer_dt1_back_kernel, du2 and db1 from the two kernels below.
 // du2[b, r4] = sum_{a, r1} dP[a, b, r1] T1[a, r4, r1]: a block per b, the
 // (a, r1) pairs split over the threads with R4 accumulators each, then a
 // fixed-order reduction (deterministic).
+template <int RB>   // rank bound: R4 <= RB
 __global__ void __launch_bounds__(kLayerThreads) layer_du2_kernel(const LayerShape sh, const float *__restrict__ dP,
                                                                   const float *__restrict__ T1, float *__restrict__ du2) {
-  __shared__ float red[kLayerThreads / 32][kLayerMaxRank];
+  __shared__ float red[kLayerThreads / 32][RB];
   const int A = sh.n[0] * sh.m[0], B = sh.n[1] * sh.m[1];
   const int R1 = sh.r1, R4 = sh.r4, b = blockIdx.x;
-  float acc[kLayerMaxRank];
+  float acc[RB];
 #pragma unroll
-  for (int r = 0; r < kLayerMaxRank; ++r) acc[r] = 0.f;
+  for (int r = 0; r < RB; ++r) acc[r] = 0.f;
   for (int e = threadIdx.x; e < A * R1; e += kLayerThreads) {
     const int a = e / R1, r1 = e - a * R1;
     const float g = dP[(static_cast<long long>(a) * B + b) * R1 + r1];
     const float *t = T1 + static_cast<long long>(a) * R4 * R1 + r1;
 #pragma unroll
-    for (int r = 0; r < kLayerMaxRank; ++r)
+    for (int r = 0; r < RB; ++r)
       if (r < R4) acc[r] = fmaf(g, t[r * R1], acc[r]);
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int r = 0; r < kLayerMaxRank; ++r) {
+  for (int r = 0; r < RB; ++r) {
     float v = acc[r];
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     if (lane == 0) red[warp][r] = v;
@@ -403,23 +457,24 @@ __global__ void __launch_bounds__(kLayerThreads) layer_du2_kernel(const LayerSha
 
 // db1[r1, r2] = sum_c dQ[c, r1] u3[c, r2]: a block per r1, c split over the
 // threads with R2 accumulators each, fixed-order reduction.
+template <int RB>   // rank bound: R2 <= RB
 __global__ void __launch_bounds__(kLayerThreads) layer_db1_kernel(const LayerShape sh, const float *__restrict__ dQ,
                                                                   const float *__restrict__ u3, float *__restrict__ db1) {
-  __shared__ float red[kLayerThreads / 32][kLayerMaxRank];
+  __shared__ float red[kLayerThreads / 32][RB];
   const int C = sh.n[2] * sh.m[2], R1 = sh.r1, R2 = sh.r2, r1 = blockIdx.x;
-  float acc[kLayerMaxRank];
+  float acc[RB];
 #pragma unroll
-  for (int r = 0; r < kLayerMaxRank; ++r) acc[r] = 0.f;
+  for (int r = 0; r < RB; ++r) acc[r] = 0.f;
   for (int c = threadIdx.x; c < C; c += kLayerThreads) {
     const float g = dQ[static_cast<long long>(c) * R1 + r1];
     const float *u = u3 + static_cast<long long>(c) * R2;
 #pragma unroll
-    for (int r = 0; r < kLayerMaxRank; ++r)
+    for (int r = 0; r < RB; ++r)
       if (r < R2) acc[r] = fmaf(g, u[r], acc[r]);
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int r = 0; r < kLayerMaxRank; ++r) {
+  for (int r = 0; r < RB; ++r) {
     float v = acc[r];
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     if (lane == 0) red[warp][r] = v;
@@ -429,31 +484,6 @@ __global__ void __launch_bounds__(kLayerThreads) layer_db1_kernel(const LayerSha
     float v = 0.f;
     for (int w = 0; w < kLayerThreads / 32; ++w) v += red[w][r];
     db1[static_cast<long long>(r1) * R2 + r] = v;
-  }
-}
-
-// Stage 2: du1, db2 from dT1.
-__global__ void layer_grad2_kernel(const LayerShape sh, const float *__restrict__ u1, const float *__restrict__ b2,
-                                   const float *__restrict__ dT1, float *__restrict__ du1, float *__restrict__ db2) {
-  const int A = sh.n[0] * sh.m[0];
-  const int R1 = sh.r1, R3 = sh.r3, R4 = sh.r4;
-  const long long n_du1 = static_cast<long long>(A) * R3, n_db2 = static_cast<long long>(R3) * R4 * R1;
-  for (long long e = blockIdx.x * static_cast<long long>(kLayerThreads) + threadIdx.x; e < n_du1 + n_db2;
-       e += static_cast<long long>(gridDim.x) * kLayerThreads) {
-    if (e < n_du1) {
-      const int a = static_cast<int>(e / R3), r3 = static_cast<int>(e - static_cast<long long>(a) * R3);
-      float s = 0.f;
-      for (int q = 0; q < R4 * R1; ++q)
-        s = fmaf(dT1[static_cast<long long>(a) * R4 * R1 + q], b2[static_cast<long long>(r3) * R4 * R1 + q], s);
-      du1[e] = s;
-    } else {
-      const long long f = e - n_du1;
-      const int r3 = static_cast<int>(f / (R4 * R1)), q = static_cast<int>(f - static_cast<long long>(r3) * R4 * R1);
-      float s = 0.f;
-      for (int a = 0; a < A; ++a)
-        s = fmaf(u1[a * R3 + r3], dT1[static_cast<long long>(a) * R4 * R1 + q], s);
-      db2[f] = s;
-    }
   }
 }
 
@@ -513,7 +543,7 @@ cudaError_t bias_act_launch(float *y, const float *bias, long long batch, long l
 }
 
 int layer_colsum_chunks(long long batch) {
-  long long c = batch / 256;
+  long long c = (batch + 15) / 16;   // at most 16 rows of dy per thread at small batch
   if (c < 1) c = 1;
   if (c > 64) c = 64;
   return static_cast<int>(c);
@@ -569,13 +599,19 @@ cudaError_t layer_factor_grads_launch(const LayerShape &sh, const float *dW, con
     layer_dp_kernel<<<static_cast<unsigned>(A * B), kLayerThreads, smem, s>>>(sh, dW, Q, dP);
     layer_dq_kernel<<<static_cast<unsigned>(C), kLayerThreads, 0, s>>>(sh, dW, P, dQ);
   }
-  const long long n1 = static_cast<long long>(A) * sh.r4 * sh.r1 + static_cast<long long>(C) * sh.r2;
-  layer_grad1_kernel<<<grid_for_layer(n1), kLayerThreads, 0, s>>>(sh, u2, u3, b1, T1, dP, dQ, dT1, nullptr, du3,
-                                                                   nullptr);
-  layer_du2_kernel<<<static_cast<unsigned>(B), kLayerThreads, 0, s>>>(sh, dP, T1, du2);
-  layer_db1_kernel<<<static_cast<unsigned>(sh.r1), kLayerThreads, 0, s>>>(sh, dQ, u3, db1);
-  const long long n2 = static_cast<long long>(A) * sh.r3 + static_cast<long long>(sh.r3) * sh.r4 * sh.r1;
-  layer_grad2_kernel<<<grid_for_layer(n2), kLayerThreads, 0, s>>>(sh, u1, b2, dT1, du1, db2);
+  const long long du3_blocks = (static_cast<long long>(C) * sh.r2 + kLayerThreads - 1) / kLayerThreads;
+  layer_dt1_kernel<<<static_cast<unsigned>(A + du3_blocks), kLayerThreads, 0, s>>>(sh, u2, b1, dP, dQ, dT1, du3);
+  if (sh.r4 <= 16) layer_du2_kernel<16><<<static_cast<unsigned>(B), kLayerThreads, 0, s>>>(sh, dP, T1, du2);
+  else if (sh.r4 <= 32) layer_du2_kernel<32><<<static_cast<unsigned>(B), kLayerThreads, 0, s>>>(sh, dP, T1, du2);
+  else layer_du2_kernel<kLayerMaxRank><<<static_cast<unsigned>(B), kLayerThreads, 0, s>>>(sh, dP, T1, du2);
+  if (sh.r2 <= 16) layer_db1_kernel<16><<<static_cast<unsigned>(sh.r1), kLayerThreads, 0, s>>>(sh, dQ, u3, db1);
+  else if (sh.r2 <= 32) layer_db1_kernel<32><<<static_cast<unsigned>(sh.r1), kLayerThreads, 0, s>>>(sh, dQ, u3, db1);
+  else layer_db1_kernel<kLayerMaxRank><<<static_cast<unsigned>(sh.r1), kLayerThreads, 0, s>>>(sh, dQ, u3, db1);
+  const long long du1_blocks = (static_cast<long long>(A) * sh.r3 + kLayerThreads / 32 - 1) / (kLayerThreads / 32);
+  const long long db2_blocks =
+      (static_cast<long long>(sh.r3) * sh.r4 * sh.r1 + kLayerThreads - 1) / kLayerThreads;
+  layer_dt1_back_kernel<<<static_cast<unsigned>(du1_blocks + db2_blocks), kLayerThreads, 0, s>>>(
+      sh, u1, b2, dT1, du1, db2, static_cast<int>(du1_blocks));
   return cudaGetLastError();
 }
 

@@ -41,7 +41,23 @@ def layer_shape(n: Sequence[int], m: Sequence[int], ranks: Sequence[int]) -> HtL
     return s
 
 
+_SHAPES = {}
+
+
 def shape_of(u1, u2, u3, b2, b1) -> HtLayerShape:
+    """The C shape struct of a factor set (cached by the factors' shapes: the C
+    side only reads it)."""
+    key = (tuple(u1.shape), tuple(u2.shape), tuple(u3.shape), tuple(b2.shape), tuple(b1.shape))
+    sh = _SHAPES.get(key)
+    if sh is None:
+        sh = _make_shape(u1, u2, u3, b2, b1)
+        if len(_SHAPES) >= 256:
+            _SHAPES.clear()
+        _SHAPES[key] = sh
+    return sh
+
+
+def _make_shape(u1, u2, u3, b2, b1) -> HtLayerShape:
     for name, t, d in (("u1", u1, 3), ("u2", u2, 3), ("u3", u3, 3), ("b2", b2, 3), ("b1", b1, 2)):
         if t.dim() != d:
             raise ValueError(f"{name} must have {d} dimensions")
@@ -54,7 +70,7 @@ def shape_of(u1, u2, u3, b2, b1) -> HtLayerShape:
 def _dev(t):
     if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32):
         raise TypeError("HT layer tensors must be float32 CUDA tensors")
-    return t.contiguous()
+    return t if t.is_contiguous() else t.contiguous()
 
 
 def _stream(t):

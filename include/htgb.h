@@ -256,6 +256,9 @@ typedef struct {
     int gpu_launches;        /* kernels launched per batch                                   */
     int graph_replayed;      /* 1 when the cached CUDA graph of an identical batch ran       */
     int lanes;               /* concurrent streams the batch was spread over                 */
+    int grouped;             /* 1: every leaf eigen-problem ran in one grouped launch        */
+    float ms_phase[3];       /* grouped: device ms of the lanes up to the leaf Grams, of the
+                                grouped leaf solver, of the lanes after it (else 0)           */
 } ht_batch_report_t;
 
 /* Decompose `count` tensors of the same order in one call.  Replaces the

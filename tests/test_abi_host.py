@@ -212,3 +212,25 @@ def test_header_compiles_and_links_from_c_and_cpp(tmp_path, lang, compiler, flag
     run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert run.returncode == 0, (run.returncode, run.stderr)
     assert run.stdout.split()[-1] == "1"
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every ABI struct that the Python layer mirrors has the header's size
+    (compiled with gcc against include/htgb.h alone)."""
+    import ctypes
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not installed")
+    pairs = [("ht_tree_t", _lib.HtTree), ("ht_config_t", _lib.HtConfig), ("ht_report_t", _lib.HtReport),
+             ("ht_batch_report_t", _lib.HtBatchReport), ("ht_layer_shape_t", _lib.HtLayerShape)]
+    src = tmp_path / "sizes.c"
+    src.write_text('#include "htgb.h"\n#include <stdio.h>\nint main(void) {\n' +
+                   "".join(f'  printf("%zu\\n", sizeof({name}));\n' for name, _ in pairs) + "  return 0;\n}\n")
+    exe = tmp_path / "sizes"
+    r = subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60).stdout.split()
+    for (name, cls), size in zip(pairs, out):
+        assert ctypes.sizeof(cls) == int(size), (name, ctypes.sizeof(cls), size)

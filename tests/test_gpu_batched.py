@@ -66,6 +66,9 @@ def test_graph_replay_same_and_new_contents(family):
     e1 = [r.report["rel_err"] for r in r1]
     r2, rep2 = bd(xs)
     assert rep2["graph_replayed"], "identical second call must replay the recorded graph"
+    # small modes: every leaf in one grouped solver launch, timed inside the graph
+    assert rep2["grouped"] and min(rep2["ms_phase"].values()) > 0, rep2
+    assert sum(rep2["ms_phase"].values()) <= rep2["ms_total"] * 1.01 + 0.05
     for a, r in zip(U1, r2):
         for t in a:
             np.testing.assert_array_equal(a[t], r.U[t].cpu().numpy())
@@ -115,7 +118,8 @@ def test_batched_large_mode_uses_per_lane_solver(prec):
     for i, d in enumerate([(520, 24, 20), (40, 36, 32), (33, 47, 61)]):
         tree = ht.reference_tree_3d([1, 8, 6, 5, 7])
         pairs.append((synth.exact_ht(d, tree, noise_rel=1e-3, seed=300 + i), tree))
-    _check_batch(pairs, prec)
+    rep = _check_batch(pairs, prec)
+    assert not rep["grouped"]
 
 
 @pytest.mark.parametrize("prec", ["fp32", "bf16"])
