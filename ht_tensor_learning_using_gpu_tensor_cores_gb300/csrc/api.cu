@@ -211,6 +211,13 @@ struct Ctx {
   std::vector<unsigned char> *eig_table = nullptr;
   int eig_iters_used = 0, eig_refine_used = 0;
   bool mute_pre = false, mute_post = false, past_eig = false;
+  // Batched path: the tensor's conversion (with its ||X||^2) and the copies of
+  // its factors to the caller's buffers are left to one grouped launch each
+  // (defer_io), described into conv_out / copy_out when those are set.
+  bool defer_io = false;
+  std::vector<ConvJob> *conv_out = nullptr;
+  std::vector<CopySeg> *copy_out = nullptr;
+  std::vector<unsigned char> *gram_out[2] = {nullptr, nullptr};   // grouped Gram items by class
   bool dry() const { return ar.dry || (past_eig ? mute_post : mute_pre); }
 };
 
@@ -270,6 +277,19 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
     probe.a = q.a16; probe.b = q.b16; probe.splits = 1;
     std::string why;
     if (!tc_gemm_supported(probe, q.bn_tc, &why)) use_tc = false;
+  }
+  // grouped batch (eig_mode != 0): a leaf Gram of a mode of at most 256 is one
+  // item of the batch's grouped Gram launch -- described by the plan pass,
+  // launched by the batch, never launched here
+  const int gcls = tc_gram_class(q.t_n);
+  if (c.eig_mode != 0 && use_tc && q.tiles_kind == TILES_GRAM && q.a16.ptr == q.b16.ptr && !q.accumulate &&
+      !q.part_ext && gcls >= 0) {
+    if (c.gram_out[gcls] && !c.ar.dry) {
+      std::string why;
+      if (!tc_gram_item(q.a16, q.t_n, q.out, c.err, *c.gram_out[gcls], &why))
+        return fail(HT_ERR_CUDA, "grouped Gram item: " + why);
+    }
+    return HT_OK;
   }
   const int bn = use_tc ? q.bn_tc : q.bn_simt;
   const int mt = use_tc ? q.mt_tc : 1;
@@ -1388,11 +1408,29 @@ ht_status_t enqueue_body(Ctx &c, const Tree &T, const ht_config_t &cfg, const fl
   // (the tcgen05 path's TMA rows must be 16-byte multiples); the other products
   // of such a tensor run on the FP32 operands
   const long n1 = a.dims[0], n1p = (n1 + 7) / 8 * 8;
+  // grouped conversion job of the batched path (plain or padded copy, or sums only)
+  auto defer = [&](__nv_bfloat16 *dst, long pad) {
+    if (c.conv_out) {
+      ConvJob j;
+      j.x = xd; j.xb = dst; j.partials = nparts; j.dsum = dsum;
+      j.n1 = n1; j.n1p = pad; j.rest = total / n1;
+      j.blk0 = 0;
+      j.nblk = static_cast<int>(std::min<long long>(1024, std::max<long long>(1, (pad * (total / n1)) / 4096)));
+      c.conv_out->push_back(j);
+    }
+  };
   if (c.tc && n1 % 8 != 0 && cfg.leaf_method == HT_LEAF_GRAM) {
     xp = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total / n1 * n1p) + 64);
     if (!xp) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (padded bf16 tensor)");
-    if (!c.dry()) HT_CUDA(convert_bf16_pad_launch(xd, xp, n1, n1p, total / n1, nparts, 1024, c.st));
+    if (c.defer_io) defer(xp, n1p);
+    else if (!c.dry()) HT_CUDA(convert_bf16_pad_launch(xd, xp, n1, n1p, total / n1, nparts, 1024, c.st));
     lb = 0;
+  } else if (c.tc && c.defer_io && !(lb && (reinterpret_cast<uintptr_t>(xd) & 15u) == 0)) {
+    xb = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
+    if (!xb) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (bf16 tensor)");
+    defer(xb, n1);
+  } else if (!c.tc && c.defer_io) {
+    defer(nullptr, n1);
   } else if (c.tc) {
     xb = c.ar.take<__nv_bfloat16>(static_cast<size_t>(total) + 64);
     if (!xb) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (bf16 tensor)");
@@ -1407,7 +1445,8 @@ ht_status_t enqueue_body(Ctx &c, const Tree &T, const ht_config_t &cfg, const fl
   } else if (!c.dry()) {
     HT_CUDA(sumsq_launch(xd, total, nparts, 1024, c.st));
   }
-  if (!c.dry()) {
+  const bool deferred = c.defer_io && !xbt;
+  if (!c.dry() && !deferred) {
     HT_CUDA(sumsq_finish_launch(nparts, 1024, dsum, c.st));
     c.launches += 2;
   }
@@ -1418,7 +1457,12 @@ ht_status_t enqueue_body(Ctx &c, const Tree &T, const ht_config_t &cfg, const fl
   for (int t = 0; t < T.n_nodes; ++t) {
     float *dst = T.leaf(t) ? a.U[t] : a.B[t];
     const float *src = T.leaf(t) ? res.U[t] : res.B[t];
-    if (dst && !c.dry()) HT_CUDA(cudaMemcpyAsync(dst, src, factor_count(T, a.dims, t) * sizeof(float), cudaMemcpyDefault, c.st));
+    if (!dst) continue;
+    if (c.defer_io) {
+      if (c.copy_out) c.copy_out->push_back(CopySeg{src, dst, static_cast<long long>(factor_count(T, a.dims, t))});
+    } else if (!c.dry()) {
+      HT_CUDA(cudaMemcpyAsync(dst, src, factor_count(T, a.dims, t) * sizeof(float), cudaMemcpyDefault, c.st));
+    }
   }
   if (a.want_err) HT_TRY(error_core(c, T, xd, a.dims, a.order, res.U, res.B, dsum + 1));
   return HT_OK;
@@ -1554,7 +1598,12 @@ ht_status_t enqueue_pipelined(Ctx &c, const Tree &T, const ht_config_t &cfg, con
   for (int t = 0; t < T.n_nodes; ++t) {
     float *dst = T.leaf(t) ? a.U[t] : a.B[t];
     const float *src = T.leaf(t) ? res.U[t] : res.B[t];
-    if (dst && !c.dry()) HT_CUDA(cudaMemcpyAsync(dst, src, factor_count(T, a.dims, t) * sizeof(float), cudaMemcpyDefault, c.st));
+    if (!dst) continue;
+    if (c.defer_io) {
+      if (c.copy_out) c.copy_out->push_back(CopySeg{src, dst, static_cast<long long>(factor_count(T, a.dims, t))});
+    } else if (!c.dry()) {
+      HT_CUDA(cudaMemcpyAsync(dst, src, factor_count(T, a.dims, t) * sizeof(float), cudaMemcpyDefault, c.st));
+    }
   }
   if (a.want_err) HT_TRY(error_core(c, T, xd, a.dims, a.order, res.U, res.B, dsum + 1));
   return HT_OK;
@@ -1697,6 +1746,12 @@ struct BatchState {
   int launches = 0, lanes = 0;
   void *table = nullptr;    // device: the grouped leaf solver's problem table
   size_t table_bytes = 0;
+  void *conv = nullptr;     // device: grouped conversion jobs
+  size_t conv_bytes = 0;
+  void *copies = nullptr;   // device: grouped output copies
+  size_t copies_bytes = 0;
+  void *grams = nullptr;    // device: grouped Gram items, class 0 then class 1
+  size_t grams_bytes = 0;
 };
 
 // Workspace layout of one batch.  Per-lane mode: tensor i runs in lane
@@ -1709,6 +1764,8 @@ struct BatchLayout {
   size_t lane_bytes = 0;
   std::vector<size_t> off;
   int nprob = 0, iters = 0, refine = 0;
+  int nconv = 0, conv_blocks = 0, ncopy = 0;   // grouped conversion jobs (their blocks), output copies
+  int ngram[2] = {0, 0};                       // grouped Grams per class
 };
 // Leaves of at most this size go through the grouped solver (one CTA each);
 // batches with larger modes keep the per-lane cooperative solver.
@@ -1746,7 +1803,9 @@ ht_status_t batch_streams(BatchState &b) {
 ht_status_t batch_pass(BatchState &b, const BatchLayout &L, int phase, cudaStream_t st, int count,
                        const float *const *x, const long *dims, int order, const std::vector<Tree> &trees,
                        const ht_config_t &cfg, float *const *U, float *const *B, bool want_err, int eig_ctas,
-                       std::vector<unsigned char> *table, int *iters_used, int *refine_used) {
+                       std::vector<unsigned char> *table, int *iters_used, int *refine_used,
+                       std::vector<ConvJob> *conv = nullptr, std::vector<CopySeg> *copies = nullptr,
+                       std::vector<unsigned char> *grams = nullptr) {
   if (phase != 3) {
     HT_CUDA(cudaEventRecord(b.fork, st));
     for (int l = 0; l < b.lanes; ++l) HT_CUDA(cudaStreamWaitEvent(b.lane[l], b.fork, 0));
@@ -1765,6 +1824,13 @@ ht_status_t batch_pass(BatchState &b, const BatchLayout &L, int phase, cudaStrea
       c.eig_table = table;
       c.mute_pre = phase == 2 || phase == 3;
       c.mute_post = phase == 1 || phase == 3;
+      c.defer_io = true;
+      c.conv_out = conv;
+      c.copy_out = copies;
+      if (grams) {
+        c.gram_out[0] = &grams[0];
+        c.gram_out[1] = &grams[1];
+      }
     } else {
       c.ar.base = static_cast<char *>(b.ws) + static_cast<size_t>(l) * L.lane_bytes;
       c.ar.cap = L.lane_bytes;
@@ -1801,6 +1867,11 @@ ht_status_t batch_enqueue(BatchState &b, const BatchLayout &L, cudaStream_t st, 
   if (!L.grouped)
     return batch_pass(b, L, 0, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas, nullptr, nullptr,
                       nullptr);
+  HT_CUDA(convert_grouped_launch(static_cast<const ConvJob *>(b.conv), L.nconv, L.conv_blocks, st));
+  b.launches += L.nconv > 0 ? 2 : 0;
+  HT_CUDA(tc_gram_grouped_launch(0, b.grams, L.ngram[0], st));
+  HT_CUDA(tc_gram_grouped_launch(1, static_cast<char *>(b.grams) + tc_gram_item_bytes() * L.ngram[0], L.ngram[1], st));
+  b.launches += (L.ngram[0] > 0) + (L.ngram[1] > 0);
   HT_TRY(batch_pass(b, L, 1, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas, nullptr, nullptr,
                     nullptr));
   // external records: inside a capture they become event-record nodes of the graph
@@ -1808,8 +1879,24 @@ ht_status_t batch_enqueue(BatchState &b, const BatchLayout &L, cudaStream_t st, 
   HT_CUDA(eig_grouped_launch(b.table, L.nprob, L.iters, L.refine, st));
   HT_CUDA(cudaEventRecordWithFlags(b.tp[1], st, cudaEventRecordExternal));
   b.launches += 1;
-  return batch_pass(b, L, 2, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas, nullptr, nullptr,
-                    nullptr);
+  HT_TRY(batch_pass(b, L, 2, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas, nullptr, nullptr,
+                    nullptr));
+  HT_CUDA(copy_segments_launch(static_cast<const CopySeg *>(b.copies), L.ncopy, st));
+  b.launches += L.ncopy > 0 ? 1 : 0;
+  return HT_OK;
+}
+
+// Copy a host table into a device buffer that grows as needed.
+ht_status_t upload_table(void *&buf, size_t &cap, const void *data, size_t bytes) {
+  if (bytes > cap) {
+    if (buf) HT_CUDA(cudaFree(buf));
+    buf = nullptr;
+    cap = 0;
+    HT_CUDA(cudaMalloc(&buf, bytes));
+    cap = bytes;
+  }
+  if (bytes) HT_CUDA(cudaMemcpy(buf, data, bytes, cudaMemcpyHostToDevice));
+  return HT_OK;
 }
 
 // Host-only pass that lays out every leaf problem of the batch for the
@@ -1818,22 +1905,33 @@ ht_status_t batch_plan_grouped(BatchState &b, BatchLayout &L, int count, const f
                                int order, const std::vector<Tree> &trees, const ht_config_t &cfg, float *const *U,
                                float *const *B, bool want_err) {
   std::vector<unsigned char> table;
+  std::vector<ConvJob> conv;
+  std::vector<CopySeg> copies;
+  std::vector<unsigned char> grams[2];
   int iters = 0, refine = 0;
   const int launches = b.launches;
-  HT_TRY(batch_pass(b, L, 3, nullptr, count, x, dims, order, trees, cfg, U, B, want_err, 0, &table, &iters, &refine));
+  HT_TRY(batch_pass(b, L, 3, nullptr, count, x, dims, order, trees, cfg, U, B, want_err, 0, &table, &iters, &refine,
+                    &conv, &copies, grams));
+  L.ngram[0] = static_cast<int>(grams[0].size() / tc_gram_item_bytes());
+  L.ngram[1] = static_cast<int>(grams[1].size() / tc_gram_item_bytes());
+  grams[0].insert(grams[0].end(), grams[1].begin(), grams[1].end());
+  HT_TRY(upload_table(b.grams, b.grams_bytes, grams[0].data(), grams[0].size()));
   b.launches = launches;
   eig_grouped_order(table);
   L.nprob = static_cast<int>(table.size() / eig_grouped_entry_bytes());
   L.iters = iters;
   L.refine = refine;
-  if (table.size() > b.table_bytes) {
-    if (b.table) HT_CUDA(cudaFree(b.table));
-    b.table = nullptr;
-    b.table_bytes = 0;
-    HT_CUDA(cudaMalloc(&b.table, table.size()));
-    b.table_bytes = table.size();
+  int blk = 0;
+  for (ConvJob &j : conv) {
+    j.blk0 = blk;
+    blk += j.nblk;
   }
-  if (!table.empty()) HT_CUDA(cudaMemcpy(b.table, table.data(), table.size(), cudaMemcpyHostToDevice));
+  L.nconv = static_cast<int>(conv.size());
+  L.conv_blocks = blk;
+  L.ncopy = static_cast<int>(copies.size());
+  HT_TRY(upload_table(b.table, b.table_bytes, table.data(), table.size()));
+  HT_TRY(upload_table(b.conv, b.conv_bytes, conv.data(), sizeof(ConvJob) * conv.size()));
+  HT_TRY(upload_table(b.copies, b.copies_bytes, copies.data(), sizeof(CopySeg) * copies.size()));
   return HT_OK;
 }
 
@@ -2331,6 +2429,15 @@ ht_status_t ht_release_batch(void) {
   if (b.table) HT_CUDA(cudaFree(b.table));
   b.table = nullptr;
   b.table_bytes = 0;
+  if (b.conv) HT_CUDA(cudaFree(b.conv));
+  b.conv = nullptr;
+  b.conv_bytes = 0;
+  if (b.copies) HT_CUDA(cudaFree(b.copies));
+  b.copies = nullptr;
+  b.copies_bytes = 0;
+  if (b.grams) HT_CUDA(cudaFree(b.grams));
+  b.grams = nullptr;
+  b.grams_bytes = 0;
   return HT_OK;
 }
 

@@ -86,6 +86,16 @@ struct GemmArgs {
 // Returns false (and fills *why) when the operand shapes cannot be expressed as
 // TMA tensor maps (strides not multiples of 16 bytes, dims too large).
 bool tc_gemm_supported(const GemmArgs &g, int bn, std::string *why);
+// Grouped Grams of the batched path: one CTA per n x n Gram (n <= 256), the
+// whole K range as one tile written column-major to G (ld = n).  Class 0:
+// n <= 128 (128 x 128 tiles), class 1: n <= 256 (256 x 256); -1: not grouped.
+// tc_gram_item appends an item (tensor maps included) to `out` (false: the
+// operand cannot be read by TMA; why says so); the items of one class are
+// copied to device memory (64-byte aligned) for tc_gram_grouped_launch.
+int tc_gram_class(long n);
+size_t tc_gram_item_bytes();
+bool tc_gram_item(const Operand &a, long n, float *G, int *err, std::vector<unsigned char> &out, std::string *why);
+cudaError_t tc_gram_grouped_launch(int cls, const void *items_dev, int count, cudaStream_t s);
 cudaError_t tc_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s);
 // One-time set-up (kernel attributes, the tensor-map encoder) so that later
 // launches can be recorded into a CUDA graph.
@@ -135,6 +145,27 @@ cudaError_t round_bf16_launch(float *x, __nv_bfloat16 *y, long long n, cudaStrea
 // BF16 rounding hi(W), columns [h, h + k) the rounding of W - hi(W), the rest 0.
 cudaError_t split_bf16_launch(const float *W, long long rows, int k, int h, __nv_bfloat16 *Y, cudaStream_t s);
 cudaError_t sumsq_finish_launch(const double *partials, int n, double *out, cudaStream_t s);
+// Grouped conversion of a batch (one launch for every tensor, then one finish
+// launch): job j converts x (n1 x rest, FP32) to xb (n1p x rest BF16, rows
+// zero-padded; null: sums only) in blocks [blk0, blk0 + nblk) of the launch
+// (jobs in ascending blk0, nblk <= the capacity of partials) and leaves
+// ||x||^2 in dsum[0].  The job table lives in device memory.
+struct ConvJob {
+  const float *x;
+  __nv_bfloat16 *xb;
+  double *partials, *dsum;
+  long long n1, n1p, rest;
+  int blk0, nblk;
+};
+cudaError_t convert_grouped_launch(const ConvJob *jobs_dev, int njobs, int total_blocks, cudaStream_t s);
+// dst[0, count) = src[0, count) for every segment, one launch (table in device memory).
+struct CopySeg {
+  const float *src;
+  float *dst;
+  long long count;
+};
+cudaError_t copy_segments_launch(const CopySeg *segs_dev, int nseg, cudaStream_t s);
+
 // C (m x n) = A^T B with A (K x m), B (K x n), column-major, compensated FP32.
 cudaError_t gemm_tn_small_launch(const float *A, int lda, const float *B, int ldb, float *C, int ldc, int m, int n,
                                  int K, cudaStream_t s);

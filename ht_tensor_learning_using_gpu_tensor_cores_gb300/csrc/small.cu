@@ -149,6 +149,62 @@ __global__ void sumsq_kernel(const float *__restrict__ x, long long n, double *p
   if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
 }
 
+// Grouped conversion of a batch: job j owns blocks [blk0, blk0 + nblk) of the
+// launch and converts its tensor x (n1 x rest, FP32) to xb (n1p x rest, BF16,
+// rows padded with zeros; xb null: sums only), writing one compensated
+// partial sum of squares per block; the finish kernel (a block per job) sums
+// a job's partials in block order into its dsum[0].
+__global__ void __launch_bounds__(256) convert_grouped_kernel(const ConvJob *__restrict__ jobs, int njobs) {
+  __shared__ ConvJob J;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = njobs - 1;   // last job with blk0 <= blockIdx.x
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].blk0 <= static_cast<int>(blockIdx.x)) lo = mid;
+      else hi = mid - 1;
+    }
+    J = jobs[lo];
+  }
+  __syncthreads();
+  const int b = blockIdx.x - J.blk0;
+  Acc2 a = {0.f, 0.f};
+  const long long total = J.n1p * J.rest;
+  for (long long e = b * 256ll + threadIdx.x; e < total; e += J.nblk * 256ll) {
+    const long long r = e / J.n1p, i = e - r * J.n1p;
+    const float v = i < J.n1 ? __ldcs(J.x + i + J.n1 * r) : 0.f;
+    acc2_add_prod(a, v, v);
+    if (J.xb) J.xb[e] = __float2bfloat16_rn(v);
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = static_cast<double>(a.s) + static_cast<double>(a.c);
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) J.partials[b] = red[0];
+}
+
+__global__ void convert_grouped_finish_kernel(const ConvJob *__restrict__ jobs) {
+  const ConvJob &J = jobs[blockIdx.x];
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < J.nblk; i += 256) s += J.partials[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) J.dsum[0] = red[0];
+}
+
+// Grouped copy: block i copies segment segs[i] (count floats).
+__global__ void copy_segments_kernel(const CopySeg *__restrict__ segs) {
+  const CopySeg g = segs[blockIdx.x];
+  for (long long e = threadIdx.x; e < g.count; e += 256) g.dst[e] = g.src[e];
+}
+
 // x[i] = the BF16 rounding of x[i] (kept in FP32), and the BF16 copy in y.
 __global__ void round_bf16_kernel(float *__restrict__ x, __nv_bfloat16 *__restrict__ y, long long n) {
   for (long long i = blockIdx.x * 256ll + threadIdx.x; i < n; i += gridDim.x * 256ll) {
@@ -462,6 +518,21 @@ cudaError_t round_bf16_launch(float *x, __nv_bfloat16 *y, long long n, cudaStrea
 
 cudaError_t split_bf16_launch(const float *W, long long rows, int k, int h, __nv_bfloat16 *Y, cudaStream_t s) {
   split_bf16_kernel<<<grid_for(rows * 2 * h), 256, 0, s>>>(W, rows, k, h, Y);
+  return cudaGetLastError();
+}
+
+cudaError_t convert_grouped_launch(const ConvJob *jobs_dev, int njobs, int total_blocks, cudaStream_t s) {
+  if (njobs < 1) return cudaSuccess;
+  if (!jobs_dev || total_blocks < njobs) return cudaErrorInvalidValue;
+  convert_grouped_kernel<<<total_blocks, 256, 0, s>>>(jobs_dev, njobs);
+  convert_grouped_finish_kernel<<<njobs, 256, 0, s>>>(jobs_dev);
+  return cudaGetLastError();
+}
+
+cudaError_t copy_segments_launch(const CopySeg *segs_dev, int nseg, cudaStream_t s) {
+  if (nseg < 1) return cudaSuccess;
+  if (!segs_dev) return cudaErrorInvalidValue;
+  copy_segments_kernel<<<nseg, 256, 0, s>>>(segs_dev);
   return cudaGetLastError();
 }
 

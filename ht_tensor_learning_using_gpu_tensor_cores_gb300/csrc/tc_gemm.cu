@@ -21,6 +21,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cstring>
 #include <mutex>
 
 #include "common.cuh"
@@ -83,10 +84,11 @@ HT_DEV uint64_t op_desc(int kind, uint32_t base, int kk) {
   return make_sdesc_sw128(base + kk * 32, 16, 1024);
 }
 
+// One output tile (split `split` of its K range) of a CTA; the tensor maps
+// may live in the kernel parameters or in global memory.
 template <int BN, int MT>
-__global__ void __launch_bounds__(kThreads, 1)
-    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                   const KParams p, const TileGen gen) {
+HT_DEV void tc_gemm_tile(const CUtensorMap *tmA, const CUtensorMap *tmB, const KParams &p, const Tile &tile,
+                         int tile_idx, int split) {
   using C = TcCfg<BN, MT>;
   constexpr int BMT = BM * MT;
   extern __shared__ uint8_t smem_raw[];
@@ -98,9 +100,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tile_idx = blockIdx.x % p.num_tiles;
-  const int split = blockIdx.x / p.num_tiles;
-  const Tile tile = gen_tile(gen, tile_idx);
   const int kb0 = split * p.kb_per_split;
   const int nk = max(0, min(p.num_kb, kb0 + p.kb_per_split) - kb0);
   // a diagonal tile of a Gram with BN == BMT: A's rows are B's rows, so A is
@@ -115,8 +114,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     mbar_init(done, 1);
     *abort_flag = 0;
     mbar_fence_init();
-    tma_prefetch_desc(&tmA);
-    tma_prefetch_desc(&tmB);
+    tma_prefetch_desc(tmA);
+    tma_prefetch_desc(tmB);
   }
   if (warp == 1) {
     tmem_alloc(tmem_slot, C::TMEM_COLS);
@@ -141,8 +140,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         uint8_t *sa = smem + s * C::STAGE_BYTES;
         uint8_t *sb = sa + C::A_BYTES;
         mbar_arrive_expect_tx(&full[s], a_in_b ? C::B_BYTES : C::STAGE_BYTES);
-        if (!a_in_b) load_operand<BMT>(&tmA, p.a_kind, p.a_lblocks, kb0 + i, tile.a_row, tile.a_z, sa, &full[s]);
-        load_operand<BN>(&tmB, p.b_kind, p.b_lblocks, kb0 + i, tile.b_row, 0, sb, &full[s]);
+        if (!a_in_b) load_operand<BMT>(tmA, p.a_kind, p.a_lblocks, kb0 + i, tile.a_row, tile.a_z, sa, &full[s]);
+        load_operand<BN>(tmB, p.b_kind, p.b_lblocks, kb0 + i, tile.b_row, 0, sb, &full[s]);
         issued = i + 1;
       }
       if (*abort_flag) {
@@ -233,6 +232,30 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_fence_after();
     tmem_dealloc(tmem, C::TMEM_COLS);
   }
+}
+
+template <int BN, int MT>
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   const KParams p, const TileGen gen) {
+  const int tile_idx = blockIdx.x % p.num_tiles;
+  tc_gemm_tile<BN, MT>(&tmA, &tmB, p, gen_tile(gen, tile_idx), tile_idx, blockIdx.x / p.num_tiles);
+}
+
+// Grouped Grams of a batch: CTA i computes items[i]'s whole n x n Gram
+// (n <= BM * MT) as one tile over its full K range, written column-major.
+struct GramItem {
+  CUtensorMap map_a, map_b;   // 64-byte aligned (CUtensorMap's own alignment)
+  KParams p;
+  Tile tile;
+};
+
+template <int BN, int MT>
+__global__ void __launch_bounds__(kThreads, 1) tc_gram_grouped_kernel(const GramItem *__restrict__ items) {
+  const GramItem &it = items[blockIdx.x];
+  const KParams p = it.p;
+  const Tile tile = it.tile;
+  tc_gemm_tile<BN, MT>(&it.map_a, &it.map_b, p, tile, 0, 0);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -345,9 +368,72 @@ cudaError_t launch_bn(const GemmArgs &g, cudaStream_t s) {
 
 long tc_num_kblocks(const Operand &a) { return kblocks_of(a); }
 
+// ---- grouped Grams of the batched path
+int tc_gram_class(long n) { return n <= BM ? 0 : (n <= 2 * BM ? 1 : -1); }
+
+size_t tc_gram_item_bytes() { return sizeof(GramItem); }
+
+bool tc_gram_item(const Operand &a, long n, float *G, int *err, std::vector<unsigned char> &out, std::string *why) {
+  const int cls = tc_gram_class(n);
+  if (cls < 0 || !check_operand(a, why)) return false;
+  GramItem it;
+  std::memset(&it, 0, sizeof(it));
+  const int bmt = cls == 0 ? BM : 2 * BM, bn = cls == 0 ? BM : 2 * BM;
+  if (!make_map(a, bmt, &it.map_a, why) || !make_map(a, bn, &it.map_b, why)) return false;
+  KParams &p = it.p;
+  p.a_kind = p.b_kind = a.kind;
+  p.a_lblocks = p.b_lblocks = int((a.d0 + BK - 1) / BK);
+  p.num_kb = int(kblocks_of(a));
+  p.kb_per_split = p.num_kb;
+  p.num_tiles = 1;
+  p.out_mode = OUT_COLMAJOR;
+  p.out = G;
+  p.ld_out = n;
+  p.err = err;
+  p.fold = 0;
+  p.same = 1;
+  p.out16 = nullptr;
+  it.tile.a_row = it.tile.b_row = it.tile.a_z = 0;
+  it.tile.valid_rows = int(n);
+  it.tile.out_row = 0;
+  it.tile.out_col = 0;
+  it.tile.valid_cols = int(n);
+  const unsigned char *raw = reinterpret_cast<const unsigned char *>(&it);
+  out.insert(out.end(), raw, raw + sizeof(it));
+  return true;
+}
+
+template <int BN, int MT>
+cudaError_t set_grouped_smem() {
+  static bool done[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (done[dev]) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(tc_gram_grouped_kernel<BN, MT>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(TcCfg<BN, MT>::SMEM));
+  if (e == cudaSuccess) done[dev] = true;
+  return e;
+}
+
+cudaError_t tc_gram_grouped_launch(int cls, const void *items_dev, int count, cudaStream_t s) {
+  if (count < 1) return cudaSuccess;
+  if (!items_dev || (reinterpret_cast<uintptr_t>(items_dev) % alignof(GramItem)) != 0) return cudaErrorInvalidValue;
+  const GramItem *it = static_cast<const GramItem *>(items_dev);
+  if (cls == 0) {
+    tc_gram_grouped_kernel<128, 1><<<count, kThreads, TcCfg<128, 1>::SMEM, s>>>(it);
+  } else if (cls == 1) {
+    tc_gram_grouped_kernel<256, 2><<<count, kThreads, TcCfg<256, 2>::SMEM, s>>>(it);
+  } else {
+    return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t tc_prepare() {
   if (!encode_fn()) return cudaErrorNotSupported;
   cudaError_t e;
+  if ((e = set_grouped_smem<128, 1>()) != cudaSuccess) return e;
+  if ((e = set_grouped_smem<256, 2>()) != cudaSuccess) return e;
   if ((e = set_smem<64, 1>()) != cudaSuccess) return e;
   if ((e = set_smem<128, 1>()) != cudaSuccess) return e;
   if ((e = set_smem<256, 1>()) != cudaSuccess) return e;

@@ -131,3 +131,16 @@ def test_batched_4d_and_direct_leaves(prec):
         tree = ht.balanced_tree_4d([1, 12, 12, 6, 6, 6, 6])
         pairs.append((synth.exact_ht(d, tree, noise_rel=1e-3, seed=400 + i), tree))
     _check_batch(pairs, prec)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_batched_grouped_gram_classes(prec):
+    """Modes of at most 128 and 129..256 (the two grouped Gram tile classes),
+    a mode of 260 (its Gram launched on its own inside a grouped batch), first
+    modes that are not multiples of 8 (padded BF16 copies) and one that is."""
+    pairs = []
+    for i, d in enumerate([(150, 40, 200), (260, 30, 24), (64, 129, 33), (37, 256, 45)]):
+        tree = ht.reference_tree_3d([1, 10, 8, 9, 7])
+        pairs.append((synth.exact_ht(d, tree, noise_rel=1e-3, seed=500 + i), tree))
+    rep = _check_batch(pairs, prec)
+    assert rep["grouped"]
