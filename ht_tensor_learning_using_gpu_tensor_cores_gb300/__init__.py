@@ -374,8 +374,9 @@ class BatchDecomposer:
         summary = {"rel_err_p50": rep.rel_err_p50, "rel_err_p99": rep.rel_err_p99, "rel_err_max": rep.rel_err_max,
                    "ms_total": rep.ms_total, "gpu_launches": rep.gpu_launches, "graph_replayed": bool(rep.graph_replayed),
                    "lanes": rep.lanes, "grouped": bool(rep.grouped),
-                   "ms_phase": {"lanes_to_grams": rep.ms_phase[0], "grouped_leaf_solver": rep.ms_phase[1],
-                                "lanes_after": rep.ms_phase[2]},
+                   "ms_phase": {name: rep.ms_phase[i] for i, name in enumerate(
+                       ["conversion_grams", "leaf_solver", "core_pass_lanes", "transfer_tails", "error_pass",
+                        "copies"])},
                    "note": (lib().ht_last_error() or b"").decode()}
         return results, summary
 

@@ -48,7 +48,7 @@ class HtReport(Structure):
 class HtBatchReport(Structure):
     _fields_ = [("rel_err_p50", c_double), ("rel_err_p99", c_double), ("rel_err_max", c_double),
                 ("ms_total", c_float), ("gpu_launches", c_int), ("graph_replayed", c_int), ("lanes", c_int),
-                ("grouped", c_int), ("ms_phase", c_float * 3)]
+                ("grouped", c_int), ("ms_phase", c_float * 6)]
 
 
 class HtLayerShape(Structure):

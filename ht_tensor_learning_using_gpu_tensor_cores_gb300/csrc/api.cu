@@ -201,16 +201,20 @@ struct Ctx {
   int path = 0;         // bit 0 tcgen05, bit 1 SIMT
   bool tc = false;
   int eig_ctas = 0;     // cap on the cooperative eigen-solver's grid (0 = every SM)
-  // Two-phase enqueue of the batched path.  eig_mode 0: leaf_eigs launches
-  // the cooperative solver; 1: it appends its problems to eig_table (the
-  // grouped solver's entries) and launches nothing; 2: it launches nothing
-  // (the batch launches the grouped solver).  Launches before the leaf
-  // solver (mute_pre) or after it (mute_post) are skipped while the arena
-  // still hands out the same real pointers, so the phases of one tensor agree.
+  // Staged enqueue of the batched path.  eig_mode 0: leaf_eigs launches the
+  // cooperative solver; 1: it appends its problems to eig_table (the grouped
+  // solver's entries) and launches nothing; 2: it launches nothing (the batch
+  // launches the grouped solver).  Every launch belongs to a stage -- 0 before
+  // the leaf solver, 1 after it, 2 the 3rd-order transfer tail, 3 the error
+  // pass (4 for 3rd order) -- and only the stages in `live` launch; the arena still hands out
+  // the same real pointers, so a tensor's passes agree on every buffer.
   int eig_mode = 0;
   std::vector<unsigned char> *eig_table = nullptr;
   int eig_iters_used = 0, eig_refine_used = 0;
-  bool mute_pre = false, mute_post = false, past_eig = false;
+  int stage = 0;
+  unsigned live = ~0u;
+  std::vector<TailJob> *tail_out = nullptr;   // grouped transfer tails (3rd order)
+  std::vector<ErrJob> *err_out = nullptr;     // grouped error passes (3rd order, stage 4)
   // Batched path: the tensor's conversion (with its ||X||^2) and the copies of
   // its factors to the caller's buffers are left to one grouped launch each
   // (defer_io), described into conv_out / copy_out when those are set.
@@ -218,7 +222,7 @@ struct Ctx {
   std::vector<ConvJob> *conv_out = nullptr;
   std::vector<CopySeg> *copy_out = nullptr;
   std::vector<unsigned char> *gram_out[2] = {nullptr, nullptr};   // grouped Gram items by class
-  bool dry() const { return ar.dry || (past_eig ? mute_post : mute_pre); }
+  bool dry() const { return ar.dry || !((live >> stage) & 1u); }
 };
 
 View view_of_group(const long *dims, int order, int lo, int hi) {   // modes [lo, hi]
@@ -688,7 +692,7 @@ ht_status_t leaf_eigs(Ctx &c, const Tree &T, const ht_config_t &cfg, const long 
     bool sketched = false;
     for (int m = 0; m < order; ++m) sketched = sketched || cfg.sketch[m] != nullptr;
     const int refine = (cfg.precision == HT_PREC_FP32 || iters < 4 || sketched) ? 2 : 0;
-    c.past_eig = true;
+    c.stage = 1;
     c.eig_iters_used = iters;
     c.eig_refine_used = refine;
     if (c.eig_mode == 1 && !c.ar.dry) HT_CUDA(eig_grouped_fill(ep, order, ews, eb, *c.eig_table));
@@ -876,6 +880,16 @@ ht_status_t transfer3_from_z(Ctx &c, const Plan3 &P, const long *dims, const Eig
   const EigProblem &ec = ep[P.mc];
   HT_TRY(core_contract(c, Z, static_cast<int>(dims[P.mp]), static_cast<int>(dims[P.mq]), P.kt, ep[P.mp].U, P.kp,
                        ep[P.mq].U, P.kq, tr.C));
+  const int stage_before = c.stage;
+  c.stage = 2;
+  if (c.tail_out && !c.ar.dry && !WG_ready) {
+    TailJob j;
+    j.U = ec.U; j.GU = ec.GU; j.C = tr.C;
+    j.M = tr.M; j.Bkt = tr.Bkt; j.Broot = tr.Broot; j.Bt = tr.Bt;
+    j.kpq = static_cast<long long>(P.kp) * P.kq;
+    j.nc = static_cast<int>(dims[P.mc]); j.kw = P.kw; j.kt = P.kt; j.kc = P.kc; j.t_is_left = P.t_is_left ? 1 : 0;
+    c.tail_out->push_back(j);
+  }
   if (!c.dry()) {
     const int nc = static_cast<int>(dims[P.mc]);
     if (!WG_ready) {
@@ -891,6 +905,7 @@ ht_status_t transfer3_from_z(Ctx &c, const Plan3 &P, const long *dims, const Eig
       ++c.launches;
     }
   }
+  c.stage = stage_before;
   res.B[P.t] = tr.Bt;
   res.B[0] = P.t_is_left ? tr.Bkt : tr.Broot;
   return HT_OK;
@@ -955,12 +970,14 @@ ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const 
     // Z = X_(t) V by ~2^-9 of X's energy, which dominates the error of nearly
     // exact low-rank inputs.
     const int fold_h = kz <= 32 ? 32 : 64;
+    // (no BF16 copy of X in its plain layout -- a first mode padded for the
+    // Grams -- means an FP32 product: no split V either)
     __nv_bfloat16 *V16 =
-        c.tc ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(dims[P.mc]) * 2 * fold_h + 64) : nullptr;
+        (c.tc && x16) ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(dims[P.mc]) * 2 * fold_h + 64) : nullptr;
     float *Rz = sketch ? c.ar.take<float>(static_cast<size_t>(kz) * kz) : nullptr;
     const size_t qbytes = sketch ? tsqr_workspace_bytes(zrows, kz) : 0;
     void *qws = sketch ? c.ar.take<char>(qbytes) : nullptr;
-    if (!Z || (c.tc && !V16) || (sketch && (!Rz || !qws)))
+    if (!Z || (c.tc && x16 && !V16) || (sketch && (!Rz || !qws)))
       return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (core pass)");
     // 3. core pass: Z = X_(t) V, V = leading kz columns of the complementary leaf's basis
     if (V16 && !c.dry()) {
@@ -1074,6 +1091,34 @@ ht_status_t error_core(Ctx &c, const Tree &T, const float *x32, const long *dims
     nb = error_fused_blocks(Rr, Cc) * batch;
     parts = c.ar.take<double>(static_cast<size_t>(nb) + 8);
     if (!Bkt || !core || !Tm || !Wm || !parts) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (error)");
+    c.stage = 4;
+    if (c.err_out && !c.ar.dry) {   // the batch's grouped error pass
+      ErrJob j;
+      j.Bt = B[P.t]; j.B0 = B[0]; j.t_is_left = P.t_is_left ? 1 : 0;
+      j.kpq = static_cast<long long>(P.kp) * P.kq; j.kt = P.kt; j.kc = P.kc;
+      j.core = core; j.Tm = Tm; j.Wm = Wm;
+      j.Up = U[P.p]; j.Uq = U[P.q];
+      j.np = static_cast<int>(np_); j.nq = static_cast<int>(nq_); j.kp = P.kp; j.kq = P.kq;
+      j.X = x32; j.R = Rr; j.Cn = Cc; j.kk = P.kc; j.slabs = batch;
+      if (P.mc == 2) {
+        j.ldx = Rr; j.sx = 0; j.A = Wm; j.lda = Rr; j.sa = 0; j.B = U[P.c]; j.ldb = nc_;
+      } else if (P.mc == 0) {
+        j.ldx = Rr; j.sx = 0; j.A = U[P.c]; j.lda = nc_; j.sa = 0; j.B = Wm; j.ldb = np_ * nq_;
+      } else {
+        j.ldx = np_; j.sx = np_ * nc_; j.A = Wm; j.lda = np_ * nq_; j.sa = np_; j.B = U[P.c]; j.ldb = nc_;
+      }
+      j.parts = parts; j.out = dev_out;
+      auto blocks = [](long long n, long long cap) {
+        return static_cast<int>(std::min<long long>(cap, std::max<long long>(1, (n + 255) / 256)));
+      };
+      j.nblk[0] = blocks(j.kpq * P.kc, 8);
+      j.nblk[1] = blocks(np_ * P.kq * P.kc, 16);
+      j.nblk[2] = blocks(np_ * nq_ * P.kc, 32);
+      j.ntile = nb;
+      j.nblk[3] = std::min(nb, 32);
+      for (int k = 0; k < 4; ++k) j.blk0[k] = 0;
+      c.err_out->push_back(j);
+    }
     if (!c.dry()) {
       if (P.t_is_left) HT_CUDA(cudaMemcpyAsync(Bkt, B[0], sizeof(float) * P.kt * P.kc, cudaMemcpyDeviceToDevice, c.st));
       else HT_CUDA(transpose_small_launch(B[0], P.kc, P.kt, Bkt, c.st));
@@ -1113,7 +1158,7 @@ ht_status_t error_core(Ctx &c, const Tree &T, const float *x32, const long *dims
       c.launches += 6;
     }
   }
-  if (!c.dry()) {
+  if (!c.dry()) {   // (stage 4 for 3rd order: part of the grouped error pass)
     HT_CUDA(sumsq_finish_launch(parts, nb, dev_out, c.st));
     ++c.launches;
   }
@@ -1415,7 +1460,7 @@ ht_status_t enqueue_body(Ctx &c, const Tree &T, const ht_config_t &cfg, const fl
       j.x = xd; j.xb = dst; j.partials = nparts; j.dsum = dsum;
       j.n1 = n1; j.n1p = pad; j.rest = total / n1;
       j.blk0 = 0;
-      j.nblk = static_cast<int>(std::min<long long>(1024, std::max<long long>(1, (pad * (total / n1)) / 4096)));
+      j.nblk = static_cast<int>(std::min<long long>(32, std::max<long long>(1, (pad * (total / n1)) / 16384)));
       c.conv_out->push_back(j);
     }
   };
@@ -1464,6 +1509,7 @@ ht_status_t enqueue_body(Ctx &c, const Tree &T, const ht_config_t &cfg, const fl
       HT_CUDA(cudaMemcpyAsync(dst, src, factor_count(T, a.dims, t) * sizeof(float), cudaMemcpyDefault, c.st));
     }
   }
+  c.stage = 3;
   if (a.want_err) HT_TRY(error_core(c, T, xd, a.dims, a.order, res.U, res.B, dsum + 1));
   return HT_OK;
 }
@@ -1605,6 +1651,7 @@ ht_status_t enqueue_pipelined(Ctx &c, const Tree &T, const ht_config_t &cfg, con
       HT_CUDA(cudaMemcpyAsync(dst, src, factor_count(T, a.dims, t) * sizeof(float), cudaMemcpyDefault, c.st));
     }
   }
+  c.stage = 3;
   if (a.want_err) HT_TRY(error_core(c, T, xd, a.dims, a.order, res.U, res.B, dsum + 1));
   return HT_OK;
 }
@@ -1739,7 +1786,9 @@ struct BatchState {
   cudaStream_t lane[kLanes] = {};
   cudaStream_t cap = nullptr;   // capture origin (the caller's stream may be the legacy stream)
   cudaEvent_t fork = nullptr, join[kLanes] = {}, t0 = nullptr, t1 = nullptr;
-  cudaEvent_t tp[2] = {};   // grouped mode: after the lanes' first phase, after the grouped solver
+  cudaEvent_t tp[5] = {};   // grouped mode: ends of the first five phases (ms_phase)
+  cudaStream_t side = nullptr;                    // grouped mode: the first half's tails and error pass
+  cudaEvent_t mid[kLanes] = {}, side_done = nullptr;
   bool grouped = false;
   double *sums = nullptr;   // device: [count][2] (||X||^2, ||X - Xhat||^2)
   int *errw = nullptr;      // device: one error word per lane
@@ -1752,6 +1801,12 @@ struct BatchState {
   size_t copies_bytes = 0;
   void *grams = nullptr;    // device: grouped Gram items, class 0 then class 1
   size_t grams_bytes = 0;
+  void *tails = nullptr;    // device: grouped transfer tails
+  size_t tails_bytes = 0;
+  void *errs = nullptr;     // device: grouped error passes
+  size_t errs_bytes = 0;
+  void *maps = nullptr;     // device: block -> job maps of the grouped conversion and error launches
+  size_t maps_bytes = 0;
 };
 
 // Workspace layout of one batch.  Per-lane mode: tensor i runs in lane
@@ -1766,6 +1821,12 @@ struct BatchLayout {
   int nprob = 0, iters = 0, refine = 0;
   int nconv = 0, conv_blocks = 0, ncopy = 0;   // grouped conversion jobs (their blocks), output copies
   int ngram[2] = {0, 0};                       // grouped Grams per class
+  // tensors [0, half) and [half, count): the first half's transfer tails and
+  // error pass overlap the second half's core passes
+  int half = 0;
+  int ntail_h[2] = {0, 0}, nerr_h[2] = {0, 0};   // jobs per half (tails, error passes)
+  int err_blocks[2][4] = {};                     // launch sizes of each half's error steps
+  size_t map_off[9] = {};                        // ints into BatchState::maps: conversion, then per half error steps 0-3
 };
 // Leaves of at most this size go through the grouped solver (one CTA each);
 // batches with larger modes keep the per-lane cooperative solver.
@@ -1791,26 +1852,50 @@ ht_status_t batch_streams(BatchState &b) {
   HT_CUDA(cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming));
   HT_CUDA(cudaEventCreate(&b.t0));
   HT_CUDA(cudaEventCreate(&b.t1));
-  HT_CUDA(cudaEventCreate(&b.tp[0]));
-  HT_CUDA(cudaEventCreate(&b.tp[1]));
+  for (int i = 0; i < 5; ++i) HT_CUDA(cudaEventCreate(&b.tp[i]));
+  HT_CUDA(cudaStreamCreateWithFlags(&b.side, cudaStreamNonBlocking));
+  for (int l = 0; l < kLanes; ++l) HT_CUDA(cudaEventCreateWithFlags(&b.mid[l], cudaEventDisableTiming));
+  HT_CUDA(cudaEventCreateWithFlags(&b.side_done, cudaEventDisableTiming));
   return HT_OK;
 }
 
+// Host-side tables of a grouped batch, filled by its plan pass.
+struct BatchPlanOut {
+  std::vector<unsigned char> table;          // grouped leaf solver problems
+  std::vector<ConvJob> conv;
+  std::vector<CopySeg> copies;
+  std::vector<unsigned char> grams[2];       // grouped Gram items by class
+  std::vector<TailJob> tails;
+  std::vector<ErrJob> errs;
+  int iters = 0, refine = 0;
+  size_t tails_at = 0, errs_at = 0;          // jobs of the tensors before the half point
+};
+
 // One pass over every tensor of the batch.  phase 0: the whole chain of each
-// tensor; 1: its launches up to the leaf Grams; 2: its launches after the leaf
-// solver; 3: no launches, the grouped solver's table is filled (host only).
-// Phases 0-2 run on the lanes, forked from and joined back into `st`.
+// tensor (per-lane mode); 1, 2, 3: the tensor's launches of stage 0 (up to the
+// leaf Grams), stage 1 (after the leaf solver) or stage 3 (the error pass);
+// 4: no launches, the grouped stages' tables are filled into *plan_out (host
+// only).  Phases 0-3 run on the lanes, forked from and joined back into `st`;
+// phase 2 also records b.mid[l] on every lane once the tensors before L.half
+// are enqueued.
 ht_status_t batch_pass(BatchState &b, const BatchLayout &L, int phase, cudaStream_t st, int count,
                        const float *const *x, const long *dims, int order, const std::vector<Tree> &trees,
                        const ht_config_t &cfg, float *const *U, float *const *B, bool want_err, int eig_ctas,
-                       std::vector<unsigned char> *table, int *iters_used, int *refine_used,
-                       std::vector<ConvJob> *conv = nullptr, std::vector<CopySeg> *copies = nullptr,
-                       std::vector<unsigned char> *grams = nullptr) {
-  if (phase != 3) {
+                       BatchPlanOut *plan_out = nullptr) {
+  const bool plan = phase == 4;
+  if (!plan) {
     HT_CUDA(cudaEventRecord(b.fork, st));
     for (int l = 0; l < b.lanes; ++l) HT_CUDA(cudaStreamWaitEvent(b.lane[l], b.fork, 0));
   }
   for (int i = 0; i < count; ++i) {
+    if (i == L.half && L.half > 0) {
+      if (plan) {
+        plan_out->tails_at = plan_out->tails.size();
+        plan_out->errs_at = plan_out->errs.size();
+      } else if (phase == 2) {
+        for (int l = 0; l < b.lanes; ++l) HT_CUDA(cudaEventRecord(b.mid[l], b.lane[l]));
+      }
+    }
     const int l = i % b.lanes;
     Ctx c;
     c.st = b.lane[l];
@@ -1820,16 +1905,17 @@ ht_status_t batch_pass(BatchState &b, const BatchLayout &L, int phase, cudaStrea
     if (L.grouped) {
       c.ar.base = static_cast<char *>(b.ws) + L.off[i];
       c.ar.cap = L.off[i + 1] - L.off[i];
-      c.eig_mode = phase == 3 ? 1 : 2;
-      c.eig_table = table;
-      c.mute_pre = phase == 2 || phase == 3;
-      c.mute_post = phase == 1 || phase == 3;
+      c.eig_mode = plan ? 1 : 2;
+      c.live = plan ? 0u : (phase == 1 ? 1u : (phase == 2 ? 2u : 8u));
       c.defer_io = true;
-      c.conv_out = conv;
-      c.copy_out = copies;
-      if (grams) {
-        c.gram_out[0] = &grams[0];
-        c.gram_out[1] = &grams[1];
+      if (plan) {
+        c.eig_table = &plan_out->table;
+        c.tail_out = &plan_out->tails;
+        c.err_out = &plan_out->errs;
+        c.conv_out = &plan_out->conv;
+        c.copy_out = &plan_out->copies;
+        c.gram_out[0] = &plan_out->grams[0];
+        c.gram_out[1] = &plan_out->grams[1];
       }
     } else {
       c.ar.base = static_cast<char *>(b.ws) + static_cast<size_t>(l) * L.lane_bytes;
@@ -1843,10 +1929,12 @@ ht_status_t batch_pass(BatchState &b, const BatchLayout &L, int phase, cudaStrea
     Result res;
     HT_TRY(enqueue_body(c, trees[i], cfg, x[i], a, nparts, b.sums + 2 * static_cast<size_t>(i), tl, res));
     b.launches += c.launches;
-    if (iters_used) *iters_used = c.eig_iters_used;
-    if (refine_used) *refine_used = c.eig_refine_used;
+    if (plan) {
+      plan_out->iters = c.eig_iters_used;
+      plan_out->refine = c.eig_refine_used;
+    }
   }
-  if (phase != 3) {
+  if (!plan) {
     for (int l = 0; l < b.lanes; ++l) {
       HT_CUDA(cudaEventRecord(b.join[l], b.lane[l]));
       HT_CUDA(cudaStreamWaitEvent(st, b.join[l], 0));
@@ -1855,32 +1943,58 @@ ht_status_t batch_pass(BatchState &b, const BatchLayout &L, int phase, cudaStrea
   return HT_OK;
 }
 
-// Enqueue the whole batch on `st`.  Grouped mode: the lanes run every
-// tensor's conversion and leaf Grams, ONE launch of the grouped leaf solver
-// covers every leaf of every tensor (its table uploaded beforehand by
-// batch_plan_grouped), then the lanes run the rest of every tensor.
+// The transfer tails and error passes of tensors [0, half) (h = 0) or
+// [half, count) (h = 1) on stream s.
+ht_status_t batch_tail_and_error(BatchState &b, const BatchLayout &L, int h, cudaStream_t s, bool record_mid) {
+  const int t0 = h == 0 ? 0 : L.ntail_h[0], e0 = h == 0 ? 0 : L.nerr_h[0];
+  HT_CUDA(transfer_tail_grouped_launch(static_cast<const TailJob *>(b.tails) + t0, L.ntail_h[h], s));
+  b.launches += L.ntail_h[h] > 0 ? 1 : 0;
+  if (record_mid) HT_CUDA(cudaEventRecordWithFlags(b.tp[3], s, cudaEventRecordExternal));
+  if (L.nerr_h[h] > 0) {
+    const int *maps = static_cast<const int *>(b.maps);
+    const int *emaps[4];
+    for (int k = 0; k < 4; ++k) emaps[k] = maps + L.map_off[1 + 4 * h + k];
+    HT_CUDA(error_grouped_launch(static_cast<const ErrJob *>(b.errs) + e0, L.nerr_h[h], L.err_blocks[h], emaps, s));
+    b.launches += 5;
+  }
+  return HT_OK;
+}
+
+// Enqueue the whole batch on `st`.  Grouped mode: one conversion launch, the
+// grouped Grams, one launch of the grouped leaf solver for every leaf of every
+// tensor (tables uploaded beforehand by batch_plan_grouped), the core passes
+// on the lanes, the grouped transfer tails and error passes -- the first
+// half's on a side stream, overlapping the second half's core passes -- and
+// one copy of every factor to the caller's buffers.
 ht_status_t batch_enqueue(BatchState &b, const BatchLayout &L, cudaStream_t st, int count, const float *const *x,
                           const long *dims, int order, const std::vector<Tree> &trees, const ht_config_t &cfg,
                           float *const *U, float *const *B, bool want_err, int eig_ctas) {
   HT_CUDA(cudaMemsetAsync(b.errw, 0, sizeof(int) * kLanes, st));
   b.launches = 0;
-  if (!L.grouped)
-    return batch_pass(b, L, 0, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas, nullptr, nullptr,
-                      nullptr);
-  HT_CUDA(convert_grouped_launch(static_cast<const ConvJob *>(b.conv), L.nconv, L.conv_blocks, st));
+  if (!L.grouped) return batch_pass(b, L, 0, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas);
+  const int *maps = static_cast<const int *>(b.maps);
+  HT_CUDA(convert_grouped_launch(static_cast<const ConvJob *>(b.conv), L.nconv, L.conv_blocks, maps + L.map_off[0], st));
   b.launches += L.nconv > 0 ? 2 : 0;
   HT_CUDA(tc_gram_grouped_launch(0, b.grams, L.ngram[0], st));
   HT_CUDA(tc_gram_grouped_launch(1, static_cast<char *>(b.grams) + tc_gram_item_bytes() * L.ngram[0], L.ngram[1], st));
   b.launches += (L.ngram[0] > 0) + (L.ngram[1] > 0);
-  HT_TRY(batch_pass(b, L, 1, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas, nullptr, nullptr,
-                    nullptr));
+  HT_TRY(batch_pass(b, L, 1, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas));
   // external records: inside a capture they become event-record nodes of the graph
   HT_CUDA(cudaEventRecordWithFlags(b.tp[0], st, cudaEventRecordExternal));
   HT_CUDA(eig_grouped_launch(b.table, L.nprob, L.iters, L.refine, st));
   HT_CUDA(cudaEventRecordWithFlags(b.tp[1], st, cudaEventRecordExternal));
   b.launches += 1;
-  HT_TRY(batch_pass(b, L, 2, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas, nullptr, nullptr,
-                    nullptr));
+  HT_TRY(batch_pass(b, L, 2, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas));
+  if (L.half > 0) {   // the first half, on the side stream, as soon as the lanes are past it
+    for (int l = 0; l < b.lanes; ++l) HT_CUDA(cudaStreamWaitEvent(b.side, b.mid[l], 0));
+    HT_TRY(batch_tail_and_error(b, L, 0, b.side, false));
+    HT_CUDA(cudaEventRecord(b.side_done, b.side));
+  }
+  HT_CUDA(cudaEventRecordWithFlags(b.tp[2], st, cudaEventRecordExternal));
+  HT_TRY(batch_tail_and_error(b, L, 1, st, true));
+  HT_TRY(batch_pass(b, L, 3, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas));
+  if (L.half > 0) HT_CUDA(cudaStreamWaitEvent(st, b.side_done, 0));
+  HT_CUDA(cudaEventRecordWithFlags(b.tp[4], st, cudaEventRecordExternal));
   HT_CUDA(copy_segments_launch(static_cast<const CopySeg *>(b.copies), L.ncopy, st));
   b.launches += L.ncopy > 0 ? 1 : 0;
   return HT_OK;
@@ -1904,34 +2018,54 @@ ht_status_t upload_table(void *&buf, size_t &cap, const void *data, size_t bytes
 ht_status_t batch_plan_grouped(BatchState &b, BatchLayout &L, int count, const float *const *x, const long *dims,
                                int order, const std::vector<Tree> &trees, const ht_config_t &cfg, float *const *U,
                                float *const *B, bool want_err) {
-  std::vector<unsigned char> table;
-  std::vector<ConvJob> conv;
-  std::vector<CopySeg> copies;
-  std::vector<unsigned char> grams[2];
-  int iters = 0, refine = 0;
+  BatchPlanOut P;
   const int launches = b.launches;
-  HT_TRY(batch_pass(b, L, 3, nullptr, count, x, dims, order, trees, cfg, U, B, want_err, 0, &table, &iters, &refine,
-                    &conv, &copies, grams));
-  L.ngram[0] = static_cast<int>(grams[0].size() / tc_gram_item_bytes());
-  L.ngram[1] = static_cast<int>(grams[1].size() / tc_gram_item_bytes());
-  grams[0].insert(grams[0].end(), grams[1].begin(), grams[1].end());
-  HT_TRY(upload_table(b.grams, b.grams_bytes, grams[0].data(), grams[0].size()));
+  HT_TRY(batch_pass(b, L, 4, nullptr, count, x, dims, order, trees, cfg, U, B, want_err, 0, &P));
   b.launches = launches;
-  eig_grouped_order(table);
-  L.nprob = static_cast<int>(table.size() / eig_grouped_entry_bytes());
-  L.iters = iters;
-  L.refine = refine;
+  if (L.half <= 0) P.tails_at = P.errs_at = 0;
+  // block -> job maps: the conversion, then each half's four error steps
+  // (job indices relative to the half's first job)
+  std::vector<int> maps;
   int blk = 0;
-  for (ConvJob &j : conv) {
-    j.blk0 = blk;
-    blk += j.nblk;
+  for (size_t j = 0; j < P.conv.size(); ++j) {
+    P.conv[j].blk0 = blk;
+    blk += P.conv[j].nblk;
+    maps.insert(maps.end(), P.conv[j].nblk, static_cast<int>(j));
   }
-  L.nconv = static_cast<int>(conv.size());
+  L.map_off[0] = 0;
+  L.nconv = static_cast<int>(P.conv.size());
   L.conv_blocks = blk;
-  L.ncopy = static_cast<int>(copies.size());
-  HT_TRY(upload_table(b.table, b.table_bytes, table.data(), table.size()));
-  HT_TRY(upload_table(b.conv, b.conv_bytes, conv.data(), sizeof(ConvJob) * conv.size()));
-  HT_TRY(upload_table(b.copies, b.copies_bytes, copies.data(), sizeof(CopySeg) * copies.size()));
+  const size_t ebeg[2] = {0, P.errs_at}, eend[2] = {P.errs_at, P.errs.size()};
+  for (int h = 0; h < 2; ++h) {
+    L.nerr_h[h] = static_cast<int>(eend[h] - ebeg[h]);
+    for (int k = 0; k < 4; ++k) {
+      L.map_off[1 + 4 * h + k] = maps.size();
+      int eb = 0;
+      for (size_t i = ebeg[h]; i < eend[h]; ++i) {
+        P.errs[i].blk0[k] = eb;
+        eb += P.errs[i].nblk[k];
+        maps.insert(maps.end(), P.errs[i].nblk[k], static_cast<int>(i - ebeg[h]));
+      }
+      L.err_blocks[h][k] = eb;
+    }
+  }
+  L.ntail_h[0] = static_cast<int>(P.tails_at);
+  L.ntail_h[1] = static_cast<int>(P.tails.size() - P.tails_at);
+  L.ngram[0] = static_cast<int>(P.grams[0].size() / tc_gram_item_bytes());
+  L.ngram[1] = static_cast<int>(P.grams[1].size() / tc_gram_item_bytes());
+  P.grams[0].insert(P.grams[0].end(), P.grams[1].begin(), P.grams[1].end());
+  eig_grouped_order(P.table);
+  L.nprob = static_cast<int>(P.table.size() / eig_grouped_entry_bytes());
+  L.iters = P.iters;
+  L.refine = P.refine;
+  L.ncopy = static_cast<int>(P.copies.size());
+  HT_TRY(upload_table(b.maps, b.maps_bytes, maps.data(), sizeof(int) * maps.size()));
+  HT_TRY(upload_table(b.errs, b.errs_bytes, P.errs.data(), sizeof(ErrJob) * P.errs.size()));
+  HT_TRY(upload_table(b.tails, b.tails_bytes, P.tails.data(), sizeof(TailJob) * P.tails.size()));
+  HT_TRY(upload_table(b.grams, b.grams_bytes, P.grams[0].data(), P.grams[0].size()));
+  HT_TRY(upload_table(b.table, b.table_bytes, P.table.data(), P.table.size()));
+  HT_TRY(upload_table(b.conv, b.conv_bytes, P.conv.data(), sizeof(ConvJob) * P.conv.size()));
+  HT_TRY(upload_table(b.copies, b.copies_bytes, P.copies.data(), sizeof(CopySeg) * P.copies.size()));
   return HT_OK;
 }
 
@@ -2274,6 +2408,7 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
     for (int i = 0; i < count; ++i)
       for (int m = 0; m < order; ++m) L.grouped = L.grouped && dims[static_cast<size_t>(i) * order + m] <= kGroupedMaxN;
     L.off.assign(static_cast<size_t>(count) + 1, 0);
+    L.half = count >= 4 ? count / 2 : 0;
     for (int i = 0; i < count; ++i) {
       const long *di = dims + static_cast<size_t>(i) * order;
       HT_TRY(parse_tree(&trees[i], di, order, T[i]));
@@ -2390,12 +2525,14 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
     report->graph_replayed = replay ? 1 : 0;
     report->lanes = b.lanes;
     report->grouped = b.grouped ? 1 : 0;
-    if (b.grouped &&
-        (cudaEventElapsedTime(&report->ms_phase[0], b.t0, b.tp[0]) != cudaSuccess ||
-         cudaEventElapsedTime(&report->ms_phase[1], b.tp[0], b.tp[1]) != cudaSuccess ||
-         cudaEventElapsedTime(&report->ms_phase[2], b.tp[1], b.t1) != cudaSuccess)) {
-      cudaGetLastError();   // timing unavailable: report zeros, leave no error behind
-      report->ms_phase[0] = report->ms_phase[1] = report->ms_phase[2] = 0.f;
+    if (b.grouped) {
+      const cudaEvent_t ev[7] = {b.t0, b.tp[0], b.tp[1], b.tp[2], b.tp[3], b.tp[4], b.t1};
+      for (int i = 0; i < 6; ++i)
+        if (cudaEventElapsedTime(&report->ms_phase[i], ev[i], ev[i + 1]) != cudaSuccess) {
+          cudaGetLastError();   // timing unavailable: report zeros, leave no error behind
+          for (int j = 0; j < 6; ++j) report->ms_phase[j] = 0.f;
+          break;
+        }
     }
   }
   return HT_OK;
@@ -2438,6 +2575,15 @@ ht_status_t ht_release_batch(void) {
   if (b.grams) HT_CUDA(cudaFree(b.grams));
   b.grams = nullptr;
   b.grams_bytes = 0;
+  if (b.tails) HT_CUDA(cudaFree(b.tails));
+  b.tails = nullptr;
+  b.tails_bytes = 0;
+  if (b.errs) HT_CUDA(cudaFree(b.errs));
+  b.errs = nullptr;
+  b.errs_bytes = 0;
+  if (b.maps) HT_CUDA(cudaFree(b.maps));
+  b.maps = nullptr;
+  b.maps_bytes = 0;
   return HT_OK;
 }
 

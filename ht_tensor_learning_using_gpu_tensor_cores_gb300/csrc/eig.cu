@@ -284,14 +284,13 @@ HT_DEV void jacobi_smem(float (*A)[SMAX + 1], float (*A2)[SMAX + 1], float (*V)[
 // (u < min(kt, kc)) V^T G_c U_c = GV[:, u], so Broot = diag(lam^1/2) P^T there:
 // writing it that way makes B_t Broot = C_V P P^T exactly, instead of relying on
 // lam^-1 * lam cancelling in FP32, which fails for ill-conditioned Grams.
-__global__ void __launch_bounds__(256) transfer_eig_kernel(const float *WG, int kw, int kt, int kc, int t_is_left,
-                                                           float *M, float *Broot) {
-  __shared__ float A[SMAX][SMAX + 1];
-  __shared__ float V[SMAX][SMAX + 1];
-  extern __shared__ float jac_scratch[];   // SMAX * (SMAX + 1) floats
-  float (*A2)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(jac_scratch);
-  __shared__ int order[SMAX];
-  __shared__ float inv[SMAX];
+// Transfer-tensor eigen step on WG (kw x kw, leading dimension kw, global or
+// shared memory): the top-kt eigenpairs of sym(WG[:kt, :kt]) by Jacobi give
+// M (kt x kt) = V diag(lambda^-1/2) and the root transfer tensor
+// Broot (kt x kc, or kc x kt when !t_is_left).
+HT_DEV void transfer_eig_body(const float *WG, int kw, int kt, int kc, int t_is_left, float *M, float *Broot,
+                              float (*A)[SMAX + 1], float (*V)[SMAX + 1], float (*A2)[SMAX + 1], int *order,
+                              float *inv) {
   const int t = threadIdx.x;
   for (int e = t; e < SMAX * SMAX; e += 256) {
     const int i = e % SMAX, j = e / SMAX;
@@ -324,6 +323,60 @@ __global__ void __launch_bounds__(256) transfer_eig_kernel(const float *WG, int 
     }
     if (t_is_left) Broot[r + kt * u] = acc;
     else Broot[u + kc * r] = acc;
+  }
+}
+
+__global__ void __launch_bounds__(256) transfer_eig_kernel(const float *WG, int kw, int kt, int kc, int t_is_left,
+                                                           float *M, float *Broot) {
+  __shared__ float A[SMAX][SMAX + 1];
+  __shared__ float V[SMAX][SMAX + 1];
+  extern __shared__ float jac_scratch[];   // SMAX * (SMAX + 1) floats
+  float (*A2)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(jac_scratch);
+  __shared__ int order[SMAX];
+  __shared__ float inv[SMAX];
+  transfer_eig_body(WG, kw, kt, kc, t_is_left, M, Broot, A, V, A2, order, inv);
+}
+
+// Grouped transfer tail of the batched path, a CTA per tensor:
+//   WG = U^T GU (kw x kw, compensated dot products as gemm_tn_small),
+//   the transfer eigen step (M, Bkt; Broot = Bkt^T when t is the right child),
+//   Bt = C M (kpq x kt, as matmul_nn).
+__global__ void __launch_bounds__(256) transfer_tail_grouped_kernel(const TailJob *__restrict__ jobs) {
+  __shared__ float A[SMAX][SMAX + 1];
+  __shared__ float V[SMAX][SMAX + 1];
+  extern __shared__ float tail_sm[];   // A2 (SMAX * (SMAX + 1)), WG (SMAX * SMAX), M (SMAX * SMAX)
+  float (*A2)[SMAX + 1] = reinterpret_cast<float (*)[SMAX + 1]>(tail_sm);
+  float *WG = tail_sm + SMAX * (SMAX + 1);
+  float *Ms = WG + SMAX * SMAX;
+  __shared__ int order[SMAX];
+  __shared__ float inv[SMAX];
+  __shared__ TailJob J;
+  if (threadIdx.x == 0) J = jobs[blockIdx.x];
+  __syncthreads();
+  const int kw = J.kw, kt = J.kt, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int e = warp; e < kw * kw; e += 8) {
+    const int i = e % kw, j = e / kw;
+    Acc2 acc = {0.f, 0.f};
+    for (int k = lane; k < J.nc; k += 32)
+      acc2_add_prod(acc, J.U[k + static_cast<long long>(J.nc) * i], J.GU[k + static_cast<long long>(J.nc) * j]);
+    double v = static_cast<double>(acc.s) + static_cast<double>(acc.c);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) WG[i + kw * j] = static_cast<float>(v);
+  }
+  __syncthreads();
+  transfer_eig_body(WG, kw, kt, J.kc, 1, Ms, J.Bkt, A, V, A2, order, inv);
+  __syncthreads();
+  for (int e = threadIdx.x; e < kt * J.kc && !J.t_is_left; e += 256) {
+    const int i = e % kt, j = e / kt;
+    J.Broot[j + J.kc * i] = J.Bkt[i + kt * j];
+  }
+  for (long long idx = threadIdx.x; idx < J.kpq * kt; idx += 256) {
+    const long long i = idx % J.kpq;
+    const int j = static_cast<int>(idx / J.kpq);
+    float sacc = 0.f;
+    for (int k = 0; k < kt; ++k) sacc = fmaf(J.C[i + J.kpq * k], Ms[k + kt * j], sacc);
+    J.Bt[i + J.kpq * j] = sacc;
   }
 }
 
@@ -1539,6 +1592,17 @@ cudaError_t svd_from_gram_launch(const float *GW, int s, int k1, int k2, float *
                                  cudaStream_t st) {
   SvdGramProb q{GW, s, k1, k2, M1, M2, Broot};
   return svd_from_gram_batched_launch(&q, 1, st);
+}
+
+cudaError_t transfer_tail_grouped_launch(const TailJob *jobs_dev, int njobs, cudaStream_t st) {
+  if (njobs < 1) return cudaSuccess;
+  if (!jobs_dev) return cudaErrorInvalidValue;
+  constexpr size_t kSmem = sizeof(float) * (SMAX * (SMAX + 1) + 2 * SMAX * SMAX);
+  static bool attr_set[64] = {};
+  const cudaError_t e = opt_in_smem(transfer_tail_grouped_kernel, static_cast<int>(kSmem), attr_set);
+  if (e != cudaSuccess) return e;
+  transfer_tail_grouped_kernel<<<njobs, 256, kSmem, st>>>(jobs_dev);
+  return cudaGetLastError();
 }
 
 cudaError_t transfer_eig_launch(const float *WG, int kw, int kt, int kc, int t_is_left, float *M, float *Broot,

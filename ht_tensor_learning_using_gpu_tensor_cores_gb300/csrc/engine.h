@@ -148,8 +148,9 @@ cudaError_t sumsq_finish_launch(const double *partials, int n, double *out, cuda
 // Grouped conversion of a batch (one launch for every tensor, then one finish
 // launch): job j converts x (n1 x rest, FP32) to xb (n1p x rest BF16, rows
 // zero-padded; null: sums only) in blocks [blk0, blk0 + nblk) of the launch
-// (jobs in ascending blk0, nblk <= the capacity of partials) and leaves
-// ||x||^2 in dsum[0].  The job table lives in device memory.
+// (nblk <= the capacity of partials; job_of_block, in device memory, maps each
+// block of the launch to its job) and leaves ||x||^2 in dsum[0].  The job
+// table lives in device memory.
 struct ConvJob {
   const float *x;
   __nv_bfloat16 *xb;
@@ -157,7 +158,27 @@ struct ConvJob {
   long long n1, n1p, rest;
   int blk0, nblk;
 };
-cudaError_t convert_grouped_launch(const ConvJob *jobs_dev, int njobs, int total_blocks, cudaStream_t s);
+// Grouped error pass of the batched path (3rd order): five launches for every
+// job -- core = Bt Bkt, the two expansion steps into Tm and Wm, the fused
+// error tiles (as error_fused_launch, ntile = tiles x slabs of X) into parts,
+// and their sum into out[0].  blk0[k] / nblk[k]: the job's blocks in launch k
+// (grid-stride within the job); blocks[k] = the launch sizes and
+// job_of_block[k] (device) the job of each block of launch k.  Job table in
+// device memory.
+struct ErrJob {
+  const float *Bt, *B0;        // B_t (kpq x kt); B0 = Bkt (kt x kc) or its transpose
+  float *core, *Tm, *Wm;
+  const float *Up, *Uq;        // leaves p (np x kp) and q (nq x kq)
+  const float *X, *A, *B;      // error tiles: X (R x Cn per slab) against A B^T
+  double *parts, *out;
+  long long kpq, ldx, sx, lda, sa, ldb, R, Cn;
+  int kt, kc, t_is_left, np, nq, kp, kq, kk, slabs, ntile;
+  int blk0[4], nblk[4];
+};
+cudaError_t error_grouped_launch(const ErrJob *jobs_dev, int njobs, const int *blocks, const int *const *job_of_block,
+                                 cudaStream_t s);
+cudaError_t convert_grouped_launch(const ConvJob *jobs_dev, int njobs, int total_blocks, const int *job_of_block,
+                                   cudaStream_t s);
 // dst[0, count) = src[0, count) for every segment, one launch (table in device memory).
 struct CopySeg {
   const float *src;
@@ -232,6 +253,17 @@ cudaError_t cholqr_batched(EigProblem *probs, int nprob, int passes, void *ws, s
 // whose barrier expects ctas + 1 members; every CTA gives up after limit_ns
 // (<= the library's 2 s wait limit) and sets kErrTimeout in *err.  ws: 16 bytes.
 cudaError_t wait_probe_launch(int ctas, uint64_t limit_ns, void *ws, int *err, cudaStream_t st);
+// Grouped transfer tail of the batched path (3rd order), a CTA per tensor:
+// WG = U^T GU, the transfer eigen step into M and Bkt (Broot = Bkt^T when
+// !t_is_left), Bt = C M.  kw, kt <= 64.  Job table in device memory.
+struct TailJob {
+  const float *U, *GU;   // complementary leaf: basis and G U, nc x kw
+  const float *C;        // kpq x kt core product
+  float *M, *Bkt, *Broot, *Bt;
+  long long kpq;
+  int nc, kw, kt, kc, t_is_left;
+};
+cudaError_t transfer_tail_grouped_launch(const TailJob *jobs_dev, int njobs, cudaStream_t st);
 // Transfer-tensor eigen step (see eig.cu).  WG: kw x kw.  M: kt x kt, Bkt: kt x kc.
 cudaError_t transfer_eig_launch(const float *WG, int kw, int kt, int kc, int t_is_left, float *M, float *Broot,
                                 cudaStream_t st);

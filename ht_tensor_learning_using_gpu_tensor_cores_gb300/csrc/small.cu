@@ -154,18 +154,19 @@ __global__ void sumsq_kernel(const float *__restrict__ x, long long n, double *p
 // rows padded with zeros; xb null: sums only), writing one compensated
 // partial sum of squares per block; the finish kernel (a block per job) sums
 // a job's partials in block order into its dsum[0].
-__global__ void __launch_bounds__(256) convert_grouped_kernel(const ConvJob *__restrict__ jobs, int njobs) {
-  __shared__ ConvJob J;
-  if (threadIdx.x == 0) {
-    int lo = 0, hi = njobs - 1;   // last job with blk0 <= blockIdx.x
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (jobs[mid].blk0 <= static_cast<int>(blockIdx.x)) lo = mid;
-      else hi = mid - 1;
-    }
-    J = jobs[lo];
-  }
+// Job j of a grouped launch into shared memory, one 4-byte word per thread.
+template <class Job>
+HT_DEV void load_job(const Job *__restrict__ jobs, int j, Job &J) {
+  static_assert(sizeof(Job) % 4 == 0 && sizeof(Job) <= 4 * 256, "job table entries are copied word by word");
+  if (threadIdx.x < sizeof(Job) / 4)
+    reinterpret_cast<uint32_t *>(&J)[threadIdx.x] = reinterpret_cast<const uint32_t *>(jobs + j)[threadIdx.x];
   __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) convert_grouped_kernel(const ConvJob *__restrict__ jobs,
+                                                              const int *__restrict__ job_of_block) {
+  __shared__ ConvJob J;
+  load_job(jobs, job_of_block[blockIdx.x], J);
   const int b = blockIdx.x - J.blk0;
   Acc2 a = {0.f, 0.f};
   const long long total = J.n1p * J.rest;
@@ -315,10 +316,10 @@ __global__ void sum_parts_kernel(const float *__restrict__ part, int nparts, lon
 
 // W[i0 + n0*i1, c] = sum_{a,b} U0[i0,a] U1[i1,b] core[a + k0*b + k0*k1*c]
 // step 1: T[i0, b, c] = sum_a U0[i0,a] core[a,b,c]
-__global__ void expand_step1_kernel(const float *__restrict__ U0, int n0, int k0, const float *__restrict__ core,
-                                    int k1, int k2, float *__restrict__ T) {
+HT_DEV void expand_step1_body(const float *__restrict__ U0, int n0, int k0, const float *__restrict__ core, int k1,
+                              int k2, float *__restrict__ T, long long blk, long long nblk) {
   const long long total = static_cast<long long>(n0) * k1 * k2;
-  for (long long idx = blockIdx.x * 256ll + threadIdx.x; idx < total; idx += gridDim.x * 256ll) {
+  for (long long idx = blk * 256ll + threadIdx.x; idx < total; idx += nblk * 256ll) {
     const int i0 = static_cast<int>(idx % n0);
     const long long bc = idx / n0;   // b + k1*c
     float s = 0.f;
@@ -326,11 +327,15 @@ __global__ void expand_step1_kernel(const float *__restrict__ U0, int n0, int k0
     T[idx] = s;
   }
 }
+__global__ void expand_step1_kernel(const float *__restrict__ U0, int n0, int k0, const float *__restrict__ core,
+                                    int k1, int k2, float *__restrict__ T) {
+  expand_step1_body(U0, n0, k0, core, k1, k2, T, blockIdx.x, gridDim.x);
+}
 // step 2: W[i0 + n0*i1 + n0*n1*c] = sum_b T[i0 + n0*(b + k1*c)] U1[i1 + n1*b]
-__global__ void expand_step2_kernel(const float *__restrict__ T, int n0, int k1, const float *__restrict__ U1, int n1,
-                                    int k2, float *__restrict__ W) {
+HT_DEV void expand_step2_body(const float *__restrict__ T, int n0, int k1, const float *__restrict__ U1, int n1, int k2,
+                              float *__restrict__ W, long long blk, long long nblk) {
   const long long total = static_cast<long long>(n0) * n1 * k2;
-  for (long long idx = blockIdx.x * 256ll + threadIdx.x; idx < total; idx += gridDim.x * 256ll) {
+  for (long long idx = blk * 256ll + threadIdx.x; idx < total; idx += nblk * 256ll) {
     const int i0 = static_cast<int>(idx % n0);
     const long long r = idx / n0;
     const int i1 = static_cast<int>(r % n1);
@@ -340,6 +345,10 @@ __global__ void expand_step2_kernel(const float *__restrict__ T, int n0, int k1,
       s = fmaf(T[i0 + static_cast<long long>(n0) * (b + static_cast<long long>(k1) * c)], U1[i1 + static_cast<long long>(n1) * b], s);
     W[idx] = s;
   }
+}
+__global__ void expand_step2_kernel(const float *__restrict__ T, int n0, int k1, const float *__restrict__ U1, int n1,
+                                    int k2, float *__restrict__ W) {
+  expand_step2_body(T, n0, k1, U1, n1, k2, W, blockIdx.x, gridDim.x);
 }
 
 // C (m x n) = A (m x K) * B (K x n), column-major, small K and n
@@ -358,17 +367,18 @@ __global__ void matmul_nn_kernel(const float *__restrict__ A, long long lda, con
 // err partial over a 128 x 64 tile: sum (X[r + R*c] - sum_k A[r + R*k] B[c + Cn*k])^2.
 // Thread layout: 32 row groups of 4 rows x 8 column groups of 8 columns, so a
 // warp reads 128 consecutive rows of one column of X.
-__global__ void __launch_bounds__(256) error_fused_kernel(const float *__restrict__ X, long long ldx, long long sx,
-                                                          const float *__restrict__ A, long long lda, long long sa,
-                                                          const float *__restrict__ B, long long ldb, long long R,
-                                                          long long Cn, int kk, double *partials) {
-  X += sx * blockIdx.y;
-  A += sa * blockIdx.y;
+// Tile `tile` of slab `y` (X and A advanced by sx, sa per slab); the tile's
+// partial goes to partials[tile + ntiles * y].
+HT_DEV void error_fused_body(const float *__restrict__ X, long long ldx, long long sx, const float *__restrict__ A,
+                             long long lda, long long sa, const float *__restrict__ B, long long ldb, long long R,
+                             long long Cn, int kk, double *partials, long long tile, long long ntiles, long long y) {
+  X += sx * y;
+  A += sa * y;
   __shared__ __align__(16) float As[32][128];
   __shared__ float Bs[32][64];
   __shared__ double red[256];
   const long long tiles_r = (R + 127) / 128;
-  const long long tr = blockIdx.x % tiles_r, tc = blockIdx.x / tiles_r;
+  const long long tr = tile % tiles_r, tc = tile / tiles_r;
   const long long r0 = tr * 128, c0 = tc * 64;
   const int t = threadIdx.x;
   const int rg = t % 32, cg = t / 32;
@@ -388,8 +398,9 @@ __global__ void __launch_bounds__(256) error_fused_kernel(const float *__restric
       Bs[k][cc] = (k0 + k < kk && c0 + cc < Cn) ? B[c0 + cc + ldb * (k0 + k)] : 0.f;
     }
     __syncthreads();
+    const int kn = kk - k0 < 32 ? kk - k0 : 32;   // no products with the zero-padded k slices
 #pragma unroll 4
-    for (int k = 0; k < 32; ++k) {
+    for (int k = 0; k < kn; ++k) {
       const float4 a4 = *reinterpret_cast<const float4 *>(&As[k][rg * 4]);
       const float a[4] = {a4.x, a4.y, a4.z, a4.w};
 #pragma unroll
@@ -419,7 +430,69 @@ __global__ void __launch_bounds__(256) error_fused_kernel(const float *__restric
     if (t < w) red[t] += red[t + w];
     __syncthreads();
   }
-  if (t == 0) partials[blockIdx.x + static_cast<long long>(gridDim.x) * blockIdx.y] = red[0];
+  if (t == 0) partials[tile + ntiles * y] = red[0];
+}
+
+__global__ void __launch_bounds__(256) error_fused_kernel(const float *__restrict__ X, long long ldx, long long sx,
+                                                          const float *__restrict__ A, long long lda, long long sa,
+                                                          const float *__restrict__ B, long long ldb, long long R,
+                                                          long long Cn, int kk, double *partials) {
+  error_fused_body(X, ldx, sx, A, lda, sa, B, ldb, R, Cn, kk, partials, blockIdx.x, gridDim.x, blockIdx.y);
+}
+
+// Grouped error pass of the batched path (3rd order), one launch per step
+// for every job; job_of_block[step] maps a block of launch `step` to its job.
+
+// step 0: core (kpq x kc) = Bt (kpq x kt) Bkt (kt x kc); Bkt is B0 itself when
+// t is the root's left child, else B0 is its transpose (kc x kt)
+__global__ void __launch_bounds__(256) err_core_grouped_kernel(const ErrJob *__restrict__ jobs, const int *__restrict__ job_of_block) {
+  __shared__ ErrJob J;
+  load_job(jobs, job_of_block[blockIdx.x], J);
+  const long long b = blockIdx.x - J.blk0[0], total = J.kpq * J.kc;
+  for (long long idx = b * 256 + threadIdx.x; idx < total; idx += J.nblk[0] * 256ll) {
+    const long long i = idx % J.kpq;
+    const int u = static_cast<int>(idx / J.kpq);
+    float s = 0.f;
+    for (int r = 0; r < J.kt; ++r)
+      s = fmaf(J.Bt[i + J.kpq * r], J.t_is_left ? J.B0[r + J.kt * u] : J.B0[u + J.kc * r], s);
+    J.core[idx] = s;
+  }
+}
+
+__global__ void __launch_bounds__(256) err_expand1_grouped_kernel(const ErrJob *__restrict__ jobs, const int *__restrict__ job_of_block) {
+  __shared__ ErrJob J;
+  load_job(jobs, job_of_block[blockIdx.x], J);
+  expand_step1_body(J.Up, J.np, J.kp, J.core, J.kq, J.kc, J.Tm, blockIdx.x - J.blk0[1], J.nblk[1]);
+}
+
+__global__ void __launch_bounds__(256) err_expand2_grouped_kernel(const ErrJob *__restrict__ jobs, const int *__restrict__ job_of_block) {
+  __shared__ ErrJob J;
+  load_job(jobs, job_of_block[blockIdx.x], J);
+  expand_step2_body(J.Tm, J.np, J.kq, J.Uq, J.nq, J.kc, J.Wm, blockIdx.x - J.blk0[2], J.nblk[2]);
+}
+
+__global__ void __launch_bounds__(256) err_fused_grouped_kernel(const ErrJob *__restrict__ jobs, const int *__restrict__ job_of_block) {
+  __shared__ ErrJob J;
+  load_job(jobs, job_of_block[blockIdx.x], J);
+  const long long ntiles = J.ntile / J.slabs;
+  for (long long tb = blockIdx.x - J.blk0[3]; tb < J.ntile; tb += J.nblk[3])
+    error_fused_body(J.X, J.ldx, J.sx, J.A, J.lda, J.sa, J.B, J.ldb, J.R, J.Cn, J.kk, J.parts, tb % ntiles, ntiles,
+                     tb / ntiles);
+}
+
+// the sum of a job's tile partials, as sumsq_finish_kernel sums them
+__global__ void err_finish_grouped_kernel(const ErrJob *__restrict__ jobs) {
+  const ErrJob &J = jobs[blockIdx.x];
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < J.ntile; i += 256) s += J.parts[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) J.out[0] = red[0];
 }
 
 __global__ void gaussian_fill_kernel(float *dst, long long n, unsigned long long seed, unsigned long long stream) {
@@ -521,10 +594,11 @@ cudaError_t split_bf16_launch(const float *W, long long rows, int k, int h, __nv
   return cudaGetLastError();
 }
 
-cudaError_t convert_grouped_launch(const ConvJob *jobs_dev, int njobs, int total_blocks, cudaStream_t s) {
+cudaError_t convert_grouped_launch(const ConvJob *jobs_dev, int njobs, int total_blocks, const int *job_of_block,
+                                   cudaStream_t s) {
   if (njobs < 1) return cudaSuccess;
-  if (!jobs_dev || total_blocks < njobs) return cudaErrorInvalidValue;
-  convert_grouped_kernel<<<total_blocks, 256, 0, s>>>(jobs_dev, njobs);
+  if (!jobs_dev || !job_of_block || total_blocks < njobs) return cudaErrorInvalidValue;
+  convert_grouped_kernel<<<total_blocks, 256, 0, s>>>(jobs_dev, job_of_block);
   convert_grouped_finish_kernel<<<njobs, 256, 0, s>>>(jobs_dev);
   return cudaGetLastError();
 }
@@ -595,6 +669,20 @@ cudaError_t error_fused_launch(const float *X, long long ldx, long long sx, cons
   if (kk > 64 || batch < 1 || batch > 65535) return cudaErrorInvalidValue;
   error_fused_kernel<<<dim3(error_fused_blocks(R, Cn), batch), 256, 0, s>>>(X, ldx, sx, A, lda, sa, B, ldb, R, Cn, kk,
                                                                            partials);
+  return cudaGetLastError();
+}
+
+cudaError_t error_grouped_launch(const ErrJob *jobs_dev, int njobs, const int *blocks, const int *const *job_of_block,
+                                 cudaStream_t s) {
+  if (njobs < 1) return cudaSuccess;
+  if (!jobs_dev) return cudaErrorInvalidValue;
+  for (int k = 0; k < 4; ++k)
+    if (blocks[k] < njobs || !job_of_block[k]) return cudaErrorInvalidValue;
+  err_core_grouped_kernel<<<blocks[0], 256, 0, s>>>(jobs_dev, job_of_block[0]);
+  err_expand1_grouped_kernel<<<blocks[1], 256, 0, s>>>(jobs_dev, job_of_block[1]);
+  err_expand2_grouped_kernel<<<blocks[2], 256, 0, s>>>(jobs_dev, job_of_block[2]);
+  err_fused_grouped_kernel<<<blocks[3], 256, 0, s>>>(jobs_dev, job_of_block[3]);
+  err_finish_grouped_kernel<<<njobs, 256, 0, s>>>(jobs_dev);
   return cudaGetLastError();
 }
 

@@ -257,8 +257,10 @@ typedef struct {
     int graph_replayed;      /* 1 when the cached CUDA graph of an identical batch ran       */
     int lanes;               /* concurrent streams the batch was spread over                 */
     int grouped;             /* 1: every leaf eigen-problem ran in one grouped launch        */
-    float ms_phase[3];       /* grouped: device ms of the lanes up to the leaf Grams, of the
-                                grouped leaf solver, of the lanes after it (else 0)           */
+    float ms_phase[6];       /* grouped: device ms of (0) conversion and leaf Grams, (1) the
+                                grouped leaf solver, (2) the lanes after it (core pass),
+                                (3) the grouped transfer tails, (4) the error pass, (5) the
+                                copies to the caller's buffers (else 0)                       */
 } ht_batch_report_t;
 
 /* Decompose `count` tensors of the same order in one call.  Replaces the

@@ -67,7 +67,7 @@ def test_graph_replay_same_and_new_contents(family):
     r2, rep2 = bd(xs)
     assert rep2["graph_replayed"], "identical second call must replay the recorded graph"
     # small modes: every leaf in one grouped solver launch, timed inside the graph
-    assert rep2["grouped"] and min(rep2["ms_phase"].values()) > 0, rep2
+    assert rep2["grouped"] and min(rep2["ms_phase"].values()) >= 0 and rep2["ms_phase"]["leaf_solver"] > 0, rep2
     assert sum(rep2["ms_phase"].values()) <= rep2["ms_total"] * 1.01 + 0.05
     for a, r in zip(U1, r2):
         for t in a:
