@@ -215,6 +215,16 @@ struct Ctx {
   unsigned live = ~0u;
   std::vector<TailJob> *tail_out = nullptr;   // grouped transfer tails (3rd order)
   std::vector<ErrJob> *err_out = nullptr;     // grouped error passes (3rd order, stage 4)
+  // grouped 3rd-order core pass: the mode product (group 0) and the first
+  // core contraction (group 1) as grouped FP32 GEMM tiles, the second
+  // contraction as a grouped step; set by enqueue_body for a grouped batch
+  bool core_grouped = false;
+  int core_seq = 0;
+  std::vector<SParamsBlob> *core_gemms = nullptr;
+  std::vector<SimtBlockBlob> *core_blocks[2] = {nullptr, nullptr};
+  std::vector<Step2Job> *step2_out = nullptr;
+  std::vector<NarrowJob> *narrow_out = nullptr;   // mode products with contiguous rows of X
+  std::vector<T1Job> *t1_out = nullptr;           // first core contractions
   // Batched path: the tensor's conversion (with its ||X||^2) and the copies of
   // its factors to the caller's buffers are left to one grouped launch each
   // (defer_io), described into conv_out / copy_out when those are set.
@@ -281,6 +291,52 @@ ht_status_t run_gemm(Ctx &c, const GemmReq &q) {
     probe.a = q.a16; probe.b = q.b16; probe.splits = 1;
     std::string why;
     if (!tc_gemm_supported(probe, q.bn_tc, &why)) use_tc = false;
+  }
+  // grouped 3rd-order batch: the core pass's products are grouped FP32 GEMMs
+  if (c.core_grouped && c.stage == 1) {
+    if (c.core_seq > 1 || q.out_mode != OUT_COLMAJOR ||
+        (q.tiles_kind != TILES_ROWS && q.tiles_kind != TILES_SLABS))
+      return fail(HT_ERR_UNSUPPORTED, "grouped core pass: unexpected product");
+    const int seq = c.core_seq++;
+    if (!c.core_gemms || c.ar.dry) return HT_OK;
+    if (seq == 0 && q.a32.kind == OP_MN3 && q.a32.d0 >= 32 && q.b32.kind == OP_KM3 && q.t_cols <= 64 &&
+        q.ld_out == q.a32.d0 * q.a32.d2) {   // Z = X_(t) V, a thread per row of X
+      NarrowJob j;
+      j.X = static_cast<const float *>(q.a32.ptr); j.V = static_cast<const float *>(q.b32.ptr); j.Z = q.out;
+      j.L = q.a32.d0; j.R = q.a32.d2; j.N = static_cast<int>(q.a32.d1); j.kz = q.t_cols;
+      j.blk0 = 0;
+      j.nblk = static_cast<int>(std::min<long long>(32, (j.L * j.R + 255) / 256));
+      c.narrow_out->push_back(j);
+      return HT_OK;
+    }
+    if (seq == 1 && q.a32.kind == OP_KM3 && q.b32.kind == OP_KM3 && q.a32.d2 == 1 && q.t_cols <= 64 &&
+        q.ld_out == q.a32.d1 && q.tiles_kind == TILES_ROWS) {   // T1 = Z-rows x Up
+      T1Job j;
+      j.Z = static_cast<const float *>(q.a32.ptr); j.Up = static_cast<const float *>(q.b32.ptr); j.T1 = q.out;
+      j.rows = q.a32.d1; j.np = static_cast<int>(q.a32.d0); j.kp = q.t_cols;
+      j.blk0 = 0;
+      j.nblk = static_cast<int>(std::min<long long>(16, (j.rows + 63) / 64));
+      c.t1_out->push_back(j);
+      return HT_OK;
+    }
+    {
+      GemmArgs g;
+      g.a = q.a32;
+      g.b = q.b32;
+      g.gen = q.tiles_kind == TILES_ROWS ? make_rows_gen(q.t_rows, q.t_cols, 64) : make_slabs_gen(q.t_L, q.t_R, q.t_cols, 64);
+      g.num_tiles = g.gen.count;
+      g.splits = 1;
+      g.out_mode = OUT_COLMAJOR;
+      g.out = q.out;
+      g.ld_out = q.ld_out;
+      g.err = c.err;
+      g.fold = 0;
+      g.out16 = nullptr;
+      g.mt = 1;
+      if (!simt_grouped_add(g, *c.core_gemms, *c.core_blocks[seq]))
+        return fail(HT_ERR_UNSUPPORTED, "grouped core pass: product not groupable");
+    }
+    return HT_OK;
   }
   // grouped batch (eig_mode != 0): a leaf Gram of a mode of at most 256 is one
   // item of the batch's grouped Gram launch -- described by the plan pass,
@@ -519,7 +575,7 @@ ht_status_t core_contract(Ctx &c, const float *Z, int np, int nq, int ku, const 
   const size_t mark = c.ar.off;
   const long long rows = static_cast<long long>(nq) * ku;
   float *T1 = c.ar.take<float>(static_cast<size_t>(rows) * kp);
-  const int ranges = core_step2_ranges(nq, ku);
+  const int ranges = c.core_grouped ? 1 : core_step2_ranges(nq, ku);
   float *parts = ranges > 1 ? c.ar.take<float>(static_cast<size_t>(ranges) * kp * kq * ku) : nullptr;
   if (!T1 || (ranges > 1 && !parts)) return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (core)");
   // T1[(j + nq*u) + rows*a] = sum_i Z[i + np*(j + nq*u)] Up[i + np*a]
@@ -533,7 +589,11 @@ ht_status_t core_contract(Ctx &c, const float *Z, int np, int nq, int ku, const 
   q.out = T1;
   q.ld_out = rows;
   HT_TRY(run_gemm(c, q));
-  if (!c.dry()) {
+  // grouped: the batch's step reads T1 later; its memory, released below, is
+  // only written again by this tensor's error pass, which runs after the step
+  if (c.core_grouped) {
+    if (c.step2_out && !c.ar.dry) c.step2_out->push_back(Step2Job{T1, Uq, C, rows, nq, kp, kq, ku, 0, 0});
+  } else if (!c.dry()) {
     HT_CUDA(core_step2_launch(T1, rows, nq, kp, Uq, kq, ku, C, parts, c.st));
     c.launches += ranges > 1 ? 2 : 1;
   }
@@ -973,11 +1033,12 @@ ht_status_t decompose_core(Ctx &c, const Tree &T, const ht_config_t &cfg, const 
     // (no BF16 copy of X in its plain layout -- a first mode padded for the
     // Grams -- means an FP32 product: no split V either)
     __nv_bfloat16 *V16 =
-        (c.tc && x16) ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(dims[P.mc]) * 2 * fold_h + 64) : nullptr;
+        (c.tc && x16 && !c.core_grouped) ? c.ar.take<__nv_bfloat16>(static_cast<size_t>(dims[P.mc]) * 2 * fold_h + 64)
+                                         : nullptr;
     float *Rz = sketch ? c.ar.take<float>(static_cast<size_t>(kz) * kz) : nullptr;
     const size_t qbytes = sketch ? tsqr_workspace_bytes(zrows, kz) : 0;
     void *qws = sketch ? c.ar.take<char>(qbytes) : nullptr;
-    if (!Z || (c.tc && x16 && !V16) || (sketch && (!Rz || !qws)))
+    if (!Z || (c.tc && x16 && !c.core_grouped && !V16) || (sketch && (!Rz || !qws)))
       return fail(HT_ERR_OUT_OF_MEMORY, "workspace too small (core pass)");
     // 3. core pass: Z = X_(t) V, V = leading kz columns of the complementary leaf's basis
     if (V16 && !c.dry()) {
@@ -1113,10 +1174,19 @@ ht_status_t error_core(Ctx &c, const Tree &T, const float *x32, const long *dims
       };
       j.nblk[0] = blocks(j.kpq * P.kc, 8);
       j.nblk[1] = blocks(np_ * P.kq * P.kc, 16);
-      j.nblk[2] = blocks(np_ * nq_ * P.kc, 32);
-      j.ntile = nb;
-      j.nblk[3] = std::min(nb, 32);
-      for (int k = 0; k < 4; ++k) j.blk0[k] = 0;
+      // narrow: the last mode is the complementary leaf (rows of X contiguous)
+      j.narrow = (P.mc == 2 && P.kc <= 64 && Rr >= 32) ? 1 : 0;
+      if (j.narrow) {
+        j.nblk[2] = j.nblk[3] = 0;
+        j.nblk[4] = static_cast<int>(std::min<long long>(32, (Rr + 255) / 256));
+        j.ntile = j.nblk[4];
+      } else {
+        j.nblk[2] = blocks(np_ * nq_ * P.kc, 32);
+        j.nblk[3] = std::min(nb, 32);
+        j.nblk[4] = 0;
+        j.ntile = nb;
+      }
+      for (int k = 0; k < 5; ++k) j.blk0[k] = 0;
       c.err_out->push_back(j);
     }
     if (!c.dry()) {
@@ -1445,6 +1515,7 @@ struct CallArgs {
 // so it can be captured into a CUDA graph.
 ht_status_t enqueue_body(Ctx &c, const Tree &T, const ht_config_t &cfg, const float *xd, const CallArgs &a,
                          double *nparts, double *dsum, Timeline &tl, Result &res) {
+  c.core_grouped = c.eig_mode != 0 && a.order == 3 && cfg.leaf_method == HT_LEAF_GRAM;
   long long total = 1;
   for (int m = 0; m < a.order; ++m) total *= a.dims[m];
   __nv_bfloat16 *xb = nullptr, *xbt = nullptr, *xp = nullptr;
@@ -1787,8 +1858,7 @@ struct BatchState {
   cudaStream_t cap = nullptr;   // capture origin (the caller's stream may be the legacy stream)
   cudaEvent_t fork = nullptr, join[kLanes] = {}, t0 = nullptr, t1 = nullptr;
   cudaEvent_t tp[5] = {};   // grouped mode: ends of the first five phases (ms_phase)
-  cudaStream_t side = nullptr;                    // grouped mode: the first half's tails and error pass
-  cudaEvent_t mid[kLanes] = {}, side_done = nullptr;
+
   bool grouped = false;
   double *sums = nullptr;   // device: [count][2] (||X||^2, ||X - Xhat||^2)
   int *errw = nullptr;      // device: one error word per lane
@@ -1805,8 +1875,16 @@ struct BatchState {
   size_t tails_bytes = 0;
   void *errs = nullptr;     // device: grouped error passes
   size_t errs_bytes = 0;
-  void *maps = nullptr;     // device: block -> job maps of the grouped conversion and error launches
+  void *maps = nullptr;     // device: block -> job maps of the grouped conversion, step-2 and error launches
   size_t maps_bytes = 0;
+  void *core = nullptr;     // device: grouped core-pass GEMM parameters, then their tiles (group 0, group 1)
+  size_t core_bytes = 0;
+  void *step2 = nullptr;    // device: grouped step-2 jobs
+  size_t step2_bytes = 0;
+  void *narrow = nullptr;   // device: grouped narrow mode products
+  size_t narrow_bytes = 0;
+  void *t1jobs = nullptr;   // device: grouped first core contractions
+  size_t t1jobs_bytes = 0;
 };
 
 // Workspace layout of one batch.  Per-lane mode: tensor i runs in lane
@@ -1821,12 +1899,14 @@ struct BatchLayout {
   int nprob = 0, iters = 0, refine = 0;
   int nconv = 0, conv_blocks = 0, ncopy = 0;   // grouped conversion jobs (their blocks), output copies
   int ngram[2] = {0, 0};                       // grouped Grams per class
-  // tensors [0, half) and [half, count): the first half's transfer tails and
-  // error pass overlap the second half's core passes
-  int half = 0;
-  int ntail_h[2] = {0, 0}, nerr_h[2] = {0, 0};   // jobs per half (tails, error passes)
-  int err_blocks[2][4] = {};                     // launch sizes of each half's error steps
-  size_t map_off[9] = {};                        // ints into BatchState::maps: conversion, then per half error steps 0-3
+  int ntail = 0, nerr = 0;                     // grouped transfer tails and error passes
+  int err_blocks[5] = {};                      // launch sizes of the error steps
+  int err_narrow_kb = 0;                       // widest kc of the narrow error jobs
+  size_t map_off[7] = {};                      // ints into BatchState::maps: conversion, step 2, error steps 0-4
+  int ncore_blocks[2] = {0, 0}, nstep2_blocks = 0;   // grouped core pass: GEMM tiles per group, step-2 blocks
+  size_t core_params = 0;                      // bytes of GEMM parameters before the tiles in BatchState::core
+  int nnarrow_blocks = 0, narrow_kb = 0, nt1_blocks = 0;   // narrow mode products (their widest kz), T1 blocks
+  size_t map_narrow = 0, map_t1 = 0;           // their block -> job maps in BatchState::maps
 };
 // Leaves of at most this size go through the grouped solver (one CTA each);
 // batches with larger modes keep the per-lane cooperative solver.
@@ -1853,9 +1933,7 @@ ht_status_t batch_streams(BatchState &b) {
   HT_CUDA(cudaEventCreate(&b.t0));
   HT_CUDA(cudaEventCreate(&b.t1));
   for (int i = 0; i < 5; ++i) HT_CUDA(cudaEventCreate(&b.tp[i]));
-  HT_CUDA(cudaStreamCreateWithFlags(&b.side, cudaStreamNonBlocking));
-  for (int l = 0; l < kLanes; ++l) HT_CUDA(cudaEventCreateWithFlags(&b.mid[l], cudaEventDisableTiming));
-  HT_CUDA(cudaEventCreateWithFlags(&b.side_done, cudaEventDisableTiming));
+
   return HT_OK;
 }
 
@@ -1867,17 +1945,19 @@ struct BatchPlanOut {
   std::vector<unsigned char> grams[2];       // grouped Gram items by class
   std::vector<TailJob> tails;
   std::vector<ErrJob> errs;
+  std::vector<SParamsBlob> core_gemms;
+  std::vector<SimtBlockBlob> core_blocks[2];
+  std::vector<Step2Job> step2;
+  std::vector<NarrowJob> narrow;
+  std::vector<T1Job> t1;
   int iters = 0, refine = 0;
-  size_t tails_at = 0, errs_at = 0;          // jobs of the tensors before the half point
 };
 
 // One pass over every tensor of the batch.  phase 0: the whole chain of each
 // tensor (per-lane mode); 1, 2, 3: the tensor's launches of stage 0 (up to the
 // leaf Grams), stage 1 (after the leaf solver) or stage 3 (the error pass);
 // 4: no launches, the grouped stages' tables are filled into *plan_out (host
-// only).  Phases 0-3 run on the lanes, forked from and joined back into `st`;
-// phase 2 also records b.mid[l] on every lane once the tensors before L.half
-// are enqueued.
+// only).  Phases 0-3 run on the lanes, forked from and joined back into `st`.
 ht_status_t batch_pass(BatchState &b, const BatchLayout &L, int phase, cudaStream_t st, int count,
                        const float *const *x, const long *dims, int order, const std::vector<Tree> &trees,
                        const ht_config_t &cfg, float *const *U, float *const *B, bool want_err, int eig_ctas,
@@ -1888,14 +1968,6 @@ ht_status_t batch_pass(BatchState &b, const BatchLayout &L, int phase, cudaStrea
     for (int l = 0; l < b.lanes; ++l) HT_CUDA(cudaStreamWaitEvent(b.lane[l], b.fork, 0));
   }
   for (int i = 0; i < count; ++i) {
-    if (i == L.half && L.half > 0) {
-      if (plan) {
-        plan_out->tails_at = plan_out->tails.size();
-        plan_out->errs_at = plan_out->errs.size();
-      } else if (phase == 2) {
-        for (int l = 0; l < b.lanes; ++l) HT_CUDA(cudaEventRecord(b.mid[l], b.lane[l]));
-      }
-    }
     const int l = i % b.lanes;
     Ctx c;
     c.st = b.lane[l];
@@ -1916,6 +1988,12 @@ ht_status_t batch_pass(BatchState &b, const BatchLayout &L, int phase, cudaStrea
         c.copy_out = &plan_out->copies;
         c.gram_out[0] = &plan_out->grams[0];
         c.gram_out[1] = &plan_out->grams[1];
+        c.core_gemms = &plan_out->core_gemms;
+        c.core_blocks[0] = &plan_out->core_blocks[0];
+        c.core_blocks[1] = &plan_out->core_blocks[1];
+        c.step2_out = &plan_out->step2;
+        c.narrow_out = &plan_out->narrow;
+        c.t1_out = &plan_out->t1;
       }
     } else {
       c.ar.base = static_cast<char *>(b.ws) + static_cast<size_t>(l) * L.lane_bytes;
@@ -1943,29 +2021,11 @@ ht_status_t batch_pass(BatchState &b, const BatchLayout &L, int phase, cudaStrea
   return HT_OK;
 }
 
-// The transfer tails and error passes of tensors [0, half) (h = 0) or
-// [half, count) (h = 1) on stream s.
-ht_status_t batch_tail_and_error(BatchState &b, const BatchLayout &L, int h, cudaStream_t s, bool record_mid) {
-  const int t0 = h == 0 ? 0 : L.ntail_h[0], e0 = h == 0 ? 0 : L.nerr_h[0];
-  HT_CUDA(transfer_tail_grouped_launch(static_cast<const TailJob *>(b.tails) + t0, L.ntail_h[h], s));
-  b.launches += L.ntail_h[h] > 0 ? 1 : 0;
-  if (record_mid) HT_CUDA(cudaEventRecordWithFlags(b.tp[3], s, cudaEventRecordExternal));
-  if (L.nerr_h[h] > 0) {
-    const int *maps = static_cast<const int *>(b.maps);
-    const int *emaps[4];
-    for (int k = 0; k < 4; ++k) emaps[k] = maps + L.map_off[1 + 4 * h + k];
-    HT_CUDA(error_grouped_launch(static_cast<const ErrJob *>(b.errs) + e0, L.nerr_h[h], L.err_blocks[h], emaps, s));
-    b.launches += 5;
-  }
-  return HT_OK;
-}
-
 // Enqueue the whole batch on `st`.  Grouped mode: one conversion launch, the
 // grouped Grams, one launch of the grouped leaf solver for every leaf of every
-// tensor (tables uploaded beforehand by batch_plan_grouped), the core passes
-// on the lanes, the grouped transfer tails and error passes -- the first
-// half's on a side stream, overlapping the second half's core passes -- and
-// one copy of every factor to the caller's buffers.
+// tensor (tables uploaded beforehand by batch_plan_grouped), the core pass
+// (grouped for 3rd order, on the lanes for 4th), the grouped transfer tails
+// and error passes, and one copy of every factor to the caller's buffers.
 ht_status_t batch_enqueue(BatchState &b, const BatchLayout &L, cudaStream_t st, int count, const float *const *x,
                           const long *dims, int order, const std::vector<Tree> &trees, const ht_config_t &cfg,
                           float *const *U, float *const *B, bool want_err, int eig_ctas) {
@@ -1984,16 +2044,33 @@ ht_status_t batch_enqueue(BatchState &b, const BatchLayout &L, cudaStream_t st, 
   HT_CUDA(eig_grouped_launch(b.table, L.nprob, L.iters, L.refine, st));
   HT_CUDA(cudaEventRecordWithFlags(b.tp[1], st, cudaEventRecordExternal));
   b.launches += 1;
-  HT_TRY(batch_pass(b, L, 2, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas));
-  if (L.half > 0) {   // the first half, on the side stream, as soon as the lanes are past it
-    for (int l = 0; l < b.lanes; ++l) HT_CUDA(cudaStreamWaitEvent(b.side, b.mid[l], 0));
-    HT_TRY(batch_tail_and_error(b, L, 0, b.side, false));
-    HT_CUDA(cudaEventRecord(b.side_done, b.side));
+  if (L.nstep2_blocks > 0) {   // 3rd order: the grouped core pass
+    const SParamsBlob *params = static_cast<const SParamsBlob *>(b.core);
+    const SimtBlockBlob *tiles =
+        reinterpret_cast<const SimtBlockBlob *>(static_cast<const char *>(b.core) + L.core_params);
+    HT_CUDA(modeprod_narrow_grouped_launch(static_cast<const NarrowJob *>(b.narrow), maps + L.map_narrow,
+                                           L.nnarrow_blocks, L.narrow_kb, st));
+    HT_CUDA(simt_grouped_launch(params, tiles, L.ncore_blocks[0], st));
+    HT_CUDA(core_t1_grouped_launch(static_cast<const T1Job *>(b.t1jobs), maps + L.map_t1, L.nt1_blocks, st));
+    HT_CUDA(simt_grouped_launch(params, tiles + L.ncore_blocks[0], L.ncore_blocks[1], st));
+    HT_CUDA(core_step2_grouped_launch(static_cast<const Step2Job *>(b.step2), maps + L.map_off[1], L.nstep2_blocks,
+                                      st));
+    b.launches += (L.nnarrow_blocks > 0) + (L.ncore_blocks[0] > 0) + (L.nt1_blocks > 0) + (L.ncore_blocks[1] > 0) + 1;
   }
+  HT_TRY(batch_pass(b, L, 2, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas));
   HT_CUDA(cudaEventRecordWithFlags(b.tp[2], st, cudaEventRecordExternal));
-  HT_TRY(batch_tail_and_error(b, L, 1, st, true));
+  HT_CUDA(transfer_tail_grouped_launch(static_cast<const TailJob *>(b.tails), L.ntail, st));
+  b.launches += L.ntail > 0 ? 1 : 0;
+  HT_CUDA(cudaEventRecordWithFlags(b.tp[3], st, cudaEventRecordExternal));
+  if (L.nerr > 0) {
+    const int *emaps[5] = {maps + L.map_off[2], maps + L.map_off[3], maps + L.map_off[4], maps + L.map_off[5],
+                           maps + L.map_off[6]};
+    HT_CUDA(error_grouped_launch(static_cast<const ErrJob *>(b.errs), L.nerr, L.err_blocks, emaps, L.err_narrow_kb,
+                                 st));
+    for (int k = 0; k < 5; ++k) b.launches += L.err_blocks[k] > 0 ? 1 : 0;
+    b.launches += 1;
+  }
   HT_TRY(batch_pass(b, L, 3, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas));
-  if (L.half > 0) HT_CUDA(cudaStreamWaitEvent(st, b.side_done, 0));
   HT_CUDA(cudaEventRecordWithFlags(b.tp[4], st, cudaEventRecordExternal));
   HT_CUDA(copy_segments_launch(static_cast<const CopySeg *>(b.copies), L.ncopy, st));
   b.launches += L.ncopy > 0 ? 1 : 0;
@@ -2022,9 +2099,7 @@ ht_status_t batch_plan_grouped(BatchState &b, BatchLayout &L, int count, const f
   const int launches = b.launches;
   HT_TRY(batch_pass(b, L, 4, nullptr, count, x, dims, order, trees, cfg, U, B, want_err, 0, &P));
   b.launches = launches;
-  if (L.half <= 0) P.tails_at = P.errs_at = 0;
-  // block -> job maps: the conversion, then each half's four error steps
-  // (job indices relative to the half's first job)
+  // block -> job maps: the conversion, the core pass's step 2, the four error steps
   std::vector<int> maps;
   int blk = 0;
   for (size_t j = 0; j < P.conv.size(); ++j) {
@@ -2035,22 +2110,62 @@ ht_status_t batch_plan_grouped(BatchState &b, BatchLayout &L, int count, const f
   L.map_off[0] = 0;
   L.nconv = static_cast<int>(P.conv.size());
   L.conv_blocks = blk;
-  const size_t ebeg[2] = {0, P.errs_at}, eend[2] = {P.errs_at, P.errs.size()};
-  for (int h = 0; h < 2; ++h) {
-    L.nerr_h[h] = static_cast<int>(eend[h] - ebeg[h]);
-    for (int k = 0; k < 4; ++k) {
-      L.map_off[1 + 4 * h + k] = maps.size();
-      int eb = 0;
-      for (size_t i = ebeg[h]; i < eend[h]; ++i) {
-        P.errs[i].blk0[k] = eb;
-        eb += P.errs[i].nblk[k];
-        maps.insert(maps.end(), P.errs[i].nblk[k], static_cast<int>(i - ebeg[h]));
-      }
-      L.err_blocks[h][k] = eb;
-    }
+  L.map_off[1] = maps.size();
+  blk = 0;
+  for (size_t j = 0; j < P.step2.size(); ++j) {
+    P.step2[j].blk0 = blk;
+    blk += P.step2[j].kc;
+    maps.insert(maps.end(), P.step2[j].kc, static_cast<int>(j));
   }
-  L.ntail_h[0] = static_cast<int>(P.tails_at);
-  L.ntail_h[1] = static_cast<int>(P.tails.size() - P.tails_at);
+  L.nstep2_blocks = blk;
+  L.map_narrow = maps.size();
+  blk = 0;
+  L.narrow_kb = 0;
+  for (size_t j = 0; j < P.narrow.size(); ++j) {
+    P.narrow[j].blk0 = blk;
+    blk += P.narrow[j].nblk;
+    maps.insert(maps.end(), P.narrow[j].nblk, static_cast<int>(j));
+    L.narrow_kb = std::max(L.narrow_kb, P.narrow[j].kz);
+  }
+  L.nnarrow_blocks = blk;
+  L.map_t1 = maps.size();
+  blk = 0;
+  for (size_t j = 0; j < P.t1.size(); ++j) {
+    P.t1[j].blk0 = blk;
+    blk += P.t1[j].nblk;
+    maps.insert(maps.end(), P.t1[j].nblk, static_cast<int>(j));
+  }
+  L.nt1_blocks = blk;
+  HT_TRY(upload_table(b.narrow, b.narrow_bytes, P.narrow.data(), sizeof(NarrowJob) * P.narrow.size()));
+  HT_TRY(upload_table(b.t1jobs, b.t1jobs_bytes, P.t1.data(), sizeof(T1Job) * P.t1.size()));
+  for (int k = 0; k < 5; ++k) {
+    L.map_off[2 + k] = maps.size();
+    int eb = 0;
+    for (size_t i = 0; i < P.errs.size(); ++i) {
+      P.errs[i].blk0[k] = eb;
+      eb += P.errs[i].nblk[k];
+      maps.insert(maps.end(), P.errs[i].nblk[k], static_cast<int>(i));
+    }
+    L.err_blocks[k] = eb;
+  }
+  L.err_narrow_kb = 0;
+  for (const ErrJob &j : P.errs)
+    if (j.narrow) L.err_narrow_kb = std::max(L.err_narrow_kb, j.kc);
+  L.nerr = static_cast<int>(P.errs.size());
+  L.ntail = static_cast<int>(P.tails.size());
+  // core pass: the GEMM parameters, then group 0's tiles, then group 1's
+  L.ncore_blocks[0] = static_cast<int>(P.core_blocks[0].size());
+  L.ncore_blocks[1] = static_cast<int>(P.core_blocks[1].size());
+  L.core_params = sizeof(SParamsBlob) * P.core_gemms.size();
+  std::vector<unsigned char> core(L.core_params + sizeof(SimtBlockBlob) * (L.ncore_blocks[0] + L.ncore_blocks[1]));
+  if (!core.empty()) {
+    std::memcpy(core.data(), P.core_gemms.data(), L.core_params);
+    std::memcpy(core.data() + L.core_params, P.core_blocks[0].data(), sizeof(SimtBlockBlob) * L.ncore_blocks[0]);
+    std::memcpy(core.data() + L.core_params + sizeof(SimtBlockBlob) * L.ncore_blocks[0], P.core_blocks[1].data(),
+                sizeof(SimtBlockBlob) * L.ncore_blocks[1]);
+  }
+  HT_TRY(upload_table(b.core, b.core_bytes, core.data(), core.size()));
+  HT_TRY(upload_table(b.step2, b.step2_bytes, P.step2.data(), sizeof(Step2Job) * P.step2.size()));
   L.ngram[0] = static_cast<int>(P.grams[0].size() / tc_gram_item_bytes());
   L.ngram[1] = static_cast<int>(P.grams[1].size() / tc_gram_item_bytes());
   P.grams[0].insert(P.grams[0].end(), P.grams[1].begin(), P.grams[1].end());
@@ -2408,7 +2523,6 @@ ht_status_t ht_decompose_batched(int count, const float *const *x, const long *d
     for (int i = 0; i < count; ++i)
       for (int m = 0; m < order; ++m) L.grouped = L.grouped && dims[static_cast<size_t>(i) * order + m] <= kGroupedMaxN;
     L.off.assign(static_cast<size_t>(count) + 1, 0);
-    L.half = count >= 4 ? count / 2 : 0;
     for (int i = 0; i < count; ++i) {
       const long *di = dims + static_cast<size_t>(i) * order;
       HT_TRY(parse_tree(&trees[i], di, order, T[i]));
@@ -2584,6 +2698,18 @@ ht_status_t ht_release_batch(void) {
   if (b.maps) HT_CUDA(cudaFree(b.maps));
   b.maps = nullptr;
   b.maps_bytes = 0;
+  if (b.core) HT_CUDA(cudaFree(b.core));
+  b.core = nullptr;
+  b.core_bytes = 0;
+  if (b.step2) HT_CUDA(cudaFree(b.step2));
+  b.step2 = nullptr;
+  b.step2_bytes = 0;
+  if (b.narrow) HT_CUDA(cudaFree(b.narrow));
+  b.narrow = nullptr;
+  b.narrow_bytes = 0;
+  if (b.t1jobs) HT_CUDA(cudaFree(b.t1jobs));
+  b.t1jobs = nullptr;
+  b.t1jobs_bytes = 0;
   return HT_OK;
 }
 

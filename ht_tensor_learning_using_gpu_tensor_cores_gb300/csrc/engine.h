@@ -104,6 +104,21 @@ cudaError_t tc_prepare();
 long tc_num_kblocks(const Operand &a);
 
 // SIMT FP32 path (float operands), BM = 128, BN in {64, 128}.
+// Grouped FP32 GEMMs of the batched path (the 3rd-order core pass): every
+// tile of every GEMM of a group in one launch, each block a whole tile over
+// the full K range (128 x 64 tiles, column-major output, row or slab tile
+// generators).  simt_grouped_add appends the GEMM's parameters and its tiles
+// (false: not a groupable GEMM); both tables are copied to device memory
+// (8-byte aligned) for simt_grouped_launch.  The blobs are opaque storage.
+struct SParamsBlob {
+  unsigned long long w[24];
+};
+struct SimtBlockBlob {
+  unsigned long long w[6];
+};
+bool simt_grouped_add(const GemmArgs &g, std::vector<SParamsBlob> &gemms, std::vector<SimtBlockBlob> &blocks);
+cudaError_t simt_grouped_launch(const SParamsBlob *gemms_dev, const SimtBlockBlob *blocks_dev, int nblocks,
+                                cudaStream_t s);
 cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s);
 long simt_k_total(const Operand &a);
 
@@ -158,13 +173,16 @@ struct ConvJob {
   long long n1, n1p, rest;
   int blk0, nblk;
 };
-// Grouped error pass of the batched path (3rd order): five launches for every
-// job -- core = Bt Bkt, the two expansion steps into Tm and Wm, the fused
-// error tiles (as error_fused_launch, ntile = tiles x slabs of X) into parts,
-// and their sum into out[0].  blk0[k] / nblk[k]: the job's blocks in launch k
-// (grid-stride within the job); blocks[k] = the launch sizes and
-// job_of_block[k] (device) the job of each block of launch k.  Job table in
-// device memory.
+// Grouped error pass of the batched path (3rd order): core = Bt Bkt (launch
+// 0) and the first expansion step into Tm (1) for every job; then either the
+// second expansion step into Wm (2) and the fused error tiles (3, as
+// error_fused_launch, ntile = tiles x slabs of X) or, for a narrow job (the
+// complementary leaf is the last mode, kc <= narrow_kb <= 64), the narrow
+// error kernel (4, W formed per row, ntile = nblk[4] partials); then the sum
+// of the partials into out[0].  blk0[k] / nblk[k]: the job's blocks in launch
+// k (grid-stride within the job, 0 when it takes no part); blocks[k] = the
+// launch sizes and job_of_block[k] (device) the job of each block of launch
+// k.  Job table in device memory.
 struct ErrJob {
   const float *Bt, *B0;        // B_t (kpq x kt); B0 = Bkt (kt x kc) or its transpose
   float *core, *Tm, *Wm;
@@ -172,11 +190,43 @@ struct ErrJob {
   const float *X, *A, *B;      // error tiles: X (R x Cn per slab) against A B^T
   double *parts, *out;
   long long kpq, ldx, sx, lda, sa, ldb, R, Cn;
-  int kt, kc, t_is_left, np, nq, kp, kq, kk, slabs, ntile;
-  int blk0[4], nblk[4];
+  int kt, kc, t_is_left, np, nq, kp, kq, kk, slabs, ntile, narrow;
+  int blk0[5], nblk[5];
 };
 cudaError_t error_grouped_launch(const ErrJob *jobs_dev, int njobs, const int *blocks, const int *const *job_of_block,
-                                 cudaStream_t s);
+                                 int narrow_kb, cudaStream_t s);
+// Grouped narrow mode product (3rd-order core pass, rows of X contiguous,
+// L >= 32): Z[row + L R j] = sum_i X[l + L (i + N r)] V[i + N j], row = l + L r,
+// j < kz <= kb (kb <= 64, the largest kz of the launch).  Blocks
+// [blk0, blk0 + nblk) of the launch stride over the job's rows.
+struct NarrowJob {
+  const float *X, *V;
+  float *Z;
+  long long L, R;
+  int N, kz, blk0, nblk;
+};
+cudaError_t modeprod_narrow_grouped_launch(const NarrowJob *jobs_dev, const int *job_of_block, int nblocks, int kb,
+                                          cudaStream_t s);
+// Grouped first core contraction: T1[row + rows a] = sum_i Z[i + np row] Up[i + np a],
+// a < kp <= 64; blocks [blk0, blk0 + nblk) stride over tiles of 64 rows.
+struct T1Job {
+  const float *Z, *Up;
+  float *T1;
+  long long rows;
+  int np, kp, blk0, nblk;
+};
+cudaError_t core_t1_grouped_launch(const T1Job *jobs_dev, const int *job_of_block, int nblocks, cudaStream_t s);
+// Grouped second core-contraction step (C[a, b, c] = sum_j T1[(j + nq c) +
+// ldt a] Uq[j + nq b], as core_step2_launch without j ranges): job j owns the
+// blocks [blk0, blk0 + kc) of the launch, one per c; job_of_block (device)
+// maps the launch's blocks to jobs.  kp, kq <= 64, kp kq <= 4096.
+struct Step2Job {
+  const float *T1, *Uq;
+  float *C;
+  long long ldt;
+  int nq, kp, kq, kc, blk0, pad;
+};
+cudaError_t core_step2_grouped_launch(const Step2Job *jobs_dev, const int *job_of_block, int nblocks, cudaStream_t s);
 cudaError_t convert_grouped_launch(const ConvJob *jobs_dev, int njobs, int total_blocks, const int *job_of_block,
                                    cudaStream_t s);
 // dst[0, count) = src[0, count) for every segment, one launch (table in device memory).

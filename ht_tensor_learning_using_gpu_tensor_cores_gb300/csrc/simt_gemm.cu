@@ -8,6 +8,10 @@
 //
 // Tile 128 x BN (BN = 128 or 64), K step 16, 256 threads, 8 x (BN/16)
 // register tile per thread, double-buffered shared memory.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
 #include "common.cuh"
 #include "engine.h"
 #include "tiles.cuh"
@@ -90,8 +94,9 @@ HT_DEV const float *op_ptr(int kind, const float *p, long long d0, long long d1,
   return p + row + d0 * (k + d1 * static_cast<long long>(z));
 }
 
+// One output tile (split `split` of its K range) of a CTA.
 template <int BN>
-__global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p, const TileGen gen) {
+HT_DEV void simt_gemm_tile(const SParams &p, const Tile &tile, int tile_idx, int split) {
   constexpr int TN = BN / 16;   // columns per thread (8 or 4)
   constexpr int A_PER = BM * BKS / 256;   // 8
   constexpr int B_PER = BN * BKS / 256;   // 8 or 4
@@ -99,9 +104,6 @@ __global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p, const T
   __shared__ __align__(16) float Bs[2][BKS][BN + 4];
 
   const int tid = threadIdx.x;
-  const int tile_idx = blockIdx.x % p.num_tiles;
-  const int split = blockIdx.x / p.num_tiles;
-  const Tile tile = gen_tile(gen, tile_idx);
   const long long kbeg = static_cast<long long>(split) * p.k_per_split;
   const long long kend = min(p.k_total, kbeg + p.k_per_split);
 
@@ -235,6 +237,33 @@ __global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p, const T
   }
 }
 
+template <int BN>
+__global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p, const TileGen gen) {
+  const int tile_idx = blockIdx.x % p.num_tiles;
+  simt_gemm_tile<BN>(p, gen_tile(gen, tile_idx), tile_idx, blockIdx.x / p.num_tiles);
+}
+
+// Grouped GEMMs of the batched path: block i computes the tile blocks[i].tile
+// of GEMM gemms[blocks[i].gemm] over its whole K range (column-major output).
+struct SimtBlock {
+  int gemm, pad;
+  Tile tile;
+};
+
+// The tables hold one SParams / SimtBlock per blob-sized slot.
+__global__ void __launch_bounds__(256, 2) simt_gemm_grouped_kernel(const SParamsBlob *__restrict__ gemms,
+                                                                const SimtBlockBlob *__restrict__ blocks) {
+  __shared__ SParams P;
+  __shared__ Tile T;
+  if (threadIdx.x == 0) {
+    const SimtBlock b = *reinterpret_cast<const SimtBlock *>(blocks + blockIdx.x);
+    P = *reinterpret_cast<const SParams *>(gemms + b.gemm);
+    T = b.tile;
+  }
+  __syncthreads();
+  simt_gemm_tile<64>(P, T, 0, 0);
+}
+
 // Sum partial tiles [splits][num_tiles][128][bn] in a fixed order.  A block
 // is (256 / G) consecutive outputs x G split groups: thread (o, g) sums the
 // partials of group g in order (8 loads in flight), then the G group sums are
@@ -302,8 +331,8 @@ long simt_k_total(const Operand &a) {
   return a.d1;
 }
 
-cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s) {
-  SParams p;
+namespace {
+bool make_sparams(const GemmArgs &g, SParams &p) {
   p.a_kind = g.a.kind;
   p.b_kind = g.b.kind;
   p.a = static_cast<const float *>(g.a.ptr);
@@ -311,7 +340,7 @@ cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s) {
   p.a0 = g.a.d0; p.a1 = g.a.d1; p.a2 = g.a.d2;
   p.b0 = g.b.d0; p.b1 = g.b.d1; p.b2 = g.b.d2;
   p.k_total = simt_k_total(g.a);
-  if (simt_k_total(g.b) != p.k_total) return cudaErrorInvalidValue;
+  if (simt_k_total(g.b) != p.k_total) return false;
   const int splits = g.splits < 1 ? 1 : g.splits;
   long long kps = (p.k_total + splits - 1) / splits;
   kps = (kps + BKS - 1) / BKS * BKS;
@@ -331,6 +360,76 @@ cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s) {
   };
   p.a_vec = vec_of(g.a);
   p.b_vec = vec_of(g.b);
+  return true;
+}
+
+// The host's copy of gen_tile for the row and slab generators.
+bool host_tile(const TileGen &g, int idx, Tile &t) {
+  t.a_z = 0;
+  t.b_row = 0;
+  t.out_col = 0;
+  if (g.kind == TILES_ROWS) {
+    t.a_row = 128 * idx;
+    t.out_row = 128ll * idx;
+    t.valid_rows = static_cast<int>(std::min(128ll, g.rows - 128ll * idx));
+    t.valid_cols = std::min(g.cols, g.bn);
+    return true;
+  }
+  if (g.kind == TILES_SLABS) {
+    const long long nlb = (g.L + 127) / 128;
+    const long long r = idx / nlb, lb = idx - r * nlb;
+    t.a_row = static_cast<int>(128 * lb);
+    t.a_z = static_cast<int>(r);
+    t.out_row = 128 * lb + g.L * r;
+    t.valid_rows = static_cast<int>(std::min(128ll, g.L - 128 * lb));
+    t.valid_cols = std::min(g.cols, g.bn);
+    return true;
+  }
+  return false;
+}
+}  // namespace
+
+bool simt_grouped_add(const GemmArgs &g, std::vector<SParamsBlob> &gemms, std::vector<SimtBlockBlob> &blocks) {
+  static_assert(sizeof(SParams) <= sizeof(SParamsBlob) && sizeof(SimtBlock) <= sizeof(SimtBlockBlob) &&
+                    alignof(SParams) <= alignof(SParamsBlob) && alignof(SimtBlock) <= alignof(SimtBlockBlob),
+                "blob sizes");
+  if (g.gen.bn != 64 || g.out_mode != OUT_COLMAJOR || (g.gen.kind != TILES_ROWS && g.gen.kind != TILES_SLABS))
+    return false;
+  GemmArgs g1 = g;
+  g1.splits = 1;
+  SParams p;
+  std::memset(&p, 0, sizeof(p));
+  if (!make_sparams(g1, p)) return false;
+  SParamsBlob pb;
+  std::memset(&pb, 0, sizeof(pb));
+  std::memcpy(&pb, &p, sizeof(p));
+  const int gi = static_cast<int>(gemms.size());
+  gemms.push_back(pb);
+  for (int t = 0; t < g.num_tiles; ++t) {
+    SimtBlock b;
+    std::memset(&b, 0, sizeof(b));
+    b.gemm = gi;
+    if (!host_tile(g.gen, t, b.tile)) return false;
+    SimtBlockBlob bb;
+    std::memset(&bb, 0, sizeof(bb));
+    std::memcpy(&bb, &b, sizeof(b));
+    blocks.push_back(bb);
+  }
+  return true;
+}
+
+cudaError_t simt_grouped_launch(const SParamsBlob *gemms_dev, const SimtBlockBlob *blocks_dev, int nblocks,
+                                cudaStream_t s) {
+  if (nblocks < 1) return cudaSuccess;
+  if (!gemms_dev || !blocks_dev) return cudaErrorInvalidValue;
+  simt_gemm_grouped_kernel<<<nblocks, 256, 0, s>>>(gemms_dev, blocks_dev);
+  return cudaGetLastError();
+}
+
+cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s) {
+  SParams p;
+  if (!make_sparams(g, p)) return cudaErrorInvalidValue;
+  const int splits = g.splits < 1 ? 1 : g.splits;
   const int grid = g.num_tiles * splits;
   if (bn == 128)
     simt_gemm_kernel<128><<<grid, 256, 0, s>>>(p, g.gen);

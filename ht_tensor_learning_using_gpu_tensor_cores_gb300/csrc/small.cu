@@ -267,10 +267,9 @@ __global__ void gemm_tn_small_kernel(const float *__restrict__ A, int lda, const
 
 // C[a, b, c] = sum_j T1[(j + nq*c) + ldt*a] * Uq[j + nq*b]: a CTA per (c, range
 // of jc values of j); with several ranges C points at partials [range][kp kq kc].
-__global__ void __launch_bounds__(256) core_step2_kernel(const float *__restrict__ T1, long long ldt, int nq, int kp,
-                                                         const float *__restrict__ Uq, int kq, int jc,
-                                                         float *__restrict__ C) {
-  const int c = blockIdx.x, j_lo = blockIdx.y * jc, j_hi = min(nq, j_lo + jc);
+// Entries (:, :, c) of C from the j range [j_lo, j_hi); writes Co[pr + kp kq c].
+HT_DEV void core_step2_body(const float *__restrict__ T1, long long ldt, int nq, int kp, const float *__restrict__ Uq,
+                            int kq, int c, int j_lo, int j_hi, float *__restrict__ Co) {
   __shared__ float Ts[64][65];
   __shared__ float Us[64][65];
   const int t = threadIdx.x;
@@ -297,12 +296,112 @@ __global__ void __launch_bounds__(256) core_step2_kernel(const float *__restrict
       }
     }
   }
-  float *Co = C + static_cast<long long>(blockIdx.y) * npair * gridDim.x;
 #pragma unroll
   for (int q = 0; q < 16; ++q) {
     const int pr = t + 256 * q;
     if (pr < npair) Co[pr + static_cast<long long>(npair) * c] = acc[q];
   }
+}
+
+__global__ void __launch_bounds__(256) core_step2_kernel(const float *__restrict__ T1, long long ldt, int nq, int kp,
+                                                         const float *__restrict__ Uq, int kq, int jc,
+                                                         float *__restrict__ C) {
+  const int c = blockIdx.x, j_lo = blockIdx.y * jc, j_hi = min(nq, j_lo + jc);
+  core_step2_body(T1, ldt, nq, kp, Uq, kq, c, j_lo, j_hi,
+                  C + static_cast<long long>(blockIdx.y) * kp * kq * gridDim.x);
+}
+
+// Grouped narrow mode product of the batched path (the 3rd-order core pass,
+// rows of X contiguous): Z[row + L R j] = sum_i X[l + L (i + N r)] V[i + N j]
+// for row = l + L r, j < kz <= KB.  A thread per row, V staged in 64-row chunks
+// of shared memory; the job's blocks stride over its rows.
+template <int KB>
+__global__ void __launch_bounds__(256) modeprod_narrow_grouped_kernel(const NarrowJob *__restrict__ jobs,
+                                                                      const int *__restrict__ job_of_block) {
+  __shared__ NarrowJob J;
+  __shared__ float Vs[64][KB];
+  load_job(jobs, job_of_block[blockIdx.x], J);
+  const int t = threadIdx.x, kz = J.kz, N = J.N;
+  const long long L = J.L, total = J.L * J.R;
+  for (long long base = static_cast<long long>(blockIdx.x - J.blk0) * 256; base < total; base += J.nblk * 256ll) {
+    const long long row = base + t;
+    const bool valid = row < total;
+    const long long r = valid ? row / L : 0, l = valid ? row - r * L : 0;
+    const float *x = J.X + l + L * N * r;
+    float acc[KB];
+#pragma unroll
+    for (int j = 0; j < KB; ++j) acc[j] = 0.f;
+    for (int i0 = 0; i0 < N; i0 += 64) {
+      const int ni = min(64, N - i0);
+      __syncthreads();
+      for (int e = t; e < 64 * KB; e += 256) {
+        const int ii = e / KB, j = e - ii * KB;
+        Vs[ii][j] = (ii < ni && j < kz) ? J.V[(i0 + ii) + static_cast<long long>(N) * j] : 0.f;
+      }
+      __syncthreads();
+      if (valid) {
+        for (int ii = 0; ii < ni; ++ii) {
+          const float xv = __ldg(x + L * (i0 + ii));
+#pragma unroll
+          for (int j = 0; j < KB; ++j) acc[j] = fmaf(xv, Vs[ii][j], acc[j]);
+        }
+      }
+    }
+    if (valid)
+#pragma unroll
+      for (int j = 0; j < KB; ++j)
+        if (j < kz) J.Z[row + total * j] = acc[j];
+  }
+}
+
+// Grouped first core contraction of the batched path:
+// T1[row + rows a] = sum_i Z[i + np row] Up[i + np a], a < kp <= 64.  The job's
+// blocks stride over tiles of 64 rows (consecutive rows of Z are contiguous);
+// Z and Up staged in 64-wide chunks of i; thread (row t % 64, a = t / 64 + 4 m).
+__global__ void __launch_bounds__(256) core_t1_grouped_kernel(const T1Job *__restrict__ jobs,
+                                                              const int *__restrict__ job_of_block) {
+  __shared__ T1Job J;
+  __shared__ float Zs[64][65];   // [i][row]
+  __shared__ float Us[64][65];   // [i][a]
+  load_job(jobs, job_of_block[blockIdx.x], J);
+  const int t = threadIdx.x, np = J.np, kp = J.kp, rr = t & 63, ag = t >> 6;
+  for (long long r0 = static_cast<long long>(blockIdx.x - J.blk0) * 64; r0 < J.rows; r0 += J.nblk * 64ll) {
+    const int nr = static_cast<int>(min(64ll, J.rows - r0));
+    float acc[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) acc[m] = 0.f;
+    for (int i0 = 0; i0 < np; i0 += 64) {
+      const int ni = min(64, np - i0);
+      __syncthreads();
+      for (int e = t; e < 64 * 64; e += 256) {
+        const int a = e >> 6, ii = e & 63;   // i fastest: contiguous reads of a Z row and of an Up column
+        Zs[ii][a] = (ii < ni && a < nr) ? J.Z[(i0 + ii) + static_cast<long long>(np) * (r0 + a)] : 0.f;
+        Us[ii][a] = (ii < ni && a < kp) ? J.Up[(i0 + ii) + static_cast<long long>(np) * a] : 0.f;
+      }
+      __syncthreads();
+      for (int ii = 0; ii < ni; ++ii) {
+        const float z = Zs[ii][rr];
+#pragma unroll
+        for (int m = 0; m < 16; ++m) acc[m] = fmaf(z, Us[ii][ag + 4 * m], acc[m]);
+      }
+    }
+    if (rr < nr)
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const int a = ag + 4 * m;
+        if (a < kp) J.T1[r0 + rr + J.rows * a] = acc[m];
+      }
+  }
+}
+
+// Grouped second core-contraction step of the batched path: block b is
+// entry c = b - blk0 of job job_of_block[b] (the whole j range).
+__global__ void __launch_bounds__(256) core_step2_grouped_kernel(const Step2Job *__restrict__ jobs,
+                                                                 const int *__restrict__ job_of_block) {
+  __shared__ Step2Job J;
+  if (threadIdx.x == 0) J = jobs[job_of_block[blockIdx.x]];
+  __syncthreads();
+  core_step2_body(J.T1, J.ldt, J.nq, J.kp, J.Uq, J.kq, static_cast<int>(blockIdx.x) - J.blk0, 0, J.nq, J.C);
 }
 
 // out[e] = sum_r part[r * count + e], r in order
@@ -480,6 +579,64 @@ __global__ void __launch_bounds__(256) err_fused_grouped_kernel(const ErrJob *__
                      tb / ntiles);
 }
 
+// Narrow error pass (complementary leaf = the last mode, rows l = i1 + np i2
+// of X contiguous): a thread per row forms W[l, c] = sum_b T[i1 + np (b + kq c)]
+// Uq[i2 + nq b] in registers, then for every i3 the difference
+// X[l + L i3] - sum_c W[l, c] U3[i3 + nc c] (U3 staged in 64-row chunks of
+// shared memory); the compensated sum of squares of a block's rows is its
+// partial (ntile = nblk[4] partials).
+template <int KB>
+__global__ void __launch_bounds__(256) err_narrow_grouped_kernel(const ErrJob *__restrict__ jobs,
+                                                                 const int *__restrict__ job_of_block) {
+  __shared__ ErrJob J;
+  __shared__ float Us[64][KB];
+  __shared__ double red[256];
+  load_job(jobs, job_of_block[blockIdx.x], J);
+  const int t = threadIdx.x, kc = J.kc, np = J.np, kq = J.kq;
+  const long long L = J.R, nc = J.Cn;
+  const long long b = blockIdx.x - J.blk0[4];
+  Acc2 acc = {0.f, 0.f};
+  for (long long base = b * 256; base < L; base += J.nblk[4] * 256ll) {
+    const long long l = base + t;
+    const bool valid = l < L;
+    const int i1 = valid ? static_cast<int>(l % np) : 0, i2 = valid ? static_cast<int>(l / np) : 0;
+    float w[KB];
+#pragma unroll
+    for (int c = 0; c < KB; ++c) {
+      float v = 0.f;
+      if (valid && c < kc)
+        for (int bq = 0; bq < kq; ++bq)
+          v = fmaf(J.Tm[i1 + static_cast<long long>(np) * (bq + static_cast<long long>(kq) * c)],
+                   J.Uq[i2 + static_cast<long long>(J.nq) * bq], v);
+      w[c] = v;
+    }
+    for (long long i0 = 0; i0 < nc; i0 += 64) {
+      const int ni = static_cast<int>(min(64ll, nc - i0));
+      __syncthreads();
+      for (int e = t; e < 64 * KB; e += 256) {
+        const int ii = e / KB, c = e - ii * KB;
+        Us[ii][c] = (ii < ni && c < kc) ? J.B[(i0 + ii) + J.ldb * c] : 0.f;
+      }
+      __syncthreads();
+      if (valid)
+        for (int ii = 0; ii < ni; ++ii) {
+          float xh = 0.f;
+#pragma unroll
+          for (int c = 0; c < KB; ++c) xh = fmaf(w[c], Us[ii][c], xh);
+          const float d = __ldcs(J.X + l + L * (i0 + ii)) - xh;
+          acc2_add_prod(acc, d, d);
+        }
+    }
+  }
+  red[t] = static_cast<double>(acc.s) + static_cast<double>(acc.c);
+  __syncthreads();
+  for (int w2 = 128; w2 > 0; w2 >>= 1) {
+    if (t < w2) red[t] += red[t + w2];
+    __syncthreads();
+  }
+  if (t == 0) J.parts[b] = red[0];
+}
+
 // the sum of a job's tile partials, as sumsq_finish_kernel sums them
 __global__ void err_finish_grouped_kernel(const ErrJob *__restrict__ jobs) {
   const ErrJob &J = jobs[blockIdx.x];
@@ -646,6 +803,31 @@ cudaError_t core_step2_launch(const float *T1, long long ldt, int nq, int kp, co
   return cudaGetLastError();
 }
 
+cudaError_t modeprod_narrow_grouped_launch(const NarrowJob *jobs_dev, const int *job_of_block, int nblocks, int kb,
+                                          cudaStream_t s) {
+  if (nblocks < 1) return cudaSuccess;
+  if (!jobs_dev || !job_of_block) return cudaErrorInvalidValue;
+  if (kb <= 16) modeprod_narrow_grouped_kernel<16><<<nblocks, 256, 0, s>>>(jobs_dev, job_of_block);
+  else if (kb <= 32) modeprod_narrow_grouped_kernel<32><<<nblocks, 256, 0, s>>>(jobs_dev, job_of_block);
+  else if (kb <= 64) modeprod_narrow_grouped_kernel<64><<<nblocks, 256, 0, s>>>(jobs_dev, job_of_block);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t core_t1_grouped_launch(const T1Job *jobs_dev, const int *job_of_block, int nblocks, cudaStream_t s) {
+  if (nblocks < 1) return cudaSuccess;
+  if (!jobs_dev || !job_of_block) return cudaErrorInvalidValue;
+  core_t1_grouped_kernel<<<nblocks, 256, 0, s>>>(jobs_dev, job_of_block);
+  return cudaGetLastError();
+}
+
+cudaError_t core_step2_grouped_launch(const Step2Job *jobs_dev, const int *job_of_block, int nblocks, cudaStream_t s) {
+  if (nblocks < 1) return cudaSuccess;
+  if (!jobs_dev || !job_of_block) return cudaErrorInvalidValue;
+  core_step2_grouped_kernel<<<nblocks, 256, 0, s>>>(jobs_dev, job_of_block);
+  return cudaGetLastError();
+}
+
 cudaError_t expand2_launch(const float *U0, int n0, int k0, const float *core, const float *U1, int n1, int k1, int k2,
                            float *T, float *W, cudaStream_t s) {
   expand_step1_kernel<<<grid_for(static_cast<long long>(n0) * k1 * k2), 256, 0, s>>>(U0, n0, k0, core, k1, k2, T);
@@ -673,15 +855,22 @@ cudaError_t error_fused_launch(const float *X, long long ldx, long long sx, cons
 }
 
 cudaError_t error_grouped_launch(const ErrJob *jobs_dev, int njobs, const int *blocks, const int *const *job_of_block,
-                                 cudaStream_t s) {
+                                 int narrow_kb, cudaStream_t s) {
   if (njobs < 1) return cudaSuccess;
   if (!jobs_dev) return cudaErrorInvalidValue;
-  for (int k = 0; k < 4; ++k)
-    if (blocks[k] < njobs || !job_of_block[k]) return cudaErrorInvalidValue;
+  for (int k = 0; k < 5; ++k)
+    if (blocks[k] > 0 && !job_of_block[k]) return cudaErrorInvalidValue;
+  if (blocks[0] < njobs || blocks[1] < njobs) return cudaErrorInvalidValue;
   err_core_grouped_kernel<<<blocks[0], 256, 0, s>>>(jobs_dev, job_of_block[0]);
   err_expand1_grouped_kernel<<<blocks[1], 256, 0, s>>>(jobs_dev, job_of_block[1]);
-  err_expand2_grouped_kernel<<<blocks[2], 256, 0, s>>>(jobs_dev, job_of_block[2]);
-  err_fused_grouped_kernel<<<blocks[3], 256, 0, s>>>(jobs_dev, job_of_block[3]);
+  if (blocks[2] > 0) err_expand2_grouped_kernel<<<blocks[2], 256, 0, s>>>(jobs_dev, job_of_block[2]);
+  if (blocks[3] > 0) err_fused_grouped_kernel<<<blocks[3], 256, 0, s>>>(jobs_dev, job_of_block[3]);
+  if (blocks[4] > 0) {
+    if (narrow_kb <= 16) err_narrow_grouped_kernel<16><<<blocks[4], 256, 0, s>>>(jobs_dev, job_of_block[4]);
+    else if (narrow_kb <= 32) err_narrow_grouped_kernel<32><<<blocks[4], 256, 0, s>>>(jobs_dev, job_of_block[4]);
+    else if (narrow_kb <= 64) err_narrow_grouped_kernel<64><<<blocks[4], 256, 0, s>>>(jobs_dev, job_of_block[4]);
+    else return cudaErrorInvalidValue;
+  }
   err_finish_grouped_kernel<<<njobs, 256, 0, s>>>(jobs_dev);
   return cudaGetLastError();
 }
