@@ -1,10 +1,11 @@
 """Autotuner of the batched path (``ht_decompose_batched``), per size bucket.
 
-Many small tensors per call are latency-bound chains of kernels spread over
-concurrent streams; what runs fastest depends on the tensor sizes: how many
-streams ("lanes") share the GPU, how many CTAs each lane's cooperative
-eigen-solver takes, and how many subspace iterations and how much oversampling
-the leaf solver needs before the error stops moving.  ``tune_batched`` times
+Batches whose modes are all at most ``GROUPED_MAX_DIM`` run as grouped stages
+(one launch per stage for every tensor); what moves them is how many subspace
+iterations and how much oversampling the leaf solver needs before the error
+stops moving.  Larger tensors run as per-tensor chains spread over concurrent
+streams ("lanes"), where the number of lanes and the CTAs each lane's
+cooperative eigen-solver takes matter as well.  ``tune_batched`` times
 every candidate on a sample batch of a size bucket, keeps the candidates whose
 p99 and maximum relative errors stay within a relative slack of the default
 configuration's, and returns the fastest.  ``tune_table`` does this for a list
@@ -27,6 +28,9 @@ from ._lib import check, lib
 TABLE_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning", "batched_gb300.json")
 DEFAULT = {"lanes": 16, "eig_ctas": 0, "eig_iters": 10, "oversample": 16}
 CANDIDATES = {"lanes": (8, 16, 32), "eig_ctas": (0, 3, 6), "eig_iters": (10, 6, 4), "oversample": (16, 8)}
+# the library groups the stages of a batch whose modes are all at most this
+GROUPED_MAX_DIM = 512
+CANDIDATES_GROUPED = {"lanes": (16,), "eig_ctas": (0,), "eig_iters": (10, 6, 4), "oversample": (16, 8)}
 
 
 def set_launch_shape(lanes: int, eig_ctas: int) -> None:
@@ -58,7 +62,8 @@ def tune_batched(trees: Sequence, dims: Sequence[Sequence[int]], tensors: Sequen
     relative errors exceed the default configuration's by at most a factor
     (1 + err_slack).  Returns the choice, its tensors/s and errors, and the
     default's."""
-    cand = candidates or CANDIDATES
+    grouped = max(max(int(v) for v in d) for d in dims) <= GROUPED_MAX_DIM
+    cand = candidates or (CANDIDATES_GROUPED if grouped else CANDIDATES)
     base_wall, base = _time_config(trees, dims, tensors, DEFAULT, precision, repeats)
     best, best_wall, best_rep = dict(DEFAULT), base_wall, base
     tried = []
@@ -131,4 +136,4 @@ def lookup(dims: Sequence[Sequence[int]], table: Optional[Dict] = None, precisio
 
 
 __all__ = ["tune_batched", "tune_table", "load_table", "lookup", "set_launch_shape", "DEFAULT", "CANDIDATES",
-           "TABLE_PATH"]
+           "CANDIDATES_GROUPED", "GROUPED_MAX_DIM", "TABLE_PATH"]
