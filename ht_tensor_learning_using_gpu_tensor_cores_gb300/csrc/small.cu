@@ -169,12 +169,27 @@ __global__ void __launch_bounds__(256) convert_grouped_kernel(const ConvJob *__r
   load_job(jobs, job_of_block[blockIdx.x], J);
   const int b = blockIdx.x - J.blk0;
   Acc2 a = {0.f, 0.f};
-  const long long total = J.n1p * J.rest;
-  for (long long e = b * 256ll + threadIdx.x; e < total; e += J.nblk * 256ll) {
-    const long long r = e / J.n1p, i = e - r * J.n1p;
-    const float v = i < J.n1 ? __ldcs(J.x + i + J.n1 * r) : 0.f;
-    acc2_add_prod(a, v, v);
-    if (J.xb) J.xb[e] = __float2bfloat16_rn(v);
+  // a warp per row of n1 inputs (n1p outputs), four loads in flight per lane
+  const int lane = threadIdx.x & 31, n1 = static_cast<int>(J.n1), n1p = static_cast<int>(J.n1p);
+  for (long long r = static_cast<long long>(b) * 8 + (threadIdx.x >> 5); r < J.rest; r += J.nblk * 8ll) {
+    const float *src = J.x + J.n1 * r;
+    __nv_bfloat16 *dst = J.xb ? J.xb + J.n1p * r : nullptr;
+    for (int i0 = lane; i0 < n1p; i0 += 128) {
+      float v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = i0 + 32 * u;
+        v[u] = i < n1 ? __ldcs(src + i) : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = i0 + 32 * u;
+        if (i < n1p) {
+          acc2_add_prod(a, v[u], v[u]);
+          if (dst) dst[i] = __float2bfloat16_rn(v[u]);
+        }
+      }
+    }
   }
   __shared__ double red[256];
   red[threadIdx.x] = static_cast<double>(a.s) + static_cast<double>(a.c);
@@ -319,7 +334,7 @@ template <int KB>
 __global__ void __launch_bounds__(256) modeprod_narrow_grouped_kernel(const NarrowJob *__restrict__ jobs,
                                                                       const int *__restrict__ job_of_block) {
   __shared__ NarrowJob J;
-  __shared__ float Vs[64][KB];
+  __shared__ __align__(16) float Vs[64][KB];
   load_job(jobs, job_of_block[blockIdx.x], J);
   const int t = threadIdx.x, kz = J.kz, N = J.N;
   const long long L = J.L, total = J.L * J.R;
@@ -340,10 +355,22 @@ __global__ void __launch_bounds__(256) modeprod_narrow_grouped_kernel(const Narr
       }
       __syncthreads();
       if (valid) {
-        for (int ii = 0; ii < ni; ++ii) {
-          const float xv = __ldg(x + L * (i0 + ii));
+        for (int ii = 0; ii < ni; ii += 8) {
+          float xv[8];   // eight independent loads in flight before the products
 #pragma unroll
-          for (int j = 0; j < KB; ++j) acc[j] = fmaf(xv, Vs[ii][j], acc[j]);
+          for (int u = 0; u < 8; ++u) xv[u] = ii + u < ni ? __ldg(x + L * (i0 + ii + u)) : 0.f;
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const float4 *v4 = reinterpret_cast<const float4 *>(&Vs[(ii + u) & 63][0]);
+#pragma unroll
+            for (int j4 = 0; j4 < KB / 4; ++j4) {
+              const float4 v = v4[j4];
+              acc[4 * j4] = fmaf(xv[u], v.x, acc[4 * j4]);
+              acc[4 * j4 + 1] = fmaf(xv[u], v.y, acc[4 * j4 + 1]);
+              acc[4 * j4 + 2] = fmaf(xv[u], v.z, acc[4 * j4 + 2]);
+              acc[4 * j4 + 3] = fmaf(xv[u], v.w, acc[4 * j4 + 3]);
+            }
+          }
         }
       }
     }
@@ -589,7 +616,7 @@ template <int KB>
 __global__ void __launch_bounds__(256) err_narrow_grouped_kernel(const ErrJob *__restrict__ jobs,
                                                                  const int *__restrict__ job_of_block) {
   __shared__ ErrJob J;
-  __shared__ float Us[64][KB];
+  __shared__ __align__(16) float Us[64][KB];
   __shared__ double red[256];
   load_job(jobs, job_of_block[blockIdx.x], J);
   const int t = threadIdx.x, kc = J.kc, np = J.np, kq = J.kq;
@@ -602,14 +629,15 @@ __global__ void __launch_bounds__(256) err_narrow_grouped_kernel(const ErrJob *_
     const int i1 = valid ? static_cast<int>(l % np) : 0, i2 = valid ? static_cast<int>(l / np) : 0;
     float w[KB];
 #pragma unroll
-    for (int c = 0; c < KB; ++c) {
-      float v = 0.f;
-      if (valid && c < kc)
-        for (int bq = 0; bq < kq; ++bq)
-          v = fmaf(J.Tm[i1 + static_cast<long long>(np) * (bq + static_cast<long long>(kq) * c)],
-                   J.Uq[i2 + static_cast<long long>(J.nq) * bq], v);
-      w[c] = v;
-    }
+    for (int c = 0; c < KB; ++c) w[c] = 0.f;
+    if (valid)
+      for (int bq = 0; bq < kq; ++bq) {   // the KB loads of one bq are independent: issued together
+        const float uq = J.Uq[i2 + static_cast<long long>(J.nq) * bq];
+        const float *tp = J.Tm + i1 + static_cast<long long>(np) * bq;
+        const long long cs = static_cast<long long>(np) * kq;
+#pragma unroll
+        for (int c = 0; c < KB; ++c) w[c] = fmaf(c < kc ? tp[cs * c] : 0.f, uq, w[c]);
+      }
     for (long long i0 = 0; i0 < nc; i0 += 64) {
       const int ni = static_cast<int>(min(64ll, nc - i0));
       __syncthreads();
@@ -619,12 +647,27 @@ __global__ void __launch_bounds__(256) err_narrow_grouped_kernel(const ErrJob *_
       }
       __syncthreads();
       if (valid)
-        for (int ii = 0; ii < ni; ++ii) {
-          float xh = 0.f;
+        for (int ii = 0; ii < ni; ii += 8) {
+          float xv[8];   // eight independent loads in flight before the products
 #pragma unroll
-          for (int c = 0; c < KB; ++c) xh = fmaf(w[c], Us[ii][c], xh);
-          const float d = __ldcs(J.X + l + L * (i0 + ii)) - xh;
-          acc2_add_prod(acc, d, d);
+          for (int u = 0; u < 8; ++u) xv[u] = ii + u < ni ? __ldcs(J.X + l + L * (i0 + ii + u)) : 0.f;
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            if (ii + u < ni) {
+              const float4 *u4 = reinterpret_cast<const float4 *>(&Us[ii + u][0]);
+              float xh = 0.f;
+#pragma unroll
+              for (int c4 = 0; c4 < KB / 4; ++c4) {
+                const float4 v = u4[c4];
+                xh = fmaf(w[4 * c4], v.x, xh);
+                xh = fmaf(w[4 * c4 + 1], v.y, xh);
+                xh = fmaf(w[4 * c4 + 2], v.z, xh);
+                xh = fmaf(w[4 * c4 + 3], v.w, xh);
+              }
+              const float d = xv[u] - xh;
+              acc2_add_prod(acc, d, d);
+            }
+          }
         }
     }
   }
