@@ -485,10 +485,18 @@ struct CoopBatch {
   int *err;
 };
 
-constexpr size_t kCoopRing = size_t(CNS) * (RBMAX + SMAX) * CLD;              // floats
 constexpr size_t kCoopAlias = 2 * ESMAX + 3 * SMAX * (SMAX + 1);                // Sd (doubles) + A + V + A2
-constexpr size_t kCoopSmem =
-    sizeof(float) * (SMAX * SMAX + SMAX + 2 * RBMAX * SMAX + (kCoopRing > kCoopAlias ? kCoopRing : kCoopAlias)) + 64;
+// dynamic shared memory of a solver whose G * Y product runs a `stages`-deep ring
+constexpr size_t coop_smem(int stages) {
+  return sizeof(float) * (SMAX * SMAX + SMAX + 2 * RBMAX * SMAX +
+                          (size_t(stages) * (RBMAX + SMAX) * CLD > kCoopAlias ? size_t(stages) * (RBMAX + SMAX) * CLD
+                                                                                : kCoopAlias)) +
+         64;
+}
+constexpr size_t kCoopSmem = coop_smem(CNS);
+// the grouped solver (a CTA per problem): a 2-stage ring, so that two CTAs share an SM
+constexpr int kGroupedStages = 2;
+constexpr size_t kGroupedSmem = coop_smem(kGroupedStages);
 
 // Bounded grid barrier over the first `members` CTAs.  False (and the error
 // word set) when the wait ran past limit_ns; the caller then returns.
@@ -525,7 +533,7 @@ HT_DEV bool grid_barrier(unsigned *bar, unsigned members, int *err, int *s_ok, u
 // k = 8w .. 8w+7 of every 64-wide chunk, lane l columns l and l + 32, and
 // every row (RT >= rows, padded); the G operand is a broadcast shared-memory
 // load.  The eight partial blocks are summed in a fixed order at the end.
-template <int RT, int NC>
+template <int RT, int NC, int NS>
 HT_DEV void coop_product_t(const float *G, const float *Y, int n, int s, int r0, int rows, float *ring, float *Zs) {
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const bool vec = (n % 4 == 0) && ((reinterpret_cast<uintptr_t>(G) | reinterpret_cast<uintptr_t>(Y)) & 15u) == 0;
@@ -533,7 +541,7 @@ HT_DEV void coop_product_t(const float *G, const float *Y, int n, int s, int r0,
   constexpr int STAGE = (RBMAX + SMAX) * CLD;
   auto issue = [&](int c) {
     const int kc = c * 64;
-    float *Gd = ring + (c % CNS) * STAGE, *Yd = Gd + RBMAX * CLD;
+    float *Gd = ring + (c % NS) * STAGE, *Yd = Gd + RBMAX * CLD;
     if (vec) {
       for (int idx = t; idx < RT * 16; idx += 256) {
         const int i = idx >> 4, k4 = (idx & 15) * 4, kk = kc + k4;
@@ -563,16 +571,16 @@ HT_DEV void coop_product_t(const float *G, const float *Y, int n, int s, int r0,
   for (int r = 0; r < RT; ++r)
 #pragma unroll
     for (int c = 0; c < NC; ++c) acc[r][c] = 0.f;
-  for (int c = 0; c < CNS - 1; ++c) {
+  for (int c = 0; c < NS - 1; ++c) {
     if (c < nchunks) issue(c);
     cp_async_commit();
   }
   for (int c = 0; c < nchunks; ++c) {
-    if (c + CNS - 1 < nchunks) issue(c + CNS - 1);
+    if (c + NS - 1 < nchunks) issue(c + NS - 1);
     cp_async_commit();
-    cp_async_wait<CNS - 1>();
+    cp_async_wait<NS - 1>();
     __syncthreads();
-    const float *Gd = ring + (c % CNS) * STAGE, *Yd = Gd + RBMAX * CLD;
+    const float *Gd = ring + (c % NS) * STAGE, *Yd = Gd + RBMAX * CLD;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int kk = 8 * warp + 4 * h;
@@ -587,7 +595,7 @@ HT_DEV void coop_product_t(const float *G, const float *Y, int n, int s, int r0,
           acc[r][q] = fmaf(g.x, y[q].x, fmaf(g.y, y[q].y, fmaf(g.z, y[q].z, fmaf(g.w, y[q].w, acc[r][q]))));
       }
     }
-    __syncthreads();   // this stage is refilled CNS-1 chunks later
+    __syncthreads();   // this stage is refilled NS-1 chunks later
   }
   cp_async_wait<0>();
   __syncthreads();
@@ -610,17 +618,18 @@ HT_DEV void coop_product_t(const float *G, const float *Y, int n, int s, int r0,
   __syncthreads();
 }
 
+template <int NS>
 HT_DEV void coop_product(const float *G, const float *Y, int n, int s, int r0, int rows, float *ring, float *Zs) {
   if (s <= 32) {
-    if (rows <= 8) coop_product_t<8, 1>(G, Y, n, s, r0, rows, ring, Zs);
-    else if (rows <= 16) coop_product_t<16, 1>(G, Y, n, s, r0, rows, ring, Zs);
-    else if (rows <= 24) coop_product_t<24, 1>(G, Y, n, s, r0, rows, ring, Zs);
-    else coop_product_t<32, 1>(G, Y, n, s, r0, rows, ring, Zs);
+    if (rows <= 8) coop_product_t<8, 1, NS>(G, Y, n, s, r0, rows, ring, Zs);
+    else if (rows <= 16) coop_product_t<16, 1, NS>(G, Y, n, s, r0, rows, ring, Zs);
+    else if (rows <= 24) coop_product_t<24, 1, NS>(G, Y, n, s, r0, rows, ring, Zs);
+    else coop_product_t<32, 1, NS>(G, Y, n, s, r0, rows, ring, Zs);
   } else {
-    if (rows <= 8) coop_product_t<8, 2>(G, Y, n, s, r0, rows, ring, Zs);
-    else if (rows <= 16) coop_product_t<16, 2>(G, Y, n, s, r0, rows, ring, Zs);
-    else if (rows <= 24) coop_product_t<24, 2>(G, Y, n, s, r0, rows, ring, Zs);
-    else coop_product_t<32, 2>(G, Y, n, s, r0, rows, ring, Zs);
+    if (rows <= 8) coop_product_t<8, 2, NS>(G, Y, n, s, r0, rows, ring, Zs);
+    else if (rows <= 16) coop_product_t<16, 2, NS>(G, Y, n, s, r0, rows, ring, Zs);
+    else if (rows <= 24) coop_product_t<24, 2, NS>(G, Y, n, s, r0, rows, ring, Zs);
+    else coop_product_t<32, 2, NS>(G, Y, n, s, r0, rows, ring, Zs);
   }
 }
 
@@ -933,6 +942,7 @@ HT_DEV void coop_load_S(const CoopProb &P, double *Sd) {
 // One CholeskyQR-type step over the CTA's rows: X = src rows (optionally
 // G * src + mu src), apply the current transform Rs (unless identity), store to dst,
 // accumulate the Gram partial.  mode 0: ITER, 1: APPLY, 2: RR (also Q rows).
+template <int NS>
 HT_DEV void coop_step(const CoopProb &P, int cl, int mode, const float *src, float *dst, float *dst2, bool ident,
                       float mu, const float *Rs, float *Zs, float *Qr, float *ring, bool want_s = true) {
   Acc2 acc[kMaxEntPerThread];
@@ -943,7 +953,7 @@ HT_DEV void coop_step(const CoopProb &P, int cl, int mode, const float *src, flo
     const int rows = min(RBMAX, re - r0);
     coop_load_rows(src, P.n, P.s, r0, rows, Qr);
     if (mode != 1) {
-      coop_product(P.G, src, P.n, P.s, r0, rows, ring, Zs);
+      coop_product<NS>(P.G, src, P.n, P.s, r0, rows, ring, Zs);
       if (mode == 0)
         for (int e = threadIdx.x; e < RBMAX * SMAX; e += 256) Zs[e] = fmaf(mu, Qr[e], Zs[e]);
     } else {
@@ -1123,7 +1133,7 @@ struct LocalSync {
 
 // Subspace iteration, Rayleigh-Ritz and the final U / GU / residual of one
 // problem; CTA `cl` of the problem's P.ncta owns rows [cl * P.rows, ...).
-template <class Sync>
+template <class Sync, int NS>
 HT_DEV void eig_iterate(const CoopProb &P, int cl, const Sync &sy, int iters, int refine, const EigSmem &m) {
   const int t = threadIdx.x;
   float *Rs = m.Rs, *Zs = m.Zs, *Qr = m.Qr, *ring = m.ring, *red = m.red;
@@ -1164,7 +1174,7 @@ HT_DEV void eig_iterate(const CoopProb &P, int cl, const Sync &sy, int iters, in
   int cur = 0;
   bool ident = true;
   for (int it = 0; it < iters; ++it) {
-    coop_step(P, cl, 0, P.buf[cur], P.buf[cur ^ 1], nullptr, ident, mu, Rs, Zs, Qr, ring);
+    coop_step<NS>(P, cl, 0, P.buf[cur], P.buf[cur ^ 1], nullptr, ident, mu, Rs, Zs, Qr, ring);
     if (!reduce_and_factor(1e-12)) return;
     ident = false;
     cur ^= 1;
@@ -1176,20 +1186,20 @@ HT_DEV void eig_iterate(const CoopProb &P, int cl, const Sync &sy, int iters, in
   // Y_L loses digits to cancellation.
   // The FP32 path asks for `refine` CholeskyQR passes on Q_L all the same
   // (orthonormal to FP32 rounding, the last digit of its error).
-  coop_step(P, cl, 1, P.buf[cur], P.buf[2], nullptr, ident, 0.f, Rs, Zs, Qr, ring, ident || refine > 0);
+  coop_step<NS>(P, cl, 1, P.buf[cur], P.buf[2], nullptr, ident, 0.f, Rs, Zs, Qr, ring, ident || refine > 0);
   bool rr_ident = true;
   if (ident || refine > 0) {   // ident: no iteration ran, orthonormalise the start block
     if (!reduce_and_factor(1e-12)) return;
     rr_ident = false;
     for (int r = 1; r < refine; ++r) {   // row-local, so in place
-      coop_step(P, cl, 1, P.buf[2], P.buf[2], nullptr, false, 0.f, Rs, Zs, Qr, ring);
+      coop_step<NS>(P, cl, 1, P.buf[2], P.buf[2], nullptr, false, 0.f, Rs, Zs, Qr, ring);
       if (!reduce_and_factor(1e-14)) return;
     }
   } else if (!sy.bar()) {
     return;
   }
   // Rayleigh-Ritz: Q -> buf3, G Q -> buf0, H = Q^T G Q
-  coop_step(P, cl, 2, P.buf[2], P.buf[3], P.buf[0], rr_ident, 0.f, Rs, Zs, Qr, ring);
+  coop_step<NS>(P, cl, 2, P.buf[2], P.buf[3], P.buf[0], rr_ident, 0.f, Rs, Zs, Qr, ring);
   if (!sy.bar()) return;
   sy.reduce();
   if (!sy.bar()) return;
@@ -1267,7 +1277,7 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const __grid_constant_
     double *A64 = m.Sd + ESMAX;
     for (int pass = 0; pass <= B.orth_passes; ++pass) {
       // row-local: in place; the last pass only applies the transform
-      coop_step(P, cl, 1, Q, Q, nullptr, pass == 0, 0.f, m.Rs, m.Zs, m.Qr, m.ring, pass < B.orth_passes);
+      coop_step<CNS>(P, cl, 1, Q, Q, nullptr, pass == 0, 0.f, m.Rs, m.Zs, m.Qr, m.ring, pass < B.orth_passes);
       if (pass == B.orth_passes) break;
       if (!grid_barrier(B.bar, members, B.err, m.s_ok)) return;
       coop_reduce(B);
@@ -1279,13 +1289,13 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const __grid_constant_
     return;
   }
   const CoopSync sy{&B, members, m.s_ok};
-  eig_iterate(P, cl, sy, B.iters, B.refine, m);
+  eig_iterate<CoopSync, CNS>(P, cl, sy, B.iters, B.refine, m);
 }
 
 // Grouped solver of the batched path: CTA b solves problem tab[b] alone (all
 // of its rows, block barriers only), so one ordinary launch covers every leaf
 // of every tensor of a batch and no CTA waits on another.
-__global__ void __launch_bounds__(256, 1) eig_grouped_kernel(const CoopProb *__restrict__ tab, int iters, int refine) {
+__global__ void __launch_bounds__(256, 2) eig_grouped_kernel(const CoopProb *__restrict__ tab, int iters, int refine) {
   extern __shared__ __align__(16) float sm[];
   const EigSmem m = eig_smem(sm);
   __shared__ CoopProb sP;
@@ -1297,7 +1307,7 @@ __global__ void __launch_bounds__(256, 1) eig_grouped_kernel(const CoopProb *__r
     return;
   }
   const LocalSync sy{&P};
-  eig_iterate(P, 0, sy, iters, refine, m);
+  eig_iterate<LocalSync, kGroupedStages>(P, 0, sy, iters, refine, m);
 }
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -1344,7 +1354,8 @@ cudaError_t eig_prepare() {
   cudaError_t e = cudaFuncSetAttribute(transfer_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            static_cast<int>(kJacScratch));
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(eig_grouped_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kCoopSmem));
+  e = cudaFuncSetAttribute(eig_grouped_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(kGroupedSmem));
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(svd_from_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               static_cast<int>(kJacScratch));
@@ -1496,7 +1507,7 @@ void eig_grouped_order(std::vector<unsigned char> &table) {
 cudaError_t eig_grouped_launch(const void *table_dev, int nprob, int iters, int refine, cudaStream_t st) {
   if (nprob <= 0) return cudaSuccess;
   if (!table_dev || (reinterpret_cast<uintptr_t>(table_dev) % alignof(CoopProb)) != 0) return cudaErrorInvalidValue;
-  eig_grouped_kernel<<<nprob, 256, kCoopSmem, st>>>(static_cast<const CoopProb *>(table_dev), iters,
+  eig_grouped_kernel<<<nprob, 256, kGroupedSmem, st>>>(static_cast<const CoopProb *>(table_dev), iters,
                                                     refine < 0 ? 0 : (refine > 2 ? 2 : refine));
   return cudaGetLastError();
 }
