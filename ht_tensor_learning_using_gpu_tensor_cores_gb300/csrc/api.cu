@@ -1179,14 +1179,15 @@ ht_status_t error_core(Ctx &c, const Tree &T, const float *x32, const long *dims
       if (j.narrow) {
         j.nblk[2] = j.nblk[3] = 0;
         j.nblk[4] = static_cast<int>(std::min<long long>(32, (Rr + 255) / 256));
+        j.nblk[5] = P.kc * static_cast<int>((np_ + 255) / 256);
         j.ntile = j.nblk[4];
       } else {
         j.nblk[2] = blocks(np_ * nq_ * P.kc, 32);
         j.nblk[3] = std::min(nb, 32);
-        j.nblk[4] = 0;
+        j.nblk[4] = j.nblk[5] = 0;
         j.ntile = nb;
       }
-      for (int k = 0; k < 5; ++k) j.blk0[k] = 0;
+      for (int k = 0; k < 6; ++k) j.blk0[k] = 0;
       c.err_out->push_back(j);
     }
     if (!c.dry()) {
@@ -1900,9 +1901,9 @@ struct BatchLayout {
   int nconv = 0, conv_blocks = 0, ncopy = 0;   // grouped conversion jobs (their blocks), output copies
   int ngram[2] = {0, 0};                       // grouped Grams per class
   int ntail = 0, nerr = 0;                     // grouped transfer tails and error passes
-  int err_blocks[5] = {};                      // launch sizes of the error steps
-  int err_narrow_kb = 0;                       // widest kc of the narrow error jobs
-  size_t map_off[7] = {};                      // ints into BatchState::maps: conversion, step 2, error steps 0-4
+  int err_blocks[6] = {};                      // launch sizes of the error steps
+  int err_narrow_kb = 0, err_narrow_kq = 0;    // widest kc and kq of the narrow error jobs
+  size_t map_off[8] = {};                      // ints into BatchState::maps: conversion, step 2, error steps 0-5
   int ncore_blocks[2] = {0, 0}, nstep2_blocks = 0;   // grouped core pass: GEMM tiles per group, step-2 blocks
   size_t core_params = 0;                      // bytes of GEMM parameters before the tiles in BatchState::core
   int nnarrow_blocks = 0, narrow_kb = 0, nt1_blocks = 0;   // narrow mode products (their widest kz), T1 blocks
@@ -2063,11 +2064,11 @@ ht_status_t batch_enqueue(BatchState &b, const BatchLayout &L, cudaStream_t st, 
   b.launches += L.ntail > 0 ? 1 : 0;
   HT_CUDA(cudaEventRecordWithFlags(b.tp[3], st, cudaEventRecordExternal));
   if (L.nerr > 0) {
-    const int *emaps[5] = {maps + L.map_off[2], maps + L.map_off[3], maps + L.map_off[4], maps + L.map_off[5],
-                           maps + L.map_off[6]};
+    const int *emaps[6];
+    for (int k = 0; k < 6; ++k) emaps[k] = maps + L.map_off[2 + k];
     HT_CUDA(error_grouped_launch(static_cast<const ErrJob *>(b.errs), L.nerr, L.err_blocks, emaps, L.err_narrow_kb,
-                                 st));
-    for (int k = 0; k < 5; ++k) b.launches += L.err_blocks[k] > 0 ? 1 : 0;
+                                 L.err_narrow_kq, st));
+    for (int k = 0; k < 6; ++k) b.launches += L.err_blocks[k] > 0 ? 1 : 0;
     b.launches += 1;
   }
   HT_TRY(batch_pass(b, L, 3, st, count, x, dims, order, trees, cfg, U, B, want_err, eig_ctas));
@@ -2138,7 +2139,7 @@ ht_status_t batch_plan_grouped(BatchState &b, BatchLayout &L, int count, const f
   L.nt1_blocks = blk;
   HT_TRY(upload_table(b.narrow, b.narrow_bytes, P.narrow.data(), sizeof(NarrowJob) * P.narrow.size()));
   HT_TRY(upload_table(b.t1jobs, b.t1jobs_bytes, P.t1.data(), sizeof(T1Job) * P.t1.size()));
-  for (int k = 0; k < 5; ++k) {
+  for (int k = 0; k < 6; ++k) {
     L.map_off[2 + k] = maps.size();
     int eb = 0;
     for (size_t i = 0; i < P.errs.size(); ++i) {
@@ -2148,9 +2149,12 @@ ht_status_t batch_plan_grouped(BatchState &b, BatchLayout &L, int count, const f
     }
     L.err_blocks[k] = eb;
   }
-  L.err_narrow_kb = 0;
+  L.err_narrow_kb = L.err_narrow_kq = 0;
   for (const ErrJob &j : P.errs)
-    if (j.narrow) L.err_narrow_kb = std::max(L.err_narrow_kb, j.kc);
+    if (j.narrow) {
+      L.err_narrow_kb = std::max(L.err_narrow_kb, j.kc);
+      L.err_narrow_kq = std::max(L.err_narrow_kq, j.kq);
+    }
   L.nerr = static_cast<int>(P.errs.size());
   L.ntail = static_cast<int>(P.tails.size());
   // core pass: the GEMM parameters, then group 0's tiles, then group 1's

@@ -177,9 +177,10 @@ struct ConvJob {
 // 0) and the first expansion step into Tm (1) for every job; then either the
 // second expansion step into Wm (2) and the fused error tiles (3, as
 // error_fused_launch, ntile = tiles x slabs of X) or, for a narrow job (the
-// complementary leaf is the last mode, kc <= narrow_kb <= 64), the narrow
-// error kernel (4, W formed per row, ntile = nblk[4] partials); then the sum
-// of the partials into out[0].  blk0[k] / nblk[k]: the job's blocks in launch
+// complementary leaf is the last mode, kc <= narrow_kb <= 64, kq <= narrow_kq
+// <= 64), the second expansion step as small products (5, a block per (c, 256
+// values of i1)) and the narrow error kernel (4, ntile = nblk[4] partials);
+// then the sum of the partials into out[0].  blk0[k] / nblk[k]: the job's blocks in launch
 // k (grid-stride within the job, 0 when it takes no part); blocks[k] = the
 // launch sizes and job_of_block[k] (device) the job of each block of launch
 // k.  Job table in device memory.
@@ -191,10 +192,10 @@ struct ErrJob {
   double *parts, *out;
   long long kpq, ldx, sx, lda, sa, ldb, R, Cn;
   int kt, kc, t_is_left, np, nq, kp, kq, kk, slabs, ntile, narrow;
-  int blk0[5], nblk[5];
+  int blk0[6], nblk[6];
 };
 cudaError_t error_grouped_launch(const ErrJob *jobs_dev, int njobs, const int *blocks, const int *const *job_of_block,
-                                 int narrow_kb, cudaStream_t s);
+                                 int narrow_kb, int narrow_kq, cudaStream_t s);
 // Grouped narrow mode product (3rd-order core pass, rows of X contiguous,
 // L >= 32): Z[row + L R j] = sum_i X[l + L (i + N r)] V[i + N j], row = l + L r,
 // j < kz <= kb (kb <= 64, the largest kz of the launch).  Blocks

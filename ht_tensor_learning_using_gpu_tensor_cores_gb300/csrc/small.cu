@@ -606,9 +606,46 @@ __global__ void __launch_bounds__(256) err_fused_grouped_kernel(const ErrJob *__
                      tb / ntiles);
 }
 
+// Expansion of a narrow error job: W[i1 + np i2 + L c] = sum_b T[i1 + np (b + kq c)]
+// Uq[i2 + nq b] (L = np nq), kq <= KQ.  Block (c, i1 range of 256): a thread
+// per i1 keeps its row of T_c in registers, Uq is staged in 64-row chunks of
+// shared memory, and the thread loops over every i2.
+template <int KQ>
+__global__ void __launch_bounds__(256) err_expand2w_grouped_kernel(const ErrJob *__restrict__ jobs,
+                                                                   const int *__restrict__ job_of_block) {
+  __shared__ ErrJob J;
+  __shared__ float Us[64][KQ + 1];
+  load_job(jobs, job_of_block[blockIdx.x], J);
+  const int np = J.np, nq = J.nq, kq = J.kq, t = threadIdx.x;
+  const int chunks = (np + 255) / 256;
+  const int b = blockIdx.x - J.blk0[5], c = b / chunks, i1 = (b - c * chunks) * 256 + t;
+  const bool valid = i1 < np;
+  const long long L = static_cast<long long>(np) * nq;
+  float tr[KQ];
+#pragma unroll
+  for (int q = 0; q < KQ; ++q)
+    tr[q] = (valid && q < kq) ? J.Tm[i1 + static_cast<long long>(np) * (q + static_cast<long long>(kq) * c)] : 0.f;
+  for (int j0 = 0; j0 < nq; j0 += 64) {
+    const int nj = min(64, nq - j0);
+    __syncthreads();
+    for (int e = t; e < 64 * KQ; e += 256) {
+      const int jj = e / KQ, q = e - jj * KQ;
+      Us[jj][q] = (jj < nj && q < kq) ? J.Uq[(j0 + jj) + static_cast<long long>(nq) * q] : 0.f;
+    }
+    __syncthreads();
+    if (valid)
+      for (int jj = 0; jj < nj; ++jj) {
+        float v = 0.f;
+#pragma unroll
+        for (int q = 0; q < KQ; ++q) v = fmaf(tr[q], Us[jj][q], v);
+        J.Wm[i1 + static_cast<long long>(np) * (j0 + jj) + L * c] = v;
+      }
+  }
+}
+
 // Narrow error pass (complementary leaf = the last mode, rows l = i1 + np i2
-// of X contiguous): a thread per row forms W[l, c] = sum_b T[i1 + np (b + kq c)]
-// Uq[i2 + nq b] in registers, then for every i3 the difference
+// of X contiguous): a thread per row takes its row W[l, :] of the expansion,
+// then for every i3 the difference
 // X[l + L i3] - sum_c W[l, c] U3[i3 + nc c] (U3 staged in 64-row chunks of
 // shared memory); the compensated sum of squares of a block's rows is its
 // partial (ntile = nblk[4] partials).
@@ -627,17 +664,9 @@ __global__ void __launch_bounds__(256) err_narrow_grouped_kernel(const ErrJob *_
     const long long l = base + t;
     const bool valid = l < L;
     const int i1 = valid ? static_cast<int>(l % np) : 0, i2 = valid ? static_cast<int>(l / np) : 0;
-    float w[KB];
+    float w[KB];   // this row of the expansion (err_expand2w_grouped_kernel)
 #pragma unroll
-    for (int c = 0; c < KB; ++c) w[c] = 0.f;
-    if (valid)
-      for (int bq = 0; bq < kq; ++bq) {   // the KB loads of one bq are independent: issued together
-        const float uq = J.Uq[i2 + static_cast<long long>(J.nq) * bq];
-        const float *tp = J.Tm + i1 + static_cast<long long>(np) * bq;
-        const long long cs = static_cast<long long>(np) * kq;
-#pragma unroll
-        for (int c = 0; c < KB; ++c) w[c] = fmaf(c < kc ? tp[cs * c] : 0.f, uq, w[c]);
-      }
+    for (int c = 0; c < KB; ++c) w[c] = (valid && c < kc) ? J.Wm[l + L * c] : 0.f;
     for (long long i0 = 0; i0 < nc; i0 += 64) {
       const int ni = static_cast<int>(min(64ll, nc - i0));
       __syncthreads();
@@ -898,14 +927,20 @@ cudaError_t error_fused_launch(const float *X, long long ldx, long long sx, cons
 }
 
 cudaError_t error_grouped_launch(const ErrJob *jobs_dev, int njobs, const int *blocks, const int *const *job_of_block,
-                                 int narrow_kb, cudaStream_t s) {
+                                 int narrow_kb, int narrow_kq, cudaStream_t s) {
   if (njobs < 1) return cudaSuccess;
   if (!jobs_dev) return cudaErrorInvalidValue;
-  for (int k = 0; k < 5; ++k)
+  for (int k = 0; k < 6; ++k)
     if (blocks[k] > 0 && !job_of_block[k]) return cudaErrorInvalidValue;
   if (blocks[0] < njobs || blocks[1] < njobs) return cudaErrorInvalidValue;
   err_core_grouped_kernel<<<blocks[0], 256, 0, s>>>(jobs_dev, job_of_block[0]);
   err_expand1_grouped_kernel<<<blocks[1], 256, 0, s>>>(jobs_dev, job_of_block[1]);
+  if (blocks[5] > 0) {
+    if (narrow_kq <= 16) err_expand2w_grouped_kernel<16><<<blocks[5], 256, 0, s>>>(jobs_dev, job_of_block[5]);
+    else if (narrow_kq <= 32) err_expand2w_grouped_kernel<32><<<blocks[5], 256, 0, s>>>(jobs_dev, job_of_block[5]);
+    else if (narrow_kq <= 64) err_expand2w_grouped_kernel<64><<<blocks[5], 256, 0, s>>>(jobs_dev, job_of_block[5]);
+    else return cudaErrorInvalidValue;
+  }
   if (blocks[2] > 0) err_expand2_grouped_kernel<<<blocks[2], 256, 0, s>>>(jobs_dev, job_of_block[2]);
   if (blocks[3] > 0) err_fused_grouped_kernel<<<blocks[3], 256, 0, s>>>(jobs_dev, job_of_block[3]);
   if (blocks[4] > 0) {
