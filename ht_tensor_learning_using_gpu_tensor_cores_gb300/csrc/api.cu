@@ -1906,7 +1906,7 @@ struct BatchLayout {
   size_t map_off[8] = {};                      // ints into BatchState::maps: conversion, step 2, error steps 0-5
   int ncore_blocks[2] = {0, 0}, nstep2_blocks = 0;   // grouped core pass: GEMM tiles per group, step-2 blocks
   size_t core_params = 0;                      // bytes of GEMM parameters before the tiles in BatchState::core
-  int nnarrow_blocks = 0, narrow_kb = 0, nt1_blocks = 0;   // narrow mode products (their widest kz), T1 blocks
+  int nnarrow_blocks = 0, narrow_kb = 0, nt1_blocks = 0, t1_kp = 0;   // narrow mode products (widest kz), T1 (widest kp)
   size_t map_narrow = 0, map_t1 = 0;           // their block -> job maps in BatchState::maps
 };
 // Leaves of at most this size go through the grouped solver (one CTA each);
@@ -2052,7 +2052,7 @@ ht_status_t batch_enqueue(BatchState &b, const BatchLayout &L, cudaStream_t st, 
     HT_CUDA(modeprod_narrow_grouped_launch(static_cast<const NarrowJob *>(b.narrow), maps + L.map_narrow,
                                            L.nnarrow_blocks, L.narrow_kb, st));
     HT_CUDA(simt_grouped_launch(params, tiles, L.ncore_blocks[0], st));
-    HT_CUDA(core_t1_grouped_launch(static_cast<const T1Job *>(b.t1jobs), maps + L.map_t1, L.nt1_blocks, st));
+    HT_CUDA(core_t1_grouped_launch(static_cast<const T1Job *>(b.t1jobs), maps + L.map_t1, L.nt1_blocks, L.t1_kp, st));
     HT_CUDA(simt_grouped_launch(params, tiles + L.ncore_blocks[0], L.ncore_blocks[1], st));
     HT_CUDA(core_step2_grouped_launch(static_cast<const Step2Job *>(b.step2), maps + L.map_off[1], L.nstep2_blocks,
                                       st));
@@ -2134,6 +2134,7 @@ ht_status_t batch_plan_grouped(BatchState &b, BatchLayout &L, int count, const f
   for (size_t j = 0; j < P.t1.size(); ++j) {
     P.t1[j].blk0 = blk;
     blk += P.t1[j].nblk;
+    L.t1_kp = std::max(L.t1_kp, P.t1[j].kp);
     maps.insert(maps.end(), P.t1[j].nblk, static_cast<int>(j));
   }
   L.nt1_blocks = blk;

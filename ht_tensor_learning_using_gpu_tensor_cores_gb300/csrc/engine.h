@@ -216,7 +216,9 @@ struct T1Job {
   long long rows;
   int np, kp, blk0, nblk;
 };
-cudaError_t core_t1_grouped_launch(const T1Job *jobs_dev, const int *job_of_block, int nblocks, cudaStream_t s);
+// kp_max: the largest kp of the launch's jobs
+cudaError_t core_t1_grouped_launch(const T1Job *jobs_dev, const int *job_of_block, int nblocks, int kp_max,
+                                   cudaStream_t s);
 // Grouped second core-contraction step (C[a, b, c] = sum_j T1[(j + nq c) +
 // ldt a] Uq[j + nq b], as core_step2_launch without j ranges): job j owns the
 // blocks [blk0, blk0 + kc) of the launch, one per c; job_of_block (device)

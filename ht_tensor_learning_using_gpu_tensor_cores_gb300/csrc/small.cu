@@ -384,7 +384,9 @@ __global__ void __launch_bounds__(256) modeprod_narrow_grouped_kernel(const Narr
 // Grouped first core contraction of the batched path:
 // T1[row + rows a] = sum_i Z[i + np row] Up[i + np a], a < kp <= 64.  The job's
 // blocks stride over tiles of 64 rows (consecutive rows of Z are contiguous);
-// Z and Up staged in 64-wide chunks of i; thread (row t % 64, a = t / 64 + 4 m).
+// Z and Up staged in 64-wide chunks of i; thread (row t % 64, a = t / 64 + 4 m),
+// m < M (kp <= 4 M).
+template <int M>
 __global__ void __launch_bounds__(256) core_t1_grouped_kernel(const T1Job *__restrict__ jobs,
                                                               const int *__restrict__ job_of_block) {
   __shared__ T1Job J;
@@ -394,27 +396,27 @@ __global__ void __launch_bounds__(256) core_t1_grouped_kernel(const T1Job *__res
   const int t = threadIdx.x, np = J.np, kp = J.kp, rr = t & 63, ag = t >> 6;
   for (long long r0 = static_cast<long long>(blockIdx.x - J.blk0) * 64; r0 < J.rows; r0 += J.nblk * 64ll) {
     const int nr = static_cast<int>(min(64ll, J.rows - r0));
-    float acc[16];
+    float acc[M];
 #pragma unroll
-    for (int m = 0; m < 16; ++m) acc[m] = 0.f;
+    for (int m = 0; m < M; ++m) acc[m] = 0.f;
     for (int i0 = 0; i0 < np; i0 += 64) {
       const int ni = min(64, np - i0);
       __syncthreads();
       for (int e = t; e < 64 * 64; e += 256) {
         const int a = e >> 6, ii = e & 63;   // i fastest: contiguous reads of a Z row and of an Up column
         Zs[ii][a] = (ii < ni && a < nr) ? J.Z[(i0 + ii) + static_cast<long long>(np) * (r0 + a)] : 0.f;
-        Us[ii][a] = (ii < ni && a < kp) ? J.Up[(i0 + ii) + static_cast<long long>(np) * a] : 0.f;
+        if (a < 4 * M) Us[ii][a] = (ii < ni && a < kp) ? J.Up[(i0 + ii) + static_cast<long long>(np) * a] : 0.f;
       }
       __syncthreads();
       for (int ii = 0; ii < ni; ++ii) {
         const float z = Zs[ii][rr];
 #pragma unroll
-        for (int m = 0; m < 16; ++m) acc[m] = fmaf(z, Us[ii][ag + 4 * m], acc[m]);
+        for (int m = 0; m < M; ++m) acc[m] = fmaf(z, Us[ii][ag + 4 * m], acc[m]);
       }
     }
     if (rr < nr)
 #pragma unroll
-      for (int m = 0; m < 16; ++m) {
+      for (int m = 0; m < M; ++m) {
         const int a = ag + 4 * m;
         if (a < kp) J.T1[r0 + rr + J.rows * a] = acc[m];
       }
@@ -886,10 +888,14 @@ cudaError_t modeprod_narrow_grouped_launch(const NarrowJob *jobs_dev, const int 
   return cudaGetLastError();
 }
 
-cudaError_t core_t1_grouped_launch(const T1Job *jobs_dev, const int *job_of_block, int nblocks, cudaStream_t s) {
+cudaError_t core_t1_grouped_launch(const T1Job *jobs_dev, const int *job_of_block, int nblocks, int kp_max,
+                                   cudaStream_t s) {
   if (nblocks < 1) return cudaSuccess;
   if (!jobs_dev || !job_of_block) return cudaErrorInvalidValue;
-  core_t1_grouped_kernel<<<nblocks, 256, 0, s>>>(jobs_dev, job_of_block);
+  if (kp_max <= 16) core_t1_grouped_kernel<4><<<nblocks, 256, 0, s>>>(jobs_dev, job_of_block);
+  else if (kp_max <= 32) core_t1_grouped_kernel<8><<<nblocks, 256, 0, s>>>(jobs_dev, job_of_block);
+  else if (kp_max <= 64) core_t1_grouped_kernel<16><<<nblocks, 256, 0, s>>>(jobs_dev, job_of_block);
+  else return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 
