@@ -144,3 +144,17 @@ def test_batched_grouped_gram_classes(prec):
         pairs.append((synth.exact_ht(d, tree, noise_rel=1e-3, seed=500 + i), tree))
     rep = _check_batch(pairs, prec)
     assert rep["grouped"]
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_batched_other_trees_take_the_general_grouped_paths(prec):
+    """Trees {1},{2,3} and {2},{1,3}: the complementary leaf is not the last
+    mode, so the grouped core pass runs FP32 tiles and the error pass the
+    expansion + fused tiles; mixed with reference-tree tensors in one batch."""
+    pairs = []
+    trees = [ht.left_first_tree_3d, ht.middle_tree_3d, ht.reference_tree_3d, ht.left_first_tree_3d]
+    for i, (tf, d) in enumerate(zip(trees, [(40, 52, 36), (61, 33, 47), (48, 40, 56), (130, 24, 40)])):
+        tree = tf([1, 9, 8, 7, 6])
+        pairs.append((synth.exact_ht(d, tree, noise_rel=1e-3, seed=600 + i), tree))
+    rep = _check_batch(pairs, prec)
+    assert rep["grouped"]
