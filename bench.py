@@ -249,7 +249,9 @@ def secondary_configs(ht, synth, torch, stream, steps=10, warmup=3):
         out[name] = rec
         del X
     # c4: 512 tensors, dims ~ U[32, 160], ranks ~ U[8, 16], exact HT + 1e-3 noise,
-    # through the batched C ABI (the recorded CUDA graph replayed on fixed buffers)
+    # through the batched C ABI (the recorded CUDA graph replayed on fixed buffers;
+    # every stage one launch for the whole batch); tensors/s from the host's wall
+    # clock per call (graph launch, error readback), device time beside it
     fam = synth.batch_family(512, seed=31, device="cuda")
     trees = [t for _, t in fam]
     xs = [x for x, _ in fam]
@@ -274,7 +276,8 @@ def secondary_configs(ht, synth, torch, stream, steps=10, warmup=3):
         rec[key] = {"tensors_per_s": len(xs) / wall, "ms_per_batch": wall * 1e3,
                     "device_ms_per_batch": statistics.median(dev_ms), "rel_err_p50": rep["rel_err_p50"],
                     "rel_err_p99": rep["rel_err_p99"], "graph_replayed": rep["graph_replayed"],
-                    "lanes": rep["lanes"], "gpu_launches_per_batch": rep["gpu_launches"]}
+                    "lanes": rep["lanes"], "gpu_launches_per_batch": rep["gpu_launches"],
+                    "grouped_stages": rep["grouped"], "device_ms_per_phase": rep["ms_phase"]}
         del bd
     ht.release_batch()
     out["c4"] = rec
