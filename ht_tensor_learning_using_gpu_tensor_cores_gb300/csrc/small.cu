@@ -381,20 +381,16 @@ __global__ void __launch_bounds__(256) modeprod_narrow_grouped_kernel(const Narr
   }
 }
 
-// Grouped first core contraction of the batched path:
-// T1[row + rows a] = sum_i Z[i + np row] Up[i + np a], a < kp <= 64.  The job's
-// blocks stride over tiles of 64 rows (consecutive rows of Z are contiguous);
-// Z and Up staged in 64-wide chunks of i; thread (row t % 64, a = t / 64 + 4 m),
-// m < M (kp <= 4 M).
+// First core contraction: T1[row + rows a] = sum_i Z[i + np row] Up[i + np a],
+// a < kp <= 4 M.  Block `blk` of `nblk` strides over tiles of 64 rows
+// (consecutive rows of Z are contiguous); Z and Up staged in 64-wide chunks of
+// i; thread (row t % 64, a = t / 64 + 4 m).
 template <int M>
-__global__ void __launch_bounds__(256) core_t1_grouped_kernel(const T1Job *__restrict__ jobs,
-                                                              const int *__restrict__ job_of_block) {
-  __shared__ T1Job J;
+HT_DEV void core_t1_body(const T1Job &J, long long blk, long long nblk) {
   __shared__ float Zs[64][65];   // [i][row]
   __shared__ float Us[64][65];   // [i][a]
-  load_job(jobs, job_of_block[blockIdx.x], J);
   const int t = threadIdx.x, np = J.np, kp = J.kp, rr = t & 63, ag = t >> 6;
-  for (long long r0 = static_cast<long long>(blockIdx.x - J.blk0) * 64; r0 < J.rows; r0 += J.nblk * 64ll) {
+  for (long long r0 = blk * 64; r0 < J.rows; r0 += nblk * 64) {
     const int nr = static_cast<int>(min(64ll, J.rows - r0));
     float acc[M];
 #pragma unroll
@@ -421,6 +417,15 @@ __global__ void __launch_bounds__(256) core_t1_grouped_kernel(const T1Job *__res
         if (a < kp) J.T1[r0 + rr + J.rows * a] = acc[m];
       }
   }
+}
+
+// Grouped (batched path): the job of block b is job_of_block[b].
+template <int M>
+__global__ void __launch_bounds__(256) core_t1_grouped_kernel(const T1Job *__restrict__ jobs,
+                                                              const int *__restrict__ job_of_block) {
+  __shared__ T1Job J;
+  load_job(jobs, job_of_block[blockIdx.x], J);
+  core_t1_body<M>(J, blockIdx.x - J.blk0, J.nblk);
 }
 
 // Grouped second core-contraction step of the batched path: block b is
