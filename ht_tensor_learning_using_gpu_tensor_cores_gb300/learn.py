@@ -15,7 +15,7 @@ the three n x n by n x s products in FP32, the s x s algebra of CholeskyQR in
 FP64), the update is Adam (``ht_sketch_adam``).  The trained S is used through
 the ordinary C ABI: ``decompose(..., sketch=[S_0, S_1, S_2], eig_iters=1)``;
 ``sketch=None`` keeps the Gaussian start block, which stays the default and the
-judge of the learned one.
+yardstick of the learned one.
 """
 from __future__ import annotations
 

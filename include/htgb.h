@@ -293,7 +293,7 @@ ht_status_t ht_batch_set_tuning(int lanes, int eig_ctas);
  * finder, used as ht_config_t.sketch[m] with eig_iters = 1 (Y = G S, Rayleigh-
  * Ritz on span(Y)).  No counterpart in the reference, whose range finder draws a
  * Gaussian test matrix (3D/Opt/kernel.cu:595-680); the Gaussian start block
- * stays the default and the judge of the learned one.
+ * stays the default and the yardstick of the learned one.
  *
  * ht_sketch_loss_grad: for `batch` mode Grams G (batch x n x n, column-major,
  * device) with traces trG (device), the forward value

@@ -113,8 +113,8 @@ def bf16_round(t):
 @pytest.mark.parametrize("prec", ["fp32", "bf16"])
 def test_backward_matches_autograd(N, M, r, batch, prec):
     """FP32 path against float64 autograd of the chain.  BF16 path: its products
-    consume bf16(x), bf16(dy) and bf16(W) and sum in FP32, so it is judged
-    against float64 on exactly those operands: dx = bf16(dy) bf16(W), the factor
+    consume bf16(x), bf16(dy) and bf16(W) and sum in FP32, so it is compared
+    with float64 on exactly those operands: dx = bf16(dy) bf16(W), the factor
     gradients from the chain at bf16(x), bf16(dy).  What remains is FP32
     rounding, hence the same bars as the FP32 path (a flat BF16 tolerance
     cannot hold where a gradient is a short sum with cancellation)."""
