@@ -158,3 +158,19 @@ def test_batched_other_trees_take_the_general_grouped_paths(prec):
         pairs.append((synth.exact_ht(d, tree, noise_rel=1e-3, seed=600 + i), tree))
     rep = _check_batch(pairs, prec)
     assert rep["grouped"]
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+def test_batched_tiny_tensors_and_single_tensor_batch(prec):
+    """Modes of 3..12 (first modes padded for TMA, fewer than 32 rows in the
+    mode product, leaf problems solved directly) in one grouped batch; then a
+    batch of one tensor."""
+    pairs = []
+    for i, d in enumerate([(5, 6, 7), (3, 12, 4), (9, 4, 11), (12, 12, 12), (7, 3, 5)]):
+        r = [1, min(3, d[2]), min(3, d[2]), min(2, d[0]), min(3, d[1])]
+        tree = ht.reference_tree_3d(r)
+        pairs.append((synth.exact_ht(d, tree, noise_rel=1e-3, seed=700 + i), tree))
+    rep = _check_batch(pairs, prec)
+    assert rep["grouped"]
+    rep1 = _check_batch(pairs[3:4], prec)
+    assert rep1["grouped"] and rep1["gpu_launches"] > 0
