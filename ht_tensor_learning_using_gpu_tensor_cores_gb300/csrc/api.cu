@@ -707,9 +707,20 @@ ht_status_t leaf_eigs(Ctx &c, const Tree &T, const ht_config_t &cfg, const long 
     const int leaf = T.leaf_of_mode(m);
     const int K = (d3 && leaf == P3.c) ? P3.kw : T.rank[leaf];
     const int n = static_cast<int>(dims[m]);
-    // modes of size <= 64: the block is the whole space and the eigen-solver
-    // reduces to a Jacobi eigen-decomposition of the Gram itself
-    const int s = n <= 64 ? n : std::max(K, std::min<int>({n, K + p_over, 64}));
+    // s = k + oversampling (at most 64); a mode no larger than that is the
+    // whole block, and the eigen-solver reduces to a Jacobi eigen-decomposition
+    // of the Gram itself.  A mode of at most 64 above s takes whichever of the
+    // two is cheaper by a cost model (µs, one CTA) from measured costs: a Jacobi
+    // round on an m x m matrix ~0.85 (m / 64)^2 and ~10 sweeps of m - 1 rounds
+    // (~2e-3 m^3; 535 µs at m = 64, 172 at 48), against per iteration a fixed
+    // ~10 µs of barriers and pivots, the float-pair factor (~2.5e-4 s^3) and the
+    // product (~2e-5 n^2 s), plus the Rayleigh-Ritz Jacobi on s x s.
+    int s = std::max(K, std::min<int>({static_cast<int>(n), K + p_over, 64}));
+    if (s < n && n <= 64) {
+      const double direct = 2e-3 * n * n * n;
+      const double iterate = iters * (10.0 + 2.5e-4 * s * s * s + 2e-5 * n * n * s) + 2e-3 * s * s * s;
+      if (direct <= iterate) s = static_cast<int>(n);
+    }
     if (s > 64) return fail(HT_ERR_UNSUPPORTED, "subspace size above 64");
     EigProblem &e = ep[m];
     e.G = G[m]; e.n = n; e.s = s; e.K = K;

@@ -26,7 +26,7 @@
 // Cholesky runs on the unit-diagonal scaled matrix with a small shift, so it
 // cannot break down on rank-deficient blocks.  mu = 1e-9 trace(G) keeps Y
 // nonzero on exactly null directions without moving any eigenvector or
-// slowing convergence.  Modes with n <= 64 (s == n) skip the iteration: Q = I
+// slowing convergence.  Modes no larger than the block (s == n) skip the iteration: Q = I
 // and the Rayleigh-Ritz step is a Jacobi eigen-decomposition of G itself.
 #include <algorithm>
 #include <cstring>
@@ -1060,7 +1060,7 @@ HT_DEV EigSmem eig_smem(float *sm) {
   return m;
 }
 
-// Direct problem (s == n <= 64): Jacobi eigen-decomposition of G itself.
+// Direct problem (s == n): Jacobi eigen-decomposition of G itself.
 HT_DEV void eig_direct(const CoopProb &P, const EigSmem &m) {
   const int t = threadIdx.x, n = P.n, K = P.K;
   float (*A)[SMAX + 1] = m.A;
@@ -1254,7 +1254,7 @@ __global__ void __launch_bounds__(256, 1) eig_coop_kernel(const __grid_constant_
   const EigSmem m = eig_smem(sm);
 
   if (static_cast<int>(blockIdx.x) >= B.nsync) {
-    // ---- direct problem (s == n <= 64): Jacobi on G itself, no barriers
+    // ---- direct problem (s == n): Jacobi on G itself, no barriers
     eig_direct(B.p[B.direct_idx[blockIdx.x - B.nsync]], m);
     return;
   }

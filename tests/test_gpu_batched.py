@@ -125,7 +125,8 @@ def test_batched_large_mode_uses_per_lane_solver(prec):
 @pytest.mark.parametrize("prec", ["fp32", "bf16"])
 def test_batched_4d_and_direct_leaves(prec):
     """4th-order tensors (four leaves each, the root's range finder after the
-    grouped leaf solver) and leaves of size <= 64 solved directly, in one batch."""
+    grouped leaf solver); leaves no larger than k + oversampling are solved
+    directly, the others iterated, in one batch."""
     pairs = []
     for i, d in enumerate([(20, 24, 18, 22), (30, 16, 26, 20), (12, 28, 20, 24)]):
         tree = ht.balanced_tree_4d([1, 12, 12, 6, 6, 6, 6])
