@@ -528,7 +528,7 @@ ht_status_t mode_product(Ctx &c, const View &v, const float *x32, const __nv_bfl
   q.a32 = opA(x32); q.b32 = opB(W32, k);
   if (x16 && W16) { q.a16 = opA(x16); q.b16 = opB(W16, fold_h > 0 ? 2 * fold_h : k); }
   else q.a16.ptr = q.b16.ptr = nullptr;
-  q.bn_tc = fold_h > 0 ? 2 * fold_h : 64; q.bn_simt = 64;
+  q.bn_tc = fold_h > 0 ? 2 * fold_h : 64; q.bn_simt = k <= 32 ? 32 : 64;
   q.fold = fold_h > 0;
   if (v.L == 1) {
     q.tiles_kind = TILES_ROWS; q.t_rows = v.R; q.t_cols = k;
@@ -561,7 +561,7 @@ ht_status_t corange_product(Ctx &c, const View &v, const float *x32, const __nv_
   q.a32 = gram_operand(v, x32); q.b32 = opB(Q32);
   if ((x16 || a16) && Q16) { q.a16 = a16 ? *a16 : gram_operand(v, x16); q.b16 = opB(Q16); }
   else q.a16.ptr = q.b16.ptr = nullptr;
-  q.bn_tc = 64; q.bn_simt = 64;
+  q.bn_tc = 64; q.bn_simt = k <= 32 ? 32 : 64;
   q.tiles_kind = TILES_ROWS; q.t_rows = v.N; q.t_cols = k;
   q.out_mode = OUT_COLMAJOR;
   q.out = Z;
@@ -583,7 +583,7 @@ ht_status_t core_contract(Ctx &c, const float *Z, int np, int nq, int ku, const 
   q.a32.kind = OP_KM3; q.a32.ptr = Z; q.a32.d0 = np; q.a32.d1 = rows; q.a32.d2 = 1;
   q.b32.kind = OP_KM3; q.b32.ptr = Up; q.b32.d0 = np; q.b32.d1 = kp; q.b32.d2 = 1;
   q.a16.ptr = q.b16.ptr = nullptr;
-  q.bn_simt = 64;
+  q.bn_simt = kp <= 32 ? 32 : 64;
   q.tiles_kind = TILES_ROWS; q.t_rows = rows; q.t_cols = kp;
   q.out_mode = OUT_COLMAJOR;
   q.out = T1;

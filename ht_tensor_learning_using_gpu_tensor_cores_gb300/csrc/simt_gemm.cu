@@ -6,8 +6,10 @@
 // Grams with cublasSgemm, ttm.cu:2-36 TTM chains).  Same operand/tile model as
 // tc_gemm.cu: operands are read in place from the column-major tensor.
 //
-// Tile 128 x BN (BN = 128 or 64), K step 16, 256 threads, 8 x (BN/16)
-// register tile per thread, double-buffered shared memory.
+// Tile 128 x BN (BN = 128, 64 or 32), K step 16, 256 threads, 8 x (BN/16)
+// register tile per thread, double-buffered shared memory.  BN = 32 serves
+// products with at most 32 columns (rank-32 core contractions), which a 64-wide
+// tile would compute half in padding.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -97,9 +99,11 @@ HT_DEV const float *op_ptr(int kind, const float *p, long long d0, long long d1,
 // One output tile (split `split` of its K range) of a CTA.
 template <int BN>
 HT_DEV void simt_gemm_tile(const SParams &p, const Tile &tile, int tile_idx, int split) {
-  constexpr int TN = BN / 16;   // columns per thread (8 or 4)
+  constexpr int TN = BN / 16;   // columns per thread (8, 4 or 2)
   constexpr int A_PER = BM * BKS / 256;   // 8
-  constexpr int B_PER = BN * BKS / 256;   // 8 or 4
+  constexpr int B_PER = BN * BKS / 256;   // 8, 4 or 2
+  // a 32-row B tile is 128 float4: fewer than one per thread, so it loads scalar
+  constexpr bool kBVec = BN >= 64;
   __shared__ __align__(16) float As[2][BKS][BM + 4];
   __shared__ __align__(16) float Bs[2][BKS][BN + 4];
 
@@ -120,7 +124,7 @@ HT_DEV void simt_gemm_tile(const SParams &p, const Tile &tile, int tile_idx, int
   bool a_v = false, b_v = false;
   auto load_tiles = [&](long long k0) {
     a_v = p.a_vec != 0 && k0 + BKS <= kend;
-    b_v = p.b_vec != 0 && k0 + BKS <= kend;
+    b_v = kBVec && p.b_vec != 0 && k0 + BKS <= kend;
     if (a_v) load_vec<BM>(p.a_vec, p.a_kind, p.a, p.a0, p.a1, k0, tile.a_row, tile.a_z, p.a_rows, ra);
     if (b_v) load_vec<BN>(p.b_vec, p.b_kind, p.b, p.b0, p.b1, k0, tile.b_row, 0, p.b_rows, rb);
     if (a_v && b_v) return;
@@ -205,8 +209,13 @@ HT_DEV void simt_gemm_tile(const SParams &p, const Tile &tile, int tile_idx, int
       const float4 a1 = *reinterpret_cast<const float4 *>(&As[buf][kk][64 + ty * 4]);
       a[0] = a0.x; a[1] = a0.y; a[2] = a0.z; a[3] = a0.w;
       a[4] = a1.x; a[5] = a1.y; a[6] = a1.z; a[7] = a1.w;
-      const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][tx * 4]);
-      b[0] = b0.x; b[1] = b0.y; b[2] = b0.z; b[3] = b0.w;
+      if constexpr (TN == 2) {
+        const float2 b0 = *reinterpret_cast<const float2 *>(&Bs[buf][kk][tx * 2]);
+        b[0] = b0.x; b[1] = b0.y;
+      } else {
+        const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][tx * 4]);
+        b[0] = b0.x; b[1] = b0.y; b[2] = b0.z; b[3] = b0.w;
+      }
       if constexpr (TN == 8) {
         const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][64 + tx * 4]);
         b[4] = b1.x; b[5] = b1.y; b[6] = b1.z; b[7] = b1.w;
@@ -227,7 +236,7 @@ HT_DEV void simt_gemm_tile(const SParams &p, const Tile &tile, int tile_idx, int
     const int row = (i < 4) ? (ty * 4 + i) : (64 + ty * 4 + i - 4);
 #pragma unroll
     for (int j = 0; j < TN; ++j) {
-      const int col = (j < 4) ? (tx * 4 + j) : (64 + tx * 4 + j - 4);
+      const int col = TN == 2 ? tx * 2 + j : ((j < 4) ? (tx * 4 + j) : (64 + tx * 4 + j - 4));
       if (p.out_mode == OUT_PARTIAL) {
         p.out[((static_cast<size_t>(split) * p.num_tiles + tile_idx) * BM + row) * BN + col] = acc[i][j];
       } else if (row < tile.valid_rows && col < tile.valid_cols) {
@@ -241,6 +250,12 @@ template <int BN>
 __global__ void __launch_bounds__(256) simt_gemm_kernel(const SParams p, const TileGen gen) {
   const int tile_idx = blockIdx.x % p.num_tiles;
   simt_gemm_tile<BN>(p, gen_tile(gen, tile_idx), tile_idx, blockIdx.x / p.num_tiles);
+}
+
+// 32-column tiles at three blocks per SM (80 registers, no spills)
+__global__ void __launch_bounds__(256, 3) simt_gemm_narrow_kernel(const SParams p, const TileGen gen) {
+  const int tile_idx = blockIdx.x % p.num_tiles;
+  simt_gemm_tile<32>(p, gen_tile(gen, tile_idx), tile_idx, blockIdx.x / p.num_tiles);
 }
 
 // Grouped GEMMs of the batched path: block i computes the tile blocks[i].tile
@@ -435,6 +450,8 @@ cudaError_t simt_gemm_launch(const GemmArgs &g, int bn, cudaStream_t s) {
     simt_gemm_kernel<128><<<grid, 256, 0, s>>>(p, g.gen);
   else if (bn == 64)
     simt_gemm_kernel<64><<<grid, 256, 0, s>>>(p, g.gen);
+  else if (bn == 32)
+    simt_gemm_narrow_kernel<<<grid, 256, 0, s>>>(p, g.gen);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();
