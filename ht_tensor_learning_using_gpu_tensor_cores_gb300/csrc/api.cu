@@ -625,7 +625,7 @@ ht_status_t check_device() {
     return fail(HT_ERR_NO_DEVICE, "cannot query the CUDA device");
   }
   if (!(major == 10 && minor == 3))
-    return fail(HT_ERR_NO_DEVICE, "this build targets sm_103a (GB300); device is sm_" + std::to_string(major) +
+    return fail(HT_ERR_NO_DEVICE, "the library is compiled for sm_103a (GB300); device is sm_" + std::to_string(major) +
                                       std::to_string(minor));
   if (dev >= 0 && dev < 64) g_dev_ok[dev] = 1;
   return HT_OK;
