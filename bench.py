@@ -38,7 +38,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_FULL, RANK, DECAY = 1024, 32, 1.5
-CPU_SAMPLE_N = 512
+CPU_SAMPLE_N = 704   # about 10-15 s of the CPU port on 16 host cores
 METRIC = "HT-decomp ms @1024^3 r32, err<=1e-3 vs FP64: mixed/learned vs plain FP32"
 # DRAM bytes (read + write) of one leaf-Gram launch at 1024^3, from a one-pass ncu capture:
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none
@@ -156,7 +156,7 @@ def cpu_decompose(n):
     contractions), on an n^3 tensor of the headline family.  Timed region: the
     decomposition, X -> (U_t, B_t), the region the GPU headline times.
     Returns (seconds, rel_err or None); the error pass runs after the timed
-    region and only for n <= 512 (the full-size reconstruction would double
+    region and only for n <= 704 (the full-size reconstruction would double
     the CPU time)."""
     import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -167,7 +167,7 @@ def cpu_decompose(n):
     t0 = time.perf_counter()
     U, B, _ = O.ht_decompose(X, tr, dtype=np.float32)
     t = time.perf_counter() - t0
-    err = O.ht_error(X, tr, U, B) if n <= 512 else None
+    err = O.ht_error(X, tr, U, B) if n <= 704 else None
     return t, err
 
 
@@ -181,7 +181,7 @@ def cpu_baseline(sample_n=CPU_SAMPLE_N):
     threads, blas = blas_info()
     return {"value": t * scale * 1e3, "unit": "ms", "cores": threads, "kind": "port",
             "sample": f"FP32 decomposition of a {sample_n}^3 tensor of the same family (numpy port of "
-                      f"HT_TensorLy.py), {t:.2f} s measured, scaled x{scale:.0f} by the n^4 operation count to "
+                      f"HT_TensorLy.py), {t:.2f} s measured, scaled x{scale:.2f} by the n^4 operation count to "
                       f"{N_FULL}^3 (extrapolated; --impl reference measures {N_FULL}^3)",
             "blas": blas, "sample_seconds": t, "sample_err": err, "extrapolated": True}
 
