@@ -1,5 +1,6 @@
-"""Host logic of the batched path's autotuner: the table lookup by the
-batch's largest dimension (no GPU)."""
+"""Host logic of the batched path's autotuner (no GPU): the table lookup by the
+batch's largest dimension, and the candidate search with its error guard run
+against a stand-in timer."""
 from ht_tensor_learning_using_gpu_tensor_cores_gb300 import autotune
 
 
@@ -22,3 +23,61 @@ def test_committed_table_is_well_formed():
         assert b["lo"] <= b["hi"]
         assert set(b["config"]) == set(autotune.DEFAULT)
         assert b["tensors_per_s"] >= 0.95 * b["default_tensors_per_s"]
+
+
+def _fake_timer(profile):
+    """A stand-in for the GPU timing of one configuration: (seconds per batch,
+    report) looked up by (eig_iters, oversample, lanes)."""
+    calls = []
+
+    def timer(trees, dims, tensors, cfg, precision, repeats):
+        calls.append(dict(cfg))
+        wall, p99, mx = profile.get((cfg["eig_iters"], cfg["oversample"], cfg["lanes"]), (1.0, 1e-3, 2e-3))
+        return wall, {"rel_err_p50": p99 / 2, "rel_err_p99": p99, "rel_err_max": mx}
+
+    return timer, calls
+
+
+def test_tuner_takes_the_fastest_candidate_inside_the_error_guard(monkeypatch):
+    # four iterations at oversampling 16 would be fastest here but move the p99 error past
+    # the guard; four at oversampling 8 keep both errors within 0.1 % of the default's and win
+    profile = {(10, 16, 16): (1.00, 1.000e-3, 2.000e-3),
+               (4, 16, 16): (0.50, 1.200e-3, 2.000e-3),     # p99 outside the guard
+               (4, 8, 16): (0.60, 1.0009e-3, 2.0019e-3),    # inside
+               (6, 8, 16): (0.70, 0.990e-3, 1.990e-3),      # inside, slower
+               (6, 16, 16): (0.65, 1.000e-3, 2.300e-3)}     # max outside the guard
+    timer, calls = _fake_timer(profile)
+    monkeypatch.setattr(autotune, "_time_config", timer)
+    monkeypatch.setattr(autotune, "set_launch_shape", lambda lanes, ctas: None)
+    dims = [(100, 120, 90)] * 4
+    res = autotune.tune_batched([None] * 4, dims, [None] * 4)
+    assert res["config"] == {"lanes": 16, "eig_ctas": 0, "eig_iters": 4, "oversample": 8}
+    assert abs(res["tensors_per_s"] - 4 / 0.60) < 1e-9
+    assert abs(res["default_tensors_per_s"] - 4.0) < 1e-9
+    # a grouped batch (every mode <= 512) tries iterations x oversampling only, default first
+    assert calls[0] == autotune.DEFAULT
+    assert {c["lanes"] for c in calls} == {16} and {c["eig_ctas"] for c in calls} == {0}
+    assert len(calls) == len(autotune.CANDIDATES_GROUPED["eig_iters"]) * len(autotune.CANDIDATES_GROUPED["oversample"])
+    assert res["candidates_tried"] == len(calls)
+
+
+def test_tuner_keeps_the_default_when_nothing_faster_passes_the_guard(monkeypatch):
+    profile = {(it, ov, 16): (0.5, 5e-3, 9e-3) for it in (6, 4) for ov in (16, 8)}
+    profile[(10, 8, 16)] = (1.2, 1e-3, 2e-3)    # inside the guard but slower
+    timer, _ = _fake_timer(profile)
+    monkeypatch.setattr(autotune, "_time_config", timer)
+    monkeypatch.setattr(autotune, "set_launch_shape", lambda lanes, ctas: None)
+    res = autotune.tune_batched([None] * 2, [(64, 64, 64)] * 2, [None] * 2)
+    assert res["config"] == autotune.DEFAULT
+
+
+def test_tuner_searches_the_launch_shape_of_batches_too_large_to_group(monkeypatch):
+    timer, calls = _fake_timer({})
+    monkeypatch.setattr(autotune, "_time_config", timer)
+    monkeypatch.setattr(autotune, "set_launch_shape", lambda lanes, ctas: None)
+    autotune.tune_batched([None], [(600, 64, 64)], [None])
+    n = 1
+    for v in autotune.CANDIDATES.values():
+        n *= len(v)
+    assert len(calls) == n   # the default once, every other combination once
+    assert {c["lanes"] for c in calls} == set(autotune.CANDIDATES["lanes"])
