@@ -375,7 +375,7 @@ class BatchDecomposer:
                    "ms_total": rep.ms_total, "gpu_launches": rep.gpu_launches, "graph_replayed": bool(rep.graph_replayed),
                    "lanes": rep.lanes, "grouped": bool(rep.grouped),
                    "ms_phase": {name: rep.ms_phase[i] for i, name in enumerate(
-                       ["conversion_grams", "leaf_solver", "core_pass_lanes", "transfer_tails", "error_pass",
+                       ["conversion_grams", "leaf_solver", "core_pass", "transfer_tails", "error_pass",
                         "copies"])},
                    "note": (lib().ht_last_error() or b"").decode()}
         return results, summary

@@ -256,11 +256,11 @@ typedef struct {
     int gpu_launches;        /* kernels launched per batch                                   */
     int graph_replayed;      /* 1 when the cached CUDA graph of an identical batch ran       */
     int lanes;               /* concurrent streams the batch was spread over                 */
-    int grouped;             /* 1: every leaf eigen-problem ran in one grouped launch        */
+    int grouped;             /* 1: the batch ran as grouped stages (every mode <= 512)       */
     float ms_phase[6];       /* grouped: device ms of (0) conversion and leaf Grams, (1) the
-                                grouped leaf solver, (2) the lanes after it (core pass),
-                                (3) the grouped transfer tails, (4) the error pass, (5) the
-                                copies to the caller's buffers (else 0)                       */
+                                leaf solver, (2) the core pass, (3) the transfer tails,
+                                (4) the error pass, (5) the copies to the caller's buffers
+                                (else 0)                                                      */
 } ht_batch_report_t;
 
 /* Decompose `count` tensors of the same order in one call.  Replaces the
@@ -271,7 +271,10 @@ typedef struct {
  *   U, B   count x HT_MAX_NODES tables of DEVICE output pointers: U[i*HT_MAX_NODES + t]
  *          and B[i*HT_MAX_NODES + t] as in ht_decompose for tensor i;
  *   rel_err host array of count (HT_FLAG_COMPUTE_ERROR) or NULL.
- * The tensors are spread over concurrent streams, each with its own workspace.
+ * When every mode of the batch is at most 512 it runs stage by stage, one launch
+ * per stage for all tensors (conversion, leaf Grams, leaf solver, core pass,
+ * transfer tensors, error, copies), each tensor in a workspace region of its
+ * own; otherwise the tensors are spread over concurrent streams.
  * The first call records the whole batch into a CUDA graph; a later call with
  * the same count, dims, trees, config and pointers replays it (fixed buffers,
  * new contents).  Synchronous with respect to the host. */
